@@ -1,0 +1,334 @@
+/*
+ * texo_gp.h — C ABI of the GB300 electrostatic global-placement engine.
+ *
+ * This library replaces one stage of the Texo place-and-route flow: the
+ * elfPlace/ePlace electrostatic global placement `eplace::place`
+ * (crates/texo-pnr/src/eplace.rs:242-421) together with everything it calls on
+ * its hot path:
+ *   - the dynamic preconditioned Nesterov step
+ *     (crates/texo-pnr/src/global_placement.rs:121-335),
+ *   - the quadratic-B-spline electrostatic density model and its spectral
+ *     Poisson solve (crates/texo-pnr/src/electrostatic_placement.rs:130-441,
+ *     602-776, 895-976),
+ *   - the weighted-average (WA) hypernet wirelength
+ *     (crates/texo-pnr/src/analytical_placement.rs:366-463, 520-703).
+ *
+ * The reference function is crate-private Rust with no FFI. The entry points
+ * below are what a Rust caller (`analytical_place`,
+ * crates/texo-pnr/src/lib.rs:4129-4143) would bind through `extern "C"`:
+ * plain pointers and sizes, caller-owned host arrays, no allocation visible to
+ * the caller except the opaque handles created here.
+ *
+ * Coordinates are tile (site) coordinates, exactly as in the reference: the
+ * optimizer vector is [x0, y0, x1, y1, ...] over all placement units followed
+ * by one (x, y) pair per density filler.
+ *
+ * All functions are synchronous with respect to the caller. A handle owns one
+ * CUDA stream; distinct handles are independent and may be driven from
+ * different host threads. Results are bit-for-bit deterministic run to run.
+ */
+#ifndef TEXO_GP_H
+#define TEXO_GP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TEXO_GP_ABI_VERSION 1u
+
+/* ------------------------------------------------------------------------ */
+/* Status codes: one per variant of the reference's error enums.            */
+/* ------------------------------------------------------------------------ */
+typedef enum texo_gp_status {
+  TEXO_GP_OK = 0,
+  /* ElectrostaticError, crates/texo-pnr/src/electrostatic_placement.rs:15-69 */
+  TEXO_GP_ERR_EMPTY_GRID = 1,
+  TEXO_GP_ERR_GRID_TOO_LARGE = 2,
+  TEXO_GP_ERR_DENSITY_LENGTH = 3,
+  TEXO_GP_ERR_NONFINITE_DENSITY = 4,
+  TEXO_GP_ERR_EMPTY_UNIT = 5,
+  TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE = 6,
+  TEXO_GP_ERR_INVALID_MEMBER_CHARGE = 7,
+  TEXO_GP_ERR_POINT_OUTSIDE_GRID = 8,
+  TEXO_GP_ERR_FIXED_CAPACITY_EXHAUSTED = 9,
+  TEXO_GP_ERR_INSUFFICIENT_CAPACITY = 10,
+  TEXO_GP_ERR_INSUFFICIENT_AREA = 11,
+  TEXO_GP_ERR_NONFINITE_FILLER = 12,
+  TEXO_GP_ERR_NEGATIVE_FILLER_CHARGE = 13,
+  TEXO_GP_ERR_UNEXPECTED_FILLER_KIND = 14,
+  TEXO_GP_ERR_FILLER_CHARGE_MISMATCH = 15,
+  /* NesterovError, crates/texo-pnr/src/global_placement.rs:80-109 */
+  TEXO_GP_ERR_INVALID_BOUNDS = 32,
+  TEXO_GP_ERR_INVALID_METRIC_LENGTH = 33,
+  TEXO_GP_ERR_NONPOSITIVE_METRIC = 34,
+  TEXO_GP_ERR_INVALID_INITIAL_COORDINATE = 35,
+  TEXO_GP_ERR_INVALID_MOMENTUM_PARAMETER = 36,
+  TEXO_GP_ERR_INVALID_LIPSCHITZ_ESTIMATE = 37,
+  TEXO_GP_ERR_INVALID_OBJECTIVE = 38,
+  TEXO_GP_ERR_INVALID_GRADIENT_LENGTH = 39,
+  TEXO_GP_ERR_NONFINITE_GRADIENT = 40,
+  TEXO_GP_ERR_LINE_SEARCH_OVERFLOW = 41,
+  TEXO_GP_ERR_ITERATION_OVERFLOW = 42,
+  TEXO_GP_ERR_EVALUATION = 43,
+  /* EplaceError, crates/texo-pnr/src/eplace.rs:27-38 */
+  TEXO_GP_ERR_DENSITY_FIELD_CHANGED = 64,
+  TEXO_GP_ERR_INVALID_NORMALIZATION = 65,
+  TEXO_GP_ERR_DID_NOT_CONVERGE = 66,
+  /* Errors of this boundary itself (no reference counterpart). */
+  TEXO_GP_ERR_INVALID_ARGUMENT = 96,
+  TEXO_GP_ERR_CUDA = 97,
+  TEXO_GP_ERR_OUT_OF_MEMORY = 98,
+  TEXO_GP_ERR_DEVICE_TIMEOUT = 99,   /* a bounded device-side wait ran out */
+  TEXO_GP_ERR_FIXED_POINT_RANGE = 100, /* a weight or charge exceeds the int64 accumulator range */
+  TEXO_GP_ERR_UNSUPPORTED = 101,
+  TEXO_GP_ERR_BUSY = 102
+} texo_gp_status;
+
+/* Resource kinds in the reference's `ResourceKind` order
+ * (crates/texo-model/src/lib.rs:69-87). Only LUT, REGISTER and MEMORY are
+ * density fields (`density_kind_is_exchangeable`, eplace.rs:1417-1422). */
+typedef enum texo_gp_kind {
+  TEXO_GP_KIND_LOGIC = 0,
+  TEXO_GP_KIND_LUT = 1,
+  TEXO_GP_KIND_REGISTER = 2,
+  TEXO_GP_KIND_MEMORY = 3,
+  TEXO_GP_KIND_CLOCK = 4,
+  TEXO_GP_KIND_IO = 5,
+  TEXO_GP_KIND_CONSTANT = 6,
+  TEXO_GP_KIND_DSP = 7
+} texo_gp_kind;
+
+/* One density field (one exchangeable resource kind). Fields must be listed
+ * in ascending (kind, lut_inputs) order, which is the reference's BTreeMap
+ * order; fields without any member are ignored, as in the reference. */
+typedef struct texo_gp_field {
+  uint32_t kind;         /* texo_gp_kind */
+  uint32_t lut_inputs;   /* ResourceKind::Lut(k) payload; 0 otherwise */
+} texo_gp_field;
+
+/* Flattened `eplace::place` inputs (eplace.rs:242-253 and the data it reads
+ * from `Device`, `PlacementUnit` and `AnalyticalHypergraph`). All arrays are
+ * caller-owned and only read during texo_gp_create / texo_gp_place. */
+typedef struct texo_gp_problem {
+  uint32_t width, height;            /* Device::width/height: the tile grid */
+  uint32_t num_fields;
+  const texo_gp_field* fields;       /* [num_fields] */
+  const uint32_t* capacity;          /* [num_fields][width*height] BELs per tile */
+  uint32_t num_fixed_occupancy;      /* exchangeable BELs held by fixed units */
+  const uint32_t* fixed_occupancy;   /* [num_fixed_occupancy][3] = field, x, y */
+
+  uint32_t num_units;                /* all PlacementUnits, movable and fixed */
+  const double* initial_xy;          /* [2U] initial_x/initial_y interleaved */
+  const double* lower_xy;            /* [2U] choice_bounds (eplace.rs:1470-1481) */
+  const double* upper_xy;            /* [2U]; fixed units have lower == upper */
+  const uint32_t* member_ptr;        /* [U+1] CSR of density members per unit */
+  const uint32_t* member_field;      /* [members] index into fields */
+  const double* member_offset_xy;    /* [2*members] offset from the unit origin */
+  const double* member_charge;       /* [members] physical area (1.0 by default) */
+  const uint32_t* member_cell;       /* [members] logical cell of the member */
+
+  uint32_t num_cells;
+  const uint32_t* cell_unit;         /* [cells] unit_by_cell */
+  const double* cell_offset_xy;      /* [2*cells] macro_offset_by_cell */
+  const uint8_t* cell_fixed;         /* [cells] 1 when fixed_coordinates[cell] is Some */
+  const double* cell_fixed_xy;       /* [2*cells] fixed coordinate (read when fixed) */
+
+  uint32_t num_nets;                 /* hypernets with >= 2 pins, driver first */
+  const uint32_t* net_ptr;           /* [E+1] */
+  const uint32_t* pin_cell;          /* [P] */
+  uint32_t num_timed_arcs;
+  const uint32_t* arc_driver_cell;   /* [A] */
+  const uint32_t* arc_sink_cell;     /* [A] */
+  const uint64_t* arc_extra_weight;  /* [A] sink weight - 1 (> 0) */
+} texo_gp_problem;
+
+/* DCT forms for the spectral Poisson solve. */
+typedef enum texo_gp_dct_mode {
+  TEXO_GP_DCT_FP32 = 0,     /* plain FP32 CUDA-core GEMM transform */
+  TEXO_GP_DCT_BF16X3 = 1    /* tcgen05 tensor cores, BF16x3 split, FP32 accumulate */
+} texo_gp_dct_mode;
+
+/* Controller forms. */
+typedef enum texo_gp_engine {
+  TEXO_GP_ENGINE_HOST = 0,      /* host-driven line search, one sync per evaluation */
+  TEXO_GP_ENGINE_DEVICE = 1     /* whole eplace loop in one persistent cooperative kernel */
+} texo_gp_engine;
+
+/* Parameters. texo_gp_default_params() returns the reference constants
+ * (eplace.rs:125-134), under which the engine reduces to reference
+ * semantics. The bin-grid, target-density and gamma-unit fields are
+ * extensions for grids that differ from the tile grid. */
+typedef struct texo_gp_params {
+  double gamma_base;             /* ePlace gamma base in bin widths (8.0) */
+  uint32_t max_iterations;       /* MAX_EPLACE_ITERATIONS (3000) */
+  double beta;                   /* AUGMENTED_DENSITY_BETA (2000) */
+  double initial_density_weight; /* INITIAL_DENSITY_WEIGHT (1e-4) */
+  double alpha_low, alpha_high;  /* MULTIPLIER_ALPHA_LOW/HIGH (1.05, 1.06) */
+  double overflow_target_override; /* < 0: per-kind targets (0.10 / 0.20) */
+  uint32_t bins_x, bins_y;       /* density grid; 0 = the tile grid */
+  double target_density;         /* 1.0 = reference semantics */
+  int32_t best_effort;           /* keep the best checkpoint instead of DidNotConverge */
+  int32_t dct_mode;              /* texo_gp_dct_mode */
+  int32_t engine;                /* texo_gp_engine */
+  int32_t device;                /* CUDA device ordinal */
+  double objective_margin_ulps;  /* line-search rounding margin in FP32 ulps of |f| (see DESIGN) */
+  uint32_t reserved[8];
+} texo_gp_params;
+
+#define TEXO_GP_MAX_FIELDS 4
+
+/* Per-call results; filled by texo_gp_place / texo_gp_run. */
+typedef struct texo_gp_stats {
+  int32_t status;                /* texo_gp_status of the call */
+  uint32_t iterations;           /* completed eplace iterations */
+  uint64_t evaluations;          /* objective evaluations */
+  uint64_t line_search_trials;
+  uint32_t num_fields;
+  double overflow[TEXO_GP_MAX_FIELDS];  /* normalized positive overflow per field */
+  double energy[TEXO_GP_MAX_FIELDS];
+  double gamma;                  /* last global gamma */
+  double objective;              /* last accepted combined objective */
+  double hpwl;                   /* HPWL of the final continuous coordinates */
+  uint64_t error_index;          /* first offending index for indexed errors */
+  uint32_t error_field;
+  uint32_t converged;            /* 1 when every field reached its target */
+  double elapsed_ms;             /* device time of the placement loop */
+} texo_gp_stats;
+
+/* One evaluation of the objective components at given coordinates
+ * (`ContinuousProblem::evaluate`, eplace.rs:137-205). */
+typedef struct texo_gp_field_eval {
+  double energy;                 /* 1/2 <rho - mean, phi> */
+  double normalized_overflow;    /* physical positive overflow / real area */
+  double net_charge;             /* sum of the density grid */
+  double force_l1;               /* sum_members q (|gx| + |gy|) */
+  double real_area;
+  double filler_charge;
+  int64_t overflow_fixed;        /* positive overflow, 2^-32 fixed point (device form) */
+  uint64_t overflow_bins;        /* bins with positive physical overflow */
+} texo_gp_field_eval;
+
+typedef struct texo_gp_eval {
+  double wirelength;             /* WA value, baseline + timing overlays */
+  uint32_t num_fields;
+  texo_gp_field_eval fields[TEXO_GP_MAX_FIELDS];
+} texo_gp_eval;
+
+typedef struct texo_gp_handle_s* texo_gp_handle;
+
+/* ---- version / defaults ------------------------------------------------- */
+uint32_t texo_gp_abi_version(void);
+void texo_gp_default_params(texo_gp_params* out);
+const char* texo_gp_status_name(int32_t status);
+/* Last CUDA error text seen by this thread (for TEXO_GP_ERR_CUDA). */
+const char* texo_gp_last_error(void);
+
+/* ---- one-shot drop-in ----------------------------------------------------
+ * Replaces `eplace::place` (eplace.rs:242-421) with routing_capacity = None:
+ * builds the density model, fillers and bounds, runs the augmented-Lagrangian
+ * Nesterov loop and writes the best checkpoint's rounded unit targets
+ * (`rounded_targets_from_coordinates`, eplace.rs:954-971) to out_targets_xy
+ * [2U]. out_coordinates [2(U+F)] (optional, may be NULL) receives the final
+ * continuous coordinates. */
+int32_t texo_gp_place(const texo_gp_problem* problem, const texo_gp_params* params,
+                      uint32_t* out_targets_xy, double* out_coordinates,
+                      texo_gp_stats* stats);
+
+/* ---- device-resident handle ----------------------------------------------
+ * create = `DensityModel::new` + `initial_fillers` +
+ * `initial_coordinates_and_bounds` (eplace.rs:312-318); device buffers are
+ * allocated once here. */
+int32_t texo_gp_create(const texo_gp_problem* problem, const texo_gp_params* params,
+                       texo_gp_handle* out);
+int32_t texo_gp_destroy(texo_gp_handle h);
+/* Sizes: units, fillers, optimizer coordinates (2(U+F)), bin grid. */
+int32_t texo_gp_sizes(texo_gp_handle h, uint64_t* units, uint64_t* fillers,
+                      uint64_t* coordinates, uint32_t* bins_x, uint32_t* bins_y,
+                      uint32_t* num_fields);
+/* Initial optimizer vector and bounds (each [2(U+F)]); any may be NULL. */
+int32_t texo_gp_initial(texo_gp_handle h, double* coordinates, double* lower,
+                        double* upper);
+/* Filler table (`initial_fillers`, electrostatic_placement.rs:198-240):
+ * field index and charge per filler; either may be NULL. */
+int32_t texo_gp_fillers(texo_gp_handle h, uint32_t* field, double* charge);
+
+/* Evaluates wirelength and every density field at `coordinates` [2(U+F)]
+ * with WA smoothing `gamma` (tile units). Optional outputs (NULL to skip):
+ *   wa_gradient [2U], field_gradient [num_fields][2(U+F)] (raw, coefficient 1),
+ *   density [num_fields][bins] (after fillers), potential [num_fields][bins]. */
+int32_t texo_gp_evaluate(texo_gp_handle h, const double* coordinates, double gamma,
+                         texo_gp_eval* out, double* wa_gradient,
+                         double* field_gradient, double* density,
+                         double* potential);
+/* Raw device form of the density scatter at `coordinates`: int64 2^-32
+ * fixed-point grids of the physical members (minus the smoothed capacity) and
+ * of the fillers, [num_fields][bins] each; either may be NULL. */
+int32_t texo_gp_scatter(texo_gp_handle h, const double* coordinates,
+                        int64_t* physical_grid, int64_t* filler_grid);
+/* Spectral Poisson solve of one grid `density` [bins] on the handle's bin
+ * grid with the handle's DCT mode: writes potential [bins], returns energy. */
+int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potential,
+                        double* energy);
+
+/* Runs the placement loop from the handle's current state (the initial
+ * coordinates after create) to convergence, the iteration cap, or
+ * `max_iterations` more iterations when nonzero. Writes the best rounded
+ * targets [2U] and optionally the current coordinates [2(U+F)]. */
+int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_targets_xy,
+                    double* out_coordinates, texo_gp_stats* stats);
+/* Restores the handle to its just-created state (positions, multipliers,
+ * optimizer state) without touching the device allocations. */
+int32_t texo_gp_reset(texo_gp_handle h);
+
+/* HPWL = sum over hypernets of the x and y pin spans at `coordinates`
+ * (the continuous form of `exact_objective`, analytical_placement.rs:473-511),
+ * FP64 reduction. */
+int32_t texo_gp_hpwl(texo_gp_handle h, const double* coordinates, double* hpwl);
+
+/* ---- synthetic ECP5-like netlists ----------------------------------------
+ * Seeded generator of the benchmark netlists: movable unit-area LUT cells on a
+ * side x side site fabric with one LUT per site, fixed IO cells evenly spaced
+ * on the perimeter, nets in 2 / 3-5 / 6-32 pin bands with Gaussian index-grid
+ * locality. Owned by the returned handle; `problem` points into it. */
+typedef struct texo_gp_synth_spec {
+  uint32_t side;          /* fabric side in sites */
+  uint32_t cells;         /* movable unit-area cells */
+  uint32_t io;            /* fixed perimeter IO cells */
+  uint32_t nets;
+  double sigma;           /* locality radius in sites */
+  double p_local;         /* probability that a sink is local (0.8) */
+  double jitter;          /* initial N(0, jitter) sites around the centre */
+  uint64_t seed;
+} texo_gp_synth_spec;
+typedef struct texo_gp_synth_s* texo_gp_synth;
+int32_t texo_gp_synth_create(const texo_gp_synth_spec* spec, texo_gp_synth* out,
+                             const texo_gp_problem** problem);
+int32_t texo_gp_synth_destroy(texo_gp_synth s);
+
+/* ---- batched and served placement ----------------------------------------
+ * Many independent placements resident on the device at once; the device
+ * engine advances all of them in one persistent kernel per chunk of
+ * iterations. A job retires when its stop rule fires. */
+typedef struct texo_gp_batch_s* texo_gp_batch;
+int32_t texo_gp_batch_create(const texo_gp_params* params, uint64_t hbm_budget_bytes,
+                             uint32_t max_slots, texo_gp_batch* out);
+int32_t texo_gp_batch_destroy(texo_gp_batch b);
+/* Admits one job when its footprint fits; returns TEXO_GP_ERR_BUSY otherwise. */
+int32_t texo_gp_batch_admit(texo_gp_batch b, const texo_gp_problem* problem,
+                            uint64_t job_id, uint32_t* out_slot);
+/* Advances every resident job by up to `iterations` eplace iterations. */
+int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations);
+/* Pops one finished job: its id, rounded targets (caller buffer of 2U) and stats.
+ * Returns TEXO_GP_ERR_BUSY when no job has finished. */
+int32_t texo_gp_batch_retire(texo_gp_batch b, uint64_t* job_id, uint32_t* out_targets_xy,
+                             uint64_t targets_capacity, texo_gp_stats* stats);
+int32_t texo_gp_batch_counts(texo_gp_batch b, uint32_t* resident, uint32_t* finished,
+                             uint64_t* bytes_in_use);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TEXO_GP_H */

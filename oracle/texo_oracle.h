@@ -1,0 +1,158 @@
+/*
+ * texo_oracle.h — TEST INFRASTRUCTURE ONLY.
+ *
+ * C API of the FP64 CPU restatement of Texo's electrostatic global placement
+ * (the parity oracle). Only the test suite, the smoke check and the CPU
+ * baseline leg of the benchmark load this library, and only as the checker or
+ * as the timed CPU baseline; the product path never links or calls it.
+ *
+ * Every function restates the reference algorithm in the reference's
+ * operation order; the citation next to each names the Rust source it
+ * follows (paths relative to the texo repository).
+ */
+#ifndef TEXO_ORACLE_H
+#define TEXO_ORACLE_H
+
+#include <stdint.h>
+#include "../include/texo_gp.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* quadratic_bspline_axis, electrostatic_placement.rs:950-976 */
+void orc_bspline_axis(uint64_t length, double coordinate, uint64_t index[3], double weight[3],
+                      double derivative[3]);
+/* deposit_quadratic_bspline, electrostatic_placement.rs:900-916 */
+void orc_deposit(double* density, uint64_t width, uint64_t height, double x, double y,
+                 double charge);
+/* sample_quadratic_bspline_with_gradient, electrostatic_placement.rs:919-941 */
+void orc_sample(const double* potential, uint64_t width, uint64_t height, double x, double y,
+                double out[3]);
+/* deposit_bilinear / sample_bilinear_with_gradient, electrostatic_placement.rs:979-1027 */
+void orc_deposit_bilinear(double* density, uint64_t width, uint64_t height, double x, double y,
+                          double charge);
+void orc_sample_bilinear(const double* potential, uint64_t width, uint64_t height, double x,
+                         double y, double out[3]);
+
+/* Poisson2d::solve (fast, electrostatic_placement.rs:725-776) when matrix == 0;
+ * Poisson2d::solve_reference (matrix form, :780-859) when matrix != 0. */
+int32_t orc_poisson(uint32_t width, uint32_t height, const double* density, double* potential,
+                    double* energy, int32_t matrix);
+/* orthonormal_dct2_basis, electrostatic_placement.rs:862-883 ([n][n], row = frequency) */
+void orc_dct_basis(uint32_t n, double* basis);
+
+/* ---- problem-level oracle ------------------------------------------------ */
+typedef struct orc_handle_s* orc_handle;
+
+typedef struct orc_field_result {
+  uint32_t kind, lut_inputs;
+  uint64_t available_capacity;
+  uint64_t real_charge;
+  double real_area, filler_charge, energy, normalized_overflow, net_charge, force_l1;
+} orc_field_result;
+
+/* Builds `ContinuousProblem` (eplace.rs:254-346). error_index receives the
+ * offending unit/member/filler index for indexed errors. */
+int32_t orc_create(const texo_gp_problem* problem, const texo_gp_params* params,
+                   orc_handle* out, uint64_t* error_index);
+void orc_destroy(orc_handle h);
+void orc_sizes(orc_handle h, uint64_t* units, uint64_t* fillers, uint64_t* coordinates,
+               uint32_t* bins_x, uint32_t* bins_y, uint32_t* num_fields);
+void orc_initial(orc_handle h, double* coordinates, double* lower, double* upper);
+void orc_fillers(orc_handle h, uint32_t* field, double* charge, double* xy);
+/* Overrides one filler's charge (to reproduce the reference's typed-error tests). */
+void orc_set_filler_charge(orc_handle h, uint64_t filler, double charge);
+/* Discrete capacity after fixed occupancy, [bins_tile] for one field. */
+void orc_capacity(orc_handle h, uint32_t field, uint32_t* out);
+
+/* ContinuousProblem::evaluate at coordinates [2(U+F)] (eplace.rs:137-205).
+ * Optional arrays (NULL to skip): wa_gradient [2U]; field_gradient
+ * [K][2(U+F)] raw; density [K][B]; potential [K][B]. threads: 1 = serial,
+ * >1 = the reference's fork-join shape on std::thread. */
+int32_t orc_evaluate(orc_handle h, const double* coordinates, double gamma, int32_t threads,
+                     double* wa_value, orc_field_result* fields, double* wa_gradient,
+                     double* field_gradient, double* density, double* potential,
+                     uint64_t* error_index);
+/* The device's fixed-point scatter restated on the CPU: FP32 taps, int64
+ * 2^-32 accumulation; grids [K][B]. Also returns per-field positive overflow
+ * (fixed point) and overflowed-bin counts. */
+int32_t orc_scatter_fixed(orc_handle h, const double* coordinates, int64_t* physical,
+                          int64_t* fillers, int64_t* overflow_fixed, uint64_t* overflow_bins);
+
+/* Runs `optimize_density_once` + `place` (Final criterion). threads as above;
+ * max_iterations (0 = params) caps this call. Returns the status; targets [2U],
+ * coordinates [2(U+F)] optional. */
+typedef struct orc_run_stats {
+  uint32_t iterations;
+  uint64_t evaluations;
+  uint64_t line_search_trials;
+  uint32_t num_fields;
+  double overflow[TEXO_GP_MAX_FIELDS];
+  double gamma;
+  double objective;
+  uint32_t converged;
+  uint32_t exhausted;
+  int32_t inner_status;
+  double hpwl;
+} orc_run_stats;
+int32_t orc_place(orc_handle h, int32_t threads, uint32_t max_iterations, uint32_t* targets,
+                  double* coordinates, orc_run_stats* stats);
+/* The same loop restarted from the handle's initial state, running exactly
+ * `iterations` outer iterations (for timing a bounded sample). */
+int32_t orc_hpwl(orc_handle h, const double* coordinates, double* hpwl);
+
+/* Preconditioners (analytical_placement.rs:177-231). */
+void orc_wirelength_preconditioner(orc_handle h, double* out_units);
+void orc_cell_incidence_weights(orc_handle h, double* out_cells);
+
+/* ---- Nesterov step with a caller-supplied evaluator ----------------------
+ * dynamic_nesterov_step, global_placement.rs:121-335. The callback returns 0
+ * on success or a nonzero error, which the step reports as
+ * TEXO_GP_ERR_EVALUATION with the callback's code in out->inner. */
+typedef int32_t (*orc_eval_cb)(void* user, const double* coordinates, uint64_t n, double* value,
+                               double* gradient, uint64_t* gradient_len, int64_t* payload);
+typedef struct orc_nesterov_state {
+  double* coordinates;            /* [n] */
+  double* previous;               /* [n] */
+  uint64_t n;
+  double momentum;
+  int32_t has_lipschitz;
+  double lipschitz;
+} orc_nesterov_state;
+typedef struct orc_step_out {
+  int32_t stationary;             /* 0 Accepted, 1 NumericallyStationary */
+  double objective, stationarity, coordinate_change;
+  uint64_t trials;
+  int64_t payload;
+  int32_t inner;
+  uint64_t error_index;
+  uint64_t expected, actual;
+} orc_step_out;
+int32_t orc_nesterov_step(orc_nesterov_state* state, const double* lower, uint64_t lower_len,
+                          const double* upper, uint64_t upper_len, const double* metric,
+                          uint64_t metric_len, orc_eval_cb cb, void* user, orc_step_out* out);
+/* DynamicNesterovState::new (global_placement.rs:38-53): projects when possible. */
+void orc_nesterov_init(orc_nesterov_state* state, const double* initial, const double* lower,
+                       uint64_t lower_len, const double* upper, uint64_t upper_len);
+double orc_box_metric_kkt(const double* gradient, const double* coordinates, const double* lower,
+                          const double* upper, const double* metric, uint64_t n);
+
+/* ---- eplace scalar rules (eplace.rs) ------------------------------------ */
+void orc_augmented(double energy, double initial_energy, double multiplier, double beta,
+                   double* value, double* coefficient);                  /* :1111-1124 */
+int32_t orc_multiplier_growth(double logarithm, double low, double high, double* growth); /* :1286-1298 */
+int32_t orc_area_adjusted_multiplier_step(const double* multipliers, uint64_t n, double high,
+                                          double* step);                 /* :1220-1232 */
+int32_t orc_field_gamma(double overflow, double target, double base, double* gamma); /* :1349-1367 */
+int32_t orc_weighted_gamma_mean(const double* gammas, const double* weights, uint64_t n,
+                                double fallback, double* mean);          /* :1369-1395 */
+double orc_overflow_target(uint32_t kind);                              /* :1300-1308 */
+int32_t orc_checkpoint_better(double max_excess, double total_excess, double best_max,
+                              double best_total);                       /* :106-119 */
+int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t* error_index);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,202 @@
+"""ctypes mirror of include/texo_gp.h (the C ABI of the placement engine).
+
+The structures here are byte-for-byte the C declarations; `load()` opens the
+in-tree CUDA library built by `texo_gb300.build`. There is no CPU fallback:
+if the library is missing, `load()` raises.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtexo_gp.so")
+
+# texo_gp_status (include/texo_gp.h), one per reference error variant.
+STATUS = {
+    0: "OK",
+    1: "EMPTY_GRID", 2: "GRID_TOO_LARGE", 3: "DENSITY_LENGTH", 4: "NONFINITE_DENSITY",
+    5: "EMPTY_UNIT", 6: "NONFINITE_UNIT_COORDINATE", 7: "INVALID_MEMBER_CHARGE",
+    8: "POINT_OUTSIDE_GRID", 9: "FIXED_CAPACITY_EXHAUSTED", 10: "INSUFFICIENT_CAPACITY",
+    11: "INSUFFICIENT_AREA", 12: "NONFINITE_FILLER", 13: "NEGATIVE_FILLER_CHARGE",
+    14: "UNEXPECTED_FILLER_KIND", 15: "FILLER_CHARGE_MISMATCH",
+    32: "INVALID_BOUNDS", 33: "INVALID_METRIC_LENGTH", 34: "NONPOSITIVE_METRIC",
+    35: "INVALID_INITIAL_COORDINATE", 36: "INVALID_MOMENTUM_PARAMETER",
+    37: "INVALID_LIPSCHITZ_ESTIMATE", 38: "INVALID_OBJECTIVE", 39: "INVALID_GRADIENT_LENGTH",
+    40: "NONFINITE_GRADIENT", 41: "LINE_SEARCH_OVERFLOW", 42: "ITERATION_OVERFLOW",
+    43: "EVALUATION",
+    64: "DENSITY_FIELD_CHANGED", 65: "INVALID_NORMALIZATION", 66: "DID_NOT_CONVERGE",
+    96: "INVALID_ARGUMENT", 97: "CUDA", 98: "OUT_OF_MEMORY", 99: "DEVICE_TIMEOUT",
+    100: "FIXED_POINT_RANGE", 101: "UNSUPPORTED", 102: "BUSY",
+}
+CODE = {v: k for k, v in STATUS.items()}
+
+KIND_LOGIC, KIND_LUT, KIND_REGISTER, KIND_MEMORY, KIND_CLOCK, KIND_IO, KIND_CONSTANT, KIND_DSP = range(8)
+DCT_FP32, DCT_BF16X3 = 0, 1
+ENGINE_HOST, ENGINE_DEVICE = 0, 1
+MAX_FIELDS = 4
+
+c_u32p = C.POINTER(C.c_uint32)
+c_u64p = C.POINTER(C.c_uint64)
+c_i64p = C.POINTER(C.c_int64)
+c_f64p = C.POINTER(C.c_double)
+c_u8p = C.POINTER(C.c_uint8)
+
+
+class TexoGpError(RuntimeError):
+    def __init__(self, code, where="", detail=""):
+        self.code = int(code)
+        self.name = STATUS.get(self.code, "UNKNOWN_%d" % self.code)
+        msg = "%s failed: %s" % (where, self.name) if where else self.name
+        if detail:
+            msg += " (" + detail + ")"
+        super().__init__(msg)
+
+
+class Field(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("lut_inputs", C.c_uint32)]
+
+
+class ProblemC(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32),
+        ("num_fields", C.c_uint32), ("fields", C.POINTER(Field)),
+        ("capacity", c_u32p),
+        ("num_fixed_occupancy", C.c_uint32), ("fixed_occupancy", c_u32p),
+        ("num_units", C.c_uint32),
+        ("initial_xy", c_f64p), ("lower_xy", c_f64p), ("upper_xy", c_f64p),
+        ("member_ptr", c_u32p), ("member_field", c_u32p), ("member_offset_xy", c_f64p),
+        ("member_charge", c_f64p), ("member_cell", c_u32p),
+        ("num_cells", C.c_uint32), ("cell_unit", c_u32p), ("cell_offset_xy", c_f64p),
+        ("cell_fixed", c_u8p), ("cell_fixed_xy", c_f64p),
+        ("num_nets", C.c_uint32), ("net_ptr", c_u32p), ("pin_cell", c_u32p),
+        ("num_timed_arcs", C.c_uint32), ("arc_driver_cell", c_u32p), ("arc_sink_cell", c_u32p),
+        ("arc_extra_weight", c_u64p),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gamma_base", C.c_double), ("max_iterations", C.c_uint32), ("beta", C.c_double),
+        ("initial_density_weight", C.c_double), ("alpha_low", C.c_double),
+        ("alpha_high", C.c_double), ("overflow_target_override", C.c_double),
+        ("bins_x", C.c_uint32), ("bins_y", C.c_uint32), ("target_density", C.c_double),
+        ("best_effort", C.c_int32), ("dct_mode", C.c_int32), ("engine", C.c_int32),
+        ("device", C.c_int32), ("objective_margin_ulps", C.c_double),
+        ("reserved", C.c_uint32 * 8),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32), ("iterations", C.c_uint32), ("evaluations", C.c_uint64),
+        ("line_search_trials", C.c_uint64), ("num_fields", C.c_uint32),
+        ("overflow", C.c_double * MAX_FIELDS), ("energy", C.c_double * MAX_FIELDS),
+        ("gamma", C.c_double), ("objective", C.c_double), ("hpwl", C.c_double),
+        ("error_index", C.c_uint64), ("error_field", C.c_uint32), ("converged", C.c_uint32),
+        ("elapsed_ms", C.c_double),
+    ]
+
+
+class FieldEval(C.Structure):
+    _fields_ = [
+        ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
+        ("force_l1", C.c_double), ("real_area", C.c_double), ("filler_charge", C.c_double),
+        ("overflow_fixed", C.c_int64), ("overflow_bins", C.c_uint64),
+    ]
+
+
+class Eval(C.Structure):
+    _fields_ = [("wirelength", C.c_double), ("num_fields", C.c_uint32),
+                ("fields", FieldEval * MAX_FIELDS)]
+
+
+class SynthSpec(C.Structure):
+    _fields_ = [("side", C.c_uint32), ("cells", C.c_uint32), ("io", C.c_uint32),
+                ("nets", C.c_uint32), ("sigma", C.c_double), ("p_local", C.c_double),
+                ("jitter", C.c_double), ("seed", C.c_uint64)]
+
+
+def default_params_py():
+    """The reference constants (eplace.rs:125-134), without loading the library."""
+    p = Params()
+    p.gamma_base = 8.0
+    p.max_iterations = 3000
+    p.beta = 2000.0
+    p.initial_density_weight = 1.0e-4
+    p.alpha_low = 1.05
+    p.alpha_high = 1.06
+    p.overflow_target_override = -1.0
+    p.bins_x = 0
+    p.bins_y = 0
+    p.target_density = 1.0
+    p.best_effort = 0
+    p.dct_mode = DCT_FP32
+    p.engine = ENGINE_HOST
+    p.device = 0
+    p.objective_margin_ulps = 64.0
+    return p
+
+
+# Every symbol include/texo_gp.h declares, with its ctypes signature.
+_P = C.c_void_p
+SIGNATURES = {
+    "texo_gp_abi_version": (C.c_uint32, []),
+    "texo_gp_default_params": (None, [C.POINTER(Params)]),
+    "texo_gp_status_name": (C.c_char_p, [C.c_int32]),
+    "texo_gp_last_error": (C.c_char_p, []),
+    "texo_gp_place": (C.c_int32, [C.POINTER(ProblemC), C.POINTER(Params), c_u32p, c_f64p, C.POINTER(Stats)]),
+    "texo_gp_create": (C.c_int32, [C.POINTER(ProblemC), C.POINTER(Params), C.POINTER(_P)]),
+    "texo_gp_destroy": (C.c_int32, [_P]),
+    "texo_gp_sizes": (C.c_int32, [_P, c_u64p, c_u64p, c_u64p, c_u32p, c_u32p, c_u32p]),
+    "texo_gp_initial": (C.c_int32, [_P, c_f64p, c_f64p, c_f64p]),
+    "texo_gp_fillers": (C.c_int32, [_P, c_u32p, c_f64p]),
+    "texo_gp_evaluate": (C.c_int32, [_P, c_f64p, C.c_double, C.POINTER(Eval), c_f64p, c_f64p, c_f64p, c_f64p]),
+    "texo_gp_scatter": (C.c_int32, [_P, c_f64p, c_i64p, c_i64p]),
+    "texo_gp_poisson": (C.c_int32, [_P, c_f64p, c_f64p, c_f64p]),
+    "texo_gp_run": (C.c_int32, [_P, C.c_uint32, c_u32p, c_f64p, C.POINTER(Stats)]),
+    "texo_gp_reset": (C.c_int32, [_P]),
+    "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
+    "texo_gp_synth_create": (C.c_int32, [C.POINTER(SynthSpec), C.POINTER(_P), C.POINTER(C.POINTER(ProblemC))]),
+    "texo_gp_synth_destroy": (C.c_int32, [_P]),
+    "texo_gp_batch_create": (C.c_int32, [C.POINTER(Params), C.c_uint64, C.c_uint32, C.POINTER(_P)]),
+    "texo_gp_batch_destroy": (C.c_int32, [_P]),
+    "texo_gp_batch_admit": (C.c_int32, [_P, C.POINTER(ProblemC), C.c_uint64, c_u32p]),
+    "texo_gp_batch_advance": (C.c_int32, [_P, C.c_uint32]),
+    "texo_gp_batch_retire": (C.c_int32, [_P, c_u64p, c_u32p, C.c_uint64, C.POINTER(Stats)]),
+    "texo_gp_batch_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u64p]),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Opens the in-tree engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("texo_gp CUDA library not built: %s (run texo_gb300.build.build())" % p)
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(code, where=""):
+    if code != 0:
+        detail = ""
+        if code == CODE["CUDA"] and _lib is not None:
+            detail = (_lib.texo_gp_last_error() or b"").decode()
+        raise TexoGpError(code, where, detail)
+    return code
+
+
+def ptr(arr, ctype):
+    """ctypes pointer into a contiguous numpy array (None for None)."""
+    if arr is None:
+        return None
+    return arr.ctypes.data_as(C.POINTER(ctype))
