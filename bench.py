@@ -1,0 +1,312 @@
+"""Benchmark: electrostatic global-placement iterations per second.
+
+Workload (default): the LFE5U-85-scale synthetic netlist — 42,000 movable
+unit-area LUT cells on a 210x210 site fabric, 365 fixed perimeter IO cells,
+50,000 nets in 2 / 3-5 / 6-32-pin bands with Gaussian index-grid locality
+(sigma 12 sites), a 256x256 bin grid, target density 0.9, WA gamma base 4
+bin widths, iteration cap 1000. Data are seeded synthetic (no public netlist
+is available offline).
+
+A step is one GP iteration: one dynamic Nesterov step with its objective
+evaluations plus the multiplier update, on a device-resident instance. Each
+step is timed with CUDA events on the engine's stream; between steps the L2
+is flushed by writing a 512 MiB buffer (outside the timed region). With N
+GPUs every rank places its own instance (replicas, seeds differ) and the
+value is all iterations over the max rank time.
+
+`--impl reference` times the CPU restatement of the reference path (the
+oracle port; the Rust reference cannot be built here) on the host cores.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (side, cells, io, nets, sigma, bins, target density, gamma base, cap)
+    "lfe5u-85-42k": (210, 42000, 365, 50000, 12.0, 256, 0.9, 4.0, 1000),
+    "ecp5-2k": (48, 2000, 96, 2400, 6.0, 64, 1.0, 4.0, 300),
+    "stress-1m": (1024, 1000000, 4096, 1200000, 24.0, 1024, 0.9, 4.0, 1000),
+}
+METRIC = "GP iters/s at 42k cells"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_problem(name, seed):
+    from texo_gb300 import problem as P
+    side, cells, io, nets, sigma = WORKLOADS[name][:5]
+    return P.synthetic(side, cells, io, nets, sigma, seed)
+
+
+def make_params(name, engine, dct):
+    from texo_gb300.placer import default_params
+    _, _, _, _, _, bins, td, gamma, cap = WORKLOADS[name]
+    return default_params(bins_x=bins, bins_y=bins, target_density=td, gamma_base=gamma,
+                          max_iterations=cap, best_effort=1, engine=engine, dct_mode=dct)
+
+
+def problem_bytes(p):
+    arrs = [p.capacity, p.initial_xy, p.lower_xy, p.upper_xy, p.member_ptr, p.member_field,
+            p.member_offset_xy, p.member_charge, p.member_cell, p.cell_unit, p.cell_offset_xy,
+            p.cell_fixed, p.cell_fixed_xy, p.net_ptr, p.pin_cell]
+    return int(sum(a.nbytes for a in arrs))
+
+
+# Algorithmic (compulsory) bytes per launch of each stage: every input read
+# once and every output written once, at the sizes of the instance.
+def stage_bytes(stage, n):
+    U, F, M, B, E, P, K = n["U"], n["F"], n["M"], n["B"], n["E"], n["P"], n["K"]
+    nobj = U + F
+    return {
+        "init": K * B * (8 + 8 + 8) + 2 * U * 8,
+        "scatter": M * (16 + 16 + 4 + 4 + 4) + F * (16 + 4 + 4) + K * B * 2 * 8 * 2,
+        "wa": P * (4 + 16) + nobj * 0 + U * 16 + E * (4 + 4) + 2 * U * 8 * 2,
+        "prep": K * B * (8 + 8 + 4),
+        "dct_row_fwd": K * B * 4 * 2 + B // max(1, n["Hb"]) * 0,
+        "dct_col_fwd": K * B * 4 * 3,
+        "dct_col_inv": K * B * 4 * 2,
+        "dct_row_inv": K * B * 4 * 3,
+        "gather": nobj * (16 + 8 * K) + M * (16 + 4 + 4) + K * B * 4,
+        "combine": nobj * (16 + 8 * K) + 2 * U * 8,
+        "extrapolate": nobj * (16 * 4 + 16),
+        "candidate": nobj * (16 * 4 + 8 + 16),
+        "kkt": nobj * (16 * 4 + 8 + 16),
+        "precond": nobj * (8 + 8 * K + 8),
+        "finalize": 0,
+    }.get(stage, 0)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            for line in out.strip().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    self.rows.append(f)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(name, seconds=15.0, threads=None):
+    """The oracle (CPU restatement) on a bounded sample of the same workload."""
+    from oracle import ffi
+    p = make_problem(name, 0)
+    prm = make_params(name, 0, 0)
+    threads = threads or 5
+    o = ffi.Oracle(p, prm)
+    iters, total = 0, 0.0
+    sample = 4
+    while total < seconds:
+        t = time.perf_counter()
+        st, _, _, s = o.place(threads=threads, max_iterations=sample)
+        dt = time.perf_counter() - t
+        iters += s.iterations
+        total += dt
+        if s.iterations < sample:
+            break
+        sample = min(sample * 2, 64)
+    return {"value": iters / total, "unit": "iter/s", "cores": threads, "kind": "port",
+            "sample": "%d oracle iterations from the start of the %s placement (%.1f s)" % (iters, name, total)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = max(1, min(os.cpu_count() or 1, 5))
+    from oracle import ffi
+    p = make_problem(args.workload, 0)
+    prm = make_params(args.workload, 0, 0)
+    o = ffi.Oracle(p, prm)
+    sample = args.reference_sample
+    for _ in range(args.warmup):
+        o.place(threads=threads, max_iterations=1)
+    iters, total = 0, 0.0
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        _, _, _, s = o.place(threads=threads, max_iterations=sample)
+        total += time.perf_counter() - t
+        iters += s.iterations
+    v = iters / total
+    line = {"metric": METRIC, "value": v, "unit": "iter/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(args),
+            "cpu_baseline": {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
+                             "sample": "%d-iteration prefix of the placement per step" % sample},
+            "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args):
+    side, cells, io, nets, sigma, bins, td, gamma, cap = WORKLOADS[args.workload]
+    return {"workload": args.workload, "cells": cells, "io": io, "nets": nets, "fabric": "%dx%d" % (side, side),
+            "bins": "%dx%d" % (bins, bins), "target_density": td, "gamma_base_bins": gamma, "cap": cap,
+            "engine": args.engine, "dct": args.dct, "l2": "flushed between steps (512 MiB write)",
+            "parallelism": "replicas x%d" % args.gpus}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="lfe5u-85-42k", choices=sorted(WORKLOADS))
+    ap.add_argument("--engine", default="host", choices=["host", "device"])
+    ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3"])
+    ap.add_argument("--reference-sample", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+    from texo_gb300 import build as engine_build
+    engine_build.build()
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer, place
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    engine = abi.ENGINE_HOST if args.engine == "host" else abi.ENGINE_DEVICE
+    dct = abi.DCT_FP32 if args.dct == "fp32" else abi.DCT_BF16X3
+    prob = make_problem(args.workload, rank)
+    prm = make_params(args.workload, engine, dct)
+    prm.device = local
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    g = Placer(prob, prm)
+    n = dict(U=g.units, F=g.num_fillers, M=int(prob.member_ptr[-1]), B=g.bins, Hb=g.bins_y,
+             E=prob.num_nets, P=prob.num_pins, K=g.num_fields)
+
+    state = {"prev": 0, "restarts": 0}
+
+    def one_step():
+        _, _, s = g.run(1, allow_nonconverged=True)
+        if s["iterations"] <= state["prev"]:
+            # the placement finished: start it again (outside the timed region)
+            g.reset()
+            state["restarts"] += 1
+            _, _, s = g.run(1, allow_nonconverged=True)
+        state["prev"] = s["iterations"]
+        return s
+
+    for _ in range(args.warmup):
+        s = one_step()
+    # timed steps
+    total_ms, launches = 0.0, 0
+    with Clocks(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            s = one_step()
+            total_ms += s["elapsed_ms"]
+            launches += s["kernel_launches"]
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * args.steps / (max_ms / 1000.0)
+    # per-stage device times and the dominant kernel's roofline
+    stages = g.stage_times(reps=20)
+    peak, peak_kind = peaks()
+    per_eval = {k: v for k, v in stages.items()}
+    order = sorted(per_eval, key=lambda k: -per_eval[k] * (1 if k not in ("finalize",) else 0))
+    dom = order[0]
+    achieved = stage_bytes(dom, n) / (stages[dom] * 1e-3) / 1e9
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                "stage_ms": stages}
+    # end to end through the C ABI from host buffers
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        targets, coords, s2 = place(prob, prm)
+        dt = time.perf_counter() - t0
+        e2e = {"value": s2["iterations"] / dt, "unit": "iter/s", "h2d_bytes_per_step": problem_bytes(prob),
+               "d2h_bytes_per_step": int(targets.nbytes + coords.nbytes),
+               "placement_s": dt, "iterations": s2["iterations"], "final_overflow": s2["overflow"],
+               "final_hpwl": s2["hpwl"], "converged": s2["converged"]}
+    line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": config_dict(args), "clocks": clk.summary(), "gpu_launches": int(launches),
+            "roofline": roofline, "e2e": e2e, "restarts": state["restarts"]}
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(args.workload)
+        except Exception as e:  # the oracle build can fail on an odd host
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -195,7 +195,8 @@ typedef struct texo_gp_stats {
   uint64_t error_index;          /* first offending index for indexed errors */
   uint32_t error_field;
   uint32_t converged;            /* 1 when every field reached its target */
-  double elapsed_ms;             /* device time of the placement loop */
+  double elapsed_ms;             /* device time of the call (CUDA events on the handle's stream) */
+  uint64_t kernel_launches;      /* kernels this library launched during the call */
 } texo_gp_stats;
 
 /* One evaluation of the objective components at given coordinates
@@ -282,6 +283,15 @@ int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_tar
 /* Restores the handle to its just-created state (positions, multipliers,
  * optimizer state) without touching the device allocations. */
 int32_t texo_gp_reset(texo_gp_handle h);
+
+/* Per-stage device times: runs each stage of one full objective evaluation at
+ * the handle's current coordinates `reps` times and writes the mean time of
+ * one launch in milliseconds, measured with CUDA events on the handle's
+ * stream, to ms[i] for the stages named by texo_gp_stage_name(i). Returns
+ * the stage count in *count. */
+int32_t texo_gp_stage_times(texo_gp_handle h, uint32_t reps, double* ms, uint32_t capacity,
+                            uint32_t* count);
+const char* texo_gp_stage_name(uint32_t stage);
 
 /* HPWL = sum over hypernets of the x and y pin spans at `coordinates`
  * (the continuous form of `exact_objective`, analytical_placement.rs:473-511),

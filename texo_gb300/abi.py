@@ -92,7 +92,7 @@ class Stats(C.Structure):
         ("overflow", C.c_double * MAX_FIELDS), ("energy", C.c_double * MAX_FIELDS),
         ("gamma", C.c_double), ("objective", C.c_double), ("hpwl", C.c_double),
         ("error_index", C.c_uint64), ("error_field", C.c_uint32), ("converged", C.c_uint32),
-        ("elapsed_ms", C.c_double),
+        ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64),
     ]
 
 
@@ -155,6 +155,8 @@ SIGNATURES = {
     "texo_gp_run": (C.c_int32, [_P, C.c_uint32, c_u32p, c_f64p, C.POINTER(Stats)]),
     "texo_gp_reset": (C.c_int32, [_P]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
+    "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),
+    "texo_gp_stage_name": (C.c_char_p, [C.c_uint32]),
     "texo_gp_synth_create": (C.c_int32, [C.POINTER(SynthSpec), C.POINTER(_P), C.POINTER(C.POINTER(ProblemC))]),
     "texo_gp_synth_destroy": (C.c_int32, [_P]),
     "texo_gp_batch_create": (C.c_int32, [C.POINTER(Params), C.c_uint64, C.c_uint32, C.POINTER(_P)]),

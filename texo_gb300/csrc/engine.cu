@@ -1,0 +1,1090 @@
+// engine.cu — device buffers of one instance, the host-driven controller and
+// the C ABI entry points of include/texo_gp.h.
+//
+// The controller restates, on device buffers, the reference's
+//   optimize_density_once          (crates/texo-pnr/src/eplace.rs:439-582)
+//   dynamic_nesterov_step          (crates/texo-pnr/src/global_placement.rs:121-335)
+// Every vector operation and reduction runs on the GPU; the host reads back a
+// small scalar block once per objective evaluation.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "engine.h"
+
+namespace tgp {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& s) { g_last_error = s; }
+
+#define CU(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+      return e_ == cudaErrorMemoryAllocation ? TEXO_GP_ERR_OUT_OF_MEMORY : TEXO_GP_ERR_CUDA; \
+    }                                                                                      \
+  } while (0)
+#define TRY(call)                \
+  do {                           \
+    int32_t s_ = (call);         \
+    if (s_ != TEXO_GP_OK) return s_; \
+  } while (0)
+
+Instance::~Instance() {
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  for (void* p : allocations) cudaFree(p);
+  if (h_scal) cudaFreeHost(h_scal);
+  if (h_iscal) cudaFreeHost(h_iscal);
+}
+
+int32_t Instance::alloc(void** p, size_t n) {
+  n = n ? n : 16;
+  CU(cudaMalloc(p, n));
+  allocations.push_back(*p);
+  bytes += n;
+  return TEXO_GP_OK;
+}
+
+namespace {
+template <typename T>
+int32_t upload_vec(Instance& I, T** dst, const std::vector<T>& v) {
+  TRY(I.alloc((void**)dst, v.size() * sizeof(T)));
+  if (!v.empty()) CU(cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, I.stream));
+  return TEXO_GP_OK;
+}
+template <typename T>
+int32_t zeros(Instance& I, T** dst, size_t n) {
+  TRY(I.alloc((void**)dst, n * sizeof(T)));
+  CU(cudaMemsetAsync(*dst, 0, n * sizeof(T), I.stream));
+  return TEXO_GP_OK;
+}
+std::vector<double> dct_basis(uint32_t n) {
+  const double nf = (double)n;
+  std::vector<double> b((size_t)n * n);
+  for (uint32_t f = 0; f < n; ++f) {
+    const double s = f == 0 ? std::sqrt(1.0 / nf) : std::sqrt(2.0 / nf);
+    for (uint32_t c = 0; c < n; ++c) b[(size_t)f * n + c] = s * std::cos(3.14159265358979323846 * f * (c + 0.5) / nf);
+  }
+  return b;
+}
+}  // namespace
+
+int32_t Instance::upload() {
+  HostModel& h = m;
+  CU(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CU(cudaGetDeviceProperties(&prop, device));
+  sms = prop.multiProcessorCount;
+  CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  const size_t nobj = (size_t)h.U + h.F, B = h.bins(), K = h.K;
+  // enough blocks to cover the widest stage, up to 8 per SM
+  const size_t widest = std::max(std::max(std::max(nobj, (size_t)h.Mm + h.F), std::max(B, h.pin_unit.size() / 2)), (size_t)1);
+  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * 8), (size_t)kMaxPartials);
+  nvb = std::max(nvb, 1);
+  Dev& D = d;
+  D.U = (int)h.U;
+  D.F = (int)h.F;
+  D.nobj = (int)nobj;
+  D.K = (int)K;
+  D.Mm = (int)h.Mm;
+  D.B = (int)B;
+  D.g = Grid{(int)h.W, (int)h.H, (int)h.Wb, (int)h.Hb, h.sx, h.sy, h.identity ? 1 : 0};
+  TRY(upload_vec(*this, (int**)&D.mem_unit, h.mem_unit));
+  TRY(upload_vec(*this, (double**)&D.mem_off, h.mem_off));
+  TRY(upload_vec(*this, (float**)&D.mem_q, h.mem_q));
+  TRY(upload_vec(*this, (int**)&D.mem_field, h.mem_field));
+  TRY(upload_vec(*this, (int**)&D.unit_mem_ptr, h.unit_mem_ptr));
+  TRY(upload_vec(*this, (int**)&D.fil_field, h.fil_field));
+  std::vector<float> fq(h.fil_q.begin(), h.fil_q.end());
+  TRY(upload_vec(*this, (float**)&D.fil_q, fq));
+  D.n_classes = h.n_classes;
+  std::memcpy(D.class_begin, h.class_begin, sizeof(D.class_begin));
+  std::memcpy(D.class_group, h.class_group, sizeof(D.class_group));
+  D.n_hpwl_nets = h.n_hpwl_nets;
+  TRY(upload_vec(*this, (int**)&D.net_ptr, h.net_ptr));
+  TRY(upload_vec(*this, (int**)&D.pin_unit, h.pin_unit));
+  TRY(upload_vec(*this, (double**)&D.pin_base, h.pin_base));
+  TRY(upload_vec(*this, (float**)&D.net_w, h.net_w));
+  // grids
+  TRY(zeros(*this, &D.phys, K * B));
+  TRY(zeros(*this, &D.fill, K * B));
+  std::vector<long long> capfix(K * B), capsum(std::max<size_t>(K, 1), 0);
+  for (size_t f = 0; f < K; ++f)
+    for (size_t i = 0; i < B; ++i) {
+      capfix[f * B + i] = (long long)std::nearbyint(h.smoothed[f][i] * kFix);
+      capsum[f] += capfix[f * B + i];
+    }
+  TRY(upload_vec(*this, (long long**)&D.capfix, capfix));
+  TRY(upload_vec(*this, (long long**)&D.capsum, capsum));
+  TRY(zeros(*this, &D.rho, K * B));
+  TRY(zeros(*this, &D.t1, K * B));
+  TRY(zeros(*this, &D.t2, K * B));
+  TRY(zeros(*this, &D.phi, K * B));
+  auto bx = dct_basis(h.Wb), by = dct_basis(h.Hb);
+  std::vector<float> cx(bx.size()), cxt(bx.size()), cy(by.size()), cyt(by.size());
+  for (uint32_t i = 0; i < h.Wb; ++i)
+    for (uint32_t j = 0; j < h.Wb; ++j) {
+      cx[(size_t)i * h.Wb + j] = (float)bx[(size_t)i * h.Wb + j];
+      cxt[(size_t)j * h.Wb + i] = (float)bx[(size_t)i * h.Wb + j];
+    }
+  for (uint32_t i = 0; i < h.Hb; ++i)
+    for (uint32_t j = 0; j < h.Hb; ++j) {
+      cy[(size_t)i * h.Hb + j] = (float)by[(size_t)i * h.Hb + j];
+      cyt[(size_t)j * h.Hb + i] = (float)by[(size_t)i * h.Hb + j];
+    }
+  TRY(upload_vec(*this, (float**)&D.Cx, cx));
+  TRY(upload_vec(*this, (float**)&D.CxT, cxt));
+  TRY(upload_vec(*this, (float**)&D.Cy, cy));
+  TRY(upload_vec(*this, (float**)&D.CyT, cyt));
+  std::vector<float> ie(B);
+  for (uint32_t ky = 0; ky < h.Hb; ++ky) {
+    const double sy = std::sin(3.14159265358979323846 * ky / (2.0 * h.Hb));
+    const double ly = 4.0 * (sy * sy);
+    for (uint32_t kx = 0; kx < h.Wb; ++kx) {
+      const double sx = std::sin(3.14159265358979323846 * kx / (2.0 * h.Wb));
+      const double l = 4.0 * (sx * sx) + ly;
+      ie[(size_t)ky * h.Wb + kx] = (kx == 0 && ky == 0) ? 0.0f : (float)(1.0 / l);
+    }
+  }
+  TRY(upload_vec(*this, (float**)&D.inv_eig, ie));
+  TRY(zeros(*this, &D.wa_fix, 2 * (size_t)h.U));
+  TRY(zeros(*this, &D.graw, std::max<size_t>(K, 1) * nobj));
+  // optimizer
+  std::vector<double> lo(h.lo), hi(h.hi);
+  TRY(upload_vec(*this, (double**)&D.lo, lo));
+  TRY(upload_vec(*this, (double**)&D.hi, hi));
+  TRY(zeros(*this, &D.P, nobj));
+  TRY(upload_vec(*this, (double**)&D.pre_static, h.pre_static));
+  TRY(upload_vec(*this, (double**)&D.pre_q, h.pre_q));
+  TRY(zeros(*this, &bufX, nobj));
+  TRY(zeros(*this, &bufXp, nobj));
+  TRY(zeros(*this, &bufY, nobj));
+  TRY(zeros(*this, &bufC, nobj));
+  TRY(zeros(*this, &gX, nobj));
+  TRY(zeros(*this, &gY, nobj));
+  TRY(zeros(*this, &gC, nobj));
+  TRY(zeros(*this, &best, std::max<size_t>(h.U, 1)));
+  TRY(zeros(*this, &prev_targets, 2 * (size_t)h.U));
+  TRY(zeros(*this, &mismatch, 1));
+  // reductions
+  TRY(zeros(*this, &r.p.sum, (size_t)kSlots * kMaxPartials));
+  TRY(zeros(*this, &r.p.isum, (size_t)kISlots * kMaxPartials));
+  TRY(zeros(*this, &r.p.mx, (size_t)kMSlots * kMaxPartials));
+  TRY(zeros(*this, &r.scal, kScalars));
+  TRY(zeros(*this, &r.iscal, kIScalars));
+  CU(cudaMallocHost((void**)&h_scal, kScalars * sizeof(double)));
+  CU(cudaMallocHost((void**)&h_iscal, kIScalars * sizeof(long long)));
+  std::memset(h_scal, 0, kScalars * sizeof(double));
+  h_scal[SC_BETA] = h.params.beta;
+  for (uint32_t f = 0; f < K; ++f) {
+    h_scal[SC_REAL_AREA + f] = h.real_area[f];
+    h_scal[SC_E0 + f] = 1.0;
+    h_scal[SC_LAMBDA + f] = 0.0;
+  }
+  CU(cudaMemcpyAsync(r.scal, h_scal, kScalars * sizeof(double), cudaMemcpyHostToDevice, stream));
+  CU(cudaMemcpyAsync(bufX, h.init.data(), nobj * sizeof(double2), cudaMemcpyHostToDevice, stream));
+  CU(cudaStreamSynchronize(stream));
+  return TEXO_GP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-driven controller.
+// ---------------------------------------------------------------------------
+struct EvalRec {
+  double value = 0, wa = 0, wal1 = 0;
+  double energy[kMaxFields] = {}, overflow[kMaxFields] = {}, force[kMaxFields] = {}, rawl1[kMaxFields] = {};
+  double net_charge[kMaxFields] = {};
+  long long overflow_fixed[kMaxFields] = {}, overflow_bins[kMaxFields] = {};
+  long long bad = std::numeric_limits<long long>::max();
+};
+
+static inline double midpoint1(double b) {
+  const double hi = std::numeric_limits<double>::max() / 2.0;
+  if (std::fabs(b) <= hi) return (1.0 + b) / 2.0;
+  return 0.5 + b / 2.0;
+}
+static inline double half_nonzero(double v) {
+  const double h = v * 0.5;
+  return h == 0.0 ? v : h;
+}
+
+struct Controller {
+  Instance& I;
+  // eplace state (eplace.rs:439-582)
+  int phase = 0;              // 0 fresh, 1 running, 2 finished
+  std::vector<double> lambda, e0;
+  double mstep = 0.0;
+  EvalRec current;
+  double gamma = 0.0;
+  uint32_t completed = 0;
+  double best_max = 0, best_tot = 0;
+  bool have_prev_stationary = false;
+  bool converged = false, exhausted = false;
+  int32_t final_status = TEXO_GP_OK;
+  // Nesterov state (global_placement.rs:29-58)
+  double a = 1.0;
+  bool has_L = false;
+  double L = 0.0;
+  bool density_at_x = false;  // graw/phi/energies describe bufX
+  // statistics
+  uint64_t evaluations = 0, device_evaluations = 0, trials = 0;
+  double last_objective = 0.0;
+  double elapsed_ms = 0.0;
+  unsigned long long launches = 0;
+
+  explicit Controller(Instance& i) : I(i) {}
+
+  double margin(double x, double y) const {
+    const double eps = std::max(std::numeric_limits<double>::epsilon(), I.m.params.objective_margin_ulps * 0x1p-24);
+    return eps * (1.0 + std::fabs(x) + std::fabs(y));
+  }
+
+  int32_t sync_read() {
+    CU(cudaMemcpyAsync(I.h_scal, I.r.scal, kScalars * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaMemcpyAsync(I.h_iscal, I.r.iscal, kIScalars * sizeof(long long), cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaStreamSynchronize(I.stream));
+    CU(cudaGetLastError());
+    return TEXO_GP_OK;
+  }
+  int32_t push_inputs() {
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      I.h_scal[SC_LAMBDA + f] = lambda.empty() ? 0.0 : lambda[f];
+      I.h_scal[SC_E0 + f] = e0.empty() ? 1.0 : e0[f];
+    }
+    CU(cudaMemcpyAsync(I.r.scal + SC_LAMBDA, I.h_scal + SC_LAMBDA, 2 * kMaxFields * sizeof(double),
+                       cudaMemcpyHostToDevice, I.stream));
+    return TEXO_GP_OK;
+  }
+
+  // Enqueues one objective evaluation (ContinuousProblem::evaluate +
+  // combined_objective). With reuse, the density side of `pos` is the one
+  // already on the device (same coordinates), and only WA and the
+  // combination are recomputed.
+  void enqueue_eval(const double2* pos, double2* g, double gam, bool reuse) {
+    const Dev& D = I.d;
+    cudaStream_t s = I.stream;
+    const int nvb = I.nvb;
+    if (!reuse && I.m.has_density) {
+      launch_init(D, true, true, nvb, s);
+      launch_scatter(D, I.r, pos, nvb, s);
+      launch_prep(D, I.r, nvb, s);
+      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, nvb, s);
+      launch_gather(D, I.r, pos, nvb, s);
+    } else {
+      launch_init(D, false, true, nvb, s);
+    }
+    launch_wa(D, I.r, pos, gam, nvb, s);
+    launch_finalize(D, I.r, nvb, (reuse || !I.m.has_density) ? FIN_WA : FIN_ENERGY, s);
+    launch_combine(D, I.r, g, nvb, s);
+    launch_finalize(D, I.r, nvb, FIN_COMBINE, s);
+    device_evaluations++;
+  }
+  void read_eval(EvalRec& e) const {
+    const double* sc = I.h_scal;
+    const long long* si = I.h_iscal;
+    e.value = sc[SC_VALUE];
+    e.wa = sc[SC_WA];
+    e.wal1 = sc[SC_WAL1];
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      e.energy[f] = sc[SC_ENERGY + f];
+      e.overflow[f] = sc[SC_OVERFLOW + f];
+      e.force[f] = sc[SC_FORCE + f];
+      e.rawl1[f] = sc[SC_RAWL1 + f];
+      e.net_charge[f] = sc[SC_MEAN + f];
+      e.overflow_fixed[f] = si[SI_OVERFLOW_FIXED + f];
+      e.overflow_bins[f] = si[SI_OVER_BINS + f];
+    }
+    e.bad = si[SI_BAD];
+  }
+  int32_t evaluate(const double2* pos, double2* g, double gam, bool reuse, EvalRec& e) {
+    enqueue_eval(pos, g, gam, reuse);
+    TRY(sync_read());
+    read_eval(e);
+    evaluations++;
+    return TEXO_GP_OK;
+  }
+  int32_t checked(const EvalRec& e) const {
+    if (!std::isfinite(e.value)) return TEXO_GP_ERR_INVALID_OBJECTIVE;
+    if (e.bad != std::numeric_limits<long long>::max()) return TEXO_GP_ERR_NONFINITE_GRADIENT;
+    return TEXO_GP_OK;
+  }
+
+  // ---- eplace rules (eplace.rs:1111-1415) ----
+  int32_t field_gamma(double overflow, double target, double base, double& g) const {
+    if (!std::isfinite(overflow) || overflow < 0.0 || !(target >= 0.0 && target < 1.0) || !(base > 0.0))
+      return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    const double slope = 2.0 / (1.0 - target), intercept = 1.0 - slope;
+    g = base * std::pow(10.0, slope * overflow + intercept);
+    return (std::isfinite(g) && g > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
+  int32_t adaptive_gamma(const EvalRec& e, double& out) const {
+    const double base = I.m.gamma_base_tiles();
+    double ws = 0.0, wsum = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      double g;
+      TRY(field_gamma(e.overflow[f], I.m.overflow_target(f), base, g));
+      const double w = I.m.gamma_weight[f];
+      ws += g * w;
+      wsum += w;
+    }
+    out = wsum == 0.0 ? base : ws / wsum;
+    return (std::isfinite(out) && out > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
+  bool stop_reached(const EvalRec& e) const {
+    for (uint32_t f = 0; f < I.m.K; ++f)
+      if (!(e.overflow[f] <= I.m.overflow_target(f))) return false;
+    return true;
+  }
+  void excess(const EvalRec& e, double& mx, double& tot) const {
+    mx = 0.0;
+    tot = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      const double x = std::fmax(e.overflow[f] - I.m.overflow_target(f), 0.0);
+      mx = std::fmax(mx, x);
+      tot += x;
+    }
+  }
+  int32_t validate_initial(const EvalRec& e) const {
+    bool ok = std::isfinite(e.wa) && e.bad == std::numeric_limits<long long>::max();
+    for (uint32_t f = 0; f < I.m.K && ok; ++f)
+      ok = std::isfinite(e.energy[f]) && e.energy[f] >= 0.0 && std::isfinite(e.overflow[f]) &&
+           std::isfinite(e.force[f]) && e.force[f] >= 0.0;
+    return ok ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
+  int32_t validate_fields(const EvalRec& e) const {
+    for (uint32_t f = 0; f < I.m.K; ++f)
+      if (!std::isfinite(e.energy[f]) || !std::isfinite(e0[f]) || e0[f] <= 0.0) return TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
+    return TEXO_GP_OK;
+  }
+  int32_t update_multipliers(const EvalRec& e) {
+    TRY(validate_fields(e));
+    const double beta = I.m.params.beta;
+    double sg[kMaxFields], nn = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      const double ne = e.energy[f] / e0[f];
+      sg[f] = ne + 0.5 * beta * ne * ne;
+      if (!std::isfinite(sg[f]) || sg[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+      nn += sg[f] * sg[f];
+    }
+    const double norm = std::sqrt(nn);
+    if (norm != 0.0) {
+      if (!std::isfinite(norm) || !std::isfinite(mstep) || mstep <= 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+      for (uint32_t f = 0; f < I.m.K; ++f) {
+        lambda[f] += mstep * sg[f] / norm;
+        if (!std::isfinite(lambda[f]) || lambda[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+      }
+    }
+    // next_multiplier_step (eplace.rs:1261-1298)
+    double en = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      const double ne = e.energy[f] / e0[f];
+      en += ne * ne;
+    }
+    const double lg = std::log(beta * std::sqrt(en) + 1.0);
+    if (!std::isfinite(lg) || lg < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    const double lo = I.m.params.alpha_low, hi = I.m.params.alpha_high;
+    const double growth = lo + (1.0 - 1.0 / (1.0 + lg)) * (hi - lo);
+    if (!(growth >= lo && growth <= hi)) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    mstep *= growth;
+    return (std::isfinite(mstep) && mstep > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
+
+  // ---- one dynamic Nesterov step on the device buffers ----
+  int32_t nesterov_step(double gam, EvalRec& payload, bool& stationary) {
+    const Dev& D = I.d;
+    cudaStream_t s = I.stream;
+    const int nvb = I.nvb;
+    if (!std::isfinite(a) || a < 1.0) return TEXO_GP_ERR_INVALID_MOMENTUM_PARAMETER;
+    if (has_L && (!std::isfinite(L) || L <= 0.0)) return TEXO_GP_ERR_INVALID_LIPSCHITZ_ESTIMATE;
+    // preconditioner range for the denominator checks
+    launch_precond(D, I.r, nvb, s);
+    launch_finalize(D, I.r, nvb, FIN_PRECOND, s);
+    EvalRec eo;
+    TRY(evaluate(I.bufX, I.gX, gam, density_at_x, eo));
+    if (I.h_iscal[SI_PBAD]) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    const double pmin = I.h_scal[SC_PMIN], pmax = I.h_scal[SC_PMAX];
+    TRY(checked(eo));
+    bool restart = false;
+    bool has_wL = has_L;
+    double wL = L;
+    uint64_t step_trials = 0;
+    for (;;) {  // 'step
+      const double momentum = restart ? 1.0 : a;
+      const double next_m = midpoint1(std::sqrt(1.0 + 4.0 * momentum * momentum));
+      if (!std::isfinite(next_m)) return TEXO_GP_ERR_ITERATION_OVERFLOW;
+      const double extrap = (momentum - 1.0) / next_m;
+      bool y_is_origin = true;
+      if (!restart) {
+        launch_extrapolate(D, I.r, I.bufX, I.bufXp, extrap, I.bufY, nvb, s);
+        launch_finalize(D, I.r, nvb, FIN_DIFF, s);
+        TRY(sync_read());
+        y_is_origin = I.h_iscal[SI_DIFF] == 0;
+      }
+      const double2* ybuf = y_is_origin ? I.bufX : I.bufY;
+      const double2* gy = y_is_origin ? I.gX : I.gY;
+      double f_y = eo.value;
+      if (!y_is_origin) {
+        enqueue_eval(I.bufY, I.gY, gam, false);
+        density_at_x = false;
+      }
+      launch_kkt(D, I.r, ybuf, gy, nullptr, nvb, s);
+      launch_finalize(D, I.r, nvb, FIN_KKT, s);
+      TRY(sync_read());
+      if (!y_is_origin) {
+        EvalRec ey;
+        read_eval(ey);
+        evaluations++;
+        TRY(checked(ey));
+        f_y = ey.value;
+      }
+      const double y_stat = I.h_scal[SC_KKT];
+      if (!std::isfinite(y_stat)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+      if (y_stat == 0.0) {
+        if (!y_is_origin) {
+          restart = true;
+          continue;
+        }
+        CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        a = 1.0;
+        stationary = true;
+        payload = eo;
+        trials += step_trials;
+        last_objective = eo.value;
+        return TEXO_GP_OK;
+      }
+      double tL = half_nonzero(has_wL ? wL : y_stat);
+      bool may_reduce = true;
+      bool restart_step = false;
+      EvalRec ec;
+      for (;;) {
+        step_trials++;
+        if (!std::isfinite(tL * pmax)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+        if (tL * pmin == 0.0) {
+          tL *= 2.0;
+          may_reduce = false;
+          if (!std::isfinite(tL)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+          continue;
+        }
+        launch_candidate(D, I.r, ybuf, gy, tL, I.bufC, nvb, s);
+        launch_finalize(D, I.r, nvb, FIN_CAND, s);
+        // The candidate is evaluated speculatively in the same submission;
+        // it is discarded when the candidate equals y.
+        enqueue_eval(I.bufC, I.gC, gam, false);
+        density_at_x = false;
+        TRY(sync_read());
+        const long long changed = I.h_iscal[SI_DIFF];
+        const double dot = I.h_scal[SC_DOT], msn = I.h_scal[SC_MSN];
+        if (changed == 0) {
+          if (may_reduce) {
+            const double smaller = half_nonzero(tL);
+            if (smaller < tL) {
+              tL = smaller;
+              continue;
+            }
+          }
+          if (!y_is_origin) {
+            restart = true;
+            has_wL = true;
+            wL = tL;
+            restart_step = true;
+            break;
+          }
+          CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+          a = 1.0;
+          has_L = true;
+          L = tL;
+          stationary = true;
+          payload = eo;
+          trials += step_trials;
+          last_objective = eo.value;
+          return TEXO_GP_OK;
+        }
+        read_eval(ec);
+        evaluations++;
+        TRY(checked(ec));
+        const double upper = f_y + dot + 0.5 * tL * msn;
+        if (!std::isfinite(upper)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+        const bool smooth = ec.value <= upper + margin(ec.value, upper);
+        const bool mono = ec.value <= eo.value + margin(ec.value, eo.value);
+        if (smooth && mono) break;
+        if (smooth && !restart) {
+          restart = true;
+          has_wL = true;
+          wL = tL;
+          restart_step = true;
+          break;
+        }
+        tL *= 2.0;
+        may_reduce = false;
+        if (!std::isfinite(tL)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+      }
+      if (restart_step) continue;
+      // accept: stationarity at the candidate and the coordinate change
+      launch_kkt(D, I.r, I.bufC, I.gC, I.bufX, nvb, s);
+      launch_finalize(D, I.r, nvb, FIN_KKT, s);
+      TRY(sync_read());
+      if (!std::isfinite(I.h_scal[SC_KKT])) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
+      std::swap(I.bufXp, I.bufX);   // previous <- origin
+      std::swap(I.bufX, I.bufC);    // origin <- candidate
+      std::swap(I.gX, I.gC);
+      a = next_m;
+      has_L = true;
+      L = tL;
+      density_at_x = true;
+      stationary = false;
+      payload = ec;
+      trials += step_trials;
+      last_objective = ec.value;
+      return TEXO_GP_OK;
+    }
+  }
+
+  int32_t save_best() {
+    CU(cudaMemcpyAsync(I.best, I.bufX, (size_t)I.m.U * sizeof(double2), cudaMemcpyDeviceToDevice, I.stream));
+    return TEXO_GP_OK;
+  }
+
+  // optimize_density_once (eplace.rs:439-582), resumable: runs at most
+  // `budget` more iterations when budget > 0.
+  int32_t run(uint32_t budget) {
+    if (phase == 2) return final_status;
+    if (!I.m.has_density) {
+      phase = 2;
+      converged = true;
+      return TEXO_GP_OK;
+    }
+    const uint32_t K = I.m.K;
+    if (phase == 0) {
+      lambda.assign(K, 0.0);
+      e0.assign(K, 1.0);
+      TRY(push_inputs());
+      EvalRec probe;
+      TRY(evaluate(I.bufX, I.gX, I.m.gamma_base_tiles(), false, probe));
+      TRY(validate_initial(probe));
+      double g0;
+      TRY(adaptive_gamma(probe, g0));
+      EvalRec initial;
+      TRY(evaluate(I.bufX, I.gX, g0, true, initial));
+      TRY(validate_initial(initial));
+      for (uint32_t f = 0; f < K; ++f) e0[f] = std::fmax(initial.energy[f], 1.0);
+      TRY(validate_fields(initial));
+      CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)I.d.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, I.stream));
+      TRY(save_best());
+      excess(initial, best_max, best_tot);
+      density_at_x = true;
+      current = initial;
+      gamma = g0;
+      phase = 1;
+      if (stop_reached(initial)) {
+        phase = 2;
+        converged = true;
+        return TEXO_GP_OK;
+      }
+      // initial_density_multiplier (eplace.rs:1126-1148)
+      double dens = 0.0;
+      for (uint32_t f = 0; f < K; ++f) dens += initial.rawl1[f];
+      const double m0 = (initial.wal1 == 0.0 || dens == 0.0) ? 1.0 : I.m.params.initial_density_weight * initial.wal1 / dens;
+      if (!(std::isfinite(m0) && m0 > 0.0)) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+      lambda.assign(K, m0);
+      mstep = I.m.params.alpha_high - 1.0;
+      TRY(push_inputs());
+    }
+    uint32_t done_now = 0;
+    for (;;) {
+      if (stop_reached(current)) {
+        converged = true;
+        phase = 2;
+        break;
+      }
+      if (completed >= I.m.params.max_iterations) {
+        exhausted = true;
+        phase = 2;
+        final_status = I.m.params.best_effort ? TEXO_GP_OK : TEXO_GP_ERR_DID_NOT_CONVERGE;
+        break;
+      }
+      if (budget && done_now >= budget) break;
+      double gam;
+      TRY(adaptive_gamma(current, gam));
+      completed++;
+      done_now++;
+      gamma = gam;
+      EvalRec payload;
+      bool stationary = false;
+      TRY(nesterov_step(gam, payload, stationary));
+      TRY(validate_fields(payload));
+      current = payload;
+      double mx, tot;
+      excess(current, mx, tot);
+      if (mx < best_max || (mx == best_max && tot < best_tot)) {
+        TRY(save_best());
+        best_max = mx;
+        best_tot = tot;
+      }
+      if (stop_reached(current)) {
+        converged = true;
+        phase = 2;
+        break;
+      }
+      if (!stationary) {
+        have_prev_stationary = false;
+      } else {
+        CU(cudaMemsetAsync(I.mismatch, 0, sizeof(unsigned long long), I.stream));
+        launch_round_compare(I.d, I.bufX, I.prev_targets, (int)I.m.W, (int)I.m.H, I.mismatch, I.nvb, I.stream);
+        unsigned long long mm = 0;
+        CU(cudaMemcpyAsync(&mm, I.mismatch, sizeof(mm), cudaMemcpyDeviceToHost, I.stream));
+        CU(cudaStreamSynchronize(I.stream));
+        const bool fixed = have_prev_stationary && mm == 0;
+        have_prev_stationary = true;
+        if (fixed) {
+          exhausted = true;
+          phase = 2;
+          final_status = I.m.params.best_effort ? TEXO_GP_OK : TEXO_GP_ERR_DID_NOT_CONVERGE;
+          break;
+        }
+      }
+      TRY(update_multipliers(current));
+      TRY(push_inputs());
+    }
+    return phase == 2 ? final_status : TEXO_GP_OK;
+  }
+};
+
+}  // namespace tgp
+
+using namespace tgp;
+
+struct texo_gp_handle_s {
+  std::unique_ptr<Instance> inst;
+  std::unique_ptr<Controller> ctl;
+  std::mutex mu;
+};
+
+namespace {
+uint32_t round_coord(double v, uint32_t extent) {
+  double r = std::round(v);
+  r = r < 0.0 ? 0.0 : (r > (double)(extent - 1) ? (double)(extent - 1) : r);
+  return (uint32_t)r;
+}
+
+int32_t handle_targets(texo_gp_handle h, uint32_t* out, double* coords, texo_gp_stats* st, int32_t status) {
+  Instance& I = *h->inst;
+  Controller& C = *h->ctl;
+  const size_t nobj = (size_t)I.d.nobj;
+  std::vector<double> best(2 * (size_t)I.m.U);
+  if (I.m.has_density) {
+    CU(cudaMemcpyAsync(best.data(), I.best, best.size() * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  } else {
+    std::copy(I.m.init.begin(), I.m.init.begin() + best.size(), best.begin());
+  }
+  std::vector<double> cur(2 * nobj);
+  CU(cudaMemcpyAsync(cur.data(), I.bufX, cur.size() * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  launch_hpwl(I.d, I.r, I.bufX, I.nvb, I.stream);
+  launch_finalize(I.d, I.r, I.nvb, FIN_HPWL, I.stream);
+  CU(cudaMemcpyAsync(I.h_scal + SC_HPWL, I.r.scal + SC_HPWL, sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  if (out)
+    for (uint32_t u = 0; u < I.m.U; ++u) {
+      out[2 * (size_t)u] = round_coord(best[2 * (size_t)u], I.m.W);
+      out[2 * (size_t)u + 1] = round_coord(best[2 * (size_t)u + 1], I.m.H);
+    }
+  if (coords) std::memcpy(coords, cur.data(), cur.size() * sizeof(double));
+  if (st) {
+    st->status = status;
+    st->iterations = C.completed;
+    st->evaluations = C.evaluations;
+    st->line_search_trials = C.trials;
+    st->num_fields = I.m.K;
+    for (uint32_t f = 0; f < I.m.K && f < TEXO_GP_MAX_FIELDS; ++f) {
+      st->overflow[f] = C.current.overflow[f];
+      st->energy[f] = C.current.energy[f];
+    }
+    st->gamma = C.gamma;
+    st->objective = C.last_objective;
+    st->hpwl = I.h_scal[SC_HPWL];
+    st->converged = C.converged ? 1 : 0;
+    st->elapsed_ms = C.elapsed_ms;
+    st->kernel_launches = C.launches;
+  }
+  return TEXO_GP_OK;
+}
+}  // namespace
+
+extern "C" {
+
+uint32_t texo_gp_abi_version(void) { return TEXO_GP_ABI_VERSION; }
+
+void texo_gp_default_params(texo_gp_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->gamma_base = 8.0;
+  p->max_iterations = 3000;
+  p->beta = 2000.0;
+  p->initial_density_weight = 1.0e-4;
+  p->alpha_low = 1.05;
+  p->alpha_high = 1.06;
+  p->overflow_target_override = -1.0;
+  p->target_density = 1.0;
+  p->best_effort = 0;
+  p->dct_mode = TEXO_GP_DCT_FP32;
+  p->engine = TEXO_GP_ENGINE_HOST;
+  p->device = 0;
+  p->objective_margin_ulps = 64.0;
+}
+
+const char* texo_gp_status_name(int32_t s) {
+  switch (s) {
+    case TEXO_GP_OK: return "OK";
+    case TEXO_GP_ERR_EMPTY_GRID: return "EMPTY_GRID";
+    case TEXO_GP_ERR_GRID_TOO_LARGE: return "GRID_TOO_LARGE";
+    case TEXO_GP_ERR_DENSITY_LENGTH: return "DENSITY_LENGTH";
+    case TEXO_GP_ERR_NONFINITE_DENSITY: return "NONFINITE_DENSITY";
+    case TEXO_GP_ERR_EMPTY_UNIT: return "EMPTY_UNIT";
+    case TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE: return "NONFINITE_UNIT_COORDINATE";
+    case TEXO_GP_ERR_INVALID_MEMBER_CHARGE: return "INVALID_MEMBER_CHARGE";
+    case TEXO_GP_ERR_POINT_OUTSIDE_GRID: return "POINT_OUTSIDE_GRID";
+    case TEXO_GP_ERR_FIXED_CAPACITY_EXHAUSTED: return "FIXED_CAPACITY_EXHAUSTED";
+    case TEXO_GP_ERR_INSUFFICIENT_CAPACITY: return "INSUFFICIENT_CAPACITY";
+    case TEXO_GP_ERR_INSUFFICIENT_AREA: return "INSUFFICIENT_AREA";
+    case TEXO_GP_ERR_NONFINITE_FILLER: return "NONFINITE_FILLER";
+    case TEXO_GP_ERR_NEGATIVE_FILLER_CHARGE: return "NEGATIVE_FILLER_CHARGE";
+    case TEXO_GP_ERR_UNEXPECTED_FILLER_KIND: return "UNEXPECTED_FILLER_KIND";
+    case TEXO_GP_ERR_FILLER_CHARGE_MISMATCH: return "FILLER_CHARGE_MISMATCH";
+    case TEXO_GP_ERR_INVALID_BOUNDS: return "INVALID_BOUNDS";
+    case TEXO_GP_ERR_INVALID_METRIC_LENGTH: return "INVALID_METRIC_LENGTH";
+    case TEXO_GP_ERR_NONPOSITIVE_METRIC: return "NONPOSITIVE_METRIC";
+    case TEXO_GP_ERR_INVALID_INITIAL_COORDINATE: return "INVALID_INITIAL_COORDINATE";
+    case TEXO_GP_ERR_INVALID_MOMENTUM_PARAMETER: return "INVALID_MOMENTUM_PARAMETER";
+    case TEXO_GP_ERR_INVALID_LIPSCHITZ_ESTIMATE: return "INVALID_LIPSCHITZ_ESTIMATE";
+    case TEXO_GP_ERR_INVALID_OBJECTIVE: return "INVALID_OBJECTIVE";
+    case TEXO_GP_ERR_INVALID_GRADIENT_LENGTH: return "INVALID_GRADIENT_LENGTH";
+    case TEXO_GP_ERR_NONFINITE_GRADIENT: return "NONFINITE_GRADIENT";
+    case TEXO_GP_ERR_LINE_SEARCH_OVERFLOW: return "LINE_SEARCH_OVERFLOW";
+    case TEXO_GP_ERR_ITERATION_OVERFLOW: return "ITERATION_OVERFLOW";
+    case TEXO_GP_ERR_EVALUATION: return "EVALUATION";
+    case TEXO_GP_ERR_DENSITY_FIELD_CHANGED: return "DENSITY_FIELD_CHANGED";
+    case TEXO_GP_ERR_INVALID_NORMALIZATION: return "INVALID_NORMALIZATION";
+    case TEXO_GP_ERR_DID_NOT_CONVERGE: return "DID_NOT_CONVERGE";
+    case TEXO_GP_ERR_INVALID_ARGUMENT: return "INVALID_ARGUMENT";
+    case TEXO_GP_ERR_CUDA: return "CUDA";
+    case TEXO_GP_ERR_OUT_OF_MEMORY: return "OUT_OF_MEMORY";
+    case TEXO_GP_ERR_DEVICE_TIMEOUT: return "DEVICE_TIMEOUT";
+    case TEXO_GP_ERR_FIXED_POINT_RANGE: return "FIXED_POINT_RANGE";
+    case TEXO_GP_ERR_UNSUPPORTED: return "UNSUPPORTED";
+    case TEXO_GP_ERR_BUSY: return "BUSY";
+    default: return "UNKNOWN";
+  }
+}
+
+const char* texo_gp_last_error(void) { return g_last_error.c_str(); }
+
+int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo_gp_handle* out) {
+  if (!out) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  texo_gp_params defaults;
+  if (!prm) {
+    texo_gp_default_params(&defaults);
+    prm = &defaults;
+  }
+  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  auto h = std::make_unique<texo_gp_handle_s>();
+  h->inst = std::make_unique<Instance>();
+  h->inst->device = prm->device;
+  uint64_t err = 0;
+  int32_t s = build_model(p, prm, h->inst->m, &err);
+  if (s) return s;
+  s = h->inst->upload();
+  if (s) return s;
+  h->ctl = std::make_unique<Controller>(*h->inst);
+  *out = h.release();
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_destroy(texo_gp_handle h) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  delete h;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_sizes(texo_gp_handle h, uint64_t* units, uint64_t* fillers, uint64_t* coordinates,
+                      uint32_t* bins_x, uint32_t* bins_y, uint32_t* num_fields) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const HostModel& m = h->inst->m;
+  if (units) *units = m.U;
+  if (fillers) *fillers = m.F;
+  if (coordinates) *coordinates = m.coords();
+  if (bins_x) *bins_x = m.Wb;
+  if (bins_y) *bins_y = m.Hb;
+  if (num_fields) *num_fields = m.K;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_initial(texo_gp_handle h, double* c, double* lo, double* hi) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const HostModel& m = h->inst->m;
+  const size_t n = m.coords();
+  if (c) std::memcpy(c, m.init.data(), n * 8);
+  if (lo) std::memcpy(lo, m.lo.data(), n * 8);
+  if (hi) std::memcpy(hi, m.hi.data(), n * 8);
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_fillers(texo_gp_handle h, uint32_t* field, double* charge) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const HostModel& m = h->inst->m;
+  for (uint32_t j = 0; j < m.F; ++j) {
+    if (field) field[j] = (uint32_t)m.fil_field[j];
+    if (charge) charge[j] = m.fil_q[j];
+  }
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_evaluate(texo_gp_handle h, const double* coordinates, double gamma, texo_gp_eval* out,
+                         double* wa_gradient, double* field_gradient, double* density, double* potential) {
+  if (!h || !coordinates || !(gamma > 0.0) || !std::isfinite(gamma)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  Controller& C = *h->ctl;
+  const size_t nobj = (size_t)I.d.nobj, B = I.m.bins(), K = I.m.K;
+  for (size_t i = 0; i < 2 * nobj; ++i)
+    if (!std::isfinite(coordinates[i])) return TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE;
+  CU(cudaMemcpyAsync(I.bufY, coordinates, nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  EvalRec e;
+  TRY(C.evaluate(I.bufY, I.gY, gamma, false, e));
+  C.density_at_x = false;
+  if (out) {
+    out->wirelength = e.wa;
+    out->num_fields = (uint32_t)K;
+    for (size_t f = 0; f < K; ++f) {
+      out->fields[f].energy = e.energy[f];
+      out->fields[f].normalized_overflow = e.overflow[f];
+      out->fields[f].net_charge = e.net_charge[f];
+      out->fields[f].force_l1 = e.force[f];
+      out->fields[f].real_area = I.m.real_area[f];
+      out->fields[f].filler_charge =
+          I.m.td == 1.0 ? I.m.td * (double)I.m.available[f] - I.m.real_area[f]
+                        : std::max(I.m.td * (double)I.m.available[f] - I.m.real_area[f], 0.0);
+      out->fields[f].overflow_fixed = e.overflow_fixed[f];
+      out->fields[f].overflow_bins = (uint64_t)e.overflow_bins[f];
+    }
+  }
+  if (wa_gradient) {
+    std::vector<long long> fix(2 * (size_t)I.m.U);
+    CU(cudaMemcpyAsync(fix.data(), I.d.wa_fix, fix.size() * 8, cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaStreamSynchronize(I.stream));
+    for (size_t i = 0; i < fix.size(); ++i) wa_gradient[i] = (double)fix[i] * kInvFix;
+  }
+  if (field_gradient) {
+    std::vector<float2> g(K * nobj);
+    CU(cudaMemcpyAsync(g.data(), I.d.graw, g.size() * sizeof(float2), cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaStreamSynchronize(I.stream));
+    for (size_t f = 0; f < K; ++f)
+      for (size_t o = 0; o < nobj; ++o) {
+        bool valid = o < I.m.U || (size_t)I.m.fil_field[o - I.m.U] == f;
+        const float2 v = valid ? g[f * nobj + o] : make_float2(0.f, 0.f);
+        field_gradient[f * 2 * nobj + 2 * o] = v.x;
+        field_gradient[f * 2 * nobj + 2 * o + 1] = v.y;
+      }
+  }
+  if (density) {
+    std::vector<long long> a(K * B), b(K * B);
+    CU(cudaMemcpyAsync(a.data(), I.d.phys, a.size() * 8, cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaMemcpyAsync(b.data(), I.d.fill, b.size() * 8, cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaStreamSynchronize(I.stream));
+    for (size_t i = 0; i < K * B; ++i) density[i] = (double)(a[i] + b[i]) * kInvFix;
+  }
+  if (potential) {
+    std::vector<float> p(K * B);
+    CU(cudaMemcpyAsync(p.data(), I.d.phi, p.size() * 4, cudaMemcpyDeviceToHost, I.stream));
+    CU(cudaStreamSynchronize(I.stream));
+    for (size_t i = 0; i < K * B; ++i) potential[i] = p[i];
+  }
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_scatter(texo_gp_handle h, const double* coordinates, int64_t* physical, int64_t* fillers) {
+  if (!h || !coordinates) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  const size_t nobj = (size_t)I.d.nobj, n = (size_t)I.m.K * I.m.bins();
+  CU(cudaMemcpyAsync(I.bufY, coordinates, nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  launch_init(I.d, true, false, I.nvb, I.stream);
+  launch_scatter(I.d, I.r, I.bufY, I.nvb, I.stream);
+  if (physical) CU(cudaMemcpyAsync(physical, I.d.phys, n * 8, cudaMemcpyDeviceToHost, I.stream));
+  if (fillers) CU(cudaMemcpyAsync(fillers, I.d.fill, n * 8, cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  CU(cudaGetLastError());
+  h->ctl->density_at_x = false;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potential, double* energy) {
+  if (!h || !density) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  if (I.m.K == 0) return TEXO_GP_ERR_UNSUPPORTED;
+  const size_t B = I.m.bins();
+  double s = 0.0;
+  for (size_t i = 0; i < B; ++i) {
+    if (!std::isfinite(density[i])) return TEXO_GP_ERR_NONFINITE_DENSITY;
+    s += density[i];
+  }
+  const double mean = s / (double)B;
+  std::vector<float> rho(B);
+  for (size_t i = 0; i < B; ++i) rho[i] = (float)(density[i] - mean);
+  // Field 0's buffers carry the solve; K is forced to one for the call.
+  Dev D = I.d;
+  D.K = 1;
+  CU(cudaMemcpyAsync(D.rho, rho.data(), B * 4, cudaMemcpyHostToDevice, I.stream));
+  for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream);
+  launch_finalize(D, I.r, I.nvb, FIN_ENERGY, I.stream);
+  std::vector<float> phi(B);
+  CU(cudaMemcpyAsync(phi.data(), D.phi, B * 4, cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaMemcpyAsync(I.h_scal, I.r.scal, kScalars * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  CU(cudaGetLastError());
+  if (potential)
+    for (size_t i = 0; i < B; ++i) potential[i] = phi[i];
+  if (energy) *energy = I.h_scal[SC_ENERGY];
+  h->ctl->density_at_x = false;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_targets, double* out_coords,
+                    texo_gp_stats* stats) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Controller& C = *h->ctl;
+  Instance& I = *h->inst;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  const unsigned long long l0 = launches_issued();
+  CU(cudaEventRecord(e0, I.stream));
+  int32_t s = C.run(max_iterations);
+  cudaEventRecord(e1, I.stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  C.elapsed_ms = ms;
+  C.launches = launches_issued() - l0;
+  if (s != TEXO_GP_OK && s != TEXO_GP_ERR_DID_NOT_CONVERGE) {
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->status = s;
+      stats->iterations = C.completed;
+    }
+    return s;
+  }
+  int32_t t = handle_targets(h, out_targets, out_coords, stats, s);
+  return t ? t : s;
+}
+
+int32_t texo_gp_reset(texo_gp_handle h) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  h->ctl = std::make_unique<Controller>(I);
+  CU(cudaMemcpyAsync(I.bufX, I.m.init.data(), (size_t)I.d.nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  CU(cudaMemsetAsync(I.prev_targets, 0, 2 * (size_t)I.m.U * 4, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_hpwl(texo_gp_handle h, const double* coordinates, double* hpwl) {
+  if (!h || !coordinates || !hpwl) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  CU(cudaMemcpyAsync(I.bufY, coordinates, (size_t)I.d.nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  launch_hpwl(I.d, I.r, I.bufY, I.nvb, I.stream);
+  launch_finalize(I.d, I.r, I.nvb, FIN_HPWL, I.stream);
+  CU(cudaMemcpyAsync(I.h_scal + SC_HPWL, I.r.scal + SC_HPWL, sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  *hpwl = I.h_scal[SC_HPWL];
+  return TEXO_GP_OK;
+}
+
+static const char* kStageNames[] = {"init", "scatter", "wa", "prep", "dct_row_fwd", "dct_col_fwd",
+                                     "dct_col_inv", "dct_row_inv", "gather", "combine", "finalize",
+                                     "extrapolate", "candidate", "kkt", "precond"};
+constexpr uint32_t kNumStages = sizeof(kStageNames) / sizeof(kStageNames[0]);
+
+const char* texo_gp_stage_name(uint32_t i) { return i < kNumStages ? kStageNames[i] : nullptr; }
+
+int32_t texo_gp_stage_times(texo_gp_handle h, uint32_t reps, double* ms, uint32_t capacity, uint32_t* count) {
+  if (!h || !ms || reps == 0) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  const Dev& D = I.d;
+  cudaStream_t s = I.stream;
+  const int nvb = I.nvb;
+  if (count) *count = kNumStages;
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  const double gam = I.m.gamma_base_tiles();
+  // one evaluation first so that every input of every stage is populated
+  h->ctl->enqueue_eval(I.bufX, I.gX, gam, false);
+  launch_precond(D, I.r, nvb, s);
+  for (uint32_t st = 0; st < kNumStages && st < capacity; ++st) {
+    CU(cudaStreamSynchronize(s));
+    CU(cudaEventRecord(a, s));
+    for (uint32_t k = 0; k < reps; ++k) {
+      switch (st) {
+        case 0: launch_init(D, true, true, nvb, s); break;
+        case 1: launch_scatter(D, I.r, I.bufX, nvb, s); break;
+        case 2: launch_wa(D, I.r, I.bufX, gam, nvb, s); break;
+        case 3: launch_prep(D, I.r, nvb, s); break;
+        case 4: case 5: case 6: case 7: launch_dct(D, I.r, (int)st - 4, nvb, s); break;
+        case 8: launch_gather(D, I.r, I.bufX, nvb, s); break;
+        case 9: launch_combine(D, I.r, I.gX, nvb, s); break;
+        case 10: launch_finalize(D, I.r, nvb, FIN_ENERGY | FIN_COMBINE, s); break;
+        case 11: launch_extrapolate(D, I.r, I.bufX, I.bufXp, 0.5, I.bufY, nvb, s); break;
+        case 12: launch_candidate(D, I.r, I.bufX, I.gX, 1.0, I.bufC, nvb, s); break;
+        case 13: launch_kkt(D, I.r, I.bufX, I.gX, I.bufXp, nvb, s); break;
+        default: launch_precond(D, I.r, nvb, s); break;
+      }
+    }
+    CU(cudaEventRecord(b, s));
+    CU(cudaEventSynchronize(b));
+    float t = 0.f;
+    CU(cudaEventElapsedTime(&t, a, b));
+    ms[st] = (double)t / reps;
+    // restore the accumulation grids that repeated launches disturbed
+    if (st == 1 || st == 2) h->ctl->enqueue_eval(I.bufX, I.gX, gam, false);
+  }
+  CU(cudaStreamSynchronize(s));
+  CU(cudaGetLastError());
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  h->ctl->density_at_x = false;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_place(const texo_gp_problem* p, const texo_gp_params* prm, uint32_t* out_targets, double* out_coords,
+                      texo_gp_stats* stats) {
+  texo_gp_handle h = nullptr;
+  int32_t s = texo_gp_create(p, prm, &h);
+  if (s) {
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->status = s;
+    }
+    return s;
+  }
+  s = texo_gp_run(h, 0, out_targets, out_coords, stats);
+  texo_gp_destroy(h);
+  return s;
+}
+
+}  // extern "C"

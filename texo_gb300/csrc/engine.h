@@ -1,0 +1,89 @@
+// engine.h — host-side model of one placement instance and its device state.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/texo_gp.h"
+#include "kernels.cuh"
+
+namespace tgp {
+
+void set_last_error(const std::string& s);
+
+// Host preprocessing of a texo_gp_problem into the device layout. Mirrors
+// `eplace::place` setup (eplace.rs:254-346), `DensityModel::new` and
+// `initial_fillers` (electrostatic_placement.rs:139-240) and the hypergraph
+// preconditioners (analytical_placement.rs:177-231).
+struct HostModel {
+  texo_gp_params params{};
+  uint32_t W = 0, H = 0, Wb = 0, Hb = 0;
+  double sx = 1, sy = 1;
+  bool identity = true;
+  double td = 1.0;
+  uint32_t K = 0;
+  std::vector<texo_gp_field> kinds;
+  std::vector<std::vector<uint32_t>> cap;        // [K][W*H] after fixed occupancy
+  std::vector<uint64_t> available;               // [K]
+  std::vector<std::vector<double>> smoothed;     // [K][B] td-scaled smoothed capacity
+  std::vector<uint64_t> real_count;              // [K]
+  std::vector<double> real_area;                 // [K]
+  uint32_t U = 0, F = 0, Mm = 0;
+  // members (flattened, density units only)
+  std::vector<int> mem_unit, mem_field;
+  std::vector<double> mem_off;                   // [2Mm]
+  std::vector<float> mem_q;
+  std::vector<int> unit_mem_ptr;                 // [U+1]
+  // fillers
+  std::vector<int> fil_field;
+  std::vector<double> fil_q;
+  // optimizer vector
+  std::vector<double> init, lo, hi;              // [2(U+F)]
+  std::vector<double> pre_static;                // [U+F]
+  std::vector<double> pre_q;                     // [K][U+F]
+  std::vector<double> gamma_weight;              // [K]
+  // WA
+  std::vector<int> net_ptr, pin_unit;
+  std::vector<double> pin_base;                  // [2P]
+  std::vector<float> net_w;
+  int n_classes = 0;
+  int class_begin[kMaxClasses + 1] = {0};
+  int class_group[kMaxClasses] = {0};
+  int n_hpwl_nets = 0;
+  bool has_density = false;
+
+  uint64_t coords() const { return 2ull * (U + F); }
+  uint64_t bins() const { return (uint64_t)Wb * Hb; }
+  double overflow_target(uint32_t f) const;
+  double gamma_base_tiles() const;
+};
+
+int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostModel& m, uint64_t* err_index);
+
+// Device-resident instance: every buffer one placement needs.
+struct Instance {
+  HostModel m;
+  int device = 0;
+  int sms = 152;
+  int nvb = 1;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocations;
+  Dev d{};
+  Reduce r{};
+  double2 *bufX = nullptr, *bufXp = nullptr, *bufY = nullptr, *bufC = nullptr;
+  double2 *gX = nullptr, *gY = nullptr, *gC = nullptr;
+  double2* best = nullptr;                       // best checkpoint coordinates [U]
+  uint32_t* prev_targets = nullptr;              // [2U]
+  unsigned long long* mismatch = nullptr;
+  double* h_scal = nullptr;                      // pinned host mirror
+  long long* h_iscal = nullptr;
+  uint64_t bytes = 0;
+
+  ~Instance();
+  int32_t alloc(void** p, size_t bytes);
+  int32_t upload();
+};
+
+}  // namespace tgp
+
+struct texo_gp_handle_s;

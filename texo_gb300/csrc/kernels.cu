@@ -1,0 +1,236 @@
+// kernels.cu — standalone kernels (one stage each) and their launchers.
+#include "kernels.cuh"
+
+namespace tgp {
+
+__global__ void __launch_bounds__(kThreads) k_init(Dev d, bool grids, bool wa) {
+  stage_init(d, blockIdx.x, gridDim.x, grids, wa);
+}
+__global__ void __launch_bounds__(kThreads) k_scatter(Dev d, Partials p, const double2* pos) {
+  __shared__ Shared sh;
+  stage_scatter(d, pos, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_wa(Dev d, Partials p, const double2* pos, double gamma) {
+  __shared__ Shared sh;
+  stage_wa(d, pos, gamma, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_prep(Dev d, Partials p) {
+  __shared__ Shared sh;
+  stage_prep(d, p, gridDim.x, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_dct(Dev d, Partials p, int step, bool large) {
+  __shared__ GemmShared sm;
+  __shared__ Shared sh;
+  stage_dct(d, step, large, p, blockIdx.x, gridDim.x, sm, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_gather(Dev d, Partials p, const double2* pos) {
+  __shared__ Shared sh;
+  stage_gather(d, pos, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_combine(Dev d, Partials p, const double* coef, double2* gout) {
+  __shared__ Shared sh;
+  stage_combine(d, coef, gout, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_extrapolate(Dev d, Partials p, const double2* x, const double2* xp,
+                                                         double e, double2* y) {
+  __shared__ Shared sh;
+  stage_extrapolate(d, x, xp, e, y, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_candidate(Dev d, Partials p, const double2* y, const double2* gy,
+                                                       double L, double2* c) {
+  __shared__ Shared sh;
+  stage_candidate(d, y, gy, L, c, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_kkt(Dev d, Partials p, const double2* x, const double2* g,
+                                                 const double2* ref) {
+  __shared__ Shared sh;
+  stage_kkt(d, x, g, ref, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_precond(Dev d, Partials p, const double* lambda) {
+  __shared__ Shared sh;
+  stage_precond(d, lambda, p, blockIdx.x, gridDim.x, sh);
+}
+__global__ void __launch_bounds__(kThreads) k_hpwl(Dev d, Partials p, const double2* pos) {
+  __shared__ Shared sh;
+  stage_hpwl(d, pos, p, blockIdx.x, gridDim.x, sh);
+}
+
+// Reduces the partials selected by `mask` in a fixed order and derives the
+// objective scalars (combined_objective / augmented_density_value_and_coefficient,
+// eplace.rs:1022-1044, 1111-1124).
+__global__ void __launch_bounds__(kThreads) k_finalize(Dev d, Reduce r, int nvb, int mask) {
+  __shared__ double shd[kThreads / 32];
+  __shared__ long long shl[kThreads / 32];
+  const Partials& p = r.p;
+  double* sc = r.scal;
+  long long* si = r.iscal;
+  if (mask & (FIN_ENERGY | FIN_WA)) {
+    const double wa = block_reduce_array(pslot(p, SLOT_WA_VALUE), nvb, 0.0, OpAdd(), shd);
+    if (threadIdx.x == 0) sc[SC_WA] = wa;
+  }
+  if (mask & FIN_ENERGY) {
+    for (int f = 0; f < d.K; ++f) {
+      const double e = block_reduce_array(pslot(p, SLOT_ENERGY + f), nvb, 0.0, OpAdd(), shd);
+      const long long ov = block_reduce_array(islot(p, IS_OVERFLOW + f), nvb, 0ll, OpAdd(), shl);
+      const long long bins = block_reduce_array(islot(p, IS_OVER_BINS + f), nvb, 0ll, OpAdd(), shl);
+      const long long gs = block_reduce_array(islot(p, IS_GRID_SUM + f), nvb, 0ll, OpAdd(), shl);
+      if (threadIdx.x == 0) {
+        sc[SC_ENERGY + f] = 0.5 * e;
+        si[SI_OVERFLOW_FIXED + f] = ov;
+        si[SI_OVER_BINS + f] = bins;
+        si[SI_GRID_SUM + f] = gs;
+        sc[SC_OVERFLOW + f] = ((double)ov * kInvFix) / sc[SC_REAL_AREA + f];
+        sc[SC_MEAN + f] = (double)(gs - d.capsum[f]) * kInvFix;
+      }
+    }
+  }
+  if (mask & (FIN_ENERGY | FIN_WA)) {
+    if (threadIdx.x == 0) {
+      double value = sc[SC_WA];
+      const double beta = sc[SC_BETA];
+      for (int f = 0; f < d.K; ++f) {
+        const double e0 = sc[SC_E0 + f], lam = sc[SC_LAMBDA + f];
+        const double ne = sc[SC_ENERGY + f] / e0;
+        value += lam * e0 * (ne + 0.5 * beta * ne * ne);
+        sc[SC_COEF + f] = lam * (1.0 + beta * ne);
+      }
+      sc[SC_VALUE] = value;
+    }
+    __syncthreads();
+  }
+  if (mask & FIN_COMBINE) {
+    for (int f = 0; f < d.K; ++f) {
+      const double a = block_reduce_array(pslot(p, SLOT_RAWL1 + f), nvb, 0.0, OpAdd(), shd);
+      const double b = block_reduce_array(pslot(p, SLOT_FORCE + f), nvb, 0.0, OpAdd(), shd);
+      if (threadIdx.x == 0) {
+        sc[SC_RAWL1 + f] = a;
+        sc[SC_FORCE + f] = b;
+      }
+    }
+    const double w = block_reduce_array(pslot(p, SLOT_WAL1), nvb, 0.0, OpAdd(), shd);
+    const long long bad = block_reduce_array(islot(p, IS_BAD), nvb, 0x7fffffffffffffffll, OpMin(), shl);
+    if (threadIdx.x == 0) {
+      sc[SC_WAL1] = w;
+      si[SI_BAD] = bad;
+    }
+  }
+  if (mask & (FIN_CAND | FIN_DIFF)) {
+    const long long diff = block_reduce_array(islot(p, IS_DIFF), nvb, 0ll, OpAdd(), shl);
+    if (threadIdx.x == 0) si[SI_DIFF] = diff;
+  }
+  if (mask & FIN_CAND) {
+    const double a = block_reduce_array(pslot(p, SLOT_DOT), nvb, 0.0, OpAdd(), shd);
+    const double b = block_reduce_array(pslot(p, SLOT_MSN), nvb, 0.0, OpAdd(), shd);
+    if (threadIdx.x == 0) {
+      sc[SC_DOT] = a;
+      sc[SC_MSN] = b;
+    }
+  }
+  if (mask & FIN_KKT) {
+    const double a = block_reduce_array(mslot(p, MS_KKT), nvb, 0.0, OpMax(), shd);
+    const double b = block_reduce_array(mslot(p, MS_CHANGE), nvb, 0.0, OpMax(), shd);
+    if (threadIdx.x == 0) {
+      sc[SC_KKT] = a;
+      sc[SC_CHANGE] = b;
+    }
+  }
+  if (mask & FIN_PRECOND) {
+    const double a = block_reduce_array(mslot(p, MS_PMIN), nvb, (double)INFINITY, OpMin(), shd);
+    const double b = block_reduce_array(mslot(p, MS_PMAX), nvb, 0.0, OpMax(), shd);
+    const long long c = block_reduce_array(islot(p, IS_PBAD), nvb, 0ll, OpAdd(), shl);
+    if (threadIdx.x == 0) {
+      sc[SC_PMIN] = a;
+      sc[SC_PMAX] = b;
+      si[SI_PBAD] = c;
+    }
+  }
+  if (mask & FIN_HPWL) {
+    const double a = block_reduce_array(pslot(p, SLOT_HPWL), nvb, 0.0, OpAdd(), shd);
+    if (threadIdx.x == 0) sc[SC_HPWL] = a;
+  }
+}
+
+// rounded_targets_from_coordinates (eplace.rs:954-971) compared with the
+// previous stationary targets (stationary_target_is_fixed, :973-985).
+__global__ void k_round_compare(Dev d, const double2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < d.U; u += gridDim.x * blockDim.x) {
+    const double2 a = x[u];
+    const double rx = fmin(fmax(round(a.x), 0.0), (double)(W - 1));
+    const double ry = fmin(fmax(round(a.y), 0.0), (double)(H - 1));
+    const uint32_t tx = (uint32_t)rx, ty = (uint32_t)ry;
+    if (prev[2 * u] != tx || prev[2 * u + 1] != ty) atomicAdd(mismatch, 1ull);
+    prev[2 * u] = tx;
+    prev[2 * u + 1] = ty;
+  }
+}
+
+static thread_local unsigned long long t_launches = 0;
+unsigned long long launches_issued() { return t_launches; }
+#define COUNT ++t_launches
+
+static inline bool use_large_tiles(const Dev& d) {
+  return (long long)((d.g.Wb + 31) / 32) * ((d.g.Hb + 31) / 32) >= 1024;
+}
+
+void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s) {
+  COUNT;
+  k_init<<<nvb, kThreads, 0, s>>>(d, grids, wa);
+}
+void launch_scatter(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+  COUNT;
+  k_scatter<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
+}
+void launch_wa(const Dev& d, const Reduce& r, const double2* pos, double gamma, int nvb, cudaStream_t s) {
+  COUNT;
+  k_wa<<<nvb, kThreads, 0, s>>>(d, r.p, pos, gamma);
+}
+void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
+  COUNT;
+  k_prep<<<nvb, kThreads, 0, s>>>(d, r.p);
+}
+void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s) {
+  COUNT;
+  k_dct<<<nvb, kThreads, 0, s>>>(d, r.p, step, use_large_tiles(d));
+}
+void launch_gather(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+  COUNT;
+  k_gather<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
+}
+void launch_combine(const Dev& d, const Reduce& r, double2* gout, int nvb, cudaStream_t s) {
+  COUNT;
+  k_combine<<<nvb, kThreads, 0, s>>>(d, r.p, r.scal + SC_COEF, gout);
+}
+void launch_extrapolate(const Dev& d, const Reduce& r, const double2* x, const double2* xp, double e, double2* y,
+                        int nvb, cudaStream_t s) {
+  COUNT;
+  k_extrapolate<<<nvb, kThreads, 0, s>>>(d, r.p, x, xp, e, y);
+}
+void launch_candidate(const Dev& d, const Reduce& r, const double2* y, const double2* gy, double L, double2* c,
+                      int nvb, cudaStream_t s) {
+  COUNT;
+  k_candidate<<<nvb, kThreads, 0, s>>>(d, r.p, y, gy, L, c);
+}
+void launch_kkt(const Dev& d, const Reduce& r, const double2* x, const double2* g, const double2* ref, int nvb,
+                cudaStream_t s) {
+  COUNT;
+  k_kkt<<<nvb, kThreads, 0, s>>>(d, r.p, x, g, ref);
+}
+void launch_precond(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
+  COUNT;
+  k_precond<<<nvb, kThreads, 0, s>>>(d, r.p, r.scal + SC_LAMBDA);
+}
+void launch_hpwl(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+  COUNT;
+  k_hpwl<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
+}
+void launch_finalize(const Dev& d, const Reduce& r, int nvb, int mask, cudaStream_t s) {
+  COUNT;
+  k_finalize<<<1, kThreads, 0, s>>>(d, r, nvb, mask);
+}
+void launch_round_compare(const Dev& d, const double2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch,
+                          int nvb, cudaStream_t s) {
+  COUNT;
+  k_round_compare<<<nvb, kThreads, 0, s>>>(d, x, prev, W, H, mismatch);
+}
+
+}  // namespace tgp

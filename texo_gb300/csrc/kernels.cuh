@@ -1,0 +1,81 @@
+// kernels.cuh — standalone-kernel launchers over the stage functions, and the
+// scalar block the finalize kernels write (read back by the host controller).
+#pragma once
+#include "stages.cuh"
+
+namespace tgp {
+
+// Scalar block layout (doubles): outputs of finalize, inputs set by the host.
+enum Scalar {
+  SC_WA = 0,
+  SC_ENERGY = 1,                 // + field
+  SC_OVERFLOW = 5,               // + field, normalized
+  SC_FORCE = 9,                  // + field
+  SC_RAWL1 = 13,                 // + field
+  SC_WAL1 = 17,
+  SC_COEF = 18,                  // + field
+  SC_VALUE = 22,
+  SC_DOT = 23,
+  SC_MSN = 24,
+  SC_KKT = 25,
+  SC_CHANGE = 26,
+  SC_PMIN = 27,
+  SC_PMAX = 28,
+  SC_HPWL = 29,
+  SC_MEAN = 30,                  // + field
+  // inputs
+  SC_LAMBDA = 40,                // + field
+  SC_E0 = 44,                    // + field
+  SC_BETA = 48,
+  SC_REAL_AREA = 49,             // + field
+  kScalars = 64
+};
+enum IScalar {
+  SI_OVERFLOW_FIXED = 0,         // + field
+  SI_OVER_BINS = 4,              // + field
+  SI_DIFF = 8,
+  SI_BAD = 9,
+  SI_PBAD = 10,
+  SI_GRID_SUM = 11,              // + field
+  kIScalars = 16
+};
+
+enum FinalizeMask {
+  FIN_ENERGY = 1,     // WA value, energies, overflow, coefficients, objective value
+  FIN_COMBINE = 2,    // raw L1, WA L1, force L1, bad index
+  FIN_CAND = 4,       // diff count, dot, msn
+  FIN_KKT = 8,        // kkt residual, change
+  FIN_PRECOND = 16,   // pmin, pmax, pbad
+  FIN_DIFF = 32,      // diff count only
+  FIN_HPWL = 64,
+  FIN_WA = 128        // WA value + objective value without density refresh
+};
+
+// One instance's partial buffers and scalar block (device pointers).
+struct Reduce {
+  Partials p;
+  double* scal;          // [kScalars]
+  long long* iscal;      // [kIScalars]
+};
+
+unsigned long long launches_issued();
+void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s);
+void launch_scatter(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
+void launch_wa(const Dev& d, const Reduce& r, const double2* pos, double gamma, int nvb, cudaStream_t s);
+void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
+void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s);
+void launch_gather(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
+void launch_combine(const Dev& d, const Reduce& r, double2* gout, int nvb, cudaStream_t s);
+void launch_extrapolate(const Dev& d, const Reduce& r, const double2* x, const double2* xp, double e, double2* y,
+                        int nvb, cudaStream_t s);
+void launch_candidate(const Dev& d, const Reduce& r, const double2* y, const double2* gy, double L, double2* c,
+                      int nvb, cudaStream_t s);
+void launch_kkt(const Dev& d, const Reduce& r, const double2* x, const double2* g, const double2* ref, int nvb,
+                cudaStream_t s);
+void launch_precond(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
+void launch_hpwl(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
+void launch_finalize(const Dev& d, const Reduce& r, int nvb, int mask, cudaStream_t s);
+void launch_round_compare(const Dev& d, const double2* x, uint32_t* prev_targets, int W, int H,
+                          unsigned long long* mismatch, int nvb, cudaStream_t s);
+
+}  // namespace tgp

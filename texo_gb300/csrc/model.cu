@@ -1,0 +1,356 @@
+// model.cpp — host preprocessing of a texo_gp_problem into the device layout.
+//
+// The setup mirrors the reference: capacity per kind minus fixed occupancy and
+// its B-spline smoothing (DensityModel::new, electrostatic_placement.rs:139-196),
+// capacity-proportional fillers (initial_fillers, :198-240), coordinates and
+// bounds (initial_coordinates_and_bounds, eplace.rs:1441-1468), the wirelength
+// preconditioner and cell incidence (analytical_placement.rs:177-231) and the
+// per-kind gamma weights (density_gamma_weights, eplace.rs:1424-1439).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "engine.h"
+
+namespace tgp {
+
+namespace {
+constexpr double kPi = 3.14159265358979323846;
+
+inline double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// quadratic_bspline_axis / deposit_quadratic_bspline in FP64
+// (electrostatic_placement.rs:900-916, 950-976), used for the capacity background.
+void deposit64(std::vector<double>& g, uint32_t W, uint32_t H, double x, double y, double q) {
+  auto axis = [](uint32_t n, double c, size_t idx[3], double w[3]) {
+    const double maximum = (double)(n - 1);
+    c = clampd(c, 0.0, maximum);
+    const double cc = std::fmin(std::floor(c + 0.5), maximum);
+    const size_t center = (size_t)cc;
+    const double o = c - cc, a = 0.5 - o, b = 0.5 + o;
+    idx[0] = center == 0 ? 0 : center - 1;
+    idx[1] = center;
+    idx[2] = std::min<size_t>(center + 1, n - 1);
+    w[0] = 0.5 * (a * a);
+    w[1] = 0.75 - o * o;
+    w[2] = 0.5 * (b * b);
+  };
+  size_t ix[3], iy[3];
+  double wx[3], wy[3];
+  axis(W, x, ix, wx);
+  axis(H, y, iy, wy);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) g[iy[r] * W + ix[c]] += q * wx[c] * wy[r];
+}
+
+double u64_to_f64(uint64_t v) {
+  return (double)(uint32_t)(v >> 32) * 4294967296.0 + (double)(uint32_t)(v & 0xffffffffu);
+}
+}  // namespace
+
+double HostModel::overflow_target(uint32_t f) const {
+  if (params.overflow_target_override >= 0.0) return params.overflow_target_override;
+  switch (kinds[f].kind) {
+    case TEXO_GP_KIND_MEMORY:
+    case TEXO_GP_KIND_DSP:
+      return 0.20;
+    case TEXO_GP_KIND_LUT:
+    case TEXO_GP_KIND_REGISTER:
+      return 0.10;
+    default:
+      return 0.0;
+  }
+}
+
+double HostModel::gamma_base_tiles() const {
+  return params.gamma_base * (identity ? 1.0 : 1.0 / sx);
+}
+
+int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostModel& m, uint64_t* err) {
+  uint64_t dummy;
+  if (!err) err = &dummy;
+  *err = 0;
+  if (!p || !prm) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (p->width == 0 || p->height == 0) return TEXO_GP_ERR_EMPTY_GRID;
+  m.params = *prm;
+  m.W = p->width;
+  m.H = p->height;
+  m.Wb = prm->bins_x ? prm->bins_x : p->width;
+  m.Hb = prm->bins_y ? prm->bins_y : p->height;
+  if ((uint64_t)m.Wb * m.Hb > (1ull << 26) || (uint64_t)m.W * m.H > (1ull << 30)) return TEXO_GP_ERR_GRID_TOO_LARGE;
+  m.identity = (m.Wb == m.W && m.Hb == m.H);
+  m.sx = (double)m.Wb / (double)m.W;
+  m.sy = (double)m.Hb / (double)m.H;
+  m.td = prm->target_density;
+  if (!(m.td > 0.0 && m.td <= 1.0)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const uint32_t U = p->num_units;
+  if (U == 0 || !p->member_ptr || !p->initial_xy || !p->lower_xy || !p->upper_xy) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (p->num_fields && (!p->fields || !p->capacity)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const uint32_t M = p->member_ptr[U];
+  for (uint32_t u = 0; u < U; ++u)
+    if (p->member_ptr[u + 1] < p->member_ptr[u]) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  const size_t tiles = (size_t)m.W * m.H;
+  std::vector<uint64_t> member_count(p->num_fields, 0);
+  for (uint32_t i = 0; i < M; ++i) {
+    if (p->member_field[i] >= p->num_fields) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    member_count[p->member_field[i]]++;
+  }
+  // capacity minus fixed occupancy (electrostatic_placement.rs:146-172)
+  std::vector<std::vector<uint32_t>> caps(p->num_fields);
+  for (uint32_t f = 0; f < p->num_fields; ++f)
+    caps[f].assign(p->capacity + (size_t)f * tiles, p->capacity + (size_t)(f + 1) * tiles);
+  for (uint32_t i = 0; i < p->num_fixed_occupancy; ++i) {
+    const uint32_t f = p->fixed_occupancy[3 * (size_t)i], x = p->fixed_occupancy[3 * (size_t)i + 1],
+                   y = p->fixed_occupancy[3 * (size_t)i + 2];
+    if (x >= m.W || y >= m.H) {
+      *err = i;
+      return TEXO_GP_ERR_POINT_OUTSIDE_GRID;
+    }
+    if (f >= p->num_fields || caps[f][(size_t)y * m.W + x] == 0) {
+      *err = i;
+      return TEXO_GP_ERR_FIXED_CAPACITY_EXHAUSTED;
+    }
+    caps[f][(size_t)y * m.W + x] -= 1;
+  }
+  std::vector<int> active(p->num_fields, -1);
+  for (uint32_t f = 0; f < p->num_fields; ++f) {
+    if (member_count[f] == 0) continue;
+    active[f] = (int)m.K++;
+    m.kinds.push_back(p->fields[f]);
+    m.cap.push_back(caps[f]);
+  }
+  if (m.K > (uint32_t)kMaxFields) return TEXO_GP_ERR_UNSUPPORTED;
+  m.available.assign(m.K, 0);
+  m.smoothed.assign(m.K, std::vector<double>());
+  for (uint32_t f = 0; f < m.K; ++f) {
+    for (auto c : m.cap[f]) m.available[f] += c;
+    m.smoothed[f].assign((size_t)m.Wb * m.Hb, 0.0);
+    for (size_t i = 0; i < tiles; ++i) {
+      const uint32_t c = m.cap[f][i];
+      if (!c) continue;
+      double bx = (double)(uint32_t)(i % m.W), by = (double)(uint32_t)(i / m.W);
+      if (!m.identity) {
+        bx = (bx + 0.5) * m.sx - 0.5;
+        by = (by + 0.5) * m.sy - 0.5;
+      }
+      deposit64(m.smoothed[f], m.Wb, m.Hb, bx, by, m.td * (double)c);
+    }
+  }
+  // density units and members (eplace.rs:261-301)
+  m.U = U;
+  m.unit_mem_ptr.assign(U + 1, 0);
+  m.real_count.assign(m.K, 0);
+  m.real_area.assign(m.K, 0.0);
+  uint32_t dunit = 0;
+  for (uint32_t u = 0; u < U; ++u) {
+    const uint32_t b = p->member_ptr[u], e = p->member_ptr[u + 1];
+    for (uint32_t i = b; i < e; ++i) {
+      const double dx = p->member_offset_xy[2 * (size_t)i], dy = p->member_offset_xy[2 * (size_t)i + 1];
+      const double q = p->member_charge[i];
+      if (!std::isfinite(dx) || !std::isfinite(dy)) {
+        *err = dunit;
+        return TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE;
+      }
+      if (!std::isfinite(q) || q <= 0.0) {
+        *err = dunit;
+        return TEXO_GP_ERR_INVALID_MEMBER_CHARGE;
+      }
+      const int f = active[p->member_field[i]];
+      m.mem_unit.push_back((int)u);
+      m.mem_field.push_back(f);
+      m.mem_off.push_back(dx);
+      m.mem_off.push_back(dy);
+      m.mem_q.push_back((float)q);
+      m.real_count[f] += 1;
+      m.real_area[f] += q;
+    }
+    if (e > b) ++dunit;
+    m.unit_mem_ptr[u + 1] = (int)m.mem_unit.size();
+  }
+  m.Mm = (uint32_t)m.mem_unit.size();
+  m.has_density = m.Mm > 0;
+  // fillers (electrostatic_placement.rs:198-240)
+  std::vector<double> fx, fy;
+  for (uint32_t f = 0; f < m.K; ++f) {
+    if (m.real_count[f] > m.available[f]) {
+      *err = f;
+      return TEXO_GP_ERR_INSUFFICIENT_CAPACITY;
+    }
+    const double avail = m.td * (double)(uint32_t)m.available[f];
+    const double ra = m.real_area[f];
+    if (!std::isfinite(ra) || ra < 0.0 || (m.td == 1.0 && ra > avail + 1.0e-9)) {
+      *err = f;
+      return TEXO_GP_ERR_INSUFFICIENT_AREA;
+    }
+    double total = avail - ra;
+    if (m.td != 1.0) total = std::max(total, 0.0);
+    if (total == 0.0) continue;
+    const double denominator = (double)(uint32_t)m.available[f];
+    std::vector<size_t> occ;
+    for (size_t i = 0; i < tiles; ++i)
+      if (m.cap[f][i]) occ.push_back(i);
+    double assigned = 0.0;
+    for (size_t o = 0; o < occ.size(); ++o) {
+      const size_t i = occ[o];
+      const double q = o + 1 == occ.size() ? total - assigned : total * (double)m.cap[f][i] / denominator;
+      assigned += q;
+      m.fil_field.push_back((int)f);
+      m.fil_q.push_back(q);
+      fx.push_back((double)(uint32_t)(i % m.W));
+      fy.push_back((double)(uint32_t)(i / m.W));
+    }
+  }
+  m.F = (uint32_t)m.fil_field.size();
+  const size_t nobj = (size_t)m.U + m.F;
+  if (nobj >= (1ull << 30)) return TEXO_GP_ERR_GRID_TOO_LARGE;
+  // fixed-point range: every bin's charge stays far inside int64 at 2^32
+  for (uint32_t f = 0; f < m.K; ++f) {
+    double tot = m.real_area[f] + m.td * (double)m.available[f];
+    if (tot * 16.0 > 2147483648.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
+  }
+  // coordinates and bounds (eplace.rs:1441-1468, 316-318)
+  m.init.resize(2 * nobj);
+  m.lo.resize(2 * nobj);
+  m.hi.resize(2 * nobj);
+  for (uint32_t u = 0; u < U; ++u)
+    for (int a = 0; a < 2; ++a) {
+      const size_t i = 2 * (size_t)u + a;
+      m.init[i] = p->initial_xy[i];
+      m.lo[i] = p->lower_xy[i];
+      m.hi[i] = p->upper_xy[i];
+      if (!std::isfinite(m.lo[i]) || !std::isfinite(m.hi[i]) || m.lo[i] > m.hi[i]) return TEXO_GP_ERR_INVALID_BOUNDS;
+      if (!std::isfinite(m.init[i])) {
+        *err = i;
+        return (p->member_ptr[u + 1] > p->member_ptr[u]) ? TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE
+                                                           : TEXO_GP_ERR_INVALID_INITIAL_COORDINATE;
+      }
+    }
+  for (uint32_t j = 0; j < m.F; ++j) {
+    const size_t i = 2 * ((size_t)U + j);
+    m.init[i] = fx[j];
+    m.init[i + 1] = fy[j];
+    m.lo[i] = 0.0;
+    m.lo[i + 1] = 0.0;
+    m.hi[i] = (double)(m.W - 1);
+    m.hi[i + 1] = (double)(m.H - 1);
+  }
+  for (size_t i = 0; i < 2 * nobj; ++i) m.init[i] = clampd(m.init[i], m.lo[i], m.hi[i]);
+  // hypergraph: pins and nets (AnalyticalHypergraph::new, analytical_placement.rs:116-168)
+  const uint32_t C = p->num_cells, E = p->num_nets;
+  if (E && (!p->net_ptr || !p->pin_cell)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  for (uint32_t c = 0; c < C; ++c)
+    if (p->cell_unit[c] >= U) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  for (uint32_t i = 0; i < M; ++i)
+    if (p->member_cell && p->member_cell[i] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  auto pin_of = [&](uint32_t cell, int& unit, double& bx, double& by) {
+    if (p->cell_fixed[cell]) {
+      unit = -1;
+      bx = p->cell_fixed_xy[2 * (size_t)cell];
+      by = p->cell_fixed_xy[2 * (size_t)cell + 1];
+    } else {
+      unit = (int)p->cell_unit[cell];
+      bx = p->cell_offset_xy[2 * (size_t)cell];
+      by = p->cell_offset_xy[2 * (size_t)cell + 1];
+    }
+  };
+  // wirelength preconditioner and cell incidence
+  std::vector<double> wl(U, 0.0), inc(C, 0.0);
+  std::vector<uint32_t> tmp;
+  for (uint32_t e = 0; e < E; ++e) {
+    const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
+    if (en < b + 2) {
+      *err = e;
+      return TEXO_GP_ERR_INVALID_ARGUMENT;
+    }
+    for (uint32_t k = b; k < en; ++k)
+      if (p->pin_cell[k] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    const double w = 1.0 / (double)(uint32_t)(en - b - 1);
+    tmp.clear();
+    for (uint32_t k = b; k < en; ++k) tmp.push_back(p->cell_unit[p->pin_cell[k]]);
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    if (tmp.size() >= 2)
+      for (auto u : tmp) wl[u] += w;
+    tmp.clear();
+    for (uint32_t k = b; k < en; ++k) tmp.push_back(p->pin_cell[k]);
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    for (auto c : tmp) inc[c] += w;
+  }
+  std::vector<double> pin_weight_sum(U, 0.0);
+  for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
+    const uint32_t dc = p->arc_driver_cell[a], sc = p->arc_sink_cell[a];
+    if (dc >= C || sc >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    const uint32_t du = p->cell_unit[dc], su = p->cell_unit[sc];
+    const double w = u64_to_f64(p->arc_extra_weight[a]);
+    if (w > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
+    if (du != su) {
+      wl[du] += w;
+      wl[su] += w;
+    }
+    pin_weight_sum[du] += w;
+    pin_weight_sum[su] += w;
+  }
+  // degree classes: 2 | 3-4 | 5-8 | 9-16 | 17+ ; timed arcs last
+  static const int groups[5] = {2, 4, 8, 16, 32};
+  auto cls = [](uint32_t deg) { return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : 4; };
+  std::vector<std::vector<uint32_t>> bucket(5);
+  for (uint32_t e = 0; e < E; ++e) bucket[cls(p->net_ptr[e + 1] - p->net_ptr[e])].push_back(e);
+  m.net_ptr.assign(1, 0);
+  int nc = 0;
+  for (int c = 0; c < 5; ++c) {
+    m.class_begin[c] = (int)m.net_w.size();
+    m.class_group[c] = groups[c];
+    for (uint32_t e : bucket[c]) {
+      for (uint32_t k = p->net_ptr[e]; k < p->net_ptr[e + 1]; ++k) {
+        int unit;
+        double bx, by;
+        pin_of(p->pin_cell[k], unit, bx, by);
+        m.pin_unit.push_back(unit);
+        m.pin_base.push_back(bx);
+        m.pin_base.push_back(by);
+        if (unit >= 0) pin_weight_sum[unit] += 1.0;
+      }
+      m.net_ptr.push_back((int)m.pin_unit.size());
+      m.net_w.push_back(1.0f);
+    }
+    nc = c + 1;
+  }
+  m.n_hpwl_nets = (int)m.net_w.size();
+  m.class_begin[5] = (int)m.net_w.size();
+  m.class_group[5] = 2;
+  for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
+    for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
+      int unit;
+      double bx, by;
+      pin_of(cell, unit, bx, by);
+      m.pin_unit.push_back(unit);
+      m.pin_base.push_back(bx);
+      m.pin_base.push_back(by);
+    }
+    m.net_ptr.push_back((int)m.pin_unit.size());
+    m.net_w.push_back((float)u64_to_f64(p->arc_extra_weight[a]));
+  }
+  nc = 6;
+  m.n_classes = nc;
+  m.class_begin[6] = (int)m.net_w.size();
+  if (m.pin_unit.size() >= (1ull << 31)) return TEXO_GP_ERR_GRID_TOO_LARGE;
+  // WA fixed point: |derivative| <= 3 per pin, summed per unit, at 2^32 per unit
+  for (uint32_t u = 0; u < U; ++u)
+    if (pin_weight_sum[u] * 4.0 > 1073741824.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
+  // static preconditioner and per-field charges per optimizer object
+  m.pre_static.assign(nobj, 0.0);
+  for (uint32_t u = 0; u < U; ++u) m.pre_static[u] = wl[u];
+  m.pre_q.assign((size_t)m.K * nobj, 0.0);
+  for (uint32_t u = 0; u < U; ++u)
+    for (int i = m.unit_mem_ptr[u]; i < m.unit_mem_ptr[u + 1]; ++i)
+      m.pre_q[(size_t)m.mem_field[i] * nobj + u] += (double)p->member_charge[p->member_ptr[u] + (i - m.unit_mem_ptr[u])];
+  for (uint32_t j = 0; j < m.F; ++j) m.pre_q[(size_t)m.fil_field[j] * nobj + U + j] = m.fil_q[j];
+  // gamma weights (eplace.rs:1424-1439)
+  m.gamma_weight.assign(m.K, 0.0);
+  if (p->member_cell)
+    for (uint32_t i = 0; i < M; ++i) m.gamma_weight[active[p->member_field[i]]] += inc[p->member_cell[i]];
+  return TEXO_GP_OK;
+}
+
+}  // namespace tgp

@@ -1,0 +1,739 @@
+// stages.cuh — the placement engine's stages as block-level device functions.
+//
+// Every stage takes a virtual block index `vb` out of `nvb` and strides over
+// its items, so the same code runs as a standalone kernel (vb = blockIdx.x)
+// and inside the persistent cooperative kernel between grid barriers.
+// Reductions are written as one partial per virtual block and reduced in a
+// fixed order, so every result is bit-for-bit deterministic.
+#pragma once
+#include "common.cuh"
+
+namespace tgp {
+
+// Integer partial slots.
+enum ISlot {
+  IS_GRID_SUM = 0,                        // + field
+  IS_OVERFLOW = IS_GRID_SUM + kMaxFields, // + field
+  IS_OVER_BINS = IS_OVERFLOW + kMaxFields,
+  IS_DIFF = IS_OVER_BINS + kMaxFields,
+  IS_BAD = IS_DIFF + 1,                   // min index of a non-finite gradient
+  IS_PBAD,                                // any invalid preconditioner entry
+  kISlots
+};
+// Max/min partial slots (doubles).
+enum MSlot { MS_KKT = 0, MS_CHANGE, MS_PMIN, MS_PMAX, kMSlots };
+
+struct Partials {
+  double* sum;        // [kSlots][kMaxPartials]
+  long long* isum;    // [kISlots][kMaxPartials]
+  double* mx;         // [kMSlots][kMaxPartials]
+};
+
+__device__ __forceinline__ double* pslot(const Partials& p, int s) { return p.sum + (size_t)s * kMaxPartials; }
+__device__ __forceinline__ long long* islot(const Partials& p, int s) { return p.isum + (size_t)s * kMaxPartials; }
+__device__ __forceinline__ double* mslot(const Partials& p, int s) { return p.mx + (size_t)s * kMaxPartials; }
+
+// Fixed-order reduction of n partials by the whole block; every thread gets
+// the result. Identical in every block that calls it.
+template <typename T, typename Op>
+__device__ __forceinline__ T block_reduce_array(const T* a, int n, T init, Op op, T* sh) {
+  T v = init;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v = op(v, a[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  T r = init;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = op(r, sh[i]);
+  __syncthreads();
+  return r;
+}
+struct OpAdd {
+  template <typename T> __device__ T operator()(T a, T b) const { return a + b; }
+};
+struct OpMax {
+  __device__ double operator()(double a, double b) const { return fmax(a, b); }
+};
+struct OpMin {
+  __device__ double operator()(double a, double b) const { return fmin(a, b); }
+  __device__ long long operator()(long long a, long long b) const { return a < b ? a : b; }
+};
+
+// Block sum of a per-thread value, written as partial vb (thread 0).
+template <typename T>
+__device__ __forceinline__ void write_partial(T v, T* slot, int vb, T* sh) {
+  T r = block_sum(v, sh);
+  if (threadIdx.x == 0) slot[vb] = r;
+}
+__device__ __forceinline__ void write_partial_max(double v, double* slot, int vb, double* sh, bool is_min) {
+  v = is_min ? -warp_max(-v) : warp_max(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = sh[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = is_min ? fmin(r, sh[i]) : fmax(r, sh[i]);
+    slot[vb] = r;
+  }
+}
+
+struct Shared {
+  double d[kThreads / 32 * kMaxFields];
+  long long l[kThreads / 32];
+};
+
+// ---------------------------------------------------------------------------
+// S1: reset the accumulation grids.
+// ---------------------------------------------------------------------------
+static __device__ void stage_init(const Dev& d, int vb, int nvb, bool grids, bool wa) {
+  const int stride = nvb * blockDim.x;
+  const int t0 = vb * blockDim.x + threadIdx.x;
+  if (grids) {
+    const int n = d.K * d.B;
+    for (int i = t0; i < n; i += stride) {
+      d.phys[i] = -d.capfix[i];
+      d.fill[i] = 0;
+    }
+  }
+  if (wa)
+    for (int i = t0; i < 2 * d.U; i += stride) d.wa_fix[i] = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+// S2: density scatter. Members deposit into phys (after the capacity
+// background), fillers into fill; int64 2^-32 fixed point makes the sum
+// exact in any order. The per-field tap total is a partial for the mean.
+// (deposit_quadratic_bspline + the field loop, electrostatic_placement.rs:296-332)
+// ---------------------------------------------------------------------------
+static __device__ void stage_scatter(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb,
+                              Shared& sh) {
+  long long tot[kMaxFields];
+#pragma unroll
+  for (int f = 0; f < kMaxFields; ++f) tot[f] = 0;
+  const int stride = nvb * blockDim.x;
+  const int items = d.Mm + d.F;
+  for (int i = vb * blockDim.x + threadIdx.x; i < items; i += stride) {
+    double sxp, syp;
+    float q;
+    int f;
+    unsigned long long* grid;
+    if (i < d.Mm) {
+      const int u = d.mem_unit[i];
+      const double2 o = d.mem_off[i];
+      const double2 pu = pos[u];
+      sxp = __dadd_rn(pu.x, o.x);
+      syp = __dadd_rn(pu.y, o.y);
+      q = d.mem_q[i];
+      f = d.mem_field[i];
+      grid = (unsigned long long*)(d.phys + (size_t)f * d.B);
+    } else {
+      const int j = i - d.Mm;
+      const double2 pf = pos[d.U + j];
+      sxp = pf.x;
+      syp = pf.y;
+      q = d.fil_q[j];
+      f = d.fil_field[j];
+      grid = (unsigned long long*)(d.fill + (size_t)f * d.B);
+    }
+    const AxisTaps ax = axis_taps(d.g.Wb, to_bin(sxp, d.g.sx, d.g.identity));
+    const AxisTaps ay = axis_taps(d.g.Hb, to_bin(syp, d.g.sy, d.g.identity));
+    long long s = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const long long v = tap_fixed(q, ax.w[c], ay.w[r]);
+        s += v;
+        atomicAdd(grid + (size_t)ay.idx[r] * d.g.Wb + ax.idx[c], (unsigned long long)v);
+      }
+#pragma unroll
+    for (int ff = 0; ff < kMaxFields; ++ff)
+      if (ff == f) tot[ff] += s;
+  }
+  for (int f = 0; f < d.K; ++f) write_partial(tot[f], islot(p, IS_GRID_SUM + f), vb, sh.l);
+}
+
+// ---------------------------------------------------------------------------
+// S3: weighted-average wirelength (analytical_placement.rs:576-703).
+// A group of G lanes takes one net: hard max/min by shuffles, FP32 exp of the
+// FP64 deltas, soft means, per-pin derivative. Unit gradients accumulate as
+// int64 2^-32 fixed point, so the result is order-independent.
+// ---------------------------------------------------------------------------
+template <int G>
+__device__ __forceinline__ void wa_class(const Dev& d, const double2* __restrict__ pos, float gamma, float inv_gamma,
+                                         int nb, int ne, int vb, int nvb, double& acc) {
+  const int lane = threadIdx.x & (G - 1);
+  const int group = (vb * blockDim.x + threadIdx.x) / G;
+  const int groups = nvb * blockDim.x / G;
+  const unsigned mask = 0xffffffffu;
+  const int count = ne - nb;
+  for (int base = 0; base < count; base += groups) {
+    const int e = nb + base + group;
+    const bool active = base + group < count;
+    int p0 = 0, p1 = 0;
+    float w = 0.f;
+    if (active) {
+      p0 = d.net_ptr[e];
+      p1 = d.net_ptr[e + 1];
+      w = d.net_w[e];
+    }
+    // pass 1: max / min per axis
+    double mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
+    for (int k = p0 + lane; k < p1; k += G) {
+      const int u = d.pin_unit[k];
+      const double2 b = d.pin_base[k];
+      double x, y;
+      if (u < 0) {
+        x = b.x;
+        y = b.y;
+      } else {
+        const double2 pu = pos[u];
+        x = pu.x + b.x;
+        y = pu.y + b.y;
+      }
+      mx = fmax(mx, x);
+      mnx = fmin(mnx, x);
+      my = fmax(my, y);
+      mny = fmin(mny, y);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      mx = fmax(mx, __shfl_xor_sync(mask, mx, o, G));
+      mnx = fmin(mnx, __shfl_xor_sync(mask, mnx, o, G));
+      my = fmax(my, __shfl_xor_sync(mask, my, o, G));
+      mny = fmin(mny, __shfl_xor_sync(mask, mny, o, G));
+    }
+    // pass 2: exponential weights and their sums
+    float sw[4] = {0.f, 0.f, 0.f, 0.f}, sd[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k = p0 + lane; k < p1; k += G) {
+      const int u = d.pin_unit[k];
+      const double2 b = d.pin_base[k];
+      double x, y;
+      if (u < 0) {
+        x = b.x;
+        y = b.y;
+      } else {
+        const double2 pu = pos[u];
+        x = pu.x + b.x;
+        y = pu.y + b.y;
+      }
+      const float dxp = (float)(x - mx), dxn = (float)(x - mnx);
+      const float dyp = (float)(y - my), dyn = (float)(y - mny);
+      const float wxp = dxp == 0.f ? 1.f : __expf(dxp * inv_gamma);
+      const float wxn = dxn == 0.f ? 1.f : __expf(-dxn * inv_gamma);
+      const float wyp = dyp == 0.f ? 1.f : __expf(dyp * inv_gamma);
+      const float wyn = dyn == 0.f ? 1.f : __expf(-dyn * inv_gamma);
+      sw[0] += wxp; sd[0] += wxp * dxp;
+      sw[1] += wxn; sd[1] += wxn * dxn;
+      sw[2] += wyp; sd[2] += wyp * dyp;
+      sw[3] += wyn; sd[3] += wyn * dyn;
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        sw[a] += __shfl_xor_sync(mask, sw[a], o, G);
+        sd[a] += __shfl_xor_sync(mask, sd[a], o, G);
+      }
+    if (!active) continue;
+    float mean[4], inv[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      inv[a] = 1.f / sw[a];
+      mean[a] = sd[a] * inv[a];
+    }
+    // pass 3: per-pin derivative into the fixed-point unit gradient
+    for (int k = p0 + lane; k < p1; k += G) {
+      const int u = d.pin_unit[k];
+      if (u < 0) continue;
+      const double2 b = d.pin_base[k];
+      const double2 pu = pos[u];
+      const double x = pu.x + b.x, y = pu.y + b.y;
+      const float dxp = (float)(x - mx), dxn = (float)(x - mnx);
+      const float dyp = (float)(y - my), dyn = (float)(y - mny);
+      const float wxp = dxp == 0.f ? 1.f : __expf(dxp * inv_gamma);
+      const float wxn = dxn == 0.f ? 1.f : __expf(-dxn * inv_gamma);
+      const float wyp = dyp == 0.f ? 1.f : __expf(dyp * inv_gamma);
+      const float wyn = dyn == 0.f ? 1.f : __expf(-dyn * inv_gamma);
+      const float gx = wxp * inv[0] * (1.f + (dxp - mean[0]) * inv_gamma) -
+                       wxn * inv[1] * (1.f - (dxn - mean[1]) * inv_gamma);
+      const float gy = wyp * inv[2] * (1.f + (dyp - mean[2]) * inv_gamma) -
+                       wyn * inv[3] * (1.f - (dyn - mean[3]) * inv_gamma);
+      atomicAdd(d.wa_fix + 2 * u, (unsigned long long)__float2ll_rn(w * gx * kFixF));
+      atomicAdd(d.wa_fix + 2 * u + 1, (unsigned long long)__float2ll_rn(w * gy * kFixF));
+    }
+    if (lane == 0)
+      acc += (double)w * (((mx - mnx) + (double)mean[0] - (double)mean[1]) +
+                          ((my - mny) + (double)mean[2] - (double)mean[3]));
+  }
+  (void)gamma;
+}
+
+static __device__ void stage_wa(const Dev& d, const double2* __restrict__ pos, double gamma, Partials p, int vb, int nvb,
+                         Shared& sh) {
+  double acc = 0.0;
+  const float g = (float)gamma, ig = (float)(1.0 / gamma);
+  for (int c = 0; c < d.n_classes; ++c) {
+    const int nb = d.class_begin[c], ne = d.class_begin[c + 1];
+    if (ne <= nb) continue;
+    switch (d.class_group[c]) {
+      case 2: wa_class<2>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+      case 4: wa_class<4>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+      case 8: wa_class<8>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+      case 16: wa_class<16>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+      default: wa_class<32>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+    }
+  }
+  write_partial(acc, pslot(p, SLOT_WA_VALUE), vb, sh.d);
+}
+
+// ---------------------------------------------------------------------------
+// S4: density grid -> FP32 mean-free charge, physical overflow partials
+// (the pre-filler positive overflow, electrostatic_placement.rs:317-318).
+// ---------------------------------------------------------------------------
+static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int vb, int nvb, Shared& sh) {
+  __shared__ long long s_mean_sum[kMaxFields];
+  __shared__ long long red[kThreads / 32];
+  for (int f = 0; f < d.K; ++f) {
+    long long tot = block_reduce_array(islot(p, IS_GRID_SUM + f), nvb_scatter, 0ll, OpAdd(), red);
+    if (threadIdx.x == 0) s_mean_sum[f] = tot - d.capsum[f];
+  }
+  __syncthreads();
+  long long ov[kMaxFields], cnt[kMaxFields];
+#pragma unroll
+  for (int f = 0; f < kMaxFields; ++f) ov[f] = cnt[f] = 0;
+  const int stride = nvb * blockDim.x;
+  for (int f = 0; f < d.K; ++f) {
+    const double mean = (double)s_mean_sum[f] * kInvFix / (double)d.B;
+    const long long* ph = d.phys + (size_t)f * d.B;
+    const long long* fl = d.fill + (size_t)f * d.B;
+    float* rho = d.rho + (size_t)f * d.B;
+    for (int i = vb * blockDim.x + threadIdx.x; i < d.B; i += stride) {
+      const long long a = ph[i];
+      if (a > 0) {
+        ov[f] += a;
+        cnt[f] += 1;
+      }
+      rho[i] = (float)((double)(a + fl[i]) * kInvFix - mean);
+    }
+  }
+  for (int f = 0; f < d.K; ++f) {
+    write_partial(ov[f], islot(p, IS_OVERFLOW + f), vb, sh.l);
+    write_partial(cnt[f], islot(p, IS_OVER_BINS + f), vb, sh.l);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// S5: FP32 CUDA-core GEMM, C[MxN] = A[MxK] B[KxN], all row-major, for each
+// of nf grids (A/B/C advance by their per-grid strides; 0 = shared matrix).
+// Epilogue: 0 store; 1 store C * inv_eig; 2 store and accumulate
+// <rho, C> into per-field energy partials.
+// ---------------------------------------------------------------------------
+template <int TM, int TN, int TK, int RM, int RN>
+struct GemmSmem {
+  float a[TK][TM + 1];
+  float b[TK][TN + 4];
+};
+
+// Accumulation is compensated: plain FMAs within chunks of kChunk products,
+// and each chunk sum enters a (sum, compensation) pair through an
+// error-free TwoSum. The potential's low-frequency modes are small sums of
+// large cancelling terms that 1/lambda then amplifies; plain FP32
+// accumulation leaves ~1e-5 relative error in the field, the chunked
+// compensation ~4e-6 (against the FP64 spectral solve).
+constexpr int kChunk = 8;
+
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float part) {
+  const float t = __fadd_rn(s, part);
+  const float z = __fsub_rn(t, s);
+  const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(part, z));
+  s = t;
+  c = __fadd_rn(c, e);
+}
+
+template <int TM, int TN, int TK, int RM, int RN>
+__device__ void gemm_tiles(const float* A, long sa, const float* Bm, long sb, float* Cm, long sc, int M, int N,
+                           int Kd, int nf, int epi, const float* inv_eig, const float* rho, double* energy_acc,
+                           int vb, int nvb, GemmSmem<TM, TN, TK, RM, RN>& sm) {
+  static_assert((TM / RM) * (TN / RN) == kThreads, "tile / thread mismatch");
+  static_assert(TK % kChunk == 0, "k slab must hold whole chunks");
+  constexpr int TX = TN / RN;
+  constexpr int LA = TM * TK / kThreads, LB = TK * TN / kThreads;  // loads per thread per slab
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int tiles_m = (M + TM - 1) / TM, tiles_n = (N + TN - 1) / TN;
+  const int tiles = tiles_m * tiles_n * nf;
+  for (int t = vb; t < tiles; t += nvb) {
+    const int f = t / (tiles_m * tiles_n);
+    const int r = t % (tiles_m * tiles_n);
+    const int m0 = (r / tiles_n) * TM, n0 = (r % tiles_n) * TN;
+    const float* Af = A + f * sa;
+    const float* Bf = Bm + f * sb;
+    float sum[RM][RN], comp[RM][RN];
+#pragma unroll
+    for (int i = 0; i < RM; ++i)
+#pragma unroll
+      for (int j = 0; j < RN; ++j) sum[i][j] = comp[i][j] = 0.f;
+    // register prefetch of the next slab overlaps global latency with math
+    float ra[LA], rb[LB];
+    auto fetch = [&](int k0) {
+#pragma unroll
+      for (int q = 0; q < LA; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int mm = e / TK, kk = e % TK;
+        const int gm = m0 + mm, gk = k0 + kk;
+        ra[q] = (gm < M && gk < Kd) ? __ldg(Af + (size_t)gm * Kd + gk) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < LB; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int kk = e / TN, nn = e % TN;
+        const int gk = k0 + kk, gn = n0 + nn;
+        rb[q] = (gk < Kd && gn < N) ? __ldg(Bf + (size_t)gk * N + gn) : 0.f;
+      }
+    };
+    fetch(0);
+    for (int k0 = 0; k0 < Kd; k0 += TK) {
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < LA; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        sm.a[e % TK][e / TK] = ra[q];
+      }
+#pragma unroll
+      for (int q = 0; q < LB; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        sm.b[e / TN][e % TN] = rb[q];
+      }
+      __syncthreads();
+      if (k0 + TK < Kd) fetch(k0 + TK);
+#pragma unroll
+      for (int kc = 0; kc < TK; kc += kChunk) {
+        float part[RM][RN];
+#pragma unroll
+        for (int i = 0; i < RM; ++i)
+#pragma unroll
+          for (int j = 0; j < RN; ++j) part[i][j] = 0.f;
+#pragma unroll
+        for (int kk = kc; kk < kc + kChunk; ++kk) {
+          float av[RM], bv[RN];
+#pragma unroll
+          for (int i = 0; i < RM; ++i) av[i] = sm.a[kk][ty * RM + i];
+#pragma unroll
+          for (int j = 0; j < RN; ++j) bv[j] = sm.b[kk][tx * RN + j];
+#pragma unroll
+          for (int i = 0; i < RM; ++i)
+#pragma unroll
+            for (int j = 0; j < RN; ++j) part[i][j] = fmaf(av[i], bv[j], part[i][j]);
+        }
+#pragma unroll
+        for (int i = 0; i < RM; ++i)
+#pragma unroll
+          for (int j = 0; j < RN; ++j) two_sum_acc(sum[i][j], comp[i][j], part[i][j]);
+      }
+    }
+    float* Cf = Cm + f * sc;
+#pragma unroll
+    for (int i = 0; i < RM; ++i)
+#pragma unroll
+      for (int j = 0; j < RN; ++j) {
+        const int gm = m0 + ty * RM + i, gn = n0 + tx * RN + j;
+        if (gm < M && gn < N) {
+          const size_t idx = (size_t)gm * N + gn;
+          float v = __fadd_rn(sum[i][j], comp[i][j]);
+          if (epi == 1) v *= inv_eig[idx];
+          Cf[idx] = v;
+          if (epi == 2) energy_acc[f] += (double)rho[(size_t)f * M * N + idx] * (double)v;
+        }
+      }
+  }
+  __syncthreads();
+}
+
+// Small-grid and large-grid tile shapes.
+using SmemS = GemmSmem<32, 32, 32, 2, 2>;
+using SmemL = GemmSmem<64, 64, 16, 4, 4>;
+union GemmShared {
+  SmemS s;
+  SmemL l;
+};
+
+__device__ __forceinline__ void gemm_any(bool large, const float* A, long sa, const float* Bm, long sb, float* Cm,
+                                         long sc, int M, int N, int Kd, int nf, int epi, const float* inv_eig,
+                                         const float* rho, double* eacc, int vb, int nvb, GemmShared& sm) {
+  if (large)
+    gemm_tiles<64, 64, 16, 4, 4>(A, sa, Bm, sb, Cm, sc, M, N, Kd, nf, epi, inv_eig, rho, eacc, vb, nvb, sm.l);
+  else
+    gemm_tiles<32, 32, 32, 2, 2>(A, sa, Bm, sb, Cm, sc, M, N, Kd, nf, epi, inv_eig, rho, eacc, vb, nvb, sm.s);
+}
+
+// The four transforms of the spectral solve (Poisson2d::solve,
+// electrostatic_placement.rs:725-776) as dense GEMMs:
+//   t1 = rho Cx^T ; t2 = (Cy t1) o inv_eig ; t1 = Cy^T t2 ; phi = t1 Cx.
+// `step` selects one of the four (a grid barrier separates them).
+static __device__ void stage_dct(const Dev& d, int step, bool large, Partials p, int vb, int nvb, GemmShared& sm,
+                          Shared& sh) {
+  const int W = d.g.Wb, H = d.g.Hb;
+  const long sg = d.B;
+  double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+  switch (step) {
+    case 0: gemm_any(large, d.rho, sg, d.CxT, 0, d.t1, sg, H, W, W, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
+    case 1: gemm_any(large, d.Cy, 0, d.t1, sg, d.t2, sg, H, W, H, d.K, 1, d.inv_eig, nullptr, eacc, vb, nvb, sm); break;
+    case 2: gemm_any(large, d.CyT, 0, d.t2, sg, d.t1, sg, H, W, H, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
+    default: gemm_any(large, d.t1, sg, d.Cx, 0, d.phi, sg, H, W, W, d.K, 2, nullptr, d.rho, eacc, vb, nvb, sm); break;
+  }
+  if (step == 3)
+    for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), vb, sh.d);
+}
+
+// ---------------------------------------------------------------------------
+// S6: field gather (sample_quadratic_bspline_with_gradient + the member and
+// filler loops, electrostatic_placement.rs:338-374, 919-941): raw per-field
+// gradient q * dphi per optimizer object, and force_l1 partials.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, double sxp, double syp) {
+  const AxisTaps ax = axis_taps(d.g.Wb, to_bin(sxp, d.g.sx, d.g.identity));
+  const AxisTaps ay = axis_taps(d.g.Hb, to_bin(syp, d.g.sy, d.g.identity));
+  const float dx[3] = {ax.o - 0.5f, -2.f * ax.o, ax.o + 0.5f};
+  const float dy[3] = {ay.o - 0.5f, -2.f * ay.o, ay.o + 0.5f};
+  // The derivative weights of each axis sum to zero, so the centre tap's
+  // potential can be subtracted first: the FP32 sum then rounds relative to
+  // the local potential differences, not to the potential itself.
+  const float vc = __ldg(phi + (size_t)ay.idx[1] * d.g.Wb + ax.idx[1]);
+  float gx = 0.f, gy = 0.f;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const float* row = phi + (size_t)ay.idx[r] * d.g.Wb;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = __ldg(row + ax.idx[c]) - vc;
+      gx += dx[c] * ay.w[r] * v;
+      gy += ax.w[c] * dy[r] * v;
+    }
+  }
+  if (!d.g.identity) {
+    gx *= (float)d.g.sx;
+    gy *= (float)d.g.sy;
+  }
+  return make_float2(gx, gy);
+}
+
+static __device__ void stage_gather(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb, Shared& sh) {
+  double force[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    if (o < d.U) {
+      float2 acc[kMaxFields];
+#pragma unroll
+      for (int f = 0; f < kMaxFields; ++f) acc[f] = make_float2(0.f, 0.f);
+      const int m0 = d.unit_mem_ptr[o], m1 = d.unit_mem_ptr[o + 1];
+      const double2 pu = pos[o];
+      for (int m = m0; m < m1; ++m) {
+        const int f = d.mem_field[m];
+        const double2 off = d.mem_off[m];
+        const float q = d.mem_q[m];
+        const float2 g = sample_grad(d, d.phi + (size_t)f * d.B, pu.x + off.x, pu.y + off.y);
+#pragma unroll
+        for (int ff = 0; ff < kMaxFields; ++ff)
+          if (ff == f) {
+            acc[ff].x += q * g.x;
+            acc[ff].y += q * g.y;
+            force[ff] += (double)q * ((double)fabsf(g.x) + (double)fabsf(g.y));
+          }
+      }
+      for (int f = 0; f < d.K; ++f) d.graw[(size_t)f * d.nobj + o] = acc[f];
+    } else {
+      const int j = o - d.U;
+      const int f = d.fil_field[j];
+      const float q = d.fil_q[j];
+      const double2 pf = pos[o];
+      const float2 g = sample_grad(d, d.phi + (size_t)f * d.B, pf.x, pf.y);
+      d.graw[(size_t)f * d.nobj + o] = make_float2(q * g.x, q * g.y);
+#pragma unroll
+      for (int ff = 0; ff < kMaxFields; ++ff)
+        if (ff == f) force[ff] += (double)q * ((double)fabsf(g.x) + (double)fabsf(g.y));
+    }
+  }
+  for (int f = 0; f < d.K; ++f) write_partial(force[f], pslot(p, SLOT_FORCE + f), vb, sh.d);
+}
+
+// ---------------------------------------------------------------------------
+// S7: combined objective gradient (combined_objective, eplace.rs:1022-1044):
+// g = grad WA + sum_f coef_f grad E_f, with the non-finite check and the L1
+// norms the initial multiplier needs (eplace.rs:1126-1148).
+// ---------------------------------------------------------------------------
+static __device__ void stage_combine(const Dev& d, const double* coef, double2* __restrict__ gout, Partials p, int vb,
+                              int nvb, Shared& sh) {
+  double rawl1[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+  double wal1 = 0.0;
+  long long bad = 0x7fffffffffffffffll;
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    double gx = 0.0, gy = 0.0;
+    if (o < d.U) {
+      gx = (double)(long long)d.wa_fix[2 * o] * kInvFix;
+      gy = (double)(long long)d.wa_fix[2 * o + 1] * kInvFix;
+      wal1 += fabs(gx) + fabs(gy);
+      for (int f = 0; f < d.K; ++f) {
+        const float2 r = d.graw[(size_t)f * d.nobj + o];
+        gx += coef[f] * (double)r.x;
+        gy += coef[f] * (double)r.y;
+        rawl1[f] += (double)fabsf(r.x) + (double)fabsf(r.y);
+      }
+    } else {
+      const int f = d.fil_field[o - d.U];
+      const float2 r = d.graw[(size_t)f * d.nobj + o];
+      for (int ff = 0; ff < d.K; ++ff)
+        if (ff == f) {
+          gx += coef[ff] * (double)r.x;
+          gy += coef[ff] * (double)r.y;
+          rawl1[ff] += (double)fabsf(r.x) + (double)fabsf(r.y);
+        }
+    }
+    if (!isfinite(gx)) bad = min(bad, (long long)(2 * o));
+    else if (!isfinite(gy)) bad = min(bad, (long long)(2 * o + 1));
+    gout[o] = make_double2(gx, gy);
+  }
+  for (int f = 0; f < d.K; ++f) write_partial(rawl1[f], pslot(p, SLOT_RAWL1 + f), vb, sh.d);
+  write_partial(wal1, pslot(p, SLOT_WAL1), vb, sh.d);
+  // min-reduce the bad index
+  {
+    long long v = bad;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w < v ? w : v;
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sh.l[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      long long r = sh.l[0];
+      for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = sh.l[i] < r ? sh.l[i] : r;
+      islot(p, IS_BAD)[vb] = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Nesterov vector stages (global_placement.rs:143-335, 588-712).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rclamp(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// y = clamp(x + e (x - prev)); counts coordinates where y != x.
+static __device__ void stage_extrapolate(const Dev& d, const double2* __restrict__ x, const double2* __restrict__ xp,
+                                  double e, double2* __restrict__ y, Partials p, int vb, int nvb, Shared& sh) {
+  long long diff = 0;
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    const double2 a = x[o], b = xp[o], lo = d.lo[o], hi = d.hi[o];
+    double2 r;
+    r.x = rclamp(a.x + e * (a.x - b.x), lo.x, hi.x);
+    r.y = rclamp(a.y + e * (a.y - b.y), lo.y, hi.y);
+    diff += (r.x != a.x) + (r.y != a.y);
+    y[o] = r;
+  }
+  write_partial(diff, islot(p, IS_DIFF), vb, sh.l);
+}
+
+// c = clamp(y - g / (L P)); changed count, <g, c - y>, sum P (c - y)^2.
+static __device__ void stage_candidate(const Dev& d, const double2* __restrict__ y, const double2* __restrict__ gy,
+                                double L, double2* __restrict__ c, Partials p, int vb, int nvb, Shared& sh) {
+  long long diff = 0;
+  double dot = 0.0, msn = 0.0;
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    const double2 a = y[o], g = gy[o], lo = d.lo[o], hi = d.hi[o];
+    const double m = d.P[o];
+    const double den = L * m;
+    double2 r;
+    r.x = rclamp(a.x - g.x / den, lo.x, hi.x);
+    r.y = rclamp(a.y - g.y / den, lo.y, hi.y);
+    diff += (r.x != a.x) + (r.y != a.y);
+    const double dx = r.x - a.x, dy = r.y - a.y;
+    dot += g.x * dx + g.y * dy;
+    msn += m * dx * dx + m * dy * dy;
+    c[o] = r;
+  }
+  write_partial(diff, islot(p, IS_DIFF), vb, sh.l);
+  write_partial(dot, pslot(p, SLOT_DOT), vb, sh.d);
+  write_partial(msn, pslot(p, SLOT_MSN), vb, sh.d);
+}
+
+__device__ __forceinline__ double kkt_comp(double g, double x, double lo, double hi) {
+  if (__double_as_longlong(lo) == __double_as_longlong(hi) || (x <= lo && g > 0.0) || (x >= hi && g < 0.0))
+    return 0.0;
+  return fabs(g);
+}
+
+// box_metric_kkt_residual (global_placement.rs:648-663) and, optionally, the
+// max coordinate change against `ref`.
+static __device__ void stage_kkt(const Dev& d, const double2* __restrict__ x, const double2* __restrict__ g,
+                          const double2* __restrict__ ref, Partials p, int vb, int nvb, Shared& sh) {
+  double r = 0.0, ch = 0.0;
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    const double2 a = x[o], gg = g[o], lo = d.lo[o], hi = d.hi[o];
+    const double s = sqrt(d.P[o]);
+    r = fmax(r, kkt_comp(gg.x, a.x, lo.x, hi.x) / s);
+    r = fmax(r, kkt_comp(gg.y, a.y, lo.y, hi.y) / s);
+    if (ref) {
+      const double2 b = ref[o];
+      ch = fmax(ch, fabs(a.x - b.x));
+      ch = fmax(ch, fabs(a.y - b.y));
+    }
+  }
+  write_partial_max(r, mslot(p, MS_KKT), vb, sh.d, false);
+  if (ref) write_partial_max(ch, mslot(p, MS_CHANGE), vb, sh.d, false);
+}
+
+// diagonal_preconditioner (eplace.rs:1046-1100).
+static __device__ void stage_precond(const Dev& d, const double* lambda, Partials p, int vb, int nvb, Shared& sh) {
+  double pmin = INFINITY, pmax = 0.0;
+  long long badp = 0;
+  const int stride = nvb * blockDim.x;
+  for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
+    double v = d.pre_static[o];
+    for (int f = 0; f < d.K; ++f) {
+      const double q = d.pre_q[(size_t)f * d.nobj + o];
+      if (q == 0.0) continue;
+      v += lambda[f] * q;
+    }
+    if (!isfinite(v) || v < 0.0) badp = 1;
+    v = fmax(v, 1.0);
+    d.P[o] = v;
+    pmin = fmin(pmin, v);
+    pmax = fmax(pmax, v);
+  }
+  write_partial_max(pmin, mslot(p, MS_PMIN), vb, sh.d, true);
+  write_partial_max(pmax, mslot(p, MS_PMAX), vb, sh.d, false);
+  write_partial(badp, islot(p, IS_PBAD), vb, sh.l);
+}
+
+// HPWL over the baseline hypernets at `pos` (FP64).
+static __device__ void stage_hpwl(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb, Shared& sh) {
+  double acc = 0.0;
+  const int stride = nvb * blockDim.x;
+  for (int e = vb * blockDim.x + threadIdx.x; e < d.n_hpwl_nets; e += stride) {
+    double mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
+    for (int k = d.net_ptr[e]; k < d.net_ptr[e + 1]; ++k) {
+      const int u = d.pin_unit[k];
+      const double2 b = d.pin_base[k];
+      double x = b.x, y = b.y;
+      if (u >= 0) {
+        x = pos[u].x + b.x;
+        y = pos[u].y + b.y;
+      }
+      mx = fmax(mx, x);
+      mnx = fmin(mnx, x);
+      my = fmax(my, y);
+      mny = fmin(mny, y);
+    }
+    acc += (mx - mnx) + (my - mny);
+  }
+  write_partial(acc, pslot(p, SLOT_HPWL), vb, sh.d);
+}
+
+}  // namespace tgp

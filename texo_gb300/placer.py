@@ -1,0 +1,160 @@
+"""Python mirror of the reference's global-placement entry points.
+
+`place(problem, params)` is `eplace::place` (crates/texo-pnr/src/eplace.rs:242-421):
+it returns the rounded unit targets of the best checkpoint, or raises
+`TexoGpError` carrying the reference error variant. `Placer` exposes the
+device-resident handle underneath for per-stage parity checks
+(`ContinuousProblem::evaluate`, eplace.rs:137-205), resumable runs and
+stage timing. Every call goes through the C ABI of include/texo_gp.h; there
+is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+def default_params(**overrides):
+    p = abi.Params()
+    abi.load().texo_gp_default_params(C.byref(p))
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def _stats_dict(s):
+    K = s.num_fields
+    return dict(status=abi.STATUS.get(s.status, s.status), iterations=s.iterations,
+                evaluations=s.evaluations, line_search_trials=s.line_search_trials,
+                overflow=[s.overflow[i] for i in range(K)], energy=[s.energy[i] for i in range(K)],
+                gamma=s.gamma, objective=s.objective, hpwl=s.hpwl, converged=bool(s.converged),
+                elapsed_ms=s.elapsed_ms, kernel_launches=s.kernel_launches)
+
+
+def place(problem, params=None):
+    """eplace::place through texo_gp_place: returns (targets [U,2] uint32,
+    coordinates [2(U+F)] float64, stats dict)."""
+    lib = abi.load()
+    params = params or default_params()
+    pc = problem.c_struct()
+    targets = np.zeros(2 * problem.num_units, np.uint32)
+    # the optimizer vector length is known only after filler construction
+    with Placer(problem, params) as h:
+        coords = np.zeros(h.n)
+    st = abi.Stats()
+    code = lib.texo_gp_place(C.byref(pc), C.byref(params), abi.ptr(targets, C.c_uint32),
+                             abi.ptr(coords, C.c_double), C.byref(st))
+    abi.check(code, "texo_gp_place")
+    return targets.reshape(-1, 2), coords, _stats_dict(st)
+
+
+class Placer:
+    """A device-resident placement instance (texo_gp_handle)."""
+
+    def __init__(self, problem, params=None):
+        self.lib = abi.load()
+        self.problem = problem
+        self.params = params or default_params()
+        self._pc = problem.c_struct()
+        h = C.c_void_p()
+        abi.check(self.lib.texo_gp_create(C.byref(self._pc), C.byref(self.params), C.byref(h)),
+                  "texo_gp_create")
+        self.h = h
+        u, f, n = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        bx, by, k = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        abi.check(self.lib.texo_gp_sizes(h, C.byref(u), C.byref(f), C.byref(n), C.byref(bx),
+                                         C.byref(by), C.byref(k)), "texo_gp_sizes")
+        self.units, self.num_fillers, self.n = u.value, f.value, n.value
+        self.bins_x, self.bins_y, self.num_fields = bx.value, by.value, k.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.texo_gp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def bins(self):
+        return self.bins_x * self.bins_y
+
+    def initial(self):
+        c, lo, hi = np.zeros(self.n), np.zeros(self.n), np.zeros(self.n)
+        abi.check(self.lib.texo_gp_initial(self.h, abi.ptr(c, C.c_double), abi.ptr(lo, C.c_double),
+                                           abi.ptr(hi, C.c_double)), "texo_gp_initial")
+        return c, lo, hi
+
+    def fillers(self):
+        f = np.zeros(self.num_fillers, np.uint32)
+        q = np.zeros(self.num_fillers)
+        abi.check(self.lib.texo_gp_fillers(self.h, abi.ptr(f, C.c_uint32), abi.ptr(q, C.c_double)),
+                  "texo_gp_fillers")
+        return f, q
+
+    def evaluate(self, coords, gamma, arrays=True):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        K, n, B = self.num_fields, self.n, self.bins
+        ev = abi.Eval()
+        wag = np.zeros(2 * self.units) if arrays else None
+        fg = np.zeros(K * n) if arrays else None
+        dens = np.zeros(K * B) if arrays else None
+        pot = np.zeros(K * B) if arrays else None
+        abi.check(self.lib.texo_gp_evaluate(self.h, abi.ptr(coords, C.c_double), gamma, C.byref(ev),
+                                            abi.ptr(wag, C.c_double), abi.ptr(fg, C.c_double),
+                                            abi.ptr(dens, C.c_double), abi.ptr(pot, C.c_double)),
+                  "texo_gp_evaluate")
+        out = {"wirelength": ev.wirelength, "fields": [ev.fields[i] for i in range(K)]}
+        if arrays:
+            out.update(wa_gradient=wag, field_gradient=fg.reshape(K, n), density=dens.reshape(K, B),
+                       potential=pot.reshape(K, B))
+        return out
+
+    def scatter(self, coords):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        K, B = self.num_fields, self.bins
+        phys = np.zeros(K * B, np.int64)
+        fill = np.zeros(K * B, np.int64)
+        abi.check(self.lib.texo_gp_scatter(self.h, abi.ptr(coords, C.c_double), abi.ptr(phys, C.c_int64),
+                                           abi.ptr(fill, C.c_int64)), "texo_gp_scatter")
+        return phys.reshape(K, B), fill.reshape(K, B)
+
+    def poisson(self, density):
+        d = np.ascontiguousarray(density, dtype=np.float64)
+        pot = np.zeros(self.bins)
+        e = C.c_double()
+        abi.check(self.lib.texo_gp_poisson(self.h, abi.ptr(d, C.c_double), abi.ptr(pot, C.c_double),
+                                           C.byref(e)), "texo_gp_poisson")
+        return pot, e.value
+
+    def run(self, max_iterations=0, allow_nonconverged=False):
+        targets = np.zeros(2 * self.units, np.uint32)
+        coords = np.zeros(self.n)
+        st = abi.Stats()
+        code = self.lib.texo_gp_run(self.h, max_iterations, abi.ptr(targets, C.c_uint32),
+                                    abi.ptr(coords, C.c_double), C.byref(st))
+        if not (allow_nonconverged and code == abi.CODE["DID_NOT_CONVERGE"]):
+            abi.check(code, "texo_gp_run")
+        return targets.reshape(-1, 2), coords, _stats_dict(st)
+
+    def reset(self):
+        abi.check(self.lib.texo_gp_reset(self.h), "texo_gp_reset")
+
+    def hpwl(self, coords):
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        out = C.c_double()
+        abi.check(self.lib.texo_gp_hpwl(self.h, abi.ptr(coords, C.c_double), C.byref(out)), "texo_gp_hpwl")
+        return out.value
+
+    def stage_times(self, reps=20):
+        ms = np.zeros(64)
+        cnt = C.c_uint32()
+        abi.check(self.lib.texo_gp_stage_times(self.h, reps, abi.ptr(ms, C.c_double), 64, C.byref(cnt)),
+                  "texo_gp_stage_times")
+        return {self.lib.texo_gp_stage_name(i).decode(): float(ms[i]) for i in range(cnt.value)}
