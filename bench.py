@@ -207,6 +207,8 @@ def main():
     ap.add_argument("--reference-sample", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="warmup and timed steps only (for ncu launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -271,6 +273,11 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     max_ms = float(t.item())
     value = world * args.steps / (max_ms / 1000.0)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "iter/s", "profile": True,
+                              "gpu_launches": int(launches)}), flush=True)
+        return
     # per-stage device times and the dominant kernel's roofline
     stages = g.stage_times(reps=20)
     peak, peak_kind = peaks()

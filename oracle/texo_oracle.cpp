@@ -1700,36 +1700,91 @@ int32_t orc_evaluate(orc_handle h, const double* coords, double gamma, int32_t t
   return TEXO_GP_OK;
 }
 
-// The device's deposit arithmetic: FP64 bin coordinate, FP32 offset and
-// weights, FP32 tap, round-to-nearest-even into int64 at 2^32 per unit.
-static inline void fixed_axis(uint32_t n, double c, uint32_t idx[3], float w[3]) {
-  const double maximum = (double)(n - 1);
-  c = rclamp(c, 0.0, maximum);
-  const double cc = rmin(std::floor(c + 0.5), maximum);
-  const uint32_t center = (uint32_t)cc;
-  const float o = (float)(c - cc);
+// The device's deposit arithmetic restated: FP32 coordinates; for a bin grid
+// that differs from the tile grid, the bin coordinate is the tile centre's
+// FP64 value split into hi + lo floats plus the sub-tile fraction times the
+// FP32 scale; FP32 offset and weights; FP32 tap rounded to nearest-even into
+// int64 at 2^32 per unit charge.
+struct FixedMap {
+  bool identity;
+  uint32_t tiles, bins;
+  float scale;
+  std::vector<float> hi, lo;
+  FixedMap(uint32_t t, uint32_t b, bool id) : identity(id), tiles(t), bins(b) {
+    scale = (float)((double)b / (double)t);
+    hi.resize(t);
+    lo.resize(t);
+    const double sc = (double)b / (double)t;
+    for (uint32_t i = 0; i < t; ++i) {
+      const double v = ((double)i + 0.5) * sc - 0.5;
+      hi[i] = (float)v;
+      lo[i] = (float)(v - (double)hi[i]);
+    }
+  }
+};
+static inline void fixed_axis(const FixedMap& m, float s, uint32_t idx[3], float w[3]) {
+  const uint32_t n = m.bins;
+  const float maximum = (float)(n - 1);
+  float hi, lo;
+  if (m.identity) {
+    hi = s;
+    lo = 0.f;
+  } else {
+    float ts = std::nearbyint(s);
+    ts = ts > 0.f ? ts : 0.f;
+    ts = ts < (float)(m.tiles - 1) ? ts : (float)(m.tiles - 1);
+    const uint32_t t = (uint32_t)ts;
+    hi = m.hi[t];
+    const float frac = s - ts;
+    const float prod = frac * m.scale;
+    lo = m.lo[t] + prod;
+  }
+  const float c = hi + lo;
+  uint32_t center;
+  float o;
+  if (!(c > 0.f)) {
+    center = 0;
+    o = 0.f;
+  } else if (c >= maximum) {
+    center = n - 1;
+    o = 0.f;
+  } else {
+    const float cc = std::fmin(std::floor(c + 0.5f), maximum);
+    center = (uint32_t)cc;
+    const float d = hi - cc;
+    o = d + lo;
+  }
   const float a = 0.5f - o, b = 0.5f + o;
   idx[0] = center == 0 ? 0 : center - 1;
   idx[1] = center;
   idx[2] = std::min(center + 1, n - 1);
-  w[0] = 0.5f * (a * a);
-  w[1] = 0.75f - o * o;
-  w[2] = 0.5f * (b * b);
+  const float aa = a * a, bb = b * b, oo = o * o;
+  w[0] = 0.5f * aa;
+  w[1] = 0.75f - oo;
+  w[2] = 0.5f * bb;
 }
-static inline int64_t to_fixed(float v) { return (int64_t)std::nearbyint((double)(v * 4294967296.0f)); }
-static void deposit_fixed(int64_t* g, uint32_t Wb, uint32_t Hb, double bx, double by, float q) {
+static inline int64_t to_fixed(float v) {
+  const float scaled = v * 4294967296.0f;
+  return (int64_t)std::nearbyint((double)scaled);
+}
+static void deposit_fixed(int64_t* g, const FixedMap& mx, const FixedMap& my, float x, float y, float q) {
   uint32_t ix[3], iy[3];
   float wx[3], wy[3];
-  fixed_axis(Wb, bx, ix, wx);
-  fixed_axis(Hb, by, iy, wy);
+  fixed_axis(mx, x, ix, wx);
+  fixed_axis(my, y, iy, wy);
   for (int r = 0; r < 3; ++r)
-    for (int c = 0; c < 3; ++c) g[(size_t)iy[r] * Wb + ix[c]] += to_fixed((q * wx[c]) * wy[r]);
+    for (int c = 0; c < 3; ++c) {
+      const float t1 = q * wx[c];
+      const float t2 = t1 * wy[r];
+      g[(size_t)iy[r] * mx.bins + ix[c]] += to_fixed(t2);
+    }
 }
 
 int32_t orc_scatter_fixed(orc_handle h, const double* coords, int64_t* physical, int64_t* fill,
                           int64_t* overflow_fixed, uint64_t* overflow_bins) {
   Oracle& o = h->o;
   const size_t B = o.bins();
+  const FixedMap mapx(o.W, o.Wb, o.identity_map), mapy(o.H, o.Hb, o.identity_map);
   for (uint32_t f = 0; f < o.K; ++f) {
     int64_t* gp = physical + (size_t)f * B;
     int64_t* gf = fill + (size_t)f * B;
@@ -1738,14 +1793,17 @@ int32_t orc_scatter_fixed(orc_handle h, const double* coords, int64_t* physical,
       gf[i] = 0;
     }
     for (const auto& du : o.dunits) {
-      const double ox = coords[2 * (size_t)du.unit], oy = coords[2 * (size_t)du.unit + 1];
+      const float ox = (float)coords[2 * (size_t)du.unit], oy = (float)coords[2 * (size_t)du.unit + 1];
       for (const auto& m : du.members)
-        if (m.field == f) deposit_fixed(gp, o.Wb, o.Hb, o.to_bin_x(ox + m.dx), o.to_bin_y(oy + m.dy), (float)m.charge);
+        if (m.field == f) {
+          const float px = ox + (float)m.dx, py = oy + (float)m.dy;
+          deposit_fixed(gp, mapx, mapy, px, py, (float)m.charge);
+        }
     }
     for (size_t i = 0; i < o.fillers.size(); ++i) {
       if (o.fillers[i].field != f) continue;
       const size_t c = 2 * ((size_t)o.U + i);
-      deposit_fixed(gf, o.Wb, o.Hb, o.to_bin_x(coords[c]), o.to_bin_y(coords[c + 1]), (float)o.fillers[i].charge);
+      deposit_fixed(gf, mapx, mapy, (float)coords[c], (float)coords[c + 1], (float)o.fillers[i].charge);
     }
     int64_t ov = 0;
     uint64_t cnt = 0;

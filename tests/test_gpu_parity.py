@@ -55,11 +55,13 @@ CASES = {
 
 
 def positions(o, kind, seed=0):
+    """Identical inputs for both sides: the device holds FP32 coordinates, so
+    the coordinates are made FP32-representable before the oracle sees them."""
     c, lo, hi = o.initial()
-    if kind == "initial":
-        return c
-    rng = np.random.default_rng(seed)
-    return lo + (hi - lo) * rng.random(c.size)
+    if kind != "initial":
+        rng = np.random.default_rng(seed)
+        c = lo + (hi - lo) * rng.random(c.size)
+    return c.astype(np.float32).astype(np.float64)
 
 
 @pytest.fixture(scope="module", params=sorted(CASES))

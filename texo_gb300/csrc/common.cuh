@@ -1,4 +1,11 @@
 // common.cuh — shared device layout and arithmetic of the placement engine.
+//
+// Precision plan (GB300 runs FP64 at a small fraction of its FP32 rate):
+// every per-object, per-pin and per-bin operation is FP32 or integer; FP64
+// appears only in per-block reduction partials and in the scalar controller.
+// Positions are FP32. The B-spline offset c - round(c) of an FP32 coordinate
+// is exact in FP32, the density is accumulated in int64 2^-32 fixed point,
+// and the Poisson GEMMs accumulate with chunked compensation.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -10,6 +17,7 @@ constexpr int kMaxFields = 4;
 constexpr float kFixF = 4294967296.0f;   // density fixed point: 2^32 per unit charge
 constexpr double kFix = 4294967296.0;
 constexpr double kInvFix = 1.0 / 4294967296.0;
+constexpr float kInvFixF = 1.0f / 4294967296.0f;
 constexpr int kMaxClasses = 6;           // WA degree classes
 
 // Reduction slots (per-block partials, reduced in a fixed order).
@@ -26,23 +34,10 @@ enum Slot {
 };
 constexpr int kMaxPartials = 2048;       // partials per slot
 
-// Integer counters (exact; order-independent atomics).
-enum Counter {
-  CNT_GRID_SUM = 0,                      // + field: sum of all density taps (int64)
-  CNT_OVERFLOW = CNT_GRID_SUM + kMaxFields,   // + field: sum max(phys,0) (int64)
-  CNT_OVER_BINS = CNT_OVERFLOW + kMaxFields,  // + field
-  CNT_DIFF = CNT_OVER_BINS + kMaxFields,      // coordinates that differ
-  CNT_BAD_GRAD,                          // first non-finite gradient coordinate (min)
-  CNT_KKT,                               // max KKT component (double bits)
-  CNT_CHANGE,                            // max |delta| (double bits)
-  CNT_PMIN, CNT_PMAX,                    // preconditioner range (double bits)
-  kCounters
-};
-
 struct Grid {
   int W, H;          // tile grid
   int Wb, Hb;        // density (bin) grid
-  double sx, sy;     // bins per tile
+  float sx, sy;      // bins per tile
   int identity;      // 1 when the bin grid is the tile grid
 };
 
@@ -50,9 +45,11 @@ struct Grid {
 struct Dev {
   int U, F, nobj, K, Mm, B;
   Grid g;
+  const float2* binmap_x;    // [W] bin coordinate of each tile centre as hi+lo floats
+  const float2* binmap_y;    // [H]
   // density members (flattened) and fillers
   const int* mem_unit;
-  const double2* mem_off;
+  const float2* mem_off;
   const float* mem_q;
   const int* mem_field;
   const int* unit_mem_ptr;   // [U+1]
@@ -64,7 +61,7 @@ struct Dev {
   int class_group[kMaxClasses];
   const int* net_ptr;        // [E+1]
   const int* pin_unit;       // [P] -1 for fixed cells
-  const double2* pin_base;   // [P] fixed coordinate or cell offset
+  const float2* pin_base;    // [P] fixed coordinate or cell offset
   const float* net_w;        // [E]
   int n_hpwl_nets;           // the first nets are the baseline hypernets
   // grids
@@ -83,41 +80,57 @@ struct Dev {
   unsigned long long* wa_fix;  // [2U] WA gradient, 2^-32 fixed point
   float2* graw;              // [K][nobj] raw per-field density gradient
   // optimizer
-  const double2* lo;
-  const double2* hi;
-  double* P;                 // [nobj] preconditioner
-  const double* pre_static;  // [nobj]
-  const double* pre_q;       // [K][nobj]
-  // reductions
-  double* partials;          // [kSlots][kMaxPartials]
-  unsigned long long* counters;  // [kCounters]
-  double* scal;              // scalars written by finalize kernels
+  const float2* lo;
+  const float2* hi;
+  float* P;                  // [nobj] preconditioner
+  const float* pre_static;   // [nobj]
+  const float* pre_q;        // [K][nobj]
 };
 
-// ---- B-spline stencil, device arithmetic (bit-exact with the CPU restatement)
-__device__ __forceinline__ double to_bin(double s, double scale, int identity) {
-  return identity ? s : __dsub_rn(__dmul_rn(__dadd_rn(s, 0.5), scale), 0.5);
-}
-
+// ---- B-spline stencil (bit-exact with the oracle's fixed-point restatement)
 struct AxisTaps {
   int idx[3];
   float w[3];
   float o;
 };
 
-// quadratic_bspline_axis (electrostatic_placement.rs:950-976) with the offset
-// and weights in FP32: c is clamped, the centre is min(floor(c+1/2), n-1) and
-// out-of-range taps fold onto the edge.
-__device__ __forceinline__ AxisTaps axis_taps(int n, double c) {
+// quadratic_bspline_axis (electrostatic_placement.rs:950-976) for an FP32
+// coordinate: clamp to [0, n-1], centre min(floor(c + 1/2), n-1), offset
+// o = c - centre (exact in FP32), weights (1/2(1/2-o)^2, 3/4-o^2,
+// 1/2(1/2+o)^2), out-of-range taps folded onto the edge. For a bin grid that
+// differs from the tile grid the bin coordinate (s + 1/2) * scale - 1/2 is
+// formed from the tile's tabulated FP64 value split into hi + lo floats plus
+// the sub-tile fraction times scale, so o keeps ~1e-7 absolute accuracy.
+__device__ __forceinline__ AxisTaps axis_taps(int n, float s, const float2* __restrict__ map, float scale,
+                                              int identity, int tiles) {
   AxisTaps t;
-  const double maximum = (double)(n - 1);
-  // NaN compares false and lands on 0, so every index stays inside the grid.
-  c = c > 0.0 ? c : 0.0;
-  c = c < maximum ? c : maximum;
-  const double cc = fmin(floor(__dadd_rn(c, 0.5)), maximum);
-  int center = (int)cc;
-  center = center < 0 ? 0 : (center > n - 1 ? n - 1 : center);
-  const float o = __double2float_rn(__dsub_rn(c, cc));
+  const float maximum = (float)(n - 1);
+  float hi, lo;
+  if (identity) {
+    hi = s;
+    lo = 0.f;
+  } else {
+    float ts = rintf(s);
+    ts = ts > 0.f ? ts : 0.f;                        // NaN lands on tile 0
+    ts = ts < (float)(tiles - 1) ? ts : (float)(tiles - 1);
+    const float2 b = map[(int)ts];
+    hi = b.x;
+    lo = __fadd_rn(b.y, __fmul_rn(__fsub_rn(s, ts), scale));
+  }
+  const float c = __fadd_rn(hi, lo);
+  int center;
+  float o;
+  if (!(c > 0.f)) {          // also catches NaN
+    center = 0;
+    o = 0.f;
+  } else if (c >= maximum) {
+    center = n - 1;
+    o = 0.f;
+  } else {
+    const float cc = fminf(floorf(__fadd_rn(c, 0.5f)), maximum);
+    center = (int)cc;
+    o = __fadd_rn(__fsub_rn(hi, cc), lo);
+  }
   const float a = __fsub_rn(0.5f, o), b = __fadd_rn(0.5f, o);
   t.idx[0] = center == 0 ? 0 : center - 1;
   t.idx[1] = center;
@@ -131,10 +144,6 @@ __device__ __forceinline__ AxisTaps axis_taps(int n, double c) {
 
 __device__ __forceinline__ long long tap_fixed(float q, float wx, float wy) {
   return __float2ll_rn(__fmul_rn(__fmul_rn(__fmul_rn(q, wx), wy), kFixF));
-}
-
-__device__ __forceinline__ unsigned long long dbits(double v) {
-  return (unsigned long long)__double_as_longlong(v);
 }
 
 // ---- block reductions (fixed order within a block) --------------------------

@@ -55,6 +55,14 @@ int32_t Instance::alloc(void** p, size_t n) {
 }
 
 namespace {
+// Host FP64 coordinates -> device FP32 optimizer buffer.
+int32_t upload_coords(Instance& I, float2* dst, const double* src, size_t nobj) {
+  std::vector<float> tmp(2 * nobj);
+  for (size_t i = 0; i < 2 * nobj; ++i) tmp[i] = (float)src[i];
+  CU(cudaMemcpyAsync(dst, tmp.data(), nobj * sizeof(float2), cudaMemcpyHostToDevice, I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  return TEXO_GP_OK;
+}
 template <typename T>
 int32_t upload_vec(Instance& I, T** dst, const std::vector<T>& v) {
   TRY(I.alloc((void**)dst, v.size() * sizeof(T)));
@@ -97,9 +105,25 @@ int32_t Instance::upload() {
   D.K = (int)K;
   D.Mm = (int)h.Mm;
   D.B = (int)B;
-  D.g = Grid{(int)h.W, (int)h.H, (int)h.Wb, (int)h.Hb, h.sx, h.sy, h.identity ? 1 : 0};
+  D.g = Grid{(int)h.W, (int)h.H, (int)h.Wb, (int)h.Hb, (float)h.sx, (float)h.sy, h.identity ? 1 : 0};
+  // bin coordinate of every tile centre, (t + 1/2) * scale - 1/2 in FP64,
+  // split into hi + lo floats
+  auto binmap = [](uint32_t tiles, uint32_t bins) {
+    std::vector<float> v(2 * (size_t)tiles);
+    const double scale = (double)bins / (double)tiles;
+    for (uint32_t t = 0; t < tiles; ++t) {
+      const double b = ((double)t + 0.5) * scale - 0.5;
+      const float hi = (float)b;
+      v[2 * (size_t)t] = hi;
+      v[2 * (size_t)t + 1] = (float)(b - (double)hi);
+    }
+    return v;
+  };
+  TRY(upload_vec(*this, (float**)&D.binmap_x, binmap(h.W, h.Wb)));
+  TRY(upload_vec(*this, (float**)&D.binmap_y, binmap(h.H, h.Hb)));
   TRY(upload_vec(*this, (int**)&D.mem_unit, h.mem_unit));
-  TRY(upload_vec(*this, (double**)&D.mem_off, h.mem_off));
+  std::vector<float> moff(h.mem_off.begin(), h.mem_off.end());
+  TRY(upload_vec(*this, (float**)&D.mem_off, moff));
   TRY(upload_vec(*this, (float**)&D.mem_q, h.mem_q));
   TRY(upload_vec(*this, (int**)&D.mem_field, h.mem_field));
   TRY(upload_vec(*this, (int**)&D.unit_mem_ptr, h.unit_mem_ptr));
@@ -112,7 +136,8 @@ int32_t Instance::upload() {
   D.n_hpwl_nets = h.n_hpwl_nets;
   TRY(upload_vec(*this, (int**)&D.net_ptr, h.net_ptr));
   TRY(upload_vec(*this, (int**)&D.pin_unit, h.pin_unit));
-  TRY(upload_vec(*this, (double**)&D.pin_base, h.pin_base));
+  std::vector<float> pbase(h.pin_base.begin(), h.pin_base.end());
+  TRY(upload_vec(*this, (float**)&D.pin_base, pbase));
   TRY(upload_vec(*this, (float**)&D.net_w, h.net_w));
   // grids
   TRY(zeros(*this, &D.phys, K * B));
@@ -159,12 +184,13 @@ int32_t Instance::upload() {
   TRY(zeros(*this, &D.wa_fix, 2 * (size_t)h.U));
   TRY(zeros(*this, &D.graw, std::max<size_t>(K, 1) * nobj));
   // optimizer
-  std::vector<double> lo(h.lo), hi(h.hi);
-  TRY(upload_vec(*this, (double**)&D.lo, lo));
-  TRY(upload_vec(*this, (double**)&D.hi, hi));
+  std::vector<float> lo(h.lo.begin(), h.lo.end()), hi(h.hi.begin(), h.hi.end());
+  TRY(upload_vec(*this, (float**)&D.lo, lo));
+  TRY(upload_vec(*this, (float**)&D.hi, hi));
   TRY(zeros(*this, &D.P, nobj));
-  TRY(upload_vec(*this, (double**)&D.pre_static, h.pre_static));
-  TRY(upload_vec(*this, (double**)&D.pre_q, h.pre_q));
+  std::vector<float> pst(h.pre_static.begin(), h.pre_static.end()), pq(h.pre_q.begin(), h.pre_q.end());
+  TRY(upload_vec(*this, (float**)&D.pre_static, pst));
+  TRY(upload_vec(*this, (float**)&D.pre_q, pq));
   TRY(zeros(*this, &bufX, nobj));
   TRY(zeros(*this, &bufXp, nobj));
   TRY(zeros(*this, &bufY, nobj));
@@ -191,7 +217,9 @@ int32_t Instance::upload() {
     h_scal[SC_LAMBDA + f] = 0.0;
   }
   CU(cudaMemcpyAsync(r.scal, h_scal, kScalars * sizeof(double), cudaMemcpyHostToDevice, stream));
-  CU(cudaMemcpyAsync(bufX, h.init.data(), nobj * sizeof(double2), cudaMemcpyHostToDevice, stream));
+  std::vector<float> init32(h.init.begin(), h.init.end());
+  CU(cudaMemcpyAsync(bufX, init32.data(), nobj * sizeof(float2), cudaMemcpyHostToDevice, stream));
+  CU(cudaStreamSynchronize(stream));
   CU(cudaStreamSynchronize(stream));
   return TEXO_GP_OK;
 }
@@ -269,7 +297,7 @@ struct Controller {
   // combined_objective). With reuse, the density side of `pos` is the one
   // already on the device (same coordinates), and only WA and the
   // combination are recomputed.
-  void enqueue_eval(const double2* pos, double2* g, double gam, bool reuse) {
+  void enqueue_eval(const float2* pos, float2* g, double gam, bool reuse) {
     const Dev& D = I.d;
     cudaStream_t s = I.stream;
     const int nvb = I.nvb;
@@ -305,7 +333,7 @@ struct Controller {
     }
     e.bad = si[SI_BAD];
   }
-  int32_t evaluate(const double2* pos, double2* g, double gam, bool reuse, EvalRec& e) {
+  int32_t evaluate(const float2* pos, float2* g, double gam, bool reuse, EvalRec& e) {
     enqueue_eval(pos, g, gam, reuse);
     TRY(sync_read());
     read_eval(e);
@@ -429,8 +457,8 @@ struct Controller {
         TRY(sync_read());
         y_is_origin = I.h_iscal[SI_DIFF] == 0;
       }
-      const double2* ybuf = y_is_origin ? I.bufX : I.bufY;
-      const double2* gy = y_is_origin ? I.gX : I.gY;
+      const float2* ybuf = y_is_origin ? I.bufX : I.bufY;
+      const float2* gy = y_is_origin ? I.gX : I.gY;
       double f_y = eo.value;
       if (!y_is_origin) {
         enqueue_eval(I.bufY, I.gY, gam, false);
@@ -453,7 +481,7 @@ struct Controller {
           restart = true;
           continue;
         }
-        CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(float2), cudaMemcpyDeviceToDevice, s));
         a = 1.0;
         stationary = true;
         payload = eo;
@@ -474,7 +502,7 @@ struct Controller {
           if (!std::isfinite(tL)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
           continue;
         }
-        launch_candidate(D, I.r, ybuf, gy, tL, I.bufC, nvb, s);
+        launch_candidate(D, I.r, ybuf, gy, (float)(1.0 / tL), I.bufC, nvb, s);
         launch_finalize(D, I.r, nvb, FIN_CAND, s);
         // The candidate is evaluated speculatively in the same submission;
         // it is discarded when the candidate equals y.
@@ -498,7 +526,7 @@ struct Controller {
             restart_step = true;
             break;
           }
-          CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+          CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)D.nobj * sizeof(float2), cudaMemcpyDeviceToDevice, s));
           a = 1.0;
           has_L = true;
           L = tL;
@@ -549,7 +577,7 @@ struct Controller {
   }
 
   int32_t save_best() {
-    CU(cudaMemcpyAsync(I.best, I.bufX, (size_t)I.m.U * sizeof(double2), cudaMemcpyDeviceToDevice, I.stream));
+    CU(cudaMemcpyAsync(I.best, I.bufX, (size_t)I.m.U * sizeof(float2), cudaMemcpyDeviceToDevice, I.stream));
     return TEXO_GP_OK;
   }
 
@@ -577,7 +605,7 @@ struct Controller {
       TRY(validate_initial(initial));
       for (uint32_t f = 0; f < K; ++f) e0[f] = std::fmax(initial.energy[f], 1.0);
       TRY(validate_fields(initial));
-      CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)I.d.nobj * sizeof(double2), cudaMemcpyDeviceToDevice, I.stream));
+      CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)I.d.nobj * sizeof(float2), cudaMemcpyDeviceToDevice, I.stream));
       TRY(save_best());
       excess(initial, best_max, best_tot);
       density_at_x = true;
@@ -679,18 +707,17 @@ int32_t handle_targets(texo_gp_handle h, uint32_t* out, double* coords, texo_gp_
   Instance& I = *h->inst;
   Controller& C = *h->ctl;
   const size_t nobj = (size_t)I.d.nobj;
-  std::vector<double> best(2 * (size_t)I.m.U);
-  if (I.m.has_density) {
-    CU(cudaMemcpyAsync(best.data(), I.best, best.size() * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
-  } else {
-    std::copy(I.m.init.begin(), I.m.init.begin() + best.size(), best.begin());
-  }
-  std::vector<double> cur(2 * nobj);
-  CU(cudaMemcpyAsync(cur.data(), I.bufX, cur.size() * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  std::vector<float> best32(2 * (size_t)I.m.U), cur32(2 * nobj);
+  std::vector<double> best(2 * (size_t)I.m.U), cur(2 * nobj);
+  if (I.m.has_density)
+    CU(cudaMemcpyAsync(best32.data(), I.best, best32.size() * sizeof(float), cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaMemcpyAsync(cur32.data(), I.bufX, cur32.size() * sizeof(float), cudaMemcpyDeviceToHost, I.stream));
   launch_hpwl(I.d, I.r, I.bufX, I.nvb, I.stream);
   launch_finalize(I.d, I.r, I.nvb, FIN_HPWL, I.stream);
   CU(cudaMemcpyAsync(I.h_scal + SC_HPWL, I.r.scal + SC_HPWL, sizeof(double), cudaMemcpyDeviceToHost, I.stream));
   CU(cudaStreamSynchronize(I.stream));
+  for (size_t i = 0; i < best.size(); ++i) best[i] = I.m.has_density ? (double)best32[i] : I.m.init[i];
+  for (size_t i = 0; i < cur.size(); ++i) cur[i] = cur32[i];
   if (out)
     for (uint32_t u = 0; u < I.m.U; ++u) {
       out[2 * (size_t)u] = round_coord(best[2 * (size_t)u], I.m.W);
@@ -856,7 +883,7 @@ int32_t texo_gp_evaluate(texo_gp_handle h, const double* coordinates, double gam
   const size_t nobj = (size_t)I.d.nobj, B = I.m.bins(), K = I.m.K;
   for (size_t i = 0; i < 2 * nobj; ++i)
     if (!std::isfinite(coordinates[i])) return TEXO_GP_ERR_NONFINITE_UNIT_COORDINATE;
-  CU(cudaMemcpyAsync(I.bufY, coordinates, nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  TRY(upload_coords(I, I.bufY, coordinates, nobj));
   EvalRec e;
   TRY(C.evaluate(I.bufY, I.gY, gamma, false, e));
   C.density_at_x = false;
@@ -915,7 +942,7 @@ int32_t texo_gp_scatter(texo_gp_handle h, const double* coordinates, int64_t* ph
   std::lock_guard<std::mutex> lk(h->mu);
   Instance& I = *h->inst;
   const size_t nobj = (size_t)I.d.nobj, n = (size_t)I.m.K * I.m.bins();
-  CU(cudaMemcpyAsync(I.bufY, coordinates, nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  TRY(upload_coords(I, I.bufY, coordinates, nobj));
   launch_init(I.d, true, false, I.nvb, I.stream);
   launch_scatter(I.d, I.r, I.bufY, I.nvb, I.stream);
   if (physical) CU(cudaMemcpyAsync(physical, I.d.phys, n * 8, cudaMemcpyDeviceToHost, I.stream));
@@ -995,7 +1022,7 @@ int32_t texo_gp_reset(texo_gp_handle h) {
   std::lock_guard<std::mutex> lk(h->mu);
   Instance& I = *h->inst;
   h->ctl = std::make_unique<Controller>(I);
-  CU(cudaMemcpyAsync(I.bufX, I.m.init.data(), (size_t)I.d.nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  TRY(upload_coords(I, I.bufX, I.m.init.data(), (size_t)I.d.nobj));
   CU(cudaMemsetAsync(I.prev_targets, 0, 2 * (size_t)I.m.U * 4, I.stream));
   CU(cudaStreamSynchronize(I.stream));
   return TEXO_GP_OK;
@@ -1005,7 +1032,7 @@ int32_t texo_gp_hpwl(texo_gp_handle h, const double* coordinates, double* hpwl) 
   if (!h || !coordinates || !hpwl) return TEXO_GP_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(h->mu);
   Instance& I = *h->inst;
-  CU(cudaMemcpyAsync(I.bufY, coordinates, (size_t)I.d.nobj * sizeof(double2), cudaMemcpyHostToDevice, I.stream));
+  TRY(upload_coords(I, I.bufY, coordinates, (size_t)I.d.nobj));
   launch_hpwl(I.d, I.r, I.bufY, I.nvb, I.stream);
   launch_finalize(I.d, I.r, I.nvb, FIN_HPWL, I.stream);
   CU(cudaMemcpyAsync(I.h_scal + SC_HPWL, I.r.scal + SC_HPWL, sizeof(double), cudaMemcpyDeviceToHost, I.stream));

@@ -70,9 +70,9 @@ struct Instance {
   std::vector<void*> allocations;
   Dev d{};
   Reduce r{};
-  double2 *bufX = nullptr, *bufXp = nullptr, *bufY = nullptr, *bufC = nullptr;
-  double2 *gX = nullptr, *gY = nullptr, *gC = nullptr;
-  double2* best = nullptr;                       // best checkpoint coordinates [U]
+  float2 *bufX = nullptr, *bufXp = nullptr, *bufY = nullptr, *bufC = nullptr;
+  float2 *gX = nullptr, *gY = nullptr, *gC = nullptr;
+  float2* best = nullptr;                        // best checkpoint coordinates [U]
   uint32_t* prev_targets = nullptr;              // [2U]
   unsigned long long* mismatch = nullptr;
   double* h_scal = nullptr;                      // pinned host mirror

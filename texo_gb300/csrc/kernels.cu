@@ -6,11 +6,11 @@ namespace tgp {
 __global__ void __launch_bounds__(kThreads) k_init(Dev d, bool grids, bool wa) {
   stage_init(d, blockIdx.x, gridDim.x, grids, wa);
 }
-__global__ void __launch_bounds__(kThreads) k_scatter(Dev d, Partials p, const double2* pos) {
+__global__ void __launch_bounds__(kThreads) k_scatter(Dev d, Partials p, const float2* pos) {
   __shared__ Shared sh;
   stage_scatter(d, pos, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_wa(Dev d, Partials p, const double2* pos, double gamma) {
+__global__ void __launch_bounds__(kThreads) k_wa(Dev d, Partials p, const float2* pos, double gamma) {
   __shared__ Shared sh;
   stage_wa(d, pos, gamma, p, blockIdx.x, gridDim.x, sh);
 }
@@ -23,26 +23,26 @@ __global__ void __launch_bounds__(kThreads) k_dct(Dev d, Partials p, int step, b
   __shared__ Shared sh;
   stage_dct(d, step, large, p, blockIdx.x, gridDim.x, sm, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_gather(Dev d, Partials p, const double2* pos) {
+__global__ void __launch_bounds__(kThreads) k_gather(Dev d, Partials p, const float2* pos) {
   __shared__ Shared sh;
   stage_gather(d, pos, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_combine(Dev d, Partials p, const double* coef, double2* gout) {
+__global__ void __launch_bounds__(kThreads) k_combine(Dev d, Partials p, const double* coef, float2* gout) {
   __shared__ Shared sh;
   stage_combine(d, coef, gout, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_extrapolate(Dev d, Partials p, const double2* x, const double2* xp,
-                                                         double e, double2* y) {
+__global__ void __launch_bounds__(kThreads) k_extrapolate(Dev d, Partials p, const float2* x, const float2* xp,
+                                                         float e, float2* y) {
   __shared__ Shared sh;
   stage_extrapolate(d, x, xp, e, y, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_candidate(Dev d, Partials p, const double2* y, const double2* gy,
-                                                       double L, double2* c) {
+__global__ void __launch_bounds__(kThreads) k_candidate(Dev d, Partials p, const float2* y, const float2* gy,
+                                                       float invL, float2* c) {
   __shared__ Shared sh;
-  stage_candidate(d, y, gy, L, c, p, blockIdx.x, gridDim.x, sh);
+  stage_candidate(d, y, gy, invL, c, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_kkt(Dev d, Partials p, const double2* x, const double2* g,
-                                                 const double2* ref) {
+__global__ void __launch_bounds__(kThreads) k_kkt(Dev d, Partials p, const float2* x, const float2* g,
+                                                 const float2* ref) {
   __shared__ Shared sh;
   stage_kkt(d, x, g, ref, p, blockIdx.x, gridDim.x, sh);
 }
@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kThreads) k_precond(Dev d, Partials p, const d
   __shared__ Shared sh;
   stage_precond(d, lambda, p, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_hpwl(Dev d, Partials p, const double2* pos) {
+__global__ void __launch_bounds__(kThreads) k_hpwl(Dev d, Partials p, const float2* pos) {
   __shared__ Shared sh;
   stage_hpwl(d, pos, p, blockIdx.x, gridDim.x, sh);
 }
@@ -152,11 +152,11 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Dev d, Reduce r, int nvb,
 
 // rounded_targets_from_coordinates (eplace.rs:954-971) compared with the
 // previous stationary targets (stationary_target_is_fixed, :973-985).
-__global__ void k_round_compare(Dev d, const double2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch) {
+__global__ void k_round_compare(Dev d, const float2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < d.U; u += gridDim.x * blockDim.x) {
-    const double2 a = x[u];
-    const double rx = fmin(fmax(round(a.x), 0.0), (double)(W - 1));
-    const double ry = fmin(fmax(round(a.y), 0.0), (double)(H - 1));
+    const float2 a = x[u];
+    const float rx = fminf(fmaxf(roundf(a.x), 0.f), (float)(W - 1));
+    const float ry = fminf(fmaxf(roundf(a.y), 0.f), (float)(H - 1));
     const uint32_t tx = (uint32_t)rx, ty = (uint32_t)ry;
     if (prev[2 * u] != tx || prev[2 * u + 1] != ty) atomicAdd(mismatch, 1ull);
     prev[2 * u] = tx;
@@ -176,11 +176,11 @@ void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s) {
   COUNT;
   k_init<<<nvb, kThreads, 0, s>>>(d, grids, wa);
 }
-void launch_scatter(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+void launch_scatter(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s) {
   COUNT;
   k_scatter<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
 }
-void launch_wa(const Dev& d, const Reduce& r, const double2* pos, double gamma, int nvb, cudaStream_t s) {
+void launch_wa(const Dev& d, const Reduce& r, const float2* pos, double gamma, int nvb, cudaStream_t s) {
   COUNT;
   k_wa<<<nvb, kThreads, 0, s>>>(d, r.p, pos, gamma);
 }
@@ -192,25 +192,25 @@ void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s
   COUNT;
   k_dct<<<nvb, kThreads, 0, s>>>(d, r.p, step, use_large_tiles(d));
 }
-void launch_gather(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+void launch_gather(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s) {
   COUNT;
   k_gather<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
 }
-void launch_combine(const Dev& d, const Reduce& r, double2* gout, int nvb, cudaStream_t s) {
+void launch_combine(const Dev& d, const Reduce& r, float2* gout, int nvb, cudaStream_t s) {
   COUNT;
   k_combine<<<nvb, kThreads, 0, s>>>(d, r.p, r.scal + SC_COEF, gout);
 }
-void launch_extrapolate(const Dev& d, const Reduce& r, const double2* x, const double2* xp, double e, double2* y,
+void launch_extrapolate(const Dev& d, const Reduce& r, const float2* x, const float2* xp, float e, float2* y,
                         int nvb, cudaStream_t s) {
   COUNT;
   k_extrapolate<<<nvb, kThreads, 0, s>>>(d, r.p, x, xp, e, y);
 }
-void launch_candidate(const Dev& d, const Reduce& r, const double2* y, const double2* gy, double L, double2* c,
+void launch_candidate(const Dev& d, const Reduce& r, const float2* y, const float2* gy, float invL, float2* c,
                       int nvb, cudaStream_t s) {
   COUNT;
-  k_candidate<<<nvb, kThreads, 0, s>>>(d, r.p, y, gy, L, c);
+  k_candidate<<<nvb, kThreads, 0, s>>>(d, r.p, y, gy, invL, c);
 }
-void launch_kkt(const Dev& d, const Reduce& r, const double2* x, const double2* g, const double2* ref, int nvb,
+void launch_kkt(const Dev& d, const Reduce& r, const float2* x, const float2* g, const float2* ref, int nvb,
                 cudaStream_t s) {
   COUNT;
   k_kkt<<<nvb, kThreads, 0, s>>>(d, r.p, x, g, ref);
@@ -219,7 +219,7 @@ void launch_precond(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
   COUNT;
   k_precond<<<nvb, kThreads, 0, s>>>(d, r.p, r.scal + SC_LAMBDA);
 }
-void launch_hpwl(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s) {
+void launch_hpwl(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s) {
   COUNT;
   k_hpwl<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
 }
@@ -227,7 +227,7 @@ void launch_finalize(const Dev& d, const Reduce& r, int nvb, int mask, cudaStrea
   COUNT;
   k_finalize<<<1, kThreads, 0, s>>>(d, r, nvb, mask);
 }
-void launch_round_compare(const Dev& d, const double2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch,
+void launch_round_compare(const Dev& d, const float2* x, uint32_t* prev, int W, int H, unsigned long long* mismatch,
                           int nvb, cudaStream_t s) {
   COUNT;
   k_round_compare<<<nvb, kThreads, 0, s>>>(d, x, prev, W, H, mismatch);

@@ -60,22 +60,22 @@ struct Reduce {
 
 unsigned long long launches_issued();
 void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s);
-void launch_scatter(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
-void launch_wa(const Dev& d, const Reduce& r, const double2* pos, double gamma, int nvb, cudaStream_t s);
+void launch_scatter(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s);
+void launch_wa(const Dev& d, const Reduce& r, const float2* pos, double gamma, int nvb, cudaStream_t s);
 void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s);
-void launch_gather(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
-void launch_combine(const Dev& d, const Reduce& r, double2* gout, int nvb, cudaStream_t s);
-void launch_extrapolate(const Dev& d, const Reduce& r, const double2* x, const double2* xp, double e, double2* y,
+void launch_gather(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s);
+void launch_combine(const Dev& d, const Reduce& r, float2* gout, int nvb, cudaStream_t s);
+void launch_extrapolate(const Dev& d, const Reduce& r, const float2* x, const float2* xp, float e, float2* y,
                         int nvb, cudaStream_t s);
-void launch_candidate(const Dev& d, const Reduce& r, const double2* y, const double2* gy, double L, double2* c,
+void launch_candidate(const Dev& d, const Reduce& r, const float2* y, const float2* gy, float invL, float2* c,
                       int nvb, cudaStream_t s);
-void launch_kkt(const Dev& d, const Reduce& r, const double2* x, const double2* g, const double2* ref, int nvb,
+void launch_kkt(const Dev& d, const Reduce& r, const float2* x, const float2* g, const float2* ref, int nvb,
                 cudaStream_t s);
 void launch_precond(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
-void launch_hpwl(const Dev& d, const Reduce& r, const double2* pos, int nvb, cudaStream_t s);
+void launch_hpwl(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s);
 void launch_finalize(const Dev& d, const Reduce& r, int nvb, int mask, cudaStream_t s);
-void launch_round_compare(const Dev& d, const double2* x, uint32_t* prev_targets, int W, int H,
+void launch_round_compare(const Dev& d, const float2* x, uint32_t* prev_targets, int W, int H,
                           unsigned long long* mismatch, int nvb, cudaStream_t s);
 
 }  // namespace tgp

@@ -85,6 +85,13 @@ struct Shared {
   long long l[kThreads / 32];
 };
 
+__device__ __forceinline__ AxisTaps taps_x(const Dev& d, float s) {
+  return axis_taps(d.g.Wb, s, d.binmap_x, d.g.sx, d.g.identity, d.g.W);
+}
+__device__ __forceinline__ AxisTaps taps_y(const Dev& d, float s) {
+  return axis_taps(d.g.Hb, s, d.binmap_y, d.g.sy, d.g.identity, d.g.H);
+}
+
 // ---------------------------------------------------------------------------
 // S1: reset the accumulation grids.
 // ---------------------------------------------------------------------------
@@ -108,38 +115,37 @@ static __device__ void stage_init(const Dev& d, int vb, int nvb, bool grids, boo
 // exact in any order. The per-field tap total is a partial for the mean.
 // (deposit_quadratic_bspline + the field loop, electrostatic_placement.rs:296-332)
 // ---------------------------------------------------------------------------
-static __device__ void stage_scatter(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb,
-                              Shared& sh) {
+static __device__ void stage_scatter(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+                                     Shared& sh) {
   long long tot[kMaxFields];
 #pragma unroll
   for (int f = 0; f < kMaxFields; ++f) tot[f] = 0;
   const int stride = nvb * blockDim.x;
   const int items = d.Mm + d.F;
   for (int i = vb * blockDim.x + threadIdx.x; i < items; i += stride) {
-    double sxp, syp;
-    float q;
+    float sxp, syp, q;
     int f;
     unsigned long long* grid;
     if (i < d.Mm) {
       const int u = d.mem_unit[i];
-      const double2 o = d.mem_off[i];
-      const double2 pu = pos[u];
-      sxp = __dadd_rn(pu.x, o.x);
-      syp = __dadd_rn(pu.y, o.y);
+      const float2 o = d.mem_off[i];
+      const float2 pu = pos[u];
+      sxp = __fadd_rn(pu.x, o.x);
+      syp = __fadd_rn(pu.y, o.y);
       q = d.mem_q[i];
       f = d.mem_field[i];
       grid = (unsigned long long*)(d.phys + (size_t)f * d.B);
     } else {
       const int j = i - d.Mm;
-      const double2 pf = pos[d.U + j];
+      const float2 pf = pos[d.U + j];
       sxp = pf.x;
       syp = pf.y;
       q = d.fil_q[j];
       f = d.fil_field[j];
       grid = (unsigned long long*)(d.fill + (size_t)f * d.B);
     }
-    const AxisTaps ax = axis_taps(d.g.Wb, to_bin(sxp, d.g.sx, d.g.identity));
-    const AxisTaps ay = axis_taps(d.g.Hb, to_bin(syp, d.g.sy, d.g.identity));
+    const AxisTaps ax = taps_x(d, sxp);
+    const AxisTaps ay = taps_y(d, syp);
     long long s = 0;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -158,18 +164,27 @@ static __device__ void stage_scatter(const Dev& d, const double2* __restrict__ p
 
 // ---------------------------------------------------------------------------
 // S3: weighted-average wirelength (analytical_placement.rs:576-703).
-// A group of G lanes takes one net: hard max/min by shuffles, FP32 exp of the
-// FP64 deltas, soft means, per-pin derivative. Unit gradients accumulate as
-// int64 2^-32 fixed point, so the result is order-independent.
+// A group of G lanes takes one net: hard max/min by shuffles, exponential
+// weights of the deltas to the extrema, soft means, per-pin derivative.
+// Unit gradients accumulate as int64 2^-32 fixed point (order-independent).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* __restrict__ pos, int k) {
+  const int u = d.pin_unit[k];
+  const float2 b = d.pin_base[k];
+  if (u < 0) return b;
+  const float2 pu = pos[u];
+  return make_float2(pu.x + b.x, pu.y + b.y);
+}
+
 template <int G>
-__device__ __forceinline__ void wa_class(const Dev& d, const double2* __restrict__ pos, float gamma, float inv_gamma,
-                                         int nb, int ne, int vb, int nvb, double& acc) {
+__device__ __forceinline__ void wa_class(const Dev& d, const float2* __restrict__ pos, float inv_gamma, int nb,
+                                         int ne, int vb, int nvb, double& acc) {
   const int lane = threadIdx.x & (G - 1);
   const int group = (vb * blockDim.x + threadIdx.x) / G;
   const int groups = nvb * blockDim.x / G;
   const unsigned mask = 0xffffffffu;
   const int count = ne - nb;
+  float vacc = 0.f;
   for (int base = 0; base < count; base += groups) {
     const int e = nb + base + group;
     const bool active = base + group < count;
@@ -180,56 +195,35 @@ __device__ __forceinline__ void wa_class(const Dev& d, const double2* __restrict
       p1 = d.net_ptr[e + 1];
       w = d.net_w[e];
     }
-    // pass 1: max / min per axis
-    double mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
+    // pass 1: hard extrema per axis; the first pin is kept for the low-degree case
+    float mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
+    float2 first = make_float2(0.f, 0.f);
     for (int k = p0 + lane; k < p1; k += G) {
-      const int u = d.pin_unit[k];
-      const double2 b = d.pin_base[k];
-      double x, y;
-      if (u < 0) {
-        x = b.x;
-        y = b.y;
-      } else {
-        const double2 pu = pos[u];
-        x = pu.x + b.x;
-        y = pu.y + b.y;
-      }
-      mx = fmax(mx, x);
-      mnx = fmin(mnx, x);
-      my = fmax(my, y);
-      mny = fmin(mny, y);
+      const float2 v = pin_xy(d, pos, k);
+      if (k == p0 + lane) first = v;
+      mx = fmaxf(mx, v.x);
+      mnx = fminf(mnx, v.x);
+      my = fmaxf(my, v.y);
+      mny = fminf(mny, v.y);
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
-      mx = fmax(mx, __shfl_xor_sync(mask, mx, o, G));
-      mnx = fmin(mnx, __shfl_xor_sync(mask, mnx, o, G));
-      my = fmax(my, __shfl_xor_sync(mask, my, o, G));
-      mny = fmin(mny, __shfl_xor_sync(mask, mny, o, G));
+      mx = fmaxf(mx, __shfl_xor_sync(mask, mx, o, G));
+      mnx = fminf(mnx, __shfl_xor_sync(mask, mnx, o, G));
+      my = fmaxf(my, __shfl_xor_sync(mask, my, o, G));
+      mny = fminf(mny, __shfl_xor_sync(mask, mny, o, G));
     }
-    // pass 2: exponential weights and their sums
+    // pass 2: exponential weights (exactly 1 at the extremum) and their sums
     float sw[4] = {0.f, 0.f, 0.f, 0.f}, sd[4] = {0.f, 0.f, 0.f, 0.f};
     for (int k = p0 + lane; k < p1; k += G) {
-      const int u = d.pin_unit[k];
-      const double2 b = d.pin_base[k];
-      double x, y;
-      if (u < 0) {
-        x = b.x;
-        y = b.y;
-      } else {
-        const double2 pu = pos[u];
-        x = pu.x + b.x;
-        y = pu.y + b.y;
-      }
-      const float dxp = (float)(x - mx), dxn = (float)(x - mnx);
-      const float dyp = (float)(y - my), dyn = (float)(y - mny);
-      const float wxp = dxp == 0.f ? 1.f : __expf(dxp * inv_gamma);
-      const float wxn = dxn == 0.f ? 1.f : __expf(-dxn * inv_gamma);
-      const float wyp = dyp == 0.f ? 1.f : __expf(dyp * inv_gamma);
-      const float wyn = dyn == 0.f ? 1.f : __expf(-dyn * inv_gamma);
-      sw[0] += wxp; sd[0] += wxp * dxp;
-      sw[1] += wxn; sd[1] += wxn * dxn;
-      sw[2] += wyp; sd[2] += wyp * dyp;
-      sw[3] += wyn; sd[3] += wyn * dyn;
+      const float2 v = (k == p0 + lane) ? first : pin_xy(d, pos, k);
+      const float dxp = v.x - mx, dxn = v.x - mnx, dyp = v.y - my, dyn = v.y - mny;
+      const float wxp = expf(dxp * inv_gamma), wxn = expf(-dxn * inv_gamma);
+      const float wyp = expf(dyp * inv_gamma), wyn = expf(-dyn * inv_gamma);
+      sw[0] += wxp; sd[0] = fmaf(wxp, dxp, sd[0]);
+      sw[1] += wxn; sd[1] = fmaf(wxn, dxn, sd[1]);
+      sw[2] += wyp; sd[2] = fmaf(wyp, dyp, sd[2]);
+      sw[3] += wyn; sd[3] = fmaf(wyn, dyn, sd[3]);
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1)
@@ -249,15 +243,10 @@ __device__ __forceinline__ void wa_class(const Dev& d, const double2* __restrict
     for (int k = p0 + lane; k < p1; k += G) {
       const int u = d.pin_unit[k];
       if (u < 0) continue;
-      const double2 b = d.pin_base[k];
-      const double2 pu = pos[u];
-      const double x = pu.x + b.x, y = pu.y + b.y;
-      const float dxp = (float)(x - mx), dxn = (float)(x - mnx);
-      const float dyp = (float)(y - my), dyn = (float)(y - mny);
-      const float wxp = dxp == 0.f ? 1.f : __expf(dxp * inv_gamma);
-      const float wxn = dxn == 0.f ? 1.f : __expf(-dxn * inv_gamma);
-      const float wyp = dyp == 0.f ? 1.f : __expf(dyp * inv_gamma);
-      const float wyn = dyn == 0.f ? 1.f : __expf(-dyn * inv_gamma);
+      const float2 v = (k == p0 + lane) ? first : pin_xy(d, pos, k);
+      const float dxp = v.x - mx, dxn = v.x - mnx, dyp = v.y - my, dyn = v.y - mny;
+      const float wxp = expf(dxp * inv_gamma), wxn = expf(-dxn * inv_gamma);
+      const float wyp = expf(dyp * inv_gamma), wyn = expf(-dyn * inv_gamma);
       const float gx = wxp * inv[0] * (1.f + (dxp - mean[0]) * inv_gamma) -
                        wxn * inv[1] * (1.f - (dxn - mean[1]) * inv_gamma);
       const float gy = wyp * inv[2] * (1.f + (dyp - mean[2]) * inv_gamma) -
@@ -265,26 +254,24 @@ __device__ __forceinline__ void wa_class(const Dev& d, const double2* __restrict
       atomicAdd(d.wa_fix + 2 * u, (unsigned long long)__float2ll_rn(w * gx * kFixF));
       atomicAdd(d.wa_fix + 2 * u + 1, (unsigned long long)__float2ll_rn(w * gy * kFixF));
     }
-    if (lane == 0)
-      acc += (double)w * (((mx - mnx) + (double)mean[0] - (double)mean[1]) +
-                          ((my - mny) + (double)mean[2] - (double)mean[3]));
+    if (lane == 0) vacc += w * (((mx - mnx) + mean[0] - mean[1]) + ((my - mny) + mean[2] - mean[3]));
   }
-  (void)gamma;
+  acc += (double)vacc;
 }
 
-static __device__ void stage_wa(const Dev& d, const double2* __restrict__ pos, double gamma, Partials p, int vb, int nvb,
-                         Shared& sh) {
+static __device__ void stage_wa(const Dev& d, const float2* __restrict__ pos, double gamma, Partials p, int vb,
+                                int nvb, Shared& sh) {
   double acc = 0.0;
-  const float g = (float)gamma, ig = (float)(1.0 / gamma);
+  const float ig = (float)(1.0 / gamma);
   for (int c = 0; c < d.n_classes; ++c) {
     const int nb = d.class_begin[c], ne = d.class_begin[c + 1];
     if (ne <= nb) continue;
     switch (d.class_group[c]) {
-      case 2: wa_class<2>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
-      case 4: wa_class<4>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
-      case 8: wa_class<8>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
-      case 16: wa_class<16>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
-      default: wa_class<32>(d, pos, g, ig, nb, ne, vb, nvb, acc); break;
+      case 2: wa_class<2>(d, pos, ig, nb, ne, vb, nvb, acc); break;
+      case 4: wa_class<4>(d, pos, ig, nb, ne, vb, nvb, acc); break;
+      case 8: wa_class<8>(d, pos, ig, nb, ne, vb, nvb, acc); break;
+      case 16: wa_class<16>(d, pos, ig, nb, ne, vb, nvb, acc); break;
+      default: wa_class<32>(d, pos, ig, nb, ne, vb, nvb, acc); break;
     }
   }
   write_partial(acc, pslot(p, SLOT_WA_VALUE), vb, sh.d);
@@ -295,11 +282,11 @@ static __device__ void stage_wa(const Dev& d, const double2* __restrict__ pos, d
 // (the pre-filler positive overflow, electrostatic_placement.rs:317-318).
 // ---------------------------------------------------------------------------
 static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int vb, int nvb, Shared& sh) {
-  __shared__ long long s_mean_sum[kMaxFields];
+  __shared__ long long s_mean[kMaxFields];
   __shared__ long long red[kThreads / 32];
   for (int f = 0; f < d.K; ++f) {
     long long tot = block_reduce_array(islot(p, IS_GRID_SUM + f), nvb_scatter, 0ll, OpAdd(), red);
-    if (threadIdx.x == 0) s_mean_sum[f] = tot - d.capsum[f];
+    if (threadIdx.x == 0) s_mean[f] = (tot - d.capsum[f]) / d.B;   // fixed-point mean (DC mode only)
   }
   __syncthreads();
   long long ov[kMaxFields], cnt[kMaxFields];
@@ -307,7 +294,7 @@ static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int
   for (int f = 0; f < kMaxFields; ++f) ov[f] = cnt[f] = 0;
   const int stride = nvb * blockDim.x;
   for (int f = 0; f < d.K; ++f) {
-    const double mean = (double)s_mean_sum[f] * kInvFix / (double)d.B;
+    const long long mean = s_mean[f];
     const long long* ph = d.phys + (size_t)f * d.B;
     const long long* fl = d.fill + (size_t)f * d.B;
     float* rho = d.rho + (size_t)f * d.B;
@@ -317,7 +304,7 @@ static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int
         ov[f] += a;
         cnt[f] += 1;
       }
-      rho[i] = (float)((double)(a + fl[i]) * kInvFix - mean);
+      rho[i] = __ll2float_rn(a + fl[i] - mean) * kInvFixF;
     }
   }
   for (int f = 0; f < d.K; ++f) {
@@ -435,6 +422,7 @@ __device__ void gemm_tiles(const float* A, long sa, const float* Bm, long sb, fl
       }
     }
     float* Cf = Cm + f * sc;
+    float eacc = 0.f;
 #pragma unroll
     for (int i = 0; i < RM; ++i)
 #pragma unroll
@@ -445,9 +433,10 @@ __device__ void gemm_tiles(const float* A, long sa, const float* Bm, long sb, fl
           float v = __fadd_rn(sum[i][j], comp[i][j]);
           if (epi == 1) v *= inv_eig[idx];
           Cf[idx] = v;
-          if (epi == 2) energy_acc[f] += (double)rho[(size_t)f * M * N + idx] * (double)v;
+          if (epi == 2) eacc = fmaf(rho[(size_t)f * M * N + idx], v, eacc);
         }
       }
+    if (epi == 2) energy_acc[f] += (double)eacc;
   }
   __syncthreads();
 }
@@ -474,7 +463,7 @@ __device__ __forceinline__ void gemm_any(bool large, const float* A, long sa, co
 //   t1 = rho Cx^T ; t2 = (Cy t1) o inv_eig ; t1 = Cy^T t2 ; phi = t1 Cx.
 // `step` selects one of the four (a grid barrier separates them).
 static __device__ void stage_dct(const Dev& d, int step, bool large, Partials p, int vb, int nvb, GemmShared& sm,
-                          Shared& sh) {
+                                 Shared& sh) {
   const int W = d.g.Wb, H = d.g.Hb;
   const long sg = d.B;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
@@ -493,9 +482,9 @@ static __device__ void stage_dct(const Dev& d, int step, bool large, Partials p,
 // filler loops, electrostatic_placement.rs:338-374, 919-941): raw per-field
 // gradient q * dphi per optimizer object, and force_l1 partials.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, double sxp, double syp) {
-  const AxisTaps ax = axis_taps(d.g.Wb, to_bin(sxp, d.g.sx, d.g.identity));
-  const AxisTaps ay = axis_taps(d.g.Hb, to_bin(syp, d.g.sy, d.g.identity));
+__device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, float sxp, float syp) {
+  const AxisTaps ax = taps_x(d, sxp);
+  const AxisTaps ay = taps_y(d, syp);
   const float dx[3] = {ax.o - 0.5f, -2.f * ax.o, ax.o + 0.5f};
   const float dy[3] = {ay.o - 0.5f, -2.f * ay.o, ay.o + 0.5f};
   // The derivative weights of each axis sum to zero, so the centre tap's
@@ -514,14 +503,15 @@ __device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, do
     }
   }
   if (!d.g.identity) {
-    gx *= (float)d.g.sx;
-    gy *= (float)d.g.sy;
+    gx *= d.g.sx;
+    gy *= d.g.sy;
   }
   return make_float2(gx, gy);
 }
 
-static __device__ void stage_gather(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb, Shared& sh) {
-  double force[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+static __device__ void stage_gather(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+                                    Shared& sh) {
+  float force[kMaxFields] = {0.f, 0.f, 0.f, 0.f};
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
     if (o < d.U) {
@@ -529,18 +519,18 @@ static __device__ void stage_gather(const Dev& d, const double2* __restrict__ po
 #pragma unroll
       for (int f = 0; f < kMaxFields; ++f) acc[f] = make_float2(0.f, 0.f);
       const int m0 = d.unit_mem_ptr[o], m1 = d.unit_mem_ptr[o + 1];
-      const double2 pu = pos[o];
+      const float2 pu = pos[o];
       for (int m = m0; m < m1; ++m) {
         const int f = d.mem_field[m];
-        const double2 off = d.mem_off[m];
+        const float2 off = d.mem_off[m];
         const float q = d.mem_q[m];
-        const float2 g = sample_grad(d, d.phi + (size_t)f * d.B, pu.x + off.x, pu.y + off.y);
+        const float2 g = sample_grad(d, d.phi + (size_t)f * d.B, __fadd_rn(pu.x, off.x), __fadd_rn(pu.y, off.y));
 #pragma unroll
         for (int ff = 0; ff < kMaxFields; ++ff)
           if (ff == f) {
             acc[ff].x += q * g.x;
             acc[ff].y += q * g.y;
-            force[ff] += (double)q * ((double)fabsf(g.x) + (double)fabsf(g.y));
+            force[ff] += q * (fabsf(g.x) + fabsf(g.y));
           }
       }
       for (int f = 0; f < d.K; ++f) d.graw[(size_t)f * d.nobj + o] = acc[f];
@@ -548,15 +538,15 @@ static __device__ void stage_gather(const Dev& d, const double2* __restrict__ po
       const int j = o - d.U;
       const int f = d.fil_field[j];
       const float q = d.fil_q[j];
-      const double2 pf = pos[o];
+      const float2 pf = pos[o];
       const float2 g = sample_grad(d, d.phi + (size_t)f * d.B, pf.x, pf.y);
       d.graw[(size_t)f * d.nobj + o] = make_float2(q * g.x, q * g.y);
 #pragma unroll
       for (int ff = 0; ff < kMaxFields; ++ff)
-        if (ff == f) force[ff] += (double)q * ((double)fabsf(g.x) + (double)fabsf(g.y));
+        if (ff == f) force[ff] += q * (fabsf(g.x) + fabsf(g.y));
     }
   }
-  for (int f = 0; f < d.K; ++f) write_partial(force[f], pslot(p, SLOT_FORCE + f), vb, sh.d);
+  for (int f = 0; f < d.K; ++f) write_partial((double)force[f], pslot(p, SLOT_FORCE + f), vb, sh.d);
 }
 
 // ---------------------------------------------------------------------------
@@ -564,41 +554,44 @@ static __device__ void stage_gather(const Dev& d, const double2* __restrict__ po
 // g = grad WA + sum_f coef_f grad E_f, with the non-finite check and the L1
 // norms the initial multiplier needs (eplace.rs:1126-1148).
 // ---------------------------------------------------------------------------
-static __device__ void stage_combine(const Dev& d, const double* coef, double2* __restrict__ gout, Partials p, int vb,
-                              int nvb, Shared& sh) {
-  double rawl1[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
-  double wal1 = 0.0;
+static __device__ void stage_combine(const Dev& d, const double* coef_d, float2* __restrict__ gout, Partials p,
+                                     int vb, int nvb, Shared& sh) {
+  float coef[kMaxFields];
+#pragma unroll
+  for (int f = 0; f < kMaxFields; ++f) coef[f] = f < d.K ? (float)coef_d[f] : 0.f;
+  float rawl1[kMaxFields] = {0.f, 0.f, 0.f, 0.f};
+  float wal1 = 0.f;
   long long bad = 0x7fffffffffffffffll;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
-    double gx = 0.0, gy = 0.0;
+    float gx = 0.f, gy = 0.f;
     if (o < d.U) {
-      gx = (double)(long long)d.wa_fix[2 * o] * kInvFix;
-      gy = (double)(long long)d.wa_fix[2 * o + 1] * kInvFix;
-      wal1 += fabs(gx) + fabs(gy);
+      gx = __ll2float_rn((long long)d.wa_fix[2 * o]) * kInvFixF;
+      gy = __ll2float_rn((long long)d.wa_fix[2 * o + 1]) * kInvFixF;
+      wal1 += fabsf(gx) + fabsf(gy);
       for (int f = 0; f < d.K; ++f) {
         const float2 r = d.graw[(size_t)f * d.nobj + o];
-        gx += coef[f] * (double)r.x;
-        gy += coef[f] * (double)r.y;
-        rawl1[f] += (double)fabsf(r.x) + (double)fabsf(r.y);
+        gx = fmaf(coef[f], r.x, gx);
+        gy = fmaf(coef[f], r.y, gy);
+        rawl1[f] += fabsf(r.x) + fabsf(r.y);
       }
     } else {
       const int f = d.fil_field[o - d.U];
       const float2 r = d.graw[(size_t)f * d.nobj + o];
-      for (int ff = 0; ff < d.K; ++ff)
+#pragma unroll
+      for (int ff = 0; ff < kMaxFields; ++ff)
         if (ff == f) {
-          gx += coef[ff] * (double)r.x;
-          gy += coef[ff] * (double)r.y;
-          rawl1[ff] += (double)fabsf(r.x) + (double)fabsf(r.y);
+          gx = coef[ff] * r.x;
+          gy = coef[ff] * r.y;
+          rawl1[ff] += fabsf(r.x) + fabsf(r.y);
         }
     }
     if (!isfinite(gx)) bad = min(bad, (long long)(2 * o));
     else if (!isfinite(gy)) bad = min(bad, (long long)(2 * o + 1));
-    gout[o] = make_double2(gx, gy);
+    gout[o] = make_float2(gx, gy);
   }
-  for (int f = 0; f < d.K; ++f) write_partial(rawl1[f], pslot(p, SLOT_RAWL1 + f), vb, sh.d);
-  write_partial(wal1, pslot(p, SLOT_WAL1), vb, sh.d);
-  // min-reduce the bad index
+  for (int f = 0; f < d.K; ++f) write_partial((double)rawl1[f], pslot(p, SLOT_RAWL1 + f), vb, sh.d);
+  write_partial((double)wal1, pslot(p, SLOT_WAL1), vb, sh.d);
   {
     long long v = bad;
 #pragma unroll
@@ -618,20 +611,20 @@ static __device__ void stage_combine(const Dev& d, const double* coef, double2* 
 }
 
 // ---------------------------------------------------------------------------
-// Nesterov vector stages (global_placement.rs:143-335, 588-712).
+// Nesterov vector stages (global_placement.rs:143-335, 588-712), FP32.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rclamp(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ float fclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // y = clamp(x + e (x - prev)); counts coordinates where y != x.
-static __device__ void stage_extrapolate(const Dev& d, const double2* __restrict__ x, const double2* __restrict__ xp,
-                                  double e, double2* __restrict__ y, Partials p, int vb, int nvb, Shared& sh) {
+static __device__ void stage_extrapolate(const Dev& d, const float2* __restrict__ x, const float2* __restrict__ xp,
+                                         float e, float2* __restrict__ y, Partials p, int vb, int nvb, Shared& sh) {
   long long diff = 0;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
-    const double2 a = x[o], b = xp[o], lo = d.lo[o], hi = d.hi[o];
-    double2 r;
-    r.x = rclamp(a.x + e * (a.x - b.x), lo.x, hi.x);
-    r.y = rclamp(a.y + e * (a.y - b.y), lo.y, hi.y);
+    const float2 a = x[o], b = xp[o], lo = d.lo[o], hi = d.hi[o];
+    float2 r;
+    r.x = fclamp(a.x + e * (a.x - b.x), lo.x, hi.x);
+    r.y = fclamp(a.y + e * (a.y - b.y), lo.y, hi.y);
     diff += (r.x != a.x) + (r.y != a.y);
     y[o] = r;
   }
@@ -639,99 +632,96 @@ static __device__ void stage_extrapolate(const Dev& d, const double2* __restrict
 }
 
 // c = clamp(y - g / (L P)); changed count, <g, c - y>, sum P (c - y)^2.
-static __device__ void stage_candidate(const Dev& d, const double2* __restrict__ y, const double2* __restrict__ gy,
-                                double L, double2* __restrict__ c, Partials p, int vb, int nvb, Shared& sh) {
+static __device__ void stage_candidate(const Dev& d, const float2* __restrict__ y, const float2* __restrict__ gy,
+                                       float invL, float2* __restrict__ c, Partials p, int vb, int nvb, Shared& sh) {
   long long diff = 0;
-  double dot = 0.0, msn = 0.0;
+  float dot = 0.f, msn = 0.f;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
-    const double2 a = y[o], g = gy[o], lo = d.lo[o], hi = d.hi[o];
-    const double m = d.P[o];
-    const double den = L * m;
-    double2 r;
-    r.x = rclamp(a.x - g.x / den, lo.x, hi.x);
-    r.y = rclamp(a.y - g.y / den, lo.y, hi.y);
+    const float2 a = y[o], g = gy[o], lo = d.lo[o], hi = d.hi[o];
+    const float m = d.P[o];
+    const float s = invL / m;
+    float2 r;
+    r.x = fclamp(a.x - g.x * s, lo.x, hi.x);
+    r.y = fclamp(a.y - g.y * s, lo.y, hi.y);
     diff += (r.x != a.x) + (r.y != a.y);
-    const double dx = r.x - a.x, dy = r.y - a.y;
-    dot += g.x * dx + g.y * dy;
-    msn += m * dx * dx + m * dy * dy;
+    const float dx = r.x - a.x, dy = r.y - a.y;
+    dot = fmaf(g.x, dx, fmaf(g.y, dy, dot));
+    msn = fmaf(m * dx, dx, fmaf(m * dy, dy, msn));
     c[o] = r;
   }
   write_partial(diff, islot(p, IS_DIFF), vb, sh.l);
-  write_partial(dot, pslot(p, SLOT_DOT), vb, sh.d);
-  write_partial(msn, pslot(p, SLOT_MSN), vb, sh.d);
+  write_partial((double)dot, pslot(p, SLOT_DOT), vb, sh.d);
+  write_partial((double)msn, pslot(p, SLOT_MSN), vb, sh.d);
 }
 
-__device__ __forceinline__ double kkt_comp(double g, double x, double lo, double hi) {
-  if (__double_as_longlong(lo) == __double_as_longlong(hi) || (x <= lo && g > 0.0) || (x >= hi && g < 0.0))
-    return 0.0;
-  return fabs(g);
+__device__ __forceinline__ float kkt_comp(float g, float x, float lo, float hi) {
+  if (__float_as_int(lo) == __float_as_int(hi) || (x <= lo && g > 0.f) || (x >= hi && g < 0.f)) return 0.f;
+  return fabsf(g);
 }
 
 // box_metric_kkt_residual (global_placement.rs:648-663) and, optionally, the
 // max coordinate change against `ref`.
-static __device__ void stage_kkt(const Dev& d, const double2* __restrict__ x, const double2* __restrict__ g,
-                          const double2* __restrict__ ref, Partials p, int vb, int nvb, Shared& sh) {
-  double r = 0.0, ch = 0.0;
+static __device__ void stage_kkt(const Dev& d, const float2* __restrict__ x, const float2* __restrict__ g,
+                                 const float2* __restrict__ ref, Partials p, int vb, int nvb, Shared& sh) {
+  float r = 0.f, ch = 0.f;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
-    const double2 a = x[o], gg = g[o], lo = d.lo[o], hi = d.hi[o];
-    const double s = sqrt(d.P[o]);
-    r = fmax(r, kkt_comp(gg.x, a.x, lo.x, hi.x) / s);
-    r = fmax(r, kkt_comp(gg.y, a.y, lo.y, hi.y) / s);
+    const float2 a = x[o], gg = g[o], lo = d.lo[o], hi = d.hi[o];
+    const float s = rsqrtf(d.P[o]);
+    r = fmaxf(r, kkt_comp(gg.x, a.x, lo.x, hi.x) * s);
+    r = fmaxf(r, kkt_comp(gg.y, a.y, lo.y, hi.y) * s);
     if (ref) {
-      const double2 b = ref[o];
-      ch = fmax(ch, fabs(a.x - b.x));
-      ch = fmax(ch, fabs(a.y - b.y));
+      const float2 b = ref[o];
+      ch = fmaxf(ch, fabsf(a.x - b.x));
+      ch = fmaxf(ch, fabsf(a.y - b.y));
     }
   }
-  write_partial_max(r, mslot(p, MS_KKT), vb, sh.d, false);
-  if (ref) write_partial_max(ch, mslot(p, MS_CHANGE), vb, sh.d, false);
+  write_partial_max((double)r, mslot(p, MS_KKT), vb, sh.d, false);
+  if (ref) write_partial_max((double)ch, mslot(p, MS_CHANGE), vb, sh.d, false);
 }
 
 // diagonal_preconditioner (eplace.rs:1046-1100).
-static __device__ void stage_precond(const Dev& d, const double* lambda, Partials p, int vb, int nvb, Shared& sh) {
-  double pmin = INFINITY, pmax = 0.0;
+static __device__ void stage_precond(const Dev& d, const double* lambda_d, Partials p, int vb, int nvb, Shared& sh) {
+  float lambda[kMaxFields];
+#pragma unroll
+  for (int f = 0; f < kMaxFields; ++f) lambda[f] = f < d.K ? (float)lambda_d[f] : 0.f;
+  float pmin = INFINITY, pmax = 0.f;
   long long badp = 0;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
-    double v = d.pre_static[o];
+    float v = d.pre_static[o];
     for (int f = 0; f < d.K; ++f) {
-      const double q = d.pre_q[(size_t)f * d.nobj + o];
-      if (q == 0.0) continue;
-      v += lambda[f] * q;
+      const float q = d.pre_q[(size_t)f * d.nobj + o];
+      if (q == 0.f) continue;
+      v = fmaf(lambda[f], q, v);
     }
-    if (!isfinite(v) || v < 0.0) badp = 1;
-    v = fmax(v, 1.0);
+    if (!isfinite(v) || v < 0.f) badp = 1;
+    v = fmaxf(v, 1.f);
     d.P[o] = v;
-    pmin = fmin(pmin, v);
-    pmax = fmax(pmax, v);
+    pmin = fminf(pmin, v);
+    pmax = fmaxf(pmax, v);
   }
-  write_partial_max(pmin, mslot(p, MS_PMIN), vb, sh.d, true);
-  write_partial_max(pmax, mslot(p, MS_PMAX), vb, sh.d, false);
+  write_partial_max((double)pmin, mslot(p, MS_PMIN), vb, sh.d, true);
+  write_partial_max((double)pmax, mslot(p, MS_PMAX), vb, sh.d, false);
   write_partial(badp, islot(p, IS_PBAD), vb, sh.l);
 }
 
-// HPWL over the baseline hypernets at `pos` (FP64).
-static __device__ void stage_hpwl(const Dev& d, const double2* __restrict__ pos, Partials p, int vb, int nvb, Shared& sh) {
+// HPWL over the baseline hypernets at `pos` (per-net FP32 spans, FP64 sum).
+static __device__ void stage_hpwl(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+                                  Shared& sh) {
   double acc = 0.0;
   const int stride = nvb * blockDim.x;
   for (int e = vb * blockDim.x + threadIdx.x; e < d.n_hpwl_nets; e += stride) {
-    double mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
+    float mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
     for (int k = d.net_ptr[e]; k < d.net_ptr[e + 1]; ++k) {
-      const int u = d.pin_unit[k];
-      const double2 b = d.pin_base[k];
-      double x = b.x, y = b.y;
-      if (u >= 0) {
-        x = pos[u].x + b.x;
-        y = pos[u].y + b.y;
-      }
-      mx = fmax(mx, x);
-      mnx = fmin(mnx, x);
-      my = fmax(my, y);
-      mny = fmin(mny, y);
+      const float2 v = pin_xy(d, pos, k);
+      mx = fmaxf(mx, v.x);
+      mnx = fminf(mnx, v.x);
+      my = fmaxf(my, v.y);
+      mny = fminf(mny, v.y);
     }
-    acc += (mx - mnx) + (my - mny);
+    acc += (double)((mx - mnx) + (my - mny));
   }
   write_partial(acc, pslot(p, SLOT_HPWL), vb, sh.d);
 }
