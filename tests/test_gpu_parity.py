@@ -158,3 +158,32 @@ def test_typed_errors_through_the_abi():
     with pytest.raises(abi.TexoGpError) as e:
         Placer(q)
     assert e.value.name == "FIXED_CAPACITY_EXHAUSTED"
+
+
+def test_device_engine_placement_matches_oracle_and_repeats():
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 0)
+    prm = params(best_effort=1, max_iterations=400)
+    st, _, _, s_ref = ffi.Oracle(prob, prm).place()
+    assert st == 0 and s_ref.converged
+    prm_dev = params(best_effort=1, max_iterations=400, engine=abi.ENGINE_DEVICE)
+    g = Placer(prob, prm_dev)
+    targets, coords, s = g.run()
+    assert s["converged"] and s["overflow"][0] <= 0.10
+    assert s["kernel_launches"] == 1
+    assert abs(s["hpwl"] - s_ref.hpwl) <= 0.01 * s_ref.hpwl
+    g.reset()
+    t2, c2, s2 = g.run()
+    assert np.array_equal(targets, t2) and np.array_equal(coords, c2)
+    assert s2["iterations"] == s["iterations"]
+
+
+def test_device_engine_is_resumable():
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 3)
+    prm = params(best_effort=1, max_iterations=400, engine=abi.ENGINE_DEVICE)
+    a = Placer(prob, prm)
+    _, ca, sa = a.run(15)
+    b = Placer(prob, prm)
+    for _ in range(3):
+        _, cb, sb = b.run(5)
+    assert sa["iterations"] == sb["iterations"] == 15
+    assert np.array_equal(ca, cb)

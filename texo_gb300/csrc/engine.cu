@@ -198,6 +198,20 @@ int32_t Instance::upload() {
   TRY(zeros(*this, &gX, nobj));
   TRY(zeros(*this, &gY, nobj));
   TRY(zeros(*this, &gC, nobj));
+  posb[0] = bufX;
+  posb[1] = bufXp;
+  posb[2] = bufY;
+  posb[3] = bufC;
+  gradb[0] = gX;
+  gradb[1] = gY;
+  gradb[2] = gC;
+  TRY(zeros(*this, &run_dev, 1));
+  TRY(zeros(*this, &bar, 1));
+  {
+    const int per_sm = persistent_blocks_per_sm();
+    pblocks = std::min(std::max(per_sm, 1), 2) * sms;
+    pblocks = std::min(pblocks, kMaxPartials);
+  }
   TRY(zeros(*this, &best, std::max<size_t>(h.U, 1)));
   TRY(zeros(*this, &prev_targets, 2 * (size_t)h.U));
   TRY(zeros(*this, &mismatch, 1));
@@ -581,6 +595,80 @@ struct Controller {
     return TEXO_GP_OK;
   }
 
+  // The device engine: the same loop inside one persistent cooperative kernel.
+  DevRun hr{};
+  bool dev_ready = false;
+
+  int32_t run_device(uint32_t budget) {
+    const HostModel& m = I.m;
+    if (!dev_ready) {
+      std::memset(&hr, 0, sizeof(hr));
+      hr.K = (int)m.K;
+      hr.max_iterations = m.params.max_iterations;
+      hr.best_effort = m.params.best_effort;
+      hr.W = (int)m.W;
+      hr.H = (int)m.H;
+      hr.beta = m.params.beta;
+      hr.alpha_low = m.params.alpha_low;
+      hr.alpha_high = m.params.alpha_high;
+      hr.init_weight = m.params.initial_density_weight;
+      hr.gamma_base = m.gamma_base_tiles();
+      hr.margin_eps = std::max(std::numeric_limits<double>::epsilon(), m.params.objective_margin_ulps * 0x1p-24);
+      for (uint32_t f = 0; f < m.K; ++f) {
+        hr.target[f] = m.overflow_target(f);
+        hr.gamma_weight[f] = m.gamma_weight[f];
+        hr.real_area[f] = m.real_area[f];
+        hr.e0[f] = 1.0;
+      }
+      hr.a = 1.0;
+      hr.ix = 0;
+      hr.ixp = 1;
+      hr.iy = 2;
+      hr.ic = 3;
+      hr.igx = 0;
+      hr.igy = 1;
+      hr.igc = 2;
+      for (int i = 0; i < 4; ++i) I.posb[i] = i == 0 ? I.bufX : (i == 1 ? I.bufXp : (i == 2 ? I.bufY : I.bufC));
+      dev_ready = true;
+    }
+    hr.budget = budget;
+    Buffers b;
+    for (int i = 0; i < 4; ++i) b.pos[i] = I.posb[i];
+    for (int i = 0; i < 3; ++i) b.grad[i] = I.gradb[i];
+    b.best = I.best;
+    b.prev_targets = I.prev_targets;
+    const int32_t s = launch_persistent(I.d, I.r, b, I.run_dev, &hr, I.bar, I.pblocks, I.stream);
+    if (s) {
+      set_last_error(s == TEXO_GP_ERR_DEVICE_TIMEOUT ? "persistent kernel: a grid barrier wait ran out"
+                                                     : std::string("persistent kernel: ") +
+                                                           cudaGetErrorString(cudaGetLastError()));
+      return s;
+    }
+    // mirror the kernel's state for the common result path
+    I.bufX = I.posb[hr.ix];
+    I.bufXp = I.posb[hr.ixp];
+    I.bufY = I.posb[hr.iy];
+    I.bufC = I.posb[hr.ic];
+    I.gX = I.gradb[hr.igx];
+    I.gY = I.gradb[hr.igy];
+    I.gC = I.gradb[hr.igc];
+    completed = hr.completed;
+    evaluations = hr.evaluations;
+    trials = hr.trials;
+    converged = hr.converged != 0;
+    exhausted = hr.exhausted != 0;
+    gamma = hr.gamma;
+    last_objective = hr.last_objective;
+    for (uint32_t f = 0; f < m.K; ++f) {
+      current.overflow[f] = hr.cur_overflow[f];
+      current.energy[f] = hr.cur_energy[f];
+    }
+    phase = hr.phase;
+    final_status = hr.status;
+    density_at_x = false;   // the host engine's scalar block no longer describes X
+    return hr.status;
+  }
+
   // optimize_density_once (eplace.rs:439-582), resumable: runs at most
   // `budget` more iterations when budget > 0.
   int32_t run(uint32_t budget) {
@@ -590,6 +678,7 @@ struct Controller {
       converged = true;
       return TEXO_GP_OK;
     }
+    if (I.m.params.engine == TEXO_GP_ENGINE_DEVICE) return run_device(budget);
     const uint32_t K = I.m.K;
     if (phase == 0) {
       lambda.assign(K, 0.0);

@@ -6,6 +6,7 @@
 
 #include "../../include/texo_gp.h"
 #include "kernels.cuh"
+#include "persistent.cuh"
 
 namespace tgp {
 
@@ -75,6 +76,12 @@ struct Instance {
   float2* best = nullptr;                        // best checkpoint coordinates [U]
   uint32_t* prev_targets = nullptr;              // [2U]
   unsigned long long* mismatch = nullptr;
+  // device engine: fixed buffer tables (roles rotate inside the kernel)
+  float2* posb[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2* gradb[3] = {nullptr, nullptr, nullptr};
+  DevRun* run_dev = nullptr;
+  GridBarrier* bar = nullptr;
+  int pblocks = 0;                               // persistent grid size
   double* h_scal = nullptr;                      // pinned host mirror
   long long* h_iscal = nullptr;
   uint64_t bytes = 0;

@@ -115,7 +115,7 @@ static __device__ void stage_init(const Dev& d, int vb, int nvb, bool grids, boo
 // exact in any order. The per-field tap total is a partial for the mean.
 // (deposit_quadratic_bspline + the field loop, electrostatic_placement.rs:296-332)
 // ---------------------------------------------------------------------------
-static __device__ void stage_scatter(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+static __device__ void stage_scatter(const Dev& d, const float2* pos, Partials p, int vb, int nvb,
                                      Shared& sh) {
   long long tot[kMaxFields];
 #pragma unroll
@@ -168,7 +168,7 @@ static __device__ void stage_scatter(const Dev& d, const float2* __restrict__ po
 // weights of the deltas to the extrema, soft means, per-pin derivative.
 // Unit gradients accumulate as int64 2^-32 fixed point (order-independent).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* __restrict__ pos, int k) {
+__device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* pos, int k) {
   const int u = d.pin_unit[k];
   const float2 b = d.pin_base[k];
   if (u < 0) return b;
@@ -177,7 +177,7 @@ __device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* __restrict_
 }
 
 template <int G>
-__device__ __forceinline__ void wa_class(const Dev& d, const float2* __restrict__ pos, float inv_gamma, int nb,
+__device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float inv_gamma, int nb,
                                          int ne, int vb, int nvb, double& acc) {
   const int lane = threadIdx.x & (G - 1);
   const int group = (vb * blockDim.x + threadIdx.x) / G;
@@ -259,7 +259,7 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* __restrict_
   acc += (double)vacc;
 }
 
-static __device__ void stage_wa(const Dev& d, const float2* __restrict__ pos, double gamma, Partials p, int vb,
+static __device__ void stage_wa(const Dev& d, const float2* pos, double gamma, Partials p, int vb,
                                 int nvb, Shared& sh) {
   double acc = 0.0;
   const float ig = (float)(1.0 / gamma);
@@ -371,14 +371,14 @@ __device__ void gemm_tiles(const float* A, long sa, const float* Bm, long sb, fl
         const int e = threadIdx.x + q * kThreads;
         const int mm = e / TK, kk = e % TK;
         const int gm = m0 + mm, gk = k0 + kk;
-        ra[q] = (gm < M && gk < Kd) ? __ldg(Af + (size_t)gm * Kd + gk) : 0.f;
+        ra[q] = (gm < M && gk < Kd) ? Af[(size_t)gm * Kd + gk] : 0.f;
       }
 #pragma unroll
       for (int q = 0; q < LB; ++q) {
         const int e = threadIdx.x + q * kThreads;
         const int kk = e / TN, nn = e % TN;
         const int gk = k0 + kk, gn = n0 + nn;
-        rb[q] = (gk < Kd && gn < N) ? __ldg(Bf + (size_t)gk * N + gn) : 0.f;
+        rb[q] = (gk < Kd && gn < N) ? Bf[(size_t)gk * N + gn] : 0.f;
       }
     };
     fetch(0);
@@ -490,14 +490,14 @@ __device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, fl
   // The derivative weights of each axis sum to zero, so the centre tap's
   // potential can be subtracted first: the FP32 sum then rounds relative to
   // the local potential differences, not to the potential itself.
-  const float vc = __ldg(phi + (size_t)ay.idx[1] * d.g.Wb + ax.idx[1]);
+  const float vc = phi[(size_t)ay.idx[1] * d.g.Wb + ax.idx[1]];
   float gx = 0.f, gy = 0.f;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     const float* row = phi + (size_t)ay.idx[r] * d.g.Wb;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float v = __ldg(row + ax.idx[c]) - vc;
+      const float v = row[ax.idx[c]] - vc;
       gx += dx[c] * ay.w[r] * v;
       gy += ax.w[c] * dy[r] * v;
     }
@@ -509,7 +509,7 @@ __device__ __forceinline__ float2 sample_grad(const Dev& d, const float* phi, fl
   return make_float2(gx, gy);
 }
 
-static __device__ void stage_gather(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+static __device__ void stage_gather(const Dev& d, const float2* pos, Partials p, int vb, int nvb,
                                     Shared& sh) {
   float force[kMaxFields] = {0.f, 0.f, 0.f, 0.f};
   const int stride = nvb * blockDim.x;
@@ -554,13 +554,20 @@ static __device__ void stage_gather(const Dev& d, const float2* __restrict__ pos
 // g = grad WA + sum_f coef_f grad E_f, with the non-finite check and the L1
 // norms the initial multiplier needs (eplace.rs:1126-1148).
 // ---------------------------------------------------------------------------
-static __device__ void stage_combine(const Dev& d, const double* coef_d, float2* __restrict__ gout, Partials p,
-                                     int vb, int nvb, Shared& sh) {
+__device__ __forceinline__ float kkt_comp(float g, float x, float lo, float hi) {
+  if (__float_as_int(lo) == __float_as_int(hi) || (x <= lo && g > 0.f) || (x >= hi && g < 0.f)) return 0.f;
+  return fabsf(g);
+}
+
+// With kkt_pos, the box-metric KKT residual of the new gradient at kkt_pos is
+// reduced in the same pass (box_metric_kkt_residual, global_placement.rs:648-663).
+static __device__ void stage_combine(const Dev& d, const double* coef_d, float2* gout, Partials p,
+                                     int vb, int nvb, Shared& sh, const float2* kkt_pos = nullptr) {
   float coef[kMaxFields];
 #pragma unroll
   for (int f = 0; f < kMaxFields; ++f) coef[f] = f < d.K ? (float)coef_d[f] : 0.f;
   float rawl1[kMaxFields] = {0.f, 0.f, 0.f, 0.f};
-  float wal1 = 0.f;
+  float wal1 = 0.f, kkt = 0.f;
   long long bad = 0x7fffffffffffffffll;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
@@ -589,9 +596,16 @@ static __device__ void stage_combine(const Dev& d, const double* coef_d, float2*
     if (!isfinite(gx)) bad = min(bad, (long long)(2 * o));
     else if (!isfinite(gy)) bad = min(bad, (long long)(2 * o + 1));
     gout[o] = make_float2(gx, gy);
+    if (kkt_pos) {
+      const float2 a = kkt_pos[o], lo = d.lo[o], hi = d.hi[o];
+      const float s = rsqrtf(d.P[o]);
+      kkt = fmaxf(kkt, kkt_comp(gx, a.x, lo.x, hi.x) * s);
+      kkt = fmaxf(kkt, kkt_comp(gy, a.y, lo.y, hi.y) * s);
+    }
   }
   for (int f = 0; f < d.K; ++f) write_partial((double)rawl1[f], pslot(p, SLOT_RAWL1 + f), vb, sh.d);
   write_partial((double)wal1, pslot(p, SLOT_WAL1), vb, sh.d);
+  if (kkt_pos) write_partial_max((double)kkt, mslot(p, MS_KKT), vb, sh.d, false);
   {
     long long v = bad;
 #pragma unroll
@@ -616,8 +630,8 @@ static __device__ void stage_combine(const Dev& d, const double* coef_d, float2*
 __device__ __forceinline__ float fclamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // y = clamp(x + e (x - prev)); counts coordinates where y != x.
-static __device__ void stage_extrapolate(const Dev& d, const float2* __restrict__ x, const float2* __restrict__ xp,
-                                         float e, float2* __restrict__ y, Partials p, int vb, int nvb, Shared& sh) {
+static __device__ void stage_extrapolate(const Dev& d, const float2* x, const float2* xp,
+                                         float e, float2* y, Partials p, int vb, int nvb, Shared& sh) {
   long long diff = 0;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
@@ -632,10 +646,12 @@ static __device__ void stage_extrapolate(const Dev& d, const float2* __restrict_
 }
 
 // c = clamp(y - g / (L P)); changed count, <g, c - y>, sum P (c - y)^2.
-static __device__ void stage_candidate(const Dev& d, const float2* __restrict__ y, const float2* __restrict__ gy,
-                                       float invL, float2* __restrict__ c, Partials p, int vb, int nvb, Shared& sh) {
+// With origin, also the max coordinate change |c - origin|.
+static __device__ void stage_candidate(const Dev& d, const float2* y, const float2* gy,
+                                       float invL, float2* c, Partials p, int vb, int nvb, Shared& sh,
+                                       const float2* origin = nullptr) {
   long long diff = 0;
-  float dot = 0.f, msn = 0.f;
+  float dot = 0.f, msn = 0.f, ch = 0.f;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
     const float2 a = y[o], g = gy[o], lo = d.lo[o], hi = d.hi[o];
@@ -649,21 +665,21 @@ static __device__ void stage_candidate(const Dev& d, const float2* __restrict__ 
     dot = fmaf(g.x, dx, fmaf(g.y, dy, dot));
     msn = fmaf(m * dx, dx, fmaf(m * dy, dy, msn));
     c[o] = r;
+    if (origin) {
+      const float2 b = origin[o];
+      ch = fmaxf(ch, fmaxf(fabsf(r.x - b.x), fabsf(r.y - b.y)));
+    }
   }
   write_partial(diff, islot(p, IS_DIFF), vb, sh.l);
   write_partial((double)dot, pslot(p, SLOT_DOT), vb, sh.d);
   write_partial((double)msn, pslot(p, SLOT_MSN), vb, sh.d);
-}
-
-__device__ __forceinline__ float kkt_comp(float g, float x, float lo, float hi) {
-  if (__float_as_int(lo) == __float_as_int(hi) || (x <= lo && g > 0.f) || (x >= hi && g < 0.f)) return 0.f;
-  return fabsf(g);
+  if (origin) write_partial_max((double)ch, mslot(p, MS_CHANGE), vb, sh.d, false);
 }
 
 // box_metric_kkt_residual (global_placement.rs:648-663) and, optionally, the
 // max coordinate change against `ref`.
-static __device__ void stage_kkt(const Dev& d, const float2* __restrict__ x, const float2* __restrict__ g,
-                                 const float2* __restrict__ ref, Partials p, int vb, int nvb, Shared& sh) {
+static __device__ void stage_kkt(const Dev& d, const float2* x, const float2* g,
+                                 const float2* ref, Partials p, int vb, int nvb, Shared& sh) {
   float r = 0.f, ch = 0.f;
   const int stride = nvb * blockDim.x;
   for (int o = vb * blockDim.x + threadIdx.x; o < d.nobj; o += stride) {
@@ -708,7 +724,7 @@ static __device__ void stage_precond(const Dev& d, const double* lambda_d, Parti
 }
 
 // HPWL over the baseline hypernets at `pos` (per-net FP32 spans, FP64 sum).
-static __device__ void stage_hpwl(const Dev& d, const float2* __restrict__ pos, Partials p, int vb, int nvb,
+static __device__ void stage_hpwl(const Dev& d, const float2* pos, Partials p, int vb, int nvb,
                                   Shared& sh) {
   double acc = 0.0;
   const int stride = nvb * blockDim.x;
