@@ -187,6 +187,85 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_workload(n=64, seed0=0, lo=1000, hi=40000, sigma=6.0):
+    """Mixed-size instances: cells log-uniform in [lo, hi], fabric side
+    ceil(sqrt(cells/0.9)), bin grid the next power of two >= side clamped to
+    64..256, 1.2 nets per cell, IO on the perimeter, instance i seeded i."""
+    import math
+    import numpy as np
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import default_params
+    rng = np.random.default_rng(20261203 + seed0)
+    jobs = []
+    for i in range(n):
+        cells = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+        side = math.ceil(math.sqrt(cells / 0.9))
+        bins = min(256, max(64, 1 << (side - 1).bit_length()))
+        io = min(4 * (side - 1), 2 * side)
+        prob = P.synthetic(side, cells, io, int(round(1.2 * cells)), sigma, seed0 + i)
+        prm = default_params(bins_x=bins, bins_y=bins, target_density=1.0, gamma_base=4.0, max_iterations=1000,
+                             best_effort=1)
+        jobs.append((prob, prm))
+    return jobs
+
+
+def run_batched(jobs, chunk=20, device=0):
+    """All jobs resident in one batch, advanced `chunk` iterations per launch."""
+    import torch
+    from texo_gb300.placer import Batch
+    b = Batch(hbm_budget=200 << 30, max_slots=len(jobs) + 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i, (p, prm) in enumerate(jobs):
+        assert b.admit(p, i, prm)
+    results = {}
+    launches = 0
+    while len(results) < len(jobs):
+        b.advance(chunk)
+        launches += 1
+        while True:
+            r = b.retire()
+            if r is None:
+                break
+            results[r[0]] = r[2]
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, results, launches
+
+
+def run_serial(jobs, engine):
+    import torch
+    from texo_gb300.placer import Placer
+    total_ms, results = 0.0, {}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i, (p, prm) in enumerate(jobs):
+        prm.engine = engine
+        g = Placer(p, prm)
+        _, _, s = g.run()
+        total_ms += s["elapsed_ms"]
+        results[i] = s
+        g.close()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, results
+
+
+def batch_report(n=64):
+    from texo_gb300 import abi
+    jobs = batch_workload(n)
+    wall_b, res_b, launches = run_batched(jobs)
+    wall_d, res_d = run_serial(batch_workload(n), abi.ENGINE_DEVICE)
+    wall_h, res_h = run_serial(batch_workload(n), abi.ENGINE_HOST)
+    same = sum(1 for i in range(n) if res_b[i]["hpwl"] == res_d[i]["hpwl"])
+    iters = sum(s["iterations"] for s in res_b.values())
+    return {"instances": n, "cells": "log-uniform 1k..40k", "placements_per_s_batched": n / wall_b,
+            "placements_per_s_serial_device_engine": n / wall_d,
+            "placements_per_s_serial_host_engine_fp32": n / wall_h,
+            "speedup_vs_serial_host_fp32": wall_h / wall_b, "iterations_per_s_batched": iters / wall_b,
+            "batched_launches": launches, "identical_to_alone": "%d/%d" % (same, n),
+            "converged": sum(1 for s in res_b.values() if s["converged"]),
+            "wall_s": {"batched": wall_b, "serial_device": wall_d, "serial_host": wall_h}}
+
+
 def config_dict(args):
     side, cells, io, nets, sigma, bins, td, gamma, cap = WORKLOADS[args.workload]
     return {"workload": args.workload, "cells": cells, "io": io, "nets": nets, "fabric": "%dx%d" % (side, side),
@@ -209,6 +288,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="warmup and timed steps only (for ncu launch lists)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-instance batched comparison")
+    ap.add_argument("--batch-only", action="store_true", help="print only the batched comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -229,6 +310,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.batch_only:
+        if rank == 0:
+            print(json.dumps({"metric": "placements/s (64 mixed instances)", "batched": batch_report()}), flush=True)
+        return
     engine = abi.ENGINE_HOST if args.engine == "host" else abi.ENGINE_DEVICE
     dct = abi.DCT_FP32 if args.dct == "fp32" else abi.DCT_BF16X3
     prob = make_problem(args.workload, rank)
@@ -304,6 +389,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": config_dict(args), "clocks": clk.summary(), "gpu_launches": int(launches),
             "roofline": roofline, "e2e": e2e, "restarts": state["restarts"]}
+    if rank == 0 and not args.no_batch:
+        line["batched"] = batch_report()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)

@@ -292,6 +292,12 @@ int32_t texo_gp_reset(texo_gp_handle h);
 int32_t texo_gp_stage_times(texo_gp_handle h, uint32_t reps, double* ms, uint32_t capacity,
                             uint32_t* count);
 const char* texo_gp_stage_name(uint32_t stage);
+/* Cumulative phase profile of the device engine since create/reset, in
+ * microseconds, as seen by the persistent kernel's first block: out[0..7] =
+ * scatter+WA, prep, transforms, gather+combine, preconditioner/init,
+ * extrapolation, candidate, other; out[8] = time block 0 spent waiting in
+ * grid barriers; out[9] = number of grid barriers. */
+int32_t texo_gp_device_profile(texo_gp_handle h, double out[10]);
 
 /* HPWL = sum over hypernets of the x and y pin spans at `coordinates`
  * (the continuous form of `exact_objective`, analytical_placement.rs:473-511),
@@ -326,9 +332,12 @@ typedef struct texo_gp_batch_s* texo_gp_batch;
 int32_t texo_gp_batch_create(const texo_gp_params* params, uint64_t hbm_budget_bytes,
                              uint32_t max_slots, texo_gp_batch* out);
 int32_t texo_gp_batch_destroy(texo_gp_batch b);
-/* Admits one job when its footprint fits; returns TEXO_GP_ERR_BUSY otherwise. */
+/* Admits one job when its device footprint fits the remaining HBM budget and
+ * a slot is free; returns TEXO_GP_ERR_BUSY otherwise. `params` (NULL = the
+ * batch's) may set a per-job bin grid, target density and stop rule; the
+ * engine is always the device engine and the device the batch's. */
 int32_t texo_gp_batch_admit(texo_gp_batch b, const texo_gp_problem* problem,
-                            uint64_t job_id, uint32_t* out_slot);
+                            const texo_gp_params* params, uint64_t job_id, uint32_t* out_slot);
 /* Advances every resident job by up to `iterations` eplace iterations. */
 int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations);
 /* Pops one finished job: its id, rounded targets (caller buffer of 2U) and stats.

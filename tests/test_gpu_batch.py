@@ -1,0 +1,63 @@
+"""Batched placement on the GPU: jobs of uneven size resident together, each
+advanced by one persistent launch, must give exactly the result they give
+alone (bit-identical targets), and admission must respect the HBM budget."""
+import numpy as np
+import pytest
+
+from texo_gb300 import abi, problem as P
+from texo_gb300.placer import Batch, Placer, default_params
+
+pytestmark = pytest.mark.gpu
+
+
+def params(**kw):
+    p = default_params(best_effort=1, max_iterations=300, engine=abi.ENGINE_DEVICE)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+SIZES = [(24, 400, 40, 480, 1), (48, 2000, 96, 2400, 2), (64, 3500, 100, 4200, 3), (36, 1100, 60, 1300, 4)]
+
+
+def problems():
+    return [P.synthetic(side, cells, io, nets, 6.0, seed) for side, cells, io, nets, seed in SIZES]
+
+
+def test_batch_results_equal_results_alone():
+    probs = problems()
+    alone = []
+    for p in probs:
+        t, _, s = Placer(p, params()).run()
+        alone.append((t, s))
+    b = Batch(params())
+    for i, p in enumerate(probs):
+        assert b.admit(p, 100 + i)
+    got = {}
+    for _ in range(400):
+        b.advance(7)
+        while True:
+            r = b.retire()
+            if r is None:
+                break
+            got[r[0]] = r
+        if len(got) == len(probs):
+            break
+    assert len(got) == len(probs)
+    for i, (t, s) in enumerate(alone):
+        jid, tb, sb = got[100 + i]
+        assert np.array_equal(t, tb), "job %d differs in the mix" % i
+        assert sb["iterations"] == s["iterations"]
+        assert sb["hpwl"] == s["hpwl"]
+
+
+def test_admission_respects_the_hbm_budget():
+    probs = problems()
+    probe = Batch(params())
+    assert probe.admit(probs[1], 1)
+    _, _, one = probe.counts()
+    b = Batch(params(), hbm_budget=int(one * 1.5))
+    assert b.admit(probs[1], 1)
+    assert not b.admit(probs[1], 2)        # a second copy does not fit
+    r, f, used = b.counts()
+    assert r == 1 and used == one

@@ -157,11 +157,12 @@ SIGNATURES = {
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
     "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),
     "texo_gp_stage_name": (C.c_char_p, [C.c_uint32]),
+    "texo_gp_device_profile": (C.c_int32, [_P, c_f64p]),
     "texo_gp_synth_create": (C.c_int32, [C.POINTER(SynthSpec), C.POINTER(_P), C.POINTER(C.POINTER(ProblemC))]),
     "texo_gp_synth_destroy": (C.c_int32, [_P]),
     "texo_gp_batch_create": (C.c_int32, [C.POINTER(Params), C.c_uint64, C.c_uint32, C.POINTER(_P)]),
     "texo_gp_batch_destroy": (C.c_int32, [_P]),
-    "texo_gp_batch_admit": (C.c_int32, [_P, C.POINTER(ProblemC), C.c_uint64, c_u32p]),
+    "texo_gp_batch_admit": (C.c_int32, [_P, C.POINTER(ProblemC), C.POINTER(Params), C.c_uint64, c_u32p]),
     "texo_gp_batch_advance": (C.c_int32, [_P, C.c_uint32]),
     "texo_gp_batch_retire": (C.c_int32, [_P, c_u64p, c_u32p, C.c_uint64, C.POINTER(Stats)]),
     "texo_gp_batch_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u64p]),

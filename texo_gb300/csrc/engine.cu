@@ -96,7 +96,10 @@ int32_t Instance::upload() {
   const size_t nobj = (size_t)h.U + h.F, B = h.bins(), K = h.K;
   // enough blocks to cover the widest stage, up to 8 per SM
   const size_t widest = std::max(std::max(std::max(nobj, (size_t)h.Mm + h.F), std::max(B, h.pin_unit.size() / 2)), (size_t)1);
-  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * 8), (size_t)kMaxPartials);
+  // Virtual blocks: the reduction structure of every stage. The standalone
+  // kernels launch exactly this many blocks; the persistent engine loops its
+  // physical blocks over them, so both see the same partials.
+  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * 2), (size_t)kMaxPartials);
   nvb = std::max(nvb, 1);
   Dev& D = d;
   D.U = (int)h.U;
@@ -599,7 +602,8 @@ struct Controller {
   DevRun hr{};
   bool dev_ready = false;
 
-  int32_t run_device(uint32_t budget) {
+  // Initializes the kernel's controller state on first use.
+  void prepare_devrun() {
     const HostModel& m = I.m;
     if (!dev_ready) {
       std::memset(&hr, 0, sizeof(hr));
@@ -631,20 +635,35 @@ struct Controller {
       for (int i = 0; i < 4; ++i) I.posb[i] = i == 0 ? I.bufX : (i == 1 ? I.bufXp : (i == 2 ? I.bufY : I.bufC));
       dev_ready = true;
     }
-    hr.budget = budget;
+  }
+
+  Buffers buffers() const {
     Buffers b;
     for (int i = 0; i < 4; ++i) b.pos[i] = I.posb[i];
     for (int i = 0; i < 3; ++i) b.grad[i] = I.gradb[i];
     b.best = I.best;
     b.prev_targets = I.prev_targets;
-    const int32_t s = launch_persistent(I.d, I.r, b, I.run_dev, &hr, I.bar, I.pblocks, I.stream);
+    return b;
+  }
+
+  int32_t run_device(uint32_t budget) {
+    prepare_devrun();
+    hr.budget = budget;
+    const int32_t s = launch_persistent(I.d, I.r, buffers(), I.run_dev, &hr, I.bar, std::min(I.pblocks, I.nvb),
+                                        I.nvb, I.stream);
     if (s) {
       set_last_error(s == TEXO_GP_ERR_DEVICE_TIMEOUT ? "persistent kernel: a grid barrier wait ran out"
                                                      : std::string("persistent kernel: ") +
                                                            cudaGetErrorString(cudaGetLastError()));
       return s;
     }
-    // mirror the kernel's state for the common result path
+    return absorb_devrun();
+  }
+
+  // Mirrors the kernel's state (hr, already copied back) for the common
+  // result path.
+  int32_t absorb_devrun() {
+    const HostModel& m = I.m;
     I.bufX = I.posb[hr.ix];
     I.bufXp = I.posb[hr.ixp];
     I.bufY = I.posb[hr.iy];
@@ -784,6 +803,37 @@ struct texo_gp_handle_s {
   std::unique_ptr<Controller> ctl;
   std::mutex mu;
 };
+
+namespace tgp {
+int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, InstDesc* desc, bool* large) {
+  Instance& I = *h->inst;
+  Controller& C = *h->ctl;
+  C.prepare_devrun();
+  C.hr.budget = budget;
+  CU(cudaMemcpyAsync(I.run_dev, &C.hr, sizeof(DevRun), cudaMemcpyHostToDevice, s));
+  CU(cudaMemsetAsync(I.bar, 0, sizeof(GridBarrier), s));
+  desc->d = I.d;
+  desc->r = I.r;
+  desc->B = C.buffers();
+  desc->run = I.run_dev;
+  desc->bar = I.bar;
+  desc->V = I.nvb;
+  desc->pad = 0;
+  *large = (long long)((I.d.g.Wb + 31) / 32) * ((I.d.g.Hb + 31) / 32) >= 1024;
+  return TEXO_GP_OK;
+}
+int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s, GridBarrier* host_bar) {
+  Instance& I = *h->inst;
+  CU(cudaMemcpyAsync(&h->ctl->hr, I.run_dev, sizeof(DevRun), cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(host_bar, I.bar, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s));
+  return TEXO_GP_OK;
+}
+int32_t batch_absorb(texo_gp_handle_s* h) { return h->ctl->absorb_devrun(); }
+bool handle_finished(texo_gp_handle_s* h) { return h->ctl->phase == 2; }
+uint64_t handle_bytes(texo_gp_handle_s* h) { return h->inst->bytes; }
+int handle_virtual_blocks(texo_gp_handle_s* h) { return h->inst->nvb; }
+int handle_sms(texo_gp_handle_s* h) { return h->inst->sms; }
+}  // namespace tgp
 
 namespace {
 uint32_t round_coord(double v, uint32_t extent) {
@@ -1184,6 +1234,16 @@ int32_t texo_gp_stage_times(texo_gp_handle h, uint32_t reps, double* ms, uint32_
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   h->ctl->density_at_x = false;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_device_profile(texo_gp_handle h, double out[10]) {
+  if (!h || !out) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  const DevRun& hr = h->ctl->hr;
+  for (int i = 0; i < 8; ++i) out[i] = hr.phase_ns[i] * 1e-3;
+  out[8] = hr.barrier_wait_ns * 1e-3;
+  out[9] = (double)hr.barriers;
   return TEXO_GP_OK;
 }
 

@@ -94,3 +94,17 @@ struct Instance {
 }  // namespace tgp
 
 struct texo_gp_handle_s;
+
+namespace tgp {
+// Hooks the batch uses to drive device-engine handles through one launch.
+// stage_in queues the controller state and barrier reset on stream s and
+// fills the instance descriptor; stage_out queues the copies back; absorb
+// mirrors the state once the stream has completed.
+int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, InstDesc* desc, bool* large);
+int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s, GridBarrier* host_bar);
+int32_t batch_absorb(texo_gp_handle_s* h);
+bool handle_finished(texo_gp_handle_s* h);
+uint64_t handle_bytes(texo_gp_handle_s* h);
+int handle_virtual_blocks(texo_gp_handle_s* h);
+int handle_sms(texo_gp_handle_s* h);
+}  // namespace tgp

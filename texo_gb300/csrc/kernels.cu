@@ -18,10 +18,11 @@ __global__ void __launch_bounds__(kThreads) k_prep(Dev d, Partials p) {
   __shared__ Shared sh;
   stage_prep(d, p, gridDim.x, blockIdx.x, gridDim.x, sh);
 }
-__global__ void __launch_bounds__(kThreads) k_dct(Dev d, Partials p, int step, bool large) {
+template <bool LARGE>
+__global__ void __launch_bounds__(kThreads) k_dct(Dev d, Partials p, int step) {
   __shared__ GemmShared sm;
   __shared__ Shared sh;
-  stage_dct(d, step, large, p, blockIdx.x, gridDim.x, sm, sh);
+  stage_dct_t<LARGE>(d, step, p, blockIdx.x, gridDim.x, sm, sh);
 }
 __global__ void __launch_bounds__(kThreads) k_gather(Dev d, Partials p, const float2* pos) {
   __shared__ Shared sh;
@@ -191,7 +192,10 @@ void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
 }
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s) {
   COUNT;
-  k_dct<<<nvb, kThreads, 0, s>>>(d, r.p, step, use_large_tiles(d));
+  if (use_large_tiles(d))
+    k_dct<true><<<nvb, kThreads, 0, s>>>(d, r.p, step);
+  else
+    k_dct<false><<<nvb, kThreads, 0, s>>>(d, r.p, step);
 }
 void launch_gather(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s) {
   COUNT;

@@ -2,13 +2,20 @@
 //
 // The kernel runs `optimize_density_once` (crates/texo-pnr/src/eplace.rs:439-582)
 // with `dynamic_nesterov_step` (crates/texo-pnr/src/global_placement.rs:121-335)
-// on the device. Stages are separated by a grid barrier; after each barrier
-// every block reduces the partials it needs in the same fixed order, so all
-// blocks hold bit-identical scalars and take the same branch. Thread 0 of each
-// block keeps the controller state in shared memory; block 0 writes it back
-// when the kernel returns. Every wait is bounded: a barrier that does not
-// complete within its spin budget sets an error word, and every block then
-// leaves the kernel at its next barrier.
+// on the device. Stages are separated by a barrier over the instance's
+// blocks; after each barrier every block reduces the partials it needs in the
+// same fixed order, so all blocks hold bit-identical scalars and take the same
+// branch. Thread 0 of each block keeps the controller state in shared memory;
+// the instance's first block writes it back when the kernel returns.
+//
+// Work is split into a fixed number V of virtual blocks per instance; the
+// instance's physical blocks loop over them. Partials are indexed by virtual
+// block, so an instance computes bit-identical results whether it runs alone
+// on every SM or shares one launch with other instances (batched serving).
+//
+// Every wait is bounded: a barrier that does not complete within its spin
+// budget sets an error word, and the instance's blocks then leave the kernel
+// at their next barrier.
 #include <cmath>
 #include <cstring>
 
@@ -26,17 +33,30 @@ struct ERec {
   long long bad;
 };
 
-__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned nblocks, unsigned* gen, unsigned long long* count) {
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Barrier over the np physical blocks of one instance.
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned np, unsigned* gen, unsigned long long* count,
+                                          unsigned long long* wait_acc) {
   __syncthreads();
   if (threadIdx.x == 0) {
+    const unsigned long long t0 = wait_acc ? now_ns() : 0ull;
     const unsigned g = *gen;
     __threadfence();
-    const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
-    if (arrived == nblocks) {
-      atomicExch(&b->count, 0u);
+    // One counter: on this two-die part a barrier costs a few L2 round trips
+    // whatever the arrival pattern, and a two-level tree only adds one.
+    bool last = false;
+    if (atomicAdd(&b->root.count, 1u) + 1u == np) {
+      b->root.count = 0u;
       __threadfence();
       atomicAdd(&b->gen, 1u);
-    } else {
+      last = true;
+    }
+    if (!last) {
       unsigned spins = 0;
       while (*(volatile unsigned*)&b->gen == g) {
         if (*(volatile int*)&b->error) break;
@@ -50,11 +70,13 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned nblocks, unsi
     *gen = g + 1;
     ++*count;
     __threadfence();
+    if (wait_acc) *wait_acc += now_ns() - t0;
   }
   __syncthreads();
   return *(volatile int*)&b->error == 0;
 }
 
+template <bool LARGE>
 struct Ctx {
   const Dev& d;
   const Reduce& r;
@@ -67,18 +89,27 @@ struct Ctx {
   double* rd;         // reduction scratch (shared)
   long long* rl;
   double* coef;       // shared [kMaxFields]
-  int vb, nvb;
-  bool large;
+  int pb, np;         // physical block of the instance, physical block count
+  int V;              // virtual blocks of the instance
   unsigned long long nbar;
+  unsigned long long* clock;   // shared [8] phase accumulators, [8] last mark, [9] barrier wait
 
-  __device__ bool sync() { return grid_sync(bar, (unsigned)nvb, gen, &nbar); }
-  __device__ double rsum(int slot) { return block_reduce_array(pslot(r.p, slot), nvb, 0.0, OpAdd(), rd); }
-  __device__ long long risum(int slot) { return block_reduce_array(islot(r.p, slot), nvb, 0ll, OpAdd(), rl); }
-  __device__ long long rimin(int slot) {
-    return block_reduce_array(islot(r.p, slot), nvb, 0x7fffffffffffffffll, OpMin(), rl);
+  __device__ bool sync() { return grid_sync(bar, (unsigned)np, gen, &nbar, pb == 0 ? clock + 9 : nullptr); }
+  // Charges the time since the previous mark to phase category `cat` (block 0).
+  __device__ void mark(int cat) {
+    if (pb == 0 && threadIdx.x == 0) {
+      const unsigned long long t = now_ns();
+      clock[cat] += t - clock[8];
+      clock[8] = t;
+    }
   }
-  __device__ double rmax(int slot) { return block_reduce_array(mslot(r.p, slot), nvb, 0.0, OpMax(), rd); }
-  __device__ double rmin(int slot) { return block_reduce_array(mslot(r.p, slot), nvb, (double)INFINITY, OpMin(), rd); }
+  __device__ double rsum(int slot) { return block_reduce_array(pslot(r.p, slot), V, 0.0, OpAdd(), rd); }
+  __device__ long long risum(int slot) { return block_reduce_array(islot(r.p, slot), V, 0ll, OpAdd(), rl); }
+  __device__ long long rimin(int slot) {
+    return block_reduce_array(islot(r.p, slot), V, 0x7fffffffffffffffll, OpMin(), rl);
+  }
+  __device__ double rmax(int slot) { return block_reduce_array(mslot(r.p, slot), V, 0.0, OpMax(), rd); }
+  __device__ double rmin(int slot) { return block_reduce_array(mslot(r.p, slot), V, (double)INFINITY, OpMin(), rd); }
   __device__ float2* X() const { return B.pos[S.ix]; }
   __device__ float2* Xp() const { return B.pos[S.ixp]; }
   __device__ float2* Y() const { return B.pos[S.iy]; }
@@ -88,22 +119,26 @@ struct Ctx {
   __device__ float2* gC() const { return B.grad[S.igc]; }
 
   __device__ void copy(float2* dst, const float2* src, int n) {
-    for (int i = vb * blockDim.x + threadIdx.x; i < n; i += nvb * blockDim.x) dst[i] = src[i];
+    for (int i = pb * blockDim.x + threadIdx.x; i < n; i += np * blockDim.x) dst[i] = src[i];
   }
 
   // Objective evaluation at pos after an init phase and its barrier
   // (ContinuousProblem::evaluate + combined_objective, eplace.rs:137-205, 1022-1044).
   __device__ bool eval_tail(const float2* pos, float2* g, double gam, bool full, const float2* kkt_pos, ERec& out) {
-    if (full) stage_scatter(d, pos, r.p, vb, nvb, sh);
-    stage_wa(d, pos, gam, r.p, vb, nvb, sh);
+    if (full)
+      for (int v = pb; v < V; v += np) stage_scatter(d, pos, r.p, v, V, sh);
+    for (int v = pb; v < V; v += np) stage_wa(d, pos, gam, r.p, v, V, sh);
     if (!sync()) return false;
+    mark(PC_SCATTER_WA);
     if (full) {
-      stage_prep(d, r.p, nvb, vb, nvb, sh);
+      for (int v = pb; v < V; v += np) stage_prep(d, r.p, V, v, V, sh);
       if (!sync()) return false;
+      mark(PC_PREP);
       for (int st = 0; st < 4; ++st) {
-        stage_dct(d, st, large, r.p, vb, nvb, gsm, sh);
+        for (int v = pb; v < V; v += np) stage_dct_t<LARGE>(d, st, r.p, v, V, gsm, sh);
         if (!sync()) return false;
       }
+      mark(PC_DCT);
       for (int f = 0; f < d.K; ++f) {
         const double e = rsum(SLOT_ENERGY + f);
         const long long ov = risum(IS_OVERFLOW + f);
@@ -135,9 +170,14 @@ struct Ctx {
       out.value = value;
     }
     __syncthreads();
-    if (full) stage_gather(d, pos, r.p, vb, nvb, sh);
-    stage_combine(d, coef, g, r.p, vb, nvb, sh, kkt_pos);
+    // gather and combine of one virtual block run back to back: the same
+    // thread produces and consumes each object's raw field gradient
+    for (int v = pb; v < V; v += np) {
+      if (full) stage_gather(d, pos, r.p, v, V, sh);
+      stage_combine(d, coef, g, r.p, v, V, sh, kkt_pos);
+    }
     if (!sync()) return false;
+    mark(PC_GATHER);
     for (int f = 0; f < d.K; ++f) {
       const double a = rsum(SLOT_RAWL1 + f);
       const double b = rsum(SLOT_FORCE + f);
@@ -206,12 +246,13 @@ __device__ int checked_dev(const ERec& e) {
   if (e.bad != 0x7fffffffffffffffll) return TEXO_GP_ERR_NONFINITE_GRADIENT;
   return TEXO_GP_OK;
 }
-__device__ int update_multipliers_dev(DevRun& S, const ERec& e) {
+// update_density_multipliers + next_multiplier_step (eplace.rs:1234-1298)
+__device__ int update_multipliers_dev(DevRun& S) {
   for (int f = 0; f < S.K; ++f)
-    if (!isfinite(e.energy[f]) || !(S.e0[f] > 0.0)) return TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
+    if (!isfinite(S.cur_energy[f]) || !(S.e0[f] > 0.0)) return TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
   double sg[kMaxFields], nn = 0.0;
   for (int f = 0; f < S.K; ++f) {
-    const double ne = e.energy[f] / S.e0[f];
+    const double ne = S.cur_energy[f] / S.e0[f];
     sg[f] = ne + 0.5 * S.beta * ne * ne;
     if (!isfinite(sg[f]) || sg[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
     nn += sg[f] * sg[f];
@@ -226,7 +267,7 @@ __device__ int update_multipliers_dev(DevRun& S, const ERec& e) {
   }
   double en = 0.0;
   for (int f = 0; f < S.K; ++f) {
-    const double ne = e.energy[f] / S.e0[f];
+    const double ne = S.cur_energy[f] / S.e0[f];
     en += ne * ne;
   }
   const double lg = log(S.beta * sqrt(en) + 1.0);
@@ -259,9 +300,12 @@ struct StepVars {
   unsigned trials;
   int pending_best, pending_prev;
 };
-enum { ACT_NONE = 0, ACT_RESTART, ACT_CONTINUE, ACT_ACCEPT, ACT_STATIONARY, ACT_ERROR };
+enum { ACT_NONE = 0, ACT_RESTART, ACT_CONTINUE, ACT_ACCEPT, ACT_STATIONARY };
 
-__global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buffers B, DevRun* run, GridBarrier* bar) {
+// The placement loop of one instance, run by its np physical blocks.
+template <bool LARGE>
+__device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B, DevRun* run, GridBarrier* bar, int pb,
+                         int np, int Vn) {
   __shared__ DevRun S;
   __shared__ ERec eo, ey, ec;
   __shared__ StepVars V;
@@ -271,25 +315,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
   __shared__ long long rl[kThreads / 32];
   __shared__ double coef[kMaxFields];
   __shared__ unsigned gen;
+  __shared__ unsigned long long clock[10];
   if (threadIdx.x == 0) {
     S = *run;
     gen = *(volatile unsigned*)&bar->gen;
     V.pending_best = 0;
     V.pending_prev = 0;
+    for (int i = 0; i < 10; ++i) clock[i] = 0;
+    clock[8] = now_ns();
   }
   __syncthreads();
-  const bool large = (long long)((d.g.Wb + 31) / 32) * ((d.g.Hb + 31) / 32) >= 1024;
-  Ctx c{d, r, B, S, bar, &gen, gsm, sh, rd, rl, coef, (int)blockIdx.x, (int)gridDim.x, large, 0ull};
+  Ctx<LARGE> c{d, r, B, S, bar, &gen, gsm, sh, rd, rl, coef, pb, np, Vn, 0ull, clock};
   const int n = d.nobj;
   unsigned done = 0;
   bool ok = true;
 
 #define T0 if (threadIdx.x == 0)
-#define SYNC_OR_EXIT \
-  if (!c.sync()) {   \
-    ok = false;      \
-    goto out;        \
-  }
+#define VLOOP for (int v = c.pb; v < c.V; v += c.np)
+#define SYNC_OR_EXIT(cat) \
+  if (!c.sync()) {        \
+    ok = false;           \
+    goto out;             \
+  }                       \
+  c.mark(cat);
 #define FAIL(code)            \
   {                           \
     T0 {                      \
@@ -304,17 +352,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
   if (S.phase == 0) {
     // initial probe at the ePlace gamma base, then at the adaptive gamma with
     // the density side reused (same coordinates), eplace.rs:455-471
-    stage_init(d, c.vb, c.nvb, true, true);
-    SYNC_OR_EXIT
+    VLOOP stage_init(d, v, c.V, true, true);
+    SYNC_OR_EXIT(PC_PRECOND)
     if (!c.eval_tail(c.X(), c.gX(), S.gamma_base, true, nullptr, eo)) {
       ok = false;
       goto out;
     }
     {
-      int st = 0;
-      double g0 = 0.0;
       T0 {
-        st = validate_initial_dev(S, eo);
+        double g0 = 0.0;
+        int st = validate_initial_dev(S, eo);
         if (!st) st = adaptive_gamma_dev(S, eo.overflow, g0);
         S.status = st;
         S.gamma = g0;
@@ -323,8 +370,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
       __syncthreads();
       if (S.status) FAIL(S.status)
     }
-    stage_init(d, c.vb, c.nvb, false, true);
-    SYNC_OR_EXIT
+    VLOOP stage_init(d, v, c.V, false, true);
+    SYNC_OR_EXIT(PC_PRECOND)
     if (!c.eval_tail(c.X(), c.gX(), S.gamma, false, nullptr, eo)) {
       ok = false;
       goto out;
@@ -342,6 +389,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
         S.phase = 2;
         S.converged = 1;
       } else if (!st) {
+        // initial_density_multiplier (eplace.rs:1126-1148)
         double dens = 0.0;
         for (int f = 0; f < S.K; ++f) dens += eo.rawl1[f];
         const double m0 = (eo.wal1 == 0.0 || dens == 0.0) ? 1.0 : S.init_weight * eo.wal1 / dens;
@@ -371,7 +419,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
       } else if (S.budget && done >= S.budget) {
         V.action = ACT_CONTINUE;   // leave with the loop still running
       } else {
-        double gam;
+        double gam = 0.0;
         const int st = adaptive_gamma_dev(S, S.cur_overflow, gam);
         if (st) {
           S.status = st;
@@ -399,11 +447,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
     // when the device already holds it for these coordinates.
     {
       const bool full = !S.density_at_x;
-      stage_precond(d, S.lambda, r.p, c.vb, c.nvb, sh);
+      VLOOP {
+        stage_precond(d, S.lambda, r.p, v, c.V, sh);
+        stage_init(d, v, c.V, full, true);
+      }
       if (V.pending_best) c.copy(B.best, c.X(), d.U);
       if (V.pending_prev) c.copy(c.Xp(), c.X(), n);
-      stage_init(d, c.vb, c.nvb, full, true);
-      SYNC_OR_EXIT
+      SYNC_OR_EXIT(PC_PRECOND)
       const double pmin = c.rmin(MS_PMIN), pmax = c.rmax(MS_PMAX);
       const long long pbad = c.risum(IS_PBAD);
       T0 {
@@ -437,16 +487,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
       T0 {
         const double m = V.restart ? 1.0 : S.a;
         const double s = sqrt(1.0 + 4.0 * m * m);
-        V.next_m = fabs(s) <= 8.0e307 ? (1.0 + s) / 2.0 : 0.5 + s / 2.0;
+        V.next_m = fabs(s) <= 8.0e307 ? (1.0 + s) / 2.0 : 0.5 + s / 2.0;   // f64::midpoint(1, s)
         if (!isfinite(V.next_m)) S.status = TEXO_GP_ERR_ITERATION_OVERFLOW;
       }
       __syncthreads();
       if (S.status) FAIL(S.status)
       if (!V.restart) {
-        const double m = S.a;
-        stage_extrapolate(d, c.X(), c.Xp(), (float)((m - 1.0) / V.next_m), c.Y(), r.p, c.vb, c.nvb, sh);
-        stage_init(d, c.vb, c.nvb, true, true);
-        SYNC_OR_EXIT
+        const float e = (float)((S.a - 1.0) / V.next_m);
+        VLOOP {
+          stage_extrapolate(d, c.X(), c.Xp(), e, c.Y(), r.p, v, c.V, sh);
+          stage_init(d, v, c.V, true, true);
+        }
+        SYNC_OR_EXIT(PC_EXTRAP)
         const long long diff = c.risum(IS_DIFF);
         T0 V.y_is_origin = diff == 0;
         __syncthreads();
@@ -510,11 +562,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
           __syncthreads();
           if (S.status) FAIL(S.status)
           if (V.action == ACT_CONTINUE) continue;
-          stage_candidate(d, ybuf, gy, (float)(1.0 / V.tL), c.C(), r.p, c.vb, c.nvb, sh, c.X());
-          stage_init(d, c.vb, c.nvb, true, true);
-          SYNC_OR_EXIT
+          const float invL = (float)(1.0 / V.tL);
+          VLOOP {
+            stage_candidate(d, ybuf, gy, invL, c.C(), r.p, v, c.V, sh, c.X());
+            stage_init(d, v, c.V, true, true);
+          }
+          SYNC_OR_EXIT(PC_CANDIDATE)
           const long long changed = c.risum(IS_DIFF);
-          const double dot = c.rsum(SLOT_DOT), msn = c.rsum(SLOT_MSN), change = c.rmax(MS_CHANGE);
+          const double dot = c.rsum(SLOT_DOT), msn = c.rsum(SLOT_MSN);
           T0 {
             V.action = ACT_NONE;
             if (changed == 0) {
@@ -535,6 +590,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
             }
           }
           __syncthreads();
+          if (V.action == ACT_CONTINUE) continue;
           if (V.action != ACT_NONE) break;
           if (!c.eval_tail(c.C(), c.gC(), S.gamma, true, c.C(), ec)) {
             ok = false;
@@ -551,7 +607,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
               V.action = ACT_ACCEPT;
               if (!isfinite(ec.kkt)) S.status = TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
               S.last_objective = ec.value;
-              (void)change;
             } else if (smooth && !V.restart) {
               V.restart = 1;
               V.has_wL = 1;
@@ -608,7 +663,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
         S.best_tot = tot;
         V.pending_best = 1;
       }
-      V.action = ACT_NONE;
       if (stop_dev(S, S.cur_overflow)) {
         S.converged = 1;
         S.phase = 2;
@@ -620,18 +674,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
     if (S.phase == 2) break;
     if (V.stationary) {
       // stationary_target_is_fixed (eplace.rs:973-985): compare rounded targets
-      long long mism = 0;
       const float2* x = c.X();
-      for (int u = c.vb * blockDim.x + threadIdx.x; u < d.U; u += c.nvb * blockDim.x) {
-        const float2 a = x[u];
-        const uint32_t tx = (uint32_t)fminf(fmaxf(roundf(a.x), 0.f), (float)(S.W - 1));
-        const uint32_t ty = (uint32_t)fminf(fmaxf(roundf(a.y), 0.f), (float)(S.H - 1));
-        mism += (B.prev_targets[2 * u] != tx) + (B.prev_targets[2 * u + 1] != ty);
-        B.prev_targets[2 * u] = tx;
-        B.prev_targets[2 * u + 1] = ty;
+      VLOOP {
+        long long mism = 0;
+        for (int u = v * blockDim.x + threadIdx.x; u < d.U; u += c.V * blockDim.x) {
+          const float2 a = x[u];
+          const uint32_t tx = (uint32_t)fminf(fmaxf(roundf(a.x), 0.f), (float)(S.W - 1));
+          const uint32_t ty = (uint32_t)fminf(fmaxf(roundf(a.y), 0.f), (float)(S.H - 1));
+          mism += (B.prev_targets[2 * u] != tx) + (B.prev_targets[2 * u + 1] != ty);
+          B.prev_targets[2 * u] = tx;
+          B.prev_targets[2 * u + 1] = ty;
+        }
+        write_partial(mism, islot(r.p, IS_DIFF), v, sh.l);
       }
-      write_partial(mism, islot(r.p, IS_DIFF), c.vb, sh.l);
-      SYNC_OR_EXIT
+      SYNC_OR_EXIT(PC_OTHER)
       const long long total = c.risum(IS_DIFF);
       T0 {
         const bool fixed = S.have_prev_stationary && total == 0;
@@ -646,9 +702,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_persistent(Dev d, Reduce r, Buf
       if (S.phase == 2) break;
     }
     T0 {
-      ERec tmp;
-      for (int f = 0; f < S.K; ++f) tmp.energy[f] = S.cur_energy[f];
-      const int st = update_multipliers_dev(S, tmp);
+      const int st = update_multipliers_dev(S);
       if (st) {
         S.status = st;
         S.phase = 2;
@@ -665,32 +719,55 @@ out:
     if (V.pending_prev) c.copy(c.Xp(), c.X(), n);
     ok = c.sync();
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (pb == 0 && threadIdx.x == 0) {
     S.barriers += c.nbar;
+    for (int i = 0; i < 8; ++i) S.phase_ns[i] += clock[i];
+    S.barrier_wait_ns += clock[9];
     *run = S;
   }
 #undef T0
+#undef VLOOP
 #undef SYNC_OR_EXIT
 #undef FAIL
 }
 
-int persistent_blocks_per_sm() {
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent, kThreads, 0) != cudaSuccess) return 0;
-  return n;
+template <bool LARGE>
+__global__ void __launch_bounds__(kThreads, 2)
+    k_persistent(Dev d, Reduce r, Buffers B, DevRun* run, GridBarrier* bar, int V) {
+  run_body<LARGE>(d, r, B, run, bar, (int)blockIdx.x, (int)gridDim.x, V);
 }
 
+// Many instances in one launch: block b serves instance map[b].x as its
+// physical block map[b].y of map[b].z.
+template <bool LARGE>
+__global__ void __launch_bounds__(kThreads, 2) k_batch(const InstDesc* descs, const int4* map) {
+  __shared__ InstDesc sd;
+  const int4 m = map[blockIdx.x];
+  if (threadIdx.x == 0) sd = descs[m.x];
+  __syncthreads();
+  run_body<LARGE>(sd.d, sd.r, sd.B, sd.run, sd.bar, m.y, m.z, sd.V);
+}
+
+int persistent_blocks_per_sm() {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_persistent<false>, kThreads, 0) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<true>, kThreads, 0) != cudaSuccess) return 0;
+  return a < b ? a : b;
+}
+
+static bool large_tiles(const Dev& d) { return (long long)((d.g.Wb + 31) / 32) * ((d.g.Hb + 31) / 32) >= 1024; }
+
 int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRun* run_dev, DevRun* host_run,
-                          GridBarrier* bar, int blocks, cudaStream_t s) {
+                          GridBarrier* bar, int blocks, int V, cudaStream_t s) {
   if (cudaMemcpyAsync(run_dev, host_run, sizeof(DevRun), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return TEXO_GP_ERR_CUDA;
   if (cudaMemsetAsync(bar, 0, sizeof(GridBarrier), s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
   Dev dd = d;
   Reduce rr = r;
   Buffers bb = b;
-  void* args[] = {&dd, &rr, &bb, &run_dev, &bar};
-  if (cudaLaunchCooperativeKernel((const void*)k_persistent, dim3(blocks), dim3(kThreads), args, 0, s) != cudaSuccess)
-    return TEXO_GP_ERR_CUDA;
+  void* args[] = {&dd, &rr, &bb, &run_dev, &bar, &V};
+  const void* fn = large_tiles(d) ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+  if (cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads), args, 0, s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
   note_launch();
   GridBarrier hb;
   if (cudaMemcpyAsync(host_run, run_dev, sizeof(DevRun), cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -699,6 +776,14 @@ int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRu
     return TEXO_GP_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
   if (hb.error) return TEXO_GP_ERR_DEVICE_TIMEOUT;
+  return TEXO_GP_OK;
+}
+
+int32_t launch_batch(const InstDesc* descs_dev, const int4* map_dev, int blocks, bool large, cudaStream_t s) {
+  void* args[] = {(void*)&descs_dev, (void*)&map_dev};
+  const void* fn = large ? (const void*)k_batch<true> : (const void*)k_batch<false>;
+  if (cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads), args, 0, s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
+  note_launch();
   return TEXO_GP_OK;
 }
 

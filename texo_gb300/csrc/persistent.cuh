@@ -5,12 +5,17 @@
 
 namespace tgp {
 
-// Grid barrier words (device memory, zeroed before each launch).
-struct GridBarrier {
+// Grid barrier words (device memory, zeroed before each launch): an arrival
+// counter and, on its own 128-byte line, the generation every waiter polls.
+struct alignas(128) BarrierLine {
   unsigned int count;
-  unsigned int gen;
-  int error;          // 1 when a bounded wait ran out
-  int pad;
+  unsigned int pad[31];
+};
+struct GridBarrier {
+  BarrierLine root;                         // arrivals
+  unsigned int gen;                         // generation
+  int error;                                // 1 when a bounded wait ran out
+  unsigned int pad[30];
 };
 
 // Controller state of one placement, shared between the host and the
@@ -43,8 +48,23 @@ struct DevRun {
   int igx, igy, igc;
   // statistics
   unsigned long long evaluations, trials, barriers;
+  // grid-wide phase times seen by block 0 (ns): see PhaseClock
+  unsigned long long phase_ns[8];
+  unsigned long long barrier_wait_ns;
   // per call
   unsigned budget;
+};
+
+// Phase categories of DevRun::phase_ns.
+enum PhaseClock {
+  PC_SCATTER_WA = 0,   // scatter + WA (or WA alone) up to its barrier
+  PC_PREP = 1,
+  PC_DCT = 2,          // the four transform GEMMs
+  PC_GATHER = 3,       // gather + combine
+  PC_PRECOND = 4,      // preconditioner / init / copies
+  PC_EXTRAP = 5,       // extrapolation + init
+  PC_CANDIDATE = 6,    // candidate + init
+  PC_OTHER = 7
 };
 
 struct Buffers {
@@ -54,10 +74,25 @@ struct Buffers {
   uint32_t* prev_targets;
 };
 
-// Launches the persistent kernel for up to `budget` iterations; run lives in
-// device memory and is copied to/from host_run around the launch.
+// One instance of a batched launch (device memory).
+struct InstDesc {
+  Dev d;
+  Reduce r;
+  Buffers B;
+  DevRun* run;
+  GridBarrier* bar;
+  int V;      // virtual blocks
+  int pad;
+};
+
+// Launches the persistent kernel for up to host_run->budget iterations on
+// `blocks` physical blocks over V virtual blocks; run lives in device memory
+// and is copied to/from host_run around the launch.
 int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRun* run_dev, DevRun* host_run,
-                          GridBarrier* bar, int blocks, cudaStream_t s);
+                          GridBarrier* bar, int blocks, int V, cudaStream_t s);
+// Launches every instance of descs_dev at once; map_dev[b] = (instance,
+// physical block, physical block count, 0). Asynchronous.
+int32_t launch_batch(const InstDesc* descs_dev, const int4* map_dev, int blocks, bool large, cudaStream_t s);
 int persistent_blocks_per_sm();
 
 }  // namespace tgp

@@ -441,40 +441,118 @@ __device__ void gemm_tiles(const float* A, long sa, const float* Bm, long sb, fl
   __syncthreads();
 }
 
-// Small-grid and large-grid tile shapes.
-using SmemS = GemmSmem<32, 32, 32, 2, 2>;
+// Small grids: 16x16 output tiles, one output per thread, K in slabs of
+// 128 staged whole in shared memory. A 256x256 transform then has 256 tiles,
+// enough to occupy every SM, where 32x32 tiles left most SMs idle.
+constexpr int kT16Slab = 128;
+constexpr int kT16Pad = kT16Slab + 4;   // float4-aligned rows; 8-thread phases stay conflict-free
+struct Smem16 {
+  float a[16][kT16Pad];    // A panel, rows m, k contiguous
+  float bt[16][kT16Pad];   // B panel transposed, rows n, k contiguous
+};
+
+static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb, float* Cm, long sc, int M, int N,
+                              int Kd, int nf, int epi, const float* inv_eig, const float* rho, double* energy_acc,
+                              int vb, int nvb, Smem16& sm) {
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int tiles_m = (M + 15) / 16, tiles_n = (N + 15) / 16;
+  const int tiles = tiles_m * tiles_n * nf;
+  // slab-load roles: A element (row ra + 2j, column ca), B element (row rb + 16j, column cb)
+  const int ca = threadIdx.x & (kT16Slab - 1), ra = threadIdx.x / kT16Slab;
+  const int cb = threadIdx.x & 15, rb = threadIdx.x >> 4;
+  for (int t = vb; t < tiles; t += nvb) {
+    const int f = t / (tiles_m * tiles_n);
+    const int r = t % (tiles_m * tiles_n);
+    const int m0 = (r / tiles_n) * 16, n0 = (r % tiles_n) * 16;
+    const float* Af = A + f * sa;
+    const float* Bf = Bm + f * sb;
+    float sum = 0.f, comp = 0.f;
+    for (int k0 = 0; k0 < Kd; k0 += kT16Slab) {
+      const int kn = min(kT16Slab, Kd - k0);
+      float va[8], vbv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int gm = m0 + ra + 2 * j;
+        va[j] = (gm < M && ca < kn) ? Af[(size_t)gm * Kd + k0 + ca] : 0.f;
+        const int kk = rb + 16 * j, gn = n0 + cb;
+        vbv[j] = (kk < kn && gn < N) ? Bf[(size_t)(k0 + kk) * N + gn] : 0.f;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        sm.a[ra + 2 * j][ca] = va[j];
+        sm.bt[cb][rb + 16 * j] = vbv[j];
+      }
+      __syncthreads();
+      const float4* a4 = reinterpret_cast<const float4*>(sm.a[ty]);
+      const float4* b4 = reinterpret_cast<const float4*>(sm.bt[tx]);
+#pragma unroll 4
+      for (int kc = 0; kc < kT16Slab / 4; kc += kChunk / 4) {
+        float part = 0.f;
+#pragma unroll
+        for (int q = 0; q < kChunk / 4; ++q) {
+          const float4 x = a4[kc + q], y = b4[kc + q];
+          part = fmaf(x.x, y.x, part);
+          part = fmaf(x.y, y.y, part);
+          part = fmaf(x.z, y.z, part);
+          part = fmaf(x.w, y.w, part);
+        }
+        two_sum_acc(sum, comp, part);
+      }
+    }
+    const int gm = m0 + ty, gn = n0 + tx;
+    if (gm < M && gn < N) {
+      const size_t idx = (size_t)gm * N + gn;
+      float v = __fadd_rn(sum, comp);
+      if (epi == 1) v *= inv_eig[idx];
+      Cm[f * sc + idx] = v;
+      if (epi == 2) energy_acc[f] += (double)(rho[(size_t)f * M * N + idx] * v);
+    }
+  }
+  __syncthreads();
+}
+
+// Large-grid tile shape (register-blocked) and the small-grid one.
 using SmemL = GemmSmem<64, 64, 16, 4, 4>;
-union GemmShared {
-  SmemS s;
+union alignas(16) GemmShared {
+  Smem16 s;
   SmemL l;
 };
 
-__device__ __forceinline__ void gemm_any(bool large, const float* A, long sa, const float* Bm, long sb, float* Cm,
-                                         long sc, int M, int N, int Kd, int nf, int epi, const float* inv_eig,
-                                         const float* rho, double* eacc, int vb, int nvb, GemmShared& sm) {
-  if (large)
+template <bool LARGE>
+__device__ __forceinline__ void gemm_any(const float* A, long sa, const float* Bm, long sb, float* Cm, long sc, int M,
+                                         int N, int Kd, int nf, int epi, const float* inv_eig, const float* rho,
+                                         double* eacc, int vb, int nvb, GemmShared& sm) {
+  if (LARGE)
     gemm_tiles<64, 64, 16, 4, 4>(A, sa, Bm, sb, Cm, sc, M, N, Kd, nf, epi, inv_eig, rho, eacc, vb, nvb, sm.l);
   else
-    gemm_tiles<32, 32, 32, 2, 2>(A, sa, Bm, sb, Cm, sc, M, N, Kd, nf, epi, inv_eig, rho, eacc, vb, nvb, sm.s);
+    gemm16(A, sa, Bm, sb, Cm, sc, M, N, Kd, nf, epi, inv_eig, rho, eacc, vb, nvb, sm.s);
 }
 
 // The four transforms of the spectral solve (Poisson2d::solve,
 // electrostatic_placement.rs:725-776) as dense GEMMs:
 //   t1 = rho Cx^T ; t2 = (Cy t1) o inv_eig ; t1 = Cy^T t2 ; phi = t1 Cx.
 // `step` selects one of the four (a grid barrier separates them).
-static __device__ void stage_dct(const Dev& d, int step, bool large, Partials p, int vb, int nvb, GemmShared& sm,
-                                 Shared& sh) {
+template <bool LARGE>
+static __device__ void stage_dct_t(const Dev& d, int step, Partials p, int vb, int nvb, GemmShared& sm, Shared& sh) {
   const int W = d.g.Wb, H = d.g.Hb;
   const long sg = d.B;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
   switch (step) {
-    case 0: gemm_any(large, d.rho, sg, d.CxT, 0, d.t1, sg, H, W, W, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
-    case 1: gemm_any(large, d.Cy, 0, d.t1, sg, d.t2, sg, H, W, H, d.K, 1, d.inv_eig, nullptr, eacc, vb, nvb, sm); break;
-    case 2: gemm_any(large, d.CyT, 0, d.t2, sg, d.t1, sg, H, W, H, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
-    default: gemm_any(large, d.t1, sg, d.Cx, 0, d.phi, sg, H, W, W, d.K, 2, nullptr, d.rho, eacc, vb, nvb, sm); break;
+    case 0: gemm_any<LARGE>(d.rho, sg, d.CxT, 0, d.t1, sg, H, W, W, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
+    case 1: gemm_any<LARGE>(d.Cy, 0, d.t1, sg, d.t2, sg, H, W, H, d.K, 1, d.inv_eig, nullptr, eacc, vb, nvb, sm); break;
+    case 2: gemm_any<LARGE>(d.CyT, 0, d.t2, sg, d.t1, sg, H, W, H, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm); break;
+    default: gemm_any<LARGE>(d.t1, sg, d.Cx, 0, d.phi, sg, H, W, W, d.K, 2, nullptr, d.rho, eacc, vb, nvb, sm); break;
   }
   if (step == 3)
     for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), vb, sh.d);
+}
+__device__ __forceinline__ void stage_dct(const Dev& d, int step, bool large, Partials p, int vb, int nvb,
+                                          GemmShared& sm, Shared& sh) {
+  if (large)
+    stage_dct_t<true>(d, step, p, vb, nvb, sm, sh);
+  else
+    stage_dct_t<false>(d, step, p, vb, nvb, sm, sh);
 }
 
 // ---------------------------------------------------------------------------

@@ -49,6 +49,61 @@ def place(problem, params=None):
     return targets.reshape(-1, 2), coords, _stats_dict(st)
 
 
+class Batch:
+    """Many resident placements advanced together (texo_gp_batch)."""
+
+    def __init__(self, params=None, hbm_budget=64 << 30, max_slots=256):
+        self.lib = abi.load()
+        self.params = params or default_params()
+        h = C.c_void_p()
+        abi.check(self.lib.texo_gp_batch_create(C.byref(self.params), hbm_budget, max_slots, C.byref(h)),
+                  "texo_gp_batch_create")
+        self.h = h
+        self._units = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.texo_gp_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def admit(self, problem, job_id, params=None):
+        """Returns True when admitted, False when the batch is full (slots or HBM budget)."""
+        pc = problem.c_struct()
+        slot = C.c_uint32()
+        pp = C.byref(params) if params is not None else None
+        code = self.lib.texo_gp_batch_admit(self.h, C.byref(pc), pp, job_id, C.byref(slot))
+        if code == abi.CODE["BUSY"]:
+            return False
+        abi.check(code, "texo_gp_batch_admit")
+        self._units[job_id] = problem.num_units
+        return True
+
+    def advance(self, iterations):
+        abi.check(self.lib.texo_gp_batch_advance(self.h, iterations), "texo_gp_batch_advance")
+
+    def retire(self):
+        """Pops one finished job: (job_id, targets [U,2], stats) or None."""
+        cap = max(self._units.values()) * 2 if self._units else 0
+        targets = np.zeros(max(cap, 2), np.uint32)
+        jid = C.c_uint64()
+        st = abi.Stats()
+        code = self.lib.texo_gp_batch_retire(self.h, C.byref(jid), abi.ptr(targets, C.c_uint32), targets.size,
+                                            C.byref(st))
+        if code == abi.CODE["BUSY"]:
+            return None
+        if code not in (0, abi.CODE["DID_NOT_CONVERGE"]):
+            abi.check(code, "texo_gp_batch_retire")
+        u = self._units.pop(jid.value)
+        return jid.value, targets[:2 * u].reshape(-1, 2).copy(), _stats_dict(st)
+
+    def counts(self):
+        r, f, b = C.c_uint32(), C.c_uint32(), C.c_uint64()
+        abi.check(self.lib.texo_gp_batch_counts(self.h, C.byref(r), C.byref(f), C.byref(b)), "texo_gp_batch_counts")
+        return r.value, f.value, b.value
+
+
 class Placer:
     """A device-resident placement instance (texo_gp_handle)."""
 
@@ -151,6 +206,14 @@ class Placer:
         out = C.c_double()
         abi.check(self.lib.texo_gp_hpwl(self.h, abi.ptr(coords, C.c_double), C.byref(out)), "texo_gp_hpwl")
         return out.value
+
+    def device_profile(self):
+        """Phase times of the persistent engine (microseconds) and barrier counts."""
+        out = np.zeros(10)
+        abi.check(self.lib.texo_gp_device_profile(self.h, abi.ptr(out, C.c_double)), "texo_gp_device_profile")
+        names = ["scatter_wa", "prep", "dct", "gather_combine", "precond_init", "extrapolate", "candidate",
+                 "other", "barrier_wait", "barriers"]
+        return dict(zip(names, out.tolist()))
 
     def stage_times(self, reps=20):
         ms = np.zeros(64)
