@@ -519,7 +519,7 @@ struct Controller {
           if (!std::isfinite(tL)) return TEXO_GP_ERR_LINE_SEARCH_OVERFLOW;
           continue;
         }
-        launch_candidate(D, I.r, ybuf, gy, (float)(1.0 / tL), I.bufC, nvb, s);
+        launch_candidate(D, I.r, ybuf, gy, (float)std::fmin(1.0 / tL, 3.0e38), I.bufC, nvb, s);
         launch_finalize(D, I.r, nvb, FIN_CAND, s);
         // The candidate is evaluated speculatively in the same submission;
         // it is discarded when the candidate equals y.

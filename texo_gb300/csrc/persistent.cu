@@ -562,7 +562,9 @@ __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B, DevRun
           __syncthreads();
           if (S.status) FAIL(S.status)
           if (V.action == ACT_CONTINUE) continue;
-          const float invL = (float)(1.0 / V.tL);
+          // 1/L saturates at FLT_MAX: a huge step clamps to the box as it
+          // does in FP64, where an infinite one would turn 0 * inf into NaN
+          const float invL = (float)fmin(1.0 / V.tL, 3.0e38);
           VLOOP {
             stage_candidate(d, ybuf, gy, invL, c.C(), r.p, v, c.V, sh, c.X());
             stage_init(d, v, c.V, true, true);

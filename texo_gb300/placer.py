@@ -93,10 +93,15 @@ class Batch:
                                             C.byref(st))
         if code == abi.CODE["BUSY"]:
             return None
-        if code not in (0, abi.CODE["DID_NOT_CONVERGE"]):
+        if code in (abi.CODE["CUDA"], abi.CODE["INVALID_ARGUMENT"], abi.CODE["DEVICE_TIMEOUT"]):
             abi.check(code, "texo_gp_batch_retire")
         u = self._units.pop(jid.value)
-        return jid.value, targets[:2 * u].reshape(-1, 2).copy(), _stats_dict(st)
+        stats = _stats_dict(st)
+        if code not in (0, abi.CODE["DID_NOT_CONVERGE"]):
+            # the job failed with a placement error (a reference error variant)
+            stats["status"] = abi.STATUS.get(code, code)
+            return jid.value, None, stats
+        return jid.value, targets[:2 * u].reshape(-1, 2).copy(), stats
 
     def counts(self):
         r, f, b = C.c_uint32(), C.c_uint32(), C.c_uint64()
