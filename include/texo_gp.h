@@ -273,6 +273,24 @@ int32_t texo_gp_scatter(texo_gp_handle h, const double* coordinates,
  * grid with the handle's DCT mode: writes potential [bins], returns energy. */
 int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potential,
                         double* energy);
+/* texo_gp_scatter without allocating: the same grids, bit for bit, computed in
+ * one file-scope device scratch array (4 MiB per device) instead of the
+ * handle's buffers. It calls no cudaMalloc/cudaFree and allocates no host
+ * memory, and it leaves the handle's buffers and resumable run state as they
+ * were. For callers that may not allocate: a serving loop whose HBM budget is
+ * fully committed to admitted jobs, where a new device allocation could fail
+ * or take memory the budget promised to a job, and where cudaFree's implicit
+ * device synchronization would stall the jobs running on other streams.
+ * Limits: num_fields * bins <= 131072 and units + fillers <= 131072, else
+ * TEXO_GP_ERR_UNSUPPORTED (texo_gp_last_error says which). Nothing has to be
+ * zero beforehand; the call initializes every scratch word it reads. The
+ * first call on a device looks up the scratch address (cudaGetSymbolAddress)
+ * with that device current; make that call before any stream capture. Calls
+ * that overlap on one device (two threads, or two handles) race on the shared
+ * scratch; calls made one after another are safe (each call synchronizes
+ * before returning). No counterpart in the reference. */
+int32_t texo_gp_scatter_static(texo_gp_handle h, const double* coordinates,
+                               int64_t* physical_grid, int64_t* filler_grid);
 
 /* Runs the placement loop from the handle's current state (the initial
  * coordinates after create) to convergence, the iteration cap, or

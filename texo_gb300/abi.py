@@ -152,6 +152,7 @@ SIGNATURES = {
     "texo_gp_evaluate": (C.c_int32, [_P, c_f64p, C.c_double, C.POINTER(Eval), c_f64p, c_f64p, c_f64p, c_f64p]),
     "texo_gp_scatter": (C.c_int32, [_P, c_f64p, c_i64p, c_i64p]),
     "texo_gp_poisson": (C.c_int32, [_P, c_f64p, c_f64p, c_f64p]),
+    "texo_gp_scatter_static": (C.c_int32, [_P, c_f64p, c_i64p, c_i64p]),
     "texo_gp_run": (C.c_int32, [_P, C.c_uint32, c_u32p, c_f64p, C.POINTER(Stats)]),
     "texo_gp_reset": (C.c_int32, [_P]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),

@@ -833,6 +833,8 @@ bool handle_finished(texo_gp_handle_s* h) { return h->ctl->phase == 2; }
 uint64_t handle_bytes(texo_gp_handle_s* h) { return h->inst->bytes; }
 int handle_virtual_blocks(texo_gp_handle_s* h) { return h->inst->nvb; }
 int handle_sms(texo_gp_handle_s* h) { return h->inst->sms; }
+Instance* handle_instance(texo_gp_handle_s* h) { return h->inst.get(); }
+std::mutex* handle_mutex(texo_gp_handle_s* h) { return &h->mu; }
 }  // namespace tgp
 
 namespace {

@@ -1,6 +1,7 @@
 // engine.h — host-side model of one placement instance and its device state.
 #pragma once
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -107,4 +108,6 @@ bool handle_finished(texo_gp_handle_s* h);
 uint64_t handle_bytes(texo_gp_handle_s* h);
 int handle_virtual_blocks(texo_gp_handle_s* h);
 int handle_sms(texo_gp_handle_s* h);
+Instance* handle_instance(texo_gp_handle_s* h);
+std::mutex* handle_mutex(texo_gp_handle_s* h);
 }  // namespace tgp
