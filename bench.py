@@ -218,10 +218,14 @@ def run_batched(jobs, chunk=20, device=0):
     t0 = time.perf_counter()
     for i, (p, prm) in enumerate(jobs):
         assert b.admit(p, i, prm)
+    t_admit = time.perf_counter() - t0
     results = {}
     launches = 0
+    t_adv = 0.0
     while len(results) < len(jobs):
+        ta = time.perf_counter()
         b.advance(chunk)
+        t_adv += time.perf_counter() - ta
         launches += 1
         while True:
             r = b.retire()
@@ -229,7 +233,9 @@ def run_batched(jobs, chunk=20, device=0):
                 break
             results[r[0]] = r[2]
     torch.cuda.synchronize()
-    return time.perf_counter() - t0, results, launches
+    wall = time.perf_counter() - t0
+    b.close()
+    return wall, results, launches, {"admit": t_admit, "advance": t_adv, "retire": wall - t_admit - t_adv}
 
 
 def run_serial(jobs, engine):
@@ -256,7 +262,7 @@ def run_serial(jobs, engine):
 def batch_report(n=64):
     from texo_gb300 import abi
     jobs = batch_workload(n)
-    wall_b, res_b, launches = run_batched(jobs)
+    wall_b, res_b, launches, parts = run_batched(jobs)
     wall_d, res_d = run_serial(batch_workload(n), abi.ENGINE_DEVICE)
     wall_h, res_h = run_serial(batch_workload(n), abi.ENGINE_HOST)
     same = sum(1 for i in range(n) if res_b[i]["hpwl"] == res_d[i]["hpwl"])
@@ -268,7 +274,8 @@ def batch_report(n=64):
             "speedup_vs_serial_host_fp32": wall_h / wall_b, "iterations_per_s_batched": iters / wall_b,
             "batched_launches": launches, "identical_to_alone": "%d/%d" % (same, n), "failed": failed,
             "converged": sum(1 for s in res_b.values() if s["converged"]),
-            "wall_s": {"batched": wall_b, "serial_device": wall_d, "serial_host": wall_h}}
+            "wall_s": {"batched": wall_b, "serial_device": wall_d, "serial_host": wall_h},
+            "batched_wall_split_s": parts}
 
 
 def config_dict(args):

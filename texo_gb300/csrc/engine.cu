@@ -37,24 +37,43 @@ void set_last_error(const std::string& s) { g_last_error = s; }
   } while (0)
 
 Instance::~Instance() {
+  if (stream) cudaStreamSynchronize(stream);
+  for (void* p : allocations) cudaFreeAsync(p, stream);
   if (stream) {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
-  for (void* p : allocations) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
   if (h_iscal) cudaFreeHost(h_iscal);
 }
 
+// Device buffers come from the device's stream-ordered pool (kept, not
+// trimmed, between instances): admitting and retiring many short-lived
+// placements then reuses pooled memory instead of a driver allocation, and
+// its implicit synchronization, per buffer.
 int32_t Instance::alloc(void** p, size_t n) {
-  n = n ? n : 16;
-  CU(cudaMalloc(p, n));
+  n = ((n ? n : 16) + 255) & ~(size_t)255;
+  CU(cudaMallocAsync(p, n, stream));
   allocations.push_back(*p);
   bytes += n;
   return TEXO_GP_OK;
 }
 
 namespace {
+// The default pool of a device keeps freed memory for reuse (once per device).
+cudaError_t keep_pool(int device) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), device) != done.end()) return cudaSuccess;
+  cudaMemPool_t pool;
+  cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = ~0ull;
+  e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e == cudaSuccess) done.push_back(device);
+  return e;
+}
 // Host FP64 coordinates -> device FP32 optimizer buffer.
 int32_t upload_coords(Instance& I, float2* dst, const double* src, size_t nobj) {
   std::vector<float> tmp(2 * nobj);
@@ -89,9 +108,8 @@ std::vector<double> dct_basis(uint32_t n) {
 int32_t Instance::upload() {
   HostModel& h = m;
   CU(cudaSetDevice(device));
-  cudaDeviceProp prop;
-  CU(cudaGetDeviceProperties(&prop, device));
-  sms = prop.multiProcessorCount;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  CU(keep_pool(device));
   CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   const size_t nobj = (size_t)h.U + h.F, B = h.bins(), K = h.K;
   // enough blocks to cover the widest stage, up to 8 per SM
@@ -222,6 +240,9 @@ int32_t Instance::upload() {
   TRY(zeros(*this, &r.p.sum, (size_t)kSlots * kMaxPartials));
   TRY(zeros(*this, &r.p.isum, (size_t)kISlots * kMaxPartials));
   TRY(zeros(*this, &r.p.mx, (size_t)kMSlots * kMaxPartials));
+  TRY(zeros(*this, &r.q.sum, (size_t)kSlots * kMaxPartials));
+  TRY(zeros(*this, &r.q.isum, (size_t)kISlots * kMaxPartials));
+  TRY(zeros(*this, &r.q.mx, (size_t)kMSlots * kMaxPartials));
   TRY(zeros(*this, &r.scal, kScalars));
   TRY(zeros(*this, &r.iscal, kIScalars));
   CU(cudaMallocHost((void**)&h_scal, kScalars * sizeof(double)));

@@ -54,6 +54,7 @@ enum FinalizeMask {
 // One instance's partial buffers and scalar block (device pointers).
 struct Reduce {
   Partials p;
+  Partials q;            // second set: the persistent kernel's loop phases alternate p and q
   double* scal;          // [kScalars]
   long long* iscal;      // [kIScalars]
 };

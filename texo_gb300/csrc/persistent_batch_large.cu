@@ -1,0 +1,17 @@
+// persistent_batch_large.cu — k_batch with large DCT tiles: many placements in one launch;
+// block b serves instance map[b].x as its physical block map[b].y of map[b].z.
+#include "persistent_body.cuh"
+
+namespace tgp {
+
+__global__ void __launch_bounds__(kThreads, 2) k_batch_large(const InstDesc* descs, const int4* map) {
+  __shared__ InstDesc sd;
+  const int4 m = map[blockIdx.x];
+  if (threadIdx.x == 0) sd = descs[m.x];
+  __syncthreads();
+  run_body<true>(sd.d, sd.r, sd.B, sd.run, sd.bar, m.y, m.z, sd.V);
+}
+
+const void* batch_kernel_large() { return (const void*)k_batch_large; }
+
+}  // namespace tgp
