@@ -91,6 +91,27 @@ def stage_bytes(stage, n):
     }.get(stage, 0)
 
 
+def eval_bytes(n):
+    """Algorithmic bytes of one objective evaluation (all its stages)."""
+    st = ["init", "scatter", "wa", "prep", "dct_row_fwd", "dct_col_fwd", "dct_col_inv", "dct_row_inv",
+          "gather", "combine"]
+    return sum(stage_bytes(k, n) for k in st)
+
+
+def ncu_traffic(workload, engine):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary of this workload (a `traffic_bytes_per_launch: N` line), if any."""
+    import re
+    path = os.path.join(ROOT, "profiles", "persistent_%s.txt" % workload if engine == "device"
+                        else "stages_%s.txt" % workload)
+    try:
+        with open(path) as f:
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -238,6 +259,24 @@ def run_batched(jobs, chunk=20, device=0):
     return wall, results, launches, {"admit": t_admit, "advance": t_adv, "retire": wall - t_admit - t_adv}
 
 
+def run_served(jobs, chunk=20, threads=8):
+    """All jobs submitted at once to the serving loop (admission overlaps the
+    device work of the jobs already resident)."""
+    import torch
+    from texo_gb300.placer import Server
+    torch.cuda.synchronize()
+    with Server(chunk_iterations=chunk, admission_threads=threads) as srv:
+        t0 = time.perf_counter()
+        for i, (p, prm) in enumerate(jobs):
+            srv.submit(p, i, prm)
+        results = {}
+        while len(results) < len(jobs):
+            r = srv.poll(wait_ms=-1)
+            results[r[0]] = r[2]
+        wall = time.perf_counter() - t0
+    return wall, results
+
+
 def run_serial(jobs, engine):
     import torch
     from texo_gb300.placer import Placer
@@ -263,19 +302,104 @@ def batch_report(n=64):
     from texo_gb300 import abi
     jobs = batch_workload(n)
     wall_b, res_b, launches, parts = run_batched(jobs)
+    wall_s, res_s = run_served(batch_workload(n))
     wall_d, res_d = run_serial(batch_workload(n), abi.ENGINE_DEVICE)
     wall_h, res_h = run_serial(batch_workload(n), abi.ENGINE_HOST)
     same = sum(1 for i in range(n) if res_b[i]["hpwl"] == res_d[i]["hpwl"])
+    same_s = sum(1 for i in range(n) if res_s[i]["hpwl"] == res_d[i]["hpwl"])
     iters = sum(s["iterations"] for s in res_b.values())
     failed = {i: s["status"] for i, s in res_b.items() if s["status"] not in ("OK", "DID_NOT_CONVERGE")}
-    return {"instances": n, "cells": "log-uniform 1k..40k", "placements_per_s_batched": n / wall_b,
+    return {"instances": n, "cells": "log-uniform 1k..40k", "placements_per_s_served": n / wall_s,
+            "speedup_served_vs_serial_host_fp32": wall_h / wall_s,
+            "served_identical_to_alone": "%d/%d" % (same_s, n), "placements_per_s_batched": n / wall_b,
             "placements_per_s_serial_device_engine": n / wall_d,
             "placements_per_s_serial_host_engine_fp32": n / wall_h,
             "speedup_vs_serial_host_fp32": wall_h / wall_b, "iterations_per_s_batched": iters / wall_b,
             "batched_launches": launches, "identical_to_alone": "%d/%d" % (same, n), "failed": failed,
             "converged": sum(1 for s in res_b.values() if s["converged"]),
-            "wall_s": {"batched": wall_b, "serial_device": wall_d, "serial_host": wall_h},
+            "wall_s": {"served": wall_s, "batched": wall_b, "serial_device": wall_d, "serial_host": wall_h},
             "batched_wall_split_s": parts}
+
+
+def serve_request(i, lo=2000, hi=100000, sigma=6.0):
+    """Request i of the serving stream: cells log-uniform in [lo, hi] drawn
+    from a generator seeded by the request id, the netlist seeded by it too;
+    fabric, bins and nets as in the mixed-instance batch."""
+    import math
+    import numpy as np
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import default_params
+    rng = np.random.default_rng(1000003 + i)
+    cells = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    side = math.ceil(math.sqrt(cells / 0.9))
+    bins = min(256, max(64, 1 << (side - 1).bit_length()))
+    io = min(4 * (side - 1), 2 * side)
+    prob = P.synthetic(side, cells, io, int(round(1.2 * cells)), sigma, i)
+    prm = default_params(bins_x=bins, bins_y=bins, target_density=1.0, gamma_base=4.0, max_iterations=1000,
+                         best_effort=1)
+    return prob, prm
+
+
+def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
+    """Serving stream: Poisson arrivals at `load` x the measured batched
+    capacity of the same request distribution; placements/s and p50/p99
+    time-to-converge (submit to retire) of `n_requests` requests; final HPWL
+    of the smallest requests against the FP64 oracle."""
+    import threading
+    import numpy as np
+    from texo_gb300.placer import Server
+    # capacity: `probe` requests of the same distribution submitted at once
+    wall, _ = run_served([serve_request(100000 + k) for k in range(probe)])
+    capacity = probe / wall
+    rate = load * capacity
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    sizes = {}
+    results = {}
+    with Server(chunk_iterations=20, admission_threads=8) as srv:
+        def producer():
+            t0 = time.perf_counter()
+            for i in range(n_requests):
+                prob, prm = serve_request(i)
+                sizes[i] = prob.num_units
+                delay = arrivals[i] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                srv.submit(prob, i, prm)
+        th = threading.Thread(target=producer)
+        th.start()
+        while len(results) < n_requests:
+            r = srv.poll(wait_ms=1000)
+            if r is not None:
+                results[r[0]] = r[2]
+        th.join()
+    lat = np.array([results[i]["finish_ms"] - results[i]["submit_ms"] for i in range(n_requests)])
+    first = min(results[i]["submit_ms"] for i in range(n_requests))
+    last = max(results[i]["finish_ms"] for i in range(n_requests))
+    ok = [i for i in range(n_requests) if results[i]["status"] in ("OK", "DID_NOT_CONVERGE")]
+    conv = [i for i in ok if results[i]["converged"]]
+    within = [i for i in ok if max(results[i]["overflow"] or [0.0]) <= 0.10]
+    report = {"requests": n_requests, "cells": "log-uniform 2k..100k", "arrivals": "Poisson",
+              "offered_per_s": rate, "measured_capacity_per_s": capacity, "load": load,
+              "placements_per_s": n_requests / ((last - first) / 1000.0),
+              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+              "converged": len(conv), "overflow_le_0.10": len(within), "failed": n_requests - len(ok)}
+    # FP64 oracle on the smallest requests: relative final-HPWL difference
+    try:
+        from oracle import ffi
+        small = sorted(ok, key=lambda i: sizes[i])[:oracle_sample]
+        errs = []
+        for i in small:
+            prob, prm = serve_request(i)
+            st, _, _, s = ffi.Oracle(prob, prm).place(threads=5)
+            if s.hpwl > 0:
+                errs.append(abs(results[i]["hpwl"] - s.hpwl) / s.hpwl)
+        report["hpwl_rel_err_vs_fp64_oracle"] = {"jobs": len(errs), "max": max(errs) if errs else None,
+                                                 "mean": float(np.mean(errs)) if errs else None,
+                                                 "sample": "the %d smallest requests" % len(errs)}
+    except Exception as e:  # the oracle is optional on the box
+        report["hpwl_rel_err_vs_fp64_oracle"] = {"error": str(e)}
+    return report
 
 
 def config_dict(args):
@@ -293,7 +417,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lfe5u-85-42k", choices=sorted(WORKLOADS))
-    ap.add_argument("--engine", default="host", choices=["host", "device"])
+    ap.add_argument("--engine", default="device", choices=["host", "device"])
     ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3"])
     ap.add_argument("--reference-sample", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -302,6 +426,9 @@ def main():
                     help="warmup and timed steps only (for ncu launch lists)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-instance batched comparison")
     ap.add_argument("--batch-only", action="store_true", help="print only the batched comparison")
+    ap.add_argument("--serve-requests", type=int, default=200,
+                    help="requests in the serving-stream report (0 skips it; the full stream is 2000)")
+    ap.add_argument("--serve-only", action="store_true", help="print only the serving-stream report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -326,6 +453,11 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "placements/s (64 mixed instances)", "batched": batch_report()}), flush=True)
         return
+    if args.serve_only:
+        if rank == 0:
+            print(json.dumps({"metric": "placements/s + p99 latency (serving stream)",
+                              "serving": serve_report(args.serve_requests)}), flush=True)
+        return
     engine = abi.ENGINE_HOST if args.engine == "host" else abi.ENGINE_DEVICE
     dct = abi.DCT_FP32 if args.dct == "fp32" else abi.DCT_BF16X3
     prob = make_problem(args.workload, rank)
@@ -336,22 +468,26 @@ def main():
     n = dict(U=g.units, F=g.num_fillers, M=int(prob.member_ptr[-1]), B=g.bins, Hb=g.bins_y,
              E=prob.num_nets, P=prob.num_pins, K=g.num_fields)
 
-    state = {"prev": 0, "restarts": 0}
+    state = {"prev": 0, "restarts": 0, "evals": 0, "trials": 0}
 
     def one_step():
         _, _, s = g.run(1, allow_nonconverged=True)
         if s["iterations"] <= state["prev"]:
             # the placement finished: start it again (outside the timed region)
             g.reset()
-            state["restarts"] += 1
+            state.update(restarts=state["restarts"] + 1, evals=0, trials=0)
             _, _, s = g.run(1, allow_nonconverged=True)
         state["prev"] = s["iterations"]
+        # objective evaluations and line-search trials of this step
+        s["d_evals"] = s["evaluations"] - state["evals"]
+        s["d_trials"] = s["line_search_trials"] - state["trials"]
+        state.update(evals=s["evaluations"], trials=s["line_search_trials"])
         return s
 
     for _ in range(args.warmup):
         s = one_step()
     # timed steps
-    total_ms, launches = 0.0, 0
+    total_ms, launches, evals, trials = 0.0, 0, 0, 0
     with Clocks(local) as clk:
         if dist:
             dist.barrier()
@@ -362,6 +498,8 @@ def main():
             s = one_step()
             total_ms += s["elapsed_ms"]
             launches += s["kernel_launches"]
+            evals += s["d_evals"]
+            trials += s["d_trials"]
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -375,16 +513,32 @@ def main():
             print(json.dumps({"metric": METRIC, "value": value, "unit": "iter/s", "profile": True,
                               "gpu_launches": int(launches)}), flush=True)
         return
-    # per-stage device times and the dominant kernel's roofline
+    # per-stage device times (standalone stage kernels) and the roofline
     stages = g.stage_times(reps=20)
     peak, peak_kind = peaks()
-    per_eval = {k: v for k, v in stages.items()}
-    order = sorted(per_eval, key=lambda k: -per_eval[k] * (1 if k not in ("finalize",) else 0))
-    dom = order[0]
-    achieved = stage_bytes(dom, n) / (stages[dom] * 1e-3) / 1e9
+    stage_roofline = {k: {"ms": v, "algorithmic_bytes": stage_bytes(k, n),
+                          "gbs": stage_bytes(k, n) / (v * 1e-3) / 1e9 if v > 0 else None}
+                      for k, v in stages.items()}
+    if engine == abi.ENGINE_DEVICE:
+        # one persistent launch per step runs the whole iteration: its
+        # algorithmic bytes are the evaluations' and the vector updates' of
+        # the step, and its duration is the step's CUDA-event time
+        per_step_bytes = (evals * eval_bytes(n) + trials * stage_bytes("candidate", n)
+                          + args.steps * (stage_bytes("precond", n) + stage_bytes("extrapolate", n))) / args.steps
+        dom = "k_persistent (one GP iteration per launch)"
+        dom_ms = max_ms / args.steps
+        achieved = per_step_bytes / (dom_ms * 1e-3) / 1e9
+    else:
+        order = sorted(stages, key=lambda k: -stages[k])
+        dom = order[0]
+        per_step_bytes = stage_bytes(dom, n)
+        dom_ms = stages[dom]
+        achieved = per_step_bytes / (dom_ms * 1e-3) / 1e9
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                "stage_ms": stages}
+                "frac": achieved / peak, "traffic": ncu_traffic(args.workload, args.engine),
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_step_bytes,
+                "launch_ms": dom_ms, "evaluations_per_step": evals / args.steps,
+                "trials_per_step": trials / args.steps, "stages": stage_roofline}
     # end to end through the C ABI from host buffers
     e2e = None
     if not args.no_e2e:
@@ -403,6 +557,8 @@ def main():
             "roofline": roofline, "e2e": e2e, "restarts": state["restarts"]}
     if rank == 0 and not args.no_batch:
         line["batched"] = batch_report()
+    if rank == 0 and args.serve_requests > 0 and not args.no_batch:
+        line["serving"] = serve_report(args.serve_requests)
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)

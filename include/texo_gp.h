@@ -365,6 +365,55 @@ int32_t texo_gp_batch_retire(texo_gp_batch b, uint64_t* job_id, uint32_t* out_ta
 int32_t texo_gp_batch_counts(texo_gp_batch b, uint32_t* resident, uint32_t* finished,
                              uint64_t* bytes_in_use);
 
+/* ---- Serving loop (continuous batching) ----------------------------------
+ * Placement requests are submitted at any time from any thread. Admission
+ * threads build each job's model and upload it once its device footprint
+ * fits the HBM budget; the serving thread adds uploaded jobs to the resident
+ * batch at the next launch boundary, advances all resident jobs together
+ * (one persistent launch per `chunk_iterations`), and retires each job when
+ * it stops (overflow target reached, iteration cap, or an error), freeing
+ * its memory for waiting jobs. A job's result does not depend on the other
+ * jobs in the batch. No counterpart in the reference (its placement is one
+ * synchronous call); the per-job semantics are those of texo_gp_place. */
+typedef struct texo_gp_server_s* texo_gp_server;
+typedef struct texo_gp_server_options {
+  uint64_t hbm_budget_bytes;   /* device bytes uploaded jobs may hold (0: 3/4 of free memory) */
+  uint32_t max_resident;       /* jobs advanced together (0: 256) */
+  uint32_t chunk_iterations;   /* iterations per launch between admissions (0: 20) */
+  uint32_t admission_threads;  /* host threads building and uploading jobs (0: 4) */
+  uint32_t reserved[5];
+} texo_gp_server_options;
+typedef struct texo_gp_job_result {
+  uint64_t job_id;
+  int32_t status;              /* TEXO_GP_OK, DID_NOT_CONVERGE, or the job's error */
+  uint32_t units;              /* targets written: 2 * units */
+  texo_gp_stats stats;
+  double submit_ms;            /* server clock (ms since texo_gp_server_create) */
+  double admit_ms;             /* upload finished, waiting for the next launch */
+  double finish_ms;            /* retired */
+} texo_gp_job_result;
+
+int32_t texo_gp_server_create(const texo_gp_params* defaults, const texo_gp_server_options* options,
+                              texo_gp_server* out);
+/* Stops the serving and admission threads (finishing the launch in flight)
+ * and frees every job. */
+int32_t texo_gp_server_destroy(texo_gp_server s);
+/* Queues one request; the problem is copied, so the caller's arrays may be
+ * released on return. `params` NULL = the server defaults (engine and device
+ * are the server's). */
+int32_t texo_gp_server_submit(texo_gp_server s, const texo_gp_problem* problem,
+                              const texo_gp_params* params, uint64_t job_id);
+/* Pops one finished job, waiting up to `wait_ms` (negative: forever) for
+ * one; TEXO_GP_ERR_BUSY when none finished in time. `out_targets_xy` (may be
+ * NULL) receives 2U rounded targets when `targets_capacity` >= 2U, else the
+ * call returns TEXO_GP_ERR_INVALID_ARGUMENT, sets out->job_id and out->units
+ * and keeps the job for a call with a larger buffer. */
+int32_t texo_gp_server_poll(texo_gp_server s, int32_t wait_ms, texo_gp_job_result* out,
+                            uint32_t* out_targets_xy, uint64_t targets_capacity);
+int32_t texo_gp_server_counts(texo_gp_server s, uint32_t* queued, uint32_t* resident,
+                              uint32_t* finished, uint64_t* bytes_in_use);
+double texo_gp_server_clock_ms(texo_gp_server s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,3 +61,33 @@ def test_admission_respects_the_hbm_budget():
     assert not b.admit(probs[1], 2)        # a second copy does not fit
     r, f, used = b.counts()
     assert r == 1 and used == one
+
+
+@pytest.mark.parametrize("chunk", [1, 20])
+def test_crowded_batch_is_deterministic(chunk):
+    """48 copies of one job share the GPU's blocks (fewer physical blocks
+    than virtual blocks each, many jobs per SM) and are advanced `chunk`
+    iterations per launch: every copy must finish exactly as the job does
+    alone. Under this load, any block whose threads or warps disagree about
+    the controller state shows up as a diverging copy or a barrier timeout."""
+    p = P.synthetic(48, 2000, 96, 2400, 6.0, 11)
+    t0, _, s0 = Placer(p, params()).run()
+    b = Batch(params(), max_slots=64)
+    for i in range(48):
+        assert b.admit(p, i)
+    got = {}
+    for _ in range(2000):
+        b.advance(chunk)
+        while True:
+            r = b.retire()
+            if r is None:
+                break
+            got[r[0]] = r
+        if len(got) == 48:
+            break
+    assert len(got) == 48
+    for i in range(48):
+        _, t, s = got[i]
+        assert s["status"] == s0["status"]
+        assert t is not None and np.array_equal(t, t0), "copy %d diverged" % i
+        assert s["iterations"] == s0["iterations"] and s["hpwl"] == s0["hpwl"]

@@ -109,6 +109,16 @@ class Eval(C.Structure):
                 ("fields", FieldEval * MAX_FIELDS)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_uint32), ("chunk_iterations", C.c_uint32),
+                ("admission_threads", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("job_id", C.c_uint64), ("status", C.c_int32), ("units", C.c_uint32), ("stats", Stats),
+                ("submit_ms", C.c_double), ("admit_ms", C.c_double), ("finish_ms", C.c_double)]
+
+
 class SynthSpec(C.Structure):
     _fields_ = [("side", C.c_uint32), ("cells", C.c_uint32), ("io", C.c_uint32),
                 ("nets", C.c_uint32), ("sigma", C.c_double), ("p_local", C.c_double),
@@ -167,6 +177,12 @@ SIGNATURES = {
     "texo_gp_batch_advance": (C.c_int32, [_P, C.c_uint32]),
     "texo_gp_batch_retire": (C.c_int32, [_P, c_u64p, c_u32p, C.c_uint64, C.POINTER(Stats)]),
     "texo_gp_batch_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u64p]),
+    "texo_gp_server_create": (C.c_int32, [C.POINTER(Params), C.POINTER(ServerOptions), C.POINTER(_P)]),
+    "texo_gp_server_destroy": (C.c_int32, [_P]),
+    "texo_gp_server_submit": (C.c_int32, [_P, C.POINTER(ProblemC), C.POINTER(Params), C.c_uint64]),
+    "texo_gp_server_poll": (C.c_int32, [_P, C.c_int32, C.POINTER(JobResult), c_u32p, C.c_uint64]),
+    "texo_gp_server_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u32p, c_u64p]),
+    "texo_gp_server_clock_ms": (C.c_double, [_P]),
 }
 
 _lib = None

@@ -125,6 +125,28 @@ int32_t texo_gp_batch_admit(texo_gp_batch b, const texo_gp_problem* problem, con
   return TEXO_GP_OK;
 }
 
+}  // extern "C"
+
+namespace tgp {
+// Adds an uploaded handle as a resident job; the caller has accounted its
+// device bytes (the serving loop admits by its own HBM budget).
+int32_t batch_add_handle(texo_gp_batch b, texo_gp_handle h, uint64_t job_id) {
+  if (!b || !h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (b->resident.size() + b->done.size() >= b->max_slots) return TEXO_GP_ERR_BUSY;
+  Job j;
+  j.id = job_id;
+  j.h = h;
+  j.bytes = handle_bytes(h);
+  j.V = handle_virtual_blocks(h);
+  b->used += j.bytes;
+  b->resident.push_back(j);
+  return TEXO_GP_OK;
+}
+}  // namespace tgp
+
+extern "C" {
+
 int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
   if (!b) return TEXO_GP_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lk(b->mu);

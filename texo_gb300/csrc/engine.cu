@@ -11,6 +11,8 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -36,6 +38,8 @@ void set_last_error(const std::string& s) { g_last_error = s; }
     if (s_ != TEXO_GP_OK) return s_; \
   } while (0)
 
+void release_mirror(double* scal);
+
 Instance::~Instance() {
   if (stream) cudaStreamSynchronize(stream);
   for (void* p : allocations) cudaFreeAsync(p, stream);
@@ -43,8 +47,7 @@ Instance::~Instance() {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
-  if (h_scal) cudaFreeHost(h_scal);
-  if (h_iscal) cudaFreeHost(h_iscal);
+  release_mirror(h_scal);
 }
 
 // Device buffers come from the device's stream-ordered pool (kept, not
@@ -82,18 +85,6 @@ int32_t upload_coords(Instance& I, float2* dst, const double* src, size_t nobj) 
   CU(cudaStreamSynchronize(I.stream));
   return TEXO_GP_OK;
 }
-template <typename T>
-int32_t upload_vec(Instance& I, T** dst, const std::vector<T>& v) {
-  TRY(I.alloc((void**)dst, v.size() * sizeof(T)));
-  if (!v.empty()) CU(cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, I.stream));
-  return TEXO_GP_OK;
-}
-template <typename T>
-int32_t zeros(Instance& I, T** dst, size_t n) {
-  TRY(I.alloc((void**)dst, n * sizeof(T)));
-  CU(cudaMemsetAsync(*dst, 0, n * sizeof(T), I.stream));
-  return TEXO_GP_OK;
-}
 std::vector<double> dct_basis(uint32_t n) {
   const double nf = (double)n;
   std::vector<double> b((size_t)n * n);
@@ -103,7 +94,261 @@ std::vector<double> dct_basis(uint32_t n) {
   }
   return b;
 }
+
+// Spectral tables of a bin grid (DCT basis and its transpose per axis, the
+// inverse Laplacian eigenvalues), read-only and identical for every
+// instance with the same grid: built once per device and size and shared.
+struct SpectralTables {
+  float *Cx = nullptr, *CxT = nullptr, *Cy = nullptr, *CyT = nullptr, *inv_eig = nullptr;
+};
+cudaError_t shared_basis(int device, uint32_t n, float** c, float** ct) {
+  static std::mutex mu;
+  static std::map<std::pair<int, uint32_t>, std::pair<float*, float*>> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({device, n});
+  if (it == cache.end()) {
+    const auto b = dct_basis(n);
+    std::vector<float> m((size_t)n * n), mt((size_t)n * n);
+    for (uint32_t i = 0; i < n; ++i)
+      for (uint32_t j = 0; j < n; ++j) {
+        m[(size_t)i * n + j] = (float)b[(size_t)i * n + j];
+        mt[(size_t)j * n + i] = (float)b[(size_t)i * n + j];
+      }
+    float *d = nullptr, *dt = nullptr;
+    cudaError_t e = cudaMalloc(&d, m.size() * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dt, m.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d, m.data(), m.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, mt.data(), mt.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    it = cache.emplace(std::make_pair(device, n), std::make_pair(d, dt)).first;
+  }
+  *c = it->second.first;
+  *ct = it->second.second;
+  return cudaSuccess;
+}
+cudaError_t shared_inv_eig(int device, uint32_t Wb, uint32_t Hb, float** out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint32_t, uint32_t>, float*> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({device, Wb, Hb});
+  if (it == cache.end()) {
+    std::vector<float> ie((size_t)Wb * Hb);
+    for (uint32_t ky = 0; ky < Hb; ++ky) {
+      const double sy = std::sin(3.14159265358979323846 * ky / (2.0 * Hb));
+      const double ly = 4.0 * (sy * sy);
+      for (uint32_t kx = 0; kx < Wb; ++kx) {
+        const double sx = std::sin(3.14159265358979323846 * kx / (2.0 * Wb));
+        const double l = 4.0 * (sx * sx) + ly;
+        ie[(size_t)ky * Wb + kx] = (kx == 0 && ky == 0) ? 0.0f : (float)(1.0 / l);
+      }
+    }
+    float* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, ie.size() * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d, ie.data(), ie.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    it = cache.emplace(std::make_tuple(device, Wb, Hb), d).first;
+  }
+  *out = it->second;
+  return cudaSuccess;
+}
 }  // namespace
+
+// Pinned host mirrors of the reduction scalars, carved from shared slabs:
+// page-locking memory per instance would dominate admitting small jobs.
+namespace {
+constexpr size_t kMirrorBytes = ((kScalars * sizeof(double) + kIScalars * sizeof(long long)) + 255) & ~(size_t)255;
+std::mutex g_mirror_mu;
+std::vector<char*> g_mirror_free;
+}  // namespace
+int32_t acquire_mirror(double** scal, long long** iscal) {
+  std::lock_guard<std::mutex> lk(g_mirror_mu);
+  if (g_mirror_free.empty()) {
+    constexpr int kPerSlab = 64;
+    char* slab = nullptr;
+    CU(cudaMallocHost((void**)&slab, kMirrorBytes * kPerSlab));
+    for (int i = kPerSlab - 1; i >= 0; --i) g_mirror_free.push_back(slab + i * kMirrorBytes);
+  }
+  char* b = g_mirror_free.back();
+  g_mirror_free.pop_back();
+  *scal = (double*)b;
+  *iscal = (long long*)(b + kScalars * sizeof(double));
+  return TEXO_GP_OK;
+}
+void release_mirror(double* scal) {
+  if (!scal) return;
+  std::lock_guard<std::mutex> lk(g_mirror_mu);
+  g_mirror_free.push_back((char*)scal);
+}
+
+// Device layout of one instance: every buffer is a 256-byte aligned slice
+// of one pool allocation. The slices with host data come first and are
+// filled by one copy from a pinned staging buffer; the rest are zeroed by
+// one memset. The same plan sizes the instance before anything is
+// allocated (admission by HBM footprint).
+namespace {
+struct Slicer {
+  char* base = nullptr;     // device arena (null while sizing)
+  char* stage = nullptr;    // host staging for the uploaded region
+  size_t up = 0, zero = 0, zero_at = 0;
+  static size_t round(size_t b) { return ((b ? b : 16) + 255) & ~(size_t)255; }
+  // a slice with host data: returns the host slot to fill (null while sizing)
+  template <typename T>
+  T* put(T** dev, size_t count) {
+    const size_t at = up;
+    up += round(count * sizeof(T));
+    if (!base) return nullptr;
+    *dev = (T*)(base + at);
+    return (T*)(stage + at);
+  }
+  template <typename T, typename D>
+  void put_const(const D** dev, size_t count) {
+    T* d = nullptr;
+    put(&d, count);
+    if (base) *dev = (const D*)d;
+  }
+  template <typename T>
+  void zeroed(T** dev, size_t count) {
+    const size_t at = zero;
+    zero += round(count * sizeof(T));
+    if (base) *dev = (T*)(base + zero_at + at);
+  }
+};
+// per-thread pinned staging buffer, kept for the thread's next upload
+struct Staging {
+  char* p = nullptr;
+  size_t bytes = 0;
+  ~Staging() {
+    if (p) cudaFreeHost(p);
+  }
+};
+thread_local Staging t_stage;
+}  // namespace
+
+void Instance::plan(bool fill, void* slicer_ptr) {
+  Slicer& S = *(Slicer*)slicer_ptr;
+  const HostModel& h = m;
+  const size_t nobj = (size_t)h.U + h.F, B = h.bins(), K = h.K;
+  Dev& D = d;
+  // bin coordinate of every tile centre, (t + 1/2) * scale - 1/2 in FP64,
+  // split into hi + lo floats
+  auto binmap = [&](const float2** dst, uint32_t tiles, uint32_t bins) {
+    float2* v = nullptr;
+    float2* slot = S.put(&v, tiles);
+    if (fill) {
+      const double scale = (double)bins / (double)tiles;
+      for (uint32_t t = 0; t < tiles; ++t) {
+        const double b = ((double)t + 0.5) * scale - 0.5;
+        const float hi = (float)b;
+        slot[t] = make_float2(hi, (float)(b - (double)hi));
+      }
+    }
+    *dst = v;
+  };
+  auto copy_i = [&](const int** dst, const std::vector<int>& v) {
+    int* p = nullptr;
+    int* slot = S.put(&p, v.size());
+    if (fill && !v.empty()) std::memcpy(slot, v.data(), v.size() * sizeof(int));
+    *dst = p;
+  };
+  auto copy_f = [&](const float** dst, const auto& v) {   // any numeric vector -> float
+    float* p = nullptr;
+    float* slot = S.put(&p, v.size());
+    if (fill)
+      for (size_t i = 0; i < v.size(); ++i) slot[i] = (float)v[i];
+    *dst = p;
+  };
+  auto copy_f2 = [&](const float2** dst, const std::vector<double>& v) {   // interleaved pairs
+    float2* p = nullptr;
+    float2* slot = S.put(&p, v.size() / 2);
+    if (fill)
+      for (size_t i = 0; i < v.size() / 2; ++i) slot[i] = make_float2((float)v[2 * i], (float)v[2 * i + 1]);
+    *dst = p;
+  };
+  binmap(&D.binmap_x, h.W, h.Wb);
+  binmap(&D.binmap_y, h.H, h.Hb);
+  copy_i(&D.mem_unit, h.mem_unit);
+  copy_f2(&D.mem_off, h.mem_off);
+  copy_f(&D.mem_q, h.mem_q);
+  copy_i(&D.mem_field, h.mem_field);
+  copy_i(&D.unit_mem_ptr, h.unit_mem_ptr);
+  copy_i(&D.fil_field, h.fil_field);
+  copy_f(&D.fil_q, h.fil_q);
+  copy_i(&D.net_ptr, h.net_ptr);
+  copy_i(&D.pin_unit, h.pin_unit);
+  copy_f2(&D.pin_base, h.pin_base);
+  copy_f(&D.net_w, h.net_w);
+  {
+    long long *cf = nullptr, *cs = nullptr;
+    long long* slot = S.put(&cf, K * B);
+    long long* sum = S.put(&cs, std::max<size_t>(K, 1));
+    if (fill) {
+      sum[0] = 0;
+      for (size_t f = 0; f < K; ++f) {
+        long long acc = 0;
+        for (size_t i = 0; i < B; ++i) {
+          slot[f * B + i] = (long long)std::nearbyint(h.smoothed[f][i] * kFix);
+          acc += slot[f * B + i];
+        }
+        sum[f] = acc;
+      }
+    }
+    D.capfix = cf;
+    D.capsum = cs;
+  }
+  copy_f2(&D.lo, h.lo);
+  copy_f2(&D.hi, h.hi);
+  copy_f(&D.pre_static, h.pre_static);
+  copy_f(&D.pre_q, h.pre_q);
+  {
+    float2* slot = S.put(&bufX, nobj);   // the initial coordinates
+    if (fill)
+      for (size_t i = 0; i < nobj; ++i) slot[i] = make_float2((float)h.init[2 * i], (float)h.init[2 * i + 1]);
+    double* sc = S.put(&r.scal, kScalars);
+    if (fill) {
+      std::memset(sc, 0, kScalars * sizeof(double));
+      sc[SC_BETA] = h.params.beta;
+      for (uint32_t f = 0; f < K; ++f) {
+        sc[SC_REAL_AREA + f] = h.real_area[f];
+        sc[SC_E0 + f] = 1.0;
+        sc[SC_LAMBDA + f] = 0.0;
+      }
+    }
+  }
+  // zero-initialized slices
+  S.zeroed(&D.phys, K * B);
+  S.zeroed(&D.fill, K * B);
+  S.zeroed(&D.rho, K * B);
+  S.zeroed(&D.t1, K * B);
+  S.zeroed(&D.t2, K * B);
+  S.zeroed(&D.phi, K * B);
+  S.zeroed(&D.wa_fix, 2 * (size_t)h.U);
+  S.zeroed(&D.graw, std::max<size_t>(K, 1) * nobj);
+  S.zeroed(&D.P, nobj);
+  S.zeroed(&bufXp, nobj);
+  S.zeroed(&bufY, nobj);
+  S.zeroed(&bufC, nobj);
+  S.zeroed(&gX, nobj);
+  S.zeroed(&gY, nobj);
+  S.zeroed(&gC, nobj);
+  S.zeroed(&run_dev, 1);
+  S.zeroed(&bar, 1);
+  S.zeroed(&best, std::max<size_t>(h.U, 1));
+  S.zeroed(&prev_targets, 2 * (size_t)h.U);
+  S.zeroed(&mismatch, 1);
+  S.zeroed(&r.p.sum, (size_t)kSlots * kMaxPartials);
+  S.zeroed(&r.p.isum, (size_t)kISlots * kMaxPartials);
+  S.zeroed(&r.p.mx, (size_t)kMSlots * kMaxPartials);
+  S.zeroed(&r.q.sum, (size_t)kSlots * kMaxPartials);
+  S.zeroed(&r.q.isum, (size_t)kISlots * kMaxPartials);
+  S.zeroed(&r.q.mx, (size_t)kMSlots * kMaxPartials);
+  S.zeroed(&r.iscal, kIScalars);
+}
+
+uint64_t Instance::device_bytes() {
+  Slicer S;
+  plan(false, &S);
+  return S.up + S.zero;
+}
 
 int32_t Instance::upload() {
   HostModel& h = m;
@@ -127,98 +372,42 @@ int32_t Instance::upload() {
   D.Mm = (int)h.Mm;
   D.B = (int)B;
   D.g = Grid{(int)h.W, (int)h.H, (int)h.Wb, (int)h.Hb, (float)h.sx, (float)h.sy, h.identity ? 1 : 0};
-  // bin coordinate of every tile centre, (t + 1/2) * scale - 1/2 in FP64,
-  // split into hi + lo floats
-  auto binmap = [](uint32_t tiles, uint32_t bins) {
-    std::vector<float> v(2 * (size_t)tiles);
-    const double scale = (double)bins / (double)tiles;
-    for (uint32_t t = 0; t < tiles; ++t) {
-      const double b = ((double)t + 0.5) * scale - 0.5;
-      const float hi = (float)b;
-      v[2 * (size_t)t] = hi;
-      v[2 * (size_t)t + 1] = (float)(b - (double)hi);
-    }
-    return v;
-  };
-  TRY(upload_vec(*this, (float**)&D.binmap_x, binmap(h.W, h.Wb)));
-  TRY(upload_vec(*this, (float**)&D.binmap_y, binmap(h.H, h.Hb)));
-  TRY(upload_vec(*this, (int**)&D.mem_unit, h.mem_unit));
-  std::vector<float> moff(h.mem_off.begin(), h.mem_off.end());
-  TRY(upload_vec(*this, (float**)&D.mem_off, moff));
-  TRY(upload_vec(*this, (float**)&D.mem_q, h.mem_q));
-  TRY(upload_vec(*this, (int**)&D.mem_field, h.mem_field));
-  TRY(upload_vec(*this, (int**)&D.unit_mem_ptr, h.unit_mem_ptr));
-  TRY(upload_vec(*this, (int**)&D.fil_field, h.fil_field));
-  std::vector<float> fq(h.fil_q.begin(), h.fil_q.end());
-  TRY(upload_vec(*this, (float**)&D.fil_q, fq));
   D.n_classes = h.n_classes;
   std::memcpy(D.class_begin, h.class_begin, sizeof(D.class_begin));
   std::memcpy(D.class_group, h.class_group, sizeof(D.class_group));
   D.n_hpwl_nets = h.n_hpwl_nets;
-  TRY(upload_vec(*this, (int**)&D.net_ptr, h.net_ptr));
-  TRY(upload_vec(*this, (int**)&D.pin_unit, h.pin_unit));
-  std::vector<float> pbase(h.pin_base.begin(), h.pin_base.end());
-  TRY(upload_vec(*this, (float**)&D.pin_base, pbase));
-  TRY(upload_vec(*this, (float**)&D.net_w, h.net_w));
-  // grids
-  TRY(zeros(*this, &D.phys, K * B));
-  TRY(zeros(*this, &D.fill, K * B));
-  std::vector<long long> capfix(K * B), capsum(std::max<size_t>(K, 1), 0);
-  for (size_t f = 0; f < K; ++f)
-    for (size_t i = 0; i < B; ++i) {
-      capfix[f * B + i] = (long long)std::nearbyint(h.smoothed[f][i] * kFix);
-      capsum[f] += capfix[f * B + i];
-    }
-  TRY(upload_vec(*this, (long long**)&D.capfix, capfix));
-  TRY(upload_vec(*this, (long long**)&D.capsum, capsum));
-  TRY(zeros(*this, &D.rho, K * B));
-  TRY(zeros(*this, &D.t1, K * B));
-  TRY(zeros(*this, &D.t2, K * B));
-  TRY(zeros(*this, &D.phi, K * B));
-  auto bx = dct_basis(h.Wb), by = dct_basis(h.Hb);
-  std::vector<float> cx(bx.size()), cxt(bx.size()), cy(by.size()), cyt(by.size());
-  for (uint32_t i = 0; i < h.Wb; ++i)
-    for (uint32_t j = 0; j < h.Wb; ++j) {
-      cx[(size_t)i * h.Wb + j] = (float)bx[(size_t)i * h.Wb + j];
-      cxt[(size_t)j * h.Wb + i] = (float)bx[(size_t)i * h.Wb + j];
-    }
-  for (uint32_t i = 0; i < h.Hb; ++i)
-    for (uint32_t j = 0; j < h.Hb; ++j) {
-      cy[(size_t)i * h.Hb + j] = (float)by[(size_t)i * h.Hb + j];
-      cyt[(size_t)j * h.Hb + i] = (float)by[(size_t)i * h.Hb + j];
-    }
-  TRY(upload_vec(*this, (float**)&D.Cx, cx));
-  TRY(upload_vec(*this, (float**)&D.CxT, cxt));
-  TRY(upload_vec(*this, (float**)&D.Cy, cy));
-  TRY(upload_vec(*this, (float**)&D.CyT, cyt));
-  std::vector<float> ie(B);
-  for (uint32_t ky = 0; ky < h.Hb; ++ky) {
-    const double sy = std::sin(3.14159265358979323846 * ky / (2.0 * h.Hb));
-    const double ly = 4.0 * (sy * sy);
-    for (uint32_t kx = 0; kx < h.Wb; ++kx) {
-      const double sx = std::sin(3.14159265358979323846 * kx / (2.0 * h.Wb));
-      const double l = 4.0 * (sx * sx) + ly;
-      ie[(size_t)ky * h.Wb + kx] = (kx == 0 && ky == 0) ? 0.0f : (float)(1.0 / l);
-    }
+  {
+    float *cx, *cxt, *cy, *cyt, *ie;
+    CU(shared_basis(device, h.Wb, &cx, &cxt));
+    CU(shared_basis(device, h.Hb, &cy, &cyt));
+    CU(shared_inv_eig(device, h.Wb, h.Hb, &ie));
+    D.Cx = cx;
+    D.CxT = cxt;
+    D.Cy = cy;
+    D.CyT = cyt;
+    D.inv_eig = ie;
   }
-  TRY(upload_vec(*this, (float**)&D.inv_eig, ie));
-  TRY(zeros(*this, &D.wa_fix, 2 * (size_t)h.U));
-  TRY(zeros(*this, &D.graw, std::max<size_t>(K, 1) * nobj));
-  // optimizer
-  std::vector<float> lo(h.lo.begin(), h.lo.end()), hi(h.hi.begin(), h.hi.end());
-  TRY(upload_vec(*this, (float**)&D.lo, lo));
-  TRY(upload_vec(*this, (float**)&D.hi, hi));
-  TRY(zeros(*this, &D.P, nobj));
-  std::vector<float> pst(h.pre_static.begin(), h.pre_static.end()), pq(h.pre_q.begin(), h.pre_q.end());
-  TRY(upload_vec(*this, (float**)&D.pre_static, pst));
-  TRY(upload_vec(*this, (float**)&D.pre_q, pq));
-  TRY(zeros(*this, &bufX, nobj));
-  TRY(zeros(*this, &bufXp, nobj));
-  TRY(zeros(*this, &bufY, nobj));
-  TRY(zeros(*this, &bufC, nobj));
-  TRY(zeros(*this, &gX, nobj));
-  TRY(zeros(*this, &gY, nobj));
-  TRY(zeros(*this, &gC, nobj));
+  // size, allocate, pack, copy
+  Slicer sizing;
+  plan(false, &sizing);
+  const size_t up_bytes = sizing.up, zero_bytes = sizing.zero;
+  void* base = nullptr;
+  TRY(alloc(&base, up_bytes + zero_bytes));
+  if (t_stage.bytes < up_bytes) {
+    if (t_stage.p) cudaFreeHost(t_stage.p);
+    t_stage.p = nullptr;
+    t_stage.bytes = 0;
+    const size_t want = std::max(up_bytes, (size_t)4 << 20) * 2;
+    CU(cudaMallocHost((void**)&t_stage.p, want));
+    t_stage.bytes = want;
+  }
+  Slicer S;
+  S.base = (char*)base;
+  S.stage = t_stage.p;
+  S.zero_at = up_bytes;
+  plan(true, &S);
+  CU(cudaMemcpyAsync(base, t_stage.p, up_bytes, cudaMemcpyHostToDevice, stream));
+  CU(cudaMemsetAsync((char*)base + up_bytes, 0, zero_bytes, stream));
   posb[0] = bufX;
   posb[1] = bufXp;
   posb[2] = bufY;
@@ -226,38 +415,21 @@ int32_t Instance::upload() {
   gradb[0] = gX;
   gradb[1] = gY;
   gradb[2] = gC;
-  TRY(zeros(*this, &run_dev, 1));
-  TRY(zeros(*this, &bar, 1));
   {
-    const int per_sm = persistent_blocks_per_sm();
+    static const int per_sm = persistent_blocks_per_sm();
     pblocks = std::min(std::max(per_sm, 1), 2) * sms;
     pblocks = std::min(pblocks, kMaxPartials);
   }
-  TRY(zeros(*this, &best, std::max<size_t>(h.U, 1)));
-  TRY(zeros(*this, &prev_targets, 2 * (size_t)h.U));
-  TRY(zeros(*this, &mismatch, 1));
-  // reductions
-  TRY(zeros(*this, &r.p.sum, (size_t)kSlots * kMaxPartials));
-  TRY(zeros(*this, &r.p.isum, (size_t)kISlots * kMaxPartials));
-  TRY(zeros(*this, &r.p.mx, (size_t)kMSlots * kMaxPartials));
-  TRY(zeros(*this, &r.q.sum, (size_t)kSlots * kMaxPartials));
-  TRY(zeros(*this, &r.q.isum, (size_t)kISlots * kMaxPartials));
-  TRY(zeros(*this, &r.q.mx, (size_t)kMSlots * kMaxPartials));
-  TRY(zeros(*this, &r.scal, kScalars));
-  TRY(zeros(*this, &r.iscal, kIScalars));
-  CU(cudaMallocHost((void**)&h_scal, kScalars * sizeof(double)));
-  CU(cudaMallocHost((void**)&h_iscal, kIScalars * sizeof(long long)));
+  TRY(acquire_mirror(&h_scal, &h_iscal));
   std::memset(h_scal, 0, kScalars * sizeof(double));
+  std::memset(h_iscal, 0, kIScalars * sizeof(long long));
   h_scal[SC_BETA] = h.params.beta;
   for (uint32_t f = 0; f < K; ++f) {
     h_scal[SC_REAL_AREA + f] = h.real_area[f];
     h_scal[SC_E0 + f] = 1.0;
     h_scal[SC_LAMBDA + f] = 0.0;
   }
-  CU(cudaMemcpyAsync(r.scal, h_scal, kScalars * sizeof(double), cudaMemcpyHostToDevice, stream));
-  std::vector<float> init32(h.init.begin(), h.init.end());
-  CU(cudaMemcpyAsync(bufX, init32.data(), nobj * sizeof(float2), cudaMemcpyHostToDevice, stream));
-  CU(cudaStreamSynchronize(stream));
+  // the staging buffer is reused by this thread's next upload
   CU(cudaStreamSynchronize(stream));
   return TEXO_GP_OK;
 }
@@ -855,6 +1027,32 @@ uint64_t handle_bytes(texo_gp_handle_s* h) { return h->inst->bytes; }
 int handle_virtual_blocks(texo_gp_handle_s* h) { return h->inst->nvb; }
 int handle_sms(texo_gp_handle_s* h) { return h->inst->sms; }
 Instance* handle_instance(texo_gp_handle_s* h) { return h->inst.get(); }
+int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_gp_handle_s** out,
+                     uint64_t* err_index) {
+  *out = nullptr;
+  texo_gp_params defaults;
+  if (!prm) {
+    texo_gp_default_params(&defaults);
+    prm = &defaults;
+  }
+  if (!p) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  auto h = std::make_unique<texo_gp_handle_s>();
+  h->inst = std::make_unique<Instance>();
+  h->inst->device = prm->device;
+  uint64_t err = 0;
+  const int32_t s = build_model(p, prm, h->inst->m, &err);
+  if (err_index) *err_index = err;
+  if (s) return s;
+  *out = h.release();
+  return TEXO_GP_OK;
+}
+uint64_t handle_device_bytes(texo_gp_handle_s* h) { return h->inst->device_bytes(); }
+int32_t handle_upload(texo_gp_handle_s* h) {
+  TRY(h->inst->upload());
+  h->ctl = std::make_unique<Controller>(*h->inst);
+  return TEXO_GP_OK;
+}
 std::mutex* handle_mutex(texo_gp_handle_s* h) { return &h->mu; }
 }  // namespace tgp
 
@@ -978,22 +1176,14 @@ const char* texo_gp_last_error(void) { return g_last_error.c_str(); }
 int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo_gp_handle* out) {
   if (!out) return TEXO_GP_ERR_INVALID_ARGUMENT;
   *out = nullptr;
-  texo_gp_params defaults;
-  if (!prm) {
-    texo_gp_default_params(&defaults);
-    prm = &defaults;
+  texo_gp_handle h = nullptr;
+  TRY(tgp::handle_build(p, prm, &h, nullptr));
+  const int32_t s = tgp::handle_upload(h);
+  if (s) {
+    delete h;
+    return s;
   }
-  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  auto h = std::make_unique<texo_gp_handle_s>();
-  h->inst = std::make_unique<Instance>();
-  h->inst->device = prm->device;
-  uint64_t err = 0;
-  int32_t s = build_model(p, prm, h->inst->m, &err);
-  if (s) return s;
-  s = h->inst->upload();
-  if (s) return s;
-  h->ctl = std::make_unique<Controller>(*h->inst);
-  *out = h.release();
+  *out = h;
   return TEXO_GP_OK;
 }
 

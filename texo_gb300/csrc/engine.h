@@ -90,6 +90,10 @@ struct Instance {
   ~Instance();
   int32_t alloc(void** p, size_t bytes);
   int32_t upload();
+  // device layout: sizes every slice (fill = false) or also packs the host
+  // data of the uploaded slices into the staging buffer (fill = true)
+  void plan(bool fill, void* slicer);
+  uint64_t device_bytes();   // the one allocation upload() makes
 };
 
 }  // namespace tgp
@@ -109,5 +113,12 @@ uint64_t handle_bytes(texo_gp_handle_s* h);
 int handle_virtual_blocks(texo_gp_handle_s* h);
 int handle_sms(texo_gp_handle_s* h);
 Instance* handle_instance(texo_gp_handle_s* h);
+// texo_gp_create in two steps: the host model (no device work), then the
+// device upload; between them handle_device_bytes gives the footprint.
+int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_gp_handle_s** out,
+                     uint64_t* err_index);
+uint64_t handle_device_bytes(texo_gp_handle_s* h);
+int32_t handle_upload(texo_gp_handle_s* h);
+int32_t batch_add_handle(texo_gp_batch b, texo_gp_handle h, uint64_t job_id);
 std::mutex* handle_mutex(texo_gp_handle_s* h);
 }  // namespace tgp

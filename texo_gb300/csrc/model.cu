@@ -139,6 +139,10 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   // density units and members (eplace.rs:261-301)
   m.U = U;
   m.unit_mem_ptr.assign(U + 1, 0);
+  m.mem_unit.reserve(M);
+  m.mem_field.reserve(M);
+  m.mem_off.reserve(2 * (size_t)M);
+  m.mem_q.reserve(M);
   m.real_count.assign(m.K, 0);
   m.real_area.assign(m.K, 0.0);
   uint32_t dunit = 0;
@@ -171,6 +175,12 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   m.has_density = m.Mm > 0;
   // fillers (electrostatic_placement.rs:198-240)
   std::vector<double> fx, fy;
+  fx.reserve(tiles * m.K);
+  fy.reserve(tiles * m.K);
+  m.fil_field.reserve(tiles * m.K);
+  m.fil_q.reserve(tiles * m.K);
+  std::vector<size_t> occ;
+  occ.reserve(tiles);
   for (uint32_t f = 0; f < m.K; ++f) {
     if (m.real_count[f] > m.available[f]) {
       *err = f;
@@ -186,7 +196,7 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     if (m.td != 1.0) total = std::max(total, 0.0);
     if (total == 0.0) continue;
     const double denominator = (double)(uint32_t)m.available[f];
-    std::vector<size_t> occ;
+    occ.clear();
     for (size_t i = 0; i < tiles; ++i)
       if (m.cap[f][i]) occ.push_back(i);
     double assigned = 0.0;
@@ -253,9 +263,10 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
       by = p->cell_offset_xy[2 * (size_t)cell + 1];
     }
   };
-  // wirelength preconditioner and cell incidence
+  // wirelength preconditioner and cell incidence: each distinct unit (cell)
+  // of a net counts once, found with a per-net stamp instead of a sort
   std::vector<double> wl(U, 0.0), inc(C, 0.0);
-  std::vector<uint32_t> tmp;
+  std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
   for (uint32_t e = 0; e < E; ++e) {
     const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
     if (en < b + 2) {
@@ -265,17 +276,29 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     for (uint32_t k = b; k < en; ++k)
       if (p->pin_cell[k] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
     const double w = 1.0 / (double)(uint32_t)(en - b - 1);
-    tmp.clear();
-    for (uint32_t k = b; k < en; ++k) tmp.push_back(p->cell_unit[p->pin_cell[k]]);
-    std::sort(tmp.begin(), tmp.end());
-    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-    if (tmp.size() >= 2)
-      for (auto u : tmp) wl[u] += w;
-    tmp.clear();
-    for (uint32_t k = b; k < en; ++k) tmp.push_back(p->pin_cell[k]);
-    std::sort(tmp.begin(), tmp.end());
-    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-    for (auto c : tmp) inc[c] += w;
+    uint32_t distinct = 0;
+    for (uint32_t k = b; k < en; ++k) {
+      const uint32_t u = p->cell_unit[p->pin_cell[k]];
+      if (unit_seen[u] != e) {
+        unit_seen[u] = e;
+        ++distinct;
+      }
+    }
+    if (distinct >= 2)
+      for (uint32_t k = b; k < en; ++k) {
+        const uint32_t u = p->cell_unit[p->pin_cell[k]];
+        if (unit_seen[u] == e) {
+          unit_seen[u] = ~0u - 1;   // counted for this net
+          wl[u] += w;
+        }
+      }
+    for (uint32_t k = b; k < en; ++k) {
+      const uint32_t c = p->pin_cell[k];
+      if (cell_seen[c] != e) {
+        cell_seen[c] = e;
+        inc[c] += w;
+      }
+    }
   }
   std::vector<double> pin_weight_sum(U, 0.0);
   for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
@@ -296,6 +319,11 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   auto cls = [](uint32_t deg) { return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : 4; };
   std::vector<std::vector<uint32_t>> bucket(5);
   for (uint32_t e = 0; e < E; ++e) bucket[cls(p->net_ptr[e + 1] - p->net_ptr[e])].push_back(e);
+  const size_t pins = E ? p->net_ptr[E] : 0;
+  m.net_ptr.reserve((size_t)E + p->num_timed_arcs + 1);
+  m.net_w.reserve((size_t)E + p->num_timed_arcs);
+  m.pin_unit.reserve(pins + 2 * (size_t)p->num_timed_arcs);
+  m.pin_base.reserve(2 * (pins + 2 * (size_t)p->num_timed_arcs));
   m.net_ptr.assign(1, 0);
   int nc = 0;
   for (int c = 0; c < 5; ++c) {

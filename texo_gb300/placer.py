@@ -109,6 +109,73 @@ class Batch:
         return r.value, f.value, b.value
 
 
+class Server:
+    """The serving loop (texo_gp_server): submit requests at any time, poll
+    finished jobs. Results are (job_id, targets [U,2] or None, info dict)."""
+
+    def __init__(self, params=None, hbm_budget=0, max_resident=256, chunk_iterations=20, admission_threads=4):
+        self.lib = abi.load()
+        self.params = params or default_params()
+        opt = abi.ServerOptions()
+        opt.hbm_budget_bytes = hbm_budget
+        opt.max_resident = max_resident
+        opt.chunk_iterations = chunk_iterations
+        opt.admission_threads = admission_threads
+        h = C.c_void_p()
+        abi.check(self.lib.texo_gp_server_create(C.byref(self.params), C.byref(opt), C.byref(h)),
+                  "texo_gp_server_create")
+        self.h = h
+        self._units = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.texo_gp_server_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, problem, job_id, params=None):
+        pc = problem.c_struct()
+        pp = C.byref(params) if params is not None else None
+        abi.check(self.lib.texo_gp_server_submit(self.h, C.byref(pc), pp, job_id), "texo_gp_server_submit")
+        self._units[job_id] = problem.num_units
+
+    def clock_ms(self):
+        return self.lib.texo_gp_server_clock_ms(self.h)
+
+    def poll(self, wait_ms=-1):
+        """One finished job or None (nothing finished within wait_ms)."""
+        cap = 2 * max(self._units.values(), default=1)
+        targets = np.zeros(cap, np.uint32)
+        r = abi.JobResult()
+        code = self.lib.texo_gp_server_poll(self.h, wait_ms, C.byref(r), abi.ptr(targets, C.c_uint32), targets.size)
+        if code == abi.CODE["INVALID_ARGUMENT"] and 2 * r.units > targets.size:
+            # a job submitted (by another thread) during the wait finished first
+            targets = np.zeros(2 * r.units, np.uint32)
+            code = self.lib.texo_gp_server_poll(self.h, 0, C.byref(r), abi.ptr(targets, C.c_uint32), targets.size)
+        if code == abi.CODE["BUSY"]:
+            return None
+        abi.check(code, "texo_gp_server_poll")
+        self._units.pop(r.job_id, None)
+        info = _stats_dict(r.stats)
+        info.update(status=abi.STATUS.get(r.status, r.status), submit_ms=r.submit_ms, admit_ms=r.admit_ms,
+                    finish_ms=r.finish_ms)
+        ok = r.status in (0, abi.CODE["DID_NOT_CONVERGE"])
+        return r.job_id, (targets[:2 * r.units].reshape(-1, 2).copy() if ok else None), info
+
+    def counts(self):
+        q, r, f, b = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint64()
+        abi.check(self.lib.texo_gp_server_counts(self.h, C.byref(q), C.byref(r), C.byref(f), C.byref(b)),
+                  "texo_gp_server_counts")
+        return q.value, r.value, f.value, b.value
+
+
 class Placer:
     """A device-resident placement instance (texo_gp_handle)."""
 
