@@ -1037,6 +1037,10 @@ int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_g
   }
   if (!p) return TEXO_GP_ERR_INVALID_ARGUMENT;
   if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (prm->dct_mode == TEXO_GP_DCT_BF16X3) {
+    set_last_error("the BF16x3 tensor-core DCT is not available in this build");
+    return TEXO_GP_ERR_UNSUPPORTED;
+  }
   auto h = std::make_unique<texo_gp_handle_s>();
   h->inst = std::make_unique<Instance>();
   h->inst->device = prm->device;
