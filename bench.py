@@ -91,6 +91,18 @@ def stage_bytes(stage, n):
     }.get(stage, 0)
 
 
+def aggregate_ranks(total_ms, steps, dist=None, device="cuda"):
+    """Replicas: every rank places its own instance (seeded by its rank); the
+    whole-job value is all ranks' steps over the slowest rank's time."""
+    import torch
+    world = dist.get_world_size() if dist else 1
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return max_ms, world * steps / (max_ms / 1000.0)
+
+
 def eval_bytes(n):
     """Algorithmic bytes of one objective evaluation (all its stages)."""
     st = ["init", "scatter", "wa", "prep", "dct_row_fwd", "dct_col_fwd", "dct_col_inv", "dct_row_inv",
@@ -503,11 +515,7 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = world * args.steps / (max_ms / 1000.0)
+    max_ms, value = aggregate_ranks(total_ms, args.steps, dist, "cuda")
     if args.profile:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "iter/s", "profile": True,
