@@ -414,6 +414,59 @@ def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
     return report
 
 
+def precision_report(iterations=1000, seed=0, threads=5):
+    """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
+    1024^2 bins, target density 0.9): potential, field gradient and energy of
+    the FP32 and BF16x3 (tensor-core) DCT forms against the FP64 oracle at
+    identical spread positions, gradient cosine similarity, and each form's
+    final HPWL / overflow after `iterations` GP iterations. The oracle cannot
+    run 1000 FP64 iterations of this size in a bench, so the final HPWL is
+    compared between the two GPU forms."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer
+    prob = make_problem("stress-1m", seed)
+    prm64 = make_params("stress-1m", abi.ENGINE_HOST, abi.DCT_FP32)
+    prm64.max_iterations = iterations
+    t0 = time.perf_counter()
+    o = ffi.Oracle(prob, prm64)
+    c, lo, hi = o.initial()
+    c = (lo + (hi - lo) * np.random.default_rng(seed + 1).random(c.size)).astype(np.float32).astype(np.float64)
+    gamma = 4.0
+    r = o.evaluate(c, gamma, threads=threads)
+    t_oracle = time.perf_counter() - t0
+
+    def nw(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    def cos(a, b):
+        return float(np.dot(a.ravel(), b.ravel()) / (np.linalg.norm(a) * np.linalg.norm(b)))
+
+    out = {"workload": "stress-1m", "positions": "uniform in the bounds, FP32-representable",
+           "oracle_eval_s": t_oracle}
+    for name, mode in (("fp32", abi.DCT_FP32), ("bf16x3", abi.DCT_BF16X3)):
+        prm = make_params("stress-1m", abi.ENGINE_HOST, mode)
+        prm.max_iterations = iterations
+        with Placer(prob, prm) as g:
+            d = g.evaluate(c, gamma)
+            st = g.stage_times(reps=5)
+            t1 = time.perf_counter()
+            _, _, s = g.run(allow_nonconverged=True)
+            run_s = time.perf_counter() - t1
+        out[name] = {"potential_max_rel_err": nw(d["potential"], r["potential"]),
+                     "field_gradient_max_rel_err": nw(d["field_gradient"], r["field_gradient"]),
+                     "field_gradient_cosine": cos(d["field_gradient"], r["field_gradient"]),
+                     "wa_gradient_cosine": cos(d["wa_gradient"], r["wa_gradient"]),
+                     "energy_rel_err": abs(d["fields"][0].energy - r["fields"][0].energy) / abs(r["fields"][0].energy),
+                     "dct_pass_us": [round(1000 * st[k], 2) for k in ("dct_row_fwd", "dct_col_fwd", "dct_col_inv",
+                                                                       "dct_row_inv")],
+                     "final_hpwl": s["hpwl"], "final_overflow": s["overflow"], "iterations": s["iterations"],
+                     "converged": s["converged"], "run_s": run_s, "gpu_ms": s["elapsed_ms"]}
+    out["final_hpwl_bf16x3_vs_fp32"] = out["bf16x3"]["final_hpwl"] / out["fp32"]["final_hpwl"] - 1.0
+    return out
+
+
 def config_dict(args):
     side, cells, io, nets, sigma, bins, td, gamma, cap = WORKLOADS[args.workload]
     return {"workload": args.workload, "cells": cells, "io": io, "nets": nets, "fabric": "%dx%d" % (side, side),
@@ -441,6 +494,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests in the serving-stream report (0 skips it; the full stream is 2000)")
     ap.add_argument("--serve-only", action="store_true", help="print only the serving-stream report")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 1M-cell precision report")
+    ap.add_argument("--precision-only", action="store_true", help="print only the 1M-cell precision report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -464,6 +519,11 @@ def main():
     if args.batch_only:
         if rank == 0:
             print(json.dumps({"metric": "placements/s (64 mixed instances)", "batched": batch_report()}), flush=True)
+        return
+    if args.precision_only:
+        if rank == 0:
+            print(json.dumps({"metric": "BF16x3 / FP32 / FP64 precision at 1M cells",
+                              "precision": precision_report()}), flush=True)
         return
     if args.serve_only:
         if rank == 0:
@@ -567,6 +627,8 @@ def main():
         line["batched"] = batch_report()
     if rank == 0 and args.serve_requests > 0 and not args.no_batch:
         line["serving"] = serve_report(args.serve_requests)
+    if rank == 0 and not args.no_precision and not args.no_batch:
+        line["precision"] = precision_report()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)

@@ -330,7 +330,7 @@ int32_t texo_gp_hpwl(texo_gp_handle h, const double* coordinates, double* hpwl);
 typedef struct texo_gp_synth_spec {
   uint32_t side;          /* fabric side in sites */
   uint32_t cells;         /* movable unit-area cells */
-  uint32_t io;            /* fixed perimeter IO cells */
+  uint32_t io;            /* fixed perimeter IO cells (evenly spaced; may share sites) */
   uint32_t nets;
   double sigma;           /* locality radius in sites */
   double p_local;         /* probability that a sink is local (0.8) */

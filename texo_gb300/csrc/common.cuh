@@ -76,6 +76,15 @@ struct Dev {
   const float* Cx;  const float* CxT;   // [Wb][Wb]
   const float* Cy;  const float* CyT;   // [Hb][Hb]
   const float* inv_eig;      // [B]
+  // Tensor-core DCT (BF16x3): every GEMM operand is kept as bfloat16 hi/lo
+  // halves in the tile layout the tensor cores read (see dct_tc.cuh). A
+  // operands (rows x K) in 128 x 32 blocks, B operands (output columns x K)
+  // in 64 x 32 blocks, zero-padded; rho_t and t3_t are A operands (H x W),
+  // t1_t and t2_t B operands (W x H); the bases are shared read-only tables.
+  int tc;                    // 1: the DCT passes run on tcgen05 tensor cores
+  int Hp128, Hp32, Wp64, Wp32;   // padded extents
+  uint16_t *rho_t, *t1_t, *t2_t, *t3_t;
+  const uint16_t *CxB_t, *CyA_t, *CyTA_t, *CxTB_t;
   // gradients
   unsigned long long* wa_fix;  // [2U] WA gradient, 2^-32 fixed point
   float2* graw;              // [K][nobj] raw per-field density gradient

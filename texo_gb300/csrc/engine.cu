@@ -13,11 +13,14 @@
 #include <limits>
 #include <map>
 #include <tuple>
+
+#include <cuda_bf16.h>
 #include <memory>
 #include <mutex>
 #include <string>
 
 #include "engine.h"
+#include "dct_tc.cuh"
 
 namespace tgp {
 
@@ -101,29 +104,57 @@ std::vector<double> dct_basis(uint32_t n) {
 struct SpectralTables {
   float *Cx = nullptr, *CxT = nullptr, *Cy = nullptr, *CyT = nullptr, *inv_eig = nullptr;
 };
-cudaError_t shared_basis(int device, uint32_t n, float** c, float** ct) {
+struct BasisTables {
+  float *c = nullptr, *ct = nullptr;   // FP32 C and C^T, row-major n x n
+  // tensor-core operands (dct_tc.cuh layout): C and C^T as B operands
+  // (rows padded to 64) and as A operands (rows padded to 128), K padded to 32
+  uint16_t *cB = nullptr, *ctB = nullptr, *cA = nullptr, *ctA = nullptr;
+};
+cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
   static std::mutex mu;
-  static std::map<std::pair<int, uint32_t>, std::pair<float*, float*>> cache;
+  static std::map<std::pair<int, uint32_t>, BasisTables> cache;
   std::lock_guard<std::mutex> lk(mu);
   auto it = cache.find({device, n});
   if (it == cache.end()) {
     const auto b = dct_basis(n);
-    std::vector<float> m((size_t)n * n), mt((size_t)n * n);
-    for (uint32_t i = 0; i < n; ++i)
-      for (uint32_t j = 0; j < n; ++j) {
-        m[(size_t)i * n + j] = (float)b[(size_t)i * n + j];
-        mt[(size_t)j * n + i] = (float)b[(size_t)i * n + j];
+    const size_t nn = (size_t)n * n;
+    const int N = (int)n, kp = tc::pad(N, tc::kKC);
+    std::vector<float> m(nn), mt(nn);
+    std::vector<uint16_t> cB((size_t)tc::pad(N, tc::kN) * kp * 2, 0), ctB(cB.size(), 0);
+    std::vector<uint16_t> cA((size_t)tc::pad(N, tc::kM) * kp * 2, 0), ctA(cA.size(), 0);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        const float v = (float)b[(size_t)i * n + j];   // C[i][j] = C^T[j][i]
+        m[(size_t)i * n + j] = v;
+        mt[(size_t)j * n + i] = v;
+        uint16_t h, l;
+        tc::split(v, h, l);
+        cB[tc::b_index(i, j, kp, 0)] = h;
+        cB[tc::b_index(i, j, kp, 1)] = l;
+        ctB[tc::b_index(j, i, kp, 0)] = h;
+        ctB[tc::b_index(j, i, kp, 1)] = l;
+        cA[tc::a_index(i, j, kp, 0)] = h;
+        cA[tc::a_index(i, j, kp, 1)] = l;
+        ctA[tc::a_index(j, i, kp, 0)] = h;
+        ctA[tc::a_index(j, i, kp, 1)] = l;
       }
-    float *d = nullptr, *dt = nullptr;
-    cudaError_t e = cudaMalloc(&d, m.size() * 4);
-    if (e == cudaSuccess) e = cudaMalloc(&dt, m.size() * 4);
-    if (e == cudaSuccess) e = cudaMemcpy(d, m.data(), m.size() * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(dt, mt.data(), mt.size() * 4, cudaMemcpyHostToDevice);
+    BasisTables t;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](auto** dst, const auto& v) {
+      if (e != cudaSuccess) return;
+      e = cudaMalloc((void**)dst, v.size() * sizeof(v[0]));
+      if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+    };
+    up(&t.c, m);
+    up(&t.ct, mt);
+    up(&t.cB, cB);
+    up(&t.ctB, ctB);
+    up(&t.cA, cA);
+    up(&t.ctA, ctA);
     if (e != cudaSuccess) return e;
-    it = cache.emplace(std::make_pair(device, n), std::make_pair(d, dt)).first;
+    it = cache.emplace(std::make_pair(device, n), t).first;
   }
-  *c = it->second.first;
-  *ct = it->second.second;
+  *out = it->second;
   return cudaSuccess;
 }
 cudaError_t shared_inv_eig(int device, uint32_t Wb, uint32_t Hb, float** out) {
@@ -342,6 +373,14 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&r.q.isum, (size_t)kISlots * kMaxPartials);
   S.zeroed(&r.q.mx, (size_t)kMSlots * kMaxPartials);
   S.zeroed(&r.iscal, kIScalars);
+  if (h.params.dct_mode == TEXO_GP_DCT_BF16X3) {   // tensor-core operands (zero padding)
+    const size_t a = (size_t)tc::pad((int)h.Hb, tc::kM) * tc::pad((int)h.Wb, tc::kKC) * 2 * K;
+    const size_t b = (size_t)tc::pad((int)h.Wb, tc::kN) * tc::pad((int)h.Hb, tc::kKC) * 2 * K;
+    S.zeroed(&D.rho_t, a);
+    S.zeroed(&D.t3_t, a);
+    S.zeroed(&D.t1_t, b);
+    S.zeroed(&D.t2_t, b);
+  }
 }
 
 uint64_t Instance::device_bytes() {
@@ -377,15 +416,25 @@ int32_t Instance::upload() {
   std::memcpy(D.class_group, h.class_group, sizeof(D.class_group));
   D.n_hpwl_nets = h.n_hpwl_nets;
   {
-    float *cx, *cxt, *cy, *cyt, *ie;
-    CU(shared_basis(device, h.Wb, &cx, &cxt));
-    CU(shared_basis(device, h.Hb, &cy, &cyt));
+    BasisTables bx, by;
+    float* ie;
+    CU(shared_basis(device, h.Wb, &bx));
+    CU(shared_basis(device, h.Hb, &by));
     CU(shared_inv_eig(device, h.Wb, h.Hb, &ie));
-    D.Cx = cx;
-    D.CxT = cxt;
-    D.Cy = cy;
-    D.CyT = cyt;
+    D.Cx = bx.c;
+    D.CxT = bx.ct;
+    D.Cy = by.c;
+    D.CyT = by.ct;
     D.inv_eig = ie;
+    D.tc = h.params.dct_mode == TEXO_GP_DCT_BF16X3 ? 1 : 0;
+    D.Hp128 = tc::pad((int)h.Hb, tc::kM);
+    D.Hp32 = tc::pad((int)h.Hb, tc::kKC);
+    D.Wp64 = tc::pad((int)h.Wb, tc::kN);
+    D.Wp32 = tc::pad((int)h.Wb, tc::kKC);
+    D.CxB_t = bx.cB;      // pass 0: B = rows of Cx
+    D.CxTB_t = bx.ctB;    // pass 3: B = rows of Cx^T
+    D.CyA_t = by.cA;      // pass 1: A = Cy
+    D.CyTA_t = by.ctA;    // pass 2: A = Cy^T
   }
   // size, allocate, pack, copy
   Slicer sizing;
@@ -491,6 +540,10 @@ struct Controller {
     CU(cudaMemcpyAsync(I.h_iscal, I.r.iscal, kIScalars * sizeof(long long), cudaMemcpyDeviceToHost, I.stream));
     CU(cudaStreamSynchronize(I.stream));
     CU(cudaGetLastError());
+    if (I.h_iscal[SI_TC_FAIL]) {
+      set_last_error("tensor-core DCT: an mbarrier wait ran out");
+      return TEXO_GP_ERR_DEVICE_TIMEOUT;
+    }
     return TEXO_GP_OK;
   }
   int32_t push_inputs() {
@@ -1037,8 +1090,8 @@ int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_g
   }
   if (!p) return TEXO_GP_ERR_INVALID_ARGUMENT;
   if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  if (prm->dct_mode == TEXO_GP_DCT_BF16X3) {
-    set_last_error("the BF16x3 tensor-core DCT is not available in this build");
+  if (prm->dct_mode == TEXO_GP_DCT_BF16X3 && prm->engine == TEXO_GP_ENGINE_DEVICE) {
+    set_last_error("the BF16x3 tensor-core DCT runs with the host engine only");
     return TEXO_GP_ERR_UNSUPPORTED;
   }
   auto h = std::make_unique<texo_gp_handle_s>();
@@ -1327,13 +1380,19 @@ int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potenti
   Dev D = I.d;
   D.K = 1;
   CU(cudaMemcpyAsync(D.rho, rho.data(), B * 4, cudaMemcpyHostToDevice, I.stream));
+  if (D.tc) launch_tile_rho(D, I.nvb, I.stream);
   for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream);
   launch_finalize(D, I.r, I.nvb, FIN_ENERGY, I.stream);
   std::vector<float> phi(B);
   CU(cudaMemcpyAsync(phi.data(), D.phi, B * 4, cudaMemcpyDeviceToHost, I.stream));
   CU(cudaMemcpyAsync(I.h_scal, I.r.scal, kScalars * sizeof(double), cudaMemcpyDeviceToHost, I.stream));
+  CU(cudaMemcpyAsync(I.h_iscal, I.r.iscal, kIScalars * sizeof(long long), cudaMemcpyDeviceToHost, I.stream));
   CU(cudaStreamSynchronize(I.stream));
   CU(cudaGetLastError());
+  if (I.h_iscal[SI_TC_FAIL]) {
+    set_last_error("tensor-core DCT: an mbarrier wait ran out");
+    return TEXO_GP_ERR_DEVICE_TIMEOUT;
+  }
   if (potential)
     for (size_t i = 0; i < B; ++i) potential[i] = phi[i];
   if (energy) *energy = I.h_scal[SC_ENERGY];

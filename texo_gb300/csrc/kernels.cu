@@ -1,7 +1,30 @@
 // kernels.cu — standalone kernels (one stage each) and their launchers.
+#include "dct_tc.cuh"
 #include "kernels.cuh"
 
 namespace tgp {
+
+// The tensor cores' A-operand form of rho (for callers that set rho directly).
+__global__ void __launch_bounds__(kThreads) k_tile_rho(Dev d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.K * d.B; i += gridDim.x * blockDim.x)
+    tc::put_rho(d, i / d.B, i % d.B, d.rho[i]);
+}
+
+// One DCT pass on tcgen05 tensor cores (BF16x3), one 128 x 64 tile per block
+// iteration; the energy partials of pass 3 are per block as in k_dct.
+__global__ void __launch_bounds__(kThreads) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err) {
+  extern __shared__ __align__(128) unsigned char tc_dyn[];
+  tc::Smem& sm = *reinterpret_cast<tc::Smem*>(tc_dyn);
+  __shared__ Shared sh;
+  double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+  if ((int)blockIdx.x < tc::pass_tiles(d)) {   // blocks without a tile only write zero partials
+    tc::setup(sm);
+    tc::dct_pass(d, step, blockIdx.x, gridDim.x, sm, eacc, err);
+    tc::teardown(sm);
+  }
+  if (step == 3)
+    for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), (int)blockIdx.x, sh.d);
+}
 
 __global__ void __launch_bounds__(kThreads) k_init(Dev d, bool grids, bool wa) {
   stage_init(d, blockIdx.x, gridDim.x, grids, wa);
@@ -190,8 +213,19 @@ void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
   COUNT;
   k_prep<<<nvb, kThreads, 0, s>>>(d, r.p);
 }
+void launch_tile_rho(const Dev& d, int nvb, cudaStream_t s) {
+  COUNT;
+  k_tile_rho<<<nvb, kThreads, 0, s>>>(d);
+}
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s) {
   COUNT;
+  if (d.tc) {
+    static const bool attr = cudaFuncSetAttribute(k_dct_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)sizeof(tc::Smem)) == cudaSuccess;
+    (void)attr;
+    k_dct_tc<<<nvb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL));
+    return;
+  }
   if (use_large_tiles(d))
     k_dct<true><<<nvb, kThreads, 0, s>>>(d, r.p, step);
   else

@@ -7,6 +7,7 @@
 // fixed order, so every result is bit-for-bit deterministic.
 #pragma once
 #include "common.cuh"
+#include "dct_tc.cuh"
 
 namespace tgp {
 
@@ -305,6 +306,7 @@ static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int
         cnt[f] += 1;
       }
       rho[i] = __ll2float_rn(a + fl[i] - mean) * kInvFixF;
+      if (d.tc) tc::put_rho(d, f, i, rho[i]);
     }
   }
   for (int f = 0; f < d.K; ++f) {

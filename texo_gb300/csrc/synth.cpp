@@ -65,7 +65,7 @@ struct texo_gp_synth_s {
 extern "C" int32_t texo_gp_synth_create(const texo_gp_synth_spec* spec, texo_gp_synth* out,
                                         const texo_gp_problem** problem) {
   if (!spec || !out || spec->side < 2 || spec->cells == 0 ||
-      (uint64_t)spec->cells > (uint64_t)spec->side * spec->side || spec->io > 4u * (spec->side - 1) ||
+      (uint64_t)spec->cells > (uint64_t)spec->side * spec->side || spec->io > 64u * (spec->side - 1) ||
       !(spec->sigma > 0.0) || !(spec->p_local >= 0.0 && spec->p_local <= 1.0) || !(spec->jitter >= 0.0))
     return TEXO_GP_ERR_INVALID_ARGUMENT;
   auto s = std::make_unique<texo_gp_synth_s>();
@@ -100,7 +100,8 @@ extern "C" int32_t texo_gp_synth_create(const texo_gp_synth_spec* spec, texo_gp_
     s->member_ptr[i + 1] = (uint32_t)s->member_field.size();
     s->cell_unit[i] = i;
   }
-  // IO evenly spaced along the perimeter walk (x grows on y=0, then up x=S-1, ...)
+  // IO evenly spaced along the perimeter walk (x grows on y=0, then up x=S-1, ...);
+  // with more IO cells than perimeter sites, neighbours share a site
   const uint64_t perim = 4ull * (S - 1);
   for (uint32_t k = 0; k < IO; ++k) {
     const uint64_t t = (uint64_t)k * perim / (IO ? IO : 1);
