@@ -81,7 +81,7 @@ int32_t texo_gp_batch_create(const texo_gp_params* params, uint64_t hbm_budget_b
   BCU(cudaSetDevice(b->params.device));
   cudaDeviceProp prop;
   BCU(cudaGetDeviceProperties(&prop, b->params.device));
-  const int per_sm = std::min(std::max(persistent_blocks_per_sm(), 1), 2);
+  const int per_sm = std::min(std::max(batch_blocks_per_sm(), 1), kBatchBlocksPerSm);
   b->pblocks = per_sm * prop.multiProcessorCount;
   BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCU(cudaMalloc(&b->d_descs, sizeof(InstDesc) * max_slots));

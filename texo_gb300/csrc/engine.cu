@@ -396,12 +396,12 @@ int32_t Instance::upload() {
   CU(keep_pool(device));
   CU(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   const size_t nobj = (size_t)h.U + h.F, B = h.bins(), K = h.K;
-  // enough blocks to cover the widest stage, up to 8 per SM
+  // enough blocks to cover the widest stage, up to kBlocksPerSm per SM
   const size_t widest = std::max(std::max(std::max(nobj, (size_t)h.Mm + h.F), std::max(B, h.pin_unit.size() / 2)), (size_t)1);
   // Virtual blocks: the reduction structure of every stage. The standalone
   // kernels launch exactly this many blocks; the persistent engine loops its
   // physical blocks over them, so both see the same partials.
-  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * 2), (size_t)kMaxPartials);
+  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * kBlocksPerSm), (size_t)kMaxPartials);
   nvb = std::max(nvb, 1);
   Dev& D = d;
   D.U = (int)h.U;
@@ -466,7 +466,7 @@ int32_t Instance::upload() {
   gradb[2] = gC;
   {
     static const int per_sm = persistent_blocks_per_sm();
-    pblocks = std::min(std::max(per_sm, 1), 2) * sms;
+    pblocks = std::min(std::max(per_sm, 1), kBlocksPerSm) * sms;
     pblocks = std::min(pblocks, kMaxPartials);
   }
   TRY(acquire_mirror(&h_scal, &h_iscal));

@@ -13,6 +13,13 @@ int persistent_blocks_per_sm() {
   int a = 0, b = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, persistent_kernel_small(), kThreads, 0) != cudaSuccess)
     return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, persistent_kernel_large(), kThreads, 0) != cudaSuccess)
+    return 0;
+  return a < b ? a : b;
+}
+int batch_blocks_per_sm() {
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, batch_kernel_small(), kThreads, 0) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batch_kernel_large(), kThreads, 0) != cudaSuccess) return 0;
   return a < b ? a : b;
 }

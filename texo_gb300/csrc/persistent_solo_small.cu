@@ -4,7 +4,7 @@
 
 namespace tgp {
 
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kBlocksPerSm)
     k_persistent_small(Dev d, Reduce r, Buffers B, DevRun* run, GridBarrier* bar, int V) {
   run_body<false>(d, r, B, run, bar, (int)blockIdx.x, (int)gridDim.x, V);
 }
