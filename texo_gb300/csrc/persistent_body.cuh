@@ -44,39 +44,51 @@ __device__ __forceinline__ unsigned long long now_ns() {
   return t;
 }
 
-// Barrier over the np physical blocks of one instance.
+// (generation, error) of a barrier in one acquire load: every write made
+// before the releasing arrival is visible once the new generation is seen
+__device__ __forceinline__ unsigned long long load_gen_error(const GridBarrier* b) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(&b->gen) : "memory");
+  return v;
+}
+
+// Barrier over the np physical blocks of one instance. Arrival is an
+// acq_rel add on one counter (release publishes this block's writes, acquire
+// makes the last arriver see everyone's); the last arriver resets the
+// counter and release-increments the generation the others poll with
+// acquire loads, which also carry the error word.
 __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned np, unsigned* gen, unsigned long long* count,
                                           unsigned long long* wait_acc, int* failed) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned long long t0 = wait_acc ? now_ns() : 0ull;
     const unsigned g = *gen;
-    __threadfence();
     // One counter: on this two-die part a barrier costs a few L2 round trips
     // whatever the arrival pattern, and a two-level tree only adds one.
-    bool last = false;
-    if (atomicAdd(&b->root.count, 1u) + 1u == np) {
-      b->root.count = 0u;
-      __threadfence();
-      atomicAdd(&b->gen, 1u);
-      last = true;
-    }
-    if (!last) {
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(&b->root.count) : "memory");
+    unsigned long long ge;
+    if (old + 1u == np) {
+      asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&b->root.count) : "memory");
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&b->gen) : "memory");
+      ge = load_gen_error(b);
+    } else {
       unsigned spins = 0;
-      while (*(volatile unsigned*)&b->gen == g) {
-        if (*(volatile int*)&b->error) break;
+      for (;;) {
+        ge = load_gen_error(b);
+        if ((unsigned)ge != g || (ge >> 32) != 0ull) break;
         if (++spins > kSpinLimit) {
           atomicExch(&b->error, 1);
+          ge |= 1ull << 32;
           break;
         }
-        __nanosleep(32);
+        if (spins > 64) __nanosleep(32);
       }
     }
     *gen = g + 1;
     ++*count;
-    __threadfence();
     if (wait_acc) *wait_acc += now_ns() - t0;
-    *failed = *(volatile int*)&b->error;
+    *failed = (int)(ge >> 32);
   }
   __syncthreads();
   // one read of the error word per block, so all its threads agree
