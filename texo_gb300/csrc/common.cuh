@@ -59,6 +59,9 @@ struct Dev {
   int n_classes;
   int class_begin[kMaxClasses + 1];
   int class_group[kMaxClasses];
+  // lanes of a V-virtual-block launch given to each class, warp-aligned
+  // prefix offsets: the classes run side by side, not one after another
+  int class_lane[kMaxClasses + 1];
   const int* net_ptr;        // [E+1]
   const int* pin_unit;       // [P] -1 for fixed cells
   const float2* pin_base;    // [P] fixed coordinate or cell offset

@@ -211,6 +211,36 @@ void release_mirror(double* scal) {
   g_mirror_free.push_back((char*)scal);
 }
 
+// Lanes of the WA stage per degree class: every class gets its own
+// warp-aligned segment of the launch's T lanes (one G-lane group per net),
+// all nets in one pass when they fit, otherwise segments in proportion to the
+// lanes each class needs, so the classes finish together.
+void wa_lane_split(const int* begin, const int* group, int n, long long T, int* lane) {
+  long long need[kMaxClasses + 1] = {0}, total = 0;
+  for (int c = 0; c < n; ++c) {
+    need[c] = (long long)(begin[c + 1] - begin[c]) * group[c];
+    total += need[c];
+  }
+  long long give[kMaxClasses + 1] = {0}, sum = 0;
+  for (int c = 0; c < n; ++c) {
+    if (!need[c]) continue;
+    long long g = total <= T ? (need[c] + 31) / 32 * 32 : (long long)((double)T * need[c] / total) / 32 * 32;
+    give[c] = std::max<long long>(g, 32);
+    sum += give[c];
+  }
+  while (sum > T) {   // rounding overshoot: trim the largest segment
+    int big = 0;
+    for (int c = 1; c < n; ++c)
+      if (give[c] > give[big]) big = c;
+    if (give[big] <= 32) break;
+    give[big] -= 32;
+    sum -= 32;
+  }
+  lane[0] = 0;
+  for (int c = 0; c < n; ++c) lane[c + 1] = lane[c] + (int)give[c];
+  for (int c = n; c < kMaxClasses; ++c) lane[c + 1] = lane[n];
+}
+
 // Device layout of one instance: every buffer is a 256-byte aligned slice
 // of one pool allocation. The slices with host data come first and are
 // filled by one copy from a pinned staging buffer; the rest are zeroed by
@@ -415,6 +445,7 @@ int32_t Instance::upload() {
   std::memcpy(D.class_begin, h.class_begin, sizeof(D.class_begin));
   std::memcpy(D.class_group, h.class_group, sizeof(D.class_group));
   D.n_hpwl_nets = h.n_hpwl_nets;
+  wa_lane_split(h.class_begin, h.class_group, h.n_classes, (long long)nvb * kThreads, D.class_lane);
   {
     BasisTables bx, by;
     float* ie;

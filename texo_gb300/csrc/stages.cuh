@@ -177,12 +177,15 @@ __device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* pos, int k)
   return make_float2(pu.x + b.x, pu.y + b.y);
 }
 
+// `slot` is this lane's index within the class's lane segment of `seg`
+// lanes (both multiples of 32 at the segment start, so a group never
+// straddles a warp and every lane of a warp makes the same passes).
 template <int G>
 __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float inv_gamma, int nb,
-                                         int ne, int vb, int nvb, double& acc) {
-  const int lane = threadIdx.x & (G - 1);
-  const int group = (vb * blockDim.x + threadIdx.x) / G;
-  const int groups = nvb * blockDim.x / G;
+                                         int ne, int slot, int seg, double& acc) {
+  const int lane = slot & (G - 1);
+  const int group = slot / G;
+  const int groups = seg / G;
   const unsigned mask = 0xffffffffu;
   const int count = ne - nb;
   float vacc = 0.f;
@@ -264,15 +267,20 @@ static __device__ void stage_wa(const Dev& d, const float2* pos, double gamma, P
                                 int nvb, Shared& sh) {
   double acc = 0.0;
   const float ig = (float)(1.0 / gamma);
-  for (int c = 0; c < d.n_classes; ++c) {
+  const int gl = vb * blockDim.x + threadIdx.x;
+  int c = 0;
+  while (c < d.n_classes && gl >= d.class_lane[c + 1]) ++c;
+  if (c < d.n_classes) {
     const int nb = d.class_begin[c], ne = d.class_begin[c + 1];
-    if (ne <= nb) continue;
-    switch (d.class_group[c]) {
-      case 2: wa_class<2>(d, pos, ig, nb, ne, vb, nvb, acc); break;
-      case 4: wa_class<4>(d, pos, ig, nb, ne, vb, nvb, acc); break;
-      case 8: wa_class<8>(d, pos, ig, nb, ne, vb, nvb, acc); break;
-      case 16: wa_class<16>(d, pos, ig, nb, ne, vb, nvb, acc); break;
-      default: wa_class<32>(d, pos, ig, nb, ne, vb, nvb, acc); break;
+    const int slot = gl - d.class_lane[c], seg = d.class_lane[c + 1] - d.class_lane[c];
+    if (ne > nb && seg > 0) {
+      switch (d.class_group[c]) {
+        case 2: wa_class<2>(d, pos, ig, nb, ne, slot, seg, acc); break;
+        case 4: wa_class<4>(d, pos, ig, nb, ne, slot, seg, acc); break;
+        case 8: wa_class<8>(d, pos, ig, nb, ne, slot, seg, acc); break;
+        case 16: wa_class<16>(d, pos, ig, nb, ne, slot, seg, acc); break;
+        default: wa_class<32>(d, pos, ig, nb, ne, slot, seg, acc); break;
+      }
     }
   }
   write_partial(acc, pslot(p, SLOT_WA_VALUE), vb, sh.d);
