@@ -109,6 +109,7 @@ struct Ctx {
   double* rd;         // reduction scratch (shared)
   long long* rl;
   double* coef;       // shared [kMaxFields]
+  long long* fmean;   // shared [kMaxFields] fixed-point density means
   int pb, np;         // physical block of the instance, physical block count
   int V;              // virtual blocks of the instance
   unsigned long long nbar;
@@ -167,10 +168,23 @@ struct Ctx {
     if (!sync()) return false;
     mark(PC_SCATTER_WA);
     if (full) {
-      for (int v = pb; v < V; v += np) stage_prep(d, r.p, V, v, V, sh);
-      if (!sync()) return false;
-      mark(PC_PREP);
-      for (int st = 0; st < 4; ++st) {
+      int st0 = 0;
+      if (LARGE) {
+        for (int v = pb; v < V; v += np) stage_prep(d, r.p, V, v, V, sh);
+        if (!sync()) return false;
+        mark(PC_PREP);
+      } else {
+        // density preparation folded into the first transform (one phase less)
+        for (int f = 0; f < d.K; ++f) {
+          const long long tot = block_reduce_array(islot(r.p, IS_GRID_SUM + f), V, 0ll, OpAdd(), rl);
+          if (threadIdx.x == 0) fmean[f] = (tot - d.capsum[f]) / d.B;
+        }
+        __syncthreads();
+        for (int v = pb; v < V; v += np) stage_prep_dct0(d, fmean, r.p, v, V, gsm, sh);
+        if (!sync()) return false;
+        st0 = 1;
+      }
+      for (int st = st0; st < 4; ++st) {
         for (int v = pb; v < V; v += np) stage_dct_t<LARGE>(d, st, r.p, v, V, gsm, sh);
         if (!sync()) return false;
       }
@@ -350,6 +364,7 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
   __shared__ double rd[kThreads / 32];
   __shared__ long long rl[kThreads / 32];
   __shared__ double coef[kMaxFields];
+  __shared__ long long fmean[kMaxFields];
   __shared__ unsigned gen;
   __shared__ int bar_failed;
   __shared__ unsigned long long clock[10];
@@ -362,7 +377,7 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
     clock[8] = now_ns();
   }
   __syncthreads();
-  Ctx<LARGE> c{d, r, B, S, bar, &gen, &bar_failed, gsm, sh, rd, rl, coef, pb, np, Vn, 0ull, clock};
+  Ctx<LARGE> c{d, r, B, S, bar, &gen, &bar_failed, gsm, sh, rd, rl, coef, fmean, pb, np, Vn, 0ull, clock};
   const int n = d.nobj;
   unsigned done = 0;
   bool ok = true;

@@ -461,9 +461,20 @@ struct Smem16 {
   float bt[16][kT16Pad];   // B panel transposed, rows n, k contiguous
 };
 
+// Pass 0 of the spectral solve with the density preparation folded in: the
+// A operand is formed while it is loaded, rho = (phys + fill - mean) 2^-32
+// (the formula of stage_prep), and the tiles of the first column band, which
+// load every bin exactly once, also store rho and count the physical
+// overflow (per thread, one slot per field).
+struct PrepFold {
+  const long long* mean;   // [K] fixed-point mean per field
+  long long ov[kMaxFields], cnt[kMaxFields];
+};
+
+template <bool FOLD = false>
 static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb, float* Cm, long sc, int M, int N,
                               int Kd, int nf, int epi, const float* inv_eig, const float* rho, double* energy_acc,
-                              int vb, int nvb, Smem16& sm) {
+                              int vb, int nvb, Smem16& sm, const Dev* dp = nullptr, PrepFold* pf = nullptr) {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int tiles_m = (M + 15) / 16, tiles_n = (N + 15) / 16;
   const int tiles = tiles_m * tiles_n * nf;
@@ -483,7 +494,27 @@ static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb,
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int gm = m0 + ra + 2 * j;
-        va[j] = (gm < M && ca < kn) ? Af[(size_t)gm * Kd + k0 + ca] : 0.f;
+        if (FOLD) {
+          float v = 0.f;
+          if (gm < M && ca < kn) {
+            const size_t i = (size_t)f * dp->B + (size_t)gm * Kd + k0 + ca;
+            const long long a = dp->phys[i];
+            v = __ll2float_rn(a + dp->fill[i] - pf->mean[f]) * kInvFixF;
+            if (n0 == 0) {
+              dp->rho[i] = v;
+              if (a > 0)
+#pragma unroll
+                for (int ff = 0; ff < kMaxFields; ++ff)
+                  if (ff == f) {
+                    pf->ov[ff] += a;
+                    pf->cnt[ff] += 1;
+                  }
+            }
+          }
+          va[j] = v;
+        } else {
+          va[j] = (gm < M && ca < kn) ? Af[(size_t)gm * Kd + k0 + ca] : 0.f;
+        }
         const int kk = rb + 16 * j, gn = n0 + cb;
         vbv[j] = (kk < kn && gn < N) ? Bf[(size_t)(k0 + kk) * N + gn] : 0.f;
       }
@@ -556,6 +587,24 @@ static __device__ void stage_dct_t(const Dev& d, int step, Partials p, int vb, i
   }
   if (step == 3)
     for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), vb, sh.d);
+}
+// stage_prep + pass 0 of stage_dct_t<false> in one phase (small tiles only):
+// the same rho, overflow sums and t1 as the two phases, bit for bit.
+// `mean` holds the fixed-point mean of each field (from the scatter totals).
+static __device__ void stage_prep_dct0(const Dev& d, const long long* mean, Partials p, int vb, int nvb,
+                                       GemmShared& sm, Shared& sh) {
+  const int W = d.g.Wb, H = d.g.Hb;
+  const long sg = d.B;
+  PrepFold pf;
+  pf.mean = mean;
+#pragma unroll
+  for (int f = 0; f < kMaxFields; ++f) pf.ov[f] = pf.cnt[f] = 0;
+  double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
+  gemm16<true>(nullptr, sg, d.CxT, 0, d.t1, sg, H, W, W, d.K, 0, nullptr, nullptr, eacc, vb, nvb, sm.s, &d, &pf);
+  for (int f = 0; f < d.K; ++f) {
+    write_partial(pf.ov[f], islot(p, IS_OVERFLOW + f), vb, sh.l);
+    write_partial(pf.cnt[f], islot(p, IS_OVER_BINS + f), vb, sh.l);
+  }
 }
 __device__ __forceinline__ void stage_dct(const Dev& d, int step, bool large, Partials p, int vb, int nvb,
                                           GemmShared& sm, Shared& sh) {
