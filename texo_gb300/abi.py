@@ -81,7 +81,7 @@ class Params(C.Structure):
         ("bins_x", C.c_uint32), ("bins_y", C.c_uint32), ("target_density", C.c_double),
         ("best_effort", C.c_int32), ("dct_mode", C.c_int32), ("engine", C.c_int32),
         ("device", C.c_int32), ("objective_margin_ulps", C.c_double),
-        ("reserved", C.c_uint32 * 8),
+        ("autotune", C.c_int32), ("reserved", C.c_uint32 * 7),
     ]
 
 
@@ -143,6 +143,7 @@ def default_params_py():
     p.engine = ENGINE_HOST
     p.device = 0
     p.objective_margin_ulps = 64.0
+    p.autotune = 0
     return p
 
 
@@ -164,6 +165,7 @@ SIGNATURES = {
     "texo_gp_poisson": (C.c_int32, [_P, c_f64p, c_f64p, c_f64p]),
     "texo_gp_scatter_static": (C.c_int32, [_P, c_f64p, c_i64p, c_i64p]),
     "texo_gp_run": (C.c_int32, [_P, C.c_uint32, c_u32p, c_f64p, C.POINTER(Stats)]),
+    "texo_gp_dct_form": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "texo_gp_reset": (C.c_int32, [_P]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
     "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),

@@ -158,35 +158,42 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
   std::vector<size_t> pick(n);
   for (size_t i = 0; i < n; ++i) pick[i] = (b->rr + i) % nres;
   b->rr = (b->rr + n) % std::max<size_t>(nres, 1);
-  // physical blocks proportional to virtual blocks, at least one each
-  long long vsum = 0;
-  for (size_t i = 0; i < n; ++i) vsum += b->resident[pick[i]].V;
-  std::vector<int> share(n, 1);
-  int used = (int)n;
+  std::vector<char> lg(n, 0);
   for (size_t i = 0; i < n; ++i) {
-    const int V = b->resident[pick[i]].V;
-    const int want = std::max(1, (int)((long long)(P - (int)n) * V / std::max(vsum, 1ll)) + 1);
-    const int add = std::min(std::min(want, V) - 1, P - used);
-    if (add > 0) {
-      share[i] += add;
-      used += add;
-    }
-  }
-  b->h_map.clear();
-  bool large = false;
-  for (size_t i = 0; i < n; ++i) {
-    bool lg = false;
-    const int32_t s = batch_stage_in(b->resident[pick[i]].h, iterations, b->stream, &b->h_descs[i], &lg);
-    if (s) return s;
-    large |= lg;
-    for (int k = 0; k < share[i]; ++k) b->h_map.push_back(make_int4((int)i, k, share[i], 0));
+    bool large = false;
+    const int32_t st = batch_stage_in(b->resident[pick[i]].h, iterations, b->stream, &b->h_descs[i], &large);
+    if (st) return st;
+    lg[i] = large ? 1 : 0;
   }
   BCU(cudaMemcpyAsync(b->d_descs, b->h_descs.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, b->stream));
-  BCU(cudaMemcpyAsync(b->d_map, b->h_map.data(), sizeof(int4) * b->h_map.size(), cudaMemcpyHostToDevice, b->stream));
-  int32_t s = launch_batch(b->d_descs, b->d_map, (int)b->h_map.size(), large, b->stream);
-  if (s) {
-    set_last_error(std::string("batch launch: ") + cudaGetErrorString(cudaGetLastError()));
-    return s;
+  // One launch per DCT tile family (a job runs the same kernel instantiation
+  // as it does alone); physical blocks proportional to virtual blocks, at
+  // least one each.
+  int32_t s = TEXO_GP_OK;
+  for (int fam = 0; fam < 2; ++fam) {
+    std::vector<size_t> jobs;
+    for (size_t i = 0; i < n; ++i)
+      if (lg[i] == fam) jobs.push_back(i);
+    if (jobs.empty()) continue;
+    const int nj = (int)jobs.size();
+    long long vsum = 0;
+    for (size_t i : jobs) vsum += b->resident[pick[i]].V;
+    b->h_map.clear();
+    int used = nj;
+    for (size_t i : jobs) {
+      const int V = b->resident[pick[i]].V;
+      const int want = std::max(1, (int)((long long)(P - nj) * V / std::max(vsum, 1ll)) + 1);
+      const int add = std::max(0, std::min(std::min(want, V) - 1, P - used));
+      used += add;
+      for (int k = 0; k < 1 + add; ++k) b->h_map.push_back(make_int4((int)i, k, 1 + add, 0));
+    }
+    BCU(cudaMemcpyAsync(b->d_map, b->h_map.data(), sizeof(int4) * b->h_map.size(), cudaMemcpyHostToDevice,
+                        b->stream));
+    s = launch_batch(b->d_descs, b->d_map, (int)b->h_map.size(), fam == 1, b->stream);
+    if (s) {
+      set_last_error(std::string("batch launch: ") + cudaGetErrorString(cudaGetLastError()));
+      return s;
+    }
   }
   for (size_t i = 0; i < n; ++i) {
     s = batch_stage_out(b->resident[pick[i]].h, b->stream, &b->resident[pick[i]].hbar);

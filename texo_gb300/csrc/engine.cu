@@ -458,6 +458,8 @@ int32_t Instance::upload() {
     D.CyT = by.ct;
     D.inv_eig = ie;
     D.tc = h.params.dct_mode == TEXO_GP_DCT_BF16X3 ? 1 : 0;
+    // fixed rule unless autotuned: large tiles once the grid has >= 1024 32x32 blocks
+    D.dct_large = (long long)((h.Wb + 31) / 32) * ((h.Hb + 31) / 32) >= 1024 ? 1 : 0;
     D.Hp128 = tc::pad((int)h.Hb, tc::kM);
     D.Hp32 = tc::pad((int)h.Hb, tc::kKC);
     D.Wp64 = tc::pad((int)h.Wb, tc::kN);
@@ -1096,7 +1098,7 @@ int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, Ins
   desc->bar = I.bar;
   desc->V = I.nvb;
   desc->pad = 0;
-  *large = (long long)((I.d.g.Wb + 31) / 32) * ((I.d.g.Hb + 31) / 32) >= 1024;
+  *large = I.d.dct_large != 0;
   return TEXO_GP_OK;
 }
 int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s, GridBarrier* host_bar) {
@@ -1145,6 +1147,66 @@ std::mutex* handle_mutex(texo_gp_handle_s* h) { return &h->mu; }
 }  // namespace tgp
 
 namespace {
+// The autotuner: times the four DCT passes of every admissible form on this
+// instance (5 repetitions after a warm-up, CUDA events on its stream) and
+// keeps the fastest. The FP32 tile families are always admissible; the
+// tensor-core form only when the caller asked for BF16x3 (the FP32 forms are
+// more accurate, so they may replace it). Choices are cached per device,
+// grid, field count, engine and requested mode.
+int32_t autotune_dct(Instance& I) {
+  struct Form {
+    int large, tc;
+  };
+  const texo_gp_params& prm = I.m.params;
+  std::vector<Form> forms = {{0, 0}, {1, 0}};
+  if (prm.dct_mode == TEXO_GP_DCT_BF16X3 && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1});
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, int, int>, Form> cache;
+  const auto key = std::make_tuple(I.device, I.m.Wb, I.m.Hb, I.m.K, prm.engine, prm.dct_mode);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      I.d.dct_large = it->second.large;
+      I.d.tc = it->second.tc;
+      return TEXO_GP_OK;
+    }
+  }
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  float best = 1e30f;
+  Form pick = forms[0];
+  for (const Form& f : forms) {
+    Dev D = I.d;
+    D.dct_large = f.large;
+    D.tc = f.tc;
+    float t = 1e30f;
+    for (int rep = 0; rep < 6; ++rep) {
+      CU(cudaEventRecord(a, I.stream));
+      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream);
+      CU(cudaEventRecord(b, I.stream));
+      CU(cudaEventSynchronize(b));
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0) t = std::min(t, ms);   // the first run is a warm-up
+    }
+    if (t < best) {
+      best = t;
+      pick = f;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CU(cudaMemsetAsync(I.r.iscal + SI_TC_FAIL, 0, sizeof(long long), I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  I.d.dct_large = pick.large;
+  I.d.tc = pick.tc;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = pick;
+  return TEXO_GP_OK;
+}
+
 uint32_t round_coord(double v, uint32_t extent) {
   double r = std::round(v);
   r = r < 0.0 ? 0.0 : (r > (double)(extent - 1) ? (double)(extent - 1) : r);
@@ -1210,6 +1272,7 @@ void texo_gp_default_params(texo_gp_params* p) {
   p->target_density = 1.0;
   p->best_effort = 0;
   p->dct_mode = TEXO_GP_DCT_FP32;
+  p->autotune = 0;
   p->engine = TEXO_GP_ENGINE_HOST;
   p->device = 0;
   p->objective_margin_ulps = 64.0;
@@ -1266,12 +1329,19 @@ int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo
   *out = nullptr;
   texo_gp_handle h = nullptr;
   TRY(tgp::handle_build(p, prm, &h, nullptr));
-  const int32_t s = tgp::handle_upload(h);
+  int32_t s = tgp::handle_upload(h);
+  if (!s && h->inst->m.params.autotune) s = autotune_dct(*h->inst);
   if (s) {
     delete h;
     return s;
   }
   *out = h;
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_dct_form(texo_gp_handle h, int32_t* form) {
+  if (!h || !form) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  *form = h->inst->d.tc ? 2 : (h->inst->d.dct_large ? 1 : 0);
   return TEXO_GP_OK;
 }
 

@@ -193,9 +193,7 @@ unsigned long long launches_issued() { return t_launches; }
 void note_launch() { ++t_launches; }
 #define COUNT ++t_launches
 
-static inline bool use_large_tiles(const Dev& d) {
-  return (long long)((d.g.Wb + 31) / 32) * ((d.g.Hb + 31) / 32) >= 1024;
-}
+static inline bool use_large_tiles(const Dev& d) { return d.dct_large != 0; }
 
 void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s) {
   COUNT;

@@ -24,7 +24,7 @@ int batch_blocks_per_sm() {
   return a < b ? a : b;
 }
 
-static bool large_tiles(const Dev& d) { return (long long)((d.g.Wb + 31) / 32) * ((d.g.Hb + 31) / 32) >= 1024; }
+static bool large_tiles(const Dev& d) { return d.dct_large != 0; }
 
 int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRun* run_dev, DevRun* host_run,
                           GridBarrier* bar, int blocks, int V, cudaStream_t s) {
