@@ -422,6 +422,13 @@ int32_t texo_gp_server_counts(texo_gp_server s, uint32_t* queued, uint32_t* resi
                               uint32_t* finished, uint64_t* bytes_in_use);
 double texo_gp_server_clock_ms(texo_gp_server s);
 
+/* Diagnostic: runs the engine's bounded device waits (the grid barrier of
+ * the persistent loop and the mbarrier wait of the tensor-core pipeline)
+ * against partners that never arrive, with a short limit. Both must run out
+ * (flags set to 1) and return without faulting; the device stays usable. No
+ * counterpart in the reference. */
+int32_t texo_gp_selftest_waits(int32_t device, int32_t* barrier_timed_out, int32_t* mbarrier_timed_out);
+
 #ifdef __cplusplus
 }
 #endif

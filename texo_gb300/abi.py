@@ -185,6 +185,7 @@ SIGNATURES = {
     "texo_gp_server_poll": (C.c_int32, [_P, C.c_int32, C.POINTER(JobResult), c_u32p, C.c_uint64]),
     "texo_gp_server_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u32p, c_u64p]),
     "texo_gp_server_clock_ms": (C.c_double, [_P]),
+    "texo_gp_selftest_waits": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
 }
 
 _lib = None

@@ -58,7 +58,7 @@ __device__ __forceinline__ unsigned long long load_gen_error(const GridBarrier* 
 // counter and release-increments the generation the others poll with
 // acquire loads, which also carry the error word.
 __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned np, unsigned* gen, unsigned long long* count,
-                                          unsigned long long* wait_acc, int* failed) {
+                                          unsigned long long* wait_acc, int* failed, unsigned limit = kSpinLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned long long t0 = wait_acc ? now_ns() : 0ull;
@@ -77,7 +77,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned np, unsigned*
       for (;;) {
         ge = load_gen_error(b);
         if ((unsigned)ge != g || (ge >> 32) != 0ull) break;
-        if (++spins > kSpinLimit) {
+        if (++spins > limit) {
           atomicExch(&b->error, 1);
           ge |= 1ull << 32;
           break;
