@@ -15,8 +15,9 @@
 // in the layout the next pass reads, so no pass converts its inputs.
 //
 // One 128 x 64 output tile per block iteration. Thread 0 runs a four-stage
-// pipeline: TMA bulk copies (cp.async.bulk, complete_tx on a "full"
-// mbarrier) keep the next three K-chunks in flight while the six MMAs of
+// pipeline: TMA tensor copies (cp.async.bulk.tensor through the operands'
+// tensor maps, complete_tx on a "full" mbarrier) keep the next three K-chunks
+// in flight while the six MMAs of
 // chunk c (two K = 16 steps x three split terms) run, and each commit
 // arrives on that stage's "empty" mbarrier before the stage is reloaded.
 // The accumulator occupies 64 TMEM columns (row i = lane i); the epilogue
@@ -27,6 +28,7 @@
 // `failed` and the caller's error word), waits once more (bounded) for its
 // own copies and MMAs, frees its tensor memory and leaves its tiles undone.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -49,6 +51,15 @@ constexpr unsigned kWaitLimit = 1u << 22;      // mbarrier polls before giving u
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
+
+// TMA descriptors of the tiled operands, each a 2-D view of one operand
+// buffer as rows of 128 bytes (64 bf16 halves): an A block is a 64 x 128
+// box (16 KB), a B block a 64 x 64 box (8 KB). The data are already in the
+// MMA's shared-memory layout, so the copies use no swizzle.
+enum TcMap { TM_RHO = 0, TM_T1, TM_T2, TM_T3, TM_CXB, TM_CYA, TM_CYTA, TM_CXTB, TM_COUNT };
+struct alignas(64) TcMaps {
+  CUtensorMap m[TM_COUNT];
+};
 
 // ---- layout (host and device) ------------------------------------------------
 __host__ __device__ inline uint32_t kmaj(int r, int k) {
@@ -120,10 +131,13 @@ __device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(mbar)
-               : "memory");
+// One block of a tiled operand: box of 128-byte rows starting at row y.
+__device__ __forceinline__ void tensor_load(uint32_t dst, const CUtensorMap* map, int y, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((unsigned long long)map), "r"(0), "r"(y), "r"(mbar)
+      : "memory");
 }
 
 // Block-wide: tensor memory and the mbarriers (every thread calls it).
@@ -212,8 +226,8 @@ __device__ __forceinline__ void emit(const Out& o, int f, int row, int col, int 
 // C[f] = A[f] (M x K) * B[f]^T, B given as N x K, both tiled; output tiles
 // t = vb, vb + nvb, ... of 128 x 64, written by `out`. kp = K padded to 32.
 // The block must have called setup(); blockDim.x must be 256.
-static __device__ void gemm(const uint16_t* A, long sa, const uint16_t* B, long sb, int M, int N, int kp, int nf,
-                            const Out& out, double* eacc, int vb, int nvb, Smem& sm, unsigned long long* err) {
+static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* mB, long sb, int M, int N, int kp,
+                            int nf, const Out& out, double* eacc, int vb, int nvb, Smem& sm, unsigned long long* err) {
   const int tiles_m = (M + kM - 1) / kM, tiles_n = (N + kN - 1) / kN;
   const int tiles = tiles_m * tiles_n * nf;
   const int nkc = kp / kKC;
@@ -226,8 +240,9 @@ static __device__ void gemm(const uint16_t* A, long sa, const uint16_t* B, long 
     const int mt = rr / tiles_n, nt = rr % tiles_n;
     if (threadIdx.x == 0) {
       fence_global_async();
-      const uint16_t* a0 = A + (size_t)f * sa + (size_t)mt * nkc * kABlock;
-      const uint16_t* b0 = B + (size_t)f * sb + (size_t)nt * nkc * kBBlock;
+      // first 128-byte row of this tile's K-chunk 0 in each operand
+      const int a0 = (int)(((size_t)f * sa + (size_t)mt * nkc * kABlock) / 64);
+      const int b0 = (int)(((size_t)f * sb + (size_t)nt * nkc * kBBlock) / 64);
       bool bad = false;
       bool busy[kStages], loading[kStages];   // a commit / a copy not yet waited for
       for (int s = 0; s < kStages; ++s) busy[s] = loading[s] = false;
@@ -246,8 +261,8 @@ static __device__ void gemm(const uint16_t* A, long sa, const uint16_t* B, long 
         if (bad) return;
         const uint32_t fb = saddr(&sm.full[s]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kTx) : "memory");
-        bulk_load(saddr(sm.st[s].a), a0 + (size_t)c * kABlock, kABlock * 2u, fb);
-        bulk_load(saddr(sm.st[s].b), b0 + (size_t)c * kBBlock, kBBlock * 2u, fb);
+        tensor_load(saddr(sm.st[s].a), mA, a0 + c * (int)(kABlock / 64), fb);
+        tensor_load(saddr(sm.st[s].b), mB, b0 + c * (int)(kBBlock / 64), fb);
         loading[s] = true;
       };
       for (int c = 0; c < kStages - 1 && c < nkc; ++c) produce(c);
@@ -325,29 +340,29 @@ __device__ __forceinline__ int pass_tiles(const Dev& d) {
 // One of the four GEMM passes of the spectral solve (the passes of the FP32
 // form): t1 = rho Cx^T, t2 = (Cy t1) / lambda, t3 = Cy^T t2, phi = t3 Cx with
 // the energy <rho, phi>.
-static __device__ void dct_pass(const Dev& d, int step, int vb, int nvb, Smem& sm, double* eacc,
+static __device__ void dct_pass(const Dev& d, const TcMaps& tm, int step, int vb, int nvb, Smem& sm, double* eacc,
                                 unsigned long long* err) {
   const int W = d.g.Wb, H = d.g.Hb;
   const long sA = (long)d.Hp128 * d.Wp32 * 2, sB = (long)d.Wp64 * d.Hp32 * 2;
   switch (step) {
     case 0: {
       const Out o{0, d.t1_t, sB, d.Hp32, nullptr, nullptr, nullptr};
-      gemm(d.rho_t, sA, d.CxB_t, 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
+      gemm(&tm.m[TM_RHO], sA, &tm.m[TM_CXB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
     }
     case 1: {
       const Out o{1, d.t2_t, sB, d.Hp32, nullptr, nullptr, d.inv_eig};
-      gemm(d.CyA_t, 0, d.t1_t, sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+      gemm(&tm.m[TM_CYA], 0, &tm.m[TM_T1], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
     }
     case 2: {
       const Out o{2, d.t3_t, sA, d.Wp32, nullptr, nullptr, nullptr};
-      gemm(d.CyTA_t, 0, d.t2_t, sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+      gemm(&tm.m[TM_CYTA], 0, &tm.m[TM_T2], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
     }
     default: {
       const Out o{3, nullptr, 0, 0, d.phi, d.rho, nullptr};
-      gemm(d.t3_t, sA, d.CxTB_t, 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
+      gemm(&tm.m[TM_T3], sA, &tm.m[TM_CXTB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
     }
   }

@@ -211,6 +211,38 @@ void release_mirror(double* scal) {
   g_mirror_free.push_back((char*)scal);
 }
 
+// A 2-D tensor map over a tiled tensor-core operand: rows of 64 bf16 halves
+// (128 B), boxes of `box_rows` rows (one A or B block).
+int32_t encode_operand_map(CUtensorMap* m, const uint16_t* base, size_t elems, uint32_t box_rows) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return (Encode)fn;
+  }();
+  if (!encode) {
+    set_last_error("cuTensorMapEncodeTiled is not available from the driver");
+    return TEXO_GP_ERR_CUDA;
+  }
+  const cuuint64_t dims[2] = {64, (cuuint64_t)(elems / 64)};
+  const cuuint64_t strides[1] = {128};
+  const cuuint32_t box[2] = {64, box_rows};
+  const cuuint32_t unit[2] = {1, 1};
+  if (encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, (void*)base, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+    set_last_error("cuTensorMapEncodeTiled rejected a tensor-core operand map");
+    return TEXO_GP_ERR_CUDA;
+  }
+  return TEXO_GP_OK;
+}
+
 // Lanes of the WA stage per degree class: every class gets its own
 // warp-aligned segment of the launch's T lanes (one G-lane group per net),
 // all nets in one pass when they fit, otherwise segments in proportion to the
@@ -511,6 +543,18 @@ int32_t Instance::upload() {
     h_scal[SC_E0 + f] = 1.0;
     h_scal[SC_LAMBDA + f] = 0.0;
   }
+  if (h.params.dct_mode == TEXO_GP_DCT_BF16X3) {   // tensor maps of the tensor-core operands
+    const size_t a = (size_t)D.Hp128 * D.Wp32 * 2 * K, b = (size_t)D.Wp64 * D.Hp32 * 2 * K;
+    const uint32_t ra = tc::kABlock / 64, rb = tc::kBBlock / 64;
+    TRY(encode_operand_map(&tmaps.m[tc::TM_RHO], D.rho_t, a, ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_T3], D.t3_t, a, ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_T1], D.t1_t, b, rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_T2], D.t2_t, b, rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CXB], D.CxB_t, (size_t)D.Wp64 * D.Wp32 * 2, rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CXTB], D.CxTB_t, (size_t)D.Wp64 * D.Wp32 * 2, rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CYA], D.CyA_t, (size_t)D.Hp128 * D.Hp32 * 2, ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CYTA], D.CyTA_t, (size_t)D.Hp128 * D.Hp32 * 2, ra));
+  }
   // the staging buffer is reused by this thread's next upload
   CU(cudaStreamSynchronize(stream));
   return TEXO_GP_OK;
@@ -601,7 +645,7 @@ struct Controller {
       launch_init(D, true, true, nvb, s);
       launch_scatter(D, I.r, pos, nvb, s);
       launch_prep(D, I.r, nvb, s);
-      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, nvb, s);
+      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, nvb, s, &I.tmaps);
       launch_gather(D, I.r, pos, nvb, s);
     } else {
       launch_init(D, false, true, nvb, s);
@@ -1184,7 +1228,7 @@ int32_t autotune_dct(Instance& I) {
     float t = 1e30f;
     for (int rep = 0; rep < 6; ++rep) {
       CU(cudaEventRecord(a, I.stream));
-      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream);
+      for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream, &I.tmaps);
       CU(cudaEventRecord(b, I.stream));
       CU(cudaEventSynchronize(b));
       float ms = 0.f;
@@ -1482,7 +1526,7 @@ int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potenti
   D.K = 1;
   CU(cudaMemcpyAsync(D.rho, rho.data(), B * 4, cudaMemcpyHostToDevice, I.stream));
   if (D.tc) launch_tile_rho(D, I.nvb, I.stream);
-  for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream);
+  for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream, &I.tmaps);
   launch_finalize(D, I.r, I.nvb, FIN_ENERGY, I.stream);
   std::vector<float> phi(B);
   CU(cudaMemcpyAsync(phi.data(), D.phi, B * 4, cudaMemcpyDeviceToHost, I.stream));
@@ -1588,7 +1632,7 @@ int32_t texo_gp_stage_times(texo_gp_handle h, uint32_t reps, double* ms, uint32_
         case 1: launch_scatter(D, I.r, I.bufX, nvb, s); break;
         case 2: launch_wa(D, I.r, I.bufX, gam, nvb, s); break;
         case 3: launch_prep(D, I.r, nvb, s); break;
-        case 4: case 5: case 6: case 7: launch_dct(D, I.r, (int)st - 4, nvb, s); break;
+        case 4: case 5: case 6: case 7: launch_dct(D, I.r, (int)st - 4, nvb, s, &I.tmaps); break;
         case 8: launch_gather(D, I.r, I.bufX, nvb, s); break;
         case 9: launch_combine(D, I.r, I.gX, nvb, s); break;
         case 10: launch_finalize(D, I.r, nvb, FIN_ENERGY | FIN_COMBINE, s); break;

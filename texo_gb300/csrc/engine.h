@@ -86,6 +86,7 @@ struct Instance {
   double* h_scal = nullptr;                      // pinned host mirror
   long long* h_iscal = nullptr;
   uint64_t bytes = 0;
+  tc::TcMaps tmaps{};                            // tensor maps of the tensor-core DCT operands
 
   ~Instance();
   int32_t alloc(void** p, size_t bytes);

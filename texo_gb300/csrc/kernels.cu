@@ -12,14 +12,15 @@ __global__ void __launch_bounds__(kThreads) k_tile_rho(Dev d) {
 
 // One DCT pass on tcgen05 tensor cores (BF16x3), one 128 x 64 tile per block
 // iteration; the energy partials of pass 3 are per block as in k_dct.
-__global__ void __launch_bounds__(kThreads) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err) {
+__global__ void __launch_bounds__(kThreads) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err,
+                                                    const __grid_constant__ tc::TcMaps maps) {
   extern __shared__ __align__(128) unsigned char tc_dyn[];
   tc::Smem& sm = *reinterpret_cast<tc::Smem*>(tc_dyn);
   __shared__ Shared sh;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
   if ((int)blockIdx.x < tc::pass_tiles(d)) {   // blocks without a tile only write zero partials
     tc::setup(sm);
-    tc::dct_pass(d, step, blockIdx.x, gridDim.x, sm, eacc, err);
+    tc::dct_pass(d, maps, step, blockIdx.x, gridDim.x, sm, eacc, err);
     tc::teardown(sm);
   }
   if (step == 3)
@@ -215,13 +216,15 @@ void launch_tile_rho(const Dev& d, int nvb, cudaStream_t s) {
   COUNT;
   k_tile_rho<<<nvb, kThreads, 0, s>>>(d);
 }
-void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s) {
+void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s, const tc::TcMaps* maps) {
   COUNT;
   if (d.tc) {
+    if (!maps) return;   // the tensor-core form needs the instance's tensor maps
     static const bool attr = cudaFuncSetAttribute(k_dct_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)sizeof(tc::Smem)) == cudaSuccess;
     (void)attr;
-    k_dct_tc<<<nvb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL));
+    k_dct_tc<<<nvb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL),
+                                                     *maps);
     return;
   }
   if (use_large_tiles(d))

@@ -67,7 +67,8 @@ void launch_scatter(const Dev& d, const Reduce& r, const float2* pos, int nvb, c
 void launch_tile_rho(const Dev& d, int nvb, cudaStream_t s);
 void launch_wa(const Dev& d, const Reduce& r, const float2* pos, double gamma, int nvb, cudaStream_t s);
 void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
-void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s);
+void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s,
+                const tc::TcMaps* maps = nullptr);
 void launch_gather(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s);
 void launch_combine(const Dev& d, const Reduce& r, float2* gout, int nvb, cudaStream_t s);
 void launch_extrapolate(const Dev& d, const Reduce& r, const float2* x, const float2* xp, float e, float2* y,

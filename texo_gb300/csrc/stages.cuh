@@ -488,9 +488,11 @@ static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb,
     const float* Af = A + f * sa;
     const float* Bf = Bm + f * sb;
     float sum = 0.f, comp = 0.f;
-    for (int k0 = 0; k0 < Kd; k0 += kT16Slab) {
+    float va[8], vbv[8];
+    // slab k0 -> registers (the next slab's loads are issued before the
+    // current slab's products, into the registers its smem copy freed)
+    auto fetch = [&](int k0) {
       const int kn = min(kT16Slab, Kd - k0);
-      float va[8], vbv[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int gm = m0 + ra + 2 * j;
@@ -518,6 +520,9 @@ static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb,
         const int kk = rb + 16 * j, gn = n0 + cb;
         vbv[j] = (kk < kn && gn < N) ? Bf[(size_t)(k0 + kk) * N + gn] : 0.f;
       }
+    };
+    fetch(0);
+    for (int k0 = 0; k0 < Kd; k0 += kT16Slab) {
       __syncthreads();
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
@@ -525,6 +530,7 @@ static __device__ void gemm16(const float* A, long sa, const float* Bm, long sb,
         sm.bt[cb][rb + 16 * j] = vbv[j];
       }
       __syncthreads();
+      if (k0 + kT16Slab < Kd) fetch(k0 + kT16Slab);
       const float4* a4 = reinterpret_cast<const float4*>(sm.a[ty]);
       const float4* b4 = reinterpret_cast<const float4*>(sm.bt[tx]);
 #pragma unroll 4
