@@ -176,8 +176,9 @@ typedef struct texo_gp_params {
   int32_t device;                /* CUDA device ordinal */
   double objective_margin_ulps;  /* line-search rounding margin: max(eps64, ulps * 2^-24) (1 + |a| + |b|) */
   int32_t autotune;              /* 1: time the DCT forms on this instance at creation and keep the
-                                    fastest (16x16 or 64x64 FP32 tiles; with dct_mode BF16X3 also the
-                                    tensor-core form, which may give way to the more accurate FP32) */
+                                    fastest (FP32 GEMM with 16x16 or 64x64 tiles, FP32 FFT on
+                                    power-of-two grids; with dct_mode BF16X3 also the tensor-core
+                                    form, which may give way to the more accurate FP32 forms) */
   uint32_t reserved[7];
 } texo_gp_params;
 
@@ -295,9 +296,10 @@ int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potenti
 int32_t texo_gp_scatter_static(texo_gp_handle h, const double* coordinates,
                                int64_t* physical_grid, int64_t* filler_grid);
 
-/* The DCT form the handle runs: 0 FP32 16x16 slab tiles, 1 FP32 64x64
- * register-blocked tiles, 2 tcgen05 tensor cores (BF16x3). No counterpart
- * in the reference (it has one CPU transform). */
+/* The DCT form the handle runs: 0 FP32 GEMM with 16x16 slab tiles, 1 FP32
+ * GEMM with 64x64 register-blocked tiles, 2 tcgen05 tensor cores (BF16x3),
+ * 3 FP32 FFT-based transforms (power-of-two grids; the default there). No
+ * counterpart in the reference (it has one CPU transform). */
 int32_t texo_gp_dct_form(texo_gp_handle h, int32_t* form);
 
 /* Runs the placement loop from the handle's current state (the initial

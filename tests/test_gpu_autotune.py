@@ -32,7 +32,7 @@ def test_autotuned_fp32_form_keeps_the_fp32_bound():
     c = (lo + (hi - lo) * np.random.default_rng(3).random(c.size)).astype(np.float32).astype(np.float64)
     r = o.evaluate(c, 2.0)
     with Placer(prob, default_params(autotune=1, engine=abi.ENGINE_HOST)) as g:
-        assert form(g) in (0, 1)
+        assert form(g) in (0, 1)      # 48 x 48 tiles: not a power of two
         d = g.evaluate(c, 2.0)
         d2 = g.evaluate(c, 2.0)
     for k in ("potential", "field_gradient"):
@@ -44,13 +44,20 @@ def test_autotune_may_choose_the_tensor_cores_only_when_allowed():
     prob = P.synthetic(64, 3000, 100, 3600, 6.0, 4)
     with Placer(prob, default_params(autotune=1, bins_x=1024, bins_y=1024, engine=abi.ENGINE_HOST,
                                      dct_mode=abi.DCT_BF16X3)) as g:
-        assert form(g) in (0, 1, 2)
+        assert form(g) in (0, 1, 2, 3)
     with Placer(prob, default_params(autotune=1, bins_x=1024, bins_y=1024, engine=abi.ENGINE_HOST)) as g:
-        assert form(g) in (0, 1)
+        assert form(g) in (0, 1, 3)
+    # the fixed rules: the FFT form on power-of-two grids, else the GEMM form
+    # with 64x64 tiles from 1024 blocks of 32 x 32 bins up
     with Placer(prob, default_params(bins_x=1024, bins_y=1024)) as g:
-        assert form(g) == 1      # the fixed rule: >= 1024 blocks of 32 x 32 bins
-    with Placer(prob, default_params(bins_x=256, bins_y=256)) as g:
+        assert form(g) == 3
+    with Placer(prob, default_params(bins_x=1000, bins_y=1000)) as g:
+        assert form(g) == 1
+    with Placer(prob, default_params(bins_x=250, bins_y=250)) as g:
         assert form(g) == 0
+    with Placer(prob, default_params(bins_x=1024, bins_y=1024, dct_mode=abi.DCT_BF16X3,
+                                     engine=abi.ENGINE_HOST)) as g:
+        assert form(g) == 2
 
 
 def test_tile_families_share_a_batch_and_match_alone():

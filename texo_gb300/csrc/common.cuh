@@ -85,7 +85,14 @@ struct Dev {
   // in 64 x 32 blocks, zero-padded; rho_t and t3_t are A operands (H x W),
   // t1_t and t2_t B operands (W x H); the bases are shared read-only tables.
   int tc;                    // 1: the DCT passes run on tcgen05 tensor cores
-  int dct_large;             // FP32 form: 1 = 64x64 register-blocked tiles, 0 = 16x16 slab tiles
+  int dct_large;             // FP32 GEMM form: 1 = 64x64 register-blocked tiles, 0 = 16x16 slab tiles
+  // FFT form (power-of-two grids): twiddle tables per axis (dct_fft.cuh)
+  int fft;                   // 1: the DCT passes run as FFT-based transforms
+  int logW, logH;
+  const float2 *fx_tw, *fx_post, *fx_pre;
+  const float* fx_inv_s;
+  const float2 *fy_tw, *fy_post, *fy_pre;
+  const float* fy_inv_s;
   int Hp128, Hp32, Wp64, Wp32;   // padded extents
   uint16_t *rho_t, *t1_t, *t2_t, *t3_t;
   const uint16_t *CxB_t, *CyA_t, *CyTA_t, *CxTB_t;

@@ -157,6 +157,56 @@ cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
   *out = it->second;
   return cudaSuccess;
 }
+// Twiddle tables of the FFT form for one power-of-two length n (FP64 values
+// rounded to FP32): tw[n/2] = exp(-2 pi i j / n), post[n] = s_k exp(-i pi k /
+// 2n), pre[n] = exp(-i pi k / 2n), inv_s[n] = 1 / s_k.
+struct FftTables {
+  float2 *tw = nullptr, *post = nullptr, *pre = nullptr;
+  float* inv_s = nullptr;
+};
+cudaError_t shared_fft(int device, uint32_t n, FftTables* out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, uint32_t>, FftTables> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find({device, n});
+  if (it == cache.end()) {
+    const double pi = 3.14159265358979323846, nf = (double)n;
+    std::vector<float2> tw(n / 2), post(n), pre(n);
+    std::vector<float> inv_s(n);
+    for (uint32_t j = 0; j < n / 2; ++j)
+      tw[j] = make_float2((float)std::cos(-2.0 * pi * j / nf), (float)std::sin(-2.0 * pi * j / nf));
+    for (uint32_t k = 0; k < n; ++k) {
+      const double sk = k == 0 ? std::sqrt(1.0 / nf) : std::sqrt(2.0 / nf);
+      const double c = std::cos(-pi * k / (2.0 * nf)), sn = std::sin(-pi * k / (2.0 * nf));
+      post[k] = make_float2((float)(sk * c), (float)(sk * sn));
+      pre[k] = make_float2((float)c, (float)sn);
+      inv_s[k] = (float)(1.0 / sk);
+    }
+    FftTables t;
+    cudaError_t e = cudaSuccess;
+    auto up = [&](auto** dst, const auto& v) {
+      if (e != cudaSuccess) return;
+      e = cudaMalloc((void**)dst, std::max<size_t>(v.size(), 1) * sizeof(v[0]));
+      if (e == cudaSuccess && !v.empty())
+        e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+    };
+    up(&t.tw, tw);
+    up(&t.post, post);
+    up(&t.pre, pre);
+    up(&t.inv_s, inv_s);
+    if (e != cudaSuccess) return e;
+    it = cache.emplace(std::make_pair(device, n), t).first;
+  }
+  *out = it->second;
+  return cudaSuccess;
+}
+bool fft_length(uint32_t n) { return n >= 2 && n <= 2048 && (n & (n - 1)) == 0; }
+int ilog2(uint32_t n) {
+  int l = 0;
+  while ((1u << l) < n) ++l;
+  return l;
+}
+
 cudaError_t shared_inv_eig(int device, uint32_t Wb, uint32_t Hb, float** out) {
   static std::mutex mu;
   static std::map<std::tuple<int, uint32_t, uint32_t>, float*> cache;
@@ -492,6 +542,24 @@ int32_t Instance::upload() {
     D.tc = h.params.dct_mode == TEXO_GP_DCT_BF16X3 ? 1 : 0;
     // fixed rule unless autotuned: large tiles once the grid has >= 1024 32x32 blocks
     D.dct_large = (long long)((h.Wb + 31) / 32) * ((h.Hb + 31) / 32) >= 1024 ? 1 : 0;
+    // the FFT form for power-of-two grids (FP32 mode)
+    D.fft = 0;
+    D.logW = ilog2(h.Wb);
+    D.logH = ilog2(h.Hb);
+    if (fft_length(h.Wb) && fft_length(h.Hb)) {
+      FftTables fx, fy;
+      CU(shared_fft(device, h.Wb, &fx));
+      CU(shared_fft(device, h.Hb, &fy));
+      D.fx_tw = fx.tw;
+      D.fx_post = fx.post;
+      D.fx_pre = fx.pre;
+      D.fx_inv_s = fx.inv_s;
+      D.fy_tw = fy.tw;
+      D.fy_post = fy.post;
+      D.fy_pre = fy.pre;
+      D.fy_inv_s = fy.inv_s;
+      D.fft = D.tc ? 0 : 1;
+    }
     D.Hp128 = tc::pad((int)h.Hb, tc::kM);
     D.Hp32 = tc::pad((int)h.Hb, tc::kKC);
     D.Wp64 = tc::pad((int)h.Wb, tc::kN);
@@ -1199,11 +1267,12 @@ namespace {
 // grid, field count, engine and requested mode.
 int32_t autotune_dct(Instance& I) {
   struct Form {
-    int large, tc;
+    int large, tc, fft;
   };
   const texo_gp_params& prm = I.m.params;
-  std::vector<Form> forms = {{0, 0}, {1, 0}};
-  if (prm.dct_mode == TEXO_GP_DCT_BF16X3 && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1});
+  std::vector<Form> forms = {{0, 0, 0}, {1, 0, 0}};
+  if (fft_length(I.m.Wb) && fft_length(I.m.Hb)) forms.push_back({0, 0, 1});
+  if (prm.dct_mode == TEXO_GP_DCT_BF16X3 && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1, 0});
   static std::mutex mu;
   static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, int, int>, Form> cache;
   const auto key = std::make_tuple(I.device, I.m.Wb, I.m.Hb, I.m.K, prm.engine, prm.dct_mode);
@@ -1213,6 +1282,7 @@ int32_t autotune_dct(Instance& I) {
     if (it != cache.end()) {
       I.d.dct_large = it->second.large;
       I.d.tc = it->second.tc;
+      I.d.fft = it->second.fft;
       return TEXO_GP_OK;
     }
   }
@@ -1225,6 +1295,7 @@ int32_t autotune_dct(Instance& I) {
     Dev D = I.d;
     D.dct_large = f.large;
     D.tc = f.tc;
+    D.fft = f.fft;
     float t = 1e30f;
     for (int rep = 0; rep < 6; ++rep) {
       CU(cudaEventRecord(a, I.stream));
@@ -1246,6 +1317,7 @@ int32_t autotune_dct(Instance& I) {
   CU(cudaStreamSynchronize(I.stream));
   I.d.dct_large = pick.large;
   I.d.tc = pick.tc;
+  I.d.fft = pick.fft;
   std::lock_guard<std::mutex> lk(mu);
   cache[key] = pick;
   return TEXO_GP_OK;
@@ -1385,7 +1457,8 @@ int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo
 
 int32_t texo_gp_dct_form(texo_gp_handle h, int32_t* form) {
   if (!h || !form) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  *form = h->inst->d.tc ? 2 : (h->inst->d.dct_large ? 1 : 0);
+  const Dev& d = h->inst->d;
+  *form = d.tc ? 2 : (d.fft ? 3 : (d.dct_large ? 1 : 0));
   return TEXO_GP_OK;
 }
 

@@ -1,4 +1,5 @@
 // kernels.cu — standalone kernels (one stage each) and their launchers.
+#include "dct_fft.cuh"
 #include "dct_tc.cuh"
 #include "kernels.cuh"
 
@@ -8,6 +9,22 @@ namespace tgp {
 __global__ void __launch_bounds__(kThreads) k_tile_rho(Dev d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.K * d.B; i += gridDim.x * blockDim.x)
     tc::put_rho(d, i / d.B, i % d.B, d.rho[i]);
+}
+
+// The FFT form's three passes (dct_fft.cuh).
+__global__ void __launch_bounds__(kThreads) k_fft_rows_fwd(Dev d, Partials p) {
+  __shared__ fft::Smem sm;
+  __shared__ Shared sh;
+  fft::pass_rows_fwd(d, p, blockIdx.x, gridDim.x, sm, sh, nullptr);
+}
+__global__ void __launch_bounds__(kThreads) k_fft_cols(Dev d) {
+  __shared__ fft::Smem sm;
+  fft::pass_cols(d, blockIdx.x, gridDim.x, sm);
+}
+__global__ void __launch_bounds__(kThreads) k_fft_rows_inv(Dev d, Partials p) {
+  __shared__ fft::Smem sm;
+  __shared__ Shared sh;
+  fft::pass_rows_inv(d, p, blockIdx.x, gridDim.x, sm, sh);
 }
 
 // One DCT pass on tcgen05 tensor cores (BF16x3), one 128 x 64 tile per block
@@ -217,6 +234,17 @@ void launch_tile_rho(const Dev& d, int nvb, cudaStream_t s) {
   k_tile_rho<<<nvb, kThreads, 0, s>>>(d);
 }
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s, const tc::TcMaps* maps) {
+  if (d.fft) {   // rows, columns (forward, scale, inverse), rows: step 2 has no work
+    if (step == 2) return;
+    COUNT;
+    if (step == 0)
+      k_fft_rows_fwd<<<nvb, kThreads, 0, s>>>(d, r.p);
+    else if (step == 1)
+      k_fft_cols<<<nvb, kThreads, 0, s>>>(d);
+    else
+      k_fft_rows_inv<<<nvb, kThreads, 0, s>>>(d, r.p);
+    return;
+  }
   COUNT;
   if (d.tc) {
     if (!maps) return;   // the tensor-core form needs the instance's tensor maps

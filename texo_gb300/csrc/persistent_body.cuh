@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "dct_fft.cuh"
 #include "persistent.cuh"
 
 namespace tgp {
@@ -168,25 +169,41 @@ struct Ctx {
     if (!sync()) return false;
     mark(PC_SCATTER_WA);
     if (full) {
-      int st0 = 0;
-      if (LARGE) {
-        for (int v = pb; v < V; v += np) stage_prep(d, r.p, V, v, V, sh);
-        if (!sync()) return false;
-        mark(PC_PREP);
-      } else {
-        // density preparation folded into the first transform (one phase less)
+      if (d.fft) {
+        // FFT form: rows (with the density preparation folded in), columns, rows
         for (int f = 0; f < d.K; ++f) {
           const long long tot = block_reduce_array(islot(r.p, IS_GRID_SUM + f), V, 0ll, OpAdd(), rl);
           if (threadIdx.x == 0) fmean[f] = (tot - d.capsum[f]) / d.B;
         }
         __syncthreads();
-        for (int v = pb; v < V; v += np) stage_prep_dct0(d, fmean, r.p, v, V, gsm, sh);
+        fft::Smem& fs = *reinterpret_cast<fft::Smem*>(gsm.fft);
+        for (int v = pb; v < V; v += np) fft::pass_rows_fwd(d, r.p, v, V, fs, sh, fmean);
         if (!sync()) return false;
-        st0 = 1;
-      }
-      for (int st = st0; st < 4; ++st) {
-        for (int v = pb; v < V; v += np) stage_dct_t<LARGE>(d, st, r.p, v, V, gsm, sh);
+        for (int v = pb; v < V; v += np) fft::pass_cols(d, v, V, fs);
         if (!sync()) return false;
+        for (int v = pb; v < V; v += np) fft::pass_rows_inv(d, r.p, v, V, fs, sh);
+        if (!sync()) return false;
+      } else {
+        int st0 = 0;
+        if (LARGE) {
+          for (int v = pb; v < V; v += np) stage_prep(d, r.p, V, v, V, sh);
+          if (!sync()) return false;
+          mark(PC_PREP);
+        } else {
+          // density preparation folded into the first transform (one phase less)
+          for (int f = 0; f < d.K; ++f) {
+            const long long tot = block_reduce_array(islot(r.p, IS_GRID_SUM + f), V, 0ll, OpAdd(), rl);
+            if (threadIdx.x == 0) fmean[f] = (tot - d.capsum[f]) / d.B;
+          }
+          __syncthreads();
+          for (int v = pb; v < V; v += np) stage_prep_dct0(d, fmean, r.p, v, V, gsm, sh);
+          if (!sync()) return false;
+          st0 = 1;
+        }
+        for (int st = st0; st < 4; ++st) {
+          for (int v = pb; v < V; v += np) stage_dct_t<LARGE>(d, st, r.p, v, V, gsm, sh);
+          if (!sync()) return false;
+        }
       }
       mark(PC_DCT);
       for (int f = 0; f < d.K; ++f) {

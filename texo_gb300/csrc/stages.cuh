@@ -564,6 +564,7 @@ using SmemL = GemmSmem<64, 64, 16, 4, 4>;
 union alignas(16) GemmShared {
   Smem16 s;
   SmemL l;
+  float2 fft[2048];   // work buffer of the FFT form (fft::Smem)
 };
 
 template <bool LARGE>
