@@ -417,11 +417,11 @@ def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
-    the FP32 and BF16x3 (tensor-core) DCT forms against the FP64 oracle at
+    the FP32 FFT, FP32 GEMM and BF16x3 (tensor-core) DCT forms against the FP64 oracle at
     identical spread positions, gradient cosine similarity, and each form's
     final HPWL / overflow after `iterations` GP iterations. The oracle cannot
     run 1000 FP64 iterations of this size in a bench, so the final HPWL is
-    compared between the two GPU forms."""
+    compared between the GPU forms."""
     import numpy as np
     from oracle import ffi
     from texo_gb300 import abi
@@ -445,16 +445,19 @@ def precision_report(iterations=1000, seed=0, threads=5):
 
     out = {"workload": "stress-1m", "positions": "uniform in the bounds, FP32-representable",
            "oracle_eval_s": t_oracle}
-    for name, mode in (("fp32", abi.DCT_FP32), ("bf16x3", abi.DCT_BF16X3)):
+    import ctypes as C
+    for name, mode in (("fp32_fft", abi.DCT_FP32), ("fp32_gemm", abi.DCT_FP32_GEMM), ("bf16x3", abi.DCT_BF16X3)):
         prm = make_params("stress-1m", abi.ENGINE_HOST, mode)
         prm.max_iterations = iterations
         with Placer(prob, prm) as g:
+            form = C.c_int32()
+            g.lib.texo_gp_dct_form(g.h, C.byref(form))
             d = g.evaluate(c, gamma)
             st = g.stage_times(reps=5)
             t1 = time.perf_counter()
             _, _, s = g.run(allow_nonconverged=True)
             run_s = time.perf_counter() - t1
-        out[name] = {"potential_max_rel_err": nw(d["potential"], r["potential"]),
+        out[name] = {"dct_form": int(form.value), "potential_max_rel_err": nw(d["potential"], r["potential"]),
                      "field_gradient_max_rel_err": nw(d["field_gradient"], r["field_gradient"]),
                      "field_gradient_cosine": cos(d["field_gradient"], r["field_gradient"]),
                      "wa_gradient_cosine": cos(d["wa_gradient"], r["wa_gradient"]),
@@ -463,7 +466,8 @@ def precision_report(iterations=1000, seed=0, threads=5):
                                                                        "dct_row_inv")],
                      "final_hpwl": s["hpwl"], "final_overflow": s["overflow"], "iterations": s["iterations"],
                      "converged": s["converged"], "run_s": run_s, "gpu_ms": s["elapsed_ms"]}
-    out["final_hpwl_bf16x3_vs_fp32"] = out["bf16x3"]["final_hpwl"] / out["fp32"]["final_hpwl"] - 1.0
+    out["final_hpwl_bf16x3_vs_fp32_gemm"] = out["bf16x3"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
+    out["final_hpwl_fp32_fft_vs_fp32_gemm"] = out["fp32_fft"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
     return out
 
 
@@ -483,7 +487,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lfe5u-85-42k", choices=sorted(WORKLOADS))
     ap.add_argument("--engine", default="device", choices=["host", "device"])
-    ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3"])
+    ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3", "fp32-gemm"])
     ap.add_argument("--reference-sample", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -531,7 +535,7 @@ def main():
                               "serving": serve_report(args.serve_requests)}), flush=True)
         return
     engine = abi.ENGINE_HOST if args.engine == "host" else abi.ENGINE_DEVICE
-    dct = abi.DCT_FP32 if args.dct == "fp32" else abi.DCT_BF16X3
+    dct = {"fp32": abi.DCT_FP32, "bf16x3": abi.DCT_BF16X3, "fp32-gemm": abi.DCT_FP32_GEMM}[args.dct]
     prob = make_problem(args.workload, rank)
     prm = make_params(args.workload, engine, dct)
     prm.device = local

@@ -147,8 +147,9 @@ typedef struct texo_gp_problem {
 
 /* DCT forms for the spectral Poisson solve. */
 typedef enum texo_gp_dct_mode {
-  TEXO_GP_DCT_FP32 = 0,     /* plain FP32 CUDA-core GEMM transform */
-  TEXO_GP_DCT_BF16X3 = 1    /* tcgen05 tensor cores, BF16x3 split, FP32 accumulate */
+  TEXO_GP_DCT_FP32 = 0,      /* FP32: FFT-based transforms on power-of-two grids, else the GEMM form */
+  TEXO_GP_DCT_BF16X3 = 1,    /* tcgen05 tensor cores, BF16x3 split, FP32 accumulate */
+  TEXO_GP_DCT_FP32_GEMM = 2  /* FP32 compensated GEMM against the cosine matrices on every grid */
 } texo_gp_dct_mode;
 
 /* Controller forms. */

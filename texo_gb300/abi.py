@@ -30,7 +30,7 @@ STATUS = {
 CODE = {v: k for k, v in STATUS.items()}
 
 KIND_LOGIC, KIND_LUT, KIND_REGISTER, KIND_MEMORY, KIND_CLOCK, KIND_IO, KIND_CONSTANT, KIND_DSP = range(8)
-DCT_FP32, DCT_BF16X3 = 0, 1
+DCT_FP32, DCT_BF16X3, DCT_FP32_GEMM = 0, 1, 2
 ENGINE_HOST, ENGINE_DEVICE = 0, 1
 MAX_FIELDS = 4
 

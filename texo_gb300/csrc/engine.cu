@@ -558,7 +558,7 @@ int32_t Instance::upload() {
       D.fy_post = fy.post;
       D.fy_pre = fy.pre;
       D.fy_inv_s = fy.inv_s;
-      D.fft = D.tc ? 0 : 1;
+      D.fft = h.params.dct_mode == TEXO_GP_DCT_FP32 ? 1 : 0;
     }
     D.Hp128 = tc::pad((int)h.Hb, tc::kM);
     D.Hp32 = tc::pad((int)h.Hb, tc::kKC);
@@ -1234,7 +1234,9 @@ int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_g
     prm = &defaults;
   }
   if (!p) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3 &&
+      prm->dct_mode != TEXO_GP_DCT_FP32_GEMM)
+    return TEXO_GP_ERR_INVALID_ARGUMENT;
   if (prm->dct_mode == TEXO_GP_DCT_BF16X3 && prm->engine == TEXO_GP_ENGINE_DEVICE) {
     set_last_error("the BF16x3 tensor-core DCT runs with the host engine only");
     return TEXO_GP_ERR_UNSUPPORTED;
@@ -1271,7 +1273,7 @@ int32_t autotune_dct(Instance& I) {
   };
   const texo_gp_params& prm = I.m.params;
   std::vector<Form> forms = {{0, 0, 0}, {1, 0, 0}};
-  if (fft_length(I.m.Wb) && fft_length(I.m.Hb)) forms.push_back({0, 0, 1});
+  if (fft_length(I.m.Wb) && fft_length(I.m.Hb) && prm.dct_mode != TEXO_GP_DCT_FP32_GEMM) forms.push_back({0, 0, 1});
   if (prm.dct_mode == TEXO_GP_DCT_BF16X3 && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1, 0});
   static std::mutex mu;
   static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, int, int>, Form> cache;
