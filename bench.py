@@ -68,16 +68,22 @@ def problem_bytes(p):
 
 
 # Algorithmic (compulsory) bytes per launch of each stage: every input read
-# once and every output written once, at the sizes of the instance.
+# once and every output written once, at the sizes of the instance. The GEMM
+# forms of the DCT take four passes (rows, columns, columns, rows); the FFT
+# form takes three: rows forward, one column pass (forward, scale by the
+# inverse eigenvalues, inverse) and rows inverse with the energy.
 def stage_bytes(stage, n):
     U, F, M, B, E, P, K = n["U"], n["F"], n["M"], n["B"], n["E"], n["P"], n["K"]
     nobj = U + F
+    if n.get("dct_form") == 3 and stage.startswith("dct_"):
+        return {"dct_rows_fwd": K * B * 4 * 2, "dct_cols": K * B * 4 * 2 + B * 4,
+                "dct_rows_inv": K * B * 4 * 3}.get(stage, 0)
     return {
         "init": K * B * (8 + 8 + 8) + 2 * U * 8,
         "scatter": M * (16 + 16 + 4 + 4 + 4) + F * (16 + 4 + 4) + K * B * 2 * 8 * 2,
         "wa": P * (4 + 16) + nobj * 0 + U * 16 + E * (4 + 4) + 2 * U * 8 * 2,
         "prep": K * B * (8 + 8 + 4),
-        "dct_row_fwd": K * B * 4 * 2 + B // max(1, n["Hb"]) * 0,
+        "dct_row_fwd": K * B * 4 * 2,
         "dct_col_fwd": K * B * 4 * 3,
         "dct_col_inv": K * B * 4 * 2,
         "dct_row_inv": K * B * 4 * 3,
@@ -103,10 +109,25 @@ def aggregate_ranks(total_ms, steps, dist=None, device="cuda"):
     return max_ms, world * steps / (max_ms / 1000.0)
 
 
+FFT_PASSES = {"dct_row_fwd": "dct_rows_fwd", "dct_col_fwd": "dct_cols", "dct_row_inv": "dct_rows_inv"}
+
+
+def dct_stages(n):
+    return list(FFT_PASSES.values()) if n.get("dct_form") == 3 else [
+        "dct_row_fwd", "dct_col_fwd", "dct_col_inv", "dct_row_inv"]
+
+
+def named_stages(times, n):
+    """Stage times under the names of the instance's DCT form (the FFT form's
+    third pass slot is empty and dropped)."""
+    if n.get("dct_form") != 3:
+        return dict(times)
+    return {FFT_PASSES.get(k, k): v for k, v in times.items() if k != "dct_col_inv"}
+
+
 def eval_bytes(n):
     """Algorithmic bytes of one objective evaluation (all its stages)."""
-    st = ["init", "scatter", "wa", "prep", "dct_row_fwd", "dct_col_fwd", "dct_col_inv", "dct_row_inv",
-          "gather", "combine"]
+    st = ["init", "scatter", "wa", "prep"] + dct_stages(n) + ["gather", "combine"]
     return sum(stage_bytes(k, n) for k in st)
 
 
@@ -445,25 +466,23 @@ def precision_report(iterations=1000, seed=0, threads=5):
 
     out = {"workload": "stress-1m", "positions": "uniform in the bounds, FP32-representable",
            "oracle_eval_s": t_oracle}
-    import ctypes as C
     for name, mode in (("fp32_fft", abi.DCT_FP32), ("fp32_gemm", abi.DCT_FP32_GEMM), ("bf16x3", abi.DCT_BF16X3)):
         prm = make_params("stress-1m", abi.ENGINE_HOST, mode)
         prm.max_iterations = iterations
         with Placer(prob, prm) as g:
-            form = C.c_int32()
-            g.lib.texo_gp_dct_form(g.h, C.byref(form))
+            form = g.dct_form()
             d = g.evaluate(c, gamma)
             st = g.stage_times(reps=5)
             t1 = time.perf_counter()
             _, _, s = g.run(allow_nonconverged=True)
             run_s = time.perf_counter() - t1
-        out[name] = {"dct_form": int(form.value), "potential_max_rel_err": nw(d["potential"], r["potential"]),
+        out[name] = {"dct_form": form, "potential_max_rel_err": nw(d["potential"], r["potential"]),
                      "field_gradient_max_rel_err": nw(d["field_gradient"], r["field_gradient"]),
                      "field_gradient_cosine": cos(d["field_gradient"], r["field_gradient"]),
                      "wa_gradient_cosine": cos(d["wa_gradient"], r["wa_gradient"]),
                      "energy_rel_err": abs(d["fields"][0].energy - r["fields"][0].energy) / abs(r["fields"][0].energy),
-                     "dct_pass_us": [round(1000 * st[k], 2) for k in ("dct_row_fwd", "dct_col_fwd", "dct_col_inv",
-                                                                       "dct_row_inv")],
+                     "dct_pass_us": {k: round(1000 * v, 2) for k, v in named_stages(st, {"dct_form": form}).items()
+                                     if k.startswith("dct_")},
                      "final_hpwl": s["hpwl"], "final_overflow": s["overflow"], "iterations": s["iterations"],
                      "converged": s["converged"], "run_s": run_s, "gpu_ms": s["elapsed_ms"]}
     out["final_hpwl_bf16x3_vs_fp32_gemm"] = out["bf16x3"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
@@ -542,7 +561,7 @@ def main():
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     g = Placer(prob, prm)
     n = dict(U=g.units, F=g.num_fillers, M=int(prob.member_ptr[-1]), B=g.bins, Hb=g.bins_y,
-             E=prob.num_nets, P=prob.num_pins, K=g.num_fields)
+             E=prob.num_nets, P=prob.num_pins, K=g.num_fields, dct_form=g.dct_form())
 
     state = {"prev": 0, "restarts": 0, "evals": 0, "trials": 0}
 
@@ -586,7 +605,7 @@ def main():
                               "gpu_launches": int(launches)}), flush=True)
         return
     # per-stage device times (standalone stage kernels) and the roofline
-    stages = g.stage_times(reps=20)
+    stages = named_stages(g.stage_times(reps=20), n)
     peak, peak_kind = peaks()
     stage_roofline = {k: {"ms": v, "algorithmic_bytes": stage_bytes(k, n),
                           "gbs": stage_bytes(k, n) / (v * 1e-3) / 1e9 if v > 0 else None}

@@ -200,7 +200,8 @@ typedef struct texo_gp_stats {
   uint64_t error_index;          /* first offending index for indexed errors */
   uint32_t error_field;
   uint32_t converged;            /* 1 when every field reached its target */
-  double elapsed_ms;             /* device time of the call (CUDA events on the handle's stream) */
+  double elapsed_ms;             /* device time of the call (CUDA events on the handle's stream; for
+                                    the device engine, around its one step: state in, kernel, state out) */
   uint64_t kernel_launches;      /* kernels this library launched during the call */
 } texo_gp_stats;
 

@@ -187,3 +187,18 @@ def test_device_engine_is_resumable():
         _, cb, sb = b.run(5)
     assert sa["iterations"] == sb["iterations"] == 15
     assert np.array_equal(ca, cb)
+
+
+def test_device_engine_single_iteration_steps_replay_the_same_graph():
+    """One-iteration steps replay the captured step graph (state in, kernel,
+    state out); twenty of them end where one twenty-iteration call does."""
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 5)
+    prm = params(best_effort=1, max_iterations=400, engine=abi.ENGINE_DEVICE)
+    a = Placer(prob, prm)
+    ta, ca, sa = a.run(20)
+    b = Placer(prob, prm)
+    for _ in range(20):
+        tb, cb, sb = b.run(1)
+        assert sb["kernel_launches"] == 1 and sb["elapsed_ms"] > 0.0
+    assert sa["iterations"] == sb["iterations"] == 20
+    assert np.array_equal(ca, cb) and np.array_equal(ta, tb)

@@ -24,7 +24,6 @@ struct Job {
   texo_gp_handle h = nullptr;
   uint64_t bytes = 0;
   int V = 1;
-  GridBarrier hbar{};
 };
 
 }  // namespace
@@ -196,7 +195,7 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
     }
   }
   for (size_t i = 0; i < n; ++i) {
-    s = batch_stage_out(b->resident[pick[i]].h, b->stream, &b->resident[pick[i]].hbar);
+    s = batch_stage_out(b->resident[pick[i]].h, b->stream);
     if (s) return s;
   }
   BCU(cudaStreamSynchronize(b->stream));
@@ -205,7 +204,7 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
   for (size_t i = 0; i < n; ++i) {
     Job& j = b->resident[pick[i]];
     batch_absorb(j.h);
-    if (j.hbar.error) {
+    if (batch_timed_out(j.h)) {
       result = TEXO_GP_ERR_DEVICE_TIMEOUT;
       set_last_error("batch: a job's barrier wait ran out");
     }

@@ -174,6 +174,34 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// FP64 arithmetic issues at a low rate on this part (a warp instruction
+// occupies a sub-partition's FP64 pipe for tens of cycles), so block-level
+// FP64 folds keep the work in as few warp instructions per sub-partition as
+// the tree allows: the values go through shared memory, warps 0-3 (one per
+// sub-partition) each fold an interleaved quarter with an xor tree, and
+// thread 0 folds the four results. `sh` needs kThreads + 4 slots; the result
+// is valid in thread 0. The order is fixed, so every block folds alike.
+template <typename Op>
+__device__ __forceinline__ double block_fold_fp64(double v, double* sh, Op op) {
+  __syncthreads();   // earlier readers of sh are done
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  if (w < 4) {
+    double s = sh[threadIdx.x];
+    for (int i = threadIdx.x + 128; i < (int)blockDim.x; i += 128) s = op(s, sh[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s = op(s, __shfl_xor_sync(0xffffffffu, s, o));
+    if ((threadIdx.x & 31) == 0) sh[kThreads + w] = s;
+  }
+  __syncthreads();
+  return threadIdx.x == 0 ? op(op(op(sh[kThreads], sh[kThreads + 1]), sh[kThreads + 2]), sh[kThreads + 3]) : 0.0;
+}
+struct FoldAdd {
+  __device__ double operator()(double a, double b) const { return a + b; }
+};
+__device__ __forceinline__ double block_sum(double v, double* sh) { return block_fold_fp64(v, sh, FoldAdd()); }
+
 // Sum over the block; result valid in thread 0. `sh` needs kThreads/32 slots.
 template <typename T>
 __device__ __forceinline__ T block_sum(T v, T* sh) {

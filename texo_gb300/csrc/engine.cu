@@ -41,7 +41,7 @@ void set_last_error(const std::string& s) { g_last_error = s; }
     if (s_ != TEXO_GP_OK) return s_; \
   } while (0)
 
-void release_mirror(double* scal);
+void release_mirror(RunBlock* run);
 
 Instance::~Instance() {
   if (stream) cudaStreamSynchronize(stream);
@@ -50,7 +50,7 @@ Instance::~Instance() {
     cudaStreamSynchronize(stream);
     cudaStreamDestroy(stream);
   }
-  release_mirror(h_scal);
+  release_mirror(h_run);
 }
 
 // Device buffers come from the device's stream-ordered pool (kept, not
@@ -234,14 +234,17 @@ cudaError_t shared_inv_eig(int device, uint32_t Wb, uint32_t Hb, float** out) {
 }
 }  // namespace
 
-// Pinned host mirrors of the reduction scalars, carved from shared slabs:
-// page-locking memory per instance would dominate admitting small jobs.
+// Pinned host mirrors of the controller state, grid barrier and reduction
+// scalars of one instance, carved from shared slabs: page-locking memory per
+// instance would dominate admitting small jobs.
 namespace {
-constexpr size_t kMirrorBytes = ((kScalars * sizeof(double) + kIScalars * sizeof(long long)) + 255) & ~(size_t)255;
+constexpr size_t kMirrorBytes =
+    sizeof(RunBlock) + (((kScalars * sizeof(double) + kIScalars * sizeof(long long)) + 255) & ~(size_t)255);
+static_assert(sizeof(RunBlock) % 256 == 0, "RunBlock keeps the scalars 256-byte aligned");
 std::mutex g_mirror_mu;
 std::vector<char*> g_mirror_free;
 }  // namespace
-int32_t acquire_mirror(double** scal, long long** iscal) {
+int32_t acquire_mirror(RunBlock** run, double** scal, long long** iscal) {
   std::lock_guard<std::mutex> lk(g_mirror_mu);
   if (g_mirror_free.empty()) {
     constexpr int kPerSlab = 64;
@@ -251,14 +254,16 @@ int32_t acquire_mirror(double** scal, long long** iscal) {
   }
   char* b = g_mirror_free.back();
   g_mirror_free.pop_back();
-  *scal = (double*)b;
-  *iscal = (long long*)(b + kScalars * sizeof(double));
+  std::memset(b, 0, kMirrorBytes);
+  *run = (RunBlock*)b;
+  *scal = (double*)(b + sizeof(RunBlock));
+  *iscal = (long long*)(b + sizeof(RunBlock) + kScalars * sizeof(double));
   return TEXO_GP_OK;
 }
-void release_mirror(double* scal) {
-  if (!scal) return;
+void release_mirror(RunBlock* run) {
+  if (!run) return;
   std::lock_guard<std::mutex> lk(g_mirror_mu);
-  g_mirror_free.push_back((char*)scal);
+  g_mirror_free.push_back((char*)run);
 }
 
 // A 2-D tensor map over a tiled tensor-core operand: rows of 64 bf16 halves
@@ -474,7 +479,6 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&gY, nobj);
   S.zeroed(&gC, nobj);
   S.zeroed(&run_dev, 1);
-  S.zeroed(&bar, 1);
   S.zeroed(&best, std::max<size_t>(h.U, 1));
   S.zeroed(&prev_targets, 2 * (size_t)h.U);
   S.zeroed(&mismatch, 1);
@@ -602,7 +606,7 @@ int32_t Instance::upload() {
     pblocks = std::min(std::max(per_sm, 1), kBlocksPerSm) * sms;
     pblocks = std::min(pblocks, kMaxPartials);
   }
-  TRY(acquire_mirror(&h_scal, &h_iscal));
+  TRY(acquire_mirror(&h_run, &h_scal, &h_iscal));
   std::memset(h_scal, 0, kScalars * sizeof(double));
   std::memset(h_iscal, 0, kIScalars * sizeof(long long));
   h_scal[SC_BETA] = h.params.beta;
@@ -673,7 +677,12 @@ struct Controller {
   double elapsed_ms = 0.0;
   unsigned long long launches = 0;
 
-  explicit Controller(Instance& i) : I(i) {}
+  explicit Controller(Instance& i) : I(i), hr(i.h_run->run) { std::memset(&hr, 0, sizeof(hr)); }
+  ~Controller() {
+    if (step_exec) cudaGraphExecDestroy(step_exec);
+    for (cudaEvent_t e : step_ev)
+      if (e) cudaEventDestroy(e);
+  }
 
   double margin(double x, double y) const {
     const double eps = std::max(std::numeric_limits<double>::epsilon(), I.m.params.objective_margin_ulps * 0x1p-24);
@@ -990,8 +999,16 @@ struct Controller {
   }
 
   // The device engine: the same loop inside one persistent cooperative kernel.
-  DevRun hr{};
+  DevRun& hr;                 // the pinned mirror's controller state
   bool dev_ready = false;
+  // The device-engine step captured as a CUDA graph on first use (the
+  // descriptor it was captured with is kept: a different one recaptures),
+  // and the CUDA events that time the step's device work.
+  cudaGraphExec_t step_exec = nullptr;
+  bool step_graph_off = false;
+  Dev step_dev{};
+  cudaEvent_t step_ev[2] = {nullptr, nullptr};
+  double device_ms = -1.0;    // device time of the last device-engine step
 
   // Initializes the kernel's controller state on first use.
   void prepare_devrun() {
@@ -1040,8 +1057,34 @@ struct Controller {
   int32_t run_device(uint32_t budget) {
     prepare_devrun();
     hr.budget = budget;
-    const int32_t s = launch_persistent(I.d, I.r, buffers(), I.run_dev, &hr, I.bar, std::min(I.pblocks, I.nvb),
-                                        I.nvb, I.stream);
+    const int blocks = std::min(I.pblocks, I.nvb);
+    if (step_exec && std::memcmp(&step_dev, &I.d, sizeof(Dev)) != 0) {
+      cudaGraphExecDestroy(step_exec);
+      step_exec = nullptr;
+    }
+    if (!step_exec && !step_graph_off) {
+      if (capture_persistent(I.d, I.r, buffers(), I.run_dev, I.h_run, blocks, I.nvb, I.stream, &step_exec))
+        step_graph_off = true;   // the direct launch below takes over
+      else
+        step_dev = I.d;
+    }
+    for (cudaEvent_t& e : step_ev)
+      if (!e) CU(cudaEventCreate(&e));
+    std::memset(&I.h_run->bar, 0, sizeof(GridBarrier));
+    CU(cudaEventRecord(step_ev[0], I.stream));
+    int32_t s = step_exec ? (cudaGraphLaunch(step_exec, I.stream) == cudaSuccess ? TEXO_GP_OK : TEXO_GP_ERR_CUDA)
+                          : enqueue_persistent(I.d, I.r, buffers(), I.run_dev, I.h_run, blocks, I.nvb, I.stream);
+    if (!s) {
+      note_launch();
+      CU(cudaEventRecord(step_ev[1], I.stream));
+      if (cudaStreamSynchronize(I.stream) != cudaSuccess) s = TEXO_GP_ERR_CUDA;
+      else if (I.h_run->bar.error) s = TEXO_GP_ERR_DEVICE_TIMEOUT;
+    }
+    if (!s) {
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, step_ev[0], step_ev[1]));
+      device_ms = ms;
+    }
     if (s) {
       set_last_error(s == TEXO_GP_ERR_DEVICE_TIMEOUT ? "persistent kernel: a grid barrier wait ran out"
                                                      : std::string("persistent kernel: ") +
@@ -1201,24 +1244,24 @@ int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, Ins
   Controller& C = *h->ctl;
   C.prepare_devrun();
   C.hr.budget = budget;
-  CU(cudaMemcpyAsync(I.run_dev, &C.hr, sizeof(DevRun), cudaMemcpyHostToDevice, s));
-  CU(cudaMemsetAsync(I.bar, 0, sizeof(GridBarrier), s));
+  std::memset(&I.h_run->bar, 0, sizeof(GridBarrier));
+  CU(cudaMemcpyAsync(I.run_dev, I.h_run, sizeof(RunBlock), cudaMemcpyHostToDevice, s));
   desc->d = I.d;
   desc->r = I.r;
   desc->B = C.buffers();
-  desc->run = I.run_dev;
-  desc->bar = I.bar;
+  desc->run = &I.run_dev->run;
+  desc->bar = &I.run_dev->bar;
   desc->V = I.nvb;
   desc->pad = 0;
   *large = I.d.dct_large != 0;
   return TEXO_GP_OK;
 }
-int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s, GridBarrier* host_bar) {
+int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s) {
   Instance& I = *h->inst;
-  CU(cudaMemcpyAsync(&h->ctl->hr, I.run_dev, sizeof(DevRun), cudaMemcpyDeviceToHost, s));
-  CU(cudaMemcpyAsync(host_bar, I.bar, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s));
+  CU(cudaMemcpyAsync(I.h_run, I.run_dev, sizeof(RunBlock), cudaMemcpyDeviceToHost, s));
   return TEXO_GP_OK;
 }
+bool batch_timed_out(texo_gp_handle_s* h) { return h->inst->h_run->bar.error != 0; }
 int32_t batch_absorb(texo_gp_handle_s* h) { return h->ctl->absorb_devrun(); }
 bool handle_finished(texo_gp_handle_s* h) { return h->ctl->phase == 2; }
 uint64_t handle_bytes(texo_gp_handle_s* h) { return h->inst->bytes; }
@@ -1631,6 +1674,7 @@ int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_tar
   CU(cudaEventCreate(&e1));
   const unsigned long long l0 = launches_issued();
   CU(cudaEventRecord(e0, I.stream));
+  C.device_ms = -1.0;
   int32_t s = C.run(max_iterations);
   cudaEventRecord(e1, I.stream);
   cudaEventSynchronize(e1);
@@ -1638,7 +1682,9 @@ int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_tar
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  C.elapsed_ms = ms;
+  // the device engine times its one step (state in, kernel, state out) on
+  // the stream itself; the host engine's call is timed whole
+  C.elapsed_ms = C.device_ms >= 0.0 ? C.device_ms : ms;
   C.launches = launches_issued() - l0;
   if (s != TEXO_GP_OK && s != TEXO_GP_ERR_DID_NOT_CONVERGE) {
     if (stats) {

@@ -80,8 +80,8 @@ struct Instance {
   // device engine: fixed buffer tables (roles rotate inside the kernel)
   float2* posb[4] = {nullptr, nullptr, nullptr, nullptr};
   float2* gradb[3] = {nullptr, nullptr, nullptr};
-  DevRun* run_dev = nullptr;
-  GridBarrier* bar = nullptr;
+  RunBlock* run_dev = nullptr;                   // controller state + grid barrier
+  RunBlock* h_run = nullptr;                     // its pinned host mirror
   int pblocks = 0;                               // persistent grid size
   double* h_scal = nullptr;                      // pinned host mirror
   long long* h_iscal = nullptr;
@@ -107,7 +107,8 @@ namespace tgp {
 // fills the instance descriptor; stage_out queues the copies back; absorb
 // mirrors the state once the stream has completed.
 int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, InstDesc* desc, bool* large);
-int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s, GridBarrier* host_bar);
+int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s);
+bool batch_timed_out(texo_gp_handle_s* h);     // the last launch's barrier wait ran out
 int32_t batch_absorb(texo_gp_handle_s* h);
 bool handle_finished(texo_gp_handle_s* h);
 uint64_t handle_bytes(texo_gp_handle_s* h);

@@ -2,6 +2,8 @@
 // (defined in persistent_{solo,batch}_{small,large}.cu over run_body).
 #include "persistent.cuh"
 
+#include <cstring>
+
 namespace tgp {
 
 const void* persistent_kernel_small();
@@ -26,25 +28,50 @@ int batch_blocks_per_sm() {
 
 static bool large_tiles(const Dev& d) { return d.dct_large != 0; }
 
-int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRun* run_dev, DevRun* host_run,
-                          GridBarrier* bar, int blocks, int V, cudaStream_t s) {
-  if (cudaMemcpyAsync(run_dev, host_run, sizeof(DevRun), cudaMemcpyHostToDevice, s) != cudaSuccess)
-    return TEXO_GP_ERR_CUDA;
-  if (cudaMemsetAsync(bar, 0, sizeof(GridBarrier), s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
+int32_t enqueue_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                           int blocks, int V, cudaStream_t s) {
+  if (cudaMemcpyAsync(dev, host, sizeof(RunBlock), cudaMemcpyHostToDevice, s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
   Dev dd = d;
   Reduce rr = r;
   Buffers bb = b;
-  void* args[] = {&dd, &rr, &bb, &run_dev, &bar, &V};
+  DevRun* run = &dev->run;
+  GridBarrier* bar = &dev->bar;
+  void* args[] = {&dd, &rr, &bb, &run, &bar, &V};
   const void* fn = large_tiles(d) ? persistent_kernel_large() : persistent_kernel_small();
   if (cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kThreads), args, 0, s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
+  if (cudaMemcpyAsync(host, dev, sizeof(RunBlock), cudaMemcpyDeviceToHost, s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
+  return TEXO_GP_OK;
+}
+
+int32_t capture_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                           int blocks, int V, cudaStream_t s, cudaGraphExec_t* exec) {
+  *exec = nullptr;
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return TEXO_GP_ERR_UNSUPPORTED;
+  }
+  const int32_t q = enqueue_persistent(d, r, b, dev, host, blocks, V, s);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  bool ok = q == TEXO_GP_OK && e == cudaSuccess && g != nullptr;
+  if (ok) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    *exec = nullptr;
+    cudaGetLastError();   // a refused capture leaves no sticky error
+    return TEXO_GP_ERR_UNSUPPORTED;
+  }
+  return TEXO_GP_OK;
+}
+
+int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                          int blocks, int V, cudaStream_t s) {
+  std::memset(&host->bar, 0, sizeof(GridBarrier));
+  const int32_t q = enqueue_persistent(d, r, b, dev, host, blocks, V, s);
+  if (q) return q;
   note_launch();
-  GridBarrier hb;
-  if (cudaMemcpyAsync(host_run, run_dev, sizeof(DevRun), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return TEXO_GP_ERR_CUDA;
-  if (cudaMemcpyAsync(&hb, bar, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s) != cudaSuccess)
-    return TEXO_GP_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return TEXO_GP_ERR_CUDA;
-  if (hb.error) return TEXO_GP_ERR_DEVICE_TIMEOUT;
+  if (host->bar.error) return TEXO_GP_ERR_DEVICE_TIMEOUT;
   return TEXO_GP_OK;
 }
 

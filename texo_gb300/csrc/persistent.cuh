@@ -65,6 +65,13 @@ struct DevRun {
   unsigned budget;
 };
 
+// The controller state and the grid barrier of one instance, side by side so
+// that one copy each way moves both; the host keeps a pinned mirror of it.
+struct RunBlock {
+  DevRun run;
+  alignas(256) GridBarrier bar;
+};
+
 // Phase categories of DevRun::phase_ns.
 enum PhaseClock {
   PC_SCATTER_WA = 0,   // scatter + WA (or WA alone) up to its barrier
@@ -95,11 +102,20 @@ struct InstDesc {
   int pad;
 };
 
-// Launches the persistent kernel for up to host_run->budget iterations on
-// `blocks` physical blocks over V virtual blocks; run lives in device memory
-// and is copied to/from host_run around the launch.
-int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, DevRun* run_dev, DevRun* host_run,
-                          GridBarrier* bar, int blocks, int V, cudaStream_t s);
+// One step of the device engine on stream s: the pinned mirror `host` goes to
+// `dev`, the persistent kernel runs up to run.budget iterations on `blocks`
+// physical blocks over V virtual blocks, and `dev` comes back to `host`.
+// The caller clears host->bar first and reads host->bar.error after a sync.
+int32_t enqueue_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                           int blocks, int V, cudaStream_t s);
+// The same step captured once as a CUDA graph (the kernel arguments are
+// fixed for an instance), replayed with cudaGraphLaunch. Returns
+// TEXO_GP_ERR_UNSUPPORTED, leaving *exec null, if the capture fails.
+int32_t capture_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                           int blocks, int V, cudaStream_t s, cudaGraphExec_t* exec);
+// enqueue_persistent on a cleared barrier, then a sync and the barrier check.
+int32_t launch_persistent(const Dev& d, const Reduce& r, const Buffers& b, RunBlock* dev, RunBlock* host,
+                          int blocks, int V, cudaStream_t s);
 // Launches every instance of descs_dev at once; map_dev[b] = (instance,
 // physical block, physical block count, 0). Asynchronous.
 int32_t launch_batch(const InstDesc* descs_dev, const int4* map_dev, int blocks, bool large, cudaStream_t s);

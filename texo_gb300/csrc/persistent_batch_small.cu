@@ -7,7 +7,7 @@ namespace tgp {
 __global__ void __launch_bounds__(kThreads, kBatchBlocksPerSm) k_batch_small(const InstDesc* descs, const int4* map) {
   __shared__ InstDesc sd;
   const int4 m = map[blockIdx.x];
-  if (threadIdx.x == 0) sd = descs[m.x];
+  copy_words(&sd, descs + m.x);
   __syncthreads();
   run_body<false>(sd.d, sd.r, sd.B, sd.run, sd.bar, m.y, m.z, sd.V);
 }

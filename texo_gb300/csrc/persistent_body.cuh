@@ -369,6 +369,15 @@ struct StepVars {
 };
 enum { ACT_NONE = 0, ACT_RESTART, ACT_CONTINUE, ACT_ACCEPT, ACT_STATIONARY };
 
+// Copies *src to *dst one 8-byte word per thread of the block (a struct copy
+// by one thread waits for each load in turn). The caller synchronizes.
+template <class T>
+__device__ __forceinline__ void copy_words(T* dst, const T* src) {
+  static_assert(sizeof(T) % 8 == 0 && alignof(T) >= 8, "copied as 8-byte words");
+  for (int i = threadIdx.x; i < (int)(sizeof(T) / 8); i += blockDim.x)
+    reinterpret_cast<unsigned long long*>(dst)[i] = reinterpret_cast<const unsigned long long*>(src)[i];
+}
+
 // The placement loop of one instance, run by its np physical blocks.
 template <bool LARGE>
 static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B, DevRun* run, GridBarrier* bar, int pb,
@@ -386,13 +395,13 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
   __shared__ int bar_failed;
   __shared__ unsigned long long clock[10];
   if (threadIdx.x == 0) {
-    S = *run;
+    for (int i = 0; i < 10; ++i) clock[i] = 0;
+    clock[8] = now_ns();
     gen = *(volatile unsigned*)&bar->gen;
     V.pending_best = 0;
     V.pending_prev = 0;
-    for (int i = 0; i < 10; ++i) clock[i] = 0;
-    clock[8] = now_ns();
   }
+  copy_words(&S, run);
   __syncthreads();
   Ctx<LARGE> c{d, r, B, S, bar, &gen, &bar_failed, gsm, sh, rd, rl, coef, fmean, pb, np, Vn, 0ull, clock};
   const int n = d.nobj;
@@ -795,11 +804,16 @@ out:
     if (V.pending_prev) c.copy(c.Xp(), c.X(), n);
     ok = c.sync();
   }
-  if (pb == 0 && threadIdx.x == 0) {
-    S.barriers += c.nbar;
-    for (int i = 0; i < 8; ++i) S.phase_ns[i] += clock[i];
-    S.barrier_wait_ns += clock[9];
-    *run = S;
+  c.mark(PC_OTHER);
+  __syncthreads();
+  if (pb == 0) {
+    if (threadIdx.x == 0) {
+      S.barriers += c.nbar;
+      for (int i = 0; i < 8; ++i) S.phase_ns[i] += clock[i];
+      S.barrier_wait_ns += clock[9];
+    }
+    __syncthreads();
+    copy_words(run, &S);
   }
 #undef T0
 #undef VLOOP

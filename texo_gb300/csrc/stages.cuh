@@ -35,19 +35,24 @@ __device__ __forceinline__ long long* islot(const Partials& p, int s) { return p
 __device__ __forceinline__ double* mslot(const Partials& p, int s) { return p.mx + (size_t)s * kMaxPartials; }
 
 // Fixed-order reduction of n partials by the whole block; every thread gets
-// the result. Identical in every block that calls it.
+// the result. Identical in every block that calls it. Warps 0-3 (one per SM
+// sub-partition) fold interleaved quarters with an xor tree and thread 0
+// folds the four: FP64 folds then cost a few warp instructions per
+// sub-partition instead of a tree in every warp. `sh` needs 5 slots.
 template <typename T, typename Op>
 __device__ __forceinline__ T block_reduce_array(const T* a, int n, T init, Op op, T* sh) {
-  T v = init;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) v = op(v, a[i]);
+  const int w = threadIdx.x >> 5;
+  if (w < 4) {
+    T v = (int)threadIdx.x < n ? a[threadIdx.x] : init;
+    for (int i = threadIdx.x + 128; i < n; i += 128) v = op(v, a[i]);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) sh[w] = v;
+  }
   __syncthreads();
-  if (lane == 0) sh[w] = v;
+  if (threadIdx.x == 0) sh[4] = op(op(op(sh[0], sh[1]), sh[2]), sh[3]);
   __syncthreads();
-  T r = init;
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = op(r, sh[i]);
+  const T r = sh[4];
   __syncthreads();
   return r;
 }
@@ -68,21 +73,19 @@ __device__ __forceinline__ void write_partial(T v, T* slot, int vb, T* sh) {
   T r = block_sum(v, sh);
   if (threadIdx.x == 0) slot[vb] = r;
 }
+struct FoldMax {
+  __device__ double operator()(double a, double b) const { return fmax(a, b); }
+};
+struct FoldMin {
+  __device__ double operator()(double a, double b) const { return fmin(a, b); }
+};
 __device__ __forceinline__ void write_partial_max(double v, double* slot, int vb, double* sh, bool is_min) {
-  v = is_min ? -warp_max(-v) : warp_max(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) sh[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = sh[0];
-    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = is_min ? fmin(r, sh[i]) : fmax(r, sh[i]);
-    slot[vb] = r;
-  }
+  const double r = is_min ? block_fold_fp64(v, sh, FoldMin()) : block_fold_fp64(v, sh, FoldMax());
+  if (threadIdx.x == 0) slot[vb] = r;
 }
 
 struct Shared {
-  double d[kThreads / 32 * kMaxFields];
+  double d[kThreads + 4];   // block FP64 folds
   long long l[kThreads / 32];
 };
 
