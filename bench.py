@@ -68,31 +68,35 @@ def problem_bytes(p):
 
 
 # Algorithmic (compulsory) bytes per launch of each stage: every input read
-# once and every output written once, at the sizes of the instance. The GEMM
-# forms of the DCT take four passes (rows, columns, columns, rows); the FFT
-# form takes three: rows forward, one column pass (forward, scale by the
-# inverse eigenvalues, inverse) and rows inverse with the energy.
+# once and every output written once, at the sizes of the instance and the
+# device's data types (float2 positions and gradients, float preconditioner,
+# int32 indices, int64 fixed-point grids read-modify-written by the atomics).
+# U units, F fillers, M density members, B bins, E nets, P pins, K fields.
+# The GEMM forms of the DCT take four passes (rows, columns, columns, rows);
+# the FFT form takes three: rows forward, one column pass (forward, scale by
+# the inverse eigenvalues, inverse) and rows inverse with the energy.
 def stage_bytes(stage, n):
     U, F, M, B, E, P, K = n["U"], n["F"], n["M"], n["B"], n["E"], n["P"], n["K"]
     nobj = U + F
+    grids = 2 if F else 1                     # phys, and fill when there are fillers
     if n.get("dct_form") == 3 and stage.startswith("dct_"):
         return {"dct_rows_fwd": K * B * 4 * 2, "dct_cols": K * B * 4 * 2 + B * 4,
                 "dct_rows_inv": K * B * 4 * 3}.get(stage, 0)
     return {
-        "init": K * B * (8 + 8 + 8) + 2 * U * 8,
-        "scatter": M * (16 + 16 + 4 + 4 + 4) + F * (16 + 4 + 4) + K * B * 2 * 8 * 2,
-        "wa": P * (4 + 16) + nobj * 0 + U * 16 + E * (4 + 4) + 2 * U * 8 * 2,
-        "prep": K * B * (8 + 8 + 4),
+        "init": K * B * (8 + 8 + 8) + U * 16,                            # phys, fill := -capfix, 0; WA grads := 0
+        "scatter": M * 20 + U * 8 + F * 16 + K * B * 16 * grids,         # members, positions, grid RMW
+        "wa": P * 12 + E * 8 + U * 8 + U * 32,                           # pins, nets, positions, int64 grad RMW
+        "prep": K * B * (8 + 8 + 4),                                     # phys + fill -> rho
         "dct_row_fwd": K * B * 4 * 2,
-        "dct_col_fwd": K * B * 4 * 3,
-        "dct_col_inv": K * B * 4 * 2,
+        "dct_col_fwd": K * B * 4 * 2,
+        "dct_col_inv": K * B * 4 * 2 + B * 4,
         "dct_row_inv": K * B * 4 * 3,
-        "gather": nobj * (16 + 8 * K) + M * (16 + 4 + 4) + K * B * 4,
-        "combine": nobj * (16 + 8 * K) + 2 * U * 8,
-        "extrapolate": nobj * (16 * 4 + 16),
-        "candidate": nobj * (16 * 4 + 8 + 16),
-        "kkt": nobj * (16 * 4 + 8 + 16),
-        "precond": nobj * (8 + 8 * K + 8),
+        "gather": U * (4 + 8 + 8 * K) + M * 16 + F * (16 + 8) + K * B * 4,
+        "combine": U * 16 + nobj * (8 * K + 8) + F * 4,                  # WA grads, field grads -> gradient
+        "extrapolate": nobj * (8 * 4 + 8),                               # x, x_prev, lo, hi -> y
+        "candidate": nobj * (8 * 4 + 4 + 8),                             # y, g, lo, hi, P -> c
+        "kkt": nobj * (8 * 4 + 4),                                       # x, g, lo, hi, P
+        "precond": nobj * (4 + 4 * K + 4),                               # static + per-field charge -> P
         "finalize": 0,
     }.get(stage, 0)
 
@@ -125,10 +129,25 @@ def named_stages(times, n):
     return {FFT_PASSES.get(k, k): v for k, v in times.items() if k != "dct_col_inv"}
 
 
-def eval_bytes(n):
-    """Algorithmic bytes of one objective evaluation (all its stages)."""
+def eval_bytes(n, persistent=False):
+    """Algorithmic bytes of one objective evaluation (all its stages). In the
+    persistent engine the density preparation is folded into the first
+    transform (phys + fill read, rho and the transform written: 24 B a bin
+    instead of 20 + 8), and the combine also reads the KKT inputs (position,
+    bounds, preconditioner: 28 B an object)."""
     st = ["init", "scatter", "wa", "prep"] + dct_stages(n) + ["gather", "combine"]
-    return sum(stage_bytes(k, n) for k in st)
+    total = sum(stage_bytes(k, n) for k in st)
+    if persistent:
+        total += (n["U"] + n["F"]) * 28
+        total -= n["K"] * n["B"] * 4
+    return total
+
+
+def reused_eval_bytes(n):
+    """Algorithmic bytes of an evaluation that reuses the density side of the
+    same coordinates: WA gradients zeroed, WA, and the combine with its KKT
+    inputs (persistent engine)."""
+    return n["U"] * 16 + stage_bytes("wa", n) + stage_bytes("combine", n) + (n["U"] + n["F"]) * 28
 
 
 def ncu_traffic(workload, engine):
@@ -563,26 +582,27 @@ def main():
     n = dict(U=g.units, F=g.num_fillers, M=int(prob.member_ptr[-1]), B=g.bins, Hb=g.bins_y,
              E=prob.num_nets, P=prob.num_pins, K=g.num_fields, dct_form=g.dct_form())
 
-    state = {"prev": 0, "restarts": 0, "evals": 0, "trials": 0}
+    state = {"prev": 0, "restarts": 0, "evals": 0, "devals": 0, "trials": 0}
 
     def one_step():
         _, _, s = g.run(1, allow_nonconverged=True)
         if s["iterations"] <= state["prev"]:
             # the placement finished: start it again (outside the timed region)
             g.reset()
-            state.update(restarts=state["restarts"] + 1, evals=0, trials=0)
+            state.update(restarts=state["restarts"] + 1, evals=0, devals=0, trials=0)
             _, _, s = g.run(1, allow_nonconverged=True)
         state["prev"] = s["iterations"]
         # objective evaluations and line-search trials of this step
         s["d_evals"] = s["evaluations"] - state["evals"]
+        s["d_devals"] = s["density_evaluations"] - state["devals"]
         s["d_trials"] = s["line_search_trials"] - state["trials"]
-        state.update(evals=s["evaluations"], trials=s["line_search_trials"])
+        state.update(evals=s["evaluations"], devals=s["density_evaluations"], trials=s["line_search_trials"])
         return s
 
     for _ in range(args.warmup):
         s = one_step()
     # timed steps
-    total_ms, launches, evals, trials = 0.0, 0, 0, 0
+    total_ms, launches, evals, devals, trials = 0.0, 0, 0, 0, 0
     with Clocks(local) as clk:
         if dist:
             dist.barrier()
@@ -594,6 +614,7 @@ def main():
             total_ms += s["elapsed_ms"]
             launches += s["kernel_launches"]
             evals += s["d_evals"]
+            devals += s["d_devals"]
             trials += s["d_trials"]
         torch.cuda.synchronize()
         if dist:
@@ -612,9 +633,12 @@ def main():
                       for k, v in stages.items()}
     if engine == abi.ENGINE_DEVICE:
         # one persistent launch per step runs the whole iteration: its
-        # algorithmic bytes are the evaluations' and the vector updates' of
-        # the step, and its duration is the step's CUDA-event time
-        per_step_bytes = (evals * eval_bytes(n) + trials * stage_bytes("candidate", n)
+        # algorithmic bytes are the evaluations' (full ones, and ones that
+        # reuse the density side and run the wirelength side alone) and the
+        # vector updates' of the step; its duration is the step's CUDA-event time
+        per_step_bytes = (devals * eval_bytes(n, persistent=True)
+                          + (evals - devals) * reused_eval_bytes(n)
+                          + trials * stage_bytes("candidate", n)
                           + args.steps * (stage_bytes("precond", n) + stage_bytes("extrapolate", n))) / args.steps
         dom = "k_persistent (one GP iteration per launch)"
         dom_ms = max_ms / args.steps
@@ -629,6 +653,7 @@ def main():
                 "frac": achieved / peak, "traffic": ncu_traffic(args.workload, args.engine),
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_step_bytes,
                 "launch_ms": dom_ms, "evaluations_per_step": evals / args.steps,
+                "density_evaluations_per_step": devals / args.steps,
                 "trials_per_step": trials / args.steps, "stages": stage_roofline}
     # end to end through the C ABI from host buffers
     e2e = None

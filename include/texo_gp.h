@@ -203,6 +203,9 @@ typedef struct texo_gp_stats {
   double elapsed_ms;             /* device time of the call (CUDA events on the handle's stream; for
                                     the device engine, around its one step: state in, kernel, state out) */
   uint64_t kernel_launches;      /* kernels this library launched during the call */
+  uint64_t density_evaluations;  /* evaluations that rebuilt the density side (scatter, Poisson
+                                    solve, field gather); the others reused it for the same
+                                    coordinates and ran the wirelength side alone */
 } texo_gp_stats;
 
 /* One evaluation of the objective components at given coordinates

@@ -202,3 +202,15 @@ def test_device_engine_single_iteration_steps_replay_the_same_graph():
         assert sb["kernel_launches"] == 1 and sb["elapsed_ms"] > 0.0
     assert sa["iterations"] == sb["iterations"] == 20
     assert np.array_equal(ca, cb) and np.array_equal(ta, tb)
+
+
+@pytest.mark.parametrize("engine", [abi.ENGINE_HOST, abi.ENGINE_DEVICE])
+def test_density_evaluations_are_counted(engine):
+    """Every iteration re-evaluates its origin with the density side reused
+    (eplace's closure changes with gamma and the multipliers), so the
+    evaluations that rebuild the density side are strictly fewer than all
+    evaluations and more than the iterations."""
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 0)
+    with Placer(prob, params(best_effort=1, max_iterations=30, engine=engine)) as g:
+        _, _, s = g.run(allow_nonconverged=True)
+    assert s["iterations"] < s["density_evaluations"] < s["evaluations"]

@@ -93,6 +93,7 @@ class Stats(C.Structure):
         ("gamma", C.c_double), ("objective", C.c_double), ("hpwl", C.c_double),
         ("error_index", C.c_uint64), ("error_field", C.c_uint32), ("converged", C.c_uint32),
         ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64),
+        ("density_evaluations", C.c_uint64),
     ]
 
 

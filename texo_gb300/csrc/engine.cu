@@ -515,9 +515,13 @@ int32_t Instance::upload() {
   // enough blocks to cover the widest stage, up to kBlocksPerSm per SM
   const size_t widest = std::max(std::max(std::max(nobj, (size_t)h.Mm + h.F), std::max(B, h.pin_unit.size() / 2)), (size_t)1);
   // Virtual blocks: the reduction structure of every stage. The standalone
-  // kernels launch exactly this many blocks; the persistent engine loops its
-  // physical blocks over them, so both see the same partials.
-  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * kBlocksPerSm), (size_t)kMaxPartials);
+  // kernels of the host engine launch exactly this many blocks, up to
+  // kHostBlocksPerSm a SM so that large instances keep enough loads in
+  // flight; the persistent engine runs kBlocksPerSm a SM and loops its
+  // physical blocks over the virtual ones, which therefore match that grid.
+  constexpr size_t kHostBlocksPerSm = 8;
+  const size_t per_sm = h.params.engine == TEXO_GP_ENGINE_DEVICE ? (size_t)kBlocksPerSm : kHostBlocksPerSm;
+  nvb = (int)std::min(std::min((widest + kThreads - 1) / kThreads, (size_t)sms * per_sm), (size_t)kMaxPartials);
   nvb = std::max(nvb, 1);
   Dev& D = d;
   D.U = (int)h.U;
@@ -673,6 +677,7 @@ struct Controller {
   bool density_at_x = false;  // graw/phi/energies describe bufX
   // statistics
   uint64_t evaluations = 0, device_evaluations = 0, trials = 0;
+  uint64_t density_evaluations = 0;   // evaluations that rebuilt the density side
   double last_objective = 0.0;
   double elapsed_ms = 0.0;
   unsigned long long launches = 0;
@@ -724,6 +729,7 @@ struct Controller {
       launch_prep(D, I.r, nvb, s);
       for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, nvb, s, &I.tmaps);
       launch_gather(D, I.r, pos, nvb, s);
+      density_evaluations++;
     } else {
       launch_init(D, false, true, nvb, s);
     }
@@ -1030,7 +1036,9 @@ struct Controller {
         hr.target[f] = m.overflow_target(f);
         hr.gamma_weight[f] = m.gamma_weight[f];
         hr.real_area[f] = m.real_area[f];
+        hr.inv_real_area[f] = 1.0 / m.real_area[f];
         hr.e0[f] = 1.0;
+        hr.inv_e0[f] = 1.0;
       }
       hr.a = 1.0;
       hr.ix = 0;
@@ -1107,6 +1115,7 @@ struct Controller {
     I.gC = I.gradb[hr.igc];
     completed = hr.completed;
     evaluations = hr.evaluations;
+    density_evaluations = hr.density_evaluations;
     trials = hr.trials;
     converged = hr.converged != 0;
     exhausted = hr.exhausted != 0;
@@ -1399,6 +1408,7 @@ int32_t handle_targets(texo_gp_handle h, uint32_t* out, double* coords, texo_gp_
     st->status = status;
     st->iterations = C.completed;
     st->evaluations = C.evaluations;
+    st->density_evaluations = C.density_evaluations;
     st->line_search_trials = C.trials;
     st->num_fields = I.m.K;
     for (uint32_t f = 0; f < I.m.K && f < TEXO_GP_MAX_FIELDS; ++f) {

@@ -39,12 +39,13 @@ struct DevRun {
   int W, H;
   double beta, alpha_low, alpha_high, init_weight, gamma_base, margin_eps;
   double target[kMaxFields], gamma_weight[kMaxFields], real_area[kMaxFields];
+  double inv_real_area[kMaxFields];   // 1 / real_area (FP64 division is slow on the device)
   // loop state (optimize_density_once, eplace.rs:439-582)
   int phase;                    // 0 fresh, 1 running, 2 finished
   int status;                   // texo_gp_status
   int converged, exhausted;
   unsigned completed;
-  double lambda[kMaxFields], e0[kMaxFields], mstep, gamma;
+  double lambda[kMaxFields], e0[kMaxFields], inv_e0[kMaxFields], mstep, gamma;
   double best_max, best_tot;
   int have_prev_stationary, density_at_x;
   double cur_overflow[kMaxFields], cur_energy[kMaxFields], cur_force[kMaxFields];
@@ -57,7 +58,7 @@ struct DevRun {
   int ix, ixp, iy, ic;
   int igx, igy, igc;
   // statistics
-  unsigned long long evaluations, trials, barriers;
+  unsigned long long evaluations, density_evaluations, trials, barriers;
   // grid-wide phase times seen by block 0 (ns): see PhaseClock
   unsigned long long phase_ns[8];
   unsigned long long barrier_wait_ns;

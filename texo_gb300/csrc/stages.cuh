@@ -79,14 +79,28 @@ struct FoldMax {
 struct FoldMin {
   __device__ double operator()(double a, double b) const { return fmin(a, b); }
 };
-__device__ __forceinline__ void write_partial_max(double v, double* slot, int vb, double* sh, bool is_min) {
-  const double r = is_min ? block_fold_fp64(v, sh, FoldMin()) : block_fold_fp64(v, sh, FoldMax());
-  if (threadIdx.x == 0) slot[vb] = r;
+// Block max (or min) of per-thread FP32 values, written as FP64 partial vb:
+// folding in FP32 and widening once gives the same value as widening first.
+__device__ __forceinline__ void write_partial_max(float v, double* slot, int vb, float* sh, bool is_min) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = is_min ? fminf(v, w) : fmaxf(v, w);
+  }
+  __syncthreads();   // earlier readers of sh are done
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float r = sh[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = is_min ? fminf(r, sh[i]) : fmaxf(r, sh[i]);
+    slot[vb] = (double)r;
+  }
 }
 
 struct Shared {
   double d[kThreads + 4];   // block FP64 folds
   long long l[kThreads / 32];
+  float f[kThreads / 32];   // block FP32 max / min
 };
 
 __device__ __forceinline__ AxisTaps taps_x(const Dev& d, float s) {
@@ -752,7 +766,7 @@ static __device__ void stage_combine(const Dev& d, const double* coef_d, float2*
   }
   for (int f = 0; f < d.K; ++f) write_partial((double)rawl1[f], pslot(p, SLOT_RAWL1 + f), vb, sh.d);
   write_partial((double)wal1, pslot(p, SLOT_WAL1), vb, sh.d);
-  if (kkt_pos) write_partial_max((double)kkt, mslot(p, MS_KKT), vb, sh.d, false);
+  if (kkt_pos) write_partial_max(kkt, mslot(p, MS_KKT), vb, sh.f, false);
   {
     long long v = bad;
 #pragma unroll
@@ -820,7 +834,7 @@ static __device__ void stage_candidate(const Dev& d, const float2* y, const floa
   write_partial(diff, islot(p, IS_DIFF), vb, sh.l);
   write_partial((double)dot, pslot(p, SLOT_DOT), vb, sh.d);
   write_partial((double)msn, pslot(p, SLOT_MSN), vb, sh.d);
-  if (origin) write_partial_max((double)ch, mslot(p, MS_CHANGE), vb, sh.d, false);
+  if (origin) write_partial_max(ch, mslot(p, MS_CHANGE), vb, sh.f, false);
 }
 
 // box_metric_kkt_residual (global_placement.rs:648-663) and, optionally, the
@@ -840,8 +854,8 @@ static __device__ void stage_kkt(const Dev& d, const float2* x, const float2* g,
       ch = fmaxf(ch, fabsf(a.y - b.y));
     }
   }
-  write_partial_max((double)r, mslot(p, MS_KKT), vb, sh.d, false);
-  if (ref) write_partial_max((double)ch, mslot(p, MS_CHANGE), vb, sh.d, false);
+  write_partial_max(r, mslot(p, MS_KKT), vb, sh.f, false);
+  if (ref) write_partial_max(ch, mslot(p, MS_CHANGE), vb, sh.f, false);
 }
 
 // diagonal_preconditioner (eplace.rs:1046-1100).
@@ -865,8 +879,8 @@ static __device__ void stage_precond(const Dev& d, const double* lambda_d, Parti
     pmin = fminf(pmin, v);
     pmax = fmaxf(pmax, v);
   }
-  write_partial_max((double)pmin, mslot(p, MS_PMIN), vb, sh.d, true);
-  write_partial_max((double)pmax, mslot(p, MS_PMAX), vb, sh.d, false);
+  write_partial_max(pmin, mslot(p, MS_PMIN), vb, sh.f, true);
+  write_partial_max(pmax, mslot(p, MS_PMAX), vb, sh.f, false);
   write_partial(badp, islot(p, IS_PBAD), vb, sh.l);
 }
 

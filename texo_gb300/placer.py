@@ -29,7 +29,8 @@ def _stats_dict(s):
                 evaluations=s.evaluations, line_search_trials=s.line_search_trials,
                 overflow=[s.overflow[i] for i in range(K)], energy=[s.energy[i] for i in range(K)],
                 gamma=s.gamma, objective=s.objective, hpwl=s.hpwl, converged=bool(s.converged),
-                elapsed_ms=s.elapsed_ms, kernel_launches=s.kernel_launches)
+                elapsed_ms=s.elapsed_ms, kernel_launches=s.kernel_launches,
+                density_evaluations=s.density_evaluations)
 
 
 def place(problem, params=None):
