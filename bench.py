@@ -660,10 +660,10 @@ def main():
     if not args.no_e2e:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        targets, coords, s2 = place(prob, prm)
+        targets, _, s2 = place(prob, prm)
         dt = time.perf_counter() - t0
         e2e = {"value": s2["iterations"] / dt, "unit": "iter/s", "h2d_bytes_per_step": problem_bytes(prob),
-               "d2h_bytes_per_step": int(targets.nbytes + coords.nbytes),
+               "d2h_bytes_per_step": int(targets.nbytes),
                "placement_s": dt, "iterations": s2["iterations"], "final_overflow": s2["overflow"],
                "final_hpwl": s2["hpwl"], "converged": s2["converged"]}
     line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,

@@ -214,3 +214,16 @@ def test_density_evaluations_are_counted(engine):
     with Placer(prob, params(best_effort=1, max_iterations=30, engine=engine)) as g:
         _, _, s = g.run(allow_nonconverged=True)
     assert s["iterations"] < s["density_evaluations"] < s["evaluations"]
+
+
+def test_place_entry_matches_a_handle_run():
+    """texo_gp_place (no coordinates asked) and create / run / destroy give
+    the same targets and statistics."""
+    from texo_gb300.placer import place
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 4)
+    prm = params(best_effort=1, max_iterations=400, engine=abi.ENGINE_DEVICE)
+    t1, c1, s1 = place(prob, prm)
+    t2, c2, s2 = place(prob, prm, coordinates=True)
+    assert c1 is None and c2.ndim == 1 and c2.size >= 2 * prob.num_units
+    assert np.array_equal(t1, t2)
+    assert s1["iterations"] == s2["iterations"] and s1["hpwl"] == s2["hpwl"]

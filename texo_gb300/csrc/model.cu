@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "engine.h"
 
@@ -263,10 +264,8 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
       by = p->cell_offset_xy[2 * (size_t)cell + 1];
     }
   };
-  // wirelength preconditioner and cell incidence: each distinct unit (cell)
-  // of a net counts once, found with a per-net stamp instead of a sort
-  std::vector<double> wl(U, 0.0), inc(C, 0.0);
-  std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
+  // nets and timed arcs are validated first: the two passes below then run
+  // side by side on two threads and read only checked indices
   for (uint32_t e = 0; e < E; ++e) {
     const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
     if (en < b + 2) {
@@ -275,6 +274,91 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     }
     for (uint32_t k = b; k < en; ++k)
       if (p->pin_cell[k] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  }
+  const size_t arcs = p->num_timed_arcs;
+  for (uint32_t a = 0; a < arcs; ++a) {
+    if (p->arc_driver_cell[a] >= C || p->arc_sink_cell[a] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    if (u64_to_f64(p->arc_extra_weight[a]) > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
+  }
+
+  // Pin layout (second thread): degree classes 2 | 3-4 | 5-8 | 9-16 | 17+
+  // laid out class by class (a counting sort over the classes, nets of a
+  // class in input order), then the timed arcs as 2-pin nets; every output
+  // is sized once and filled by index. pin_count[u] = pins of unit u.
+  static const int groups[5] = {2, 4, 8, 16, 32};
+  auto cls = [](uint32_t deg) { return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : 4; };
+  const size_t pins = E ? p->net_ptr[E] : 0;
+  std::vector<double> pin_count(U, 0.0);
+  bool layout_ok = true;
+  auto layout = [&]() {
+    try {
+      size_t nets_in[5] = {0, 0, 0, 0, 0}, pins_in[5] = {0, 0, 0, 0, 0};
+      for (uint32_t e = 0; e < E; ++e) {
+        const uint32_t deg = p->net_ptr[e + 1] - p->net_ptr[e];
+        nets_in[cls(deg)]++;
+        pins_in[cls(deg)] += deg;
+      }
+      size_t net_at[5], pin_at[5];
+      for (int c = 0, n0 = 0, p0 = 0; c < 5; ++c) {
+        net_at[c] = n0;
+        pin_at[c] = p0;
+        m.class_begin[c] = n0;
+        m.class_group[c] = groups[c];
+        n0 += (int)nets_in[c];
+        p0 += (int)pins_in[c];
+      }
+      m.net_ptr.resize((size_t)E + arcs + 1);
+      m.net_w.assign((size_t)E + arcs, 1.0f);
+      m.pin_unit.resize(pins + 2 * arcs);
+      m.pin_base.resize(2 * (pins + 2 * arcs));
+      m.net_ptr[0] = 0;
+      for (uint32_t e = 0; e < E; ++e) {
+        const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
+        const int c = cls(en - b);
+        const size_t slot = net_at[c]++;
+        size_t q = pin_at[c];
+        for (uint32_t k = b; k < en; ++k, ++q) {
+          int unit;
+          pin_of(p->pin_cell[k], unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
+          m.pin_unit[q] = unit;
+          if (unit >= 0) pin_count[unit] += 1.0;
+        }
+        pin_at[c] = q;
+        m.net_ptr[slot + 1] = (int)q;
+      }
+      m.n_hpwl_nets = (int)E;
+      m.class_begin[5] = (int)E;
+      m.class_group[5] = 2;
+      for (uint32_t a = 0; a < arcs; ++a) {
+        size_t q = pins + 2 * (size_t)a;
+        for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
+          int unit;
+          pin_of(cell, unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
+          m.pin_unit[q] = unit;
+          ++q;
+        }
+        m.net_ptr[(size_t)E + a + 1] = (int)q;
+        m.net_w[(size_t)E + a] = (float)u64_to_f64(p->arc_extra_weight[a]);
+      }
+    } catch (...) {
+      layout_ok = false;
+    }
+  };
+  // this thread's buffers exist before the second thread starts, so nothing
+  // below can throw while it runs
+  std::vector<double> wl(U, 0.0), inc(C, 0.0), pin_weight_sum(U, 0.0);
+  std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
+  // small problems are not worth a thread
+  std::thread layout_thread;
+  const bool threaded = pins >= 65536;
+  if (threaded) layout_thread = std::thread(layout);
+  else layout();
+
+  // wirelength preconditioner and cell incidence (this thread): each
+  // distinct unit (cell) of a net counts once, found with a per-net stamp
+  // instead of a sort
+  for (uint32_t e = 0; e < E; ++e) {
+    const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
     const double w = 1.0 / (double)(uint32_t)(en - b - 1);
     uint32_t distinct = 0;
     for (uint32_t k = b; k < en; ++k) {
@@ -300,13 +384,9 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
       }
     }
   }
-  std::vector<double> pin_weight_sum(U, 0.0);
-  for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
-    const uint32_t dc = p->arc_driver_cell[a], sc = p->arc_sink_cell[a];
-    if (dc >= C || sc >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
-    const uint32_t du = p->cell_unit[dc], su = p->cell_unit[sc];
+  for (uint32_t a = 0; a < arcs; ++a) {
+    const uint32_t du = p->cell_unit[p->arc_driver_cell[a]], su = p->cell_unit[p->arc_sink_cell[a]];
     const double w = u64_to_f64(p->arc_extra_weight[a]);
-    if (w > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
     if (du != su) {
       wl[du] += w;
       wl[su] += w;
@@ -314,52 +394,10 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     pin_weight_sum[du] += w;
     pin_weight_sum[su] += w;
   }
-  // degree classes: 2 | 3-4 | 5-8 | 9-16 | 17+ ; timed arcs last
-  static const int groups[5] = {2, 4, 8, 16, 32};
-  auto cls = [](uint32_t deg) { return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : 4; };
-  std::vector<std::vector<uint32_t>> bucket(5);
-  for (uint32_t e = 0; e < E; ++e) bucket[cls(p->net_ptr[e + 1] - p->net_ptr[e])].push_back(e);
-  const size_t pins = E ? p->net_ptr[E] : 0;
-  m.net_ptr.reserve((size_t)E + p->num_timed_arcs + 1);
-  m.net_w.reserve((size_t)E + p->num_timed_arcs);
-  m.pin_unit.reserve(pins + 2 * (size_t)p->num_timed_arcs);
-  m.pin_base.reserve(2 * (pins + 2 * (size_t)p->num_timed_arcs));
-  m.net_ptr.assign(1, 0);
-  int nc = 0;
-  for (int c = 0; c < 5; ++c) {
-    m.class_begin[c] = (int)m.net_w.size();
-    m.class_group[c] = groups[c];
-    for (uint32_t e : bucket[c]) {
-      for (uint32_t k = p->net_ptr[e]; k < p->net_ptr[e + 1]; ++k) {
-        int unit;
-        double bx, by;
-        pin_of(p->pin_cell[k], unit, bx, by);
-        m.pin_unit.push_back(unit);
-        m.pin_base.push_back(bx);
-        m.pin_base.push_back(by);
-        if (unit >= 0) pin_weight_sum[unit] += 1.0;
-      }
-      m.net_ptr.push_back((int)m.pin_unit.size());
-      m.net_w.push_back(1.0f);
-    }
-    nc = c + 1;
-  }
-  m.n_hpwl_nets = (int)m.net_w.size();
-  m.class_begin[5] = (int)m.net_w.size();
-  m.class_group[5] = 2;
-  for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
-    for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
-      int unit;
-      double bx, by;
-      pin_of(cell, unit, bx, by);
-      m.pin_unit.push_back(unit);
-      m.pin_base.push_back(bx);
-      m.pin_base.push_back(by);
-    }
-    m.net_ptr.push_back((int)m.pin_unit.size());
-    m.net_w.push_back((float)u64_to_f64(p->arc_extra_weight[a]));
-  }
-  nc = 6;
+  if (threaded) layout_thread.join();
+  if (!layout_ok) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  for (uint32_t u = 0; u < U; ++u) pin_weight_sum[u] += pin_count[u];
+  int nc = 6;
   m.n_classes = nc;
   m.class_begin[6] = (int)m.net_w.size();
   if (m.pin_unit.size() >= (1ull << 31)) return TEXO_GP_ERR_GRID_TOO_LARGE;

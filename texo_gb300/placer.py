@@ -33,21 +33,24 @@ def _stats_dict(s):
                 density_evaluations=s.density_evaluations)
 
 
-def place(problem, params=None):
+def place(problem, params=None, coordinates=False):
     """eplace::place through texo_gp_place: returns (targets [U,2] uint32,
-    coordinates [2(U+F)] float64, stats dict)."""
-    lib = abi.load()
+    coordinates, stats dict). The continuous coordinates [2(U+F)] float64
+    come back with coordinates=True; their length is known only once the
+    fillers exist, so that form runs the same create / run / destroy
+    through a Placer. Otherwise coordinates is None."""
     params = params or default_params()
+    if coordinates:
+        with Placer(problem, params) as h:
+            targets, coords, stats = h.run()
+        return targets, coords, stats
+    lib = abi.load()
     pc = problem.c_struct()
     targets = np.zeros(2 * problem.num_units, np.uint32)
-    # the optimizer vector length is known only after filler construction
-    with Placer(problem, params) as h:
-        coords = np.zeros(h.n)
     st = abi.Stats()
-    code = lib.texo_gp_place(C.byref(pc), C.byref(params), abi.ptr(targets, C.c_uint32),
-                             abi.ptr(coords, C.c_double), C.byref(st))
+    code = lib.texo_gp_place(C.byref(pc), C.byref(params), abi.ptr(targets, C.c_uint32), None, C.byref(st))
     abi.check(code, "texo_gp_place")
-    return targets.reshape(-1, 2), coords, _stats_dict(st)
+    return targets.reshape(-1, 2), None, _stats_dict(st)
 
 
 class Batch:
