@@ -454,6 +454,41 @@ def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
     return report
 
 
+def stage_report(workload, dct_name, reps):
+    """Every stage kernel of the host engine on `workload`, timed at the
+    positions one placement ends at (cells spread at overflow <= 0.10):
+    each kernel launched `reps` times back to back (CUDA events; inputs
+    that fit in L2 stay there between launches), with its algorithmic bytes
+    and their rate against the measured HBM peak. The launches are inside
+    the NVTX range "stages", so an ncu capture can select them with
+    --nvtx --nvtx-include stages/."""
+    import torch
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer
+    dct = {"fp32": abi.DCT_FP32, "bf16x3": abi.DCT_BF16X3, "fp32-gemm": abi.DCT_FP32_GEMM}[dct_name]
+    prob = make_problem(workload, 0)
+    prm = make_params(workload, abi.ENGINE_HOST, dct)
+    peak, kind = peaks()
+    with Placer(prob, prm) as g:
+        _, _, s = g.run(allow_nonconverged=True)
+        n = dict(U=g.units, F=g.num_fillers, M=int(prob.member_ptr[-1]), B=g.bins, Hb=g.bins_y,
+                 E=prob.num_nets, P=prob.num_pins, K=g.num_fields, dct_form=g.dct_form())
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("stages")
+        st = named_stages(g.stage_times(reps=reps), n)
+        torch.cuda.nvtx.range_pop()
+    out = {}
+    for k, ms in st.items():
+        b = stage_bytes(k, n)
+        out[k] = {"us": round(ms * 1000, 2), "algorithmic_bytes": b,
+                  "gbs": round(b / (ms * 1e-3) / 1e9, 1) if ms > 0 and b else None,
+                  "frac": round(b / (ms * 1e-3) / 1e9 / peak, 4) if ms > 0 and b else None}
+    return {"metric": "stage kernels at placed positions", "workload": workload, "engine": "host",
+            "dct_form": Placer.DCT_FORMS[n["dct_form"]], "sizes": n, "placement_iterations": s["iterations"],
+            "final_overflow": s["overflow"], "reps": reps, "peak_gbs": peak, "peak_source": kind,
+            "stages": out}
+
+
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
@@ -538,6 +573,9 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="print only the serving-stream report")
     ap.add_argument("--no-precision", action="store_true", help="skip the 1M-cell precision report")
     ap.add_argument("--precision-only", action="store_true", help="print only the 1M-cell precision report")
+    ap.add_argument("--stage-report", action="store_true",
+                    help="print only the per-stage kernel report of --workload at placed positions")
+    ap.add_argument("--stage-reps", type=int, default=10)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -566,6 +604,10 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "BF16x3 / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
+        return
+    if args.stage_report:
+        if rank == 0:
+            print(json.dumps(stage_report(args.workload, args.dct, args.stage_reps)), flush=True)
         return
     if args.serve_only:
         if rank == 0:
@@ -603,6 +645,8 @@ def main():
         s = one_step()
     # timed steps
     total_ms, launches, evals, devals, trials = 0.0, 0, 0, 0, 0
+    phases0 = g.device_profile() if engine == abi.ENGINE_DEVICE else None
+    restarts0 = state["restarts"]
     with Clocks(local) as clk:
         if dist:
             dist.barrier()
@@ -620,6 +664,13 @@ def main():
         if dist:
             dist.barrier()
     max_ms, value = aggregate_ranks(total_ms, args.steps, dist, "cuda")
+    # the persistent kernel's own phase clocks (block 0, globaltimer) over
+    # the timed steps, per step; barrier_wait is the part of them block 0
+    # spent waiting in grid barriers (a restart mid-run resets them)
+    phases = None
+    if phases0 is not None and state["restarts"] == restarts0:
+        p1 = g.device_profile()
+        phases = {k: round((p1[k] - phases0[k]) / args.steps, 2) for k in p1}
     if args.profile:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "iter/s", "profile": True,
@@ -654,6 +705,7 @@ def main():
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_step_bytes,
                 "launch_ms": dom_ms, "evaluations_per_step": evals / args.steps,
                 "density_evaluations_per_step": devals / args.steps,
+                "phases_us_per_step": phases,
                 "trials_per_step": trials / args.steps, "stages": stage_roofline}
     # end to end through the C ABI from host buffers
     e2e = None
