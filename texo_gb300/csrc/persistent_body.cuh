@@ -96,6 +96,29 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned np, unsigned*
   return *failed == 0;
 }
 
+// One reduction of the V partials of a slot, folded by one warp in a fixed
+// order (lanes stride the partials, then an xor tree over the lanes).
+enum FoldOp { FOLD_DSUM, FOLD_ISUM, FOLD_IMIN, FOLD_DMAX, FOLD_DMIN };
+struct FoldJob {
+  const void* a;
+  int op;
+};
+union FoldValue {
+  double d;
+  long long l;
+};
+constexpr int kMaxFoldJobs = 3 * kMaxFields + 3;
+template <typename T, typename Op>
+__device__ __forceinline__ T warp_fold(const T* a, int n, T init, Op op) {
+  const int lane = threadIdx.x & 31;
+  T v = lane < n ? a[lane] : init;
+#pragma unroll 4
+  for (int i = lane + 32; i < n; i += 32) v = op(v, a[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
 template <bool LARGE>
 struct Ctx {
   const Dev& d;
@@ -110,6 +133,7 @@ struct Ctx {
   double* rd;         // reduction scratch (shared)
   long long* rl;
   double* coef;       // shared [kMaxFields]
+  FoldValue* fv;      // shared [kMaxFoldJobs] results of fold()
   long long* fmean;   // shared [kMaxFields] fixed-point density means
   int pb, np;         // physical block of the instance, physical block count
   int V;              // virtual blocks of the instance
@@ -137,6 +161,29 @@ struct Ctx {
       clock[8] = t;
     }
   }
+  // Several reductions of partials at once: job j is folded by warp j (mod
+  // the warp count), so the loads of all jobs are in flight together (one
+  // L2 round trip for partials that other SMs wrote, often on the other
+  // die) and the FP64 folds of different jobs run on different SM
+  // sub-partitions. Every thread reads the results in fv after the final
+  // block barrier.
+  __device__ void fold(const FoldJob* jobs, int n) {
+    __syncthreads();   // earlier readers of fv are done
+    const int nw = (int)(blockDim.x >> 5);
+    for (int j = threadIdx.x >> 5; j < n; j += nw) {
+      const FoldJob jb = jobs[j];
+      FoldValue out;
+      switch (jb.op) {
+        case FOLD_DSUM: out.d = warp_fold((const double*)jb.a, V, 0.0, OpAdd()); break;
+        case FOLD_ISUM: out.l = warp_fold((const long long*)jb.a, V, 0ll, OpAdd()); break;
+        case FOLD_IMIN: out.l = warp_fold((const long long*)jb.a, V, 0x7fffffffffffffffll, OpMin()); break;
+        case FOLD_DMAX: out.d = warp_fold((const double*)jb.a, V, 0.0, OpMax()); break;
+        default: out.d = warp_fold((const double*)jb.a, V, (double)INFINITY, OpMin()); break;
+      }
+      if ((threadIdx.x & 31) == 0) fv[j] = out;
+    }
+    __syncthreads();
+  }
   __device__ double rsum(int slot) { return block_reduce_array(pslot(r.p, slot), V, 0.0, OpAdd(), rd); }
   __device__ long long risum(int slot) { return block_reduce_array(islot(r.p, slot), V, 0ll, OpAdd(), rl); }
   __device__ long long rimin(int slot) {
@@ -160,6 +207,16 @@ struct Ctx {
     for (int i = pb * blockDim.x + threadIdx.x; i < n; i += np * blockDim.x) dst[i] = src[i];
   }
 
+  // fixed-point density mean per field (DC mode), from the scatter's grid sums
+  __device__ void fold_means() {
+    FoldJob jobs[kMaxFields];
+    for (int f = 0; f < d.K; ++f) jobs[f] = FoldJob{islot(r.p, IS_GRID_SUM + f), FOLD_ISUM};
+    fold(jobs, d.K);
+    if (threadIdx.x == 0)
+      for (int f = 0; f < d.K; ++f) fmean[f] = (fv[f].l - d.capsum[f]) / d.B;
+    __syncthreads();
+  }
+
   // Objective evaluation at pos after an init phase and its barrier
   // (ContinuousProblem::evaluate + combined_objective, eplace.rs:137-205, 1022-1044).
   __device__ bool eval_tail(const float2* pos, float2* g, double gam, bool full, const float2* kkt_pos, ERec& out) {
@@ -171,11 +228,7 @@ struct Ctx {
     if (full) {
       if (d.fft) {
         // FFT form: rows (with the density preparation folded in), columns, rows
-        for (int f = 0; f < d.K; ++f) {
-          const long long tot = block_reduce_array(islot(r.p, IS_GRID_SUM + f), V, 0ll, OpAdd(), rl);
-          if (threadIdx.x == 0) fmean[f] = (tot - d.capsum[f]) / d.B;
-        }
-        __syncthreads();
+        fold_means();
         fft::Smem& fs = *reinterpret_cast<fft::Smem*>(gsm.fft);
         for (int v = pb; v < V; v += np) fft::pass_rows_fwd(d, r.p, v, V, fs, sh, fmean);
         if (!sync()) return false;
@@ -191,11 +244,7 @@ struct Ctx {
           mark(PC_PREP);
         } else {
           // density preparation folded into the first transform (one phase less)
-          for (int f = 0; f < d.K; ++f) {
-            const long long tot = block_reduce_array(islot(r.p, IS_GRID_SUM + f), V, 0ll, OpAdd(), rl);
-            if (threadIdx.x == 0) fmean[f] = (tot - d.capsum[f]) / d.B;
-          }
-          __syncthreads();
+          fold_means();
           for (int v = pb; v < V; v += np) stage_prep_dct0(d, fmean, r.p, v, V, gsm, sh);
           if (!sync()) return false;
           st0 = 1;
@@ -206,27 +255,37 @@ struct Ctx {
         }
       }
       mark(PC_DCT);
+    }
+    {
+      // energies, overflow and overflowed bins per field (density side
+      // rebuilt), and the WA value: one fold
+      FoldJob jobs[kMaxFoldJobs];
+      int nj = 0;
+      if (full)
+        for (int f = 0; f < d.K; ++f) {
+          jobs[nj++] = FoldJob{pslot(r.p, SLOT_ENERGY + f), FOLD_DSUM};
+          jobs[nj++] = FoldJob{islot(r.p, IS_OVERFLOW + f), FOLD_ISUM};
+          jobs[nj++] = FoldJob{islot(r.p, IS_OVER_BINS + f), FOLD_ISUM};
+        }
+      jobs[nj++] = FoldJob{pslot(r.p, SLOT_WA_VALUE), FOLD_DSUM};
+      fold(jobs, nj);
+    }
+    if (threadIdx.x == 0) {
       for (int f = 0; f < d.K; ++f) {
-        const double e = rsum(SLOT_ENERGY + f);
-        const long long ov = risum(IS_OVERFLOW + f);
-        const long long nb = risum(IS_OVER_BINS + f);
-        if (threadIdx.x == 0) {
-          out.energy[f] = 0.5 * e;
+        if (full) {
+          const long long ov = fv[3 * f + 1].l;
+          out.energy[f] = 0.5 * fv[3 * f].d;
           out.ovfix[f] = ov;
-          out.bins[f] = nb;
+          out.bins[f] = fv[3 * f + 2].l;
           out.overflow[f] = ((double)ov * kInvFix) * S.inv_real_area[f];
+        } else {
+          out.energy[f] = S.cur_energy[f];
+          out.overflow[f] = S.cur_overflow[f];
+          out.ovfix[f] = S.cur_overflow_fixed[f];
+          out.bins[f] = 0;
         }
       }
-    } else if (threadIdx.x == 0) {
-      for (int f = 0; f < d.K; ++f) {
-        out.energy[f] = S.cur_energy[f];
-        out.overflow[f] = S.cur_overflow[f];
-        out.ovfix[f] = S.cur_overflow_fixed[f];
-        out.bins[f] = 0;
-      }
-    }
-    const double wa = rsum(SLOT_WA_VALUE);
-    if (threadIdx.x == 0) {
+      const double wa = fv[full ? 3 * d.K : 0].d;
       out.wa = wa;
       double value = wa;
       for (int f = 0; f < d.K; ++f) {
@@ -245,21 +304,26 @@ struct Ctx {
     }
     if (!sync()) return false;
     mark(PC_GATHER);
-    for (int f = 0; f < d.K; ++f) {
-      const double a = rsum(SLOT_RAWL1 + f);
-      const double b = rsum(SLOT_FORCE + f);
-      if (threadIdx.x == 0) {
-        out.rawl1[f] = a;
-        out.force[f] = b;
+    {
+      FoldJob jobs[kMaxFoldJobs];
+      int nj = 0;
+      for (int f = 0; f < d.K; ++f) {
+        jobs[nj++] = FoldJob{pslot(r.p, SLOT_RAWL1 + f), FOLD_DSUM};
+        jobs[nj++] = FoldJob{pslot(r.p, SLOT_FORCE + f), FOLD_DSUM};
       }
+      jobs[nj++] = FoldJob{pslot(r.p, SLOT_WAL1), FOLD_DSUM};
+      jobs[nj++] = FoldJob{islot(r.p, IS_BAD), FOLD_IMIN};
+      if (kkt_pos) jobs[nj++] = FoldJob{mslot(r.p, MS_KKT), FOLD_DMAX};
+      fold(jobs, nj);
     }
-    const double w = rsum(SLOT_WAL1);
-    const long long bad = rimin(IS_BAD);
-    const double kkt = kkt_pos ? rmax(MS_KKT) : 0.0;
     if (threadIdx.x == 0) {
-      out.wal1 = w;
-      out.bad = bad;
-      out.kkt = kkt;
+      for (int f = 0; f < d.K; ++f) {
+        out.rawl1[f] = fv[2 * f].d;
+        out.force[f] = fv[2 * f + 1].d;
+      }
+      out.wal1 = fv[2 * d.K].d;
+      out.bad = fv[2 * d.K + 1].l;
+      out.kkt = kkt_pos ? fv[2 * d.K + 2].d : 0.0;
       S.evaluations++;
       if (full) S.density_evaluations++;
     }
@@ -394,6 +458,7 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
   __shared__ double rd[kThreads / 32];
   __shared__ long long rl[kThreads / 32];
   __shared__ double coef[kMaxFields];
+  __shared__ FoldValue fvals[kMaxFoldJobs];
   __shared__ long long fmean[kMaxFields];
   __shared__ unsigned gen;
   __shared__ int bar_failed;
@@ -407,7 +472,7 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
   }
   copy_words(&S, run);
   __syncthreads();
-  Ctx<LARGE> c{d, r, B, S, bar, &gen, &bar_failed, gsm, sh, rd, rl, coef, fmean, pb, np, Vn, 0ull, clock};
+  Ctx<LARGE> c{d, r, B, S, bar, &gen, &bar_failed, gsm, sh, rd, rl, coef, fvals, fmean, pb, np, Vn, 0ull, clock};
   const int n = d.nobj;
   unsigned done = 0;
   bool ok = true;
@@ -544,8 +609,13 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
       if (V.pending_best) c.copy(B.best, c.X(), d.U);
       if (V.pending_prev) c.copy(c.Xp(), c.X(), n);
       SYNC_OR_EXIT(PC_PRECOND)
-      const double pmin = c.rmin(MS_PMIN), pmax = c.rmax(MS_PMAX);
-      const long long pbad = c.risum(IS_PBAD);
+      {
+        const FoldJob jobs[3] = {{mslot(r.p, MS_PMIN), FOLD_DMIN}, {mslot(r.p, MS_PMAX), FOLD_DMAX},
+                                 {islot(r.p, IS_PBAD), FOLD_ISUM}};
+        c.fold(jobs, 3);
+      }
+      const double pmin = c.fv[0].d, pmax = c.fv[1].d;
+      const long long pbad = c.fv[2].l;
       T0 {
         V.pmin = pmin;
         V.pmax = pmax;
@@ -660,8 +730,14 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
             stage_init(d, v, c.V, true, true);
           }
           SYNC_OR_EXIT(PC_CANDIDATE)
-          const long long changed = c.risum_prev(IS_DIFF);
-          const double dot = c.rsum_prev(SLOT_DOT), msn = c.rsum_prev(SLOT_MSN);
+          {
+            const Partials q = c.rset();
+            const FoldJob jobs[3] = {{islot(q, IS_DIFF), FOLD_ISUM}, {pslot(q, SLOT_DOT), FOLD_DSUM},
+                                     {pslot(q, SLOT_MSN), FOLD_DSUM}};
+            c.fold(jobs, 3);
+          }
+          const long long changed = c.fv[0].l;
+          const double dot = c.fv[1].d, msn = c.fv[2].d;
           T0 {
             V.action = ACT_NONE;
             if (changed == 0) {
