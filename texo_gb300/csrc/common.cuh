@@ -18,7 +18,7 @@ constexpr float kFixF = 4294967296.0f;   // density fixed point: 2^32 per unit c
 constexpr double kFix = 4294967296.0;
 constexpr double kInvFix = 1.0 / 4294967296.0;
 constexpr float kInvFixF = 1.0f / 4294967296.0f;
-constexpr int kMaxClasses = 6;           // WA degree classes
+constexpr int kMaxClasses = 7;           // WA degree classes
 
 // Reduction slots (per-block partials, reduced in a fixed order).
 enum Slot {

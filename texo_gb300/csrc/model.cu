@@ -281,25 +281,30 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     if (u64_to_f64(p->arc_extra_weight[a]) > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
   }
 
-  // Pin layout (second thread): degree classes 2 | 3-4 | 5-8 | 9-16 | 17+
-  // laid out class by class (a counting sort over the classes, nets of a
-  // class in input order), then the timed arcs as 2-pin nets; every output
-  // is sized once and filled by index. pin_count[u] = pins of unit u.
-  static const int groups[5] = {2, 4, 8, 16, 32};
-  auto cls = [](uint32_t deg) { return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : 4; };
+  // Pin layout (second thread): degree classes 2 | 3-4 | 5-8 | 9-16 | 17-32
+  // | 33+ laid out class by class (a counting sort over the classes, nets of
+  // a class in input order), then the timed arcs as 2-pin nets; every output
+  // is sized once and filled by index. pin_count[u] = pins of unit u. The
+  // WA kernel gives a net of class c groups[c] lanes, so that a lane holds
+  // at most four pins of a net up to 32 pins (33+: one warp per net).
+  constexpr int kNetClasses = 6;
+  static const int groups[kNetClasses] = {1, 1, 2, 4, 8, 32};
+  auto cls = [](uint32_t deg) {
+    return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : deg <= 32 ? 4 : 5;
+  };
   const size_t pins = E ? p->net_ptr[E] : 0;
   std::vector<double> pin_count(U, 0.0);
   bool layout_ok = true;
   auto layout = [&]() {
     try {
-      size_t nets_in[5] = {0, 0, 0, 0, 0}, pins_in[5] = {0, 0, 0, 0, 0};
+      size_t nets_in[kNetClasses] = {0, 0, 0, 0, 0, 0}, pins_in[kNetClasses] = {0, 0, 0, 0, 0, 0};
       for (uint32_t e = 0; e < E; ++e) {
         const uint32_t deg = p->net_ptr[e + 1] - p->net_ptr[e];
         nets_in[cls(deg)]++;
         pins_in[cls(deg)] += deg;
       }
-      size_t net_at[5], pin_at[5];
-      for (int c = 0, n0 = 0, p0 = 0; c < 5; ++c) {
+      size_t net_at[kNetClasses], pin_at[kNetClasses];
+      for (int c = 0, n0 = 0, p0 = 0; c < kNetClasses; ++c) {
         net_at[c] = n0;
         pin_at[c] = p0;
         m.class_begin[c] = n0;
@@ -327,8 +332,8 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
         m.net_ptr[slot + 1] = (int)q;
       }
       m.n_hpwl_nets = (int)E;
-      m.class_begin[5] = (int)E;
-      m.class_group[5] = 2;
+      m.class_begin[kNetClasses] = (int)E;   // timed arcs: 2-pin nets, one lane each
+      m.class_group[kNetClasses] = 1;
       for (uint32_t a = 0; a < arcs; ++a) {
         size_t q = pins + 2 * (size_t)a;
         for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
@@ -397,9 +402,8 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   if (threaded) layout_thread.join();
   if (!layout_ok) return TEXO_GP_ERR_INVALID_ARGUMENT;
   for (uint32_t u = 0; u < U; ++u) pin_weight_sum[u] += pin_count[u];
-  int nc = 6;
-  m.n_classes = nc;
-  m.class_begin[6] = (int)m.net_w.size();
+  m.n_classes = kNetClasses + 1;
+  m.class_begin[kNetClasses + 1] = (int)m.net_w.size();
   if (m.pin_unit.size() >= (1ull << 31)) return TEXO_GP_ERR_GRID_TOO_LARGE;
   // WA fixed point: |derivative| <= 3 per pin, summed per unit, at 2^32 per unit
   for (uint32_t u = 0; u < U; ++u)

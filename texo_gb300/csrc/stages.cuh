@@ -196,7 +196,11 @@ __device__ __forceinline__ float2 pin_xy(const Dev& d, const float2* pos, int k)
 
 // `slot` is this lane's index within the class's lane segment of `seg`
 // lanes (both multiples of 32 at the segment start, so a group never
-// straddles a warp and every lane of a warp makes the same passes).
+// straddles a warp and every lane of a warp makes the same passes). Lane l
+// of a group takes pins p0 + l, p0 + l + G, ...; the first kWaPins of them
+// stay in registers across the three passes (their loads are issued
+// together), any further ones are read again.
+constexpr int kWaPins = 4;
 template <int G>
 __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float inv_gamma, int nb,
                                          int ne, int slot, int seg, double& acc) {
@@ -216,12 +220,30 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float 
       p1 = d.net_ptr[e + 1];
       w = d.net_w[e];
     }
-    // pass 1: hard extrema per axis; the first pin is kept for the low-degree case
+    // pass 1: this lane's pins and the hard extrema per axis
+    float2 pv[kWaPins];
+    int pu[kWaPins];
+#pragma unroll
+    for (int j = 0; j < kWaPins; ++j) {
+      const int k = p0 + lane + j * G;
+      pu[j] = k < p1 ? d.pin_unit[k] : -2;   // -2: no pin, -1: fixed pin
+      pv[j] = k < p1 ? d.pin_base[k] : make_float2(0.f, 0.f);
+    }
     float mx = -INFINITY, mnx = INFINITY, my = -INFINITY, mny = INFINITY;
-    float2 first = make_float2(0.f, 0.f);
-    for (int k = p0 + lane; k < p1; k += G) {
+#pragma unroll
+    for (int j = 0; j < kWaPins; ++j) {
+      if (pu[j] == -2) continue;
+      if (pu[j] >= 0) {
+        const float2 q = pos[pu[j]];
+        pv[j] = make_float2(q.x + pv[j].x, q.y + pv[j].y);
+      }
+      mx = fmaxf(mx, pv[j].x);
+      mnx = fminf(mnx, pv[j].x);
+      my = fmaxf(my, pv[j].y);
+      mny = fminf(mny, pv[j].y);
+    }
+    for (int k = p0 + lane + kWaPins * G; k < p1; k += G) {
       const float2 v = pin_xy(d, pos, k);
-      if (k == p0 + lane) first = v;
       mx = fmaxf(mx, v.x);
       mnx = fminf(mnx, v.x);
       my = fmaxf(my, v.y);
@@ -236,8 +258,7 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float 
     }
     // pass 2: exponential weights (exactly 1 at the extremum) and their sums
     float sw[4] = {0.f, 0.f, 0.f, 0.f}, sd[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int k = p0 + lane; k < p1; k += G) {
-      const float2 v = (k == p0 + lane) ? first : pin_xy(d, pos, k);
+    auto weigh = [&](float2 v) {
       const float dxp = v.x - mx, dxn = v.x - mnx, dyp = v.y - my, dyn = v.y - mny;
       const float wxp = expf(dxp * inv_gamma), wxn = expf(-dxn * inv_gamma);
       const float wyp = expf(dyp * inv_gamma), wyn = expf(-dyn * inv_gamma);
@@ -245,7 +266,11 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float 
       sw[1] += wxn; sd[1] = fmaf(wxn, dxn, sd[1]);
       sw[2] += wyp; sd[2] = fmaf(wyp, dyp, sd[2]);
       sw[3] += wyn; sd[3] = fmaf(wyn, dyn, sd[3]);
-    }
+    };
+#pragma unroll
+    for (int j = 0; j < kWaPins; ++j)
+      if (pu[j] != -2) weigh(pv[j]);
+    for (int k = p0 + lane + kWaPins * G; k < p1; k += G) weigh(pin_xy(d, pos, k));
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
@@ -261,10 +286,7 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float 
       mean[a] = sd[a] * inv[a];
     }
     // pass 3: per-pin derivative into the fixed-point unit gradient
-    for (int k = p0 + lane; k < p1; k += G) {
-      const int u = d.pin_unit[k];
-      if (u < 0) continue;
-      const float2 v = (k == p0 + lane) ? first : pin_xy(d, pos, k);
+    auto derive = [&](int u, float2 v) {
       const float dxp = v.x - mx, dxn = v.x - mnx, dyp = v.y - my, dyn = v.y - mny;
       const float wxp = expf(dxp * inv_gamma), wxn = expf(-dxn * inv_gamma);
       const float wyp = expf(dyp * inv_gamma), wyn = expf(-dyn * inv_gamma);
@@ -274,6 +296,13 @@ __device__ __forceinline__ void wa_class(const Dev& d, const float2* pos, float 
                        wyn * inv[3] * (1.f - (dyn - mean[3]) * inv_gamma);
       atomicAdd(d.wa_fix + 2 * u, (unsigned long long)__float2ll_rn(w * gx * kFixF));
       atomicAdd(d.wa_fix + 2 * u + 1, (unsigned long long)__float2ll_rn(w * gy * kFixF));
+    };
+#pragma unroll
+    for (int j = 0; j < kWaPins; ++j)
+      if (pu[j] >= 0) derive(pu[j], pv[j]);
+    for (int k = p0 + lane + kWaPins * G; k < p1; k += G) {
+      const int u = d.pin_unit[k];
+      if (u >= 0) derive(u, pin_xy(d, pos, k));
     }
     if (lane == 0) vacc += w * (((mx - mnx) + mean[0] - mean[1]) + ((my - mny) + mean[2] - mean[3]));
   }
@@ -292,10 +321,10 @@ static __device__ void stage_wa(const Dev& d, const float2* pos, double gamma, P
     const int slot = gl - d.class_lane[c], seg = d.class_lane[c + 1] - d.class_lane[c];
     if (ne > nb && seg > 0) {
       switch (d.class_group[c]) {
+        case 1: wa_class<1>(d, pos, ig, nb, ne, slot, seg, acc); break;
         case 2: wa_class<2>(d, pos, ig, nb, ne, slot, seg, acc); break;
         case 4: wa_class<4>(d, pos, ig, nb, ne, slot, seg, acc); break;
         case 8: wa_class<8>(d, pos, ig, nb, ne, slot, seg, acc); break;
-        case 16: wa_class<16>(d, pos, ig, nb, ne, slot, seg, acc); break;
         default: wa_class<32>(d, pos, ig, nb, ne, slot, seg, acc); break;
       }
     }
