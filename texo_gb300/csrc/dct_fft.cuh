@@ -44,6 +44,29 @@ __device__ __forceinline__ Axis axis_y(const Dev& d) {
   return Axis{d.fy_tw, d.fy_post, d.fy_pre, d.fy_inv_s, d.g.Hb, d.logH};
 }
 
+// Up to 256 points the data of a group takes at most 1024 slots of the work
+// buffer, and the tables (n/2 twiddles, n post and n pre factors, n 1/s_k)
+// are copied into the other 1024 once per pass: the stages then read their
+// twiddles from shared memory instead of making an L2 round trip per stage
+// (the persistent kernel's grid barriers leave L1 cold).
+constexpr int kTableLog = 8;
+__device__ __forceinline__ Axis stage_tables(const Axis& a, float2* buf) {
+  if (a.logn > kTableLog) return a;
+  float2* tw = buf + kBuf / 2;
+  float2* post = tw + (a.n >> 1);
+  float2* pre = post + a.n;
+  float* inv_s = reinterpret_cast<float*>(pre + a.n);
+  __syncthreads();   // earlier readers of the buffer are done
+  for (int i = threadIdx.x; i < a.n; i += blockDim.x) {
+    if (i < (a.n >> 1)) tw[i] = a.tw[i];
+    post[i] = a.post[i];
+    pre[i] = a.pre[i];
+    inv_s[i] = a.inv_s[i];
+  }
+  __syncthreads();
+  return Axis{tw, post, pre, inv_s, a.n, a.logn};
+}
+
 // Vectors transformed together: one butterfly per thread per stage (n/2
 // butterflies per vector), at least one vector; many small groups keep every
 // SM busy on small grids.
@@ -135,9 +158,9 @@ __device__ __forceinline__ void dct3(float2* buf, int G, const Axis& a, Coef c) 
 // is counted into the IS_OVERFLOW / IS_OVER_BINS partials.
 static __device__ void pass_rows_fwd(const Dev& d, Partials p, int vb, int nvb, Smem& sm, Shared& sh,
                                      const long long* mean) {
-  const Axis a = axis_x(d);
-  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(a.logn), H);
+  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(d.logW), H);
   const int gpf = (H + G - 1) / G, groups = gpf * d.K;
+  const Axis a = vb < groups ? stage_tables(axis_x(d), sm.buf) : axis_x(d);
   long long ov[kMaxFields], cnt[kMaxFields];
 #pragma unroll
   for (int f = 0; f < kMaxFields; ++f) ov[f] = cnt[f] = 0;
@@ -175,9 +198,9 @@ static __device__ void pass_rows_fwd(const Dev& d, Partials p, int vb, int nvb, 
 
 // Pass 2: t2 = cols-IDCT(cols-DCT(t1) * inv_eig), whole columns per group.
 static __device__ void pass_cols(const Dev& d, int vb, int nvb, Smem& sm) {
-  const Axis a = axis_y(d);
-  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(a.logn), W);
+  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(d.logH), W);
   const int gpf = (W + G - 1) / G, groups = gpf * d.K;
+  const Axis a = vb < groups ? stage_tables(axis_y(d), sm.buf) : axis_y(d);
   const int logG = 31 - __clz(G);
   const float inv_n = 1.0f / (float)H;
   for (int t = vb; t < groups; t += nvb) {
@@ -207,9 +230,9 @@ static __device__ void pass_cols(const Dev& d, int vb, int nvb, Smem& sm) {
 
 // Pass 3: phi = rows-IDCT(t2) and the energy partials <rho, phi>.
 static __device__ void pass_rows_inv(const Dev& d, Partials p, int vb, int nvb, Smem& sm, Shared& sh) {
-  const Axis a = axis_x(d);
-  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(a.logn), H);
+  const int W = d.g.Wb, H = d.g.Hb, G = min(group_size(d.logW), H);
   const int gpf = (H + G - 1) / G, groups = gpf * d.K;
+  const Axis a = vb < groups ? stage_tables(axis_x(d), sm.buf) : axis_x(d);
   const float inv_n = 1.0f / (float)W;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
   for (int t = vb; t < groups; t += nvb) {
