@@ -1032,14 +1032,18 @@ struct Controller {
       hr.init_weight = m.params.initial_density_weight;
       hr.gamma_base = m.gamma_base_tiles();
       hr.margin_eps = std::max(std::numeric_limits<double>::epsilon(), m.params.objective_margin_ulps * 0x1p-24);
+      double weight_sum = 0.0;
       for (uint32_t f = 0; f < m.K; ++f) {
         hr.target[f] = m.overflow_target(f);
+        hr.gamma_slope[f] = 2.0 / (1.0 - hr.target[f]);
         hr.gamma_weight[f] = m.gamma_weight[f];
         hr.real_area[f] = m.real_area[f];
         hr.inv_real_area[f] = 1.0 / m.real_area[f];
         hr.e0[f] = 1.0;
         hr.inv_e0[f] = 1.0;
+        weight_sum += m.gamma_weight[f];
       }
+      hr.inv_gamma_weight_sum = weight_sum == 0.0 ? 0.0 : 1.0 / weight_sum;
       hr.a = 1.0;
       hr.ix = 0;
       hr.ixp = 1;

@@ -40,6 +40,8 @@ struct DevRun {
   double beta, alpha_low, alpha_high, init_weight, gamma_base, margin_eps;
   double target[kMaxFields], gamma_weight[kMaxFields], real_area[kMaxFields];
   double inv_real_area[kMaxFields];   // 1 / real_area (FP64 division is slow on the device)
+  double gamma_slope[kMaxFields];     // 2 / (1 - target) of field_wirelength_gamma
+  double inv_gamma_weight_sum;        // 1 / sum of gamma_weight
   // loop state (optimize_density_once, eplace.rs:439-582)
   int phase;                    // 0 fresh, 1 running, 2 finished
   int status;                   // texo_gp_status

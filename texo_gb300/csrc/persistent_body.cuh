@@ -184,14 +184,6 @@ struct Ctx {
     }
     __syncthreads();
   }
-  __device__ double rsum(int slot) { return block_reduce_array(pslot(r.p, slot), V, 0.0, OpAdd(), rd); }
-  __device__ long long risum(int slot) { return block_reduce_array(islot(r.p, slot), V, 0ll, OpAdd(), rl); }
-  __device__ long long rimin(int slot) {
-    return block_reduce_array(islot(r.p, slot), V, 0x7fffffffffffffffll, OpMin(), rl);
-  }
-  __device__ double rmax(int slot) { return block_reduce_array(mslot(r.p, slot), V, 0.0, OpMax(), rd); }
-  __device__ double rmin(int slot) { return block_reduce_array(mslot(r.p, slot), V, (double)INFINITY, OpMin(), rd); }
-  __device__ double rsum_prev(int slot) { return block_reduce_array(pslot(rset(), slot), V, 0.0, OpAdd(), rd); }
   __device__ long long risum_prev(int slot) {
     return block_reduce_array(islot(rset(), slot), V, 0ll, OpAdd(), rl);
   }
@@ -333,10 +325,10 @@ struct Ctx {
 };
 
 // ---- scalar rules (eplace.rs:1300-1415), evaluated by thread 0 ------------
-static __device__ int field_gamma_dev(double overflow, double target, double base, double& g) {
+static __device__ int field_gamma_dev(double overflow, double target, double slope, double base, double& g) {
   if (!isfinite(overflow) || overflow < 0.0 || !(target >= 0.0 && target < 1.0) || !(base > 0.0))
     return TEXO_GP_ERR_INVALID_NORMALIZATION;
-  const double slope = 2.0 / (1.0 - target), intercept = 1.0 - slope;
+  const double intercept = 1.0 - slope;   // slope = 2 / (1 - target), from the host
   // 10^t as exp(t ln 10): a fraction of pow's cost on the device, within a
   // few ulps for the exponents this rule produces
   constexpr double kLn10 = 2.302585092994045684;
@@ -347,12 +339,12 @@ static __device__ int adaptive_gamma_dev(const DevRun& S, const double* overflow
   double ws = 0.0, wsum = 0.0;
   for (int f = 0; f < S.K; ++f) {
     double g;
-    const int st = field_gamma_dev(overflow[f], S.target[f], S.gamma_base, g);
+    const int st = field_gamma_dev(overflow[f], S.target[f], S.gamma_slope[f], S.gamma_base, g);
     if (st) return st;
     ws += g * S.gamma_weight[f];
     wsum += S.gamma_weight[f];
   }
-  out = wsum == 0.0 ? S.gamma_base : ws / wsum;
+  out = wsum == 0.0 ? S.gamma_base : ws * S.inv_gamma_weight_sum;
   return (isfinite(out) && out > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
 }
 static __device__ bool stop_dev(const DevRun& S, const double* overflow) {
@@ -466,7 +458,7 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
   if (threadIdx.x == 0) {
     for (int i = 0; i < 10; ++i) clock[i] = 0;
     clock[8] = now_ns();
-    gen = *(volatile unsigned*)&bar->gen;
+    gen = 0;   // the barrier is cleared with the state copy before every launch
     V.pending_best = 0;
     V.pending_prev = 0;
   }
