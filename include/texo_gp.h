@@ -84,7 +84,10 @@ typedef enum texo_gp_status {
   TEXO_GP_ERR_DEVICE_TIMEOUT = 99,   /* a bounded device-side wait ran out */
   TEXO_GP_ERR_FIXED_POINT_RANGE = 100, /* a weight or charge exceeds the int64 accumulator range */
   TEXO_GP_ERR_UNSUPPORTED = 101,
-  TEXO_GP_ERR_BUSY = 102
+  TEXO_GP_ERR_BUSY = 102,
+  /* PnrError::InvalidPlacement of the coarse quadratic seed: "analytical PCG
+   * {breakdown|dimension} after i/n iterations" (crates/texo-pnr/src/lib.rs:4702-4752) */
+  TEXO_GP_ERR_PCG_NOT_CONVERGED = 110
 } texo_gp_status;
 
 /* Resource kinds in the reference's `ResourceKind` order
@@ -428,6 +431,34 @@ int32_t texo_gp_server_poll(texo_gp_server s, int32_t wait_ms, texo_gp_job_resul
 int32_t texo_gp_server_counts(texo_gp_server s, uint32_t* queued, uint32_t* resident,
                               uint32_t* finished, uint64_t* bytes_in_use);
 double texo_gp_server_clock_ms(texo_gp_server s);
+
+/* ---- coarse quadratic seed ------------------------------------------------
+ * Replaces `solve_quadratic` (crates/texo-pnr/src/lib.rs:4586-4752, called
+ * from `solve_analytical_axis`, lib.rs:4531-4560): Jacobi-preconditioned
+ * conjugate gradients for (D - W) x = b, D = `diagonal` (finite, > 0), W the
+ * symmetric `adjacency` (row i: weights adjacency_weight[k] to columns
+ * adjacency_index[k], k in [adjacency_ptr[i], adjacency_ptr[i+1]), in the
+ * order of the reference's Vec<(usize, f64)>), all FP64, on one GPU. Stops
+ * when |r|^2 <= 1e-8 max(|r0|^2, eps64), re-checking the true residual before
+ * accepting (and restarting from it otherwise), on a breakdown, or after n
+ * loop passes; `solution` holds the initial guess on entry and the result on
+ * return. Returns TEXO_GP_ERR_PCG_NOT_CONVERGED (with the solution anyway)
+ * when the true final residual misses the target, like the reference. */
+typedef struct texo_gp_pcg_stats {
+  int32_t status;
+  uint32_t iterations;           /* conjugate-gradient steps taken */
+  uint32_t restarts;             /* true-residual restarts */
+  int32_t stop;                  /* 0 residual, 1 breakdown, 2 dimension (the reference's labels) */
+  double initial_residual_squared;
+  double target_squared;
+  double final_residual_squared; /* |b - (D - W) x|^2 of the returned solution */
+  double elapsed_ms;             /* device time (CUDA events), copies included */
+  uint64_t kernel_launches;
+} texo_gp_pcg_stats;
+int32_t texo_gp_quadratic_solve(int32_t device, uint32_t n, const double* diagonal,
+                                const uint32_t* adjacency_ptr, const uint32_t* adjacency_index,
+                                const double* adjacency_weight, const double* rhs, double* solution,
+                                texo_gp_pcg_stats* stats);
 
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)

@@ -54,6 +54,37 @@ EVAL_CB = C.CFUNCTYPE(C.c_int32, C.c_void_p, c_f64p, C.c_uint64, c_f64p, c_f64p,
 _lib = None
 
 
+class PcgStats(C.Structure):
+    _fields_ = [("iterations", C.c_uint64), ("restarts", C.c_uint64), ("stop", C.c_int32),
+                ("converged", C.c_int32), ("initial_residual_squared", C.c_double),
+                ("target_squared", C.c_double), ("final_residual_squared", C.c_double)]
+
+
+def solve_quadratic(diagonal, ptr, index, weight, rhs, solution=None):
+    """solve_quadratic (lib.rs:4586-4752) restated in FP64: returns (x, stats, converged)."""
+    n = len(diagonal)
+    d = np.ascontiguousarray(diagonal, dtype=np.float64)
+    p = np.ascontiguousarray(ptr, dtype=np.uint32)
+    i = np.ascontiguousarray(index, dtype=np.uint32)
+    w = np.ascontiguousarray(weight, dtype=np.float64)
+    b = np.ascontiguousarray(rhs, dtype=np.float64)
+    x = np.zeros(n) if solution is None else np.array(solution, dtype=np.float64, copy=True)
+    st = PcgStats()
+    code = lib().orc_solve_quadratic(n, P(d), P(p, C.c_uint32), P(i, C.c_uint32), P(w), P(b), P(x), C.byref(st))
+    return x, st, code == 0
+
+
+def multiply_quadratic(diagonal, ptr, index, weight, values):
+    n = len(diagonal)
+    out = np.zeros(n)
+    lib().orc_multiply_quadratic(n, P(np.ascontiguousarray(diagonal, dtype=np.float64)),
+                                 P(np.ascontiguousarray(ptr, dtype=np.uint32), C.c_uint32),
+                                 P(np.ascontiguousarray(index, dtype=np.uint32), C.c_uint32),
+                                 P(np.ascontiguousarray(weight, dtype=np.float64)),
+                                 P(np.ascontiguousarray(values, dtype=np.float64)), P(out))
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -93,6 +124,9 @@ def lib():
             "orc_overflow_target": (C.c_double, [C.c_uint32]),
             "orc_checkpoint_better": (C.c_int32, [C.c_double, C.c_double, C.c_double, C.c_double]),
             "orc_validate_units": (C.c_int32, [c_u32p, C.c_uint64, c_u64p]),
+            "orc_solve_quadratic": (C.c_int32, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p,
+                                                C.POINTER(PcgStats)]),
+            "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

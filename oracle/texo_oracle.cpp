@@ -1951,4 +1951,101 @@ int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t*
   return TEXO_GP_OK;
 }
 
+// ---- coarse quadratic seed (crates/texo-pnr/src/lib.rs:4586-4790) --------
+// multiply_quadratic (lib.rs:4767-4782): diagonal * v[i], then minus
+// weight * v[j] per adjacency entry, in order.
+void orc_multiply_quadratic(uint64_t n, const double* diagonal, const uint32_t* ptr, const uint32_t* index,
+                            const double* weight, const double* values, double* product) {
+  for (uint64_t i = 0; i < n; ++i) {
+    double s = diagonal[i] * values[i];
+    for (uint32_t k = ptr[i]; k < ptr[i + 1]; ++k) s = s - weight[k] * values[index[k]];
+    product[i] = s;
+  }
+}
+static double pcg_dot(const std::vector<double>& a, const std::vector<double>& b) {   // lib.rs:4784-4789
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+// apply_jacobi_preconditioner (lib.rs:4754-4765)
+static double pcg_jacobi(const std::vector<double>& r, const double* diagonal, std::vector<double>& z) {
+  for (size_t i = 0; i < r.size(); ++i) z[i] = r[i] / diagonal[i];
+  return pcg_dot(r, z);
+}
+// solve_quadratic + finish_quadratic_solve (lib.rs:4586-4752)
+int32_t orc_solve_quadratic(uint64_t n, const double* diagonal, const uint32_t* ptr, const uint32_t* index,
+                            const double* weight, const double* rhs, double* solution, orc_pcg_stats* st) {
+  const double kTol = 1e-8;
+  std::vector<double> x(solution, solution + n), product(n, 0.0), residual(n), pre(n, 0.0);
+  orc_multiply_quadratic(n, diagonal, ptr, index, weight, x.data(), product.data());
+  for (uint64_t i = 0; i < n; ++i) residual[i] = rhs[i] - product[i];
+  double rr = pcg_dot(residual, residual);
+  const double initial = rr;
+  const double target = std::max(initial, std::numeric_limits<double>::epsilon()) * kTol;
+  double rho = pcg_jacobi(residual, diagonal, pre);
+  std::vector<double> direction = pre;
+  uint64_t iterations = 0, restarts = 0;
+  bool breakdown = false;
+  for (uint64_t loop = 0; loop < n; ++loop) {
+    if (rr <= target) break;
+    orc_multiply_quadratic(n, diagonal, ptr, index, weight, direction.data(), product.data());
+    const double den = pcg_dot(direction, product);
+    if (!std::isfinite(den) || den <= 0.0 || !std::isfinite(rho) || rho <= 0.0) {
+      breakdown = true;
+      break;
+    }
+    const double alpha = rho / den;
+    if (!std::isfinite(alpha)) {
+      breakdown = true;
+      break;
+    }
+    for (uint64_t i = 0; i < n; ++i) {
+      x[i] += alpha * direction[i];
+      residual[i] -= alpha * product[i];
+    }
+    ++iterations;
+    rr = pcg_dot(residual, residual);
+    if (rr <= target) {
+      orc_multiply_quadratic(n, diagonal, ptr, index, weight, x.data(), product.data());
+      for (uint64_t i = 0; i < n; ++i) residual[i] = rhs[i] - product[i];
+      rr = pcg_dot(residual, residual);
+      if (rr <= target) break;
+      ++restarts;
+      rho = pcg_jacobi(residual, diagonal, pre);
+      if (!std::isfinite(rho) || rho <= 0.0) {
+        breakdown = true;
+        break;
+      }
+      direction = pre;
+      continue;
+    }
+    const double next = pcg_jacobi(residual, diagonal, pre);
+    if (!std::isfinite(next) || next <= 0.0) {
+      breakdown = true;
+      break;
+    }
+    const double beta = next / rho;
+    for (uint64_t i = 0; i < n; ++i) direction[i] = pre[i] + beta * direction[i];
+    rho = next;
+  }
+  orc_multiply_quadratic(n, diagonal, ptr, index, weight, x.data(), product.data());
+  double fin = 0.0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const double r = rhs[i] - product[i];
+    fin += r * r;
+  }
+  const bool converged = fin <= target;
+  for (uint64_t i = 0; i < n; ++i) solution[i] = x[i];
+  if (st) {
+    st->iterations = iterations;
+    st->restarts = restarts;
+    st->converged = converged ? 1 : 0;
+    st->stop = converged ? 0 : (breakdown ? 1 : 2);
+    st->initial_residual_squared = initial;
+    st->target_squared = target;
+    st->final_residual_squared = fin;
+  }
+  return converged ? 0 : 1;
+}
+
 }  // extern "C"

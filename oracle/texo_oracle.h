@@ -152,6 +152,22 @@ int32_t orc_checkpoint_better(double max_excess, double total_excess, double bes
                               double best_total);                       /* :106-119 */
 int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t* error_index);
 
+/* ---- coarse quadratic seed (crates/texo-pnr/src/lib.rs:4586-4790) -------- */
+typedef struct orc_pcg_stats {
+  uint64_t iterations, restarts;
+  int32_t stop;                 /* 0 residual, 1 breakdown, 2 dimension */
+  int32_t converged;
+  double initial_residual_squared, target_squared, final_residual_squared;
+} orc_pcg_stats;
+/* solve_quadratic: Jacobi-preconditioned CG for (D - W) x = b, W in CSR rows
+ * in the reference's adjacency order; `solution` is the initial guess and the
+ * result. Returns 0, or 1 when the true final residual misses the target. */
+int32_t orc_solve_quadratic(uint64_t n, const double* diagonal, const uint32_t* ptr, const uint32_t* index,
+                            const double* weight, const double* rhs, double* solution, orc_pcg_stats* stats);
+/* multiply_quadratic (lib.rs:4767-4782) */
+void orc_multiply_quadratic(uint64_t n, const double* diagonal, const uint32_t* ptr, const uint32_t* index,
+                            const double* weight, const double* values, double* product);
+
 #ifdef __cplusplus
 }
 #endif

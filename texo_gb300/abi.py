@@ -26,6 +26,7 @@ STATUS = {
     64: "DENSITY_FIELD_CHANGED", 65: "INVALID_NORMALIZATION", 66: "DID_NOT_CONVERGE",
     96: "INVALID_ARGUMENT", 97: "CUDA", 98: "OUT_OF_MEMORY", 99: "DEVICE_TIMEOUT",
     100: "FIXED_POINT_RANGE", 101: "UNSUPPORTED", 102: "BUSY",
+    110: "PCG_NOT_CONVERGED",
 }
 CODE = {v: k for k, v in STATUS.items()}
 
@@ -110,6 +111,13 @@ class Eval(C.Structure):
                 ("fields", FieldEval * MAX_FIELDS)]
 
 
+class PcgStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_uint32), ("restarts", C.c_uint32), ("stop", C.c_int32),
+                ("initial_residual_squared", C.c_double), ("target_squared", C.c_double),
+                ("final_residual_squared", C.c_double), ("elapsed_ms", C.c_double),
+                ("kernel_launches", C.c_uint64)]
+
+
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_uint32), ("chunk_iterations", C.c_uint32),
                 ("admission_threads", C.c_uint32), ("reserved", C.c_uint32 * 5)]
@@ -187,6 +195,9 @@ SIGNATURES = {
     "texo_gp_server_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u32p, c_u64p]),
     "texo_gp_server_clock_ms": (C.c_double, [_P]),
     "texo_gp_selftest_waits": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "texo_gp_quadratic_solve": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint32),
+                                            C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(PcgStats)]),
 }
 
 _lib = None

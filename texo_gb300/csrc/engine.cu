@@ -1493,6 +1493,7 @@ const char* texo_gp_status_name(int32_t s) {
     case TEXO_GP_ERR_FIXED_POINT_RANGE: return "FIXED_POINT_RANGE";
     case TEXO_GP_ERR_UNSUPPORTED: return "UNSUPPORTED";
     case TEXO_GP_ERR_BUSY: return "BUSY";
+    case TEXO_GP_ERR_PCG_NOT_CONVERGED: return "PCG_NOT_CONVERGED";
     default: return "UNKNOWN";
   }
 }

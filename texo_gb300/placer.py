@@ -113,6 +113,37 @@ class Batch:
         return r.value, f.value, b.value
 
 
+PCG_STOP = ("residual", "breakdown", "dimension")
+
+
+def quadratic_solve(diagonal, adjacency_ptr, adjacency_index, adjacency_weight, rhs, solution=None,
+                    device=0, allow_nonconverged=False):
+    """`solve_quadratic` (lib.rs:4586-4752) through texo_gp_quadratic_solve:
+    Jacobi-preconditioned CG for (D - W) x = b on the GPU, W given as CSR rows
+    in the reference's adjacency order. Returns (x, stats dict)."""
+    lib = abi.load()
+    n = len(diagonal)
+    d = np.ascontiguousarray(diagonal, dtype=np.float64)
+    ptr = np.ascontiguousarray(adjacency_ptr, dtype=np.uint32)
+    idx = np.ascontiguousarray(adjacency_index, dtype=np.uint32)
+    w = np.ascontiguousarray(adjacency_weight, dtype=np.float64)
+    b = np.ascontiguousarray(rhs, dtype=np.float64)
+    x = np.zeros(n) if solution is None else np.array(solution, dtype=np.float64, copy=True)
+    if ptr.size != n + 1 or b.size != n or x.size != n:
+        raise ValueError("quadratic_solve: inconsistent sizes")
+    st = abi.PcgStats()
+    code = lib.texo_gp_quadratic_solve(device, n, abi.ptr(d, C.c_double), abi.ptr(ptr, C.c_uint32),
+                                       abi.ptr(idx, C.c_uint32), abi.ptr(w, C.c_double), abi.ptr(b, C.c_double),
+                                       abi.ptr(x, C.c_double), C.byref(st))
+    if not (allow_nonconverged and code == abi.CODE["PCG_NOT_CONVERGED"]):
+        abi.check(code, "texo_gp_quadratic_solve")
+    return x, dict(status=abi.STATUS.get(st.status, st.status), iterations=st.iterations, restarts=st.restarts,
+                   stop=PCG_STOP[st.stop] if 0 <= st.stop < 3 else st.stop,
+                   initial_residual_squared=st.initial_residual_squared, target_squared=st.target_squared,
+                   final_residual_squared=st.final_residual_squared, elapsed_ms=st.elapsed_ms,
+                   kernel_launches=st.kernel_launches)
+
+
 class Server:
     """The serving loop (texo_gp_server): submit requests at any time, poll
     finished jobs. Results are (job_id, targets [U,2] or None, info dict)."""
