@@ -489,6 +489,54 @@ def stage_report(workload, dct_name, reps):
             "stages": out}
 
 
+def seed_report(workload="lfe5u-85-42k", reps=5):
+    """The coarse quadratic seed's solve (`solve_quadratic`, lib.rs:4586-4752)
+    on the bound-to-bound system of `workload` at its initial positions (x
+    axis, fixed IO anchored, floating components gauged): the GPU solve
+    through texo_gp_quadratic_solve (device time with the copies, and wall
+    time of the call from host arrays) against the FP64 oracle restatement
+    on one host core (the reference's solve is sequential)."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import seed
+    from texo_gb300.placer import quadratic_solve
+    prob = make_problem(workload, 0)
+    pos = np.asarray(prob.initial_xy).reshape(-1, 2)
+    d, ptr, idx, w, rhs, anch = seed.axis_system(prob, pos, 0)
+    d, ptr, idx, w, rhs, floating = seed.finalize_gauges(d, ptr, idx, w, rhs, anch)
+    x0 = pos[:, 0].copy()
+    for comp in floating:
+        x0[comp] -= x0[comp[0]]
+    ptr32, idx32 = ptr.astype(np.uint32), idx.astype(np.uint32)
+    quadratic_solve(d, ptr32, idx32, w, rhs, x0)   # warm-up (module load, pool)
+    gpu_ms, wall_ms = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        xg, sg = quadratic_solve(d, ptr32, idx32, w, rhs, x0)
+        wall_ms.append(1000 * (time.perf_counter() - t0))
+        gpu_ms.append(sg["elapsed_ms"])
+    t0 = time.perf_counter()
+    xr, sr, ok = ffi.solve_quadratic(d, ptr32, idx32, w, rhs, x0)
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    nnz = int(ptr[-1])
+    # algorithmic bytes of one CG step: the product reads D, the row pointers,
+    # the adjacency (index + weight) and the direction, writes q; the updates
+    # read p, q, x, r, D and write x, r, z; the direction update reads z, p
+    # and writes p (FP64 vectors, int32 indices)
+    n = len(d)
+    step_bytes = (8 * n + 4 * (n + 1) + 12 * nnz + 8 * n + 8 * n) + (8 * 5 * n + 8 * 3 * n) + (8 * 3 * n)
+    best = min(gpu_ms)
+    return {"workload": workload, "axis": "x", "units": n, "adjacency_entries": nnz,
+            "floating_components": len(floating),
+            "gpu": {"iterations": sg["iterations"], "restarts": sg["restarts"], "stop": sg["stop"],
+                    "device_ms": best, "wall_ms": min(wall_ms),
+                    "relative_residual": float(np.sqrt(sg["final_residual_squared"] / sg["initial_residual_squared"])),
+                    "step_gbs": step_bytes * sg["iterations"] / (best * 1e-3) / 1e9},
+            "cpu_oracle": {"iterations": int(sr.iterations), "ms": cpu_ms, "cores": 1, "converged": bool(ok)},
+            "max_rel_diff_vs_oracle": float(np.max(np.abs(xg - xr)) / np.max(np.abs(xr))),
+            "speedup_wall_vs_cpu": cpu_ms / min(wall_ms)}
+
+
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
@@ -589,6 +637,8 @@ def main():
     ap.add_argument("--stage-report", action="store_true",
                     help="print only the per-stage kernel report of --workload at placed positions")
     ap.add_argument("--stage-reps", type=int, default=10)
+    ap.add_argument("--seed-only", action="store_true", help="print only the quadratic-seed solve report")
+    ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -617,6 +667,10 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "BF16x3 / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
+        return
+    if args.seed_only:
+        if rank == 0:
+            print(json.dumps({"metric": "quadratic seed solve", "seed": seed_report(args.workload)}), flush=True)
         return
     if args.stage_report:
         if rank == 0:
@@ -742,6 +796,8 @@ def main():
         line["serving"] = serve_report(args.serve_requests)
     if rank == 0 and not args.no_precision and not args.no_batch:
         line["precision"] = precision_report()
+    if rank == 0 and not args.no_seed and not args.no_batch:
+        line["quadratic_seed"] = seed_report(args.workload)
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)
