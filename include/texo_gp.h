@@ -460,6 +460,21 @@ int32_t texo_gp_quadratic_solve(int32_t device, uint32_t n, const double* diagon
                                 const double* adjacency_weight, const double* rhs, double* solution,
                                 texo_gp_pcg_stats* stats);
 
+/* ---- routability: continuous RUDY demand ----------------------------------
+ * Replaces `continuous_routing_demand` (crates/texo-pnr/src/eplace.rs:856-937):
+ * every net bounding box (boxes[i] = min_x, max_x, min_y, max_y, as
+ * `external_baseline_net_bounding_boxes` gives them, analytical_placement.rs:
+ * 238-276), widened by half a tile, adds dx / area to the horizontal and
+ * dy / area to the vertical demand of each tile of the width x height grid it
+ * overlaps, weighted by the overlap (area = (dx + 1)(dy + 1)). Outputs are
+ * [height][width] FP64. The demand accumulates in int64 2^-40 fixed point
+ * (deterministic; within 2^-41 per box and tile of the reference's FP64
+ * sums; at most 2^22 boxes, else TEXO_GP_ERR_FIXED_POINT_RANGE). A
+ * non-finite or unordered box returns TEXO_GP_ERR_INVALID_NORMALIZATION like
+ * the reference. `elapsed_ms` (may be NULL): device time with the copies. */
+int32_t texo_gp_routing_demand(int32_t device, uint32_t width, uint32_t height, uint64_t num_boxes,
+                               const double* boxes, double* horizontal, double* vertical, double* elapsed_ms);
+
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)
  * against partners that never arrive, with a short limit. Both must run out

@@ -74,6 +74,15 @@ def solve_quadratic(diagonal, ptr, index, weight, rhs, solution=None):
     return x, st, code == 0
 
 
+def routing_demand(width, height, boxes):
+    """continuous_routing_demand (eplace.rs:856-937) in FP64: (h, v, ok)."""
+    b = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1, 4)
+    h = np.zeros(width * height)
+    v = np.zeros(width * height)
+    code = lib().orc_routing_demand(width, height, b.shape[0], P(b), P(h), P(v))
+    return h.reshape(height, width), v.reshape(height, width), code == 0
+
+
 def multiply_quadratic(diagonal, ptr, index, weight, values):
     n = len(diagonal)
     out = np.zeros(n)
@@ -124,6 +133,7 @@ def lib():
             "orc_overflow_target": (C.c_double, [C.c_uint32]),
             "orc_checkpoint_better": (C.c_int32, [C.c_double, C.c_double, C.c_double, C.c_double]),
             "orc_validate_units": (C.c_int32, [c_u32p, C.c_uint64, c_u64p]),
+            "orc_routing_demand": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, c_f64p, c_f64p, c_f64p]),
             "orc_solve_quadratic": (C.c_int32, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p,
                                                 C.POINTER(PcgStats)]),
             "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),

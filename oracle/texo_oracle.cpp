@@ -1951,6 +1951,46 @@ int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t*
   return TEXO_GP_OK;
 }
 
+// ---- continuous RUDY demand (crates/texo-pnr/src/eplace.rs:856-937) -------
+int32_t orc_routing_demand(uint32_t width, uint32_t height, uint64_t num_boxes, const double* boxes,
+                           double* horizontal, double* vertical) {
+  const size_t tiles = (size_t)width * height;
+  for (size_t t = 0; t < tiles; ++t) horizontal[t] = vertical[t] = 0.0;
+  std::vector<std::pair<uint32_t, double>> xo, yo;
+  for (uint64_t i = 0; i < num_boxes; ++i) {
+    const double minx = boxes[4 * i], maxx = boxes[4 * i + 1], miny = boxes[4 * i + 2], maxy = boxes[4 * i + 3];
+    if (!(std::isfinite(minx) && std::isfinite(maxx) && std::isfinite(miny) && std::isfinite(maxy)) || minx > maxx ||
+        miny > maxy)
+      return 1;
+    const double dx = maxx - minx, dy = maxy - miny;
+    const double rminx = minx - 0.5, rmaxx = maxx + 0.5, rminy = miny - 0.5, rmaxy = maxy + 0.5;
+    const double area = (dx + 1.0) * (dy + 1.0);
+    if (!std::isfinite(area) || area <= 0.0) return 1;
+    const double hd = dx / area, vd = dy / area;
+    yo.clear();
+    for (uint32_t y = 0; y < height; ++y) {
+      const double o = std::max(std::min((double)y + 0.5, rmaxy) - std::max((double)y - 0.5, rminy), 0.0);
+      if (o > 0.0) yo.emplace_back(y, o);
+    }
+    xo.clear();
+    for (uint32_t x = 0; x < width; ++x) {
+      const double o = std::max(std::min((double)x + 0.5, rmaxx) - std::max((double)x - 0.5, rminx), 0.0);
+      if (o > 0.0) xo.emplace_back(x, o);
+    }
+    for (const auto& [y, oy] : yo)
+      for (const auto& [x, ox] : xo) {
+        const double overlap = ox * oy;
+        const size_t index = (size_t)y * width + x;
+        horizontal[index] += hd * overlap;
+        vertical[index] += vd * overlap;
+      }
+  }
+  for (size_t t = 0; t < tiles; ++t)
+    if (!(std::isfinite(horizontal[t]) && horizontal[t] >= 0.0 && std::isfinite(vertical[t]) && vertical[t] >= 0.0))
+      return 1;
+  return 0;
+}
+
 // ---- coarse quadratic seed (crates/texo-pnr/src/lib.rs:4586-4790) --------
 // multiply_quadratic (lib.rs:4767-4782): diagonal * v[i], then minus
 // weight * v[j] per adjacency entry, in order.

@@ -152,6 +152,11 @@ int32_t orc_checkpoint_better(double max_excess, double total_excess, double bes
                               double best_total);                       /* :106-119 */
 int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t* error_index);
 
+/* continuous_routing_demand (eplace.rs:856-937): returns 0, or 1 for a
+ * non-finite / unordered box (InvalidNormalization). */
+int32_t orc_routing_demand(uint32_t width, uint32_t height, uint64_t num_boxes, const double* boxes,
+                           double* horizontal, double* vertical);
+
 /* ---- coarse quadratic seed (crates/texo-pnr/src/lib.rs:4586-4790) -------- */
 typedef struct orc_pcg_stats {
   uint64_t iterations, restarts;

@@ -195,6 +195,8 @@ SIGNATURES = {
     "texo_gp_server_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u32p, c_u64p]),
     "texo_gp_server_clock_ms": (C.c_double, [_P]),
     "texo_gp_selftest_waits": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "texo_gp_routing_demand": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "texo_gp_quadratic_solve": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(PcgStats)]),

@@ -113,6 +113,43 @@ class Batch:
         return r.value, f.value, b.value
 
 
+def routing_demand(width, height, boxes, device=0):
+    """`continuous_routing_demand` (eplace.rs:856-937) through
+    texo_gp_routing_demand: (horizontal [H, W], vertical [H, W], device ms)."""
+    lib = abi.load()
+    b = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1, 4)
+    h = np.zeros(width * height)
+    v = np.zeros(width * height)
+    ms = C.c_double()
+    abi.check(lib.texo_gp_routing_demand(device, width, height, b.shape[0], abi.ptr(b, C.c_double),
+                                         abi.ptr(h, C.c_double), abi.ptr(v, C.c_double), C.byref(ms)),
+              "texo_gp_routing_demand")
+    return h.reshape(height, width), v.reshape(height, width), ms.value
+
+
+def net_bounding_boxes(problem, positions):
+    """`external_baseline_net_bounding_boxes` (analytical_placement.rs:238-276)
+    for unit origins `positions` [U, 2]: (min_x, max_x, min_y, max_y) of every
+    net not wholly inside one unit, fixed cells at their coordinates."""
+    net_ptr = np.asarray(problem.net_ptr, dtype=np.int64)
+    pin_cell = np.asarray(problem.pin_cell, dtype=np.int64)
+    cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
+    fixed = np.asarray(problem.cell_fixed, dtype=bool)
+    fixed_xy = np.asarray(problem.cell_fixed_xy, dtype=np.float64).reshape(-1, 2)
+    off = np.asarray(problem.cell_offset_xy, dtype=np.float64).reshape(-1, 2)
+    pos = np.asarray(positions, dtype=np.float64).reshape(-1, 2)
+    cxy = np.where(fixed[:, None], fixed_xy, pos[cell_unit] + off)
+    pin_xy = cxy[pin_cell]
+    pin_unit = cell_unit[pin_cell]
+    starts = net_ptr[:-1]
+    lo = np.minimum.reduceat(pin_xy, starts, axis=0)
+    hi = np.maximum.reduceat(pin_xy, starts, axis=0)
+    umin = np.minimum.reduceat(pin_unit, starts)
+    umax = np.maximum.reduceat(pin_unit, starts)
+    keep = umin != umax
+    return np.stack([lo[:, 0], hi[:, 0], lo[:, 1], hi[:, 1]], axis=1)[keep]
+
+
 PCG_STOP = ("residual", "breakdown", "dimension")
 
 
