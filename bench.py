@@ -537,6 +537,57 @@ def seed_report(workload="lfe5u-85-42k", reps=5):
             "speedup_wall_vs_cpu": cpu_ms / min(wall_ms)}
 
 
+def rudy_report(reps=5):
+    """Continuous RUDY demand (`continuous_routing_demand`, eplace.rs:856-937)
+    of the 42k workload's net boxes at its placed positions (one device-engine
+    placement), on the GPU against the FP64 oracle on one host core (the
+    reference's loop is sequential); and of the 1M-cell workload's boxes at
+    uniform positions on the GPU, checked against the oracle on a 20,000-box
+    sample."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer, net_bounding_boxes, routing_demand
+    out = {}
+    prob = make_problem("lfe5u-85-42k", 0)
+    with Placer(prob, make_params("lfe5u-85-42k", abi.ENGINE_DEVICE, abi.DCT_FP32)) as g:
+        _, coords, _ = g.run(allow_nonconverged=True)
+    side = WORKLOADS["lfe5u-85-42k"][0]
+    boxes = net_bounding_boxes(prob, coords[: 2 * prob.num_units].reshape(-1, 2))
+    routing_demand(side, side, boxes)   # warm-up
+    ms = []
+    for _ in range(reps):
+        h, v, m = routing_demand(side, side, boxes)
+        ms.append(m)
+    t0 = time.perf_counter()
+    hr, vr, ok = ffi.routing_demand(side, side, boxes)
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    out["lfe5u-85-42k"] = {"grid": "%dx%d" % (side, side), "boxes": int(len(boxes)), "positions": "placed",
+                           "gpu_ms": min(ms), "cpu_oracle_ms": cpu_ms, "cores": 1,
+                           "speedup": cpu_ms / min(ms),
+                           "max_abs_diff": float(max(np.max(np.abs(h - hr)), np.max(np.abs(v - vr)))),
+                           "max_demand": float(max(hr.max(), vr.max()))}
+    prob = make_problem("stress-1m", 0)
+    side = WORKLOADS["stress-1m"][0]
+    pos = np.random.default_rng(0).uniform(0, side - 1, size=(prob.num_units, 2))
+    boxes = net_bounding_boxes(prob, pos)
+    routing_demand(side, side, boxes)
+    ms = []
+    for _ in range(reps):
+        h, v, m = routing_demand(side, side, boxes)
+        ms.append(m)
+    sample = boxes[:20000]
+    hs, vs, _ = routing_demand(side, side, sample)
+    t0 = time.perf_counter()
+    hr, vr, ok = ffi.routing_demand(side, side, sample)
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    out["stress-1m"] = {"grid": "%dx%d" % (side, side), "boxes": int(len(boxes)), "positions": "uniform",
+                        "gpu_ms": min(ms), "oracle_sample_boxes": len(sample),
+                        "oracle_sample_ms": cpu_ms,
+                        "sample_max_abs_diff": float(max(np.max(np.abs(hs - hr)), np.max(np.abs(vs - vr))))}
+    return out
+
+
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
@@ -639,6 +690,7 @@ def main():
     ap.add_argument("--stage-reps", type=int, default=10)
     ap.add_argument("--seed-only", action="store_true", help="print only the quadratic-seed solve report")
     ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
+    ap.add_argument("--rudy-only", action="store_true", help="print only the RUDY demand report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -667,6 +719,10 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "BF16x3 / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
+        return
+    if args.rudy_only:
+        if rank == 0:
+            print(json.dumps({"metric": "continuous RUDY demand", "rudy": rudy_report()}), flush=True)
         return
     if args.seed_only:
         if rank == 0:
@@ -798,6 +854,7 @@ def main():
         line["precision"] = precision_report()
     if rank == 0 and not args.no_seed and not args.no_batch:
         line["quadratic_seed"] = seed_report(args.workload)
+        line["rudy"] = rudy_report()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)
