@@ -16,9 +16,17 @@ value is all iterations over the max rank time.
 
 `--impl reference` times the CPU restatement of the reference path (the
 oracle port; the Rust reference cannot be built here) on the host cores.
+
+Besides the headline, the JSON line carries: `e2e` (the placement through
+texo_gp_place from host buffers), `roofline` (with per-stage rooflines and
+the persistent kernel's phase clocks), `cpu_baseline`, `batched` (64 mixed
+instances), `serving` (Poisson request stream), `precision` (1M cells, three
+DCT forms against FP64), `quadratic_seed` (the coarse seed's PCG solve) and
+`rudy` (the continuous routing-demand map). `--stage-report`,
+`--batch-only`, `--serve-only`, `--precision-only`, `--seed-only` and
+`--rudy-only` print one of these alone.
 """
 import argparse
-import ctypes as C
 import json
 import os
 import statistics

@@ -13,7 +13,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 
 import make_golden as G  # noqa: E402
-from texo_gb300 import abi  # noqa: E402
 from texo_gb300.placer import Placer, default_params  # noqa: E402
 
 pytestmark = pytest.mark.gpu
