@@ -96,6 +96,130 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     if (p->member_field[i] >= p->num_fields) return TEXO_GP_ERR_INVALID_ARGUMENT;
     member_count[p->member_field[i]]++;
   }
+  // hypergraph: pins and nets (AnalyticalHypergraph::new, analytical_placement.rs:116-168).
+  // It is validated and its pin layout started first, on a second thread
+  // beside the density sections below; its errors are reported after
+  // theirs, in the reference's order.
+  const uint32_t C = p->num_cells, E = p->num_nets;
+  int32_t hyper_status = TEXO_GP_OK;
+  uint64_t hyper_err = 0;
+  auto hyper_check = [&]() -> int32_t {
+    if (E && (!p->net_ptr || !p->pin_cell)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    for (uint32_t c = 0; c < C; ++c)
+      if (p->cell_unit[c] >= U) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    for (uint32_t i = 0; i < M; ++i)
+      if (p->member_cell && p->member_cell[i] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    // nets and timed arcs: the two passes over them read only checked indices
+    for (uint32_t e = 0; e < E; ++e) {
+      const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
+      if (en < b + 2) {
+        hyper_err = e;
+        return TEXO_GP_ERR_INVALID_ARGUMENT;
+      }
+      for (uint32_t k = b; k < en; ++k)
+        if (p->pin_cell[k] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+    }
+    for (uint32_t a = 0; a < p->num_timed_arcs; ++a) {
+      if (p->arc_driver_cell[a] >= C || p->arc_sink_cell[a] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+      if (u64_to_f64(p->arc_extra_weight[a]) > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
+    }
+    return TEXO_GP_OK;
+  };
+  hyper_status = hyper_check();
+  const size_t arcs = p->num_timed_arcs;
+  auto pin_of = [&](uint32_t cell, int& unit, double& bx, double& by) {
+    if (p->cell_fixed[cell]) {
+      unit = -1;
+      bx = p->cell_fixed_xy[2 * (size_t)cell];
+      by = p->cell_fixed_xy[2 * (size_t)cell + 1];
+    } else {
+      unit = (int)p->cell_unit[cell];
+      bx = p->cell_offset_xy[2 * (size_t)cell];
+      by = p->cell_offset_xy[2 * (size_t)cell + 1];
+    }
+  };
+
+  // Pin layout (second thread): degree classes 2 | 3-4 | 5-8 | 9-16 | 17-32
+  // | 33+ laid out class by class (a counting sort over the classes, nets of
+  // a class in input order), then the timed arcs as 2-pin nets; every output
+  // is sized once and filled by index. pin_count[u] = pins of unit u. The
+  // WA kernel gives a net of class c groups[c] lanes, so that a lane holds
+  // at most four pins of a net up to 32 pins (33+: one warp per net).
+  constexpr int kNetClasses = 6;
+  static const int groups[kNetClasses] = {1, 1, 2, 4, 8, 32};
+  auto cls = [](uint32_t deg) {
+    return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : deg <= 32 ? 4 : 5;
+  };
+  const size_t pins = (E && !hyper_status) ? p->net_ptr[E] : 0;
+  std::vector<double> pin_count(U, 0.0);
+  bool layout_ok = true;
+  auto layout = [&]() {
+    try {
+      size_t nets_in[kNetClasses] = {0, 0, 0, 0, 0, 0}, pins_in[kNetClasses] = {0, 0, 0, 0, 0, 0};
+      for (uint32_t e = 0; e < E; ++e) {
+        const uint32_t deg = p->net_ptr[e + 1] - p->net_ptr[e];
+        nets_in[cls(deg)]++;
+        pins_in[cls(deg)] += deg;
+      }
+      size_t net_at[kNetClasses], pin_at[kNetClasses];
+      for (int c = 0, n0 = 0, p0 = 0; c < kNetClasses; ++c) {
+        net_at[c] = n0;
+        pin_at[c] = p0;
+        m.class_begin[c] = n0;
+        m.class_group[c] = groups[c];
+        n0 += (int)nets_in[c];
+        p0 += (int)pins_in[c];
+      }
+      m.net_ptr.resize((size_t)E + arcs + 1);
+      m.net_w.assign((size_t)E + arcs, 1.0f);
+      m.pin_unit.resize(pins + 2 * arcs);
+      m.pin_base.resize(2 * (pins + 2 * arcs));
+      m.net_ptr[0] = 0;
+      for (uint32_t e = 0; e < E; ++e) {
+        const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
+        const int c = cls(en - b);
+        const size_t slot = net_at[c]++;
+        size_t q = pin_at[c];
+        for (uint32_t k = b; k < en; ++k, ++q) {
+          int unit;
+          pin_of(p->pin_cell[k], unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
+          m.pin_unit[q] = unit;
+          if (unit >= 0) pin_count[unit] += 1.0;
+        }
+        pin_at[c] = q;
+        m.net_ptr[slot + 1] = (int)q;
+      }
+      m.n_hpwl_nets = (int)E;
+      m.class_begin[kNetClasses] = (int)E;   // timed arcs: 2-pin nets, one lane each
+      m.class_group[kNetClasses] = 1;
+      for (uint32_t a = 0; a < arcs; ++a) {
+        size_t q = pins + 2 * (size_t)a;
+        for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
+          int unit;
+          pin_of(cell, unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
+          m.pin_unit[q] = unit;
+          ++q;
+        }
+        m.net_ptr[(size_t)E + a + 1] = (int)q;
+        m.net_w[(size_t)E + a] = (float)u64_to_f64(p->arc_extra_weight[a]);
+      }
+    } catch (...) {
+      layout_ok = false;
+    }
+  };
+  // buffers of this thread's pass over the nets (further below)
+  std::vector<double> wl(U, 0.0), inc(C, 0.0), pin_weight_sum(U, 0.0);
+  std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
+  // small problems are not worth a thread; the guard joins the thread on
+  // every way out of this function, an early error return included
+  struct Joiner {
+    std::thread t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } layout_thread;
+  const bool threaded = !hyper_status && pins >= 65536;
+  if (threaded) layout_thread.t = std::thread(layout);
   // capacity minus fixed occupancy (electrostatic_placement.rs:146-172)
   std::vector<std::vector<uint32_t>> caps(p->num_fields);
   for (uint32_t f = 0; f < p->num_fields; ++f)
@@ -246,118 +370,12 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     m.hi[i + 1] = (double)(m.H - 1);
   }
   for (size_t i = 0; i < 2 * nobj; ++i) m.init[i] = clampd(m.init[i], m.lo[i], m.hi[i]);
-  // hypergraph: pins and nets (AnalyticalHypergraph::new, analytical_placement.rs:116-168)
-  const uint32_t C = p->num_cells, E = p->num_nets;
-  if (E && (!p->net_ptr || !p->pin_cell)) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  for (uint32_t c = 0; c < C; ++c)
-    if (p->cell_unit[c] >= U) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  for (uint32_t i = 0; i < M; ++i)
-    if (p->member_cell && p->member_cell[i] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  auto pin_of = [&](uint32_t cell, int& unit, double& bx, double& by) {
-    if (p->cell_fixed[cell]) {
-      unit = -1;
-      bx = p->cell_fixed_xy[2 * (size_t)cell];
-      by = p->cell_fixed_xy[2 * (size_t)cell + 1];
-    } else {
-      unit = (int)p->cell_unit[cell];
-      bx = p->cell_offset_xy[2 * (size_t)cell];
-      by = p->cell_offset_xy[2 * (size_t)cell + 1];
-    }
-  };
-  // nets and timed arcs are validated first: the two passes below then run
-  // side by side on two threads and read only checked indices
-  for (uint32_t e = 0; e < E; ++e) {
-    const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
-    if (en < b + 2) {
-      *err = e;
-      return TEXO_GP_ERR_INVALID_ARGUMENT;
-    }
-    for (uint32_t k = b; k < en; ++k)
-      if (p->pin_cell[k] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  // hypergraph (validated and laid out above): report its errors here, in
+  // the reference's order
+  if (hyper_status) {
+    *err = hyper_err;
+    return hyper_status;
   }
-  const size_t arcs = p->num_timed_arcs;
-  for (uint32_t a = 0; a < arcs; ++a) {
-    if (p->arc_driver_cell[a] >= C || p->arc_sink_cell[a] >= C) return TEXO_GP_ERR_INVALID_ARGUMENT;
-    if (u64_to_f64(p->arc_extra_weight[a]) > 16777216.0) return TEXO_GP_ERR_FIXED_POINT_RANGE;
-  }
-
-  // Pin layout (second thread): degree classes 2 | 3-4 | 5-8 | 9-16 | 17-32
-  // | 33+ laid out class by class (a counting sort over the classes, nets of
-  // a class in input order), then the timed arcs as 2-pin nets; every output
-  // is sized once and filled by index. pin_count[u] = pins of unit u. The
-  // WA kernel gives a net of class c groups[c] lanes, so that a lane holds
-  // at most four pins of a net up to 32 pins (33+: one warp per net).
-  constexpr int kNetClasses = 6;
-  static const int groups[kNetClasses] = {1, 1, 2, 4, 8, 32};
-  auto cls = [](uint32_t deg) {
-    return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : deg <= 32 ? 4 : 5;
-  };
-  const size_t pins = E ? p->net_ptr[E] : 0;
-  std::vector<double> pin_count(U, 0.0);
-  bool layout_ok = true;
-  auto layout = [&]() {
-    try {
-      size_t nets_in[kNetClasses] = {0, 0, 0, 0, 0, 0}, pins_in[kNetClasses] = {0, 0, 0, 0, 0, 0};
-      for (uint32_t e = 0; e < E; ++e) {
-        const uint32_t deg = p->net_ptr[e + 1] - p->net_ptr[e];
-        nets_in[cls(deg)]++;
-        pins_in[cls(deg)] += deg;
-      }
-      size_t net_at[kNetClasses], pin_at[kNetClasses];
-      for (int c = 0, n0 = 0, p0 = 0; c < kNetClasses; ++c) {
-        net_at[c] = n0;
-        pin_at[c] = p0;
-        m.class_begin[c] = n0;
-        m.class_group[c] = groups[c];
-        n0 += (int)nets_in[c];
-        p0 += (int)pins_in[c];
-      }
-      m.net_ptr.resize((size_t)E + arcs + 1);
-      m.net_w.assign((size_t)E + arcs, 1.0f);
-      m.pin_unit.resize(pins + 2 * arcs);
-      m.pin_base.resize(2 * (pins + 2 * arcs));
-      m.net_ptr[0] = 0;
-      for (uint32_t e = 0; e < E; ++e) {
-        const uint32_t b = p->net_ptr[e], en = p->net_ptr[e + 1];
-        const int c = cls(en - b);
-        const size_t slot = net_at[c]++;
-        size_t q = pin_at[c];
-        for (uint32_t k = b; k < en; ++k, ++q) {
-          int unit;
-          pin_of(p->pin_cell[k], unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
-          m.pin_unit[q] = unit;
-          if (unit >= 0) pin_count[unit] += 1.0;
-        }
-        pin_at[c] = q;
-        m.net_ptr[slot + 1] = (int)q;
-      }
-      m.n_hpwl_nets = (int)E;
-      m.class_begin[kNetClasses] = (int)E;   // timed arcs: 2-pin nets, one lane each
-      m.class_group[kNetClasses] = 1;
-      for (uint32_t a = 0; a < arcs; ++a) {
-        size_t q = pins + 2 * (size_t)a;
-        for (uint32_t cell : {p->arc_driver_cell[a], p->arc_sink_cell[a]}) {
-          int unit;
-          pin_of(cell, unit, m.pin_base[2 * q], m.pin_base[2 * q + 1]);
-          m.pin_unit[q] = unit;
-          ++q;
-        }
-        m.net_ptr[(size_t)E + a + 1] = (int)q;
-        m.net_w[(size_t)E + a] = (float)u64_to_f64(p->arc_extra_weight[a]);
-      }
-    } catch (...) {
-      layout_ok = false;
-    }
-  };
-  // this thread's buffers exist before the second thread starts, so nothing
-  // below can throw while it runs
-  std::vector<double> wl(U, 0.0), inc(C, 0.0), pin_weight_sum(U, 0.0);
-  std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
-  // small problems are not worth a thread
-  std::thread layout_thread;
-  const bool threaded = pins >= 65536;
-  if (threaded) layout_thread = std::thread(layout);
-  else layout();
 
   // wirelength preconditioner and cell incidence (this thread): each
   // distinct unit (cell) of a net counts once, found with a per-net stamp
@@ -399,7 +417,8 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     pin_weight_sum[du] += w;
     pin_weight_sum[su] += w;
   }
-  if (threaded) layout_thread.join();
+  if (threaded) layout_thread.t.join();
+  else layout();
   if (!layout_ok) return TEXO_GP_ERR_INVALID_ARGUMENT;
   for (uint32_t u = 0; u < U; ++u) pin_weight_sum[u] += pin_count[u];
   m.n_classes = kNetClasses + 1;

@@ -277,12 +277,11 @@ extern "C" int32_t texo_gp_quadratic_solve(int32_t device, uint32_t n, const dou
       return fail(TEXO_GP_ERR_INVALID_ARGUMENT, "adjacency index out of range or non-finite weight");
 
   if (cudaSetDevice(device) != cudaSuccess) return fail(TEXO_GP_ERR_CUDA, "cudaSetDevice failed");
-  static int per_sm = -1;
-  if (per_sm < 0) {
+  static const int per_sm = [] {   // thread-safe one-time initialisation
     int b = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pcg, kThreads, 0) != cudaSuccess) b = 0;
-    per_sm = b;
-  }
+    return b;
+  }();
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (per_sm <= 0 || sms <= 0) return fail(TEXO_GP_ERR_CUDA, "k_pcg cannot be resident");
