@@ -1,7 +1,9 @@
-"""The FFT-based DCT form (default FP32 form on power-of-two grids) against
-the FP64 oracle: potential normwise <= 1e-5 up to 256 x 256 (<= 2e-5 at
-1024 x 1024, measured 5.3e-6), field gradient <= 1e-5 on identical
-positions, and the same bounds for the compensated GEMM form it replaces."""
+"""The FFT-based DCT form (the default FP32 form on power-of-two grids up to
+1024, double-float butterflies) against the FP64 oracle: potential normwise
+<= 1e-6 at every size (the transforms are exact to FP32; what remains is the
+FP32 storage between passes), energy <= 1e-6 relative, field gradient <=
+1e-5 on identical positions; the compensated GEMM form meets the 1e-5 bounds
+too. Results repeat bit for bit."""
 import ctypes as C
 
 import numpy as np
@@ -25,8 +27,8 @@ def form(g):
     return f.value
 
 
-@pytest.mark.parametrize("W,H,tol", [(64, 64, 1e-5), (256, 256, 1e-5), (256, 64, 1e-5), (32, 128, 1e-5),
-                                     (1024, 1024, 2e-5)])
+@pytest.mark.parametrize("W,H,tol", [(64, 64, 1e-6), (256, 256, 1e-6), (256, 64, 1e-6), (32, 128, 1e-6),
+                                     (1024, 1024, 1e-6)])
 def test_fft_poisson_matches_fp64(W, H, tol):
     prob = P.synthetic(48, 2000, 96, 2400, 6.0, 0)
     i = np.arange(W * H)
@@ -37,7 +39,7 @@ def test_fft_poisson_matches_fp64(W, H, tol):
         pot, e = g.poisson(d)
         pot2, _ = g.poisson(d)
     assert normwise(pot, ref) <= tol
-    assert abs(e - er) <= 1e-5 * abs(er)
+    assert abs(e - er) <= 1e-6 * abs(er)
     assert np.array_equal(pot, pot2)
 
 

@@ -89,10 +89,10 @@ struct Dev {
   // FFT form (power-of-two grids): twiddle tables per axis (dct_fft.cuh)
   int fft;                   // 1: the DCT passes run as FFT-based transforms
   int logW, logH;
-  const float2 *fx_tw, *fx_post, *fx_pre;
-  const float* fx_inv_s;
-  const float2 *fy_tw, *fy_post, *fy_pre;
-  const float* fy_inv_s;
+  const float4 *fx_tw, *fx_post, *fx_pre;   // FFT tables as double-float pairs
+  const float2* fx_inv_s;
+  const float4 *fy_tw, *fy_post, *fy_pre;
+  const float2* fy_inv_s;
   int Hp128, Hp32, Wp64, Wp32;   // padded extents
   uint16_t *rho_t, *t1_t, *t2_t, *t3_t;
   const uint16_t *CxB_t, *CyA_t, *CyTA_t, *CxTB_t;

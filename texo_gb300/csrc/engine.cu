@@ -160,10 +160,20 @@ cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
 // Twiddle tables of the FFT form for one power-of-two length n (FP64 values
 // rounded to FP32): tw[n/2] = exp(-2 pi i j / n), post[n] = s_k exp(-i pi k /
 // 2n), pre[n] = exp(-i pi k / 2n), inv_s[n] = 1 / s_k.
+// FFT tables of one length as double-float pairs: an FP64 value x becomes
+// hi = (float)x, lo = (float)(x - hi), so hi + lo carries about 48 bits.
 struct FftTables {
-  float2 *tw = nullptr, *post = nullptr, *pre = nullptr;
-  float* inv_s = nullptr;
+  float4 *tw = nullptr, *post = nullptr, *pre = nullptr;   // (re.hi, im.hi, re.lo, im.lo)
+  float2* inv_s = nullptr;                                  // (hi, lo)
 };
+static float2 split_df(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
+}
+static float4 split_cdf(double re, double im) {
+  const float2 r = split_df(re), i = split_df(im);
+  return make_float4(r.x, i.x, r.y, i.y);
+}
 cudaError_t shared_fft(int device, uint32_t n, FftTables* out) {
   static std::mutex mu;
   static std::map<std::pair<int, uint32_t>, FftTables> cache;
@@ -171,16 +181,15 @@ cudaError_t shared_fft(int device, uint32_t n, FftTables* out) {
   auto it = cache.find({device, n});
   if (it == cache.end()) {
     const double pi = 3.14159265358979323846, nf = (double)n;
-    std::vector<float2> tw(n / 2), post(n), pre(n);
-    std::vector<float> inv_s(n);
-    for (uint32_t j = 0; j < n / 2; ++j)
-      tw[j] = make_float2((float)std::cos(-2.0 * pi * j / nf), (float)std::sin(-2.0 * pi * j / nf));
+    std::vector<float4> tw(n / 2), post(n), pre(n);
+    std::vector<float2> inv_s(n);
+    for (uint32_t j = 0; j < n / 2; ++j) tw[j] = split_cdf(std::cos(-2.0 * pi * j / nf), std::sin(-2.0 * pi * j / nf));
     for (uint32_t k = 0; k < n; ++k) {
       const double sk = k == 0 ? std::sqrt(1.0 / nf) : std::sqrt(2.0 / nf);
       const double c = std::cos(-pi * k / (2.0 * nf)), sn = std::sin(-pi * k / (2.0 * nf));
-      post[k] = make_float2((float)(sk * c), (float)(sk * sn));
-      pre[k] = make_float2((float)c, (float)sn);
-      inv_s[k] = (float)(1.0 / sk);
+      post[k] = split_cdf(sk * c, sk * sn);
+      pre[k] = split_cdf(c, sn);
+      inv_s[k] = split_df(1.0 / sk);
     }
     FftTables t;
     cudaError_t e = cudaSuccess;
@@ -200,7 +209,8 @@ cudaError_t shared_fft(int device, uint32_t n, FftTables* out) {
   *out = it->second;
   return cudaSuccess;
 }
-bool fft_length(uint32_t n) { return n >= 2 && n <= 2048 && (n & (n - 1)) == 0; }
+// lengths the FFT form takes: powers of two whose group data fits its buffer
+bool fft_length(uint32_t n) { return n >= 2 && n <= 1024 && (n & (n - 1)) == 0; }
 int ilog2(uint32_t n) {
   int l = 0;
   while ((1u << l) < n) ++l;
@@ -466,8 +476,10 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&D.phys, K * B);
   S.zeroed(&D.fill, K * B);
   S.zeroed(&D.rho, K * B);
-  S.zeroed(&D.t1, K * B);
-  S.zeroed(&D.t2, K * B);
+  // t1 / t2: FP32 grids of the GEMM forms; the FFT form keeps them as
+  // double-float pairs (float2 per bin), hence twice the size
+  S.zeroed(&D.t1, 2 * K * B);
+  S.zeroed(&D.t2, 2 * K * B);
   S.zeroed(&D.phi, K * B);
   S.zeroed(&D.wa_fix, 2 * (size_t)h.U);
   S.zeroed(&D.graw, std::max<size_t>(K, 1) * nobj);

@@ -610,7 +610,7 @@ using SmemL = GemmSmem<64, 64, 16, 4, 4>;
 union alignas(16) GemmShared {
   Smem16 s;
   SmemL l;
-  float2 fft[2048];   // work buffer of the FFT form (fft::Smem)
+  float4 fft[2048];   // work buffer of the FFT form (fft::Smem: double-float complex)
 };
 
 template <bool LARGE>
