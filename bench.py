@@ -88,8 +88,9 @@ def stage_bytes(stage, n):
     nobj = U + F
     grids = 2 if F else 1                     # phys, and fill when there are fillers
     if n.get("dct_form") == 3 and stage.startswith("dct_"):
-        return {"dct_rows_fwd": K * B * 4 * 2, "dct_cols": K * B * 4 * 2 + B * 4,
-                "dct_rows_inv": K * B * 4 * 3}.get(stage, 0)
+        # the FFT form keeps t1 / t2 as double-float pairs (8 B a bin)
+        return {"dct_rows_fwd": K * B * (4 + 8), "dct_cols": K * B * (8 + 8) + B * 4,
+                "dct_rows_inv": K * B * (8 + 4 + 4)}.get(stage, 0)
     return {
         "init": K * B * (8 + 8 + 8) + U * 16,                            # phys, fill := -capfix, 0; WA grads := 0
         "scatter": M * 20 + U * 8 + F * 16 + K * B * 16 * grids,         # members, positions, grid RMW
@@ -681,7 +682,9 @@ def main():
     ap.add_argument("--workload", default="lfe5u-85-42k", choices=sorted(WORKLOADS))
     ap.add_argument("--engine", default="device", choices=["host", "device"])
     ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3", "fp32-gemm"])
-    ap.add_argument("--reference-sample", type=int, default=3)
+    ap.add_argument("--reference-sample", type=int, default=30,
+                    help="GP iterations per reference step (each step places from the start, so a short "
+                         "prefix would mostly time the model build and the two initial evaluations)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile", action="store_true",
