@@ -227,3 +227,21 @@ def test_place_entry_matches_a_handle_run():
     assert c1 is None and c2.ndim == 1 and c2.size >= 2 * prob.num_units
     assert np.array_equal(t1, t2)
     assert s1["iterations"] == s2["iterations"] and s1["hpwl"] == s2["hpwl"]
+
+
+def test_device_engine_on_a_1024_bin_grid_repeats_and_tracks_the_host_engine():
+    """The persistent kernel's FFT passes at 1024 points (one vector per
+    group, 1024-slot data): two device runs agree bit for bit, and after 10
+    iterations the device and host engines (different reduction orders) agree
+    on HPWL and overflow to 1e-3."""
+    prob = P.synthetic(110, 10000, 96, 12000, 6.0, 2)
+    kw = dict(bins_x=1024, bins_y=1024, best_effort=1, max_iterations=400, target_density=0.9, gamma_base=4.0)
+    with Placer(prob, params(engine=abi.ENGINE_DEVICE, **kw)) as g:
+        t1, c1, s1 = g.run(10)
+        g.reset()
+        t2, c2, s2 = g.run(10)
+    assert np.array_equal(c1, c2) and s1["iterations"] == 10
+    with Placer(prob, params(engine=abi.ENGINE_HOST, **kw)) as h:
+        _, ch, sh = h.run(10)
+    assert abs(s1["hpwl"] - sh["hpwl"]) <= 1e-3 * sh["hpwl"]
+    assert abs(s1["overflow"][0] - sh["overflow"][0]) <= 1e-3
