@@ -22,9 +22,10 @@ texo_gp_place from host buffers), `roofline` (with per-stage rooflines and
 the persistent kernel's phase clocks), `cpu_baseline`, `batched` (64 mixed
 instances), `serving` (Poisson request stream), `precision` (1M cells, three
 DCT forms against FP64), `quadratic_seed` (the coarse seed's PCG solve) and
-`rudy` (the continuous routing-demand map). `--stage-report`,
-`--batch-only`, `--serve-only`, `--precision-only`, `--seed-only` and
-`--rudy-only` print one of these alone.
+`rudy` (the continuous routing-demand map) and `auction` (the legalizer's
+single-BEL auction on the placement's targets). `--stage-report`,
+`--batch-only`, `--serve-only`, `--precision-only`, `--seed-only`,
+`--rudy-only` and `--auction-only` print one of these alone.
 """
 import argparse
 import json
@@ -597,6 +598,51 @@ def rudy_report(reps=5):
     return out
 
 
+def auction_report(reps=5):
+    """The single-BEL capacity auction of the legalizer (`assign_implicitly`,
+    legalization/auction.rs:131-247, with the ring walk of mod.rs:876-1021)
+    on the rounded targets of the 42k-cell placement (device engine): the
+    GPU's Jacobi auction (device time with the copies, best of `reps`)
+    against the oracle's one-bidder-at-a-time auction on one host core, with
+    the epsilon-optimality certificate of the GPU result."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import abi, legalize
+    from texo_gb300.placer import Placer
+    prob = make_problem("lfe5u-85-42k", 0)
+    with Placer(prob, make_params("lfe5u-85-42k", abi.ENGINE_DEVICE, abi.DCT_FP32)) as g:
+        targets, _, _ = g.run(allow_nonconverged=True)
+    lo = prob.lower_xy.reshape(-1, 2)
+    hi = prob.upper_xy.reshape(-1, 2)
+    movable = np.nonzero(np.any(lo != hi, axis=1))[0]
+    grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
+    kind = np.zeros(len(movable), np.uint32)
+    xy = np.ascontiguousarray(targets[movable])
+    legalize.auction_singletons(grid, kind, xy)   # warm-up
+    runs, walls = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        runs.append(legalize.auction_singletons(grid, kind, xy))
+        walls.append(1000 * (time.perf_counter() - t0))
+    best = min(runs, key=lambda r: r.stats["elapsed_ms"])
+    same = all(np.array_equal(r.assignment, best.assignment) for r in runs)
+    t0 = time.perf_counter()
+    code, _, _, ost = ffi.auction_singletons(grid, kind, xy)
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices)
+    n = len(movable)
+    st = best.stats
+    return {"workload": "lfe5u-85-42k", "bidders": int(n), "bels": int(grid.num_objects),
+            "grid": "%dx%d" % (prob.width, prob.height), "targets": "rounded targets of the device-engine placement",
+            "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls), "rounds": st["rounds"], "bids": st["bids"],
+            "candidates_examined": st["candidates_examined"], "unmatched": st["unmatched"],
+            "total_displacement": st["total_base_cost"], "mean_displacement": st["total_base_cost"] / max(n, 1),
+            "deterministic_over_reps": bool(same), "certificate_violations": int(bad),
+            "cpu_oracle_ms": cpu_ms, "cpu_oracle_status": int(code), "cpu_oracle_bids": ost["bids"],
+            "cpu_oracle_unmatched": ost["unmatched"], "cpu_oracle_displacement": ost["total_base_cost"],
+            "cores": 1, "speedup": cpu_ms / st["elapsed_ms"] if st["elapsed_ms"] > 0 else None}
+
+
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
@@ -702,6 +748,7 @@ def main():
     ap.add_argument("--seed-only", action="store_true", help="print only the quadratic-seed solve report")
     ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
     ap.add_argument("--rudy-only", action="store_true", help="print only the RUDY demand report")
+    ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -734,6 +781,10 @@ def main():
     if args.rudy_only:
         if rank == 0:
             print(json.dumps({"metric": "continuous RUDY demand", "rudy": rudy_report()}), flush=True)
+        return
+    if args.auction_only:
+        if rank == 0:
+            print(json.dumps({"metric": "singleton BEL auction", "auction": auction_report()}), flush=True)
         return
     if args.seed_only:
         if rank == 0:
@@ -866,6 +917,7 @@ def main():
     if rank == 0 and not args.no_seed and not args.no_batch:
         line["quadratic_seed"] = seed_report(args.workload)
         line["rudy"] = rudy_report()
+        line["auction"] = auction_report()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)

@@ -87,7 +87,12 @@ typedef enum texo_gp_status {
   TEXO_GP_ERR_BUSY = 102,
   /* PnrError::InvalidPlacement of the coarse quadratic seed: "analytical PCG
    * {breakdown|dimension} after i/n iterations" (crates/texo-pnr/src/lib.rs:4702-4752) */
-  TEXO_GP_ERR_PCG_NOT_CONVERGED = 110
+  TEXO_GP_ERR_PCG_NOT_CONVERGED = 110,
+  /* AuctionError (crates/texo-pnr/src/legalization/auction.rs:46-54) */
+  TEXO_GP_ERR_AUCTION_RANGE = 111,            /* ArithmeticOverflow: the price range does not fit */
+  TEXO_GP_ERR_AUCTION_OBJECT_RANGE = 112,     /* ObjectOutOfRange */
+  TEXO_GP_ERR_AUCTION_COST_RANGE = 113,       /* BaseCostOutOfRange */
+  TEXO_GP_ERR_AUCTION_DUPLICATE_OBJECT = 114  /* DuplicateBestObject: an object twice in one domain */
 } texo_gp_status;
 
 /* Resource kinds in the reference's `ResourceKind` order
@@ -474,6 +479,67 @@ int32_t texo_gp_quadratic_solve(int32_t device, uint32_t n, const double* diagon
  * the reference. `elapsed_ms` (may be NULL): device time with the copies. */
 int32_t texo_gp_routing_demand(int32_t device, uint32_t width, uint32_t height, uint64_t num_boxes,
                                const double* boxes, double* horizontal, double* vertical, double* elapsed_ms);
+
+/* ---- legalization: the capacity auction ---------------------------------
+ * Replaces `assign_implicitly` (crates/texo-pnr/src/legalization/auction.rs:
+ * 131-247): the integer-cost assignment of bidders to objects with epsilon
+ * one, every bidder owning a private dummy of cost
+ * D = n * max_base_cost + n + 1 (n = bidders), so the result has exactly the
+ * maximum cardinality and a total base cost at most n above the minimum
+ * among assignments of that cardinality. A bidder's bid raises its best
+ * object's price by (second-best reduced cost - best reduced cost + 1), ties
+ * broken by the lower object id, the dummy losing equal-cost ties.
+ *
+ * The reference bids one bidder at a time from a FIFO queue; here all
+ * unassigned bidders bid at once each round and each object goes to its
+ * highest bid (equal bids: the lower bidder index). The result is
+ * deterministic and has the same guarantees, but where several assignments
+ * meet them it may be another one than the reference's.
+ *
+ * `assignment` receives, per bidder, its object or -1 (its dummy);
+ * `prices` (may be NULL) the final object prices (the certificate of the
+ * epsilon-optimality). Prices live in 32 bits on the device:
+ * n (max_base_cost + 1) + max_base_cost + 2 must stay below 2^32, else
+ * TEXO_GP_ERR_AUCTION_RANGE (the reference's ArithmeticOverflow, there at 2^64). */
+typedef struct texo_gp_auction_stats {
+  int32_t status;
+  uint32_t rounds;               /* parallel bidding rounds */
+  uint64_t bids;                 /* bids placed (each raises one object's price if it wins) */
+  uint64_t candidates_examined;  /* candidate objects visited by the searches */
+  uint64_t unmatched;            /* bidders left on their dummy */
+  uint64_t total_base_cost;      /* sum of the matched bidders' base costs */
+  double elapsed_ms;             /* device time (CUDA events), copies included */
+  uint64_t kernel_launches;
+} texo_gp_auction_stats;
+
+/* Explicit candidate lists, the form the reference's own tests drive the
+ * auction with (`explicit_best_two`, auction.rs:253-272): bidder b may take
+ * domain_object[k] at base cost domain_cost[k], k in
+ * [domain_ptr[b], domain_ptr[b+1]). An object out of range, a cost above
+ * max_base_cost or an object twice in one domain is an error. */
+int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t num_objects,
+                                 uint64_t max_base_cost, const uint32_t* domain_ptr,
+                                 const uint32_t* domain_object, const uint64_t* domain_cost,
+                                 int32_t* assignment, uint32_t* prices, texo_gp_auction_stats* stats);
+
+/* The singleton-BEL auction of `project` (`auction_singletons` and
+ * `auction_units`, legalization/mod.rs:657-677, 733-840), candidates found
+ * by Manhattan ring walks (`best_objects_on_cached_rings`,
+ * `discover_legal_ring`, mod.rs:876-1021): objects are BELs; the BELs of kind
+ * q at tile t = y * width + x are tile_object[k], k in
+ * [tile_ptr[q * width * height + t], tile_ptr[q * width * height + t + 1]);
+ * bidder b of kind bidder_kind[b] with rounded target (target_xy[2b],
+ * target_xy[2b+1]) takes an unoccupied BEL of its kind at base cost
+ * |x - tx| + |y - ty|; max_base_cost = width - 1 + height - 1. The ring walk
+ * stops after ring r once the second-best reduced cost is below r + 1.
+ * `occupied` (may be NULL): one byte per BEL, nonzero for BELs held by fixed
+ * units or earlier cohorts. Legality beyond occupancy (pin wires, shared
+ * resources) is the caller's: a BEL that fails it is passed as occupied. */
+int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, uint32_t height, uint32_t num_kinds,
+                                   const uint32_t* tile_ptr, const uint32_t* tile_object, uint32_t num_objects,
+                                   const uint8_t* occupied, uint32_t num_bidders, const uint32_t* bidder_kind,
+                                   const uint32_t* target_xy, int32_t* assignment, uint32_t* prices,
+                                   texo_gp_auction_stats* stats);
 
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)

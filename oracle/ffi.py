@@ -83,6 +83,72 @@ def routing_demand(width, height, boxes):
     return h.reshape(height, width), v.reshape(height, width), code == 0
 
 
+class AuctionStats(C.Structure):
+    _fields_ = [("bids", C.c_uint64), ("examined", C.c_uint64), ("unmatched", C.c_uint64),
+                ("total_base_cost", C.c_uint64)]
+
+
+def _stats(st):
+    return {"bids": st.bids, "candidates_examined": st.examined, "unmatched": st.unmatched,
+            "total_base_cost": st.total_base_cost}
+
+
+def auction_explicit(domains, object_count, max_base_cost):
+    """assign_implicitly with explicit_best_two (auction.rs:131-272), one
+    bidder at a time: (code, assignment with -1 for the dummy, prices, stats)."""
+    n = len(domains)
+    ptr = np.zeros(n + 1, dtype=np.uint32)
+    if n:
+        ptr[1:] = np.cumsum([len(d) for d in domains])
+    obj = np.ascontiguousarray([o for d in domains for o, _ in d] or [0], dtype=np.uint32)
+    cost = np.ascontiguousarray([c for d in domains for _, c in d] or [0], dtype=np.uint64)
+    a = np.full(max(n, 1), -1, dtype=np.int32)
+    pr = np.zeros(max(object_count, 1), dtype=np.uint64)
+    st = AuctionStats()
+    code = lib().orc_auction_explicit(n, object_count, max_base_cost, P(ptr, C.c_uint32), P(obj, C.c_uint32),
+                                      P(cost, C.c_uint64), P(a, C.c_int32), P(pr, C.c_uint64), C.byref(st))
+    return code, a[:n], pr[:object_count], _stats(st)
+
+
+def _grid_args(grid):
+    tobj = grid.tile_object if len(grid.tile_object) else np.zeros(1, np.uint32)
+    occ = None if grid.occupied is None else np.ascontiguousarray(grid.occupied, dtype=np.uint8)
+    return (grid.width, grid.height, grid.num_kinds, P(np.ascontiguousarray(grid.tile_ptr, dtype=np.uint32), C.c_uint32),
+            P(np.ascontiguousarray(tobj, dtype=np.uint32), C.c_uint32), grid.num_objects,
+            None if occ is None else P(occ, C.c_uint8))
+
+
+def auction_singletons(grid, bidder_kind, targets):
+    """auction_singletons with the ring walk (legalization/mod.rs:657-1021),
+    one bidder at a time: (code, assignment, prices, stats)."""
+    kind = np.ascontiguousarray(bidder_kind, dtype=np.uint32).reshape(-1)
+    txy = np.ascontiguousarray(targets, dtype=np.uint32).reshape(-1)
+    n = kind.shape[0]
+    a = np.full(max(n, 1), -1, dtype=np.int32)
+    pr = np.zeros(max(grid.num_objects, 1), dtype=np.uint64)
+    st = AuctionStats()
+    code = lib().orc_auction_singletons(*_grid_args(grid), n, P(kind if n else np.zeros(1, np.uint32), C.c_uint32),
+                                        P(txy if n else np.zeros(2, np.uint32), C.c_uint32), P(a, C.c_int32),
+                                        P(pr, C.c_uint64), C.byref(st))
+    return code, a[:n], pr[:grid.num_objects], _stats(st)
+
+
+def auction_certificate(grid, bidder_kind, targets, assignment, prices):
+    """Epsilon-complementary-slackness check of a singleton result: (number
+    of violations, first failing index or None, per-bidder base costs)."""
+    kind = np.ascontiguousarray(bidder_kind, dtype=np.uint32).reshape(-1)
+    txy = np.ascontiguousarray(targets, dtype=np.uint32).reshape(-1)
+    n = kind.shape[0]
+    a = np.ascontiguousarray(assignment, dtype=np.int32)
+    pr = np.ascontiguousarray(prices, dtype=np.uint32)
+    base = np.zeros(max(n, 1), dtype=np.uint64)
+    first = C.c_uint64()
+    bad = lib().orc_auction_check_singletons(*_grid_args(grid), n, P(kind, C.c_uint32), P(txy, C.c_uint32),
+                                             P(a, C.c_int32), P(pr if len(pr) else np.zeros(1, np.uint32), C.c_uint32),
+                                             P(base, C.c_uint64), C.byref(first))
+    return bad, (None if first.value == 2**64 - 1 else first.value), base[:n]
+
+
 def multiply_quadratic(diagonal, ptr, index, weight, values):
     n = len(diagonal)
     out = np.zeros(n)
@@ -137,6 +203,14 @@ def lib():
             "orc_solve_quadratic": (C.c_int32, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p,
                                                 C.POINTER(PcgStats)]),
             "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),
+            "orc_auction_explicit": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, c_u32p, c_u32p, c_u64p,
+                                                 C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
+            "orc_auction_singletons": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p, C.c_uint32,
+                                                   C.POINTER(C.c_uint8), C.c_uint32, c_u32p, c_u32p,
+                                                   C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
+            "orc_auction_check_singletons": (C.c_int64, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p,
+                                                         C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32, c_u32p,
+                                                         c_u32p, C.POINTER(C.c_int32), c_u32p, c_u64p, c_u64p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -1,0 +1,154 @@
+"""The GPU capacity auction (texo_gp_auction_explicit / _singletons) against
+the reference's own auction tests (crates/texo-pnr/src/legalization/
+auction.rs:341-505), the exact optimum of small grid problems, the oracle's
+one-bidder-at-a-time auction and the epsilon-optimality certificate, up to
+the 42k-cell placement's own targets."""
+import numpy as np
+import pytest
+
+from auction_cases import (KNOWN_ANSWERS, brute_force, exhaustive_families, grid_optimum, quality, random_grid,
+                           sixty_six_domains)
+from oracle import ffi
+from texo_gb300 import abi, legalize
+
+pytestmark = pytest.mark.gpu
+
+
+def _raises(code, fn, *args):
+    with pytest.raises(abi.TexoGpError) as e:
+        fn(*args)
+    assert e.value.code == abi.CODE[code]
+
+
+@pytest.mark.parametrize("name,domains,objects,max_cost,expected", KNOWN_ANSWERS, ids=[k[0] for k in KNOWN_ANSWERS])
+def test_known_answers(name, domains, objects, max_cost, expected):
+    r = legalize.assign_implicitly(domains, objects, max_cost)
+    assert r.as_options() == expected
+    assert r.stats["unmatched"] == 0 and r.stats["kernel_launches"] == 1
+
+
+def test_sixty_six_and_deficiency_and_range():
+    a = legalize.assign_implicitly(sixty_six_domains(), 66, 0)
+    b = legalize.assign_implicitly(sixty_six_domains(), 66, 0)
+    assert np.array_equal(a.assignment, b.assignment) and np.array_equal(a.prices, b.prices)
+    assert a.stats["unmatched"] == 0 and a.assignment[65] == 65
+    d = legalize.assign_implicitly([[(0, 0)], [(0, 0)]], 1, 0)
+    assert (d.assignment >= 0).sum() == 1 and d.stats["unmatched"] == 1
+    _raises("AUCTION_RANGE", legalize.assign_implicitly, [[]], 0, 2 ** 64 - 1)
+    # the device keeps prices in 32 bits: n (max + 1) + max + 2 must stay below 2^32
+    _raises("AUCTION_RANGE", legalize.assign_implicitly, [[(0, 0)]] * 3, 1, 2 ** 31)
+    assert legalize.assign_implicitly([[]], 0, 0).as_options() == [None]
+    assert legalize.assign_implicitly([], 0, 0).as_options() == []
+
+
+def test_malformed_domains_match_the_oracle():
+    for domains, m, mx, code in [([[(3, 0)]], 2, 0, "AUCTION_OBJECT_RANGE"),
+                                 ([[(0, 5)]], 1, 4, "AUCTION_COST_RANGE"),
+                                 ([[(0, 0), (1, 0), (0, 1)]], 2, 1, "AUCTION_DUPLICATE_OBJECT")]:
+        assert ffi.auction_explicit(domains, m, mx)[0] == abi.CODE[code]
+        _raises(code, legalize.assign_implicitly, domains, m, mx)
+
+
+def test_exhaustive_small_graphs_in_one_launch_each_family():
+    """Every case of the reference's exhaustive families, as disjoint
+    components of one auction: each component keeps the maximum cardinality
+    and the cost bound (its bidders' ε-slackness holds component by
+    component)."""
+    total = 0
+    for nb, no, max_cost, costs in exhaustive_families():
+        cases = len(costs)
+        unmatched, optimum = brute_force(costs)
+        domains = []
+        for i in range(cases):
+            for b in range(nb):
+                domains.append([(i * no + o, int(c)) for o, c in enumerate(costs[i, b]) if c >= 0])
+        r = legalize.assign_implicitly(domains, cases * no, max_cost)
+        a = r.assignment.reshape(cases, nb).astype(np.int64)
+        local = np.where(a >= 0, a - np.arange(cases)[:, None] * no, -1)
+        assert np.all((a < 0) | ((local >= 0) & (local < max(no, 1)))), "an object of another case"
+        q_unmatched, q_cost = quality(costs, local)
+        assert np.array_equal(q_unmatched, unmatched), (nb, no)
+        assert np.all(q_cost <= optimum + nb), (nb, no)
+        total += cases
+    assert total == 91205
+
+
+GRIDS = [   # (width, height, kinds, max BELs a tile, bidders, occupied fraction)
+    (12, 10, 1, 1, 100, 0.0),
+    (16, 16, 2, 2, 300, 0.1),
+    (20, 8, 3, 3, 250, 0.2),
+    (9, 9, 1, 1, 120, 0.3),
+    (1, 1, 1, 3, 5, 0.0),
+    (25, 1, 1, 1, 20, 0.0),
+    (40, 40, 1, 1, 1500, 0.0),
+]
+
+
+@pytest.mark.parametrize("seed,shape", list(enumerate(GRIDS)))
+def test_singletons_against_optimum_oracle_and_certificate(seed, shape):
+    w, h, k, cap, n, occ = shape
+    grid, kind, xy = random_grid(seed, w, h, k, cap, n, occ)
+    r = legalize.auction_singletons(grid, kind, xy)
+    unmatched, optimum = grid_optimum(grid, kind, xy)
+    assert r.stats["unmatched"] == unmatched
+    assert optimum <= r.stats["total_base_cost"] <= optimum + n
+    bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices)
+    assert bad == 0, first
+    assert int(base.sum()) == r.stats["total_base_cost"]
+    code, oa, _, ost = ffi.auction_singletons(grid, kind, xy)
+    assert code == 0 and ost["unmatched"] == r.stats["unmatched"]
+    assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n
+    again = legalize.auction_singletons(grid, kind, xy)
+    assert np.array_equal(again.assignment, r.assignment) and np.array_equal(again.prices, r.prices)
+    assert again.stats["rounds"] == r.stats["rounds"] and again.stats["bids"] == r.stats["bids"]
+
+
+def test_singleton_edge_cases():
+    ones = np.ones((1, 4, 4), dtype=np.int64)
+    grid = legalize.site_grid(ones)
+    r = legalize.auction_singletons(grid, np.zeros(0, np.uint32), np.zeros((0, 2), np.uint32))
+    assert len(r.assignment) == 0
+    full = legalize.site_grid(ones, occupied=np.ones(16, np.uint8))
+    r = legalize.auction_singletons(full, np.zeros(3, np.uint32), np.zeros((3, 2), np.uint32))
+    assert r.as_options() == [None, None, None] and r.stats["unmatched"] == 3
+    occ = np.ones(16, np.uint8)
+    occ[15] = 0
+    corner = legalize.site_grid(ones, occupied=occ)
+    r = legalize.auction_singletons(corner, np.zeros(1, np.uint32), np.zeros((1, 2), np.uint32))
+    assert r.as_options() == [15] and r.stats["total_base_cost"] == 6
+    two = legalize.site_grid(np.stack([np.ones((4, 4)), np.zeros((4, 4))]).astype(np.int64))
+    r = legalize.auction_singletons(two, np.array([1, 0], np.uint32), np.array([[0, 0], [3, 3]], np.uint32))
+    assert r.as_options() == [None, 15]
+    _raises("INVALID_ARGUMENT", legalize.auction_singletons, grid, np.zeros(1, np.uint32),
+            np.array([[4, 0]], np.uint32))
+    twice = legalize.SiteGrid(4, 4, 1, grid.tile_ptr, np.r_[np.arange(15), 14].astype(np.uint32), 16)
+    _raises("AUCTION_DUPLICATE_OBJECT", legalize.auction_singletons, twice, np.zeros(1, np.uint32),
+            np.zeros((1, 2), np.uint32))
+
+
+def test_singletons_on_the_42k_placement():
+    """The 42k-cell placement's rounded targets bid for the 210 x 210 LUT
+    sites: everyone is placed, the certificate holds, and the matched cost
+    is within the bidder count of the oracle's one-at-a-time auction."""
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import Placer, default_params
+    prob = P.synthetic(210, 42000, 365, 50000, 12.0, 0)
+    params = default_params(bins_x=256, bins_y=256, target_density=0.9, gamma_base=4.0, max_iterations=1000,
+                            best_effort=1, engine=abi.ENGINE_DEVICE, dct_mode=abi.DCT_FP32)
+    with Placer(prob, params) as g:
+        targets, _, stats = g.run(allow_nonconverged=True)
+    movable = np.nonzero(np.any(prob.lower_xy != prob.upper_xy, axis=1))[0]
+    n = len(movable)
+    assert n == 42000
+    grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
+    kind = np.zeros(n, np.uint32)
+    xy = np.ascontiguousarray(targets[movable])
+    r = legalize.auction_singletons(grid, kind, xy)
+    assert r.stats["unmatched"] == 0
+    assert len(set(r.assignment.tolist())) == n
+    bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices)
+    assert bad == 0, first
+    assert int(base.sum()) == r.stats["total_base_cost"]
+    code, _, _, ost = ffi.auction_singletons(grid, kind, xy)
+    assert code == 0 and ost["unmatched"] == 0
+    assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n

@@ -27,6 +27,8 @@ STATUS = {
     96: "INVALID_ARGUMENT", 97: "CUDA", 98: "OUT_OF_MEMORY", 99: "DEVICE_TIMEOUT",
     100: "FIXED_POINT_RANGE", 101: "UNSUPPORTED", 102: "BUSY",
     110: "PCG_NOT_CONVERGED",
+    111: "AUCTION_RANGE", 112: "AUCTION_OBJECT_RANGE", 113: "AUCTION_COST_RANGE",
+    114: "AUCTION_DUPLICATE_OBJECT",
 }
 CODE = {v: k for k, v in STATUS.items()}
 
@@ -118,6 +120,12 @@ class PcgStats(C.Structure):
                 ("kernel_launches", C.c_uint64)]
 
 
+class AuctionStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("bids", C.c_uint64),
+                ("candidates_examined", C.c_uint64), ("unmatched", C.c_uint64),
+                ("total_base_cost", C.c_uint64), ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+
+
 class ServerOptions(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_uint32), ("chunk_iterations", C.c_uint32),
                 ("admission_threads", C.c_uint32), ("reserved", C.c_uint32 * 5)]
@@ -200,6 +208,13 @@ SIGNATURES = {
     "texo_gp_quadratic_solve": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(PcgStats)]),
+    "texo_gp_auction_explicit": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32),
+                                             C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32),
+                                             C.POINTER(C.c_uint32), C.POINTER(AuctionStats)]),
+    "texo_gp_auction_singletons": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
+                                               C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32,
+                                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
+                                               C.POINTER(C.c_uint32), C.POINTER(AuctionStats)]),
 }
 
 _lib = None

@@ -1506,6 +1506,10 @@ const char* texo_gp_status_name(int32_t s) {
     case TEXO_GP_ERR_UNSUPPORTED: return "UNSUPPORTED";
     case TEXO_GP_ERR_BUSY: return "BUSY";
     case TEXO_GP_ERR_PCG_NOT_CONVERGED: return "PCG_NOT_CONVERGED";
+    case TEXO_GP_ERR_AUCTION_RANGE: return "AUCTION_RANGE";
+    case TEXO_GP_ERR_AUCTION_OBJECT_RANGE: return "AUCTION_OBJECT_RANGE";
+    case TEXO_GP_ERR_AUCTION_COST_RANGE: return "AUCTION_COST_RANGE";
+    case TEXO_GP_ERR_AUCTION_DUPLICATE_OBJECT: return "AUCTION_DUPLICATE_OBJECT";
     default: return "UNKNOWN";
   }
 }

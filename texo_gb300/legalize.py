@@ -1,0 +1,141 @@
+"""Host mirror of the legalizer's capacity auction (crates/texo-pnr/src/legalization).
+
+`project` (legalization/mod.rs:322-389) turns the rounded global-placement
+targets into BEL choices: fixed units first, then auctions of shared-row
+families and of single-BEL units, then a transactional repair. This module
+exposes the auction, which runs on the GPU through include/texo_gp.h:
+
+- `assign_implicitly(domains, object_count, max_base_cost)`: the auction
+  (auction.rs:131-247) over explicit candidate lists, the form the
+  reference's own tests drive it with;
+- `auction_singletons(grid, bidder_kind, targets)`: the single-BEL auction
+  of `project` (`auction_singletons`, mod.rs:657-677), candidates found by
+  Manhattan ring walks around each unit's target tile;
+- `SiteGrid` / `site_grid`: the BEL layout those walks read.
+
+The GPU bids all unassigned bidders at once each round; the result carries
+the reference's guarantees (exact maximum cardinality, total base cost at
+most the bidder count above the least one of that cardinality) and is
+deterministic, but where several assignments meet them it may differ from
+the reference's one-bidder-at-a-time order.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+
+
+@dataclass
+class AuctionResult:
+    """`AuctionResult` (auction.rs:36-42): per bidder its object, or -1 for
+    the bidder's private dummy; the final prices (the epsilon-optimality
+    certificate); the work done (`AuctionStats`, auction.rs:28-34, plus the
+    rounds, the matched base cost and the device time)."""
+    assignment: np.ndarray
+    prices: np.ndarray
+    stats: dict
+
+    def as_options(self):
+        """The assignment as the reference's Vec<Option<usize>>."""
+        return [None if a < 0 else int(a) for a in self.assignment]
+
+
+def _stats(st):
+    return {"bids": st.bids, "candidates_examined": st.candidates_examined, "unmatched": st.unmatched,
+            "rounds": st.rounds, "total_base_cost": st.total_base_cost, "elapsed_ms": st.elapsed_ms,
+            "kernel_launches": st.kernel_launches}
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def assign_implicitly(domains, object_count, max_base_cost, device=0):
+    """`assign_implicitly` with `explicit_best_two` (auction.rs:253-272):
+    `domains[b]` is bidder b's list of (object, base cost). Raises
+    TexoGpError with AUCTION_RANGE (ArithmeticOverflow), AUCTION_OBJECT_RANGE,
+    AUCTION_COST_RANGE or AUCTION_DUPLICATE_OBJECT like the reference's
+    AuctionError."""
+    n = len(domains)
+    ptr = np.zeros(n + 1, dtype=np.uint32)
+    ptr[1:] = np.cumsum([len(d) for d in domains]) if n else []
+    obj = _u32([o for d in domains for o, _ in d]) if ptr[-1] else np.zeros(1, np.uint32)
+    cost = np.ascontiguousarray([c for d in domains for _, c in d] if ptr[-1] else [0], dtype=np.uint64)
+    assignment = np.full(max(n, 1), -1, dtype=np.int32)
+    prices = np.zeros(max(object_count, 1), dtype=np.uint32)
+    st = abi.AuctionStats()
+    lib = abi.load()
+    abi.check(lib.texo_gp_auction_explicit(device, n, object_count, max_base_cost, abi.ptr(ptr, C.c_uint32),
+                                           abi.ptr(obj, C.c_uint32), abi.ptr(cost, C.c_uint64),
+                                           abi.ptr(assignment, C.c_int32), abi.ptr(prices, C.c_uint32),
+                                           C.byref(st)),
+              "texo_gp_auction_explicit")
+    return AuctionResult(assignment[:n].copy(), prices[:object_count].copy(), _stats(st))
+
+
+@dataclass
+class SiteGrid:
+    """BELs by (kind, tile): the BELs of kind q at tile t = y * width + x are
+    tile_object[tile_ptr[q * width * height + t] : tile_ptr[... + t + 1]];
+    `occupied` (or None) marks BELs held by fixed units or earlier cohorts."""
+    width: int
+    height: int
+    num_kinds: int
+    tile_ptr: np.ndarray
+    tile_object: np.ndarray
+    num_objects: int
+    occupied: np.ndarray = None
+
+    def bel_tiles(self):
+        """(kind, x, y) of every BEL id (-1 where an id is not on the grid)."""
+        where = np.full((self.num_objects, 3), -1, dtype=np.int64)
+        counts = np.diff(self.tile_ptr.astype(np.int64))
+        slot = np.repeat(np.arange(len(counts)), counts)
+        tiles = self.width * self.height
+        where[self.tile_object, 0] = slot // tiles
+        where[self.tile_object, 1] = (slot % tiles) % self.width
+        where[self.tile_object, 2] = (slot % tiles) // self.width
+        return where
+
+
+def site_grid(capacity, occupied=None):
+    """A SiteGrid from per-kind BEL counts `capacity` [K, H, W]: BEL ids run
+    kind-major, then row-major over tiles, then over the slots of a tile."""
+    cap = np.asarray(capacity, dtype=np.int64)
+    if cap.ndim == 2:
+        cap = cap[None]
+    k, h, w = cap.shape
+    ptr = np.zeros(k * h * w + 1, dtype=np.uint32)
+    ptr[1:] = np.cumsum(cap.reshape(-1))
+    m = int(ptr[-1])
+    occ = None if occupied is None else np.ascontiguousarray(occupied, dtype=np.uint8)
+    return SiteGrid(w, h, k, ptr, np.arange(m, dtype=np.uint32), m, occ)
+
+
+def auction_singletons(grid, bidder_kind, targets, device=0):
+    """The single-BEL auction of `project` on the GPU: bidder b (a unit of
+    kind bidder_kind[b] with rounded target targets[b] = (x, y), as
+    `rounded_targets_from_coordinates` gives them) takes one unoccupied BEL
+    of its kind at base cost |x - tx| + |y - ty|."""
+    kind = _u32(bidder_kind).reshape(-1)
+    txy = _u32(targets).reshape(-1)
+    n = kind.shape[0]
+    if txy.shape[0] != 2 * n:
+        raise ValueError("targets must hold one (x, y) per bidder")
+    assignment = np.full(max(n, 1), -1, dtype=np.int32)
+    prices = np.zeros(max(grid.num_objects, 1), dtype=np.uint32)
+    tobj = grid.tile_object if len(grid.tile_object) else np.zeros(1, np.uint32)
+    occ = None if grid.occupied is None else np.ascontiguousarray(grid.occupied, dtype=np.uint8)
+    st = abi.AuctionStats()
+    lib = abi.load()
+    abi.check(lib.texo_gp_auction_singletons(device, grid.width, grid.height, grid.num_kinds,
+                                             abi.ptr(_u32(grid.tile_ptr), C.c_uint32), abi.ptr(_u32(tobj), C.c_uint32),
+                                             grid.num_objects, None if occ is None else abi.ptr(occ, C.c_uint8), n,
+                                             abi.ptr(kind if n else np.zeros(1, np.uint32), C.c_uint32),
+                                             abi.ptr(txy if n else np.zeros(2, np.uint32), C.c_uint32),
+                                             abi.ptr(assignment, C.c_int32), abi.ptr(prices, C.c_uint32),
+                                             C.byref(st)),
+              "texo_gp_auction_singletons")
+    return AuctionResult(assignment[:n].copy(), prices[:grid.num_objects].copy(), _stats(st))
