@@ -618,29 +618,40 @@ def auction_report(reps=5):
     grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
     kind = np.zeros(len(movable), np.uint32)
     xy = np.ascontiguousarray(targets[movable])
-    legalize.auction_singletons(grid, kind, xy)   # warm-up
-    runs, walls = [], []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        runs.append(legalize.auction_singletons(grid, kind, xy))
-        walls.append(1000 * (time.perf_counter() - t0))
-    best = min(runs, key=lambda r: r.stats["elapsed_ms"])
-    same = all(np.array_equal(r.assignment, best.assignment) for r in runs)
-    t0 = time.perf_counter()
-    code, _, _, ost = ffi.auction_singletons(grid, kind, xy)
-    cpu_ms = 1000 * (time.perf_counter() - t0)
-    bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices)
     n = len(movable)
-    st = best.stats
+
+    def gpu(scale):
+        legalize.auction_singletons(grid, kind, xy, cost_scale=scale)   # warm-up
+        runs, walls = [], []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            runs.append(legalize.auction_singletons(grid, kind, xy, cost_scale=scale))
+            walls.append(1000 * (time.perf_counter() - t0))
+        best = min(runs, key=lambda r: r.stats["elapsed_ms"])
+        st = best.stats
+        bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices, cost_scale=st["cost_scale"])
+        return {"cost_scale": st["cost_scale"], "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls),
+                "rounds": st["rounds"], "bids": st["bids"], "candidates_examined": st["candidates_examined"],
+                "unmatched": st["unmatched"], "total_displacement": st["total_base_cost"],
+                "mean_displacement": st["total_base_cost"] / max(n, 1),
+                "deterministic_over_reps": all(np.array_equal(r.assignment, best.assignment) for r in runs),
+                "certificate_violations": int(bad)}
+
+    def cpu(scale):
+        t0 = time.perf_counter()
+        code, _, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
+        ms = 1000 * (time.perf_counter() - t0)
+        return {"cost_scale": scale, "cpu_ms": ms, "status": int(code), "bids": ost["bids"],
+                "unmatched": ost["unmatched"], "total_displacement": ost["total_base_cost"]}
+
+    default, like = gpu(0), gpu(1)
+    ref, ref_scaled = cpu(1), cpu(default["cost_scale"])
     return {"workload": "lfe5u-85-42k", "bidders": int(n), "bels": int(grid.num_objects),
             "grid": "%dx%d" % (prob.width, prob.height), "targets": "rounded targets of the device-engine placement",
-            "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls), "rounds": st["rounds"], "bids": st["bids"],
-            "candidates_examined": st["candidates_examined"], "unmatched": st["unmatched"],
-            "total_displacement": st["total_base_cost"], "mean_displacement": st["total_base_cost"] / max(n, 1),
-            "deterministic_over_reps": bool(same), "certificate_violations": int(bad),
-            "cpu_oracle_ms": cpu_ms, "cpu_oracle_status": int(code), "cpu_oracle_bids": ost["bids"],
-            "cpu_oracle_unmatched": ost["unmatched"], "cpu_oracle_displacement": ost["total_base_cost"],
-            "cores": 1, "speedup": cpu_ms / st["elapsed_ms"] if st["elapsed_ms"] > 0 else None}
+            "gpu": default, "gpu_reference_scale": like, "cpu_oracle": ref, "cpu_oracle_same_scale": ref_scaled,
+            "cores": 1, "speedup_vs_reference_setting": ref["cpu_ms"] / default["gpu_ms"],
+            "speedup_same_scale": ref_scaled["cpu_ms"] / default["gpu_ms"],
+            "displacement_vs_reference_setting": default["total_displacement"] / max(ref["total_displacement"], 1)}
 
 
 def precision_report(iterations=1000, seed=0, threads=5):

@@ -496,14 +496,24 @@ int32_t texo_gp_routing_demand(int32_t device, uint32_t width, uint32_t height, 
  * deterministic and has the same guarantees, but where several assignments
  * meet them it may be another one than the reference's.
  *
+ * `cost_scale` s multiplies every base cost before the auction, epsilon
+ * staying one (the reference's `cost_scale`, auction.rs:142, fixed there at
+ * 1): the dummy becomes D = n * s * max_base_cost + n + 1 and the total base
+ * cost is at most n / s above the least one of the maximum cardinality.
+ * s = 1 is the reference's setting; 0 picks the largest of 8, 4, 2, 1 whose
+ * price range fits, which on placement targets brings the result to within
+ * a fraction of a percent of the optimum for about a quarter more bids.
+ *
  * `assignment` receives, per bidder, its object or -1 (its dummy);
  * `prices` (may be NULL) the final object prices (the certificate of the
  * epsilon-optimality). Prices live in 32 bits on the device:
- * n (max_base_cost + 1) + max_base_cost + 2 must stay below 2^32, else
+ * D + 1 + s * max_base_cost must stay below 2^32, else
  * TEXO_GP_ERR_AUCTION_RANGE (the reference's ArithmeticOverflow, there at 2^64). */
 typedef struct texo_gp_auction_stats {
   int32_t status;
   uint32_t rounds;               /* parallel bidding rounds */
+  uint32_t cost_scale;           /* the scale s the auction ran with */
+  uint32_t reserved;
   uint64_t bids;                 /* bids placed (each raises one object's price if it wins) */
   uint64_t candidates_examined;  /* candidate objects visited by the searches */
   uint64_t unmatched;            /* bidders left on their dummy */
@@ -518,7 +528,7 @@ typedef struct texo_gp_auction_stats {
  * [domain_ptr[b], domain_ptr[b+1]). An object out of range, a cost above
  * max_base_cost or an object twice in one domain is an error. */
 int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t num_objects,
-                                 uint64_t max_base_cost, const uint32_t* domain_ptr,
+                                 uint64_t max_base_cost, uint32_t cost_scale, const uint32_t* domain_ptr,
                                  const uint32_t* domain_object, const uint64_t* domain_cost,
                                  int32_t* assignment, uint32_t* prices, texo_gp_auction_stats* stats);
 
@@ -531,15 +541,15 @@ int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t 
  * bidder b of kind bidder_kind[b] with rounded target (target_xy[2b],
  * target_xy[2b+1]) takes an unoccupied BEL of its kind at base cost
  * |x - tx| + |y - ty|; max_base_cost = width - 1 + height - 1. The ring walk
- * stops after ring r once the second-best reduced cost is below r + 1.
+ * stops after ring r once the second-best reduced cost is below s (r + 1).
  * `occupied` (may be NULL): one byte per BEL, nonzero for BELs held by fixed
  * units or earlier cohorts. Legality beyond occupancy (pin wires, shared
  * resources) is the caller's: a BEL that fails it is passed as occupied. */
 int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, uint32_t height, uint32_t num_kinds,
                                    const uint32_t* tile_ptr, const uint32_t* tile_object, uint32_t num_objects,
                                    const uint8_t* occupied, uint32_t num_bidders, const uint32_t* bidder_kind,
-                                   const uint32_t* target_xy, int32_t* assignment, uint32_t* prices,
-                                   texo_gp_auction_stats* stats);
+                                   const uint32_t* target_xy, uint32_t cost_scale, int32_t* assignment,
+                                   uint32_t* prices, texo_gp_auction_stats* stats);
 
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)

@@ -53,19 +53,23 @@ void insert_best_two(BestTwo& r, const Priced& c) {
 bool add_overflows(uint64_t a, uint64_t b, uint64_t* out) { return __builtin_add_overflow(a, b, out); }
 bool mul_overflows(uint64_t a, uint64_t b, uint64_t* out) { return __builtin_mul_overflow(a, b, out); }
 
-// assign_implicitly (auction.rs:131-247) with cost_scale 1.
+// assign_implicitly (auction.rs:131-247). The reference fixes cost_scale at 1
+// (:142); with a scale s the reduced costs are s * base + price and the
+// dummy n * s * max_base_cost + n + 1, which is the same rule on the scaled
+// costs.
 template <class Search>
-int32_t assign_fifo(uint64_t n, uint64_t m, uint64_t max_base_cost, Search&& search, int32_t* assignment,
-                    uint64_t* prices_out, orc_auction_stats* st) {
+int32_t assign_fifo(uint64_t n, uint64_t m, uint64_t max_base_cost, uint64_t scale, Search&& search,
+                    int32_t* assignment, uint64_t* prices_out, orc_auction_stats* st) {
   orc_auction_stats s{};
   if (n == 0) {
     if (st) *st = s;
     return 0;
   }
-  uint64_t dummy = 0, tmp = 0;
-  // D = n * max_base_cost + n + 1, and D + 1 + max_base_cost must stay representable (:143-162)
-  if (mul_overflows(n, max_base_cost, &dummy) || add_overflows(dummy, n, &dummy) || add_overflows(dummy, 1, &dummy) ||
-      add_overflows(dummy, 1, &tmp) || add_overflows(tmp, max_base_cost, &tmp))
+  uint64_t dummy = 0, tmp = 0, top = 0;
+  // D = n * s * max_base_cost + n + 1, and D + 1 + s * max_base_cost must stay representable (:143-162)
+  if (scale == 0 || mul_overflows(scale, max_base_cost, &top) || mul_overflows(n, top, &dummy) ||
+      add_overflows(dummy, n, &dummy) || add_overflows(dummy, 1, &dummy) || add_overflows(dummy, 1, &tmp) ||
+      add_overflows(tmp, top, &tmp))
     return TEXO_GP_ERR_AUCTION_RANGE;
   std::vector<uint64_t> prices(m, 0);
   std::vector<int64_t> owners(m, -1);
@@ -198,9 +202,9 @@ int32_t check_grid(const Grid& g, uint32_t m, uint32_t n, const uint32_t* kind, 
 
 }  // namespace
 
-extern "C" int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_base_cost, const uint32_t* ptr,
-                                        const uint32_t* object, const uint64_t* cost, int32_t* assignment,
-                                        uint64_t* prices, orc_auction_stats* st) {
+extern "C" int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_base_cost, uint32_t cost_scale,
+                                        const uint32_t* ptr, const uint32_t* object, const uint64_t* cost,
+                                        int32_t* assignment, uint64_t* prices, orc_auction_stats* st) {
   if (st) std::memset(st, 0, sizeof(*st));
   if (n && (!ptr || !assignment || ptr[0] != 0)) return TEXO_GP_ERR_INVALID_ARGUMENT;
   std::vector<uint32_t> stamp(m, 0);
@@ -214,19 +218,19 @@ extern "C" int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_bas
   auto search = [&](uint64_t b, const std::vector<uint64_t>& price) {
     BestTwo r;
     for (uint32_t k = ptr[b]; k < ptr[b + 1]; ++k) {
-      insert_best_two(r, Priced{object[k], cost[k], cost[k] + price[object[k]]});
+      insert_best_two(r, Priced{object[k], cost[k], cost_scale * cost[k] + price[object[k]]});
       ++r.examined;
     }
     return r;
   };
-  return assign_fifo(n, m, max_base_cost, search, assignment, prices, st);
+  return assign_fifo(n, m, max_base_cost, cost_scale, search, assignment, prices, st);
 }
 
 extern "C" int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint32_t num_kinds, const uint32_t* tile_ptr,
                                           const uint32_t* tile_object, uint32_t num_objects, const uint8_t* occupied,
                                           uint32_t num_bidders, const uint32_t* bidder_kind,
-                                          const uint32_t* target_xy, int32_t* assignment, uint64_t* prices,
-                                          orc_auction_stats* st) {
+                                          const uint32_t* target_xy, uint32_t cost_scale, int32_t* assignment,
+                                          uint64_t* prices, orc_auction_stats* st) {
   if (st) std::memset(st, 0, sizeof(*st));
   const Grid g{width, height, num_kinds, tile_ptr, tile_object, occupied};
   if (int32_t e = check_grid(g, num_objects, num_bidders, bidder_kind, target_xy)) return e;
@@ -238,15 +242,16 @@ extern "C" int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint3
     BestTwo r;
     const uint32_t tx = target_xy[2 * b], ty = target_xy[2 * b + 1];
     for (uint32_t radius = 0;; ++radius) {
+      const uint64_t ring_cost = (uint64_t)cost_scale * radius;
       r.examined += visit_ring(g, bidder_kind[b], tx, ty, radius,
-                               [&](uint32_t o) { insert_best_two(r, Priced{o, radius, radius + price[o]}); });
+                               [&](uint32_t o) { insert_best_two(r, Priced{o, radius, ring_cost + price[o]}); });
       if (radius == max_radius) break;
       // strict: an unseen object at the next radius could tie the second best
-      if (r.has_second && r.second.reduced < (uint64_t)radius + 1) break;
+      if (r.has_second && r.second.reduced < ring_cost + cost_scale) break;
     }
     return r;
   };
-  return assign_fifo(num_bidders, num_objects, max_base_cost, search, assignment, prices, st);
+  return assign_fifo(num_bidders, num_objects, max_base_cost, cost_scale, search, assignment, prices, st);
 }
 
 // Epsilon-complementary-slackness certificate of a singleton auction result:
@@ -256,14 +261,17 @@ extern "C" int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint3
 // every unassigned object at price 0. Together these bound the total base
 // cost by the optimum of the same cardinality plus the bidder count.
 // `base_costs` (may be NULL) receives each matched bidder's base cost (0 for
-// unmatched). Returns the number of violations; *first_bad the first bidder
-// (or object + num_bidders) that fails.
+// unmatched). `dual_bound` (may be NULL) receives the assignment dual's value
+// at these prices, sum over bidders of the least reduced cost (dummy
+// included) minus the sum of all prices: a lower bound on the least total
+// cost (dummies at D) of any assignment. Returns the number of violations;
+// *first_bad the first bidder (or object + num_bidders) that fails.
 extern "C" int64_t orc_auction_check_singletons(uint32_t width, uint32_t height, uint32_t num_kinds,
                                                 const uint32_t* tile_ptr, const uint32_t* tile_object,
                                                 uint32_t num_objects, const uint8_t* occupied, uint32_t num_bidders,
                                                 const uint32_t* bidder_kind, const uint32_t* target_xy,
-                                                const int32_t* assignment, const uint32_t* prices,
-                                                uint64_t* base_costs, uint64_t* first_bad) {
+                                                uint32_t cost_scale, const int32_t* assignment, const uint32_t* prices,
+                                                uint64_t* base_costs, uint64_t* first_bad, int64_t* dual_bound) {
   const Grid g{width, height, num_kinds, tile_ptr, tile_object, occupied};
   if (check_grid(g, num_objects, num_bidders, bidder_kind, target_xy)) return -1;
   int64_t bad = 0;
@@ -279,8 +287,11 @@ extern "C" int64_t orc_auction_check_singletons(uint32_t width, uint32_t height,
     for (uint32_t k = tile_ptr[s]; k < tile_ptr[s + 1]; ++k) where[tile_object[k]] = (int64_t)s;
   std::vector<int64_t> holder(num_objects, -1);
   const uint64_t n = num_bidders, max_base_cost = (uint64_t)(width - 1) + (height - 1);
-  const uint64_t dummy = n * max_base_cost + n + 1;
+  const uint64_t s = cost_scale ? cost_scale : 1;
+  const uint64_t dummy = n * s * max_base_cost + n + 1;
   const uint32_t max_radius = (width - 1) + (height - 1);
+  __int128 dual = 0;
+  for (uint32_t o = 0; o < num_objects; ++o) dual -= prices[o];
   for (uint32_t b = 0; b < num_bidders; ++b) {
     const uint32_t tx = target_xy[2 * b], ty = target_xy[2 * b + 1];
     uint64_t mine = UINT64_MAX;   // reduced cost of the held option
@@ -297,7 +308,7 @@ extern "C" int64_t orc_auction_check_singletons(uint32_t width, uint32_t height,
       const uint32_t x = (uint32_t)(t % width), y = (uint32_t)(t / width);
       const uint64_t base = (uint64_t)(x > tx ? x - tx : tx - x) + (y > ty ? y - ty : ty - y);
       if (base_costs) base_costs[b] = base;
-      mine = base + prices[o];
+      mine = s * base + prices[o];
     } else {
       mine = dummy;
     }
@@ -305,15 +316,17 @@ extern "C" int64_t orc_auction_check_singletons(uint32_t width, uint32_t height,
     // passes the best found (a ring-r object costs at least r)
     uint64_t least = dummy;
     for (uint32_t r = 0;; ++r) {
-      if ((uint64_t)r > least) break;
+      if (s * r > least) break;
       visit_ring(g, bidder_kind[b], tx, ty, r, [&](uint32_t o) {
-        const uint64_t c = r + (uint64_t)prices[o];
+        const uint64_t c = s * r + (uint64_t)prices[o];
         if (c < least) least = c;
       });
       if (r == max_radius) break;
     }
+    dual += least;
     if (mine > least + 1) fail(b);
   }
+  if (dual_bound) *dual_bound = (int64_t)dual;
   for (uint32_t o = 0; o < num_objects; ++o)
     if (holder[o] < 0 && prices[o] != 0) fail((uint64_t)num_bidders + o);
   if (first_bad) *first_bad = first;

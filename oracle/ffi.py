@@ -93,9 +93,10 @@ def _stats(st):
             "total_base_cost": st.total_base_cost}
 
 
-def auction_explicit(domains, object_count, max_base_cost):
+def auction_explicit(domains, object_count, max_base_cost, cost_scale=1):
     """assign_implicitly with explicit_best_two (auction.rs:131-272), one
-    bidder at a time: (code, assignment with -1 for the dummy, prices, stats)."""
+    bidder at a time, base costs times `cost_scale` (1 in the reference):
+    (code, assignment with -1 for the dummy, prices, stats)."""
     n = len(domains)
     ptr = np.zeros(n + 1, dtype=np.uint32)
     if n:
@@ -105,7 +106,8 @@ def auction_explicit(domains, object_count, max_base_cost):
     a = np.full(max(n, 1), -1, dtype=np.int32)
     pr = np.zeros(max(object_count, 1), dtype=np.uint64)
     st = AuctionStats()
-    code = lib().orc_auction_explicit(n, object_count, max_base_cost, P(ptr, C.c_uint32), P(obj, C.c_uint32),
+    code = lib().orc_auction_explicit(n, object_count, max_base_cost, cost_scale, P(ptr, C.c_uint32),
+                                      P(obj, C.c_uint32),
                                       P(cost, C.c_uint64), P(a, C.c_int32), P(pr, C.c_uint64), C.byref(st))
     return code, a[:n], pr[:object_count], _stats(st)
 
@@ -118,9 +120,10 @@ def _grid_args(grid):
             None if occ is None else P(occ, C.c_uint8))
 
 
-def auction_singletons(grid, bidder_kind, targets):
+def auction_singletons(grid, bidder_kind, targets, cost_scale=1):
     """auction_singletons with the ring walk (legalization/mod.rs:657-1021),
-    one bidder at a time: (code, assignment, prices, stats)."""
+    one bidder at a time, base costs times `cost_scale` (1 in the reference):
+    (code, assignment, prices, stats)."""
     kind = np.ascontiguousarray(bidder_kind, dtype=np.uint32).reshape(-1)
     txy = np.ascontiguousarray(targets, dtype=np.uint32).reshape(-1)
     n = kind.shape[0]
@@ -128,14 +131,17 @@ def auction_singletons(grid, bidder_kind, targets):
     pr = np.zeros(max(grid.num_objects, 1), dtype=np.uint64)
     st = AuctionStats()
     code = lib().orc_auction_singletons(*_grid_args(grid), n, P(kind if n else np.zeros(1, np.uint32), C.c_uint32),
-                                        P(txy if n else np.zeros(2, np.uint32), C.c_uint32), P(a, C.c_int32),
+                                        P(txy if n else np.zeros(2, np.uint32), C.c_uint32), cost_scale,
+                                        P(a, C.c_int32),
                                         P(pr, C.c_uint64), C.byref(st))
     return code, a[:n], pr[:grid.num_objects], _stats(st)
 
 
-def auction_certificate(grid, bidder_kind, targets, assignment, prices):
+def auction_certificate(grid, bidder_kind, targets, assignment, prices, dual=False, cost_scale=1):
     """Epsilon-complementary-slackness check of a singleton result: (number
-    of violations, first failing index or None, per-bidder base costs)."""
+    of violations, first failing index or None, per-bidder base costs), plus
+    with dual=True the assignment dual at these prices (a lower bound on the
+    least total cost, dummies at n * max_base_cost + n + 1)."""
     kind = np.ascontiguousarray(bidder_kind, dtype=np.uint32).reshape(-1)
     txy = np.ascontiguousarray(targets, dtype=np.uint32).reshape(-1)
     n = kind.shape[0]
@@ -143,10 +149,12 @@ def auction_certificate(grid, bidder_kind, targets, assignment, prices):
     pr = np.ascontiguousarray(prices, dtype=np.uint32)
     base = np.zeros(max(n, 1), dtype=np.uint64)
     first = C.c_uint64()
+    bound = C.c_int64()
     bad = lib().orc_auction_check_singletons(*_grid_args(grid), n, P(kind, C.c_uint32), P(txy, C.c_uint32),
-                                             P(a, C.c_int32), P(pr if len(pr) else np.zeros(1, np.uint32), C.c_uint32),
-                                             P(base, C.c_uint64), C.byref(first))
-    return bad, (None if first.value == 2**64 - 1 else first.value), base[:n]
+                                             cost_scale, P(a, C.c_int32), P(pr if len(pr) else np.zeros(1, np.uint32), C.c_uint32),
+                                             P(base, C.c_uint64), C.byref(first), C.byref(bound))
+    out = (bad, (None if first.value == 2**64 - 1 else first.value), base[:n])
+    return out + (bound.value,) if dual else out
 
 
 def multiply_quadratic(diagonal, ptr, index, weight, values):
@@ -203,14 +211,17 @@ def lib():
             "orc_solve_quadratic": (C.c_int32, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p,
                                                 C.POINTER(PcgStats)]),
             "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),
-            "orc_auction_explicit": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, c_u32p, c_u32p, c_u64p,
+            "orc_auction_explicit": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, c_u32p, c_u32p,
+                                                 c_u64p,
                                                  C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
             "orc_auction_singletons": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p, C.c_uint32,
-                                                   C.POINTER(C.c_uint8), C.c_uint32, c_u32p, c_u32p,
+                                                   C.POINTER(C.c_uint8), C.c_uint32, c_u32p, c_u32p, C.c_uint32,
                                                    C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
             "orc_auction_check_singletons": (C.c_int64, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p,
                                                          C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32, c_u32p,
-                                                         c_u32p, C.POINTER(C.c_int32), c_u32p, c_u64p, c_u64p]),
+                                                         c_u32p, C.c_uint32, C.POINTER(C.c_int32), c_u32p, c_u64p,
+                                                         c_u64p,
+                                                         c_i64p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

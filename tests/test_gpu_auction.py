@@ -20,11 +20,13 @@ def _raises(code, fn, *args):
     assert e.value.code == abi.CODE[code]
 
 
+@pytest.mark.parametrize("scale", [1, 0])
 @pytest.mark.parametrize("name,domains,objects,max_cost,expected", KNOWN_ANSWERS, ids=[k[0] for k in KNOWN_ANSWERS])
-def test_known_answers(name, domains, objects, max_cost, expected):
-    r = legalize.assign_implicitly(domains, objects, max_cost)
+def test_known_answers(name, domains, objects, max_cost, expected, scale):
+    r = legalize.assign_implicitly(domains, objects, max_cost, cost_scale=scale)
     assert r.as_options() == expected
     assert r.stats["unmatched"] == 0 and r.stats["kernel_launches"] == 1
+    assert r.stats["cost_scale"] == (scale or 8)
 
 
 def test_sixty_six_and_deficiency_and_range():
@@ -49,7 +51,8 @@ def test_malformed_domains_match_the_oracle():
         _raises(code, legalize.assign_implicitly, domains, m, mx)
 
 
-def test_exhaustive_small_graphs_in_one_launch_each_family():
+@pytest.mark.parametrize("scale", [1, 0])
+def test_exhaustive_small_graphs_in_one_launch_each_family(scale):
     """Every case of the reference's exhaustive families, as disjoint
     components of one auction: each component keeps the maximum cardinality
     and the cost bound (its bidders' ε-slackness holds component by
@@ -62,13 +65,14 @@ def test_exhaustive_small_graphs_in_one_launch_each_family():
         for i in range(cases):
             for b in range(nb):
                 domains.append([(i * no + o, int(c)) for o, c in enumerate(costs[i, b]) if c >= 0])
-        r = legalize.assign_implicitly(domains, cases * no, max_cost)
+        r = legalize.assign_implicitly(domains, cases * no, max_cost, cost_scale=scale)
+        s = r.stats["cost_scale"]
         a = r.assignment.reshape(cases, nb).astype(np.int64)
         local = np.where(a >= 0, a - np.arange(cases)[:, None] * no, -1)
         assert np.all((a < 0) | ((local >= 0) & (local < max(no, 1)))), "an object of another case"
         q_unmatched, q_cost = quality(costs, local)
         assert np.array_equal(q_unmatched, unmatched), (nb, no)
-        assert np.all(q_cost <= optimum + nb), (nb, no)
+        assert np.all(q_cost <= optimum + nb / s), (nb, no)
         total += cases
     assert total == 91205
 
@@ -84,21 +88,24 @@ GRIDS = [   # (width, height, kinds, max BELs a tile, bidders, occupied fraction
 ]
 
 
+@pytest.mark.parametrize("scale", [1, 0])
 @pytest.mark.parametrize("seed,shape", list(enumerate(GRIDS)))
-def test_singletons_against_optimum_oracle_and_certificate(seed, shape):
+def test_singletons_against_optimum_oracle_and_certificate(seed, shape, scale):
     w, h, k, cap, n, occ = shape
     grid, kind, xy = random_grid(seed, w, h, k, cap, n, occ)
-    r = legalize.auction_singletons(grid, kind, xy)
+    r = legalize.auction_singletons(grid, kind, xy, cost_scale=scale)
+    s = r.stats["cost_scale"]
+    assert s == (scale or 8)
     unmatched, optimum = grid_optimum(grid, kind, xy)
     assert r.stats["unmatched"] == unmatched
-    assert optimum <= r.stats["total_base_cost"] <= optimum + n
-    bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices)
+    assert optimum <= r.stats["total_base_cost"] <= optimum + n / s
+    bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices, cost_scale=s)
     assert bad == 0, first
     assert int(base.sum()) == r.stats["total_base_cost"]
-    code, oa, _, ost = ffi.auction_singletons(grid, kind, xy)
+    code, oa, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=s)
     assert code == 0 and ost["unmatched"] == r.stats["unmatched"]
-    assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n
-    again = legalize.auction_singletons(grid, kind, xy)
+    assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n / s
+    again = legalize.auction_singletons(grid, kind, xy, cost_scale=scale)
     assert np.array_equal(again.assignment, r.assignment) and np.array_equal(again.prices, r.prices)
     assert again.stats["rounds"] == r.stats["rounds"] and again.stats["bids"] == r.stats["bids"]
 
@@ -143,12 +150,16 @@ def test_singletons_on_the_42k_placement():
     grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
     kind = np.zeros(n, np.uint32)
     xy = np.ascontiguousarray(targets[movable])
-    r = legalize.auction_singletons(grid, kind, xy)
-    assert r.stats["unmatched"] == 0
-    assert len(set(r.assignment.tolist())) == n
-    bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices)
-    assert bad == 0, first
-    assert int(base.sum()) == r.stats["total_base_cost"]
-    code, _, _, ost = ffi.auction_singletons(grid, kind, xy)
+    code, _, _, ost = ffi.auction_singletons(grid, kind, xy)   # the reference's setting, one bidder at a time
     assert code == 0 and ost["unmatched"] == 0
-    assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n
+    for scale in (1, 0):
+        r = legalize.auction_singletons(grid, kind, xy, cost_scale=scale)
+        s = r.stats["cost_scale"]
+        assert r.stats["unmatched"] == 0
+        assert len(set(r.assignment.tolist())) == n
+        bad, first, base = ffi.auction_certificate(grid, kind, xy, r.assignment, r.prices, cost_scale=s)
+        assert bad == 0, first
+        assert int(base.sum()) == r.stats["total_base_cost"]
+        assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n
+    # the default (scaled) result moves the units less than the reference's setting does
+    assert r.stats["cost_scale"] == 8 and r.stats["total_base_cost"] <= ost["total_base_cost"]

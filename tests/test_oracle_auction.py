@@ -88,6 +88,28 @@ def test_singletons_match_the_optimum_and_certify(seed, shape):
     assert int(base.sum()) == st["total_base_cost"]
 
 
+@pytest.mark.parametrize("scale", [2, 4, 8])
+def test_scaled_costs_tighten_the_bound(scale):
+    """With base costs times s (the reference's cost_scale) the result stays
+    of maximum cardinality and within n / s of the optimum."""
+    for seed, shape in enumerate(GRIDS[:4]):
+        w, h, k, cap, n, occ = shape
+        grid, kind, xy = random_grid(seed, w, h, k, cap, n, occ)
+        code, a, prices, st = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
+        assert code == 0
+        unmatched, optimum = grid_optimum(grid, kind, xy)
+        assert st["unmatched"] == unmatched
+        assert optimum <= st["total_base_cost"] <= optimum + n / scale
+        bad, first, _ = ffi.auction_certificate(grid, kind, xy, a, prices.astype(np.uint32), cost_scale=scale)
+        assert bad == 0, first
+    for nb, no, max_cost, costs in list(exhaustive_families())[:12]:
+        unmatched, optimum = brute_force(costs)
+        got = np.array([ffi.auction_explicit(domains_of(c), no, max_cost, scale)[1] for c in costs])
+        got = got.reshape(len(costs), nb)
+        q_unmatched, q_cost = quality(costs, got)
+        assert np.array_equal(q_unmatched, unmatched) and np.all(q_cost <= optimum + nb / scale)
+
+
 def test_certificate_catches_planted_mistakes():
     grid, kind, xy = random_grid(7, 14, 12, 1, 1, 120, 0.0)
     code, a, prices, _ = ffi.auction_singletons(grid, kind, xy)

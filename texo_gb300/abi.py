@@ -121,7 +121,8 @@ class PcgStats(C.Structure):
 
 
 class AuctionStats(C.Structure):
-    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("bids", C.c_uint64),
+    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("cost_scale", C.c_uint32), ("reserved", C.c_uint32),
+                ("bids", C.c_uint64),
                 ("candidates_examined", C.c_uint64), ("unmatched", C.c_uint64),
                 ("total_base_cost", C.c_uint64), ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64)]
 
@@ -208,13 +209,14 @@ SIGNATURES = {
     "texo_gp_quadratic_solve": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(PcgStats)]),
-    "texo_gp_auction_explicit": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_uint32),
+    "texo_gp_auction_explicit": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
+                                             C.POINTER(C.c_uint32),
                                              C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32),
                                              C.POINTER(C.c_uint32), C.POINTER(AuctionStats)]),
     "texo_gp_auction_singletons": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32),
                                                C.POINTER(C.c_uint32), C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32,
-                                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
-                                               C.POINTER(C.c_uint32), C.POINTER(AuctionStats)]),
+                                               C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
+                                               C.POINTER(C.c_int32), C.POINTER(C.c_uint32), C.POINTER(AuctionStats)]),
 }
 
 _lib = None

@@ -6,9 +6,10 @@
 // The reference bids one bidder at a time from a FIFO queue. Here every
 // unassigned bidder bids in the same round (a Jacobi auction), which keeps
 // the guarantees the reference states for its result: epsilon one, a private
-// dummy of cost D = n * max_base_cost + n + 1 per bidder, so the assignment
-// has exactly the maximum cardinality and a total base cost at most n above
-// the least one of that cardinality. Prices only rise, every bid raises its
+// dummy of cost D = n * s * max_base_cost + n + 1 per bidder, so the assignment
+// has exactly the maximum cardinality and a total base cost at most n / s
+// above the least one of that cardinality (s the cost scale, 1 in the
+// reference). Prices only rise, every bid raises its
 // object's price by at least one, and an object priced above D is no better
 // than any bidder's dummy, so the rounds end.
 //
@@ -58,7 +59,8 @@ struct AucResult {
 struct AucDev {
   int grid;            // 1 ring walks over the BEL grid, 0 explicit domains
   unsigned n, m;
-  unsigned dummy;      // D = n * max_base_cost + n + 1
+  unsigned scale;      // s: reduced cost = s * base cost + price
+  unsigned dummy;      // D = n * s * max_base_cost + n + 1
   // explicit domains
   const unsigned *dptr, *dobj, *dcost;
   // BEL grid
@@ -119,7 +121,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const unsigned e = __ldg(d.dptr + b + 1);
     for (unsigned k = __ldg(d.dptr + b) + lane; k < e; k += 32) {
       const unsigned o = __ldg(d.dobj + k);
-      insert2(a1, a2, make_key(__ldg(d.dcost + k) + __ldcg(d.price + o), o));
+      insert2(a1, a2, make_key(d.scale * __ldg(d.dcost + k) + __ldcg(d.price + o), o));
       ++seen;
     }
     warp_best2(a1, a2);
@@ -129,6 +131,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const unsigned* tp = d.tptr + (size_t)__ldg(d.kind + b) * d.W * d.H;
     for (unsigned r = 0;; ++r) {
       const unsigned points = r == 0 ? 1u : 4u * r;
+      const unsigned ring_cost = d.scale * r;
       for (unsigned j = lane; j < points; j += 32) {
         int dx = 0, dy = 0;
         if (r) {
@@ -146,13 +149,13 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
           const unsigned o = __ldg(d.tobj + k);
           ++seen;
           if (d.occ && __ldg(d.occ + o)) continue;
-          insert2(a1, a2, make_key(r + __ldcg(d.price + o), o));
+          insert2(a1, a2, make_key(ring_cost + __ldcg(d.price + o), o));
         }
       }
       warp_best2(a1, a2);
       if (r == d.max_radius) break;
       // strict: an unseen object one ring further out could tie the second best
-      if (a2 != kNoKey && (unsigned)(a2 >> 32) < r + 1) break;
+      if (a2 != kNoKey && (unsigned)(a2 >> 32) < ring_cost + d.scale) break;
     }
   }
   k1 = a1;
@@ -310,6 +313,7 @@ struct AucHost {
   bool grid = false;
   uint32_t n = 0, m = 0;
   uint64_t max_base_cost = 0;
+  uint32_t scale = 1;
   // explicit
   const uint32_t* dptr = nullptr;
   const uint32_t* dobj = nullptr;
@@ -327,14 +331,28 @@ int32_t fail_with(texo_gp_auction_stats* st, int32_t code, const std::string& wh
 }
 
 // The reference's range check (auction.rs:143-162) at the device's 32-bit
-// prices: n * max_base_cost + n + 1 (the dummy cost) plus one plus
-// max_base_cost must stay below 2^32.
-bool dummy_cost(uint64_t n, uint64_t max_base_cost, uint32_t* out) {
-  unsigned __int128 d = (unsigned __int128)n * max_base_cost + n + 1;
-  if (d + 1 + max_base_cost >= ((unsigned __int128)1 << 32)) return false;
+// prices and cost scale s: the dummy cost D = n * s * max_base_cost + n + 1,
+// plus one, plus s * max_base_cost must stay below 2^32.
+bool dummy_cost(uint64_t n, uint64_t max_base_cost, uint64_t scale, uint32_t* out) {
+  const unsigned __int128 top = (unsigned __int128)scale * max_base_cost;
+  const unsigned __int128 d = (unsigned __int128)n * top + n + 1;
+  if (d + 1 + top >= ((unsigned __int128)1 << 32)) return false;
   *out = (uint32_t)d;
   return true;
 }
+
+// The scale to run with: the caller's, or (0) the largest of 8, 4, 2, 1 that
+// fits; 0 when none does.
+uint32_t pick_scale(uint64_t n, uint64_t max_base_cost, uint32_t requested) {
+  uint32_t d = 0;
+  if (requested) return dummy_cost(n, max_base_cost, requested, &d) ? requested : 0u;
+  for (uint32_t s : {8u, 4u, 2u, 1u})
+    if (dummy_cost(n, max_base_cost, s, &d)) return s;
+  return 0u;
+}
+
+constexpr const char* kRangeText =
+    "auction price range: n * s * max_base_cost + n + 2 + s * max_base_cost must stay below 2^32";
 
 // Up-front object checks shared with the oracle: in range, none twice in one list.
 int32_t check_objects(const uint32_t* objects, uint64_t count, uint32_t m, std::vector<uint32_t>& stamp, uint32_t mark) {
@@ -349,9 +367,7 @@ int32_t check_objects(const uint32_t* objects, uint64_t count, uint32_t m, std::
 
 int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* prices_out, texo_gp_auction_stats* st) {
   uint32_t dummy = 0;
-  if (!dummy_cost(h.n, h.max_base_cost, &dummy))
-    return fail_with(st, TEXO_GP_ERR_AUCTION_RANGE,
-                     "auction price range: n (max_base_cost + 1) + max_base_cost + 2 must stay below 2^32");
+  if (!dummy_cost(h.n, h.max_base_cost, h.scale, &dummy)) return fail_with(st, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   if (cudaSetDevice(device) != cudaSuccess) return fail_with(st, TEXO_GP_ERR_CUDA, "cudaSetDevice failed");
   static const int per_sm = [] {   // thread-safe one-time initialisation
     int b = 0;
@@ -394,6 +410,7 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
   d.grid = h.grid ? 1 : 0;
   d.n = h.n;
   d.m = h.m;
+  d.scale = h.scale;
   d.dummy = dummy;
   d.price = (unsigned*)take(sz_m4);
   d.owner = (int*)take(sz_m4);
@@ -478,6 +495,7 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
   if (st) {
     st->status = code;
     st->rounds = res.rounds;
+    st->cost_scale = h.scale;
     st->bids = res.bids;
     st->candidates_examined = res.examined;
     st->unmatched = res.unmatched;
@@ -491,7 +509,7 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
 }  // namespace
 
 extern "C" int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t num_objects,
-                                            uint64_t max_base_cost, const uint32_t* domain_ptr,
+                                            uint64_t max_base_cost, uint32_t cost_scale, const uint32_t* domain_ptr,
                                             const uint32_t* domain_object, const uint64_t* domain_cost,
                                             int32_t* assignment, uint32_t* prices, texo_gp_auction_stats* stats) {
   if (stats) std::memset(stats, 0, sizeof(*stats));
@@ -519,10 +537,8 @@ extern "C" int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders
   h.max_base_cost = max_base_cost;
   h.dptr = domain_ptr;
   h.dobj = domain_object;
-  uint32_t scratch = 0;
-  if (!dummy_cost(num_bidders, max_base_cost, &scratch))
-    return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE,
-                     "auction price range: n (max_base_cost + 1) + max_base_cost + 2 must stay below 2^32");
+  h.scale = pick_scale(num_bidders, max_base_cost, cost_scale);
+  if (!h.scale) return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   h.dcost.resize(domain_ptr[num_bidders]);
   for (size_t k = 0; k < h.dcost.size(); ++k) h.dcost[k] = (uint32_t)domain_cost[k];   // <= max_base_cost < 2^32
   return run_auction(device, h, assignment, prices, stats);
@@ -532,7 +548,8 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
                                               const uint32_t* tile_ptr, const uint32_t* tile_object,
                                               uint32_t num_objects, const uint8_t* occupied, uint32_t num_bidders,
                                               const uint32_t* bidder_kind, const uint32_t* target_xy,
-                                              int32_t* assignment, uint32_t* prices, texo_gp_auction_stats* stats) {
+                                              uint32_t cost_scale, int32_t* assignment, uint32_t* prices,
+                                              texo_gp_auction_stats* stats) {
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (num_bidders == 0) return fail_with(stats, TEXO_GP_OK, "");   // auction_units' empty case (mod.rs:744-747)
   if (width == 0 || height == 0 || num_kinds == 0 || !tile_ptr || !bidder_kind || !target_xy || !assignment)
@@ -560,6 +577,8 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
   h.n = num_bidders;
   h.m = num_objects;
   h.max_base_cost = (uint64_t)(width - 1) + (height - 1);
+  h.scale = pick_scale(num_bidders, h.max_base_cost, cost_scale);
+  if (!h.scale) return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   h.W = width;
   h.H = height;
   h.K = num_kinds;

@@ -17,7 +17,9 @@ The GPU bids all unassigned bidders at once each round; the result carries
 the reference's guarantees (exact maximum cardinality, total base cost at
 most the bidder count above the least one of that cardinality) and is
 deterministic, but where several assignments meet them it may differ from
-the reference's one-bidder-at-a-time order.
+the reference's one-bidder-at-a-time order. By default the base costs are
+scaled (the reference's own `cost_scale`, fixed there at 1), which tightens
+the cost bound to n / scale.
 """
 import ctypes as C
 from dataclasses import dataclass
@@ -43,8 +45,8 @@ class AuctionResult:
 
 
 def _stats(st):
-    return {"bids": st.bids, "candidates_examined": st.candidates_examined, "unmatched": st.unmatched,
-            "rounds": st.rounds, "total_base_cost": st.total_base_cost, "elapsed_ms": st.elapsed_ms,
+    return {"cost_scale": st.cost_scale, "bids": st.bids, "candidates_examined": st.candidates_examined,
+            "unmatched": st.unmatched, "rounds": st.rounds, "total_base_cost": st.total_base_cost, "elapsed_ms": st.elapsed_ms,
             "kernel_launches": st.kernel_launches}
 
 
@@ -52,9 +54,10 @@ def _u32(a):
     return np.ascontiguousarray(a, dtype=np.uint32)
 
 
-def assign_implicitly(domains, object_count, max_base_cost, device=0):
+def assign_implicitly(domains, object_count, max_base_cost, cost_scale=0, device=0):
     """`assign_implicitly` with `explicit_best_two` (auction.rs:253-272):
-    `domains[b]` is bidder b's list of (object, base cost). Raises
+    `domains[b]` is bidder b's list of (object, base cost); `cost_scale` 1 is
+    the reference's setting, 0 the largest of 8, 4, 2, 1 that fits. Raises
     TexoGpError with AUCTION_RANGE (ArithmeticOverflow), AUCTION_OBJECT_RANGE,
     AUCTION_COST_RANGE or AUCTION_DUPLICATE_OBJECT like the reference's
     AuctionError."""
@@ -67,7 +70,8 @@ def assign_implicitly(domains, object_count, max_base_cost, device=0):
     prices = np.zeros(max(object_count, 1), dtype=np.uint32)
     st = abi.AuctionStats()
     lib = abi.load()
-    abi.check(lib.texo_gp_auction_explicit(device, n, object_count, max_base_cost, abi.ptr(ptr, C.c_uint32),
+    abi.check(lib.texo_gp_auction_explicit(device, n, object_count, max_base_cost, cost_scale,
+                                           abi.ptr(ptr, C.c_uint32),
                                            abi.ptr(obj, C.c_uint32), abi.ptr(cost, C.c_uint64),
                                            abi.ptr(assignment, C.c_int32), abi.ptr(prices, C.c_uint32),
                                            C.byref(st)),
@@ -114,11 +118,13 @@ def site_grid(capacity, occupied=None):
     return SiteGrid(w, h, k, ptr, np.arange(m, dtype=np.uint32), m, occ)
 
 
-def auction_singletons(grid, bidder_kind, targets, device=0):
+def auction_singletons(grid, bidder_kind, targets, cost_scale=0, device=0):
     """The single-BEL auction of `project` on the GPU: bidder b (a unit of
     kind bidder_kind[b] with rounded target targets[b] = (x, y), as
     `rounded_targets_from_coordinates` gives them) takes one unoccupied BEL
-    of its kind at base cost |x - tx| + |y - ty|."""
+    of its kind at base cost |x - tx| + |y - ty|. `cost_scale` as in
+    `assign_implicitly`: the total base cost is at most n / scale above the
+    optimum of the maximum cardinality."""
     kind = _u32(bidder_kind).reshape(-1)
     txy = _u32(targets).reshape(-1)
     n = kind.shape[0]
@@ -135,7 +141,7 @@ def auction_singletons(grid, bidder_kind, targets, device=0):
                                              grid.num_objects, None if occ is None else abi.ptr(occ, C.c_uint8), n,
                                              abi.ptr(kind if n else np.zeros(1, np.uint32), C.c_uint32),
                                              abi.ptr(txy if n else np.zeros(2, np.uint32), C.c_uint32),
-                                             abi.ptr(assignment, C.c_int32), abi.ptr(prices, C.c_uint32),
+                                             cost_scale, abi.ptr(assignment, C.c_int32), abi.ptr(prices, C.c_uint32),
                                              C.byref(st)),
               "texo_gp_auction_singletons")
     return AuctionResult(assignment[:n].copy(), prices[:grid.num_objects].copy(), _stats(st))
