@@ -537,7 +537,9 @@ extern "C" int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders
   h.max_base_cost = max_base_cost;
   h.dptr = domain_ptr;
   h.dobj = domain_object;
-  h.scale = pick_scale(num_bidders, max_base_cost, cost_scale);
+  // whether every bidder can be matched is not known up front for explicit
+  // domains, so the automatic scale is the reference's
+  h.scale = pick_scale(num_bidders, max_base_cost, cost_scale ? cost_scale : 1u);
   if (!h.scale) return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   h.dcost.resize(domain_ptr[num_bidders]);
   for (size_t k = 0; k < h.dcost.size(); ++k) h.dcost[k] = (uint32_t)domain_cost[k];   // <= max_base_cost < 2^32
@@ -577,6 +579,20 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
   h.n = num_bidders;
   h.m = num_objects;
   h.max_base_cost = (uint64_t)(width - 1) + (height - 1);
+  // Surplus bidders leave only once prices pass the dummy cost D, about one
+  // price step a round, and D grows with the scale: scale automatically only
+  // when every kind has at least as many free BELs as bidders (then every
+  // bidder is matched and no price climbs towards D).
+  if (cost_scale == 0) {
+    std::vector<uint64_t> free_bels(num_kinds, 0), bidders(num_kinds, 0);
+    const uint64_t tiles = (uint64_t)width * height;
+    for (uint32_t q = 0; q < num_kinds; ++q)
+      for (uint32_t k = tile_ptr[q * tiles]; k < tile_ptr[(q + 1) * tiles]; ++k)
+        free_bels[q] += (occupied && occupied[tile_object[k]]) ? 0 : 1;
+    for (uint32_t b = 0; b < num_bidders; ++b) bidders[bidder_kind[b]]++;
+    for (uint32_t q = 0; q < num_kinds; ++q)
+      if (bidders[q] > free_bels[q]) cost_scale = 1;
+  }
   h.scale = pick_scale(num_bidders, h.max_base_cost, cost_scale);
   if (!h.scale) return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   h.W = width;
