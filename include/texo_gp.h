@@ -519,7 +519,7 @@ typedef struct texo_gp_auction_stats {
   int32_t status;
   uint32_t rounds;               /* parallel bidding rounds */
   uint32_t cost_scale;           /* the scale s the auction ran with */
-  uint32_t reserved;
+  uint32_t tail_rounds;          /* of the rounds, those one block ran alone (few bidders left) */
   uint64_t bids;                 /* bids placed (each raises one object's price if it wins) */
   uint64_t candidates_examined;  /* candidate objects visited by the searches */
   uint64_t unmatched;            /* bidders left on their dummy */
@@ -550,7 +550,8 @@ int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t 
  * stops after ring r once the second-best reduced cost is below s (r + 1).
  * `occupied` (may be NULL): one byte per BEL, nonzero for BELs held by fixed
  * units or earlier cohorts. Legality beyond occupancy (pin wires, shared
- * resources) is the caller's: a BEL that fails it is passed as occupied. */
+ * resources) is the caller's: a BEL that fails it is passed as occupied.
+ * Grid sides up to 16384 tiles. */
 int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, uint32_t height, uint32_t num_kinds,
                                    const uint32_t* tile_ptr, const uint32_t* tile_object, uint32_t num_objects,
                                    const uint8_t* occupied, uint32_t num_bidders, const uint32_t* bidder_kind,

@@ -121,7 +121,7 @@ class PcgStats(C.Structure):
 
 
 class AuctionStats(C.Structure):
-    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("cost_scale", C.c_uint32), ("reserved", C.c_uint32),
+    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("cost_scale", C.c_uint32), ("tail_rounds", C.c_uint32),
                 ("bids", C.c_uint64),
                 ("candidates_examined", C.c_uint64), ("unmatched", C.c_uint64),
                 ("total_base_cost", C.c_uint64), ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64)]

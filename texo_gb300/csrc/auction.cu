@@ -45,15 +45,19 @@ namespace {
 constexpr int kAucThreads = 256;
 constexpr int kAucWarps = kAucThreads / 32;
 constexpr int kAucBlocksPerSm = 4;   // resident blocks a multiprocessor runs
+constexpr int kTailPerWarp = 4;      // active bidders per warp at which block 0 finishes alone
 constexpr unsigned kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kNoKey = ~0ull;                      // "no candidate"
 constexpr unsigned long long kTimeLimitNs = 20ull * 1000000000ull; // the whole auction
 
 struct AucResult {
   unsigned rounds;
+  unsigned tail_rounds;  // rounds run by block 0 alone
   unsigned stop_round;   // nonzero: every block leaves at the top of this round (the time limit ran out)
-  unsigned long long bids, examined, total_base;
-  unsigned long long unmatched;
+  unsigned pad;
+  unsigned long long bids, examined;
+  unsigned long long total_base;   // sum of the holders' base costs (kept as holders change)
+  unsigned long long matched;      // objects held
 };
 
 struct AucDev {
@@ -67,13 +71,14 @@ struct AucDev {
   unsigned W, H, max_radius, slots;
   const unsigned *tptr, *tobj, *kind, *txy;
   const unsigned char* occ;
-  unsigned* where;     // per BEL: its (kind, tile) slot
   // auction state
   unsigned* price;
   int* owner;
   unsigned long long* bid;   // [2][m]
   int* assign;
   unsigned* want;            // object bid on this round, or kNone
+  unsigned* want_base;       // base cost of that object
+  unsigned* held_base;       // base cost of the object held
   unsigned* act;             // [2][n] active bidders
   unsigned* touched;         // [2][cap] objects bid on
   unsigned cap;
@@ -112,10 +117,27 @@ __device__ __forceinline__ void warp_best2(unsigned long long& a1, unsigned long
   }
 }
 
+// The Manhattan diamond around a target, flattened in ring order: point 0 is
+// ring 0, ring r >= 1 holds the points [1 + 2r(r-1), 1 + 2r(r+1)).
+__device__ __forceinline__ unsigned ring_of(unsigned p) {
+  if (p == 0) return 0;
+  unsigned r = (unsigned)((1.0f + sqrtf((float)(2u * p - 1u))) * 0.5f);
+  if (r == 0) r = 1;
+  while (1u + 2u * r * (r + 1u) <= p) ++r;
+  while (r > 1u && 1u + 2u * r * (r - 1u) > p) --r;
+  return r;
+}
+
 // The two least (reduced cost, object) keys among bidder b's candidates, the
 // same in every lane of the warp. Returns the candidates this lane visited.
+//
+// The ring walk hands the warp 32 consecutive points of the diamond at a
+// time and stops once the second best is below the least cost an unseen
+// object can have, s times the first ring not fully seen. Visiting rings
+// past the reference's stopping ring adds only objects that cannot enter
+// the best two, so the result is the reference's exact best two.
 __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned b, int lane, unsigned long long& k1,
-                                       unsigned long long& k2) {
+                                                       unsigned long long& k2) {
   unsigned long long a1 = kNoKey, a2 = kNoKey, seen = 0;
   if (!d.grid) {
     const unsigned e = __ldg(d.dptr + b + 1);
@@ -129,33 +151,39 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const int tx = (int)__ldg(d.txy + 2 * b), ty = (int)__ldg(d.txy + 2 * b + 1);
     const int W = (int)d.W, H = (int)d.H;
     const unsigned* tp = d.tptr + (size_t)__ldg(d.kind + b) * d.W * d.H;
-    for (unsigned r = 0;; ++r) {
-      const unsigned points = r == 0 ? 1u : 4u * r;
-      const unsigned ring_cost = d.scale * r;
-      for (unsigned j = lane; j < points; j += 32) {
+    const unsigned R = d.max_radius;
+    const unsigned total = 1u + 2u * R * (R + 1u);   // points of the whole diamond
+    for (unsigned p0 = 0;; p0 += 32) {
+      const unsigned p = p0 + lane;
+      if (p < total) {
+        const unsigned r = ring_of(p);
         int dx = 0, dy = 0;
         if (r) {
-          // the diamond |dx| + |dy| = r as four quarter turns of (r - i, i)
-          const unsigned q = j / r, i = j - q * r;
+          // ring r as four quarter turns of (r - i, i)
+          const unsigned j = p - (1u + 2u * r * (r - 1u)), q = j / r, i = j - q * r;
           const int u = (int)(r - i), v = (int)i;
           dx = q == 0 ? u : q == 1 ? -v : q == 2 ? -u : v;
           dy = q == 0 ? v : q == 1 ? u : q == 2 ? -v : -u;
         }
         const int x = tx + dx, y = ty + dy;
-        if (x < 0 || y < 0 || x >= W || y >= H) continue;
-        const int t = y * W + x;
-        const unsigned e = __ldg(tp + t + 1);
-        for (unsigned k = __ldg(tp + t); k < e; ++k) {
-          const unsigned o = __ldg(d.tobj + k);
-          ++seen;
-          if (d.occ && __ldg(d.occ + o)) continue;
-          insert2(a1, a2, make_key(ring_cost + __ldcg(d.price + o), o));
+        if (x >= 0 && y >= 0 && x < W && y < H) {
+          const int t = y * W + x;
+          const unsigned ring_cost = d.scale * r, e = __ldg(tp + t + 1);
+          for (unsigned k = __ldg(tp + t); k < e; ++k) {
+            const unsigned o = __ldg(d.tobj + k);
+            ++seen;
+            if (d.occ && __ldg(d.occ + o)) continue;
+            insert2(a1, a2, make_key(ring_cost + __ldcg(d.price + o), o));
+          }
         }
       }
       warp_best2(a1, a2);
-      if (r == d.max_radius) break;
-      // strict: an unseen object one ring further out could tie the second best
-      if (a2 != kNoKey && (unsigned)(a2 >> 32) < ring_cost + d.scale) break;
+      const unsigned last = min(p0 + 32u, total) - 1u;
+      if (last == total - 1u) break;   // every ring seen
+      const unsigned rl = ring_of(last);
+      const unsigned unseen = last == 2u * rl * (rl + 1u) ? rl + 1u : rl;   // first ring not fully seen
+      // strict: an unseen object could tie the second best
+      if (a2 != kNoKey && (unsigned)(a2 >> 32) < d.scale * unseen) break;
     }
   }
   k1 = a1;
@@ -163,10 +191,102 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
   return seen;
 }
 
+// Bid phase of round k: warps [w0, w0 + nw) of the launch take the active
+// bidders in turn.
+__device__ __forceinline__ void bid_phase(const AucDev& d, unsigned k, unsigned nA, unsigned w0, unsigned nw, int lane,
+                                          unsigned long long& bids, unsigned long long& seen) {
+  const unsigned cur = k & 1u;
+  const unsigned* A = d.act + (size_t)cur * d.n;
+  unsigned long long* bidc = d.bid + (size_t)cur * d.m;
+  unsigned* cntT = d.cnt + 4;
+  for (unsigned j = w0; j < nA; j += nw) {
+    const unsigned b = __ldcg(A + j);
+    unsigned long long k1, k2;
+    seen += best_two(d, b, lane, k1, k2);
+    if (lane == 0) {
+      const unsigned long long dummy = make_key(d.dummy, kNone);
+      if (k1 > dummy) {
+        d.want[b] = kNone;   // the private dummy is strictly better: unmatched for good
+      } else {
+        const unsigned o = (unsigned)k1, price = __ldcg(d.price + o);
+        const unsigned second = (unsigned)(min(k2, dummy) >> 32), best = (unsigned)(k1 >> 32);
+        const unsigned offer = price + (second - best) + 1u;
+        const unsigned long long old = atomicMax(bidc + o, make_key(offer, kNone - b));
+        if (old == 0) d.touched[(size_t)cur * d.cap + atomicAdd(cntT + (k & 3u), 1u)] = o;
+        d.want[b] = o;
+        d.want_base[b] = (best - price) / d.scale;
+        ++bids;
+      }
+    }
+  }
+}
+
+// Resolve phase of round k over threads [t0, t0 + nt): each touched object
+// goes to its highest bid; the holders it displaces and the round's losing
+// bidders form the next round's active list; the previous round's bid slots
+// are cleared. Returns this thread's change of the held base-cost total and
+// of the number of held objects.
+__device__ __forceinline__ void resolve_phase(const AucDev& d, unsigned k, unsigned nA, unsigned t0, unsigned nt,
+                                              long long& dbase, long long& dmatched) {
+  const unsigned cur = k & 1u, nxt = cur ^ 1u;
+  unsigned* cntA = d.cnt;
+  unsigned* cntT = d.cnt + 4;
+  const unsigned nT = __ldcg(cntT + (k & 3u));
+  const unsigned* T = d.touched + (size_t)cur * d.cap;
+  const unsigned* A = d.act + (size_t)cur * d.n;
+  const unsigned long long* bidc = d.bid + (size_t)cur * d.m;
+  unsigned* N = d.act + (size_t)nxt * d.n;
+  for (unsigned t = t0; t < nT; t += nt) {
+    const unsigned o = __ldcg(T + t);
+    const unsigned long long key = __ldcg(bidc + o);
+    const unsigned w = kNone - (unsigned)key;
+    const int prev = __ldcg(d.owner + o);
+    const unsigned wb = __ldcg(d.want_base + w);
+    d.owner[o] = (int)w;
+    d.price[o] = (unsigned)(key >> 32);
+    d.assign[w] = (int)o;
+    d.held_base[w] = wb;
+    dbase += wb;
+    if (prev >= 0) {
+      d.assign[prev] = -1;
+      dbase -= __ldcg(d.held_base + prev);
+      N[atomicAdd(cntA + ((k + 1) & 3u), 1u)] = (unsigned)prev;
+    } else {
+      ++dmatched;
+    }
+  }
+  for (unsigned j = t0; j < nA; j += nt) {
+    const unsigned b = __ldcg(A + j);
+    const unsigned o = __ldcg(d.want + b);
+    if (o == kNone) continue;
+    if (kNone - (unsigned)__ldcg(bidc + o) != b) N[atomicAdd(cntA + ((k + 1) & 3u), 1u)] = b;
+  }
+  // the previous round's touched list is stable now: clear its bid slots
+  const unsigned nP = __ldcg(cntT + ((k + 3) & 3u));
+  const unsigned* P = d.touched + (size_t)nxt * d.cap;
+  unsigned long long* bidp = d.bid + (size_t)nxt * d.m;
+  for (unsigned t = t0; t < nP; t += nt) bidp[__ldcg(P + t)] = 0;
+}
+
+// Adds the block's changes of the held totals to the result (one atomic each
+// when nonzero).
+__device__ __forceinline__ void publish_totals(const AucDev& d, long long dbase, long long dmatched, long long* sh) {
+  if (threadIdx.x == 0) sh[0] = sh[1] = 0;
+  __syncthreads();
+  if (dbase) atomicAdd((unsigned long long*)&sh[0], (unsigned long long)dbase);
+  if (dmatched) atomicAdd((unsigned long long*)&sh[1], (unsigned long long)dmatched);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (sh[0]) atomicAdd(&d.out->total_base, (unsigned long long)sh[0]);
+    if (sh[1]) atomicAdd(&d.out->matched, (unsigned long long)sh[1]);
+  }
+}
+
 __global__ void __launch_bounds__(kAucThreads, kAucBlocksPerSm) k_auction(AucDev d) {
   __shared__ unsigned gen;
-  __shared__ int failed;
-  __shared__ unsigned long long s_bids, s_seen, s_base, s_unmatched;
+  __shared__ int failed, s_stop;
+  __shared__ unsigned long long s_bids, s_seen;
+  __shared__ long long s_tot[2];
   const int pb = blockIdx.x, np = gridDim.x;
   const int lane = threadIdx.x & 31;
   const unsigned gtid = pb * blockDim.x + threadIdx.x, gstride = np * blockDim.x;
@@ -177,7 +297,7 @@ __global__ void __launch_bounds__(kAucThreads, kAucBlocksPerSm) k_auction(AucDev
   unsigned* cntT = d.cnt + 4;
   if (threadIdx.x == 0) {
     gen = 0;
-    s_bids = s_seen = s_base = s_unmatched = 0;
+    s_bids = s_seen = 0;
   }
   // initial state: every bidder active in index order, prices zero
   for (unsigned o = gtid; o < d.m; o += gstride) {
@@ -191,111 +311,65 @@ __global__ void __launch_bounds__(kAucThreads, kAucBlocksPerSm) k_auction(AucDev
     d.want[b] = kNone;
     d.act[b] = b;
   }
-  if (d.grid) {   // where[o] = the (kind, tile) slot of BEL o (each BEL sits in one slot)
-    for (unsigned s = gtid; s < d.slots; s += gstride)
-      for (unsigned q = __ldg(d.tptr + s); q < __ldg(d.tptr + s + 1); ++q) d.where[__ldg(d.tobj + q)] = s;
-  }
   if (pb == 0 && threadIdx.x < 8) d.cnt[threadIdx.x] = threadIdx.x == 0 ? d.n : 0u;
   if (!grid_sync(d.bar, (unsigned)np, &gen, &nbar, nullptr, &failed)) return;
 
   unsigned k = 0;
+  bool tail = false;
   for (;; ++k) {
-    const unsigned cur = k & 1u, nxt = cur ^ 1u;
     const unsigned nA = __ldcg(cntA + (k & 3u));
     // block 0 may set the stop round during this round's bid phase; it names
     // the next round, so every block reads the same decision at each top
     const unsigned stop = __ldcg(&d.out->stop_round);
     if (nA == 0 || (stop != 0 && k >= stop)) break;
-    // ---- bid ----
+    // The active set never grows (a bidder wins, displacing at most one
+    // holder, loses or leaves), so once it fits one block that block
+    // finishes the auction alone, without grid barriers.
+    if (nA <= (unsigned)kAucWarps * kTailPerWarp) {
+      tail = true;
+      break;
+    }
     if (pb == 0 && threadIdx.x == 0) {
       cntA[(k + 2) & 3u] = 0;
       cntT[(k + 1) & 3u] = 0;
       if (now_ns() - t_start > kTimeLimitNs) d.out->stop_round = k + 1;
     }
-    const unsigned* A = d.act + (size_t)cur * d.n;
-    unsigned long long* bidc = d.bid + (size_t)cur * d.m;
-    for (unsigned j = gwarp; j < nA; j += nwarps) {
-      const unsigned b = __ldcg(A + j);
-      unsigned long long k1, k2;
-      my_seen += best_two(d, b, lane, k1, k2);
-      if (lane == 0) {
-        const unsigned long long dummy = make_key(d.dummy, kNone);
-        if (k1 > dummy) {
-          d.want[b] = kNone;   // the private dummy is strictly better: unmatched for good
-        } else {
-          const unsigned o = (unsigned)k1;
-          const unsigned second = (unsigned)(min(k2, dummy) >> 32);
-          const unsigned offer = __ldcg(d.price + o) + (second - (unsigned)(k1 >> 32)) + 1u;
-          const unsigned long long old = atomicMax(bidc + o, make_key(offer, kNone - b));
-          if (old == 0) d.touched[(size_t)cur * d.cap + atomicAdd(cntT + (k & 3u), 1u)] = o;
-          d.want[b] = o;
-          ++my_bids;
-        }
-      }
-    }
+    bid_phase(d, k, nA, gwarp, nwarps, lane, my_bids, my_seen);
     if (!grid_sync(d.bar, (unsigned)np, &gen, &nbar, nullptr, &failed)) return;
-    // ---- resolve ----
-    {
-      const unsigned nT = __ldcg(cntT + (k & 3u));
-      const unsigned* T = d.touched + (size_t)cur * d.cap;
-      unsigned* N = d.act + (size_t)nxt * d.n;
-      for (unsigned t = gtid; t < nT; t += gstride) {
-        const unsigned o = __ldcg(T + t);
-        const unsigned long long key = __ldcg(bidc + o);
-        const unsigned w = kNone - (unsigned)key;
-        const int prev = __ldcg(d.owner + o);
-        d.owner[o] = (int)w;
-        d.price[o] = (unsigned)(key >> 32);
-        d.assign[w] = (int)o;
-        if (prev >= 0) {
-          d.assign[prev] = -1;
-          N[atomicAdd(cntA + ((k + 1) & 3u), 1u)] = (unsigned)prev;
-        }
-      }
-      for (unsigned j = gtid; j < nA; j += gstride) {
-        const unsigned b = __ldcg(A + j);
-        const unsigned o = __ldcg(d.want + b);
-        if (o == kNone) continue;
-        if (kNone - (unsigned)__ldcg(bidc + o) != b) N[atomicAdd(cntA + ((k + 1) & 3u), 1u)] = b;
-      }
-      // clear the previous round's bid slots (its touched list is stable now)
-      const unsigned nP = __ldcg(cntT + ((k + 3) & 3u));
-      const unsigned* P = d.touched + (size_t)nxt * d.cap;
-      unsigned long long* bidp = d.bid + (size_t)nxt * d.m;
-      for (unsigned t = gtid; t < nP; t += gstride) bidp[__ldcg(P + t)] = 0;
-    }
+    long long dbase = 0, dmatched = 0;
+    resolve_phase(d, k, nA, gtid, gstride, dbase, dmatched);
+    publish_totals(d, dbase, dmatched, s_tot);
     if (!grid_sync(d.bar, (unsigned)np, &gen, &nbar, nullptr, &failed)) return;
   }
-
-  // totals: bids, candidates visited, unmatched bidders, matched base cost
-  unsigned long long base = 0, unmatched = 0;
-  for (unsigned b = gtid; b < d.n; b += gstride) {
-    const int o = __ldcg(d.assign + b);
-    if (o < 0) {
-      ++unmatched;
-      continue;
-    }
-    if (d.grid) {
-      const unsigned t = __ldcg(d.where + o) % (d.W * d.H);
-      const int x = (int)(t % d.W), y = (int)(t / d.W);
-      const int tx = (int)__ldg(d.txy + 2 * b), ty = (int)__ldg(d.txy + 2 * b + 1);
-      base += (unsigned)(abs(x - tx) + abs(y - ty));
-    } else {
-      for (unsigned q = __ldg(d.dptr + b); q < __ldg(d.dptr + b + 1); ++q)
-        if (__ldg(d.dobj + q) == (unsigned)o) base += __ldg(d.dcost + q);
+  const unsigned grid_rounds = k;
+  if (tail && pb == 0) {
+    for (;; ++k) {
+      const unsigned nA = __ldcg(cntA + (k & 3u));
+      if (threadIdx.x == 0) {
+        s_stop = now_ns() - t_start > kTimeLimitNs;
+        if (s_stop) d.out->stop_round = k + 1;
+        cntA[(k + 2) & 3u] = 0;
+        cntT[(k + 1) & 3u] = 0;
+      }
+      __syncthreads();
+      if (nA == 0 || s_stop) break;
+      bid_phase(d, k, nA, threadIdx.x >> 5, kAucWarps, lane, my_bids, my_seen);
+      __syncthreads();
+      long long dbase = 0, dmatched = 0;
+      resolve_phase(d, k, nA, threadIdx.x, blockDim.x, dbase, dmatched);
+      publish_totals(d, dbase, dmatched, s_tot);   // ends with the block barrier the next round needs
     }
   }
   atomicAdd(&s_bids, my_bids);
   atomicAdd(&s_seen, my_seen);
-  atomicAdd(&s_base, base);
-  atomicAdd(&s_unmatched, unmatched);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&d.out->bids, s_bids);
     atomicAdd(&d.out->examined, s_seen);
-    atomicAdd(&d.out->total_base, s_base);
-    atomicAdd(&d.out->unmatched, s_unmatched);
-    if (pb == 0) d.out->rounds = k;
+    if (pb == 0) {
+      d.out->rounds = k;
+      d.out->tail_rounds = k - grid_rounds;
+    }
   }
 }
 
@@ -390,7 +464,7 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
   const size_t sz_touch = round(2 * cap * 4), sz_nnz = round(std::max<uint64_t>(nnz, 1) * 4);
   const size_t sz_ptr = round(((h.grid ? slots : n) + 1) * 4);
   const size_t sz_occ = round(h.occ ? m : 1), sz_txy = round(2 * std::max<uint64_t>(n, 1) * 4);
-  const size_t total = 3 * sz_m4 + sz_bid + 3 * sz_n4 + sz_act + sz_touch + 2 * sz_nnz + sz_ptr + sz_occ + sz_txy +
+  const size_t total = 2 * sz_m4 + sz_bid + 5 * sz_n4 + sz_act + sz_touch + 2 * sz_nnz + sz_ptr + sz_occ + sz_txy +
                        round(32) + round(sizeof(GridBarrier)) + round(sizeof(AucResult));
   cudaStream_t s = nullptr;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
@@ -414,10 +488,11 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
   d.dummy = dummy;
   d.price = (unsigned*)take(sz_m4);
   d.owner = (int*)take(sz_m4);
-  d.where = (unsigned*)take(sz_m4);
   d.bid = (unsigned long long*)take(sz_bid);
   d.assign = (int*)take(sz_n4);
   d.want = (unsigned*)take(sz_n4);
+  d.want_base = (unsigned*)take(sz_n4);
+  d.held_base = (unsigned*)take(sz_n4);
   unsigned* kind = (unsigned*)take(sz_n4);
   d.act = (unsigned*)take(sz_act);
   d.touched = (unsigned*)take(sz_touch);
@@ -498,7 +573,8 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
     st->cost_scale = h.scale;
     st->bids = res.bids;
     st->candidates_examined = res.examined;
-    st->unmatched = res.unmatched;
+    st->tail_rounds = res.tail_rounds;
+    st->unmatched = (uint64_t)h.n - res.matched;
     st->total_base_cost = res.total_base;
     st->elapsed_ms = ms;
     st->kernel_launches = 1;
@@ -556,7 +632,7 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
   if (num_bidders == 0) return fail_with(stats, TEXO_GP_OK, "");   // auction_units' empty case (mod.rs:744-747)
   if (width == 0 || height == 0 || num_kinds == 0 || !tile_ptr || !bidder_kind || !target_xy || !assignment)
     return fail_with(stats, TEXO_GP_ERR_INVALID_ARGUMENT, "auction: empty grid or null argument");
-  if ((uint64_t)width * height > (1ull << 28) || (uint64_t)width + height > (1ull << 20) ||
+  if ((uint64_t)width * height > (1ull << 28) || width > 16384 || height > 16384 ||
       (uint64_t)num_kinds * width * height >= (1ull << 32))
     return fail_with(stats, TEXO_GP_ERR_INVALID_ARGUMENT, "auction: BEL grid too large");
   const uint64_t slots = (uint64_t)num_kinds * width * height;
