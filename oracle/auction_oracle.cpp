@@ -13,6 +13,8 @@
 //
 // The auction is the reference's: one bidder at a time from a FIFO queue,
 // epsilon one, a private dummy of cost n * max_base_cost + n + 1 per bidder.
+// A second driver, assign_jacobi, restates the parallel rounds the GPU runs
+// with the same searches, so the GPU's result can be checked bit for bit.
 #include <cstdint>
 #include <cstring>
 #include <deque>
@@ -131,6 +133,91 @@ int32_t assign_fifo(uint64_t n, uint64_t m, uint64_t max_base_cost, uint64_t sca
   return 0;
 }
 
+// The parallel (Jacobi) form of the same auction, the rule the GPU runs:
+// every active bidder bids at the prices of the round's start; each object
+// bid on goes to its highest offer (equal offers: the lower bidder index) at
+// the offered price; its previous holder and the losing bidders form the
+// next round's active set. Bidders whose best option is their dummy leave.
+// The outcome of a round depends only on the active set, so this sequential
+// restatement gives the GPU's assignment, prices, rounds and bids exactly.
+template <class Search>
+int32_t assign_jacobi(uint64_t n, uint64_t m, uint64_t max_base_cost, uint64_t scale, Search&& search,
+                      int32_t* assignment, uint64_t* prices_out, orc_auction_stats* st, uint64_t* rounds_out) {
+  orc_auction_stats s{};
+  uint64_t rounds = 0;
+  if (n == 0) {
+    if (st) *st = s;
+    if (rounds_out) *rounds_out = 0;
+    return 0;
+  }
+  uint64_t dummy = 0, tmp = 0, top = 0;
+  if (scale == 0 || mul_overflows(scale, max_base_cost, &top) || mul_overflows(n, top, &dummy) ||
+      add_overflows(dummy, n, &dummy) || add_overflows(dummy, 1, &dummy) || add_overflows(dummy, 1, &tmp) ||
+      add_overflows(tmp, top, &tmp))
+    return TEXO_GP_ERR_AUCTION_RANGE;
+  std::vector<uint64_t> prices(m, 0), best_offer(m, 0);
+  std::vector<int64_t> owners(m, -1), winner(m, -1), assign(n, -1);
+  std::vector<uint64_t> held_base(n, 0), want_base(n, 0);
+  std::vector<int64_t> want(n, -1);
+  std::vector<uint64_t> active(n), next, touched;
+  for (uint64_t b = 0; b < n; ++b) active[b] = b;
+  while (!active.empty()) {
+    ++rounds;
+    touched.clear();
+    for (uint64_t bidder : active) {
+      BestTwo real = search(bidder, prices);
+      s.examined += real.examined;
+      const Priced dummy_choice{UINT64_MAX, max_base_cost, dummy};
+      if (!real.has_best || key_less(dummy_choice, real.best)) {
+        want[bidder] = -1;
+        continue;
+      }
+      const Priced second = (!real.has_second || key_less(dummy_choice, real.second)) ? dummy_choice : real.second;
+      const uint64_t o = real.best.object;
+      const uint64_t offer = prices[o] + (second.reduced - real.best.reduced) + 1;
+      if (winner[o] < 0) touched.push_back(o);
+      if (winner[o] < 0 || offer > best_offer[o] || (offer == best_offer[o] && (int64_t)bidder < winner[o])) {
+        best_offer[o] = offer;
+        winner[o] = (int64_t)bidder;
+      }
+      want[bidder] = (int64_t)o;
+      want_base[bidder] = real.best.base;
+      s.bids++;
+    }
+    next.clear();
+    for (uint64_t o : touched) {
+      const int64_t w = winner[o], prev = owners[o];
+      owners[o] = w;
+      prices[o] = best_offer[o];
+      assign[w] = (int64_t)o;
+      held_base[w] = want_base[w];
+      if (prev >= 0) {
+        assign[prev] = -1;
+        next.push_back((uint64_t)prev);
+      }
+    }
+    for (uint64_t bidder : active)
+      if (want[bidder] >= 0 && winner[want[bidder]] != (int64_t)bidder) next.push_back(bidder);
+    for (uint64_t o : touched) {
+      winner[o] = -1;
+      best_offer[o] = 0;
+    }
+    active.swap(next);
+  }
+  for (uint64_t b = 0; b < n; ++b) {
+    assignment[b] = (int32_t)assign[b];
+    if (assign[b] < 0)
+      s.unmatched++;
+    else
+      s.total_base_cost += held_base[b];
+  }
+  if (prices_out)
+    for (uint64_t o = 0; o < m; ++o) prices_out[o] = prices[o];
+  if (st) *st = s;
+  if (rounds_out) *rounds_out = rounds;
+  return 0;
+}
+
 // Up-front checks shared by both searches: objects in range, none listed twice.
 int32_t check_objects(const uint32_t* objects, uint64_t count, uint32_t m, std::vector<uint32_t>& stamp,
                       uint32_t mark) {
@@ -204,7 +291,8 @@ int32_t check_grid(const Grid& g, uint32_t m, uint32_t n, const uint32_t* kind, 
 
 extern "C" int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_base_cost, uint32_t cost_scale,
                                         const uint32_t* ptr, const uint32_t* object, const uint64_t* cost,
-                                        int32_t* assignment, uint64_t* prices, orc_auction_stats* st) {
+                                        int32_t* assignment, uint64_t* prices, orc_auction_stats* st,
+                                        uint64_t* rounds) {
   if (st) std::memset(st, 0, sizeof(*st));
   if (n && (!ptr || !assignment || ptr[0] != 0)) return TEXO_GP_ERR_INVALID_ARGUMENT;
   std::vector<uint32_t> stamp(m, 0);
@@ -223,6 +311,7 @@ extern "C" int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_bas
     }
     return r;
   };
+  if (rounds) return assign_jacobi(n, m, max_base_cost, cost_scale, search, assignment, prices, st, rounds);
   return assign_fifo(n, m, max_base_cost, cost_scale, search, assignment, prices, st);
 }
 
@@ -230,7 +319,7 @@ extern "C" int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint3
                                           const uint32_t* tile_object, uint32_t num_objects, const uint8_t* occupied,
                                           uint32_t num_bidders, const uint32_t* bidder_kind,
                                           const uint32_t* target_xy, uint32_t cost_scale, int32_t* assignment,
-                                          uint64_t* prices, orc_auction_stats* st) {
+                                          uint64_t* prices, orc_auction_stats* st, uint64_t* rounds) {
   if (st) std::memset(st, 0, sizeof(*st));
   const Grid g{width, height, num_kinds, tile_ptr, tile_object, occupied};
   if (int32_t e = check_grid(g, num_objects, num_bidders, bidder_kind, target_xy)) return e;
@@ -251,6 +340,8 @@ extern "C" int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint3
     }
     return r;
   };
+  if (rounds)
+    return assign_jacobi(num_bidders, num_objects, max_base_cost, cost_scale, search, assignment, prices, st, rounds);
   return assign_fifo(num_bidders, num_objects, max_base_cost, cost_scale, search, assignment, prices, st);
 }
 

@@ -88,14 +88,18 @@ class AuctionStats(C.Structure):
                 ("total_base_cost", C.c_uint64)]
 
 
-def _stats(st):
-    return {"bids": st.bids, "candidates_examined": st.examined, "unmatched": st.unmatched,
-            "total_base_cost": st.total_base_cost}
+def _stats(st, rounds=None):
+    out = {"bids": st.bids, "candidates_examined": st.examined, "unmatched": st.unmatched,
+           "total_base_cost": st.total_base_cost}
+    if rounds is not None:
+        out["rounds"] = rounds
+    return out
 
 
-def auction_explicit(domains, object_count, max_base_cost, cost_scale=1):
+def auction_explicit(domains, object_count, max_base_cost, cost_scale=1, jacobi=False):
     """assign_implicitly with explicit_best_two (auction.rs:131-272), one
-    bidder at a time, base costs times `cost_scale` (1 in the reference):
+    bidder at a time (or, with jacobi=True, all active bidders each round as
+    the GPU bids), base costs times `cost_scale` (1 in the reference):
     (code, assignment with -1 for the dummy, prices, stats)."""
     n = len(domains)
     ptr = np.zeros(n + 1, dtype=np.uint32)
@@ -106,10 +110,11 @@ def auction_explicit(domains, object_count, max_base_cost, cost_scale=1):
     a = np.full(max(n, 1), -1, dtype=np.int32)
     pr = np.zeros(max(object_count, 1), dtype=np.uint64)
     st = AuctionStats()
+    rounds = C.c_uint64()
     code = lib().orc_auction_explicit(n, object_count, max_base_cost, cost_scale, P(ptr, C.c_uint32),
-                                      P(obj, C.c_uint32),
-                                      P(cost, C.c_uint64), P(a, C.c_int32), P(pr, C.c_uint64), C.byref(st))
-    return code, a[:n], pr[:object_count], _stats(st)
+                                      P(obj, C.c_uint32), P(cost, C.c_uint64), P(a, C.c_int32), P(pr, C.c_uint64),
+                                      C.byref(st), C.byref(rounds) if jacobi else None)
+    return code, a[:n], pr[:object_count], _stats(st, rounds.value if jacobi else None)
 
 
 def _grid_args(grid):
@@ -120,9 +125,10 @@ def _grid_args(grid):
             None if occ is None else P(occ, C.c_uint8))
 
 
-def auction_singletons(grid, bidder_kind, targets, cost_scale=1):
+def auction_singletons(grid, bidder_kind, targets, cost_scale=1, jacobi=False):
     """auction_singletons with the ring walk (legalization/mod.rs:657-1021),
-    one bidder at a time, base costs times `cost_scale` (1 in the reference):
+    one bidder at a time (or, with jacobi=True, in the GPU's parallel
+    rounds), base costs times `cost_scale` (1 in the reference):
     (code, assignment, prices, stats)."""
     kind = np.ascontiguousarray(bidder_kind, dtype=np.uint32).reshape(-1)
     txy = np.ascontiguousarray(targets, dtype=np.uint32).reshape(-1)
@@ -130,11 +136,12 @@ def auction_singletons(grid, bidder_kind, targets, cost_scale=1):
     a = np.full(max(n, 1), -1, dtype=np.int32)
     pr = np.zeros(max(grid.num_objects, 1), dtype=np.uint64)
     st = AuctionStats()
+    rounds = C.c_uint64()
     code = lib().orc_auction_singletons(*_grid_args(grid), n, P(kind if n else np.zeros(1, np.uint32), C.c_uint32),
                                         P(txy if n else np.zeros(2, np.uint32), C.c_uint32), cost_scale,
-                                        P(a, C.c_int32),
-                                        P(pr, C.c_uint64), C.byref(st))
-    return code, a[:n], pr[:grid.num_objects], _stats(st)
+                                        P(a, C.c_int32), P(pr, C.c_uint64), C.byref(st),
+                                        C.byref(rounds) if jacobi else None)
+    return code, a[:n], pr[:grid.num_objects], _stats(st, rounds.value if jacobi else None)
 
 
 def auction_certificate(grid, bidder_kind, targets, assignment, prices, dual=False, cost_scale=1):
@@ -212,11 +219,11 @@ def lib():
                                                 C.POINTER(PcgStats)]),
             "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),
             "orc_auction_explicit": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, c_u32p, c_u32p,
-                                                 c_u64p,
-                                                 C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
+                                                 c_u64p, C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats),
+                                                 c_u64p]),
             "orc_auction_singletons": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p, C.c_uint32,
                                                    C.POINTER(C.c_uint8), C.c_uint32, c_u32p, c_u32p, C.c_uint32,
-                                                   C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats)]),
+                                                   C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats), c_u64p]),
             "orc_auction_check_singletons": (C.c_int64, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, c_u32p,
                                                          C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32, c_u32p,
                                                          c_u32p, C.c_uint32, C.POINTER(C.c_int32), c_u32p, c_u64p,

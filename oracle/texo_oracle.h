@@ -180,10 +180,14 @@ typedef struct orc_auction_stats {
 /* assign_implicitly (legalization/auction.rs:131-247) driven by the explicit
  * best-two search of the reference's tests (auction.rs:253-272), base costs
  * multiplied by `cost_scale` (1 in the reference). Returns 0 or a
- * TEXO_GP_ERR_AUCTION_* code; `prices` (may be NULL) gets m prices. */
+ * TEXO_GP_ERR_AUCTION_* code; `prices` (may be NULL) gets m prices. With
+ * `rounds` NULL the bidders bid one at a time from the FIFO queue (the
+ * reference); otherwise all active bidders bid each round (the GPU's rule)
+ * and *rounds receives the number of rounds. */
 int32_t orc_auction_explicit(uint32_t n, uint32_t m, uint64_t max_base_cost, uint32_t cost_scale,
                              const uint32_t* ptr, const uint32_t* object, const uint64_t* cost,
-                             int32_t* assignment, uint64_t* prices, orc_auction_stats* stats);
+                             int32_t* assignment, uint64_t* prices, orc_auction_stats* stats,
+                             uint64_t* rounds);
 /* auction_singletons (legalization/mod.rs:657-677, 733-840) with the ring
  * walk of best_objects_on_cached_rings (mod.rs:876-1021); the layout of
  * texo_gp_auction_singletons. */
@@ -191,7 +195,7 @@ int32_t orc_auction_singletons(uint32_t width, uint32_t height, uint32_t num_kin
                                const uint32_t* tile_object, uint32_t num_objects, const uint8_t* occupied,
                                uint32_t num_bidders, const uint32_t* bidder_kind, const uint32_t* target_xy,
                                uint32_t cost_scale, int32_t* assignment, uint64_t* prices,
-                               orc_auction_stats* stats);
+                               orc_auction_stats* stats, uint64_t* rounds);
 /* The epsilon-complementary-slackness certificate of a singleton result:
  * returns the number of violations (-1 for malformed input); `dual_bound`
  * (may be NULL) the assignment dual at these prices, a lower bound on the

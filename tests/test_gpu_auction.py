@@ -125,6 +125,36 @@ def test_singletons_against_optimum_oracle_and_certificate(seed, shape, scale):
     assert again.stats["rounds"] == r.stats["rounds"] and again.stats["bids"] == r.stats["bids"]
 
 
+@pytest.mark.parametrize("scale", [1, 8])
+@pytest.mark.parametrize("seed,shape", list(enumerate(GRIDS)))
+def test_singletons_bit_exact_against_the_parallel_restatement(seed, shape, scale):
+    """The oracle's restatement of the GPU's parallel rounds (the same ring
+    walk and bid rule, every active bidder bidding at the round's prices)
+    gives the same assignment, prices, rounds and bids bit for bit."""
+    w, h, k, cap, n, occ = shape
+    grid, kind, xy = random_grid(seed, w, h, k, cap, n, occ)
+    r = legalize.auction_singletons(grid, kind, xy, cost_scale=scale)
+    code, a, prices, st = ffi.auction_singletons(grid, kind, xy, cost_scale=scale, jacobi=True)
+    assert code == 0
+    assert np.array_equal(r.assignment, a)
+    assert np.array_equal(r.prices.astype(np.uint64), prices)
+    assert (r.stats["rounds"], r.stats["bids"]) == (st["rounds"], st["bids"])
+    assert (r.stats["unmatched"], r.stats["total_base_cost"]) == (st["unmatched"], st["total_base_cost"])
+
+
+def test_explicit_bit_exact_against_the_parallel_restatement():
+    for nb, no, max_cost, all_costs in exhaustive_families():
+        costs = all_costs[:2048]
+        domains = [[(i * no + o, int(c)) for o, c in enumerate(costs[i, b]) if c >= 0]
+                   for i in range(len(costs)) for b in range(nb)]
+        for scale in (1, 2):
+            r = legalize.assign_implicitly(domains, len(costs) * no, max_cost, cost_scale=scale)
+            code, a, prices, st = ffi.auction_explicit(domains, len(costs) * no, max_cost, scale, jacobi=True)
+            assert code == 0
+            assert np.array_equal(r.assignment, a) and np.array_equal(r.prices.astype(np.uint64), prices)
+            assert (r.stats["rounds"], r.stats["bids"]) == (st["rounds"], st["bids"])
+
+
 def test_singleton_edge_cases():
     ones = np.ones((1, 4, 4), dtype=np.int64)
     grid = legalize.site_grid(ones)
@@ -176,5 +206,9 @@ def test_singletons_on_the_42k_placement():
         assert bad == 0, first
         assert int(base.sum()) == r.stats["total_base_cost"]
         assert abs(ost["total_base_cost"] - r.stats["total_base_cost"]) <= n
+        # bit for bit the oracle's restatement of the parallel rounds
+        code, ja, jp, jst = ffi.auction_singletons(grid, kind, xy, cost_scale=s, jacobi=True)
+        assert code == 0 and np.array_equal(r.assignment, ja) and np.array_equal(r.prices.astype(np.uint64), jp)
+        assert (r.stats["rounds"], r.stats["bids"]) == (jst["rounds"], jst["bids"])
     # the default (scaled) result moves the units less than the reference's setting does
     assert r.stats["cost_scale"] == 8 and r.stats["total_base_cost"] <= ost["total_base_cost"]

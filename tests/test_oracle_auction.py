@@ -110,6 +110,31 @@ def test_scaled_costs_tighten_the_bound(scale):
         assert np.array_equal(q_unmatched, unmatched) and np.all(q_cost <= optimum + nb / scale)
 
 
+@pytest.mark.parametrize("scale", [1, 8])
+def test_parallel_rounds_keep_the_guarantees(scale):
+    """The restatement of the GPU's parallel rounds: maximum cardinality,
+    cost within n / s of the optimum and a clean certificate, like the
+    one-at-a-time auction."""
+    for seed, shape in enumerate(GRIDS):
+        w, h, k, cap, n, occ = shape
+        grid, kind, xy = random_grid(seed, w, h, k, cap, n, occ)
+        code, a, prices, st = ffi.auction_singletons(grid, kind, xy, cost_scale=scale, jacobi=True)
+        assert code == 0 and st["rounds"] >= 1
+        unmatched, optimum = grid_optimum(grid, kind, xy)
+        assert st["unmatched"] == unmatched
+        assert optimum <= st["total_base_cost"] <= optimum + n / scale
+        bad, first, _ = ffi.auction_certificate(grid, kind, xy, a, prices.astype(np.uint32), cost_scale=scale)
+        assert bad == 0, first
+    for nb, no, max_cost, costs in exhaustive_families():
+        unmatched, optimum = brute_force(costs[:512])
+        got = np.array([ffi.auction_explicit(domains_of(c), no, max_cost, scale, jacobi=True)[1]
+                        for c in costs[:512]]).reshape(-1, nb)
+        q_unmatched, q_cost = quality(costs[:512], got)
+        assert np.array_equal(q_unmatched, unmatched) and np.all(q_cost <= optimum + nb / scale)
+    code, a, _, st = ffi.auction_explicit(KNOWN_ANSWERS[0][1], 3, 100, 1, jacobi=True)
+    assert code == 0 and list(a) == KNOWN_ANSWERS[0][4]
+
+
 def test_certificate_catches_planted_mistakes():
     grid, kind, xy = random_grid(7, 14, 12, 1, 1, 120, 0.0)
     code, a, prices, _ = ffi.auction_singletons(grid, kind, xy)
