@@ -91,7 +91,7 @@ __device__ __forceinline__ unsigned long long make_key(unsigned reduced, unsigne
   return ((unsigned long long)reduced << 32) | object;
 }
 
-// best two of (a1 <= a2) and (b1 <= b2); real keys are distinct
+// best two of (a1 <= a2) and (b1 <= b2), drawn from disjoint candidate sets
 __device__ __forceinline__ void merge2(unsigned long long& a1, unsigned long long& a2, unsigned long long b1,
                                        unsigned long long b2) {
   const unsigned long long lo = a1 < b1 ? a1 : b1, hi = a1 < b1 ? b1 : a1;
@@ -153,6 +153,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const unsigned* tp = d.tptr + (size_t)__ldg(d.kind + b) * d.W * d.H;
     const unsigned R = d.max_radius;
     const unsigned total = 1u + 2u * R * (R + 1u);   // points of the whole diamond
+    unsigned long long m1 = kNoKey, m2 = kNoKey;
     for (unsigned p0 = 0;; p0 += 32) {
       const unsigned p = p0 + lane;
       if (p < total) {
@@ -177,14 +178,21 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
           }
         }
       }
-      warp_best2(a1, a2);
+      // the warp's best two so far, merged from copies: each lane keeps the
+      // best two of the points it visited itself, so the merge always joins
+      // disjoint candidate sets
+      m1 = a1;
+      m2 = a2;
+      warp_best2(m1, m2);
       const unsigned last = min(p0 + 32u, total) - 1u;
       if (last == total - 1u) break;   // every ring seen
       const unsigned rl = ring_of(last);
       const unsigned unseen = last == 2u * rl * (rl + 1u) ? rl + 1u : rl;   // first ring not fully seen
       // strict: an unseen object could tie the second best
-      if (a2 != kNoKey && (unsigned)(a2 >> 32) < d.scale * unseen) break;
+      if (m2 != kNoKey && (unsigned)(m2 >> 32) < d.scale * unseen) break;
     }
+    a1 = m1;
+    a2 = m2;
   }
   k1 = a1;
   k2 = a2;
