@@ -631,7 +631,8 @@ def auction_report(reps=5):
         st = best.stats
         bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices, cost_scale=st["cost_scale"])
         return {"cost_scale": st["cost_scale"], "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls),
-                "rounds": st["rounds"], "bids": st["bids"], "candidates_examined": st["candidates_examined"],
+                "rounds": st["rounds"], "tail_rounds": st["tail_rounds"], "bids": st["bids"],
+                "candidates_examined": st["candidates_examined"],
                 "unmatched": st["unmatched"], "total_displacement": st["total_base_cost"],
                 "mean_displacement": st["total_base_cost"] / max(n, 1),
                 "deterministic_over_reps": all(np.array_equal(r.assignment, best.assignment) for r in runs),
