@@ -598,61 +598,73 @@ def rudy_report(reps=5):
     return out
 
 
-def auction_report(reps=5):
+def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
     """The single-BEL capacity auction of the legalizer (`assign_implicitly`,
     legalization/auction.rs:131-247, with the ring walk of mod.rs:876-1021)
-    on the rounded targets of the 42k-cell placement (device engine): the
-    GPU's Jacobi auction (device time with the copies, best of `reps`)
-    against the oracle's one-bidder-at-a-time auction on one host core, with
-    the epsilon-optimality certificate of the GPU result."""
+    on the rounded targets of each workload's placement (the 42k workload on
+    the device engine, 1M cells on the host engine): the GPU's parallel
+    auction (device time with the copies, best of `reps`) at the default and
+    at the reference's cost scale, against the oracle's one-bidder-at-a-time
+    auction on one host core, with the epsilon-optimality certificate of each
+    GPU result."""
     import numpy as np
     from oracle import ffi
     from texo_gb300 import abi, legalize
     from texo_gb300.placer import Placer
-    prob = make_problem("lfe5u-85-42k", 0)
-    with Placer(prob, make_params("lfe5u-85-42k", abi.ENGINE_DEVICE, abi.DCT_FP32)) as g:
-        targets, _, _ = g.run(allow_nonconverged=True)
-    lo = prob.lower_xy.reshape(-1, 2)
-    hi = prob.upper_xy.reshape(-1, 2)
-    movable = np.nonzero(np.any(lo != hi, axis=1))[0]
-    grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
-    kind = np.zeros(len(movable), np.uint32)
-    xy = np.ascontiguousarray(targets[movable])
-    n = len(movable)
+    out = {}
+    for name in workloads:
+        prob = make_problem(name, 0)
+        engine = abi.ENGINE_DEVICE if name == "lfe5u-85-42k" else abi.ENGINE_HOST
+        with Placer(prob, make_params(name, engine, abi.DCT_FP32)) as g:
+            targets, _, _ = g.run(allow_nonconverged=True)
+        lo = prob.lower_xy.reshape(-1, 2)
+        hi = prob.upper_xy.reshape(-1, 2)
+        movable = np.nonzero(np.any(lo != hi, axis=1))[0]
+        grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
+        kind = np.zeros(len(movable), np.uint32)
+        xy = np.ascontiguousarray(targets[movable])
+        n = len(movable)
 
-    def gpu(scale):
-        legalize.auction_singletons(grid, kind, xy, cost_scale=scale)   # warm-up
-        runs, walls = [], []
-        for _ in range(reps):
+        def gpu(scale):
+            legalize.auction_singletons(grid, kind, xy, cost_scale=scale)   # warm-up
+            runs, walls = [], []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                runs.append(legalize.auction_singletons(grid, kind, xy, cost_scale=scale))
+                walls.append(1000 * (time.perf_counter() - t0))
+            best = min(runs, key=lambda r: r.stats["elapsed_ms"])
+            st = best.stats
+            bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices,
+                                                cost_scale=st["cost_scale"])
+            return {"cost_scale": st["cost_scale"], "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls),
+                    "rounds": st["rounds"], "tail_rounds": st["tail_rounds"], "bids": st["bids"],
+                    "candidates_examined": st["candidates_examined"],
+                    "unmatched": st["unmatched"], "total_displacement": st["total_base_cost"],
+                    "mean_displacement": st["total_base_cost"] / max(n, 1),
+                    "deterministic_over_reps": all(np.array_equal(r.assignment, best.assignment) for r in runs),
+                    "certificate_violations": int(bad)}
+
+        def cpu(scale):
             t0 = time.perf_counter()
-            runs.append(legalize.auction_singletons(grid, kind, xy, cost_scale=scale))
-            walls.append(1000 * (time.perf_counter() - t0))
-        best = min(runs, key=lambda r: r.stats["elapsed_ms"])
-        st = best.stats
-        bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices, cost_scale=st["cost_scale"])
-        return {"cost_scale": st["cost_scale"], "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls),
-                "rounds": st["rounds"], "tail_rounds": st["tail_rounds"], "bids": st["bids"],
-                "candidates_examined": st["candidates_examined"],
-                "unmatched": st["unmatched"], "total_displacement": st["total_base_cost"],
-                "mean_displacement": st["total_base_cost"] / max(n, 1),
-                "deterministic_over_reps": all(np.array_equal(r.assignment, best.assignment) for r in runs),
-                "certificate_violations": int(bad)}
+            code, _, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
+            ms = 1000 * (time.perf_counter() - t0)
+            return {"cost_scale": scale, "cpu_ms": ms, "status": int(code), "bids": ost["bids"],
+                    "unmatched": ost["unmatched"], "total_displacement": ost["total_base_cost"]}
 
-    def cpu(scale):
-        t0 = time.perf_counter()
-        code, _, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
-        ms = 1000 * (time.perf_counter() - t0)
-        return {"cost_scale": scale, "cpu_ms": ms, "status": int(code), "bids": ost["bids"],
-                "unmatched": ost["unmatched"], "total_displacement": ost["total_base_cost"]}
-
-    default, like = gpu(0), gpu(1)
-    ref, ref_scaled = cpu(1), cpu(default["cost_scale"])
-    return {"workload": "lfe5u-85-42k", "bidders": int(n), "bels": int(grid.num_objects),
-            "grid": "%dx%d" % (prob.width, prob.height), "targets": "rounded targets of the device-engine placement",
-            "gpu": default, "gpu_reference_scale": like, "cpu_oracle": ref, "cpu_oracle_same_scale": ref_scaled,
-            "cores": 1, "speedup_vs_reference_setting": ref["cpu_ms"] / default["gpu_ms"],
-            "speedup_same_scale": ref_scaled["cpu_ms"] / default["gpu_ms"],
-            "displacement_vs_reference_setting": default["total_displacement"] / max(ref["total_displacement"], 1)}
+        default, like = gpu(0), gpu(1)
+        ref = cpu(1)
+        ref_scaled = cpu(default["cost_scale"]) if default["cost_scale"] != 1 else ref
+        out[name] = {"bidders": int(n), "bels": int(grid.num_objects),
+                     "grid": "%dx%d" % (prob.width, prob.height),
+                     "targets": "rounded targets of the %s-engine placement" % (
+                         "device" if engine == abi.ENGINE_DEVICE else "host"),
+                     "gpu": default, "gpu_reference_scale": like, "cpu_oracle": ref,
+                     "cpu_oracle_same_scale": ref_scaled, "cores": 1,
+                     "speedup_vs_reference_setting": ref["cpu_ms"] / default["gpu_ms"],
+                     "speedup_same_scale": ref_scaled["cpu_ms"] / default["gpu_ms"],
+                     "displacement_vs_reference_setting":
+                         default["total_displacement"] / max(ref["total_displacement"], 1)}
+    return out
 
 
 def precision_report(iterations=1000, seed=0, threads=5):
