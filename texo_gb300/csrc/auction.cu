@@ -132,8 +132,8 @@ __device__ __forceinline__ unsigned ring_of(unsigned p) {
 // The two least (reduced cost, object) keys among bidder b's candidates, the
 // same in every lane of the warp. Returns the candidates this lane visited.
 //
-// The ring walk hands the warp 128 consecutive points of the diamond at a
-// time and stops once the second best is below the least cost an unseen
+// The ring walk hands the warp 32, then 128 consecutive points of the diamond
+// at a time and stops once the second best is below the least cost an unseen
 // object can have, s times the first ring not fully seen. Visiting rings
 // past the reference's stopping ring adds only objects that cannot enter
 // the best two, so the result is the reference's exact best two.
@@ -155,9 +155,10 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const unsigned R = d.max_radius;
     const unsigned total = 1u + 2u * R * (R + 1u);   // points of the whole diamond
     unsigned long long m1 = kNoKey, m2 = kNoKey;
-    for (unsigned p0 = 0;; p0 += 32u * kWalkUnroll) {
-      // kWalkUnroll points a lane per pass, their loads issued together so
-      // that the dependent chains (tile range, BEL id, price) overlap
+    // the first pass takes one point a lane (most walks end there); later
+    // passes take kWalkUnroll points a lane, their loads issued together so
+    // that the dependent chains (tile range, BEL id, price) overlap
+    for (unsigned p0 = 0, span = 32u;; p0 += span, span = 32u * kWalkUnroll) {
       int t[kWalkUnroll];
       unsigned cost[kWalkUnroll], kb[kWalkUnroll], ke[kWalkUnroll], first[kWalkUnroll];
 #pragma unroll
@@ -165,7 +166,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
         const unsigned p = p0 + lane + 32u * u;
         t[u] = -1;
         cost[u] = 0;
-        if (p < total) {
+        if (32u * u < span && p < total) {
           const unsigned r = ring_of(p);
           int dx = 0, dy = 0;
           if (r) {
@@ -208,7 +209,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
       m1 = a1;
       m2 = a2;
       warp_best2(m1, m2);
-      const unsigned last = min(p0 + 32u * kWalkUnroll, total) - 1u;
+      const unsigned last = min(p0 + span, total) - 1u;
       if (last == total - 1u) break;   // every ring seen
       const unsigned rl = ring_of(last);
       const unsigned unseen = last == 2u * rl * (rl + 1u) ? rl + 1u : rl;   // first ring not fully seen
