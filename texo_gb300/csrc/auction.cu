@@ -46,7 +46,6 @@ constexpr int kAucThreads = 256;
 constexpr int kAucWarps = kAucThreads / 32;
 constexpr int kAucBlocksPerSm = 2;   // resident blocks a multiprocessor runs
 constexpr int kTailPerWarp = 2;      // active bidders per warp at which block 0 finishes alone
-constexpr int kWalkUnroll = 4;       // diamond points a lane takes per pass of the ring walk
 constexpr unsigned kNone = 0xFFFFFFFFu;
 constexpr unsigned long long kNoKey = ~0ull;                      // "no candidate"
 constexpr unsigned long long kTimeLimitNs = 20ull * 1000000000ull; // the whole auction
@@ -132,8 +131,8 @@ __device__ __forceinline__ unsigned ring_of(unsigned p) {
 // The two least (reduced cost, object) keys among bidder b's candidates, the
 // same in every lane of the warp. Returns the candidates this lane visited.
 //
-// The ring walk hands the warp 32, then 128 consecutive points of the diamond
-// at a time and stops once the second best is below the least cost an unseen
+// The ring walk hands the warp 32 consecutive points of the diamond at a
+// time and stops once the second best is below the least cost an unseen
 // object can have, s times the first ring not fully seen. Visiting rings
 // past the reference's stopping ring adds only objects that cannot enter
 // the best two, so the result is the reference's exact best two.
@@ -155,52 +154,28 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
     const unsigned R = d.max_radius;
     const unsigned total = 1u + 2u * R * (R + 1u);   // points of the whole diamond
     unsigned long long m1 = kNoKey, m2 = kNoKey;
-    // the first pass takes one point a lane (most walks end there); later
-    // passes take kWalkUnroll points a lane, their loads issued together so
-    // that the dependent chains (tile range, BEL id, price) overlap
-    for (unsigned p0 = 0, span = 32u;; p0 += span, span = 32u * kWalkUnroll) {
-      int t[kWalkUnroll];
-      unsigned cost[kWalkUnroll], kb[kWalkUnroll], ke[kWalkUnroll], first[kWalkUnroll];
-#pragma unroll
-      for (int u = 0; u < kWalkUnroll; ++u) {
-        const unsigned p = p0 + lane + 32u * u;
-        t[u] = -1;
-        cost[u] = 0;
-        if (32u * u < span && p < total) {
-          const unsigned r = ring_of(p);
-          int dx = 0, dy = 0;
-          if (r) {
-            // ring r as four quarter turns of (r - i, i)
-            const unsigned j = p - (1u + 2u * r * (r - 1u)), q = j / r, i = j - q * r;
-            const int a = (int)(r - i), c = (int)i;
-            dx = q == 0 ? a : q == 1 ? -c : q == 2 ? -a : c;
-            dy = q == 0 ? c : q == 1 ? a : q == 2 ? -c : -a;
-          }
-          const int x = tx + dx, y = ty + dy;
-          if (x >= 0 && y >= 0 && x < W && y < H) {
-            t[u] = y * W + x;
-            cost[u] = d.scale * r;
-          }
+    for (unsigned p0 = 0;; p0 += 32) {
+      const unsigned p = p0 + lane;
+      if (p < total) {
+        const unsigned r = ring_of(p);
+        int dx = 0, dy = 0;
+        if (r) {
+          // ring r as four quarter turns of (r - i, i)
+          const unsigned j = p - (1u + 2u * r * (r - 1u)), q = j / r, i = j - q * r;
+          const int u = (int)(r - i), v = (int)i;
+          dx = q == 0 ? u : q == 1 ? -v : q == 2 ? -u : v;
+          dy = q == 0 ? v : q == 1 ? u : q == 2 ? -v : -u;
         }
-      }
-#pragma unroll
-      for (int u = 0; u < kWalkUnroll; ++u) {
-        kb[u] = t[u] >= 0 ? __ldg(tp + t[u]) : 0u;
-        ke[u] = t[u] >= 0 ? __ldg(tp + t[u] + 1) : 0u;
-      }
-#pragma unroll
-      for (int u = 0; u < kWalkUnroll; ++u) first[u] = kb[u] < ke[u] ? __ldg(d.tobj + kb[u]) : kNone;
-#pragma unroll
-      for (int u = 0; u < kWalkUnroll; ++u) {
-        if (first[u] == kNone) continue;
-        ++seen;
-        if (!(d.occ && __ldg(d.occ + first[u])))
-          insert2(a1, a2, make_key(cost[u] + __ldcg(d.price + first[u]), first[u]));
-        for (unsigned k = kb[u] + 1; k < ke[u]; ++k) {   // tiles with several BELs of the kind
-          const unsigned o = __ldg(d.tobj + k);
-          ++seen;
-          if (d.occ && __ldg(d.occ + o)) continue;
-          insert2(a1, a2, make_key(cost[u] + __ldcg(d.price + o), o));
+        const int x = tx + dx, y = ty + dy;
+        if (x >= 0 && y >= 0 && x < W && y < H) {
+          const int t = y * W + x;
+          const unsigned ring_cost = d.scale * r, e = __ldg(tp + t + 1);
+          for (unsigned k = __ldg(tp + t); k < e; ++k) {
+            const unsigned o = __ldg(d.tobj + k);
+            ++seen;
+            if (d.occ && __ldg(d.occ + o)) continue;
+            insert2(a1, a2, make_key(ring_cost + __ldcg(d.price + o), o));
+          }
         }
       }
       // the warp's best two so far, merged from copies: each lane keeps the
@@ -209,7 +184,7 @@ __device__ __forceinline__ unsigned long long best_two(const AucDev& d, unsigned
       m1 = a1;
       m2 = a2;
       warp_best2(m1, m2);
-      const unsigned last = min(p0 + span, total) - 1u;
+      const unsigned last = min(p0 + 32u, total) - 1u;
       if (last == total - 1u) break;   // every ring seen
       const unsigned rl = ring_of(last);
       const unsigned unseen = last == 2u * rl * (rl + 1u) ? rl + 1u : rl;   // first ring not fully seen
