@@ -212,3 +212,27 @@ def test_singletons_on_the_42k_placement():
         assert (r.stats["rounds"], r.stats["bids"]) == (jst["rounds"], jst["bids"])
     # the default (scaled) result moves the units less than the reference's setting does
     assert r.stats["cost_scale"] == 8 and r.stats["total_base_cost"] <= ost["total_base_cost"]
+
+
+def test_project_singletons_on_a_problem_with_fixed_bels():
+    """From a placement problem and its targets to one BEL per unit: fixed
+    units' BELs are never handed out, every movable single-cell unit of the
+    48 x 48 workload gets a distinct LUT site, certified."""
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import Placer, default_params
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 0)
+    with Placer(prob, default_params(best_effort=1, max_iterations=1000, engine=abi.ENGINE_DEVICE)) as g:
+        targets, _, _ = g.run(allow_nonconverged=True)
+    bel, r, multi = legalize.project_singletons(prob, targets)
+    movable = np.any(prob.lower_xy != prob.upper_xy, axis=1)
+    assert len(multi) == 0 and r.stats["unmatched"] == 0
+    assert np.all(bel[movable] >= 0) and np.all(bel[~movable] == -1)
+    assert len(set(bel[movable].tolist())) == int(movable.sum())
+    # the same problem with some LUT sites held by fixed units
+    rng = np.random.default_rng(3)
+    taken = rng.choice(48 * 48, 200, replace=False)
+    fixed = np.stack([np.zeros(200, np.int64), taken % 48, taken // 48], axis=1)
+    prob.fixed_occupancy = np.ascontiguousarray(fixed.astype(np.uint32))
+    bel2, r2, _ = legalize.project_singletons(prob, targets)
+    assert r2.stats["unmatched"] == 0
+    assert not set(bel2[movable].tolist()) & set(taken.tolist())   # BEL id = site index for one BEL a site

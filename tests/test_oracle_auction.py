@@ -203,3 +203,17 @@ def test_site_grid_layout():
     assert where[3].tolist() == [0, 1, 1] and where[5].tolist() == [0, 1, 1]
     assert where[7].tolist() == [1, 1, 0]
     assert where[9].tolist() == [1, 0, 1]
+
+
+def test_fixed_occupancy_mask():
+    cap = np.array([[[1, 2], [0, 3]], [[1, 1], [1, 1]]])   # [field, y, x]
+    g = legalize.site_grid(cap)
+    # field 0: tile (1,0) holds BELs 1-2, tile (1,1) BELs 3-5; field 1: BELs 6-9
+    occ = legalize.fixed_occupancy_mask(g, [[0, 1, 1], [0, 1, 1], [1, 0, 0], [0, 1, 0]])
+    assert np.nonzero(occ)[0].tolist() == [1, 3, 4, 6]
+    assert not legalize.fixed_occupancy_mask(g, np.zeros((0, 3))).any()
+    with pytest.raises(abi.TexoGpError) as e:
+        legalize.fixed_occupancy_mask(g, [[0, 0, 1], [0, 0, 1]])   # tile (0,1) of field 0 has no BEL
+    assert e.value.code == abi.CODE["FIXED_CAPACITY_EXHAUSTED"]
+    with pytest.raises(abi.TexoGpError):
+        legalize.fixed_occupancy_mask(g, [[0, 2, 0]])

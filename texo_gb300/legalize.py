@@ -11,7 +11,10 @@ exposes the auction, which runs on the GPU through include/texo_gp.h:
 - `auction_singletons(grid, bidder_kind, targets)`: the single-BEL auction
   of `project` (`auction_singletons`, mod.rs:657-677), candidates found by
   Manhattan ring walks around each unit's target tile;
-- `SiteGrid` / `site_grid`: the BEL layout those walks read.
+- `SiteGrid` / `site_grid`: the BEL layout those walks read;
+- `project_singletons(problem, targets)`: the single-cell part of `project`
+  for a placement problem: fixed units' BELs occupied, singleton bidders,
+  the auction, one BEL per unit.
 
 The GPU bids all unassigned bidders at once each round; the result carries
 the reference's guarantees (exact maximum cardinality, total base cost at
@@ -145,3 +148,55 @@ def auction_singletons(grid, bidder_kind, targets, cost_scale=0, device=0):
                                              C.byref(st)),
               "texo_gp_auction_singletons")
     return AuctionResult(assignment[:n].copy(), prices[:grid.num_objects].copy(), _stats(st))
+
+
+def fixed_occupancy_mask(grid, fixed_occupancy):
+    """The BELs held by fixed units (`install_fixed_units`, legalization/mod.rs:
+    391-430) as an occupied mask: each (field, x, y) entry of a problem's
+    `fixed_occupancy` takes the first free BEL of that field at that tile.
+    Raises TexoGpError (FIXED_CAPACITY_EXHAUSTED, the reference's
+    ElectrostaticError) when a tile has more fixed entries than BELs."""
+    occ = np.zeros(grid.num_objects, dtype=np.uint8)
+    fo = np.asarray(fixed_occupancy, dtype=np.int64).reshape(-1, 3)
+    if len(fo) == 0:
+        return occ
+    tiles = grid.width * grid.height
+    if np.any(fo[:, 0] >= grid.num_kinds) or np.any(fo[:, 1] >= grid.width) or np.any(fo[:, 2] >= grid.height):
+        raise abi.TexoGpError(abi.CODE["POINT_OUTSIDE_GRID"], "fixed_occupancy_mask")
+    slot = fo[:, 0] * tiles + fo[:, 2] * grid.width + fo[:, 1]
+    order = np.argsort(slot, kind="stable")
+    s = slot[order]
+    first = np.r_[0, np.nonzero(np.diff(s))[0] + 1]
+    rank = np.arange(len(s)) - np.repeat(first, np.diff(np.r_[first, len(s)]))   # k-th entry of its slot
+    ptr = np.asarray(grid.tile_ptr, dtype=np.int64)
+    if np.any(ptr[s] + rank >= ptr[s + 1]):
+        raise abi.TexoGpError(abi.CODE["FIXED_CAPACITY_EXHAUSTED"], "fixed_occupancy_mask")
+    occ[np.asarray(grid.tile_object, dtype=np.int64)[ptr[s] + rank]] = 1
+    return occ
+
+
+def project_singletons(problem, targets, cost_scale=0, device=0):
+    """The single-cell part of `project` (legalization/mod.rs:322-389) for a
+    placement problem and its rounded targets [U, 2] (what `place` returns):
+    the BELs of each density field by tile from the problem's capacity grid,
+    those of fixed units occupied, every movable unit with one density member
+    a bidder of its member's field at its target (`classify_units`,
+    mod.rs:432-471), and the
+    single-BEL auction on the GPU. Returns (BEL id per unit: -1 for fixed
+    units, unmatched ones and the units this path leaves out; the auction
+    result; the movable multi-member units, which the reference places by its
+    shared-row auctions, not built here)."""
+    k = len(problem.fields)
+    cap = np.asarray(problem.capacity, dtype=np.int64).reshape(k, problem.height, problem.width)
+    grid = site_grid(cap)
+    grid.occupied = fixed_occupancy_mask(grid, problem.fixed_occupancy)
+    ptr = np.asarray(problem.member_ptr, dtype=np.int64)
+    members = np.diff(ptr)
+    movable = np.any(problem.lower_xy != problem.upper_xy, axis=1)
+    bidders = np.nonzero(movable & (members == 1))[0]
+    kind = np.asarray(problem.member_field, dtype=np.uint32)[ptr[bidders]]
+    xy = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32).reshape(-1, 2)[bidders])
+    result = auction_singletons(grid, kind, xy, cost_scale=cost_scale, device=device)
+    bel = np.full(problem.num_units, -1, dtype=np.int64)
+    bel[bidders] = result.assignment
+    return bel, result, np.nonzero(movable & (members > 1))[0]
