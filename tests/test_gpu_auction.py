@@ -236,3 +236,35 @@ def test_project_singletons_on_a_problem_with_fixed_bels():
     bel2, r2, _ = legalize.project_singletons(prob, targets)
     assert r2.stats["unmatched"] == 0
     assert not set(bel2[movable].tolist()) & set(taken.tolist())   # BEL id = site index for one BEL a site
+
+
+def test_singletons_bit_exact_at_one_million_cells():
+    """Full size: the 1M-cell workload's placement targets (host engine) bid
+    for the 1024 x 1024 sites; at the automatic scale (2: the largest whose
+    prices fit 32 bits) and at the reference's, the GPU's assignment, prices,
+    rounds and bids equal the parallel restatement's, the certificate holds,
+    and the matched cost is within n / s of the one-at-a-time auction's."""
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import Placer, default_params
+    prob = P.synthetic(1024, 1000000, 4096, 1200000, 24.0, 0)
+    params = default_params(bins_x=1024, bins_y=1024, target_density=0.9, gamma_base=4.0, max_iterations=1000,
+                            best_effort=1, engine=abi.ENGINE_HOST, dct_mode=abi.DCT_FP32)
+    with Placer(prob, params) as g:
+        targets, _, _ = g.run(allow_nonconverged=True)
+    bel, r, multi = legalize.project_singletons(prob, targets)
+    assert len(multi) == 0 and r.stats["unmatched"] == 0 and r.stats["cost_scale"] == 2
+    movable = np.nonzero(np.any(prob.lower_xy != prob.upper_xy, axis=1))[0]
+    grid = legalize.site_grid(prob.capacity[0].reshape(1, prob.height, prob.width))
+    kind = np.zeros(len(movable), np.uint32)
+    xy = np.ascontiguousarray(targets[movable])
+    for scale in (2, 1):
+        g = r if scale == 2 else legalize.auction_singletons(grid, kind, xy, cost_scale=1)
+        code, a, prices, st = ffi.auction_singletons(grid, kind, xy, cost_scale=scale, jacobi=True)
+        assert code == 0
+        assert np.array_equal(g.assignment, a) and np.array_equal(g.prices.astype(np.uint64), prices)
+        assert (g.stats["rounds"], g.stats["bids"]) == (st["rounds"], st["bids"])
+        bad, first, _ = ffi.auction_certificate(grid, kind, xy, g.assignment, g.prices, cost_scale=scale)
+        assert bad == 0, first
+        code, _, _, fifo = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
+        assert code == 0 and fifo["unmatched"] == 0
+        assert abs(fifo["total_base_cost"] - g.stats["total_base_cost"]) <= len(movable) / scale
