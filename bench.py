@@ -610,7 +610,7 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
     import numpy as np
     from oracle import ffi
     from texo_gb300 import abi, legalize
-    from texo_gb300.placer import Placer
+    from texo_gb300.placer import Placer, net_bounding_boxes
     out = {}
     for name in workloads:
         prob = make_problem(name, 0)
@@ -637,6 +637,7 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
             bad, _, _ = ffi.auction_certificate(grid, kind, xy, best.assignment, best.prices,
                                                 cost_scale=st["cost_scale"])
             return {"cost_scale": st["cost_scale"], "gpu_ms": st["elapsed_ms"], "gpu_wall_ms": min(walls),
+                    "hpwl_legal": hpwl(best.assignment),
                     "rounds": st["rounds"], "tail_rounds": st["tail_rounds"], "bids": st["bids"],
                     "candidates_examined": st["candidates_examined"],
                     "unmatched": st["unmatched"], "total_displacement": st["total_base_cost"],
@@ -646,10 +647,24 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
 
         def cpu(scale):
             t0 = time.perf_counter()
-            code, _, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
+            code, a, _, ost = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
             ms = 1000 * (time.perf_counter() - t0)
             return {"cost_scale": scale, "cpu_ms": ms, "status": int(code), "bids": ost["bids"],
+                    "hpwl_legal": hpwl(a) if code == 0 else None,
                     "unmatched": ost["unmatched"], "total_displacement": ost["total_base_cost"]}
+
+        def hpwl(assignment):
+            # half-perimeter wirelength over the nets between units with every
+            # movable unit at the tile of its BEL (net_bounding_boxes' nets)
+            pos = np.array(prob.lower_xy, dtype=np.float64).reshape(-1, 2)
+            if assignment is None:
+                pos[movable] = xy
+            else:
+                where = grid.bel_tiles()
+                pos[movable, 0] = where[assignment, 1]
+                pos[movable, 1] = where[assignment, 2]
+            b = net_bounding_boxes(prob, pos)
+            return float(np.sum(b[:, 1] - b[:, 0]) + np.sum(b[:, 3] - b[:, 2]))
 
         default, like = gpu(0), gpu(1)
         ref = cpu(1)
@@ -658,6 +673,7 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
                      "grid": "%dx%d" % (prob.width, prob.height),
                      "targets": "rounded targets of the %s-engine placement" % (
                          "device" if engine == abi.ENGINE_DEVICE else "host"),
+                     "hpwl_targets": hpwl(None),
                      "gpu": default, "gpu_reference_scale": like, "cpu_oracle": ref,
                      "cpu_oracle_same_scale": ref_scaled, "cores": 1,
                      "speedup_vs_reference_setting": ref["cpu_ms"] / default["gpu_ms"],
