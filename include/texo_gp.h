@@ -92,7 +92,12 @@ typedef enum texo_gp_status {
   TEXO_GP_ERR_AUCTION_RANGE = 111,            /* ArithmeticOverflow: the price range does not fit */
   TEXO_GP_ERR_AUCTION_OBJECT_RANGE = 112,     /* ObjectOutOfRange */
   TEXO_GP_ERR_AUCTION_COST_RANGE = 113,       /* BaseCostOutOfRange */
-  TEXO_GP_ERR_AUCTION_DUPLICATE_OBJECT = 114  /* DuplicateBestObject: an object twice in one domain */
+  TEXO_GP_ERR_AUCTION_DUPLICATE_OBJECT = 114, /* DuplicateBestObject: an object twice in one domain */
+  /* InstanceAreaError (crates/texo-pnr/src/instance_area.rs:56-62) */
+  TEXO_GP_ERR_INSTANCE_AREA_MEMBER = 115,       /* InvalidMemberArea { member } (error_index) */
+  TEXO_GP_ERR_INSTANCE_AREA_FILLER = 116,       /* InvalidFillerArea { filler } (error_index) */
+  TEXO_GP_ERR_INSTANCE_AREA_POSTCONDITION = 117,/* PostconditionViolation */
+  TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW = 118      /* ArithmeticOverflow */
 } texo_gp_status;
 
 /* Resource kinds in the reference's `ResourceKind` order
@@ -479,6 +484,45 @@ int32_t texo_gp_quadratic_solve(int32_t device, uint32_t n, const double* diagon
  * the reference. `elapsed_ms` (may be NULL): device time with the copies. */
 int32_t texo_gp_routing_demand(int32_t device, uint32_t width, uint32_t height, uint64_t num_boxes,
                                const double* boxes, double* horizontal, double* vertical, double* elapsed_ms);
+
+/* ---- routability: instance-area adjustment (host, FP64) ------------------
+ * The arithmetic of elfPlace's charge-conserving instance-area update
+ * (crates/texo-pnr/src/instance_area.rs), in the reference's operation order
+ * without fused multiply-adds, so results are the reference's bit for bit.
+ * A resource kind is an opaque key; keys must sort like the reference's
+ * ResourceKind (e.g. kind << 8 | lut_inputs); results per kind come back in
+ * ascending key order.
+ *
+ * adjust_instance_areas (:157-253): each member asks for the largest of its
+ * routability, pin, clustering and current areas; per kind the increase is
+ * scaled by min(1, filler area / desired increase), the last member of a kind
+ * takes the rounding remainder, and the fillers of each kind shrink in
+ * proportion (the last one taking the remainder) so every kind's total is
+ * conserved. `scale_kind` / `scale` (capacity `max_scales`, count in
+ * *num_scales) receive the per-kind scales; `requires_optimizer_reset` is 1
+ * when any kind grew. `error_index` (may be NULL): the member or filler of an
+ * INSTANCE_AREA_MEMBER / _FILLER error. */
+int32_t texo_gp_adjust_instance_areas(uint64_t num_members, const uint32_t* member_kind, const double* current_area,
+                                      const double* routability_area, const double* pin_area,
+                                      const double* clustering_area, uint64_t num_fillers,
+                                      const uint32_t* filler_kind, const double* filler_area,
+                                      double* out_member_area, double* out_filler_area,
+                                      int32_t* requires_optimizer_reset, uint32_t max_scales,
+                                      uint32_t* num_scales, uint32_t* scale_kind, double* scale,
+                                      uint64_t* error_index);
+/* routability_optimized_area (:64-84), elfPlace eq. (29): current area times
+ * min(max(h, v)^2, 2). */
+int32_t texo_gp_routability_optimized_area(double current_area, double horizontal_utilization,
+                                           double vertical_utilization, double* out);
+/* routability_optimized_area_from_bin (:91-127): utilization from one RUDY
+ * bin's demand and integer channel capacity; a direction with demand but no
+ * capacity is a hotspot (twice the area), with neither it counts zero. */
+int32_t texo_gp_routability_optimized_area_from_bin(double current_area, double horizontal_demand,
+                                                    uint64_t horizontal_capacity, double vertical_demand,
+                                                    uint64_t vertical_capacity, double* out);
+/* pin_optimized_area (:130-148), elfPlace eq. (30). */
+int32_t texo_gp_pin_optimized_area(uint64_t pin_count, double unit_area_pin_capacity,
+                                   double local_pin_utilization, double* out);
 
 /* ---- legalization: the capacity auction ---------------------------------
  * Replaces `assign_implicitly` (crates/texo-pnr/src/legalization/auction.rs:

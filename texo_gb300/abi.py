@@ -29,6 +29,8 @@ STATUS = {
     110: "PCG_NOT_CONVERGED",
     111: "AUCTION_RANGE", 112: "AUCTION_OBJECT_RANGE", 113: "AUCTION_COST_RANGE",
     114: "AUCTION_DUPLICATE_OBJECT",
+    115: "INSTANCE_AREA_MEMBER", 116: "INSTANCE_AREA_FILLER", 117: "INSTANCE_AREA_POSTCONDITION",
+    118: "INSTANCE_AREA_OVERFLOW",
 }
 CODE = {v: k for k, v in STATUS.items()}
 
@@ -121,8 +123,8 @@ class PcgStats(C.Structure):
 
 
 class AuctionStats(C.Structure):
-    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("cost_scale", C.c_uint32), ("tail_rounds", C.c_uint32),
-                ("bids", C.c_uint64),
+    _fields_ = [("status", C.c_int32), ("rounds", C.c_uint32), ("cost_scale", C.c_uint32),
+                ("tail_rounds", C.c_uint32), ("bids", C.c_uint64),
                 ("candidates_examined", C.c_uint64), ("unmatched", C.c_uint64),
                 ("total_base_cost", C.c_uint64), ("elapsed_ms", C.c_double), ("kernel_launches", C.c_uint64)]
 
@@ -209,6 +211,17 @@ SIGNATURES = {
     "texo_gp_quadratic_solve": (C.c_int32, [C.c_int32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.POINTER(C.c_uint32), C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(PcgStats)]),
+    "texo_gp_adjust_instance_areas": (C.c_int32, [C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_double),
+                                                  C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                  C.POINTER(C.c_double), C.c_uint64, C.POINTER(C.c_uint32),
+                                                  C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                  C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_uint32,
+                                                  C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                                  C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
+    "texo_gp_routability_optimized_area": (C.c_int32, [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+    "texo_gp_routability_optimized_area_from_bin": (C.c_int32, [C.c_double, C.c_double, C.c_uint64, C.c_double,
+                                                                C.c_uint64, C.POINTER(C.c_double)]),
+    "texo_gp_pin_optimized_area": (C.c_int32, [C.c_uint64, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "texo_gp_auction_explicit": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                                              C.POINTER(C.c_uint32),
                                              C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32),

@@ -1510,6 +1510,10 @@ const char* texo_gp_status_name(int32_t s) {
     case TEXO_GP_ERR_AUCTION_OBJECT_RANGE: return "AUCTION_OBJECT_RANGE";
     case TEXO_GP_ERR_AUCTION_COST_RANGE: return "AUCTION_COST_RANGE";
     case TEXO_GP_ERR_AUCTION_DUPLICATE_OBJECT: return "AUCTION_DUPLICATE_OBJECT";
+    case TEXO_GP_ERR_INSTANCE_AREA_MEMBER: return "INSTANCE_AREA_MEMBER";
+    case TEXO_GP_ERR_INSTANCE_AREA_FILLER: return "INSTANCE_AREA_FILLER";
+    case TEXO_GP_ERR_INSTANCE_AREA_POSTCONDITION: return "INSTANCE_AREA_POSTCONDITION";
+    case TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW: return "INSTANCE_AREA_OVERFLOW";
     default: return "UNKNOWN";
   }
 }
