@@ -524,6 +524,28 @@ int32_t texo_gp_routability_optimized_area_from_bin(double current_area, double 
 int32_t texo_gp_pin_optimized_area(uint64_t pin_count, double unit_area_pin_capacity,
                                    double local_pin_utilization, double* out);
 
+/* ---- routability: register-clustering areas (GPU) -----------------------
+ * Replaces `clustering_areas` (crates/texo-pnr/src/register_clustering.rs:
+ * 17-80), as `propose_register_clustering_areas` (eplace.rs:760-791) calls
+ * it: register r at (xy[2r], xy[2r+1]) with control set (clock_lsr[2r],
+ * clock_lsr[2r+1]) and clock enable ce[r]; sigma = sqrt(1e-5 * count) for
+ * `movable_instance_count`, window half-width 2.5 sigma. For each register
+ * the expected registers of its control set in its window, per clock
+ * enable, are the sums of the other registers' Gaussian window
+ * probabilities (x times y, FP64 erf); areas[r] =
+ * 8 / E_focal * ceil2(E_focal) / sum_ce ceil2(E_ce) * ceil4(sum_ce ceil2(E_ce))
+ * with the reference's soft ceilings. Sums run in the reference's order
+ * (input order within a clock enable, clock enables ascending); pairs whose
+ * windows are more than 8 sigma sqrt(2) apart on an axis contribute an exact
+ * zero and are skipped. The device erf is CUDA's, not the reference's libm
+ * erf, so areas agree to rounding, not bit for bit. Returns
+ * TEXO_GP_ERR_INVALID_NORMALIZATION where the reference returns None
+ * (count above 2^32 - 1, a non-positive focal expectation, a non-finite
+ * area). `elapsed_ms` (may be NULL): device time with the copies. */
+int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t num_registers, const double* xy,
+                                          const uint64_t* clock_lsr, const uint64_t* ce,
+                                          uint64_t movable_instance_count, double* areas, double* elapsed_ms);
+
 /* ---- legalization: the capacity auction ---------------------------------
  * Replaces `assign_implicitly` (crates/texo-pnr/src/legalization/auction.rs:
  * 131-247): the integer-cost assignment of bidders to objects with epsilon

@@ -1,6 +1,6 @@
 """Build recipe for the parity oracle (TEST INFRASTRUCTURE ONLY).
 
-Compiles oracle/texo_oracle.cpp and oracle/auction_oracle.cpp into oracle/_build/libtexo_oracle.so with
+Compiles oracle/texo_oracle.cpp, auction_oracle.cpp and routability_oracle.cpp into oracle/_build/libtexo_oracle.so with
 g++ -O3 -ffp-contract=off (no fused multiply-add, matching Rust semantics).
 Only the test suite, the smoke check and the benchmark's CPU-baseline leg load
 the result.
@@ -11,7 +11,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtexo_oracle.so")
-SRC = [os.path.join(HERE, "texo_oracle.cpp"), os.path.join(HERE, "auction_oracle.cpp")]
+SRC = [os.path.join(HERE, "texo_oracle.cpp"), os.path.join(HERE, "auction_oracle.cpp"),
+       os.path.join(HERE, "routability_oracle.cpp")]
 DEPS = SRC + [os.path.join(HERE, "texo_oracle.h"),
               os.path.join(HERE, "..", "include", "texo_gp.h")]
 

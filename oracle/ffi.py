@@ -164,6 +164,22 @@ def auction_certificate(grid, bidder_kind, targets, assignment, prices, dual=Fal
     return out + (bound.value,) if dual else out
 
 
+def register_clustering_areas(xy, clock_lsr, ce, movable_instance_count):
+    """clustering_areas (register_clustering.rs:17-80) in FP64: (code, areas)."""
+    p = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1)
+    cl = np.ascontiguousarray(clock_lsr, dtype=np.uint64).reshape(-1)
+    c = np.ascontiguousarray(ce, dtype=np.uint64).reshape(-1)
+    n = c.shape[0]
+    out = np.zeros(max(n, 1))
+    code = lib().orc_register_clustering_areas(n, P(p), P(cl, C.c_uint64), P(c, C.c_uint64),
+                                               movable_instance_count, P(out))
+    return code, out[:n]
+
+
+def soft_division_ceiling(value, divisor):
+    return lib().orc_soft_division_ceiling(value, divisor)
+
+
 def multiply_quadratic(diagonal, ptr, index, weight, values):
     n = len(diagonal)
     out = np.zeros(n)
@@ -218,6 +234,8 @@ def lib():
             "orc_solve_quadratic": (C.c_int32, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p,
                                                 C.POINTER(PcgStats)]),
             "orc_multiply_quadratic": (None, [C.c_uint64, c_f64p, c_u32p, c_u32p, c_f64p, c_f64p, c_f64p]),
+            "orc_register_clustering_areas": (C.c_int32, [C.c_uint64, c_f64p, c_u64p, c_u64p, C.c_uint64, c_f64p]),
+            "orc_soft_division_ceiling": (C.c_double, [C.c_double, C.c_double]),
             "orc_auction_explicit": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, c_u32p, c_u32p,
                                                  c_u64p, C.POINTER(C.c_int32), c_u64p, C.POINTER(AuctionStats),
                                                  c_u64p]),

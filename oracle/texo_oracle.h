@@ -207,6 +207,14 @@ int64_t orc_auction_check_singletons(uint32_t width, uint32_t height, uint32_t n
                                      uint64_t* base_costs,
                                      uint64_t* first_bad, int64_t* dual_bound);
 
+/* ---- routability: register clustering (routability_oracle.cpp) ----------- */
+/* clustering_areas (register_clustering.rs:17-80): 0, or
+ * TEXO_GP_ERR_INVALID_NORMALIZATION where the reference returns None. */
+int32_t orc_register_clustering_areas(uint64_t n, const double* xy, const uint64_t* clock_lsr, const uint64_t* ce,
+                                      uint64_t movable_instance_count, double* areas);
+/* soft_division_ceiling (register_clustering.rs:89-97) */
+double orc_soft_division_ceiling(double value, double divisor);
+
 #ifdef __cplusplus
 }
 #endif

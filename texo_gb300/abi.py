@@ -222,6 +222,9 @@ SIGNATURES = {
     "texo_gp_routability_optimized_area_from_bin": (C.c_int32, [C.c_double, C.c_double, C.c_uint64, C.c_double,
                                                                 C.c_uint64, C.POINTER(C.c_double)]),
     "texo_gp_pin_optimized_area": (C.c_int32, [C.c_uint64, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+    "texo_gp_register_clustering_areas": (C.c_int32, [C.c_int32, C.c_uint64, C.POINTER(C.c_double),
+                                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_uint64,
+                                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "texo_gp_auction_explicit": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32,
                                              C.POINTER(C.c_uint32),
                                              C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32),

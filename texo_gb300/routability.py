@@ -101,3 +101,24 @@ def pin_optimized_area(pin_count, unit_area_pin_capacity, local_pin_utilization)
                                                     C.byref(out)),
               "texo_gp_pin_optimized_area")
     return out.value
+
+
+def register_clustering_areas(xy, clock_lsr, ce, movable_instance_count, device=0):
+    """`clustering_areas` (register_clustering.rs:17-80) on the GPU: the area
+    elfPlace's register clustering asks for each register at xy [R, 2] with
+    control set clock_lsr [R, 2] and clock enable ce [R]. Returns (areas,
+    device ms). Raises TexoGpError (INVALID_NORMALIZATION) where the
+    reference returns None."""
+    p = np.ascontiguousarray(np.asarray(xy, dtype=np.float64).reshape(-1))
+    cl = np.ascontiguousarray(np.asarray(clock_lsr, dtype=np.uint64).reshape(-1))
+    c = np.ascontiguousarray(np.asarray(ce, dtype=np.uint64).reshape(-1))
+    n = c.shape[0]
+    if p.shape[0] != 2 * n or cl.shape[0] != 2 * n:
+        raise ValueError("xy and clock_lsr need two entries per register")
+    out = np.zeros(max(n, 1))
+    ms = C.c_double()
+    abi.check(abi.load().texo_gp_register_clustering_areas(
+        device, n, abi.ptr(p if n else np.zeros(2), C.c_double), abi.ptr(cl if n else np.zeros(2, np.uint64), C.c_uint64),
+        abi.ptr(c if n else np.zeros(1, np.uint64), C.c_uint64), movable_instance_count, abi.ptr(out, C.c_double),
+        C.byref(ms)), "texo_gp_register_clustering_areas")
+    return out[:n].copy(), ms.value
