@@ -22,10 +22,11 @@ texo_gp_place from host buffers), `roofline` (with per-stage rooflines and
 the persistent kernel's phase clocks), `cpu_baseline`, `batched` (64 mixed
 instances), `serving` (Poisson request stream), `precision` (1M cells, three
 DCT forms against FP64), `quadratic_seed` (the coarse seed's PCG solve) and
-`rudy` (the continuous routing-demand map) and `auction` (the legalizer's
-single-BEL auction on the placement's targets). `--stage-report`,
-`--batch-only`, `--serve-only`, `--precision-only`, `--seed-only`,
-`--rudy-only` and `--auction-only` print one of these alone.
+`rudy` (the continuous routing-demand map), `auction` (the legalizer's
+single-BEL auction on the placement's targets) and `clustering` (the
+register-clustering areas). `--stage-report`, `--batch-only`,
+`--serve-only`, `--precision-only`, `--seed-only`, `--rudy-only`,
+`--auction-only` and `--clustering-only` print one of these alone.
 """
 import argparse
 import json
@@ -683,6 +684,53 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
     return out
 
 
+def clustering_report(reps=5):
+    """elfPlace's register-clustering areas (`clustering_areas`,
+    register_clustering.rs:17-80) for a synthetic register set: one register
+    at each movable position of the 42k-cell placement (device engine), 8
+    clock / LSR control sets and 16 clock enables drawn with a fixed seed,
+    84,000 movable instances (a LUT and a register per site). The GPU runs
+    the whole set (device time with the copies, best of `reps`); the oracle
+    runs control set 0 alone on one host core, a bounded sample whose areas
+    are the same registers' full-set areas (a register's area depends only
+    on its control set)."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import abi
+    from texo_gb300 import routability as R
+    from texo_gb300.placer import Placer
+    prob = make_problem("lfe5u-85-42k", 0)
+    with Placer(prob, make_params("lfe5u-85-42k", abi.ENGINE_DEVICE, abi.DCT_FP32)) as g:
+        _, coords, _ = g.run(allow_nonconverged=True)
+    movable = np.nonzero(np.any(prob.lower_xy != prob.upper_xy, axis=1))[0]
+    xy = coords[: 2 * prob.num_units].reshape(-1, 2)[movable]
+    rng = np.random.default_rng(7)
+    n = len(movable)
+    clock_lsr = np.stack([rng.integers(0, 8, n), np.zeros(n, np.int64)], axis=1).astype(np.uint64)
+    ce = rng.integers(0, 16, n).astype(np.uint64)
+    count = 2 * n
+    R.register_clustering_areas(xy, clock_lsr, ce, count)   # warm-up
+    runs = [R.register_clustering_areas(xy, clock_lsr, ce, count) for _ in range(reps)]
+    areas, _ = runs[0]
+    gpu_ms = min(ms for _, ms in runs)
+    same = all(np.array_equal(a, areas) for a, _ in runs)
+    sample = np.nonzero(clock_lsr[:, 0] == 0)[0]
+    t0 = time.perf_counter()
+    code, ref = ffi.register_clustering_areas(xy[sample], clock_lsr[sample], ce[sample], count)
+    cpu_ms = 1000 * (time.perf_counter() - t0)
+    groups = np.bincount(clock_lsr[:, 0].astype(np.int64))
+    pairs = int(np.sum(groups.astype(np.int64) ** 2))
+    sample_pairs = len(sample) ** 2
+    return {"registers": int(n), "control_sets": 8, "clock_enables": 16, "movable_instances": int(count),
+            "positions": "movable positions of the 42k device-engine placement", "pairs": pairs,
+            "gpu_ms": gpu_ms, "deterministic_over_reps": bool(same),
+            "cpu_oracle_sample": {"registers": int(len(sample)), "pairs": int(sample_pairs), "cpu_ms": cpu_ms,
+                                  "status": int(code), "cores": 1},
+            "cpu_oracle_full_estimate_ms": cpu_ms * pairs / max(sample_pairs, 1),
+            "max_rel_diff_vs_oracle": float(np.max(np.abs(areas[sample] - ref) / np.abs(ref))) if code == 0 else None,
+            "mean_area": float(np.mean(areas))}
+
+
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
@@ -789,6 +837,7 @@ def main():
     ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
     ap.add_argument("--rudy-only", action="store_true", help="print only the RUDY demand report")
     ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
+    ap.add_argument("--clustering-only", action="store_true", help="print only the register-clustering report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -821,6 +870,10 @@ def main():
     if args.rudy_only:
         if rank == 0:
             print(json.dumps({"metric": "continuous RUDY demand", "rudy": rudy_report()}), flush=True)
+        return
+    if args.clustering_only:
+        if rank == 0:
+            print(json.dumps({"metric": "register clustering areas", "clustering": clustering_report()}), flush=True)
         return
     if args.auction_only:
         if rank == 0:
@@ -958,6 +1011,7 @@ def main():
         line["quadratic_seed"] = seed_report(args.workload)
         line["rudy"] = rudy_report()
         line["auction"] = auction_report()
+        line["clustering"] = clustering_report()
     if rank == 0 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(args.workload)
