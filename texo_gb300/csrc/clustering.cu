@@ -12,7 +12,11 @@
 // BTreeMaps. Sums and soft ceilings use explicitly rounded FP64 operations
 // (no fused multiply-add, which the reference never uses); erf is CUDA's.
 // A pair whose windows lie more than 8 sigma sqrt(2) apart on an axis
-// contributes an exact zero (erf saturates), so it is skipped.
+// contributes an exact zero (erf saturates), so it is skipped, after a
+// conservative FP32 test. Threads take the registers of a control set in
+// tile order, so the lanes of a warp agree on which pairs are far (FP64
+// runs at a low rate on this part: a warp whose lanes disagree pays for the
+// slowest lane's erf work on every pair).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -45,17 +49,22 @@ __device__ __forceinline__ double window_probability(double low, double high, do
 struct ClusterDev {
   unsigned n;
   const double *x, *y;                 // sorted by (clock, lsr, ce), stable
+  const float2* xy32;                  // the same positions in FP32, for the far-pair test
   const unsigned long long* ce;
+  const unsigned* focal;               // thread -> sorted position: near registers share a warp
   const unsigned *group_begin, *group_end;   // per sorted register: its control set's range
   const unsigned* order;               // sorted position -> input index
   double half_window, scale, cutoff;
+  float cutoff32;                      // cutoff plus a margin that covers the FP32 rounding
   double* areas;                       // by input index
   int* bad;
 };
 
 __global__ void __launch_bounds__(kClusterThreads) k_clustering(ClusterDev d) {
-  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= d.n) return;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.n) return;
+  const unsigned p = __ldg(d.focal + t);
+  const float2 fi = __ldg(d.xy32 + p);
   const unsigned b = __ldg(d.group_begin + p), e = __ldg(d.group_end + p);
   const double xi = __ldg(d.x + p), yi = __ldg(d.y + p);
   const unsigned long long focal_ce = __ldg(d.ce + p);
@@ -71,6 +80,9 @@ __global__ void __launch_bounds__(kClusterThreads) k_clustering(ClusterDev d) {
       sum = 0.0;
       cur = cj;
     }
+    // far in FP32 (with margin) implies far in FP64: skip without FP64 work
+    const float2 fj = __ldg(d.xy32 + j);
+    if (fabsf(fi.x - fj.x) > d.cutoff32 || fabsf(fi.y - fj.y) > d.cutoff32) continue;
     const double xj = __ldg(d.x + j), yj = __ldg(d.y + j);
     if (fabs(__dsub_rn(xi, xj)) > d.cutoff || fabs(__dsub_rn(yi, yj)) > d.cutoff) continue;
     const double px = window_probability(xlo, xhi, xj, d.scale);
@@ -131,12 +143,18 @@ extern "C" int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t nu
     return ce[a] < ce[b];
   });
   std::vector<double> sx(n), sy(n);
+  std::vector<float> s32(2 * n);
   std::vector<unsigned long long> sce(n);
-  std::vector<uint32_t> gb(n), ge(n);
+  std::vector<uint32_t> gb(n), ge(n), focal(n);
+  double extent = 0.0;
   for (uint64_t p = 0; p < n; ++p) {
     sx[p] = xy[2 * (size_t)order[p]];
     sy[p] = xy[2 * (size_t)order[p] + 1];
+    s32[2 * p] = (float)sx[p];
+    s32[2 * p + 1] = (float)sy[p];
     sce[p] = ce[order[p]];
+    if (std::isfinite(sx[p])) extent = std::max(extent, std::fabs(sx[p]));
+    if (std::isfinite(sy[p])) extent = std::max(extent, std::fabs(sy[p]));
   }
   for (uint64_t p = 0; p < n;) {
     uint64_t q = p + 1;
@@ -148,8 +166,22 @@ extern "C" int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t nu
       gb[r] = (uint32_t)p;
       ge[r] = (uint32_t)q;
     }
+    // the threads of a control set take its registers in tile order (rows
+    // of 8-tile blocks), so a warp's registers are near one another and
+    // agree on which pairs are far
+    std::iota(focal.begin() + p, focal.begin() + q, (uint32_t)p);
+    auto block_of = [&](uint32_t r) -> uint64_t {
+      const double bx = std::isfinite(sx[r]) ? std::floor(sx[r] / 8.0) : 0.0;
+      const double by = std::isfinite(sy[r]) ? std::floor(sy[r] / 8.0) : 0.0;
+      return ((uint64_t)(int64_t)(by + 1.0e6) << 32) | (uint64_t)(uint32_t)(int64_t)(bx + 1.0e6);
+    };
+    std::stable_sort(focal.begin() + p, focal.begin() + q,
+                     [&](uint32_t a, uint32_t b) { return block_of(a) < block_of(b); });
     p = q;
   }
+  // FP32 positions are within 2^-24 |coordinate| of the FP64 ones; a margin of
+  // 2^-20 (extent + cutoff) keeps the FP32 far test conservative
+  const float cutoff32 = (float)(cutoff + std::ldexp(extent + cutoff + 1.0, -20));
 
   if (cudaSetDevice(device) != cudaSuccess) return TEXO_GP_ERR_CUDA;
   cudaStream_t s = nullptr;
@@ -157,7 +189,7 @@ extern "C" int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t nu
   auto round = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t s8 = round(n * 8), s4 = round(n * 4);
   char* base = nullptr;
-  if (cudaMallocAsync((void**)&base, 4 * s8 + 3 * s4 + 256, s) != cudaSuccess) {
+  if (cudaMallocAsync((void**)&base, 5 * s8 + 4 * s4 + 256, s) != cudaSuccess) {
     cudaStreamDestroy(s);
     return TEXO_GP_ERR_OUT_OF_MEMORY;
   }
@@ -173,7 +205,12 @@ extern "C" int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t nu
   unsigned* dgb = (unsigned*)(base + 4 * s8);
   unsigned* dge = (unsigned*)(base + 4 * s8 + s4);
   unsigned* dord = (unsigned*)(base + 4 * s8 + 2 * s4);
-  d.bad = (int*)(base + 4 * s8 + 3 * s4);
+  float2* d32 = (float2*)(base + 4 * s8 + 3 * s4);
+  unsigned* dfoc = (unsigned*)(base + 5 * s8 + 3 * s4);
+  d.bad = (int*)(base + 5 * s8 + 4 * s4);
+  d.xy32 = d32;
+  d.focal = dfoc;
+  d.cutoff32 = cutoff32;
   d.x = dx;
   d.y = dy;
   d.ce = dce;
@@ -190,6 +227,8 @@ extern "C" int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t nu
             cudaMemcpyAsync(dgb, gb.data(), n * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
             cudaMemcpyAsync(dge, ge.data(), n * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
             cudaMemcpyAsync(dord, order.data(), n * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+            cudaMemcpyAsync(d32, s32.data(), n * 8, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+            cudaMemcpyAsync(dfoc, focal.data(), n * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
             cudaMemsetAsync(d.bad, 0, sizeof(int), s) == cudaSuccess;
   if (ok) {
     k_clustering<<<(unsigned)((n + kClusterThreads - 1) / kClusterThreads), kClusterThreads, 0, s>>>(d);
