@@ -50,3 +50,70 @@ def test_reference_cases_on_the_device():
         with pytest.raises(abi.TexoGpError) as e:
             R.register_clustering_areas(*args)
         assert e.value.code == abi.CODE["INVALID_NORMALIZATION"]
+
+
+def test_propose_area_adjustment_matches_a_restatement():
+    """`propose_area_adjustment` (eplace.rs:627-740) composed from the GPU
+    RUDY map and clustering areas against the same step restated with the
+    oracle's FP64 RUDY and clustering and plain loops, on the 48 x 48
+    workload's placement with half its members turned into registers, a
+    routing-capacity map with a blocked band, and register control sets."""
+    import types
+
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import Placer, default_params, net_bounding_boxes
+    prob = P.synthetic(48, 2000, 96, 2400, 6.0, 0)
+    with Placer(prob, default_params(best_effort=1, max_iterations=1000, engine=abi.ENGINE_DEVICE)) as g:
+        _, coords, _ = g.run(allow_nonconverged=True)
+    view = types.SimpleNamespace(**{k: getattr(prob, k) for k in (
+        "num_units", "member_ptr", "lower_xy", "upper_xy", "member_offset_xy", "member_charge", "member_cell",
+        "cell_unit", "cell_offset_xy", "cell_fixed", "cell_fixed_xy", "net_ptr", "pin_cell")})
+    view.fields = [(abi.KIND_LUT, 4), (abi.KIND_REGISTER, 0)]
+    view.member_field = (np.arange(len(prob.member_field)) % 2).astype(np.uint32)
+    cap_h = np.full((48, 48), 3, np.uint32)
+    cap_v = np.full((48, 48), 4, np.uint32)
+    cap_h[20:24, :] = 0                                   # a blocked band: demand there is a hotspot
+    controls = {int(c): (int(c) % 3, 0, int(c) % 5) for c in prob.member_cell}
+    fillers = ([0, 1], [300.0, 250.0])
+    adj, m = R.propose_area_adjustment(view, coords, cap_h, cap_v, *fillers, register_controls=controls)
+
+    # the restatement
+    U = prob.num_units
+    pos = coords[: 2 * U].reshape(-1, 2)
+    h, v, ok = ffi.routing_demand(48, 48, net_bounding_boxes(view, pos))
+    assert ok
+    ptr = prob.member_ptr
+    movable = np.any(prob.lower_xy != prob.upper_xy, axis=1)
+    members = [i for u in range(U) if movable[u] for i in range(ptr[u], ptr[u + 1])]
+    unit_of = {i: u for u in range(U) for i in range(ptr[u], ptr[u + 1])}
+
+    def rnd(v_, n):
+        return int(min(max(np.floor(v_ + 0.5), 0), n - 1))
+
+    def util(dem, cap, x, y):
+        return (0.0 if dem[y, x] == 0.0 else np.sqrt(2.0)) if cap[y, x] == 0 else dem[y, x] / float(cap[y, x])
+
+    want_route, keys, cur, regs = [], [], [], []
+    for i in members:
+        u = unit_of[i]
+        x = rnd(pos[u, 0] + prob.member_offset_xy[i][0], 48)
+        y = rnd(pos[u, 1] + prob.member_offset_xy[i][1], 48)
+        hu, vu = min(util(h, cap_h, x, y), np.sqrt(2.0)), min(util(v, cap_v, x, y), np.sqrt(2.0))
+        q = float(prob.member_charge[i])
+        want_route.append(q * min(max(hu, vu) ** 2, 2.0))
+        keys.append(R.kind_key(view.fields[view.member_field[i]]))
+        cur.append(q)
+        if view.member_field[i] == 1:
+            regs.append(i)
+    rxy = np.array([pos[unit_of[i]] + prob.member_offset_xy[i] for i in regs])
+    rctl = np.array([controls[int(prob.member_cell[i])] for i in regs], dtype=np.uint64)
+    code, rarea = ffi.register_clustering_areas(rxy, rctl[:, :2], rctl[:, 2], int(np.sum(movable[prob.cell_unit])))
+    assert code == 0
+    clus = np.zeros(len(members))
+    clus[[members.index(i) for i in regs]] = rarea
+    want = R.adjust_instance_areas(keys, cur, want_route, np.zeros(len(members)),
+                                   [R.kind_key(view.fields[f]) for f in fillers[0]], fillers[1], clus)
+    assert np.max(np.abs(adj.member_areas - want.member_areas) / want.member_areas) <= 1e-9
+    assert np.max(np.abs(adj.filler_areas - want.filler_areas) / np.maximum(want.filler_areas, 1.0)) <= 1e-9
+    assert adj.requires_optimizer_reset == want.requires_optimizer_reset
+    assert m["members_inflated"] > 0 and m["maximum_horizontal_utilization"] == pytest.approx(np.sqrt(2.0))

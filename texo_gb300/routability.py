@@ -122,3 +122,98 @@ def register_clustering_areas(xy, clock_lsr, ce, movable_instance_count, device=
         abi.ptr(c if n else np.zeros(1, np.uint64), C.c_uint64), movable_instance_count, abi.ptr(out, C.c_double),
         C.byref(ms)), "texo_gp_register_clustering_areas")
     return out[:n].copy(), ms.value
+
+
+SQRT_2 = 1.4142135623730951
+
+
+def kind_key(field):
+    """The order-preserving key of a density field (kind, lut_inputs)."""
+    kind, lut = field
+    return int(kind) << 8 | int(lut)
+
+
+def _rounded(value, extent):
+    # rounded_coordinate (lib.rs:4566-4568): round half away from zero, clamp to the grid
+    r = np.where(value >= 0, np.floor(value + 0.5), np.ceil(value - 0.5))
+    return np.clip(r, 0, extent - 1).astype(np.int64)
+
+
+def _utilization(demand, capacity, x, y):
+    # ContinuousRoutingDemand::utilization (eplace.rs:822-853)
+    d = demand[y, x]
+    c = capacity[y, x].astype(np.float64)
+    u = np.where(c == 0, np.where(d == 0.0, 0.0, SQRT_2), d / np.where(c == 0, 1.0, c))
+    if not np.all(np.isfinite(u) & (u >= 0.0)):
+        raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "propose_area_adjustment")
+    return u
+
+
+def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler_field, filler_charge,
+                            member_charge=None, register_controls=None, device=0):
+    """`propose_area_adjustment` (eplace.rs:627-740) for one placement state:
+    the nets' bounding boxes at the unit origins `coordinates[:2U]`, their
+    RUDY demand on the routing-capacity grid (`capacity_h` / `capacity_v`,
+    [H, W] channel capacities) on the GPU, every movable member's
+    utilization at its rounded position, capped at sqrt(2), elfPlace eq. (29)
+    for LUT and register members (others keep their area), the register
+    clustering areas on the GPU (`register_controls`: cell -> (clock, lsr,
+    ce), for the register members), and `adjust_instance_areas` against the
+    fillers (`filler_field`, `filler_charge`, as `Placer.fillers()` gives
+    them). `member_charge` overrides the problem's member charges (after an
+    earlier round). Returns (InstanceAreaAdjustment, metrics dict)."""
+    from .placer import net_bounding_boxes, routing_demand
+    cap_h = np.asarray(capacity_h, dtype=np.uint32)
+    cap_v = np.asarray(capacity_v, dtype=np.uint32)
+    if cap_h.ndim != 2 or cap_h.shape != cap_v.shape or cap_h.size == 0:
+        raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "propose_area_adjustment")
+    H, W = cap_h.shape
+    U = problem.num_units
+    pos = np.asarray(coordinates, dtype=np.float64)[: 2 * U].reshape(-1, 2)
+    h_dem, v_dem, _ = routing_demand(W, H, net_bounding_boxes(problem, pos), device=device)
+    ptr = np.asarray(problem.member_ptr, dtype=np.int64)
+    movable = np.any(problem.lower_xy != problem.upper_xy, axis=1)
+    members = np.concatenate([np.arange(ptr[u], ptr[u + 1]) for u in np.nonzero(movable)[0]] or [np.zeros(0, int)])
+    unit_of = np.repeat(np.arange(U), np.diff(ptr))[members]
+    off = np.asarray(problem.member_offset_xy, dtype=np.float64).reshape(-1, 2)[members]
+    charge = np.asarray(problem.member_charge if member_charge is None else member_charge, dtype=np.float64)[members]
+    fields = [tuple(f) for f in problem.fields]
+    field = np.asarray(problem.member_field, dtype=np.int64)[members]
+    keys = np.array([kind_key(fields[f]) for f in field], dtype=np.uint32)
+    x = _rounded(pos[unit_of, 0] + off[:, 0], W)
+    y = _rounded(pos[unit_of, 1] + off[:, 1], H)
+    hu = _utilization(h_dem, cap_h, x, y)
+    vu = _utilization(v_dem, cap_v, x, y)
+    inflatable = np.array([fields[f][0] in (abi.KIND_LUT, abi.KIND_REGISTER) for f in field], dtype=bool)
+    routing = np.array([routability_optimized_area(c, min(a, SQRT_2), min(b, SQRT_2)) for c, a, b in zip(charge, hu, vu)])
+    routing = np.where(inflatable, routing, charge)
+    clustering = np.zeros(len(members))
+    if register_controls:
+        cells = np.asarray(problem.member_cell, dtype=np.int64)[members]
+        is_reg = np.array([fields[f][0] == abi.KIND_REGISTER for f in field], dtype=bool)
+        regs = np.nonzero(is_reg)[0]
+        if len(regs):
+            ctl = np.array([register_controls[int(c)] for c in cells[regs]], dtype=np.uint64).reshape(-1, 3)
+            cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
+            count = int(np.sum(movable[cell_unit]))   # cells of movable units (movable_instance_count)
+            areas, _ = register_clustering_areas(pos[unit_of[regs]] + off[regs], ctl[:, :2], ctl[:, 2], count,
+                                                 device=device)
+            clustering[regs] = areas
+    fk = np.array([kind_key(fields[int(f)]) for f in np.asarray(filler_field).reshape(-1)], dtype=np.uint32)
+    fq = np.asarray(filler_charge, dtype=np.float64).reshape(-1)
+    adj = adjust_instance_areas(keys, charge, routing, np.zeros(len(members)), fk, fq, clustering)
+    before, increase = {}, {}
+    for k, c, a in zip(keys.tolist(), charge, adj.member_areas):
+        before[k] = before.get(k, 0.0) + c
+        increase[k] = increase.get(k, 0.0) + (a - c)
+    total_before, total_increase = sum(before.values()), sum(increase.values())
+    rel = total_increase / total_before if total_before else float("nan")
+    rel_max = max([increase[k] / b if b else float("nan") for k, b in before.items()], default=0.0)
+    if not (np.isfinite(rel) and np.isfinite(rel_max)):   # the reference's InvalidNormalization
+        raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "propose_area_adjustment")
+    metrics = {"maximum_horizontal_utilization": float(np.max(hu, initial=0.0)),
+               "maximum_vertical_utilization": float(np.max(vu, initial=0.0)),
+               "members_inflated": int(np.sum(adj.member_areas - charge > 0.0)),
+               "total_relative_increase": rel, "maximum_relative_increase": rel_max,
+               "members": members}
+    return adj, metrics
