@@ -116,4 +116,4 @@ def test_propose_area_adjustment_matches_a_restatement():
     assert np.max(np.abs(adj.member_areas - want.member_areas) / want.member_areas) <= 1e-9
     assert np.max(np.abs(adj.filler_areas - want.filler_areas) / np.maximum(want.filler_areas, 1.0)) <= 1e-9
     assert adj.requires_optimizer_reset == want.requires_optimizer_reset
-    assert m["members_inflated"] > 0 and m["maximum_horizontal_utilization"] == pytest.approx(np.sqrt(2.0))
+    assert m["members_inflated"] > 0 and m["maximum_horizontal_utilization"] >= np.sqrt(2.0) - 1e-12
