@@ -91,3 +91,20 @@ def test_seed_axis_solve_matches_the_oracle_path():
         xr[comp] += 24.0 - xr[comp].sum() / len(comp)
     assert ok and st["stop"] == "residual"
     assert np.max(np.abs(xg - xr)) <= 1e-8 * np.max(np.abs(xr))
+
+
+def test_seed_solve_at_the_42k_workload():
+    """The 42k workload's own seed systems (42,365 unknowns an axis) on the
+    GPU against the oracle's FP64 solve."""
+    prob = P.synthetic(210, 42000, 365, 50000, 12.0, 0)
+    pos = np.asarray(prob.initial_xy).reshape(-1, 2)
+    for axis in (0, 1):
+        d, ptr, idx, w, rhs, anch = seed.axis_system(prob, pos, axis)
+        d, ptr, idx, w, rhs, _ = seed.finalize_gauges(d, ptr, idx, w, rhs, anch)
+        x0 = pos[:, axis].copy()
+        xr, sr, ok = ffi.solve_quadratic(d, ptr, idx, w, rhs, x0)
+        assert ok
+        xg, sg = quadratic_solve(d, ptr, idx, w, rhs, x0)
+        assert sg["stop"] == "residual" and sg["final_residual_squared"] <= sg["target_squared"]
+        assert abs(sg["iterations"] - sr.iterations) <= 2
+        assert np.max(np.abs(xg - xr)) <= 1e-8 * np.max(np.abs(xr))

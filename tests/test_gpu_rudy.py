@@ -43,3 +43,22 @@ def test_bad_boxes_are_rejected():
     with pytest.raises(abi.TexoGpError) as e:
         routing_demand(4, 4, [(2.0, 1.0, 0.0, 1.0)])
     assert e.value.name == "INVALID_NORMALIZATION"
+
+
+@pytest.mark.parametrize("side,cells,io,nets,sigma", [(210, 42000, 365, 50000, 12.0), (1024, 1000000, 4096, 1200000, 24.0)])
+def test_full_size_demand(side, cells, io, nets, sigma):
+    """The workloads' own sizes: the 42k workload's 50,000 boxes against the
+    oracle in full; the 1M workload's 1.2 M boxes deterministic on the GPU
+    and, on a 20,000-box sample, equal to the oracle."""
+    prob = P.synthetic(side, cells, io, nets, sigma, 0)
+    pos = np.random.default_rng(1).uniform(0, side - 1, size=(prob.num_units, 2))
+    boxes = net_bounding_boxes(prob, pos)
+    h, v, _ = routing_demand(side, side, boxes)
+    h2, v2, _ = routing_demand(side, side, boxes)
+    assert np.array_equal(h, h2) and np.array_equal(v, v2)
+    sample = boxes if len(boxes) <= 60000 else boxes[:20000]
+    hs, vs, _ = routing_demand(side, side, sample)
+    hr, vr, ok = ffi.routing_demand(side, side, sample)
+    assert ok
+    assert np.max(np.abs(hs - hr)) <= 1e-9 * np.max(hr)
+    assert np.max(np.abs(vs - vr)) <= 1e-9 * np.max(vr)
