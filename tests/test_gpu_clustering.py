@@ -117,3 +117,30 @@ def test_propose_area_adjustment_matches_a_restatement():
     assert np.max(np.abs(adj.filler_areas - want.filler_areas) / np.maximum(want.filler_areas, 1.0)) <= 1e-9
     assert adj.requires_optimizer_reset == want.requires_optimizer_reset
     assert m["members_inflated"] > 0 and m["maximum_horizontal_utilization"] >= np.sqrt(2.0) - 1e-12
+
+
+def test_full_size_register_set():
+    """The 42k workload's size: 42,000 registers at the placement's movable
+    positions in 8 control sets x 16 clock enables; control set 0 (about
+    5,000 registers, the oracle's every pair) equal to the GPU's full-set
+    areas within 1e-12, the whole set deterministic."""
+    from texo_gb300 import problem as P
+    from texo_gb300.placer import Placer, default_params
+    prob = P.synthetic(210, 42000, 365, 50000, 12.0, 0)
+    params = default_params(bins_x=256, bins_y=256, target_density=0.9, gamma_base=4.0, max_iterations=1000,
+                            best_effort=1, engine=abi.ENGINE_DEVICE, dct_mode=abi.DCT_FP32)
+    with Placer(prob, params) as g:
+        _, coords, _ = g.run(allow_nonconverged=True)
+    movable = np.nonzero(np.any(prob.lower_xy != prob.upper_xy, axis=1))[0]
+    xy = coords[: 2 * prob.num_units].reshape(-1, 2)[movable]
+    rng = np.random.default_rng(7)
+    n = len(movable)
+    clock_lsr = np.stack([rng.integers(0, 8, n), np.zeros(n, np.int64)], axis=1).astype(np.uint64)
+    ce = rng.integers(0, 16, n).astype(np.uint64)
+    areas, _ = R.register_clustering_areas(xy, clock_lsr, ce, 2 * n)
+    again, _ = R.register_clustering_areas(xy, clock_lsr, ce, 2 * n)
+    assert np.array_equal(areas, again)
+    sample = np.nonzero(clock_lsr[:, 0] == 0)[0]
+    code, ref = ffi.register_clustering_areas(xy[sample], clock_lsr[sample], ce[sample], 2 * n)
+    assert code == 0
+    assert np.max(np.abs(areas[sample] - ref) / ref) <= 1e-12
