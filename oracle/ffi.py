@@ -120,7 +120,8 @@ def auction_explicit(domains, object_count, max_base_cost, cost_scale=1, jacobi=
 def _grid_args(grid):
     tobj = grid.tile_object if len(grid.tile_object) else np.zeros(1, np.uint32)
     occ = None if grid.occupied is None else np.ascontiguousarray(grid.occupied, dtype=np.uint8)
-    return (grid.width, grid.height, grid.num_kinds, P(np.ascontiguousarray(grid.tile_ptr, dtype=np.uint32), C.c_uint32),
+    return (grid.width, grid.height, grid.num_kinds,
+            P(np.ascontiguousarray(grid.tile_ptr, dtype=np.uint32), C.c_uint32),
             P(np.ascontiguousarray(tobj, dtype=np.uint32), C.c_uint32), grid.num_objects,
             None if occ is None else P(occ, C.c_uint8))
 
@@ -158,7 +159,8 @@ def auction_certificate(grid, bidder_kind, targets, assignment, prices, dual=Fal
     first = C.c_uint64()
     bound = C.c_int64()
     bad = lib().orc_auction_check_singletons(*_grid_args(grid), n, P(kind, C.c_uint32), P(txy, C.c_uint32),
-                                             cost_scale, P(a, C.c_int32), P(pr if len(pr) else np.zeros(1, np.uint32), C.c_uint32),
+                                             cost_scale, P(a, C.c_int32),
+                                             P(pr if len(pr) else np.zeros(1, np.uint32), C.c_uint32),
                                              P(base, C.c_uint64), C.byref(first), C.byref(bound))
     out = (bad, (None if first.value == 2**64 - 1 else first.value), base[:n])
     return out + (bound.value,) if dual else out

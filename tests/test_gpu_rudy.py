@@ -45,7 +45,8 @@ def test_bad_boxes_are_rejected():
     assert e.value.name == "INVALID_NORMALIZATION"
 
 
-@pytest.mark.parametrize("side,cells,io,nets,sigma", [(210, 42000, 365, 50000, 12.0), (1024, 1000000, 4096, 1200000, 24.0)])
+@pytest.mark.parametrize("side,cells,io,nets,sigma", [(210, 42000, 365, 50000, 12.0),
+                                                     (1024, 1000000, 4096, 1200000, 24.0)])
 def test_full_size_demand(side, cells, io, nets, sigma):
     """The workloads' own sizes: the 42k workload's 50,000 boxes against the
     oracle in full; the 1M workload's 1.2 M boxes deterministic on the GPU

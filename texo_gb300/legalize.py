@@ -49,7 +49,8 @@ class AuctionResult:
 
 def _stats(st):
     return {"cost_scale": st.cost_scale, "bids": st.bids, "candidates_examined": st.candidates_examined,
-            "unmatched": st.unmatched, "rounds": st.rounds, "tail_rounds": st.tail_rounds, "total_base_cost": st.total_base_cost, "elapsed_ms": st.elapsed_ms,
+            "unmatched": st.unmatched, "rounds": st.rounds, "tail_rounds": st.tail_rounds,
+            "total_base_cost": st.total_base_cost, "elapsed_ms": st.elapsed_ms,
             "kernel_launches": st.kernel_launches}
 
 

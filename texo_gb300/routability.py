@@ -118,7 +118,8 @@ def register_clustering_areas(xy, clock_lsr, ce, movable_instance_count, device=
     out = np.zeros(max(n, 1))
     ms = C.c_double()
     abi.check(abi.load().texo_gp_register_clustering_areas(
-        device, n, abi.ptr(p if n else np.zeros(2), C.c_double), abi.ptr(cl if n else np.zeros(2, np.uint64), C.c_uint64),
+        device, n, abi.ptr(p if n else np.zeros(2), C.c_double),
+        abi.ptr(cl if n else np.zeros(2, np.uint64), C.c_uint64),
         abi.ptr(c if n else np.zeros(1, np.uint64), C.c_uint64), movable_instance_count, abi.ptr(out, C.c_double),
         C.byref(ms)), "texo_gp_register_clustering_areas")
     return out[:n].copy(), ms.value
@@ -185,7 +186,8 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     hu = _utilization(h_dem, cap_h, x, y)
     vu = _utilization(v_dem, cap_v, x, y)
     inflatable = np.array([fields[f][0] in (abi.KIND_LUT, abi.KIND_REGISTER) for f in field], dtype=bool)
-    routing = np.array([routability_optimized_area(c, min(a, SQRT_2), min(b, SQRT_2)) for c, a, b in zip(charge, hu, vu)])
+    routing = np.array([routability_optimized_area(c, min(a, SQRT_2), min(b, SQRT_2))
+                        for c, a, b in zip(charge, hu, vu)])
     routing = np.where(inflatable, routing, charge)
     clustering = np.zeros(len(members))
     if register_controls:
