@@ -550,7 +550,8 @@ int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t num_registers
  * Replaces `assign_implicitly` (crates/texo-pnr/src/legalization/auction.rs:
  * 131-247): the integer-cost assignment of bidders to objects with epsilon
  * one, every bidder owning a private dummy of cost
- * D = n * max_base_cost + n + 1 (n = bidders), so the result has exactly the
+ * D = n * max_base_cost + n + 1 (n = bidders; at the reference's cost scale
+ * 1, `cost_scale` below generalises it), so the result has exactly the
  * maximum cardinality and a total base cost at most n above the minimum
  * among assignments of that cardinality. A bidder's bid raises its best
  * object's price by (second-best reduced cost - best reduced cost + 1), ties
