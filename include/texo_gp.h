@@ -307,7 +307,10 @@ int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potenti
  * TEXO_GP_ERR_UNSUPPORTED (texo_gp_last_error says which). Nothing has to be
  * zero beforehand; the call initializes every scratch word it reads. The
  * first call on a device looks up the scratch address (cudaGetSymbolAddress)
- * with that device current; make that call before any stream capture. Calls
+ * with that device current, and because CUDA loads device code lazily, that
+ * first call is also when the 4 MiB array itself is reserved on the device:
+ * make one call at start-up, before the HBM budget is committed and before
+ * any stream capture; later calls reserve nothing. Calls
  * that overlap on one device (two threads, or two handles) race on the shared
  * scratch; calls made one after another are safe (each call synchronizes
  * before returning). No counterpart in the reference. */

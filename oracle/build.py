@@ -2,8 +2,10 @@
 
 Compiles oracle/texo_oracle.cpp, auction_oracle.cpp and routability_oracle.cpp into oracle/_build/libtexo_oracle.so with
 g++ -O3 -ffp-contract=off (no fused multiply-add, matching Rust semantics).
-Only the test suite, the smoke check and the benchmark's CPU-baseline leg load
-the result.
+The seeded synthetic-netlist generator of the engine (texo_gb300/csrc/synth.cpp,
+plain host C++) is compiled in as well, so the benchmark's reference arm builds
+its inputs without loading the engine library. Only the test suite, the smoke
+check and the benchmark's CPU-baseline and reference legs load the result.
 """
 import os
 import subprocess
@@ -12,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libtexo_oracle.so")
 SRC = [os.path.join(HERE, "texo_oracle.cpp"), os.path.join(HERE, "auction_oracle.cpp"),
-       os.path.join(HERE, "routability_oracle.cpp")]
+       os.path.join(HERE, "routability_oracle.cpp"),
+       os.path.join(HERE, "..", "texo_gb300", "csrc", "synth.cpp")]
 DEPS = SRC + [os.path.join(HERE, "texo_oracle.h"),
               os.path.join(HERE, "..", "include", "texo_gp.h")]
 

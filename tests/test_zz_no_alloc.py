@@ -79,3 +79,46 @@ def test_static_scatter_rejects_oversized_grid():
         # the handle still works through the ordinary entry point
         rp, _ = g.scatter(c)
         assert rp.shape == (g.num_fields, g.bins)
+
+
+def test_static_scatter_rejects_too_many_objects():
+    # a small bin grid (fits the grid limit) with more than 131072 units + fillers
+    lib = abi.load()
+    with Placer(P.synthetic(400, 2000, 96, 2400, 6.0, 1), _params(bins_x=64, bins_y=64)) as g:
+        assert g.num_fields * g.bins <= SCRATCH_GRID_WORDS
+        assert g.units + g.num_fillers > 131072
+        c = np.ascontiguousarray(g.initial()[0])
+        phys = np.zeros(g.num_fields * g.bins, np.int64)
+        code = lib.texo_gp_scatter_static(g.h, abi.ptr(c, C.c_double), abi.ptr(phys, C.c_int64), None)
+        assert code == abi.CODE["UNSUPPORTED"]
+        assert b"units + fillers" in lib.texo_gp_last_error()
+
+
+def test_static_scatter_allocates_nothing_after_the_first_call():
+    torch = pytest.importorskip("torch")
+    lib = abi.load()
+    make, kw = CASES["bins64-td0.9"]
+    with Placer(make(), _params(**kw)) as g:
+        c = np.ascontiguousarray(_coords(g, 5))
+        _static(lib, g, c)                      # the first call on the device reserves the array
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(3):
+            _static(lib, g, c)
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0
+
+
+def test_static_scatter_leaves_the_handle_alone():
+    # evaluate(x) is the same whether or not a static scatter at other
+    # coordinates came between two evaluations
+    lib = abi.load()
+    make, kw = CASES["tiles-2k"]
+    with Placer(make(), _params(**kw)) as g:
+        x = np.ascontiguousarray(_coords(g, 9))
+        a = g.evaluate(x, 4.0)
+        _static(lib, g, np.ascontiguousarray(_coords(g, 10)))
+        b = g.evaluate(x, 4.0)
+    for k in ("density", "potential", "wa_gradient", "field_gradient"):
+        assert np.array_equal(a[k], b[k])
+    assert a["wirelength"] == b["wirelength"]

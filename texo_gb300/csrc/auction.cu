@@ -33,6 +33,8 @@
 // slots, so no phase clears what another block may still read.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -451,11 +453,21 @@ int32_t run_auction(int32_t device, AucHost& h, int32_t* assignment, uint32_t* p
   uint32_t dummy = 0;
   if (!dummy_cost(h.n, h.max_base_cost, h.scale, &dummy)) return fail_with(st, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
   if (cudaSetDevice(device) != cudaSuccess) return fail_with(st, TEXO_GP_ERR_CUDA, "cudaSetDevice failed");
-  static const int per_sm = [] {   // thread-safe one-time initialisation
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_auction, kAucThreads, 0) != cudaSuccess) b = 0;
-    return b;
-  }();
+  // resident blocks a multiprocessor, computed once per device ordinal with
+  // that device current (the cooperative launch must fit the device it runs on)
+  static std::mutex occ_mu;
+  static std::map<int32_t, int> occupancy;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(occ_mu);
+    auto it = occupancy.find(device);
+    if (it == occupancy.end()) {
+      int b = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_auction, kAucThreads, 0) != cudaSuccess) b = 0;
+      it = occupancy.emplace(device, b).first;
+    }
+    per_sm = it->second;
+  }
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (per_sm <= 0 || sms <= 0) return fail_with(st, TEXO_GP_ERR_CUDA, "k_auction cannot be resident");
