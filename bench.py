@@ -483,7 +483,7 @@ def stage_report(workload, dct_name, reps):
     import torch
     from texo_gb300 import abi
     from texo_gb300.placer import Placer
-    dct = {"fp32": abi.DCT_FP32, "bf16x3": abi.DCT_BF16X3, "fp32-gemm": abi.DCT_FP32_GEMM}[dct_name]
+    dct = {"fp32": abi.DCT_FP32, "tensor": abi.DCT_TENSOR, "bf16x3": abi.DCT_TENSOR, "fp32-gemm": abi.DCT_FP32_GEMM}[dct_name]
     prob = make_problem(workload, 0)
     prm = make_params(workload, abi.ENGINE_HOST, dct)
     peak, kind = peaks()
@@ -741,7 +741,7 @@ def clustering_report(reps=5):
 def precision_report(iterations=1000, seed=0, threads=5):
     """Precision stress (1M cells + 4,096 IO on 1024^2 sites, 1.2M nets,
     1024^2 bins, target density 0.9): potential, field gradient and energy of
-    the FP32 FFT, FP32 GEMM and BF16x3 (tensor-core) DCT forms against the FP64 oracle at
+    the FP32 FFT, FP32 GEMM and tensor-core (integer-slice) DCT forms against the FP64 oracle at
     identical spread positions, gradient cosine similarity, and each form's
     final HPWL / overflow: once run to the stop rule (overflow <= 0.10), and
     once for exactly `iterations` GP iterations (overflow target 0, so the
@@ -771,7 +771,7 @@ def precision_report(iterations=1000, seed=0, threads=5):
 
     out = {"workload": "stress-1m", "positions": "uniform in the bounds, FP32-representable",
            "oracle_eval_s": t_oracle}
-    for name, mode in (("fp32_fft", abi.DCT_FP32), ("fp32_gemm", abi.DCT_FP32_GEMM), ("bf16x3", abi.DCT_BF16X3)):
+    for name, mode in (("fp32_fft", abi.DCT_FP32), ("fp32_gemm", abi.DCT_FP32_GEMM), ("tensor", abi.DCT_TENSOR)):
         prm = make_params("stress-1m", abi.ENGINE_HOST, mode)
         prm.max_iterations = iterations
         with Placer(prob, prm) as g:
@@ -798,10 +798,10 @@ def precision_report(iterations=1000, seed=0, threads=5):
                                      if k.startswith("dct_")},
                      "final_hpwl": s["hpwl"], "final_overflow": s["overflow"], "iterations": s["iterations"],
                      "converged": s["converged"], "run_s": run_s, "gpu_ms": s["elapsed_ms"]}
-    out["final_hpwl_bf16x3_vs_fp32_gemm"] = out["bf16x3"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
+    out["final_hpwl_tensor_vs_fp32_gemm"] = out["tensor"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
     out["final_hpwl_fp32_fft_vs_fp32_gemm"] = out["fp32_fft"]["final_hpwl"] / out["fp32_gemm"]["final_hpwl"] - 1.0
     key = "after_%d_iterations" % iterations
-    for a, b in (("bf16x3", "fp32_gemm"), ("fp32_fft", "fp32_gemm")):
+    for a, b in (("tensor", "fp32_gemm"), ("fp32_fft", "fp32_gemm")):
         out["%s_hpwl_%s_vs_%s" % (key, a, b)] = out[a][key]["final_hpwl"] / out[b][key]["final_hpwl"] - 1.0
     return out
 
@@ -822,7 +822,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lfe5u-85-42k", choices=sorted(WORKLOADS))
     ap.add_argument("--engine", default="device", choices=["host", "device"])
-    ap.add_argument("--dct", default="fp32", choices=["fp32", "bf16x3", "fp32-gemm"])
+    ap.add_argument("--dct", default="fp32", choices=["fp32", "tensor", "bf16x3", "fp32-gemm"],
+                    help="DCT form; bf16x3 is the earlier name of tensor")
     ap.add_argument("--reference-sample", type=int, default=30,
                     help="GP iterations per reference step (each step places from the start, so a short "
                          "prefix would mostly time the model build and the two initial evaluations)")
@@ -872,7 +873,7 @@ def main():
         return
     if args.precision_only:
         if rank == 0:
-            print(json.dumps({"metric": "BF16x3 / FP32 / FP64 precision at 1M cells",
+            print(json.dumps({"metric": "tensor-core / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
         return
     if args.rudy_only:
@@ -901,7 +902,7 @@ def main():
                               "serving": serve_report(args.serve_requests)}), flush=True)
         return
     engine = abi.ENGINE_HOST if args.engine == "host" else abi.ENGINE_DEVICE
-    dct = {"fp32": abi.DCT_FP32, "bf16x3": abi.DCT_BF16X3, "fp32-gemm": abi.DCT_FP32_GEMM}[args.dct]
+    dct = {"fp32": abi.DCT_FP32, "tensor": abi.DCT_TENSOR, "bf16x3": abi.DCT_TENSOR, "fp32-gemm": abi.DCT_FP32_GEMM}[args.dct]
     prob = make_problem(args.workload, rank)
     prm = make_params(args.workload, engine, dct)
     prm.device = local

@@ -161,7 +161,9 @@ typedef struct texo_gp_problem {
 /* DCT forms for the spectral Poisson solve. */
 typedef enum texo_gp_dct_mode {
   TEXO_GP_DCT_FP32 = 0,      /* FP32: FFT-based transforms on power-of-two grids, else the GEMM form */
-  TEXO_GP_DCT_BF16X3 = 1,    /* tcgen05 tensor cores, BF16x3 split, FP32 accumulate */
+  TEXO_GP_DCT_TENSOR = 1,    /* tcgen05 tensor cores: the BF16x3 split carried to four 8-bit integer
+                                slices per value, ten slice products accumulated exactly in FP32 */
+  TEXO_GP_DCT_BF16X3 = TEXO_GP_DCT_TENSOR,   /* earlier name of the same mode */
   TEXO_GP_DCT_FP32_GEMM = 2  /* FP32 compensated GEMM against the cosine matrices on every grid */
 } texo_gp_dct_mode;
 
@@ -191,7 +193,7 @@ typedef struct texo_gp_params {
   double objective_margin_ulps;  /* line-search rounding margin: max(eps64, ulps * 2^-24) (1 + |a| + |b|) */
   int32_t autotune;              /* 1: time the DCT forms on this instance at creation and keep the
                                     fastest (FP32 GEMM with 16x16 or 64x64 tiles, FP32 FFT on
-                                    power-of-two grids; with dct_mode BF16X3 also the tensor-core
+                                    power-of-two grids; with dct_mode TENSOR also the tensor-core
                                     form, which may give way to the more accurate FP32 forms) */
   uint32_t reserved[7];
 } texo_gp_params;
@@ -318,7 +320,7 @@ int32_t texo_gp_scatter_static(texo_gp_handle h, const double* coordinates,
                                int64_t* physical_grid, int64_t* filler_grid);
 
 /* The DCT form the handle runs: 0 FP32 GEMM with 16x16 slab tiles, 1 FP32
- * GEMM with 64x64 register-blocked tiles, 2 tcgen05 tensor cores (BF16x3),
+ * GEMM with 64x64 register-blocked tiles, 2 tcgen05 tensor cores (integer slices),
  * 3 FP32 FFT-based transforms (power-of-two grids; the default there). No
  * counterpart in the reference (it has one CPU transform). */
 int32_t texo_gp_dct_form(texo_gp_handle h, int32_t* form);

@@ -35,7 +35,8 @@ STATUS = {
 CODE = {v: k for k, v in STATUS.items()}
 
 KIND_LOGIC, KIND_LUT, KIND_REGISTER, KIND_MEMORY, KIND_CLOCK, KIND_IO, KIND_CONSTANT, KIND_DSP = range(8)
-DCT_FP32, DCT_BF16X3, DCT_FP32_GEMM = 0, 1, 2
+DCT_FP32, DCT_TENSOR, DCT_FP32_GEMM = 0, 1, 2
+DCT_BF16X3 = DCT_TENSOR   # earlier name of the tensor-core mode
 ENGINE_HOST, ENGINE_DEVICE = 0, 1
 MAX_FIELDS = 4
 

@@ -79,11 +79,12 @@ struct Dev {
   const float* Cx;  const float* CxT;   // [Wb][Wb]
   const float* Cy;  const float* CyT;   // [Hb][Hb]
   const float* inv_eig;      // [B]
-  // Tensor-core DCT (BF16x3): every GEMM operand is kept as bfloat16 hi/lo
-  // halves in the tile layout the tensor cores read (see dct_tc.cuh). A
-  // operands (rows x K) in 128 x 32 blocks, B operands (output columns x K)
-  // in 64 x 32 blocks, zero-padded; rho_t and t3_t are A operands (H x W),
-  // t1_t and t2_t B operands (W x H); the bases are shared read-only tables.
+  // Tensor-core DCT (dct_tc.cuh): every GEMM operand is kept as four bf16
+  // integer slices in the tile layout the tensor cores read, with one
+  // power-of-two scale per operand row. A operands (rows x K) in 128 x 32
+  // blocks, B operands (output columns x K) in 64 x 32 blocks, zero-padded;
+  // opA holds rho then t3 (H x W), opB t1 then t2 (W x H); the bases are
+  // shared read-only tables.
   int tc;                    // 1: the DCT passes run on tcgen05 tensor cores
   int dct_large;             // FP32 GEMM form: 1 = 64x64 register-blocked tiles, 0 = 16x16 slab tiles
   // FFT form (power-of-two grids): twiddle tables per axis (dct_fft.cuh)
@@ -94,8 +95,13 @@ struct Dev {
   const float4 *fy_tw, *fy_post, *fy_pre;
   const float2* fy_inv_s;
   int Hp128, Hp32, Wp64, Wp32;   // padded extents
-  uint16_t *rho_t, *t1_t, *t2_t, *t3_t;
+  uint16_t *opA, *opB;           // dynamic operands (all fields)
+  int *eA, *eB;                  // their row exponents [K][Hp128], [K][Wp64]
+  float2* tp;                    // [K][B] pass output as double-float pairs (aliases t1)
+  unsigned* tmx;                 // [2][K][Wb] column maxima of t1, t2 (float bits of |x|)
   const uint16_t *CxB_t, *CyA_t, *CyTA_t, *CxTB_t;
+  const int *eCx, *eCy;          // basis row exponents: [n] rows of C, then [n] rows of C^T
+  const float* inv_eig_lo;       // [B] low part of 1 / lambda
   // gradients
   unsigned long long* wa_fix;  // [2U] WA gradient, 2^-32 fixed point
   float2* graw;              // [K][nobj] raw per-field density gradient

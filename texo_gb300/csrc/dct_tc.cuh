@@ -1,28 +1,49 @@
-// dct_tc.cuh — the DCT GEMM passes on tcgen05 tensor cores, BF16x3 form.
+// dct_tc.cuh — the DCT GEMM passes on tcgen05 tensor cores with exact
+// accumulation (bf16 integer slices).
 //
-// Each FP32 operand x is split into bfloat16 halves x = hi + lo (+ O(2^-18 x));
-// a product is accumulated as lo*hi + hi*lo + hi*hi in FP32 in tensor memory
-// (the published bfloat16x3 scheme of Henry, Tang and Heinecke, ARITH 2019).
+// Split form. Every operand row (a row of A over K, or a row of B over K) has
+// a power-of-two scale 2^e with |value| <= 2^e over the row, and each value
+// is cut into four 8-bit integer slices,
+//     value = 2^(e-7) (s0 + 2^-8 s1 + 2^-16 s2 + 2^-24 s3),  s_i in [-128, 128],
+// each an exact bfloat16 (31 bits of the row's range in all). A product of
+// two slices is an integer of at most 2^14, so a K <= 1024 sum of them is an
+// integer of at most 2^24: the tensor cores' FP32 accumulation of one slice
+// pair is exact. The products s_i(A) s_j(B) with i + j = L go to accumulator
+// L (L = 0..3, ten products per K step; the dropped ones are below 2^-31 of
+// the row ranges), and the epilogue joins the four exact accumulators in
+// double-float arithmetic and applies the two row scales. This is the
+// Ozaki-style generalisation of the bfloat16x3 split (Henry, Tang and
+// Heinecke, ARITH 2019): the two-term split keeps about 16 bits and rounds
+// in the accumulator, which leaves the field gradient 1e-3 away from FP64 on
+// a 1024^2 grid; four integer slices with exact sums keep it at the level of
+// the FP32 output.
 //
-// Operand layout. Every operand lives in global memory already split and in
-// the exact byte layout the MMA reads from shared memory: the canonical
-// K-major no-swizzle layout of 8-row x 16-byte core matrices (128 B between
-// K-adjacent core matrices, 512 B between 8-row groups), cut into blocks of
-// 32 K-elements. An A operand (rows x K) is a grid of 128 x 32 blocks, a B
-// operand (output columns x K) a grid of 64 x 32 blocks; each block stores
-// its hi half then its lo half, blocks ordered K-chunk fastest. The tiles are
-// zero-padded to those multiples. The epilogue of each pass writes its result
-// in the layout the next pass reads, so no pass converts its inputs.
+// Passes of one spectral solve (the passes of the FP32 GEMM form):
+//   t1 = rho Cx^T ; t2 = (Cy t1) / lambda ; t3 = Cy^T t2 ; phi = t3 Cx.
+// The dynamic operands (rho, t1, t2, t3) are sliced by a memory-bound slice
+// phase before each pass. The scale of a row needs the whole row's maximum: a
+// warp per row finds it for the A operands (rho, t3); for the B operands (t1,
+// t2), whose rows are the grid's columns, the previous pass's epilogue
+// gathers it with atomicMax on the float bits of |x|, an order-independent
+// and so deterministic reduction. Each pass's epilogue writes its result as a
+// double-float pair grid. The bases are sliced once on the host from FP64.
+//
+// Operand layout. Sliced operands live in global memory in the exact byte
+// layout the MMA reads from shared memory: the canonical K-major no-swizzle
+// layout of 8-row x 16-byte core matrices (128 B between K-adjacent core
+// matrices, 512 B between 8-row groups), cut into blocks of 32 K-elements.
+// An A operand (rows x K) is a grid of 128 x 32 blocks, a B operand (output
+// columns x K) a grid of 64 x 32 blocks; a block stores its four slices one
+// after another, blocks ordered K-chunk fastest, zero-padded.
 //
 // One 128 x 64 output tile per block iteration. Thread 0 runs a four-stage
 // pipeline: TMA tensor copies (cp.async.bulk.tensor through the operands'
 // tensor maps, complete_tx on a "full" mbarrier) keep the next three K-chunks
-// in flight while the six MMAs of
-// chunk c (two K = 16 steps x three split terms) run, and each commit
-// arrives on that stage's "empty" mbarrier before the stage is reloaded.
-// The accumulator occupies 64 TMEM columns (row i = lane i); the epilogue
-// reads it with tcgen05.ld, warp w taking lanes 32 (w mod 4) ... + 31 and
-// columns 32 (w / 4) ... + 31.
+// in flight while the twenty MMAs of chunk c (two K = 16 steps x ten slice
+// pairs) run, and each commit arrives on that stage's "empty" mbarrier
+// before the stage is reloaded. The four accumulators occupy 4 x 64 TMEM
+// columns (row i = lane i); the epilogue reads them with tcgen05.ld, warp w
+// taking lanes 32 (w mod 4) ... + 31 and columns 32 (w / 4) ... + 31.
 //
 // Every wait is bounded. When one runs out the block records it (shared
 // `failed` and the caller's error word), waits once more (bounded) for its
@@ -30,6 +51,9 @@
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -40,23 +64,27 @@ constexpr int kM = 128;                        // accumulator rows (TMEM lanes)
 constexpr int kN = 64;                         // accumulator columns per tile
 constexpr int kKC = 32;                        // K per block / pipeline stage
 constexpr int kStages = 4;                     // chunks in flight (TMA prefetch depth)
-constexpr uint32_t kCols = 64;                 // TMEM columns per block
+constexpr int kSlices = 4;                     // 8-bit integer slices per value
+constexpr int kLevels = 4;                     // accumulators: slice pairs with i + j = level
+constexpr uint32_t kCols = kLevels * kN;       // TMEM columns per block
 constexpr uint32_t kCore = 128;                // one 8 x 16 B core matrix
 constexpr uint32_t kSbo = (kKC / 8) * kCore;   // next 8-row group
 constexpr uint32_t kLbo = kCore;               // next 8-element K group
-constexpr uint32_t kABlock = 2u * kM * kKC;    // elements of one A block (hi + lo)
-constexpr uint32_t kBBlock = 2u * kN * kKC;    // elements of one B block
-constexpr uint32_t kTx = (kABlock + kBBlock) * 2u;   // bytes per stage
+constexpr uint32_t kASlice = (uint32_t)kM * kKC;    // elements of one slice of an A block
+constexpr uint32_t kBSlice = (uint32_t)kN * kKC;
+constexpr uint32_t kABlock = kSlices * kASlice;     // elements of one A block (all slices)
+constexpr uint32_t kBBlock = kSlices * kBSlice;
+constexpr uint32_t kTx = (kABlock + kBBlock) * 2u;  // bytes per stage
 constexpr unsigned kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
                             ((uint32_t)(kM >> 4) << 24);
 
-// TMA descriptors of the tiled operands, each a 2-D view of one operand
-// buffer as rows of 128 bytes (64 bf16 halves): an A block is a 64 x 128
-// box (16 KB), a B block a 64 x 64 box (8 KB). The data are already in the
+// TMA descriptors of the sliced operands, each a 2-D view of one operand
+// buffer as rows of 128 bytes (64 bf16 values): an A block is a 64 x 256 box
+// (32 KB), a B block a 64 x 128 box (16 KB). The data are already in the
 // MMA's shared-memory layout, so the copies use no swizzle.
-enum TcMap { TM_RHO = 0, TM_T1, TM_T2, TM_T3, TM_CXB, TM_CYA, TM_CYTA, TM_CXTB, TM_COUNT };
+enum TcMap { TM_OPA = 0, TM_OPB, TM_CXB, TM_CYA, TM_CYTA, TM_CXTB, TM_COUNT };
 struct alignas(64) TcMaps {
   CUtensorMap m[TM_COUNT];
 };
@@ -66,23 +94,83 @@ __host__ __device__ inline uint32_t kmaj(int r, int k) {
   return (uint32_t)(r >> 3) * kSbo + (uint32_t)(k >> 3) * kCore + (uint32_t)(r & 7) * 16u + (uint32_t)(k & 7) * 2u;
 }
 __host__ __device__ inline int pad(int n, int m) { return (n + m - 1) / m * m; }
-// element index of (row r, k) half `half` in an A operand with K padded to kp
-__host__ __device__ inline size_t a_index(int r, int k, int kp, int half) {
+// element index of (row r, k) slice s in an A operand with K padded to kp
+__host__ __device__ inline size_t a_index(int r, int k, int kp, int s) {
   const size_t blk = ((size_t)(r >> 7) * (size_t)(kp >> 5) + (size_t)(k >> 5)) * kABlock;
-  return blk + (size_t)half * (kM * kKC) + kmaj(r & 127, k & 31) / 2;
+  return blk + (size_t)s * kASlice + kmaj(r & 127, k & 31) / 2;
 }
-// element index of (output column n, k) half `half` in a B operand
-__host__ __device__ inline size_t b_index(int n, int k, int kp, int half) {
+// element index of (output column n, k) slice s in a B operand
+__host__ __device__ inline size_t b_index(int n, int k, int kp, int s) {
   const size_t blk = ((size_t)(n >> 6) * (size_t)(kp >> 5) + (size_t)(k >> 5)) * kBBlock;
-  return blk + (size_t)half * (kN * kKC) + kmaj(n & 63, k & 31) / 2;
+  return blk + (size_t)s * kBSlice + kmaj(n & 63, k & 31) / 2;
 }
-__host__ __device__ inline void split(float v, uint16_t& hi, uint16_t& lo) {
-  const __nv_bfloat16 h = __float2bfloat16_rn(v);
-  hi = __bfloat16_as_ushort(h);
-  lo = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+// Operand sizes in elements (all fields).
+__host__ __device__ inline size_t a_elems(int rows, int k, int fields) {
+  return (size_t)pad(rows, kM) * pad(k, kKC) * kSlices * fields;
+}
+__host__ __device__ inline size_t b_elems(int cols, int k, int fields) {
+  return (size_t)pad(cols, kN) * pad(k, kKC) * kSlices * fields;
+}
+
+// Row scale: the exponent e with max|row| <= 2^e (0 for an all-zero row).
+inline int row_exponent_host(double mx) {
+  if (!(mx > 0.0)) return 0;
+  int e = 0;
+  std::frexp(mx, &e);   // mx = m 2^e, m in [0.5, 1)
+  return e;
+}
+// bfloat16 bits of an integer of magnitude <= 256 (exact: <= 8 significant bits)
+inline uint16_t int_bf16_host(double s) {
+  const float f = (float)s;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return (uint16_t)(u >> 16);
+}
+// The four slices of an FP64 value at row exponent e (host: the bases).
+inline void slice_host(double v, int e, uint16_t out[kSlices]) {
+  double x = std::ldexp(v, 7 - e);
+  for (int i = 0; i < kSlices; ++i) {
+    const double s = std::nearbyint(x);
+    out[i] = int_bf16_host(s);
+    x = (x - s) * 256.0;
+  }
 }
 
 #ifdef __CUDACC__
+__device__ __forceinline__ float pow2f(int e) {
+  return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.0f, e);
+}
+__device__ __forceinline__ int row_exponent(unsigned max_bits) {
+  const float m = __uint_as_float(max_bits);
+  if (!(m > 0.f)) return 0;
+  int e = 0;
+  frexpf(m, &e);
+  return e;
+}
+__device__ __forceinline__ uint16_t int_bf16(float s) { return __bfloat16_as_ushort(__float2bfloat16_rn(s)); }
+// The four slices of the double-float value hi + lo at row exponent e, as
+// bf16 bits: 2^(7-e)(hi + lo) = s0 + 2^-8 s1 + 2^-16 s2 + 2^-24 s3 + O(2^-25).
+// x - rint(x) is exact; adding the scaled lo rounds below the last slice.
+__device__ __forceinline__ void slice_pair(float hi, float lo, float scale, uint16_t s[kSlices]) {
+  const float x = hi * scale;
+  const float s0 = rintf(x);
+  float r = (x - s0) + lo * scale;
+  s[0] = int_bf16(s0);
+#pragma unroll
+  for (int i = 1; i < kSlices; ++i) {
+    r *= 256.f;
+    const float si = rintf(r);
+    r -= si;
+    s[i] = int_bf16(si);
+  }
+}
+// Error-free sum of two floats (Knuth).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
 struct alignas(128) Stage {
   uint16_t a[kABlock];
   uint16_t b[kBBlock];
@@ -187,43 +275,24 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* v) {
 }
 #undef TGP_TC_R
 
-// Where a pass puts its result: the next pass's B operand (epi 0, or 1 with
-// the inverse-eigenvalue scaling), its A operand (epi 2), or the FP32
-// potential with the energy <rho, phi> (epi 3).
+// Where a pass puts its result: the double-float pair grid (epi 0 and 2,
+// epi 1 after the inverse-eigenvalue scaling), with the column maxima the
+// next slice phase needs for epi 0 and 1 (a B operand's rows are the grid's
+// columns), or the FP32 potential with the energy <rho, phi> (epi 3).
 struct Out {
   int epi;
-  uint16_t* t;         // tiled operand for epi 0..2
-  long ts;             // its per-field stride (elements)
-  int kp;              // its padded K
-  float* phi;          // epi 3
-  const float* rho;    // epi 3 (FP32 mean-free density)
-  const float* inv_eig;
+  float2* tp;            // [K][M][N] pair grid (epi 0..2)
+  unsigned* mx;          // column maxima [K][N] for the next B operand (epi 0, 1)
+  float* phi;            // epi 3
+  const float* rho;      // epi 3 (FP32 mean-free density)
+  const float* ie_hi;    // epi 1: 1 / lambda as a double-float pair
+  const float* ie_lo;
+  const int* eA;         // row exponents of A and B (per field stride sa_e / sb_e; 0 = shared)
+  const int* eB;
+  int sa_e, sb_e;
 };
 
-__device__ __forceinline__ void emit(const Out& o, int f, int row, int col, int M, int N, float x, float& e) {
-  const size_t idx = (size_t)row * N + col;
-  uint16_t h, l;
-  switch (o.epi) {
-    case 0:
-    case 1:
-      if (o.epi == 1) x *= o.inv_eig[idx];
-      split(x, h, l);
-      o.t[(size_t)f * o.ts + b_index(col, row, o.kp, 0)] = h;
-      o.t[(size_t)f * o.ts + b_index(col, row, o.kp, 1)] = l;
-      break;
-    case 2:
-      split(x, h, l);
-      o.t[(size_t)f * o.ts + a_index(row, col, o.kp, 0)] = h;
-      o.t[(size_t)f * o.ts + a_index(row, col, o.kp, 1)] = l;
-      break;
-    default:
-      o.phi[(size_t)f * M * N + idx] = x;
-      e = fmaf(o.rho[(size_t)f * M * N + idx], x, e);
-      break;
-  }
-}
-
-// C[f] = A[f] (M x K) * B[f]^T, B given as N x K, both tiled; output tiles
+// C[f] = A[f] (M x K) * B[f]^T, B given as N x K, both sliced; output tiles
 // t = vb, vb + nvb, ... of 128 x 64, written by `out`. kp = K padded to 32.
 // The block must have called setup(); blockDim.x must be 256.
 static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* mB, long sb, int M, int N, int kp,
@@ -275,15 +344,20 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
         ++sm.full_ph[s];
         loading[s] = false;
         fence_after();
-        const uint32_t ahi = saddr(sm.st[s].a), alo = ahi + kM * kKC * 2u;
-        const uint32_t bhi = saddr(sm.st[s].b), blo = bhi + kN * kKC * 2u;
+        const uint32_t abase = saddr(sm.st[s].a), bbase = saddr(sm.st[s].b);
 #pragma unroll
         for (int q = 0; q < kKC / 16; ++q) {
           const uint32_t ko = (uint32_t)q * 2u * kCore;   // two K groups of 8 per MMA
-          const uint32_t acc0 = (c > 0 || q > 0) ? 1u : 0u;
-          mma(sm.tmem, sdesc(alo + ko), sdesc(bhi + ko), acc0);   // small terms first
-          mma(sm.tmem, sdesc(ahi + ko), sdesc(blo + ko), 1u);
-          mma(sm.tmem, sdesc(ahi + ko), sdesc(bhi + ko), 1u);
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i)
+#pragma unroll
+            for (int j = 0; j < kSlices; ++j)
+              if (i + j < kLevels) {
+                // the first product of each accumulator (i = 0) starts it afresh
+                const uint32_t acc = (c > 0 || q > 0 || i > 0) ? 1u : 0u;
+                mma(sm.tmem + (uint32_t)((i + j) * kN), sdesc(abase + i * kASlice * 2u + ko),
+                    sdesc(bbase + j * kBSlice * 2u + ko), acc);
+              }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          saddr(&sm.empty[s]))
@@ -310,22 +384,56 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
     // epilogue: this warp's 32 rows x 32 columns of the tile
     const int q = warp & 3, h = warp >> 2;
     const int row = mt * kM + q * 32 + lane;
+    const bool row_ok = row < M;
+    const float row_scale = pow2f((row_ok ? out.eA[(size_t)f * out.sa_e + row] : 0) - 14);
     float e = 0.f;
 #pragma unroll
     for (int part = 0; part < 2; ++part) {
-      uint32_t v[16];
-      ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 32 + part * 16), v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
+      uint32_t v[kLevels][16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = nt * kN + h * 32 + part * 16 + j;
-          if (col < N) emit(out, f, row, col, M, N, __uint_as_float(v[j]), e);
+      for (int L = 0; L < kLevels; ++L)
+        ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * kN + h * 32 + part * 16), v[L]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int col = nt * kN + h * 32 + part * 16 + j;
+        const bool ok = row_ok && col < N;
+        // join the exact level sums: a0 + 2^-8 a1 + 2^-16 a2 + 2^-24 a3
+        float s, r;
+        two_sum(__uint_as_float(v[0][j]), __uint_as_float(v[1][j]) * 0x1p-8f, s, r);
+        r += __uint_as_float(v[2][j]) * 0x1p-16f;
+        r += __uint_as_float(v[3][j]) * 0x1p-24f;
+        float hi, lo;
+        two_sum(s, r, hi, lo);
+        const float sc = row_scale * pow2f(col < N ? out.eB[(size_t)f * out.sb_e + col] : 0);
+        hi *= sc;
+        lo *= sc;
+        unsigned cbits = 0;
+        if (ok) {
+          const size_t idx = (size_t)row * N + col;
+          if (out.epi == 3) {
+            const float p = hi + lo;
+            out.phi[(size_t)f * M * N + idx] = p;
+            e = fmaf(out.rho[(size_t)f * M * N + idx], p, e);
+          } else {
+            if (out.epi == 1) {   // (hi + lo)(ie_hi + ie_lo) in double-float
+              const float ih = out.ie_hi[idx], il = out.ie_lo[idx];
+              const float p = hi * ih;
+              float pe = fmaf(hi, ih, -p);
+              pe = fmaf(hi, il, fmaf(lo, ih, pe));
+              two_sum(p, pe, hi, lo);
+            }
+            out.tp[(size_t)f * M * N + idx] = make_float2(hi, lo);
+            cbits = __float_as_uint(fabsf(hi));
+          }
+        }
+        if (out.epi == 0 || out.epi == 1) {   // column maxima: one atomic per column and warp
+          const unsigned m = __reduce_max_sync(0xffffffffu, cbits);
+          if (lane == 0 && m && col < N) atomicMax(out.mx + (size_t)f * N + col, m);
         }
       }
     }
     if (out.epi == 3) eacc[f] += (double)e;
-    fence_global_async();
     fence_before();
     __syncthreads();
   }
@@ -333,49 +441,151 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
 }
 
 // Output tiles of one pass (all four passes have the same H x W output).
-__device__ __forceinline__ int pass_tiles(const Dev& d) {
+__host__ __device__ __forceinline__ int pass_tiles_host(const Dev& d) {
   return ((d.g.Hb + kM - 1) / kM) * ((d.g.Wb + kN - 1) / kN) * d.K;
 }
 
-// One of the four GEMM passes of the spectral solve (the passes of the FP32
-// form): t1 = rho Cx^T, t2 = (Cy t1) / lambda, t3 = Cy^T t2, phi = t3 Cx with
-// the energy <rho, phi>.
+// Column-maximum words of t1 (which = 0) and t2 (which = 1): [2][K][Wb].
+__device__ __forceinline__ unsigned* tmx_of(const Dev& d, int which) {
+  return d.tmx + (size_t)which * d.K * d.g.Wb;
+}
+
+// One of the four GEMM passes of the spectral solve.
 static __device__ void dct_pass(const Dev& d, const TcMaps& tm, int step, int vb, int nvb, Smem& sm, double* eacc,
                                 unsigned long long* err) {
   const int W = d.g.Wb, H = d.g.Hb;
-  const long sA = (long)d.Hp128 * d.Wp32 * 2, sB = (long)d.Wp64 * d.Hp32 * 2;
+  const long sA = (long)a_elems(H, W, 1), sB = (long)b_elems(W, H, 1);
+  Out o{};
+  o.tp = d.tp;
+  o.ie_hi = d.inv_eig;
+  o.ie_lo = d.inv_eig_lo;
   switch (step) {
-    case 0: {
-      const Out o{0, d.t1_t, sB, d.Hp32, nullptr, nullptr, nullptr};
-      gemm(&tm.m[TM_RHO], sA, &tm.m[TM_CXB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
+    case 0:   // t1 = rho Cx^T: A = rho (rows y), B = rows of Cx (frequency kx)
+      o.epi = 0;
+      o.mx = tmx_of(d, 0);
+      o.eA = d.eA, o.sa_e = d.Hp128;
+      o.eB = d.eCx, o.sb_e = 0;
+      gemm(&tm.m[TM_OPA], sA, &tm.m[TM_CXB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
-    }
-    case 1: {
-      const Out o{1, d.t2_t, sB, d.Hp32, nullptr, nullptr, d.inv_eig};
-      gemm(&tm.m[TM_CYA], 0, &tm.m[TM_T1], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+    case 1:   // t2 = (Cy t1) / lambda: A = rows of Cy (ky), B = t1 columns (kx)
+      o.epi = 1;
+      o.mx = tmx_of(d, 1);
+      o.eA = d.eCy, o.sa_e = 0;
+      o.eB = d.eB, o.sb_e = d.Wp64;
+      gemm(&tm.m[TM_CYA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
-    }
-    case 2: {
-      const Out o{2, d.t3_t, sA, d.Wp32, nullptr, nullptr, nullptr};
-      gemm(&tm.m[TM_CYTA], 0, &tm.m[TM_T2], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+    case 2:   // t3 = Cy^T t2: A = rows of Cy^T (y), B = t2 columns (kx)
+      o.epi = 2;
+      o.eA = d.eCy + d.g.Hb, o.sa_e = 0;
+      o.eB = d.eB, o.sb_e = d.Wp64;
+      gemm(&tm.m[TM_CYTA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
-    }
-    default: {
-      const Out o{3, nullptr, 0, 0, d.phi, d.rho, nullptr};
-      gemm(&tm.m[TM_T3], sA, &tm.m[TM_CXTB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
+    default:  // phi = t3 Cx: A = t3 (rows y), B = rows of Cx^T (x)
+      o.epi = 3;
+      o.phi = d.phi;
+      o.rho = d.rho;
+      o.eA = d.eA, o.sa_e = d.Hp128;
+      o.eB = d.eCx + d.g.Wb, o.sb_e = 0;
+      gemm(&tm.m[TM_OPA], sA, &tm.m[TM_CXTB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
       break;
-    }
   }
 }
 
-// The A-operand form of one mean-free density value (pass 0's input).
-__device__ __forceinline__ void put_rho(const Dev& d, int f, int i, float v) {
-  const int y = i / d.g.Wb, x = i % d.g.Wb;
-  uint16_t h, l;
-  split(v, h, l);
-  const size_t base = (size_t)f * d.Hp128 * d.Wp32 * 2;
-  d.rho_t[base + a_index(y, x, d.Wp32, 0)] = h;
-  d.rho_t[base + a_index(y, x, d.Wp32, 1)] = l;
+// The slice phase before GEMM pass `step`: the dynamic operand of the pass
+// from its FP32 / pair grid. An A operand (rho before pass 0, t3 before pass
+// 3; rows y over K = x) takes one warp per row, which finds the row's maximum
+// itself; a B operand (t1 before pass 1, t2 before pass 2; rows kx over K =
+// y) takes its column maxima from the previous pass's epilogue. Before pass
+// 0 it clears the t1 maxima and before pass 1 the t2 maxima (both last read
+// one solve ago), so each is empty when its pass gathers into it.
+static __device__ void slice_phase(const Dev& d, int step, int vb, int nvb) {
+  const int W = d.g.Wb, H = d.g.Hb, K = d.K;
+  const int lane = threadIdx.x & 31;
+  if (step == 0 || step == 1) {
+    unsigned* z = tmx_of(d, step);
+    for (int i = vb * blockDim.x + threadIdx.x; i < K * W; i += nvb * blockDim.x) z[i] = 0u;
+  }
+  if (step == 0 || step == 3) {
+    const int wpb = blockDim.x >> 5;
+    const int ng = d.Wp32 / 8;
+    const size_t fs = a_elems(H, W, 1);
+    for (int rw = vb * wpb + (threadIdx.x >> 5); rw < K * H; rw += nvb * wpb) {
+      const int f = rw / H, y = rw % H;
+      const float* rrow = d.rho + (size_t)f * d.B + (size_t)y * W;
+      const float2* prow = d.tp + (size_t)f * d.B + (size_t)y * W;
+      unsigned m = 0;
+      for (int x = lane; x < W; x += 32)
+        m = max(m, __float_as_uint(fabsf(step == 0 ? rrow[x] : prow[x].x)));
+      m = __reduce_max_sync(0xffffffffu, m);
+      const int e = row_exponent(m);
+      if (lane == 0) d.eA[(size_t)f * d.Hp128 + y] = e;
+      const float sc = pow2f(7 - e);
+      uint16_t* dst = d.opA + (size_t)f * fs;
+      for (int g = lane; g < ng; g += 32) {
+        uint16_t sl[kSlices][8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int x = g * 8 + k;
+          float hi = 0.f, lo = 0.f;
+          if (x < W) {
+            if (step == 0) {
+              hi = rrow[x];
+            } else {
+              const float2 p = prow[x];
+              hi = p.x;
+              lo = p.y;
+            }
+          }
+          uint16_t s[kSlices];
+          slice_pair(hi, lo, sc, s);
+#pragma unroll
+          for (int i = 0; i < kSlices; ++i) sl[i][k] = s[i];
+        }
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) {
+          uint4 w;
+          w.x = (uint32_t)sl[i][0] | ((uint32_t)sl[i][1] << 16);
+          w.y = (uint32_t)sl[i][2] | ((uint32_t)sl[i][3] << 16);
+          w.z = (uint32_t)sl[i][4] | ((uint32_t)sl[i][5] << 16);
+          w.w = (uint32_t)sl[i][6] | ((uint32_t)sl[i][7] << 16);
+          *reinterpret_cast<uint4*>(dst + a_index(y, g * 8, d.Wp32, i)) = w;
+        }
+      }
+    }
+  } else {
+    // B operand: groups of 8 consecutive y of one column, consecutive
+    // threads on consecutive columns (coalesced reads of the pair rows)
+    const unsigned* mx = tmx_of(d, step - 1);
+    const int ng = d.Hp32 / 8;
+    const size_t fs = b_elems(W, H, 1);
+    for (int it = vb * blockDim.x + threadIdx.x; it < K * ng * W; it += nvb * blockDim.x) {
+      const int f = it / (ng * W), rem = it % (ng * W), g = rem / W, n = rem % W;
+      const int e = row_exponent(mx[(size_t)f * W + n]);
+      if (g == 0) d.eB[(size_t)f * d.Wp64 + n] = e;
+      const float sc = pow2f(7 - e);
+      uint16_t sl[kSlices][8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int y = g * 8 + k;
+        float2 p = make_float2(0.f, 0.f);
+        if (y < H) p = d.tp[(size_t)f * d.B + (size_t)y * W + n];
+        uint16_t s[kSlices];
+        slice_pair(p.x, p.y, sc, s);
+#pragma unroll
+        for (int i = 0; i < kSlices; ++i) sl[i][k] = s[i];
+      }
+      uint16_t* dst = d.opB + (size_t)f * fs;
+#pragma unroll
+      for (int i = 0; i < kSlices; ++i) {
+        uint4 w;
+        w.x = (uint32_t)sl[i][0] | ((uint32_t)sl[i][1] << 16);
+        w.y = (uint32_t)sl[i][2] | ((uint32_t)sl[i][3] << 16);
+        w.z = (uint32_t)sl[i][4] | ((uint32_t)sl[i][5] << 16);
+        w.w = (uint32_t)sl[i][6] | ((uint32_t)sl[i][7] << 16);
+        *reinterpret_cast<uint4*>(dst + b_index(n, g * 8, d.Hp32, i)) = w;
+      }
+    }
+  }
 }
 #endif  // __CUDACC__
 

@@ -106,9 +106,12 @@ struct SpectralTables {
 };
 struct BasisTables {
   float *c = nullptr, *ct = nullptr;   // FP32 C and C^T, row-major n x n
-  // tensor-core operands (dct_tc.cuh layout): C and C^T as B operands
-  // (rows padded to 64) and as A operands (rows padded to 128), K padded to 32
+  // tensor-core operands (dct_tc.cuh layout, four integer slices of the FP64
+  // values): C and C^T as B operands (rows padded to 64) and as A operands
+  // (rows padded to 128), K padded to 32; `e` the row exponents, [n] for the
+  // rows of C then [n] for the rows of C^T
   uint16_t *cB = nullptr, *ctB = nullptr, *cA = nullptr, *ctA = nullptr;
+  int* e = nullptr;
 };
 cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
   static std::mutex mu;
@@ -120,30 +123,41 @@ cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
     const size_t nn = (size_t)n * n;
     const int N = (int)n, kp = tc::pad(N, tc::kKC);
     std::vector<float> m(nn), mt(nn);
-    std::vector<uint16_t> cB((size_t)tc::pad(N, tc::kN) * kp * 2, 0), ctB(cB.size(), 0);
-    std::vector<uint16_t> cA((size_t)tc::pad(N, tc::kM) * kp * 2, 0), ctA(cA.size(), 0);
+    std::vector<uint16_t> cB(tc::b_elems(N, N, 1), 0), ctB(cB.size(), 0);
+    std::vector<uint16_t> cA(tc::a_elems(N, N, 1), 0), ctA(cA.size(), 0);
+    std::vector<int> e(2 * (size_t)n, 0);
+    std::vector<double> rmax(n, 0.0), cmax(n, 0.0);
     for (int i = 0; i < N; ++i)
       for (int j = 0; j < N; ++j) {
-        const float v = (float)b[(size_t)i * n + j];   // C[i][j] = C^T[j][i]
-        m[(size_t)i * n + j] = v;
-        mt[(size_t)j * n + i] = v;
-        uint16_t h, l;
-        tc::split(v, h, l);
-        cB[tc::b_index(i, j, kp, 0)] = h;
-        cB[tc::b_index(i, j, kp, 1)] = l;
-        ctB[tc::b_index(j, i, kp, 0)] = h;
-        ctB[tc::b_index(j, i, kp, 1)] = l;
-        cA[tc::a_index(i, j, kp, 0)] = h;
-        cA[tc::a_index(i, j, kp, 1)] = l;
-        ctA[tc::a_index(j, i, kp, 0)] = h;
-        ctA[tc::a_index(j, i, kp, 1)] = l;
+        const double v = std::fabs(b[(size_t)i * n + j]);
+        rmax[i] = std::max(rmax[i], v);
+        cmax[j] = std::max(cmax[j], v);
+      }
+    for (int i = 0; i < N; ++i) {
+      e[i] = tc::row_exponent_host(rmax[i]);
+      e[n + i] = tc::row_exponent_host(cmax[i]);
+    }
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        const double v = b[(size_t)i * n + j];   // C[i][j] = C^T[j][i]
+        m[(size_t)i * n + j] = (float)v;
+        mt[(size_t)j * n + i] = (float)v;
+        uint16_t sr[tc::kSlices], sc[tc::kSlices];
+        tc::slice_host(v, e[i], sr);       // in row i of C
+        tc::slice_host(v, e[n + j], sc);   // in row j of C^T
+        for (int s = 0; s < tc::kSlices; ++s) {
+          cB[tc::b_index(i, j, kp, s)] = sr[s];
+          cA[tc::a_index(i, j, kp, s)] = sr[s];
+          ctB[tc::b_index(j, i, kp, s)] = sc[s];
+          ctA[tc::a_index(j, i, kp, s)] = sc[s];
+        }
       }
     BasisTables t;
-    cudaError_t e = cudaSuccess;
+    cudaError_t err = cudaSuccess;
     auto up = [&](auto** dst, const auto& v) {
-      if (e != cudaSuccess) return;
-      e = cudaMalloc((void**)dst, v.size() * sizeof(v[0]));
-      if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) return;
+      err = cudaMalloc((void**)dst, v.size() * sizeof(v[0]));
+      if (err == cudaSuccess) err = cudaMemcpy(*dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
     };
     up(&t.c, m);
     up(&t.ct, mt);
@@ -151,7 +165,8 @@ cudaError_t shared_basis(int device, uint32_t n, BasisTables* out) {
     up(&t.ctB, ctB);
     up(&t.cA, cA);
     up(&t.ctA, ctA);
-    if (e != cudaSuccess) return e;
+    up(&t.e, e);
+    if (err != cudaSuccess) return err;
     it = cache.emplace(std::make_pair(device, n), t).first;
   }
   *out = it->second;
@@ -223,14 +238,19 @@ cudaError_t shared_inv_eig(int device, uint32_t Wb, uint32_t Hb, float** out) {
   std::lock_guard<std::mutex> lk(mu);
   auto it = cache.find({device, Wb, Hb});
   if (it == cache.end()) {
-    std::vector<float> ie((size_t)Wb * Hb);
+    // [B] FP32 values of 1 / lambda, then [B] their low parts (1/lambda - hi)
+    const size_t nb = (size_t)Wb * Hb;
+    std::vector<float> ie(2 * nb, 0.0f);
     for (uint32_t ky = 0; ky < Hb; ++ky) {
       const double sy = std::sin(3.14159265358979323846 * ky / (2.0 * Hb));
       const double ly = 4.0 * (sy * sy);
       for (uint32_t kx = 0; kx < Wb; ++kx) {
         const double sx = std::sin(3.14159265358979323846 * kx / (2.0 * Wb));
         const double l = 4.0 * (sx * sx) + ly;
-        ie[(size_t)ky * Wb + kx] = (kx == 0 && ky == 0) ? 0.0f : (float)(1.0 / l);
+        const double v = (kx == 0 && ky == 0) ? 0.0 : 1.0 / l;
+        const float hi = (float)v;
+        ie[(size_t)ky * Wb + kx] = hi;
+        ie[nb + (size_t)ky * Wb + kx] = (float)(v - (double)hi);
       }
     }
     float* d = nullptr;
@@ -477,8 +497,10 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&D.fill, K * B);
   S.zeroed(&D.rho, K * B);
   // t1 / t2: FP32 grids of the GEMM forms; the FFT form keeps them as
-  // double-float pairs (float2 per bin), hence twice the size
+  // double-float pairs (float2 per bin), hence twice the size, and the
+  // tensor-core form its pass outputs (tp) in t1
   S.zeroed(&D.t1, 2 * K * B);
+  D.tp = reinterpret_cast<float2*>(D.t1);
   S.zeroed(&D.t2, 2 * K * B);
   S.zeroed(&D.phi, K * B);
   S.zeroed(&D.wa_fix, 2 * (size_t)h.U);
@@ -501,13 +523,12 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&r.q.isum, (size_t)kISlots * kMaxPartials);
   S.zeroed(&r.q.mx, (size_t)kMSlots * kMaxPartials);
   S.zeroed(&r.iscal, kIScalars);
-  if (h.params.dct_mode == TEXO_GP_DCT_BF16X3) {   // tensor-core operands (zero padding)
-    const size_t a = (size_t)tc::pad((int)h.Hb, tc::kM) * tc::pad((int)h.Wb, tc::kKC) * 2 * K;
-    const size_t b = (size_t)tc::pad((int)h.Wb, tc::kN) * tc::pad((int)h.Hb, tc::kKC) * 2 * K;
-    S.zeroed(&D.rho_t, a);
-    S.zeroed(&D.t3_t, a);
-    S.zeroed(&D.t1_t, b);
-    S.zeroed(&D.t2_t, b);
+  if (h.params.dct_mode == TEXO_GP_DCT_TENSOR) {   // tensor-core operands (zero padding)
+    S.zeroed(&D.opA, tc::a_elems((int)h.Hb, (int)h.Wb, (int)K));
+    S.zeroed(&D.opB, tc::b_elems((int)h.Wb, (int)h.Hb, (int)K));
+    S.zeroed(&D.eA, (size_t)tc::pad((int)h.Hb, tc::kM) * K);
+    S.zeroed(&D.eB, (size_t)tc::pad((int)h.Wb, tc::kN) * K);
+    S.zeroed(&D.tmx, 2 * (size_t)h.Wb * K);
   }
 }
 
@@ -559,7 +580,10 @@ int32_t Instance::upload() {
     D.Cy = by.c;
     D.CyT = by.ct;
     D.inv_eig = ie;
-    D.tc = h.params.dct_mode == TEXO_GP_DCT_BF16X3 ? 1 : 0;
+    D.inv_eig_lo = ie + (size_t)h.Wb * h.Hb;
+    D.eCx = bx.e;
+    D.eCy = by.e;
+    D.tc = h.params.dct_mode == TEXO_GP_DCT_TENSOR ? 1 : 0;
     // fixed rule unless autotuned: large tiles once the grid has >= 1024 32x32 blocks
     D.dct_large = (long long)((h.Wb + 31) / 32) * ((h.Hb + 31) / 32) >= 1024 ? 1 : 0;
     // the FFT form for power-of-two grids (FP32 mode)
@@ -631,17 +655,15 @@ int32_t Instance::upload() {
     h_scal[SC_E0 + f] = 1.0;
     h_scal[SC_LAMBDA + f] = 0.0;
   }
-  if (h.params.dct_mode == TEXO_GP_DCT_BF16X3) {   // tensor maps of the tensor-core operands
-    const size_t a = (size_t)D.Hp128 * D.Wp32 * 2 * K, b = (size_t)D.Wp64 * D.Hp32 * 2 * K;
+  if (h.params.dct_mode == TEXO_GP_DCT_TENSOR) {   // tensor maps of the tensor-core operands
+    const int W = (int)h.Wb, H = (int)h.Hb;
     const uint32_t ra = tc::kABlock / 64, rb = tc::kBBlock / 64;
-    TRY(encode_operand_map(&tmaps.m[tc::TM_RHO], D.rho_t, a, ra));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_T3], D.t3_t, a, ra));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_T1], D.t1_t, b, rb));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_T2], D.t2_t, b, rb));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_CXB], D.CxB_t, (size_t)D.Wp64 * D.Wp32 * 2, rb));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_CXTB], D.CxTB_t, (size_t)D.Wp64 * D.Wp32 * 2, rb));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_CYA], D.CyA_t, (size_t)D.Hp128 * D.Hp32 * 2, ra));
-    TRY(encode_operand_map(&tmaps.m[tc::TM_CYTA], D.CyTA_t, (size_t)D.Hp128 * D.Hp32 * 2, ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_OPA], D.opA, tc::a_elems(H, W, (int)K), ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_OPB], D.opB, tc::b_elems(W, H, (int)K), rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CXB], D.CxB_t, tc::b_elems(W, W, 1), rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CXTB], D.CxTB_t, tc::b_elems(W, W, 1), rb));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CYA], D.CyA_t, tc::a_elems(H, H, 1), ra));
+    TRY(encode_operand_map(&tmaps.m[tc::TM_CYTA], D.CyTA_t, tc::a_elems(H, H, 1), ra));
   }
   // the staging buffer is reused by this thread's next upload
   CU(cudaStreamSynchronize(stream));
@@ -1302,11 +1324,11 @@ int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_g
     prm = &defaults;
   }
   if (!p) return TEXO_GP_ERR_INVALID_ARGUMENT;
-  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_BF16X3 &&
+  if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_TENSOR &&
       prm->dct_mode != TEXO_GP_DCT_FP32_GEMM)
     return TEXO_GP_ERR_INVALID_ARGUMENT;
-  if (prm->dct_mode == TEXO_GP_DCT_BF16X3 && prm->engine == TEXO_GP_ENGINE_DEVICE) {
-    set_last_error("the BF16x3 tensor-core DCT runs with the host engine only");
+  if (prm->dct_mode == TEXO_GP_DCT_TENSOR && prm->engine == TEXO_GP_ENGINE_DEVICE) {
+    set_last_error("the tensor-core DCT runs with the host engine only");
     return TEXO_GP_ERR_UNSUPPORTED;
   }
   auto h = std::make_unique<texo_gp_handle_s>();
@@ -1332,7 +1354,7 @@ namespace {
 // The autotuner: times the four DCT passes of every admissible form on this
 // instance (5 repetitions after a warm-up, CUDA events on its stream) and
 // keeps the fastest. The FP32 tile families are always admissible; the
-// tensor-core form only when the caller asked for BF16x3 (the FP32 forms are
+// tensor-core form only when the caller asked for it (the FP32 forms are
 // more accurate, so they may replace it). Choices are cached per device,
 // grid, field count, engine and requested mode.
 int32_t autotune_dct(Instance& I) {
@@ -1342,7 +1364,7 @@ int32_t autotune_dct(Instance& I) {
   const texo_gp_params& prm = I.m.params;
   std::vector<Form> forms = {{0, 0, 0}, {1, 0, 0}};
   if (fft_length(I.m.Wb) && fft_length(I.m.Hb) && prm.dct_mode != TEXO_GP_DCT_FP32_GEMM) forms.push_back({0, 0, 1});
-  if (prm.dct_mode == TEXO_GP_DCT_BF16X3 && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1, 0});
+  if (prm.dct_mode == TEXO_GP_DCT_TENSOR && prm.engine == TEXO_GP_ENGINE_HOST) forms.push_back({0, 1, 0});
   static std::mutex mu;
   static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, int, int>, Form> cache;
   const auto key = std::make_tuple(I.device, I.m.Wb, I.m.Hb, I.m.K, prm.engine, prm.dct_mode);
@@ -1678,7 +1700,6 @@ int32_t texo_gp_poisson(texo_gp_handle h, const double* density, double* potenti
   Dev D = I.d;
   D.K = 1;
   CU(cudaMemcpyAsync(D.rho, rho.data(), B * 4, cudaMemcpyHostToDevice, I.stream));
-  if (D.tc) launch_tile_rho(D, I.nvb, I.stream);
   for (int st = 0; st < 4; ++st) launch_dct(D, I.r, st, I.nvb, I.stream, &I.tmaps);
   launch_finalize(D, I.r, I.nvb, FIN_ENERGY, I.stream);
   std::vector<float> phi(B);

@@ -5,12 +5,6 @@
 
 namespace tgp {
 
-// The tensor cores' A-operand form of rho (for callers that set rho directly).
-__global__ void __launch_bounds__(kThreads) k_tile_rho(Dev d) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.K * d.B; i += gridDim.x * blockDim.x)
-    tc::put_rho(d, i / d.B, i % d.B, d.rho[i]);
-}
-
 // The FFT form's three passes (dct_fft.cuh).
 __global__ void __launch_bounds__(kThreads) k_fft_rows_fwd(Dev d, Partials p) {
   __shared__ fft::Smem sm;
@@ -27,21 +21,31 @@ __global__ void __launch_bounds__(kThreads) k_fft_rows_inv(Dev d, Partials p) {
   fft::pass_rows_inv(d, p, blockIdx.x, gridDim.x, sm, sh);
 }
 
-// One DCT pass on tcgen05 tensor cores (BF16x3), one 128 x 64 tile per block
-// iteration; the energy partials of pass 3 are per block as in k_dct.
-__global__ void __launch_bounds__(kThreads) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err,
-                                                    const __grid_constant__ tc::TcMaps maps) {
+// The slice phase before tensor-core pass `step` (memory-bound, every block).
+__global__ void __launch_bounds__(kThreads) k_tc_slice(Dev d, int step) {
+  tc::slice_phase(d, step, blockIdx.x, gridDim.x);
+}
+
+// One DCT pass on tcgen05 tensor cores, one 128 x 64 tile per block
+// iteration; gridDim.x <= the pass's tiles. The energy partials of pass 3 are
+// those of the blocks launched; the slice phase before it zeroes the rest.
+__global__ void __launch_bounds__(kThreads, 1) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err,
+                                                       const __grid_constant__ tc::TcMaps maps) {
   extern __shared__ __align__(128) unsigned char tc_dyn[];
   tc::Smem& sm = *reinterpret_cast<tc::Smem*>(tc_dyn);
   __shared__ Shared sh;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
-  if ((int)blockIdx.x < tc::pass_tiles(d)) {   // blocks without a tile only write zero partials
-    tc::setup(sm);
-    tc::dct_pass(d, maps, step, blockIdx.x, gridDim.x, sm, eacc, err);
-    tc::teardown(sm);
-  }
+  tc::setup(sm);
+  tc::dct_pass(d, maps, step, blockIdx.x, gridDim.x, sm, eacc, err);
+  tc::teardown(sm);
   if (step == 3)
     for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), (int)blockIdx.x, sh.d);
+}
+// Zero energy partials of the virtual blocks [from, nvb) (pass 3 runs fewer).
+__global__ void __launch_bounds__(kThreads) k_zero_energy(Dev d, Partials p, int from) {
+  __shared__ Shared sh;
+  if ((int)blockIdx.x >= from)
+    for (int f = 0; f < d.K; ++f) write_partial(0.0, pslot(p, SLOT_ENERGY + f), (int)blockIdx.x, sh.d);
 }
 
 __global__ void __launch_bounds__(kThreads) k_init(Dev d, bool grids, bool wa) {
@@ -229,10 +233,6 @@ void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s) {
   COUNT;
   k_prep<<<nvb, kThreads, 0, s>>>(d, r.p);
 }
-void launch_tile_rho(const Dev& d, int nvb, cudaStream_t s) {
-  COUNT;
-  k_tile_rho<<<nvb, kThreads, 0, s>>>(d);
-}
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s, const tc::TcMaps* maps) {
   if (d.fft) {   // rows, columns (forward, scale, inverse), rows: step 2 has no work
     if (step == 2) return;
@@ -245,16 +245,26 @@ void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s
       k_fft_rows_inv<<<nvb, kThreads, 0, s>>>(d, r.p);
     return;
   }
-  COUNT;
   if (d.tc) {
     if (!maps) return;   // the tensor-core form needs the instance's tensor maps
     static const bool attr = cudaFuncSetAttribute(k_dct_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)sizeof(tc::Smem)) == cudaSuccess;
     (void)attr;
-    k_dct_tc<<<nvb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL),
-                                                     *maps);
+    // one block a tile (at most one resident a multiprocessor: the pipeline
+    // holds 192 KB of shared memory and 256 TMEM columns)
+    const int gb = std::max(1, std::min(nvb, tc::pass_tiles_host(d)));
+    COUNT;
+    k_tc_slice<<<nvb, kThreads, 0, s>>>(d, step);
+    if (step == 3 && gb < nvb) {
+      COUNT;
+      k_zero_energy<<<nvb, kThreads, 0, s>>>(d, r.p, gb);
+    }
+    COUNT;
+    k_dct_tc<<<gb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL),
+                                                    *maps);
     return;
   }
+  COUNT;
   if (use_large_tiles(d))
     k_dct<true><<<nvb, kThreads, 0, s>>>(d, r.p, step);
   else

@@ -360,7 +360,6 @@ static __device__ void stage_prep(const Dev& d, Partials p, int nvb_scatter, int
         cnt[f] += 1;
       }
       rho[i] = __ll2float_rn(a + fl[i] - mean) * kInvFixF;
-      if (d.tc) tc::put_rho(d, f, i, rho[i]);
     }
   }
   for (int f = 0; f < d.K; ++f) {

@@ -359,11 +359,11 @@ class Placer:
                  "other", "barrier_wait", "barriers"]
         return dict(zip(names, out.tolist()))
 
-    DCT_FORMS = ("gemm16", "gemm64", "tensor_core_bf16x3", "fft")
+    DCT_FORMS = ("gemm16", "gemm64", "tensor_core", "fft")
 
     def dct_form(self):
         """The DCT form this instance runs: 0 GEMM (16-bin tiles), 1 GEMM
-        (64-bin tiles), 2 tensor cores (BF16x3), 3 FFT."""
+        (64-bin tiles), 2 tensor cores (integer slices, exact accumulation), 3 FFT."""
         f = C.c_int32()
         abi.check(self.lib.texo_gp_dct_form(self.h, C.byref(f)), "texo_gp_dct_form")
         return int(f.value)
