@@ -61,9 +61,12 @@ namespace tgp {
 namespace tc {
 
 constexpr int kM = 128;                        // accumulator rows (TMEM lanes)
-constexpr int kN = 64;                         // accumulator columns per tile
+#ifndef TGP_TC_N
+#define TGP_TC_N 64
+#endif
+constexpr int kN = TGP_TC_N;                   // accumulator columns per tile (64 or 128)
 constexpr int kKC = 32;                        // K per block / pipeline stage
-constexpr int kStages = 4;                     // chunks in flight (TMA prefetch depth)
+constexpr int kStages = kN == 64 ? 4 : 3;     // chunks in flight (TMA prefetch depth)
 constexpr int kSlices = 4;                     // 8-bit integer slices per value
 constexpr int kLevels = 4;                     // accumulators: slice pairs with i + j = level
 constexpr uint32_t kCols = kLevels * kN;       // TMEM columns per block
@@ -101,8 +104,8 @@ __host__ __device__ inline size_t a_index(int r, int k, int kp, int s) {
 }
 // element index of (output column n, k) slice s in a B operand
 __host__ __device__ inline size_t b_index(int n, int k, int kp, int s) {
-  const size_t blk = ((size_t)(n >> 6) * (size_t)(kp >> 5) + (size_t)(k >> 5)) * kBBlock;
-  return blk + (size_t)s * kBSlice + kmaj(n & 63, k & 31) / 2;
+  const size_t blk = ((size_t)(n / kN) * (size_t)(kp >> 5) + (size_t)(k >> 5)) * kBBlock;
+  return blk + (size_t)s * kBSlice + kmaj(n % kN, k & 31) / 2;
 }
 // Operand sizes in elements (all fields).
 __host__ __device__ inline size_t a_elems(int rows, int k, int fields) {
@@ -388,15 +391,15 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
     const float row_scale = pow2f((row_ok ? out.eA[(size_t)f * out.sa_e + row] : 0) - 14);
     float e = 0.f;
 #pragma unroll
-    for (int part = 0; part < 2; ++part) {
+    for (int part = 0; part < kN / 32; ++part) {
       uint32_t v[kLevels][16];
 #pragma unroll
       for (int L = 0; L < kLevels; ++L)
-        ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * kN + h * 32 + part * 16), v[L]);
+        ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * kN + h * (kN / 2) + part * 16), v[L]);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        const int col = nt * kN + h * 32 + part * 16 + j;
+        const int col = nt * kN + h * (kN / 2) + part * 16 + j;
         const bool ok = row_ok && col < N;
         // join the exact level sums: a0 + 2^-8 a1 + 2^-16 a2 + 2^-24 a3
         float s, r;
