@@ -350,6 +350,25 @@ const char* texo_gp_stage_name(uint32_t stage);
  * grid barriers; out[9] = number of grid barriers. */
 int32_t texo_gp_device_profile(texo_gp_handle h, double out[10]);
 
+/* Per-iteration controller trace of the host engine (diagnostic, for parity
+ * with the oracle's controller): one record per completed eplace iteration of
+ * `optimize_density_once` (eplace.rs:439-582) since create/reset, the first
+ * 4096 kept. The device engine keeps its controller on the GPU and records
+ * none (count 0). No counterpart in the reference (it only traces through
+ * its `tracing` spans). */
+typedef struct texo_gp_iteration {
+  uint32_t iteration;            /* 1-based */
+  uint32_t trials;               /* line-search trials of this Nesterov step */
+  double gamma;                  /* WA gamma of the step (tile units) */
+  double objective;              /* accepted combined objective */
+  double lipschitz;              /* Lipschitz estimate after the step */
+  double momentum;               /* Nesterov momentum parameter after the step */
+  double lambda[TEXO_GP_MAX_FIELDS];        /* density multipliers the step used */
+  double energy_scale[TEXO_GP_MAX_FIELDS];  /* E0 = max(initial energy, 1) per field */
+  double overflow[TEXO_GP_MAX_FIELDS];      /* normalized overflow at the accepted point */
+} texo_gp_iteration;
+int32_t texo_gp_trace(texo_gp_handle h, texo_gp_iteration* out, uint32_t capacity, uint32_t* count);
+
 /* HPWL = sum over hypernets of the x and y pin spans at `coordinates`
  * (the continuous form of `exact_objective`, analytical_placement.rs:473-511),
  * FP64 reduction. */

@@ -218,6 +218,7 @@ def lib():
             "orc_scatter_fixed": (C.c_int32, [C.c_void_p, c_f64p, c_i64p, c_i64p, c_i64p, c_u64p]),
             "orc_place": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint32, c_u32p, c_f64p, C.POINTER(RunStats)]),
             "orc_hpwl": (C.c_int32, [C.c_void_p, c_f64p, c_f64p]),
+            "orc_trace": (C.c_uint32, [C.c_void_p, C.POINTER(abi.Iteration), C.c_uint32]),
             "orc_wirelength_preconditioner": (None, [C.c_void_p, c_f64p]),
             "orc_cell_incidence_weights": (None, [C.c_void_p, c_f64p]),
             "orc_nesterov_step": (C.c_int32, [C.POINTER(NState), c_f64p, C.c_uint64, c_f64p, C.c_uint64,
@@ -400,6 +401,13 @@ class Oracle:
         out = C.c_double()
         lib().orc_hpwl(self.h, P(coords), C.byref(out))
         return out.value
+
+    def trace(self):
+        """Controller records of the last place() (texo_gp_iteration each)."""
+        n = lib().orc_trace(self.h, None, 0)
+        buf = (abi.Iteration * max(1, n))()
+        lib().orc_trace(self.h, buf, n)
+        return [buf[i] for i in range(n)]
 
     def wirelength_preconditioner(self):
         out = np.zeros(self.units)

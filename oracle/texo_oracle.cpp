@@ -1125,6 +1125,8 @@ struct Eplace {
   Oracle& o;
   int threads;
   double gamma_base_tiles;
+  static constexpr size_t kTraceMax = 4096;
+  std::vector<texo_gp_iteration>* trace = nullptr;   // per-iteration controller records (optional)
   explicit Eplace(Oracle& oo, int th) : o(oo), threads(th) {
     const double bin_width = o.identity_map ? 1.0 : 1.0 / o.sx;
     gamma_base_tiles = o.params.gamma_base * bin_width;
@@ -1382,6 +1384,21 @@ struct Eplace {
       stats.gamma = gamma;
       current = std::move(payloads[(size_t)so.payload]);
       if ((s = validate_fields(current, scales))) return s;
+      if (trace && trace->size() < kTraceMax) {
+        texo_gp_iteration rec{};
+        rec.iteration = completed;
+        rec.trials = (uint32_t)so.trials;
+        rec.gamma = gamma;
+        rec.objective = so.objective;
+        rec.lipschitz = st.has_L ? st.L : 0.0;
+        rec.momentum = st.a;
+        for (uint32_t f = 0; f < o.K && f < TEXO_GP_MAX_FIELDS; ++f) {
+          rec.lambda[f] = lambda[f];
+          rec.energy_scale[f] = scales[f];
+          rec.overflow[f] = current.fields[f].overflow;
+        }
+        trace->push_back(rec);
+      }
       targets(st.x, rt);
       double mx, tot;
       excess(current, mx, tot);
@@ -1427,6 +1444,7 @@ struct Eplace {
 // ---------------------------------------------------------------------------
 struct orc_handle_s {
   Oracle o;
+  std::vector<texo_gp_iteration> trace;   // of the last orc_place
 };
 
 extern "C" {
@@ -1837,12 +1855,20 @@ int32_t orc_place(orc_handle h, int32_t threads, uint32_t max_iterations, uint32
     return TEXO_GP_OK;
   }
   Eplace ep(o, threads);
+  h->trace.clear();
+  ep.trace = &h->trace;
   std::vector<uint32_t> best;
   std::vector<double> fc;
   int32_t s = ep.run(max_iterations, best, fc, *stats);
   if (targets && !best.empty()) std::memcpy(targets, best.data(), best.size() * 4);
   if (coordinates && !fc.empty()) std::memcpy(coordinates, fc.data(), fc.size() * 8);
   return s;
+}
+
+uint32_t orc_trace(orc_handle h, texo_gp_iteration* out, uint32_t capacity) {
+  const uint32_t n = (uint32_t)std::min<size_t>(h->trace.size(), capacity);
+  if (n) std::memcpy(out, h->trace.data(), n * sizeof(texo_gp_iteration));
+  return (uint32_t)h->trace.size();
 }
 
 int32_t orc_hpwl(orc_handle h, const double* coordinates, double* out) {

@@ -98,6 +98,9 @@ typedef struct orc_run_stats {
 } orc_run_stats;
 int32_t orc_place(orc_handle h, int32_t threads, uint32_t max_iterations, uint32_t* targets,
                   double* coordinates, orc_run_stats* stats);
+/* The controller records of the last orc_place (one per completed iteration,
+ * the first 4096): copies up to `capacity`, returns how many there are. */
+uint32_t orc_trace(orc_handle h, texo_gp_iteration* out, uint32_t capacity);
 /* The same loop restarted from the handle's initial state, running exactly
  * `iterations` outer iterations (for timing a bounded sample). */
 int32_t orc_hpwl(orc_handle h, const double* coordinates, double* hpwl);

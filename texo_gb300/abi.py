@@ -103,6 +103,13 @@ class Stats(C.Structure):
     ]
 
 
+class Iteration(C.Structure):
+    """texo_gp_iteration: one eplace iteration as the controller saw it."""
+    _fields_ = [("iteration", C.c_uint32), ("trials", C.c_uint32), ("gamma", C.c_double),
+                ("objective", C.c_double), ("lipschitz", C.c_double), ("momentum", C.c_double),
+                ("lambda_", C.c_double * 4), ("energy_scale", C.c_double * 4), ("overflow", C.c_double * 4)]
+
+
 class FieldEval(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
@@ -189,6 +196,7 @@ SIGNATURES = {
     "texo_gp_dct_form": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "texo_gp_reset": (C.c_int32, [_P]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
+    "texo_gp_trace": (C.c_int32, [_P, C.POINTER(Iteration), C.c_uint32, c_u32p]),
     "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),
     "texo_gp_stage_name": (C.c_char_p, [C.c_uint32]),
     "texo_gp_device_profile": (C.c_int32, [_P, c_f64p]),

@@ -715,6 +715,8 @@ struct Controller {
   double last_objective = 0.0;
   double elapsed_ms = 0.0;
   unsigned long long launches = 0;
+  static constexpr size_t kTraceMax = 4096;
+  std::vector<texo_gp_iteration> trace;   // host engine: one record per completed iteration
 
   explicit Controller(Instance& i) : I(i), hr(i.h_run->run) { std::memset(&hr, 0, sizeof(hr)); }
   ~Controller() {
@@ -1236,9 +1238,25 @@ struct Controller {
       gamma = gam;
       EvalRec payload;
       bool stationary = false;
+      const uint64_t trials_before = trials;
       TRY(nesterov_step(gam, payload, stationary));
       TRY(validate_fields(payload));
       current = payload;
+      if (trace.size() < kTraceMax) {
+        texo_gp_iteration rec{};
+        rec.iteration = completed;
+        rec.trials = (uint32_t)(trials - trials_before);
+        rec.gamma = gam;
+        rec.objective = current.value;
+        rec.lipschitz = has_L ? L : 0.0;
+        rec.momentum = a;
+        for (uint32_t f = 0; f < K && f < TEXO_GP_MAX_FIELDS; ++f) {
+          rec.lambda[f] = lambda[f];
+          rec.energy_scale[f] = e0[f];
+          rec.overflow[f] = current.overflow[f];
+        }
+        trace.push_back(rec);
+      }
       double mx, tot;
       excess(current, mx, tot);
       if (mx < best_max || (mx == best_max && tot < best_tot)) {
@@ -1762,6 +1780,16 @@ int32_t texo_gp_reset(texo_gp_handle h) {
   TRY(upload_coords(I, I.bufX, I.m.init.data(), (size_t)I.d.nobj));
   CU(cudaMemsetAsync(I.prev_targets, 0, 2 * (size_t)I.m.U * 4, I.stream));
   CU(cudaStreamSynchronize(I.stream));
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_trace(texo_gp_handle h, texo_gp_iteration* out, uint32_t capacity, uint32_t* count) {
+  if (!h || !count || (capacity && !out)) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  const auto& tr = h->ctl->trace;
+  const uint32_t n = (uint32_t)std::min<size_t>(tr.size(), capacity);
+  if (n) std::memcpy(out, tr.data(), n * sizeof(texo_gp_iteration));
+  *count = (uint32_t)tr.size();
   return TEXO_GP_OK;
 }
 

@@ -361,6 +361,14 @@ class Placer:
 
     DCT_FORMS = ("gemm16", "gemm64", "tensor_core", "fft")
 
+    def trace(self):
+        """Host-engine controller records since create/reset (texo_gp_iteration each)."""
+        n = C.c_uint32()
+        abi.check(self.lib.texo_gp_trace(self.h, None, 0, C.byref(n)), "texo_gp_trace")
+        buf = (abi.Iteration * max(1, n.value))()
+        abi.check(self.lib.texo_gp_trace(self.h, buf, n.value, C.byref(n)), "texo_gp_trace")
+        return [buf[i] for i in range(n.value)]
+
     def dct_form(self):
         """The DCT form this instance runs: 0 GEMM (16-bin tiles), 1 GEMM
         (64-bin tiles), 2 tensor cores (integer slices, exact accumulation), 3 FFT."""
