@@ -555,6 +555,34 @@ def seed_report(workload="lfe5u-85-42k", reps=5):
             "speedup_wall_vs_cpu": cpu_ms / min(wall_ms)}
 
 
+def scatter_report(workloads=("lfe5u-85-42k", "stress-1m"), reps=20):
+    """The host engine's two density-scatter forms (direct: nine global int64
+    atomics per object; tiled: counting sort by 32 x 32-bin tile, then a
+    shared-memory window per run of the sorted order) on each workload, timed
+    with CUDA events at the positions one placement ends at (the scatter
+    launch group: init excluded; for the tiled form its count, scan, place
+    and scatter kernels), with the grids checked equal between the forms."""
+    import numpy as np
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer
+    out = {}
+    for wl in workloads:
+        prob = make_problem(wl, 0)
+        res, grids = {}, []
+        for name, mode in (("direct", abi.SCATTER_DIRECT), ("tiled", abi.SCATTER_TILED)):
+            prm = make_params(wl, abi.ENGINE_HOST, abi.DCT_FP32)
+            prm.scatter_mode = mode
+            with Placer(prob, prm) as g:
+                _, c, s = g.run(allow_nonconverged=True)
+                grids.append(g.scatter(c))
+                st = g.stage_times(reps=reps)
+                res[name] = {"scatter_us": round(st["scatter"] * 1000, 2), "iterations": s["iterations"]}
+        res["grids_identical"] = bool(np.array_equal(grids[0][0], grids[1][0]) and
+                                      np.array_equal(grids[0][1], grids[1][1]))
+        out[wl] = res
+    return out
+
+
 def rudy_report(reps=5):
     """Continuous RUDY demand (`continuous_routing_demand`, eplace.rs:856-937)
     of the 42k workload's net boxes at its placed positions (one device-engine
@@ -845,6 +873,7 @@ def main():
     ap.add_argument("--seed-only", action="store_true", help="print only the quadratic-seed solve report")
     ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
     ap.add_argument("--rudy-only", action="store_true", help="print only the RUDY demand report")
+    ap.add_argument("--scatter-only", action="store_true", help="print only the density-scatter forms report")
     ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
     ap.add_argument("--clustering-only", action="store_true", help="print only the register-clustering report")
     args = ap.parse_args()
@@ -875,6 +904,10 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "tensor-core / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
+        return
+    if args.scatter_only:
+        if rank == 0:
+            print(json.dumps({"metric": "density scatter forms", "scatter": scatter_report()}), flush=True)
         return
     if args.rudy_only:
         if rank == 0:

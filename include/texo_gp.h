@@ -167,6 +167,16 @@ typedef enum texo_gp_dct_mode {
   TEXO_GP_DCT_FP32_GEMM = 2  /* FP32 compensated GEMM against the cosine matrices on every grid */
 } texo_gp_dct_mode;
 
+/* Density scatter forms of the host engine (the device engine always runs the
+ * direct form). Both give the same int64 fixed-point grids bit for bit. */
+typedef enum texo_gp_scatter_mode {
+  TEXO_GP_SCATTER_AUTO = 0,     /* the direct form; with autotune = 1 the faster of the two, timed at
+                                   creation */
+  TEXO_GP_SCATTER_DIRECT = 1,   /* nine global int64 atomics per object */
+  TEXO_GP_SCATTER_TILED = 2     /* objects sorted by 32 x 32-bin tile, taps accumulated in a shared-
+                                   memory window per run, one global atomic per touched bin */
+} texo_gp_scatter_mode;
+
 /* Controller forms. */
 typedef enum texo_gp_engine {
   TEXO_GP_ENGINE_HOST = 0,      /* host-driven line search, one sync per evaluation */
@@ -194,8 +204,11 @@ typedef struct texo_gp_params {
   int32_t autotune;              /* 1: time the DCT forms on this instance at creation and keep the
                                     fastest (FP32 GEMM with 16x16 or 64x64 tiles, FP32 FFT on
                                     power-of-two grids; with dct_mode TENSOR also the tensor-core
-                                    form, which may give way to the more accurate FP32 forms) */
-  uint32_t reserved[7];
+                                    form, which may give way to the more accurate FP32 forms), and
+                                    with the host engine and scatter_mode AUTO also the two scatter
+                                    forms, at spread coordinates */
+  int32_t scatter_mode;          /* texo_gp_scatter_mode: how the host engine deposits the density */
+  uint32_t reserved[6];
 } texo_gp_params;
 
 #define TEXO_GP_MAX_FIELDS 4

@@ -38,6 +38,7 @@ KIND_LOGIC, KIND_LUT, KIND_REGISTER, KIND_MEMORY, KIND_CLOCK, KIND_IO, KIND_CONS
 DCT_FP32, DCT_TENSOR, DCT_FP32_GEMM = 0, 1, 2
 DCT_BF16X3 = DCT_TENSOR   # earlier name of the tensor-core mode
 ENGINE_HOST, ENGINE_DEVICE = 0, 1
+SCATTER_AUTO, SCATTER_DIRECT, SCATTER_TILED = 0, 1, 2
 MAX_FIELDS = 4
 
 c_u32p = C.POINTER(C.c_uint32)
@@ -87,7 +88,7 @@ class Params(C.Structure):
         ("bins_x", C.c_uint32), ("bins_y", C.c_uint32), ("target_density", C.c_double),
         ("best_effort", C.c_int32), ("dct_mode", C.c_int32), ("engine", C.c_int32),
         ("device", C.c_int32), ("objective_margin_ulps", C.c_double),
-        ("autotune", C.c_int32), ("reserved", C.c_uint32 * 7),
+        ("autotune", C.c_int32), ("scatter_mode", C.c_int32), ("reserved", C.c_uint32 * 6),
     ]
 
 

@@ -102,6 +102,12 @@ struct Dev {
   const uint16_t *CxB_t, *CyA_t, *CyTA_t, *CxTB_t;
   const int *eCx, *eCy;          // basis row exponents: [n] rows of C, then [n] rows of C^T
   const float* inv_eig_lo;       // [B] low part of 1 / lambda
+  // Tiled scatter (scatter_tiles.cuh, host engine): objects counting-sorted by
+  // (grid, 32 x 32-bin tile of their centre bin), then deposited through a
+  // shared-memory window per run of the sorted order
+  int scatter_tiles;         // 1: the density scatter runs in the tiled form
+  int *bin_key, *bin_rank, *bin_order;   // [Mm + F]
+  int *bin_cnt, *bin_off;    // [2 K tiles], [2 K tiles + 1]
   // gradients
   unsigned long long* wa_fix;  // [2U] WA gradient, 2^-32 fixed point
   float2* graw;              // [K][nobj] raw per-field density gradient

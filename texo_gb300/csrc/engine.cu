@@ -21,6 +21,7 @@
 
 #include "engine.h"
 #include "dct_tc.cuh"
+#include "scatter_tiles.cuh"
 
 namespace tgp {
 
@@ -523,6 +524,16 @@ void Instance::plan(bool fill, void* slicer_ptr) {
   S.zeroed(&r.q.isum, (size_t)kISlots * kMaxPartials);
   S.zeroed(&r.q.mx, (size_t)kMSlots * kMaxPartials);
   S.zeroed(&r.iscal, kIScalars);
+  if (h.params.engine == TEXO_GP_ENGINE_HOST) {   // the tiled scatter's counting sort
+    const size_t items = (size_t)h.Mm + h.F;
+    const size_t nk = 2 * K * (size_t)((h.Wb + tiles::kTile - 1) / tiles::kTile) *
+                      ((h.Hb + tiles::kTile - 1) / tiles::kTile);
+    S.zeroed(&D.bin_key, items);
+    S.zeroed(&D.bin_rank, items);
+    S.zeroed(&D.bin_order, items);
+    S.zeroed(&D.bin_cnt, nk);
+    S.zeroed(&D.bin_off, nk + 1);
+  }
   if (h.params.dct_mode == TEXO_GP_DCT_TENSOR) {   // tensor-core operands (zero padding)
     S.zeroed(&D.opA, tc::a_elems((int)h.Hb, (int)h.Wb, (int)K));
     S.zeroed(&D.opB, tc::b_elems((int)h.Wb, (int)h.Hb, (int)K));
@@ -584,6 +595,8 @@ int32_t Instance::upload() {
     D.eCx = bx.e;
     D.eCy = by.e;
     D.tc = h.params.dct_mode == TEXO_GP_DCT_TENSOR ? 1 : 0;
+    // the tiled scatter (host engine) when asked for; AUTO leaves it to the autotuner
+    D.scatter_tiles = h.params.engine == TEXO_GP_ENGINE_HOST && h.params.scatter_mode == TEXO_GP_SCATTER_TILED;
     // fixed rule unless autotuned: large tiles once the grid has >= 1024 32x32 blocks
     D.dct_large = (long long)((h.Wb + 31) / 32) * ((h.Hb + 31) / 32) >= 1024 ? 1 : 0;
     // the FFT form for power-of-two grids (FP32 mode)
@@ -1345,6 +1358,8 @@ int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_g
   if (prm->dct_mode != TEXO_GP_DCT_FP32 && prm->dct_mode != TEXO_GP_DCT_TENSOR &&
       prm->dct_mode != TEXO_GP_DCT_FP32_GEMM)
     return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (prm->scatter_mode < TEXO_GP_SCATTER_AUTO || prm->scatter_mode > TEXO_GP_SCATTER_TILED)
+    return TEXO_GP_ERR_INVALID_ARGUMENT;
   if (prm->dct_mode == TEXO_GP_DCT_TENSOR && prm->engine == TEXO_GP_ENGINE_DEVICE) {
     set_last_error("the tensor-core DCT runs with the host engine only");
     return TEXO_GP_ERR_UNSUPPORTED;
@@ -1428,6 +1443,61 @@ int32_t autotune_dct(Instance& I) {
   I.d.dct_large = pick.large;
   I.d.tc = pick.tc;
   I.d.fft = pick.fft;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = pick;
+  return TEXO_GP_OK;
+}
+
+// The scatter half of the autotuner (host engine, scatter_mode AUTO): times
+// the direct and the tiled scatter (init + scatter, and for the tiled form its
+// counting sort) at spread coordinates (every object uniform in its bounds,
+// as a placement near convergence is, from a fixed hash) and keeps the faster,
+// cached per (device, grid, fields, objects). The grids both forms produce
+// are identical, so the choice changes the time only.
+int32_t autotune_scatter(Instance& I) {
+  const texo_gp_params& prm = I.m.params;
+  if (prm.engine != TEXO_GP_ENGINE_HOST || prm.scatter_mode != TEXO_GP_SCATTER_AUTO || !I.m.has_density)
+    return TEXO_GP_OK;
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint32_t, uint32_t, uint32_t, uint64_t>, int> cache;
+  const auto key = std::make_tuple(I.device, I.m.Wb, I.m.Hb, I.m.K, (uint64_t)I.m.Mm + I.m.F);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      I.d.scatter_tiles = it->second;
+      return TEXO_GP_OK;
+    }
+  }
+  launch_spread_positions(I.d, I.bufC, I.nvb, I.stream);
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  float best = 1e30f;
+  int pick = 0;
+  for (int form = 0; form < 2; ++form) {
+    Dev D = I.d;
+    D.scatter_tiles = form;
+    float t = 1e30f;
+    for (int rep = 0; rep < 6; ++rep) {
+      CU(cudaEventRecord(a, I.stream));
+      launch_init(D, true, false, I.nvb, I.stream);
+      launch_scatter(D, I.r, I.bufC, I.nvb, I.stream);
+      CU(cudaEventRecord(b, I.stream));
+      CU(cudaEventSynchronize(b));
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0) t = std::min(t, ms);   // the first run is a warm-up
+    }
+    if (t < best) {
+      best = t;
+      pick = form;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CU(cudaStreamSynchronize(I.stream));
+  I.d.scatter_tiles = pick;
   std::lock_guard<std::mutex> lk(mu);
   cache[key] = pick;
   return TEXO_GP_OK;
@@ -1567,6 +1637,7 @@ int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo
   TRY(tgp::handle_build(p, prm, &h, nullptr));
   int32_t s = tgp::handle_upload(h);
   if (!s && h->inst->m.params.autotune) s = autotune_dct(*h->inst);
+  if (!s && h->inst->m.params.autotune) s = autotune_scatter(*h->inst);
   if (s) {
     delete h;
     return s;

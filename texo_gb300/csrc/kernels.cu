@@ -2,6 +2,7 @@
 #include "dct_fft.cuh"
 #include "dct_tc.cuh"
 #include "kernels.cuh"
+#include "scatter_tiles.cuh"
 
 namespace tgp {
 
@@ -54,6 +55,30 @@ __global__ void __launch_bounds__(kThreads) k_init(Dev d, bool grids, bool wa) {
 __global__ void __launch_bounds__(kThreads) k_scatter(Dev d, Partials p, const float2* pos) {
   __shared__ Shared sh;
   stage_scatter(d, pos, p, blockIdx.x, gridDim.x, sh);
+}
+// The tiled scatter's four passes (scatter_tiles.cuh).
+__global__ void __launch_bounds__(kThreads) k_tile_count(Dev d, const float2* pos) {
+  tiles::count(d, pos, blockIdx.x, gridDim.x);
+}
+__global__ void __launch_bounds__(kThreads) k_tile_scan(Dev d) { tiles::scan(d); }
+__global__ void __launch_bounds__(kThreads) k_tile_place(Dev d) { tiles::place(d, blockIdx.x, gridDim.x); }
+__global__ void __launch_bounds__(kThreads) k_tile_scatter(Dev d, Partials p, const float2* pos) {
+  __shared__ tiles::Smem sm;
+  __shared__ Shared sh;
+  tiles::scatter(d, pos, p, blockIdx.x, gridDim.x, sm, sh);
+}
+// Every object uniform in its bounds from a fixed hash (the autotuner's
+// stand-in for a spread placement).
+__global__ void __launch_bounds__(kThreads) k_spread_positions(Dev d, float2* out) {
+  for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < d.nobj; o += gridDim.x * blockDim.x) {
+    unsigned h = (unsigned)o * 2654435761u + 12345u;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    const float fx = (float)(h & 0xffffu) * (1.0f / 65536.0f), fy = (float)(h >> 16) * (1.0f / 65536.0f);
+    const float2 lo = d.lo[o], hi = d.hi[o];
+    out[o] = make_float2(fmaf(hi.x - lo.x, fx, lo.x), fmaf(hi.y - lo.y, fy, lo.y));
+  }
 }
 __global__ void __launch_bounds__(kThreads) k_wa(Dev d, Partials p, const float2* pos, double gamma) {
   __shared__ Shared sh;
@@ -222,8 +247,20 @@ void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s) {
   k_init<<<nvb, kThreads, 0, s>>>(d, grids, wa);
 }
 void launch_scatter(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s) {
+  if (d.scatter_tiles && d.Mm + d.F > 0) {
+    t_launches += 4;
+    k_tile_count<<<nvb, kThreads, 0, s>>>(d, pos);
+    k_tile_scan<<<1, kThreads, 0, s>>>(d);
+    k_tile_place<<<nvb, kThreads, 0, s>>>(d);
+    k_tile_scatter<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
+    return;
+  }
   COUNT;
   k_scatter<<<nvb, kThreads, 0, s>>>(d, r.p, pos);
+}
+void launch_spread_positions(const Dev& d, float2* out, int nvb, cudaStream_t s) {
+  COUNT;
+  k_spread_positions<<<nvb, kThreads, 0, s>>>(d, out);
 }
 void launch_wa(const Dev& d, const Reduce& r, const float2* pos, double gamma, int nvb, cudaStream_t s) {
   COUNT;

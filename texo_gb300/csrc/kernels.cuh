@@ -64,6 +64,7 @@ unsigned long long launches_issued();
 void note_launch();
 void launch_init(const Dev& d, bool grids, bool wa, int nvb, cudaStream_t s);
 void launch_scatter(const Dev& d, const Reduce& r, const float2* pos, int nvb, cudaStream_t s);
+void launch_spread_positions(const Dev& d, float2* out, int nvb, cudaStream_t s);
 void launch_wa(const Dev& d, const Reduce& r, const float2* pos, double gamma, int nvb, cudaStream_t s);
 void launch_prep(const Dev& d, const Reduce& r, int nvb, cudaStream_t s);
 void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s,
