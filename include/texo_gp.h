@@ -429,6 +429,12 @@ int32_t texo_gp_batch_retire(texo_gp_batch b, uint64_t* job_id, uint32_t* out_ta
                              uint64_t targets_capacity, texo_gp_stats* stats);
 int32_t texo_gp_batch_counts(texo_gp_batch b, uint32_t* resident, uint32_t* finished,
                              uint64_t* bytes_in_use);
+/* An advance whose resident set (jobs, order and iteration chunk) repeats the
+ * previous advance's is captured once as a CUDA graph (state copies in, the
+ * persistent launches, state copies out) and replayed while the set stays;
+ * counts of captures and replays since create (diagnostic; no counterpart in
+ * the reference). */
+int32_t texo_gp_batch_graphs(texo_gp_batch b, uint64_t* captures, uint64_t* replays);
 
 /* ---- Serving loop (continuous batching) ----------------------------------
  * Placement requests are submitted at any time from any thread. Admission

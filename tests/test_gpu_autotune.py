@@ -86,3 +86,28 @@ def test_tile_families_share_a_batch_and_match_alone():
     for i, (t, _, s) in enumerate(alone):
         assert np.array_equal(got[i][1], t), "job %d differs in the mix" % i
         assert got[i][2]["hpwl"] == s["hpwl"]
+
+
+@pytest.mark.parametrize("workload", ["rich", "lfe5u-85-42k"])
+def test_autotuned_wa_lanes_keep_the_bound(workload):
+    # the autotuner also picks the WA lanes per net of each degree class (and
+    # the scatter form): whichever it picks, WA and the density stay within
+    # 1e-5 of FP64 and repeat bit for bit
+    from rich_problems import rich_problem
+    if workload == "rich":
+        prob, kw = rich_problem(0), {}
+    else:
+        prob = P.synthetic(210, 42000, 365, 50000, 12.0, 0)
+        kw = dict(bins_x=256, bins_y=256, target_density=0.9, gamma_base=4.0)
+    prm = default_params(autotune=1, engine=abi.ENGINE_HOST, **kw)
+    o = ffi.Oracle(prob, prm)
+    c, lo, hi = o.initial()
+    c = (lo + (hi - lo) * np.random.default_rng(5).random(c.size)).astype(np.float32).astype(np.float64)
+    r = o.evaluate(c, 1.5)
+    with Placer(prob, prm) as g:
+        d = g.evaluate(c, 1.5)
+        d2 = g.evaluate(c, 1.5)
+    assert abs(d["wirelength"] - r["wirelength"]) <= 1e-5 * abs(r["wirelength"])
+    for k in ("wa_gradient", "density", "potential", "field_gradient"):
+        assert normwise(d[k], r[k]) <= 1e-5, k
+        assert np.array_equal(d[k], d2[k])

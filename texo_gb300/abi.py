@@ -209,6 +209,7 @@ SIGNATURES = {
     "texo_gp_batch_advance": (C.c_int32, [_P, C.c_uint32]),
     "texo_gp_batch_retire": (C.c_int32, [_P, c_u64p, c_u32p, C.c_uint64, C.POINTER(Stats)]),
     "texo_gp_batch_counts": (C.c_int32, [_P, c_u32p, c_u32p, c_u64p]),
+    "texo_gp_batch_graphs": (C.c_int32, [_P, c_u64p, c_u64p]),
     "texo_gp_server_create": (C.c_int32, [C.POINTER(Params), C.POINTER(ServerOptions), C.POINTER(_P)]),
     "texo_gp_server_destroy": (C.c_int32, [_P]),
     "texo_gp_server_submit": (C.c_int32, [_P, C.POINTER(ProblemC), C.POINTER(Params), C.c_uint64]),

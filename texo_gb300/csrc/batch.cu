@@ -6,7 +6,9 @@
 // count) and runs all of them in one cooperative launch of k_batch; jobs run
 // independently inside it, each over its own physical blocks. A job's results
 // do not depend on how many physical blocks it got, so they are bit-identical
-// to the same job placed alone.
+// to the same job placed alone. When the resident set repeats from one advance
+// to the next, the whole advance (state copies in, launches, state copies
+// out) is captured once as a CUDA graph and replayed.
 #include <algorithm>
 #include <cstring>
 #include <deque>
@@ -43,9 +45,24 @@ struct texo_gp_batch_s {
   int pblocks = 0;
   size_t rr = 0;
   std::mutex mu;
+  // The advance of an unchanged resident set as one CUDA graph: the state
+  // copies in, the batch launches, the state copies out. Recaptured when the
+  // set, its order or the iteration chunk changes.
+  int4* d_map1 = nullptr;                 // the second launch family's block map
+  cudaGraphExec_t exec = nullptr;
+  std::vector<texo_gp_handle> g_jobs;     // with their state mirrors and device copies: a
+  std::vector<RunBlock*> g_hosts, g_devs; // handle at a reused address is still a new key
+  uint32_t g_iters = 0;
+  int g_launches = 0;
+  uint64_t captures = 0, replays = 0;
+  std::vector<texo_gp_handle> p_jobs;     // the set of the previous advance (captured once it repeats)
+  std::vector<RunBlock*> p_hosts;
+  uint32_t p_iters = 0;
 
   ~texo_gp_batch_s() {
     if (stream) cudaStreamSynchronize(stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (d_map1) cudaFree(d_map1);
     for (auto& j : resident) texo_gp_destroy(j.h);
     for (auto& j : done) texo_gp_destroy(j.h);
     if (d_descs) cudaFree(d_descs);
@@ -85,6 +102,7 @@ int32_t texo_gp_batch_create(const texo_gp_params* params, uint64_t hbm_budget_b
   BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   BCU(cudaMalloc(&b->d_descs, sizeof(InstDesc) * max_slots));
   BCU(cudaMalloc(&b->d_map, sizeof(int4) * b->pblocks));
+  BCU(cudaMalloc(&b->d_map1, sizeof(int4) * b->pblocks));
   b->h_descs.resize(max_slots);
   b->h_map.reserve(b->pblocks);
   *out = b.release();
@@ -158,45 +176,124 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
   for (size_t i = 0; i < n; ++i) pick[i] = (b->rr + i) % nres;
   b->rr = (b->rr + n) % std::max<size_t>(nres, 1);
   std::vector<char> lg(n, 0);
-  for (size_t i = 0; i < n; ++i) {
-    bool large = false;
-    const int32_t st = batch_stage_in(b->resident[pick[i]].h, iterations, b->stream, &b->h_descs[i], &large);
-    if (st) return st;
-    lg[i] = large ? 1 : 0;
-  }
-  BCU(cudaMemcpyAsync(b->d_descs, b->h_descs.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, b->stream));
-  // One launch per DCT tile family (a job runs the same kernel instantiation
-  // as it does alone); physical blocks proportional to virtual blocks, at
-  // least one each.
-  int32_t s = TEXO_GP_OK;
-  for (int fam = 0; fam < 2; ++fam) {
+  // Block maps of the (at most two) launches: one per DCT tile family (a job
+  // runs the same kernel instantiation as it does alone); physical blocks
+  // proportional to virtual blocks, at least one each.
+  auto block_map = [&](int fam, std::vector<int4>& map) {
     std::vector<size_t> jobs;
     for (size_t i = 0; i < n; ++i)
       if (lg[i] == fam) jobs.push_back(i);
-    if (jobs.empty()) continue;
+    map.clear();
+    if (jobs.empty()) return;
     const int nj = (int)jobs.size();
     long long vsum = 0;
     for (size_t i : jobs) vsum += b->resident[pick[i]].V;
-    b->h_map.clear();
     int used = nj;
     for (size_t i : jobs) {
       const int V = b->resident[pick[i]].V;
       const int want = std::max(1, (int)((long long)(P - nj) * V / std::max(vsum, 1ll)) + 1);
       const int add = std::max(0, std::min(std::min(want, V) - 1, P - used));
       used += add;
-      for (int k = 0; k < 1 + add; ++k) b->h_map.push_back(make_int4((int)i, k, 1 + add, 0));
+      for (int k = 0; k < 1 + add; ++k) map.push_back(make_int4((int)i, k, 1 + add, 0));
     }
-    BCU(cudaMemcpyAsync(b->d_map, b->h_map.data(), sizeof(int4) * b->h_map.size(), cudaMemcpyHostToDevice,
-                        b->stream));
-    s = launch_batch(b->d_descs, b->d_map, (int)b->h_map.size(), fam == 1, b->stream);
-    if (s) {
-      set_last_error(std::string("batch launch: ") + cudaGetErrorString(cudaGetLastError()));
-      return s;
+  };
+  int32_t s = TEXO_GP_OK;
+  bool graphed = false;
+  if (n == nres) {
+    // Every resident job in this launch: replay (or capture) the advance as a graph.
+    std::vector<texo_gp_handle> hs(n);
+    std::vector<RunBlock*> hosts(n), devs(n);
+    for (size_t i = 0; i < n; ++i) {
+      bool large = false;
+      hs[i] = b->resident[pick[i]].h;
+      batch_stage_host(hs[i], iterations, &b->h_descs[i], &large, &hosts[i], &devs[i]);
+      lg[i] = large ? 1 : 0;
+    }
+    const bool same = b->exec && b->g_jobs == hs && b->g_hosts == hosts && b->g_devs == devs &&
+                      b->g_iters == iterations;
+    // capture a set only once it repeats (a serving loop that changes the
+    // set at every launch boundary would pay a capture per launch)
+    const bool repeat = b->p_jobs == hs && b->p_hosts == hosts && b->p_iters == iterations;
+    if (!same && !repeat) {
+      b->p_jobs = hs;
+      b->p_hosts = hosts;
+      b->p_iters = iterations;
+      if (b->exec) cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    } else if (!same) {
+      if (b->exec) cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+      b->g_jobs.clear();
+      std::vector<int4> m0, m1;
+      block_map(0, m0);
+      block_map(1, m1);
+      BCU(cudaMemcpyAsync(b->d_descs, b->h_descs.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, b->stream));
+      if (!m0.empty())
+        BCU(cudaMemcpyAsync(b->d_map, m0.data(), sizeof(int4) * m0.size(), cudaMemcpyHostToDevice, b->stream));
+      if (!m1.empty())
+        BCU(cudaMemcpyAsync(b->d_map1, m1.data(), sizeof(int4) * m1.size(), cudaMemcpyHostToDevice, b->stream));
+      BCU(cudaStreamSynchronize(b->stream));
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        bool ok = true;
+        for (size_t i = 0; i < n && ok; ++i)
+          ok = cudaMemcpyAsync(devs[i], hosts[i], sizeof(RunBlock), cudaMemcpyHostToDevice, b->stream) == cudaSuccess;
+        int launches = 0;
+        if (ok && !m0.empty()) {
+          ok = launch_batch(b->d_descs, b->d_map, (int)m0.size(), false, b->stream) == TEXO_GP_OK;
+          ++launches;
+        }
+        if (ok && !m1.empty()) {
+          ok = launch_batch(b->d_descs, b->d_map1, (int)m1.size(), true, b->stream) == TEXO_GP_OK;
+          ++launches;
+        }
+        for (size_t i = 0; i < n && ok; ++i)
+          ok = cudaMemcpyAsync(hosts[i], devs[i], sizeof(RunBlock), cudaMemcpyDeviceToHost, b->stream) == cudaSuccess;
+        cudaGraph_t g = nullptr;
+        const bool ended = cudaStreamEndCapture(b->stream, &g) == cudaSuccess && g != nullptr;
+        if (ok && ended && cudaGraphInstantiate(&b->exec, g, 0) == cudaSuccess) {
+          b->g_jobs = hs;
+          b->g_hosts = hosts;
+          b->g_devs = devs;
+          b->g_iters = iterations;
+          b->g_launches = launches;
+          ++b->captures;
+        } else {
+          b->exec = nullptr;
+        }
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();   // a refused capture leaves no sticky error; the plain path runs instead
+    }
+    if (b->exec) {
+      BCU(cudaGraphLaunch(b->exec, b->stream));
+      ++b->replays;
+      for (int k = 0; k < b->g_launches; ++k) note_launch();
+      graphed = true;
     }
   }
-  for (size_t i = 0; i < n; ++i) {
-    s = batch_stage_out(b->resident[pick[i]].h, b->stream);
-    if (s) return s;
+  if (!graphed) {
+    for (size_t i = 0; i < n; ++i) {
+      bool large = false;
+      const int32_t st = batch_stage_in(b->resident[pick[i]].h, iterations, b->stream, &b->h_descs[i], &large);
+      if (st) return st;
+      lg[i] = large ? 1 : 0;
+    }
+    BCU(cudaMemcpyAsync(b->d_descs, b->h_descs.data(), sizeof(InstDesc) * n, cudaMemcpyHostToDevice, b->stream));
+    for (int fam = 0; fam < 2; ++fam) {
+      block_map(fam, b->h_map);
+      if (b->h_map.empty()) continue;
+      int4* dm = fam == 0 ? b->d_map : b->d_map1;
+      BCU(cudaMemcpyAsync(dm, b->h_map.data(), sizeof(int4) * b->h_map.size(), cudaMemcpyHostToDevice, b->stream));
+      s = launch_batch(b->d_descs, dm, (int)b->h_map.size(), fam == 1, b->stream);
+      if (s) {
+        set_last_error(std::string("batch launch: ") + cudaGetErrorString(cudaGetLastError()));
+        return s;
+      }
+    }
+    for (size_t i = 0; i < n; ++i) {
+      s = batch_stage_out(b->resident[pick[i]].h, b->stream);
+      if (s) return s;
+    }
   }
   BCU(cudaStreamSynchronize(b->stream));
   int32_t result = TEXO_GP_OK;
@@ -238,6 +335,14 @@ int32_t texo_gp_batch_retire(texo_gp_batch b, uint64_t* job_id, uint32_t* out_ta
   texo_gp_destroy(j.h);
   b->used -= j.bytes;
   return s;
+}
+
+int32_t texo_gp_batch_graphs(texo_gp_batch b, uint64_t* captures, uint64_t* replays) {
+  if (!b) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (captures) *captures = b->captures;
+  if (replays) *replays = b->replays;
+  return TEXO_GP_OK;
 }
 
 int32_t texo_gp_batch_counts(texo_gp_batch b, uint32_t* resident, uint32_t* finished, uint64_t* bytes_in_use) {

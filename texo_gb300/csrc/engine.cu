@@ -1334,6 +1334,26 @@ int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, Ins
   *large = I.d.dct_large != 0;
   return TEXO_GP_OK;
 }
+// The host half of batch_stage_in (no copy): the controller state in the
+// pinned mirror, and where the mirror and its device copy live.
+void batch_stage_host(texo_gp_handle_s* h, uint32_t budget, InstDesc* desc, bool* large, RunBlock** host,
+                      RunBlock** dev) {
+  Instance& I = *h->inst;
+  Controller& C = *h->ctl;
+  C.prepare_devrun();
+  C.hr.budget = budget;
+  std::memset(&I.h_run->bar, 0, sizeof(GridBarrier));
+  desc->d = I.d;
+  desc->r = I.r;
+  desc->B = C.buffers();
+  desc->run = &I.run_dev->run;
+  desc->bar = &I.run_dev->bar;
+  desc->V = I.nvb;
+  desc->pad = 0;
+  *large = I.d.dct_large != 0;
+  *host = I.h_run;
+  *dev = I.run_dev;
+}
 int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s) {
   Instance& I = *h->inst;
   CU(cudaMemcpyAsync(I.h_run, I.run_dev, sizeof(RunBlock), cudaMemcpyDeviceToHost, s));
@@ -1443,6 +1463,72 @@ int32_t autotune_dct(Instance& I) {
   I.d.dct_large = pick.large;
   I.d.tc = pick.tc;
   I.d.fft = pick.fft;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = pick;
+  return TEXO_GP_OK;
+}
+
+// The wirelength part of the autotuner: the lanes a net of each degree class
+// (2 | 3-4 | 5-8 | 9-16 | 17-32 | 33+ pins) gets in the WA stage. The fixed
+// table gives every lane at most four pins of a net (held in registers); the
+// candidates trade lanes for pins per lane: two (more lanes, shorter shuffle
+// trees) or eight (fewer lanes, pins beyond four read again). Each table is
+// timed on the instance (init + WA at its coordinates, both engines run the
+// same WA stage) and the fastest kept, cached per (device, class sizes,
+// virtual blocks). The per-net sums then run over a different lane count, so
+// WA values and gradients change by FP32 rounding (within the 1e-5 bounds)
+// with the table; a given table gives bit-identical results run to run.
+int32_t autotune_wa(Instance& I) {
+  static const int tables[3][6] = {{1, 1, 2, 4, 8, 32}, {1, 2, 4, 8, 32, 32}, {1, 1, 1, 2, 4, 32}};
+  HostModel& m = I.m;
+  if (m.n_classes < 6) return TEXO_GP_OK;
+  static std::mutex mu;
+  static std::map<std::vector<long long>, int> cache;
+  std::vector<long long> key = {I.device, I.nvb};
+  for (int c = 0; c <= m.n_classes; ++c) key.push_back(m.class_begin[c]);
+  auto apply = [&](int t) {
+    for (int c = 0; c < 6; ++c) {
+      m.class_group[c] = tables[t][c];
+      I.d.class_group[c] = tables[t][c];
+    }
+    wa_lane_split(m.class_begin, m.class_group, m.n_classes, (long long)I.nvb * kThreads, I.d.class_lane);
+  };
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      apply(it->second);
+      return TEXO_GP_OK;
+    }
+  }
+  cudaEvent_t a, b;
+  CU(cudaEventCreate(&a));
+  CU(cudaEventCreate(&b));
+  float best = 1e30f;
+  int pick = 0;
+  const double gamma = m.gamma_base_tiles();
+  for (int t = 0; t < 3; ++t) {
+    apply(t);
+    float tm = 1e30f;
+    for (int rep = 0; rep < 6; ++rep) {
+      CU(cudaEventRecord(a, I.stream));
+      launch_init(I.d, false, true, I.nvb, I.stream);
+      launch_wa(I.d, I.r, I.bufX, gamma, I.nvb, I.stream);
+      CU(cudaEventRecord(b, I.stream));
+      CU(cudaEventSynchronize(b));
+      float ms = 0.f;
+      CU(cudaEventElapsedTime(&ms, a, b));
+      if (rep > 0) tm = std::min(tm, ms);   // the first run is a warm-up
+    }
+    if (tm < best) {
+      best = tm;
+      pick = t;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CU(cudaStreamSynchronize(I.stream));
+  apply(pick);
   std::lock_guard<std::mutex> lk(mu);
   cache[key] = pick;
   return TEXO_GP_OK;
@@ -1638,6 +1724,7 @@ int32_t texo_gp_create(const texo_gp_problem* p, const texo_gp_params* prm, texo
   int32_t s = tgp::handle_upload(h);
   if (!s && h->inst->m.params.autotune) s = autotune_dct(*h->inst);
   if (!s && h->inst->m.params.autotune) s = autotune_scatter(*h->inst);
+  if (!s && h->inst->m.params.autotune) s = autotune_wa(*h->inst);
   if (s) {
     delete h;
     return s;

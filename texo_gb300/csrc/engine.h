@@ -108,6 +108,8 @@ namespace tgp {
 // mirrors the state once the stream has completed.
 int32_t batch_stage_in(texo_gp_handle_s* h, uint32_t budget, cudaStream_t s, InstDesc* desc, bool* large);
 int32_t batch_stage_out(texo_gp_handle_s* h, cudaStream_t s);
+void batch_stage_host(texo_gp_handle_s* h, uint32_t budget, InstDesc* desc, bool* large, RunBlock** host,
+                      RunBlock** dev);
 bool batch_timed_out(texo_gp_handle_s* h);     // the last launch's barrier wait ran out
 int32_t batch_absorb(texo_gp_handle_s* h);
 bool handle_finished(texo_gp_handle_s* h);

@@ -107,6 +107,12 @@ class Batch:
             return jid.value, None, stats
         return jid.value, targets[:2 * u].reshape(-1, 2).copy(), stats
 
+    def graphs(self):
+        """(captures, replays) of the batch advance's CUDA graph."""
+        c, r = C.c_uint64(), C.c_uint64()
+        abi.check(self.lib.texo_gp_batch_graphs(self.h, C.byref(c), C.byref(r)), "texo_gp_batch_graphs")
+        return c.value, r.value
+
     def counts(self):
         r, f, b = C.c_uint32(), C.c_uint32(), C.c_uint64()
         abi.check(self.lib.texo_gp_batch_counts(self.h, C.byref(r), C.byref(f), C.byref(b)), "texo_gp_batch_counts")
