@@ -348,6 +348,44 @@ int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_tar
  * optimizer state) without touching the device allocations. */
 int32_t texo_gp_reset(texo_gp_handle h);
 
+/* ---- routability-driven area rounds ------------------------------------
+ * The pieces of eplace::place's area-adjustment loop (eplace.rs:320-420),
+ * host engine. texo_gp_optimize_round runs one `optimize_density_once`
+ * (eplace.rs:439-582) from the handle's current coordinates with a fresh
+ * optimizer, multipliers and checkpoint: `stop` 0 stops at the final
+ * targets (10 / 10 / 20 %), 1 at AreaAdjustmentReady (LUT and register
+ * overflow <= 15 %, eplace.rs:130, 1403-1415); `reset_multipliers` sets the
+ * multipliers from elfPlace eqs. (27)-(28) (`area_adjusted_density_
+ * multipliers` / `_multiplier_step`, eplace.rs:1183-1232) instead of the
+ * initial weight; `density_scales` (NULL: this round's initial energies)
+ * fixes E0 to the first round's; the iteration cap counts
+ * `completed_iterations` of the earlier rounds. The result gives the global
+ * iteration count, whether the round was exhausted (cap or stationary) and
+ * the scales it used. texo_gp_set_charges installs an area adjustment
+ * (`apply_area_adjustment`, eplace.rs:793-818): member charges in the
+ * problem's member order and filler charges in texo_gp_fillers' order
+ * (either may be NULL); the real areas and the preconditioner follow. The
+ * caller composes the loop (the proposal between rounds is
+ * texo_gp_routing_demand, texo_gp_register_clustering_areas and
+ * texo_gp_adjust_instance_areas; texo_gb300.routability.place_routable is
+ * the Python composition). */
+typedef struct texo_gp_round {
+  int32_t stop;                  /* 0 final, 1 area-adjustment ready */
+  int32_t reset_multipliers;
+  const double* density_scales;  /* [num_fields] or NULL */
+  uint64_t completed_iterations;
+  uint32_t reserved[4];
+} texo_gp_round;
+typedef struct texo_gp_round_result {
+  uint64_t completed_iterations;
+  uint32_t exhausted;
+  uint32_t reserved;
+  double density_scales[TEXO_GP_MAX_FIELDS];
+} texo_gp_round_result;
+int32_t texo_gp_optimize_round(texo_gp_handle h, const texo_gp_round* round, uint32_t* out_targets_xy,
+                               double* out_coordinates, texo_gp_stats* stats, texo_gp_round_result* result);
+int32_t texo_gp_set_charges(texo_gp_handle h, const double* member_charge, const double* filler_charge);
+
 /* Per-stage device times: runs each stage of one full objective evaluation at
  * the handle's current coordinates `reps` times and writes the mean time of
  * one launch in milliseconds, measured with CUDA events on the handle's

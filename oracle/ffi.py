@@ -54,6 +54,16 @@ EVAL_CB = C.CFUNCTYPE(C.c_int32, C.c_void_p, c_f64p, C.c_uint64, c_f64p, c_f64p,
 _lib = None
 
 
+class OrcRound(C.Structure):
+    _fields_ = [("stop", C.c_int32), ("reset_multipliers", C.c_int32), ("density_scales", C.POINTER(C.c_double)),
+                ("completed_iterations", C.c_uint64)]
+
+
+class OrcRoundResult(C.Structure):
+    _fields_ = [("completed_iterations", C.c_uint64), ("exhausted", C.c_uint32),
+                ("density_scales", C.c_double * 4)]
+
+
 class PcgStats(C.Structure):
     _fields_ = [("iterations", C.c_uint64), ("restarts", C.c_uint64), ("stop", C.c_int32),
                 ("converged", C.c_int32), ("initial_residual_squared", C.c_double),
@@ -219,6 +229,9 @@ def lib():
             "orc_place": (C.c_int32, [C.c_void_p, C.c_int32, C.c_uint32, c_u32p, c_f64p, C.POINTER(RunStats)]),
             "orc_hpwl": (C.c_int32, [C.c_void_p, c_f64p, c_f64p]),
             "orc_trace": (C.c_uint32, [C.c_void_p, C.POINTER(abi.Iteration), C.c_uint32]),
+            "orc_set_charges": (C.c_int32, [C.c_void_p, c_f64p, c_f64p]),
+            "orc_place_round": (C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(OrcRound), c_f64p, c_u32p, c_f64p,
+                                            C.POINTER(RunStats), C.POINTER(OrcRoundResult)]),
             "orc_wirelength_preconditioner": (None, [C.c_void_p, c_f64p]),
             "orc_cell_incidence_weights": (None, [C.c_void_p, c_f64p]),
             "orc_nesterov_step": (C.c_int32, [C.POINTER(NState), c_f64p, C.c_uint64, c_f64p, C.c_uint64,
@@ -401,6 +414,34 @@ class Oracle:
         out = C.c_double()
         lib().orc_hpwl(self.h, P(coords), C.byref(out))
         return out.value
+
+    def set_charges(self, member_charge=None, filler_charge=None):
+        m = None if member_charge is None else np.ascontiguousarray(member_charge, dtype=np.float64)
+        q = None if filler_charge is None else np.ascontiguousarray(filler_charge, dtype=np.float64)
+        lib().orc_set_charges(self.h, P(m), P(q))
+
+    def place_round(self, stop, reset_multipliers, density_scales=None, completed_iterations=0, coordinates=None,
+                    threads=1):
+        """One round of eplace::place's area loop (optimize_density_once) from
+        `coordinates` (None: the initial ones): (status, targets, coords, stats, result)."""
+        r = OrcRound()
+        r.stop = int(stop)
+        r.reset_multipliers = 1 if reset_multipliers else 0
+        sc = None
+        if density_scales is not None:
+            sc = np.ascontiguousarray(density_scales, dtype=np.float64)
+            r.density_scales = P(sc)
+        r.completed_iterations = int(completed_iterations)
+        cin = None if coordinates is None else np.ascontiguousarray(coordinates, dtype=np.float64)
+        t = np.zeros(2 * self.units, np.uint32)
+        c = np.zeros(self.n)
+        s = RunStats()
+        res = OrcRoundResult()
+        st = lib().orc_place_round(self.h, threads, C.byref(r), P(cin), P(t, C.c_uint32), P(c), C.byref(s),
+                                   C.byref(res))
+        out = {"completed_iterations": res.completed_iterations, "exhausted": bool(res.exhausted),
+               "density_scales": [res.density_scales[f] for f in range(self.num_fields)]}
+        return st, t.reshape(-1, 2), c, s, out
 
     def trace(self):
         """Controller records of the last place() (texo_gp_iteration each)."""

@@ -1144,10 +1144,51 @@ struct Eplace {
     }
     return weighted_gamma_mean(gm.data(), w.data(), o.K, gamma_base_tiles, gamma);
   }
+  // density_stop_reached (eplace.rs:1397-1415): Final (every field at its
+  // target) or, before an area adjustment, AreaAdjustmentReady (the LUT and
+  // register fields at AREA_ADJUSTMENT_OVERFLOW_TARGET = 0.15, eplace.rs:130).
+  int stop_mode = 0;
   bool stop_reached(const Evaluation& ev) const {
-    for (uint32_t f = 0; f < o.K; ++f)
-      if (!(ev.fields[f].overflow <= target_of(f))) return false;
+    for (uint32_t f = 0; f < o.K; ++f) {
+      if (stop_mode == 1) {
+        const uint32_t k = o.field_kind[f].kind;
+        if (k != TEXO_GP_KIND_LUT && k != TEXO_GP_KIND_REGISTER) continue;
+        if (!(ev.fields[f].overflow <= 0.15)) return false;
+      } else if (!(ev.fields[f].overflow <= target_of(f))) {
+        return false;
+      }
+    }
     return true;
+  }
+  // area_adjusted_density_multipliers (eplace.rs:1183-1218) and
+  // area_adjusted_multiplier_step (:1220-1232): elfPlace eqs. (27)-(28).
+  int32_t area_multipliers(const Evaluation& ev, const std::vector<double>& scales, std::vector<double>& lambda,
+                           double& step) const {
+    std::vector<double> sg;
+    int32_t s = subgradient(ev, scales, sg);
+    if (s) return s;
+    double wl = 0.0;
+    for (uint32_t u = 0; u < o.U; ++u) {
+      wl += std::fabs(ev.wa_gx[u]);
+      wl += std::fabs(ev.wa_gy[u]);
+    }
+    double dens = 0.0;
+    for (uint32_t f = 0; f < o.K; ++f) dens += ev.fields[f].force_l1 * sg[f];
+    if (!std::isfinite(wl) || wl <= 0.0 || !std::isfinite(dens) || dens <= 0.0)
+      return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    const double scale = 0.1 * wl / dens;
+    lambda.assign(o.K, 0.0);
+    bool any = false;
+    for (uint32_t f = 0; f < o.K; ++f) {
+      lambda[f] = scale * sg[f];
+      if (!std::isfinite(lambda[f]) || lambda[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+      any = any || lambda[f] > 0.0;
+    }
+    if (!any) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    double nn = 0.0;
+    for (double m : lambda) nn += m * m;
+    step = (o.params.alpha_high - 1.0) * std::sqrt(nn);
+    return (std::isfinite(step) && step > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
   }
   void excess(const Evaluation& ev, double& mx, double& tot) const {
     mx = 0.0;
@@ -1294,10 +1335,20 @@ struct Eplace {
   }
 
   // optimize_density_once (eplace.rs:439-582) with the Final stop criterion.
+  // One round of eplace::place (optimize_density_once): from `start` (the
+  // initial coordinates when null), with fixed density scales when given,
+  // the area-reset multipliers when `reset`, and the iteration count of the
+  // earlier rounds (the cap counts all rounds).
+  const double* start = nullptr;
+  const double* fixed_scales = nullptr;
+  bool reset = false;
+  uint64_t offset = 0;
+  std::vector<double> scales_used;
+  bool exhausted_out = false;
   int32_t run(uint32_t cap_override, std::vector<uint32_t>& best_targets, std::vector<double>& final_coords,
               orc_run_stats& stats) {
     const size_t n = o.coord_count();
-    std::vector<double> coords = o.init_coords;
+    std::vector<double> coords = start ? std::vector<double>(start, start + n) : o.init_coords;
     Bounds b{o.lower.data(), o.lower.size(), o.upper.data(), o.upper.size()};
     uint64_t err = 0;
     stats = orc_run_stats{};
@@ -1315,7 +1366,8 @@ struct Eplace {
     if (s) return s;
     if ((s = validate_initial(initial))) return s;
     std::vector<double> scales(o.K);
-    for (uint32_t f = 0; f < o.K; ++f) scales[f] = rmax(initial.fields[f].energy, 1.0);
+    for (uint32_t f = 0; f < o.K; ++f) scales[f] = fixed_scales ? fixed_scales[f] : rmax(initial.fields[f].energy, 1.0);
+    scales_used = scales;
     if ((s = validate_fields(initial, scales))) return s;
     NState st;
     st.x = (b.lo_len == coords.size() && b.hi_len == coords.size()) ? project(coords, b) : coords;
@@ -1332,17 +1384,23 @@ struct Eplace {
     };
     if (stop_reached(initial)) {
       finish(initial);
+      stats.iterations = (uint32_t)offset;
       return TEXO_GP_OK;
     }
-    double m0;
-    if ((s = initial_multiplier(initial, n, m0))) return s;
-    std::vector<double> lambda(o.K, m0);
+    std::vector<double> lambda;
     double mstep = o.params.alpha_high - 1.0;
+    if (reset) {
+      if ((s = area_multipliers(initial, scales, lambda, mstep))) return s;
+    } else {
+      double m0;
+      if ((s = initial_multiplier(initial, n, m0))) return s;
+      lambda.assign(o.K, m0);
+    }
     Evaluation current = std::move(initial);
     std::vector<uint32_t> prev_stationary;
     bool have_prev_stationary = false;
     const uint32_t cap = cap_override ? cap_override : o.params.max_iterations;
-    uint32_t completed = 0;
+    uint32_t completed = (uint32_t)offset;
     std::vector<Evaluation> payloads;
     for (;;) {
       if (stop_reached(current)) break;
@@ -1862,6 +1920,46 @@ int32_t orc_place(orc_handle h, int32_t threads, uint32_t max_iterations, uint32
   int32_t s = ep.run(max_iterations, best, fc, *stats);
   if (targets && !best.empty()) std::memcpy(targets, best.data(), best.size() * 4);
   if (coordinates && !fc.empty()) std::memcpy(coordinates, fc.data(), fc.size() * 8);
+  return s;
+}
+
+int32_t orc_set_charges(orc_handle h, const double* member_charge, const double* filler_charge) {
+  Oracle& o = h->o;
+  if (member_charge) {
+    size_t k = 0;
+    for (auto& u : o.dunits)
+      for (auto& m : u.members) m.charge = member_charge[k++];
+  }
+  if (filler_charge)
+    for (size_t i = 0; i < o.fillers.size(); ++i) o.fillers[i].charge = filler_charge[i];
+  return TEXO_GP_OK;
+}
+
+int32_t orc_place_round(orc_handle h, int32_t threads, const orc_round* round, const double* coordinates_in,
+                        uint32_t* targets, double* coordinates, orc_run_stats* stats, orc_round_result* result) {
+  Oracle& o = h->o;
+  orc_run_stats local{};
+  if (!stats) stats = &local;
+  Eplace ep(o, threads);
+  h->trace.clear();
+  ep.trace = &h->trace;
+  ep.stop_mode = round ? round->stop : 0;
+  ep.reset = round && round->reset_multipliers;
+  ep.fixed_scales = round ? round->density_scales : nullptr;
+  ep.offset = round ? round->completed_iterations : 0;
+  ep.start = coordinates_in;
+  std::vector<uint32_t> best;
+  std::vector<double> fc;
+  const int32_t s = ep.run(0, best, fc, *stats);
+  if (targets && !best.empty()) std::memcpy(targets, best.data(), best.size() * 4);
+  if (coordinates && !fc.empty()) std::memcpy(coordinates, fc.data(), fc.size() * 8);
+  if (result) {
+    *result = orc_round_result{};
+    result->completed_iterations = stats->iterations;
+    result->exhausted = stats->exhausted;
+    for (size_t f = 0; f < ep.scales_used.size() && f < TEXO_GP_MAX_FIELDS; ++f)
+      result->density_scales[f] = ep.scales_used[f];
+  }
   return s;
 }
 

@@ -98,6 +98,29 @@ typedef struct orc_run_stats {
 } orc_run_stats;
 int32_t orc_place(orc_handle h, int32_t threads, uint32_t max_iterations, uint32_t* targets,
                   double* coordinates, orc_run_stats* stats);
+/* One round of eplace::place's area-adjustment loop (optimize_density_once,
+ * eplace.rs:439-582): stop 0 = final targets, 1 = AreaAdjustmentReady (LUT
+ * and register overflow <= 0.15); reset_multipliers = elfPlace eqs. (27)-(28)
+ * after an area adjustment; density_scales (NULL = from this round's initial
+ * energies); completed_iterations of earlier rounds (the cap counts all). */
+typedef struct orc_round {
+  int32_t stop;
+  int32_t reset_multipliers;
+  const double* density_scales;
+  uint64_t completed_iterations;
+} orc_round;
+typedef struct orc_round_result {
+  uint64_t completed_iterations;
+  uint32_t exhausted;
+  double density_scales[TEXO_GP_MAX_FIELDS];
+} orc_round_result;
+/* Member charges (the problem's member order) and filler charges; either may
+ * be NULL. */
+int32_t orc_set_charges(orc_handle h, const double* member_charge, const double* filler_charge);
+/* Runs one round from coordinates_in [2(U+F)] (NULL: the initial ones). */
+int32_t orc_place_round(orc_handle h, int32_t threads, const orc_round* round, const double* coordinates_in,
+                        uint32_t* targets, double* coordinates, orc_run_stats* stats, orc_round_result* result);
+
 /* The controller records of the last orc_place (one per completed iteration,
  * the first 4096): copies up to `capacity`, returns how many there are. */
 uint32_t orc_trace(orc_handle h, texo_gp_iteration* out, uint32_t capacity);

@@ -20,7 +20,7 @@ KIND_REG = (abi.KIND_REGISTER, 0)
 
 def rich_problem(seed=0, side=48, cells=2000, io=96, nets=2400, sigma=6.0, macro_fraction=0.4,
                  register_fraction=0.35, fixed_fraction=0.04, timed_fraction=0.15, fields=2,
-                 timed=True, macros=True, fixed=True):
+                 timed=True, macros=True, fixed=True, capacity=1):
     base = P.synthetic(side, cells, io, nets, sigma, seed, lib=ffi.lib())
     rng = np.random.default_rng(1000 + seed)
     W = H = side
@@ -74,7 +74,7 @@ def rich_problem(seed=0, side=48, cells=2000, io=96, nets=2400, sigma=6.0, macro
         upper.append(tuple(xy))
         cell_unit[c] = u
         member_ptr.append(len(mfield))
-    capacity = np.ones((fields, W * H), np.uint32)
+    capacity = np.full((fields, W * H), capacity, np.uint32)
     occupancy = []
     if fixed:
         # BELs held by fixed units (exchangeable kinds): a few tiles of each field

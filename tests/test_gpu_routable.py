@@ -1,0 +1,100 @@
+"""The routability-driven rounds of eplace::place (eplace.rs:320-420) on the
+GPU's host engine against the FP64 oracle's rounds, through the C ABI, on
+the two-kind routability case (tests/routable_rounds.py).
+
+The area rounds drive the register field's area up until it fills the free
+capacity, so the final round reaches the 10 % target only marginally (the
+oracle at iteration 222, register overflow 0.0999) and an FP32 trajectory
+may stall just above it instead; the comparison therefore caps the loop at
+200 iterations (best effort), past the area rounds and into the final round.
+
+Bounds: the same rounds (stop criteria in order, area rounds installed);
+the first proposal's relative area increase within 1e-3 relative of the
+oracle's and the installed member and filler charges within 1e-3 normwise;
+each round's iteration count within 10 % (at least 5) of the oracle's; every
+kind's member + filler total conserved to 1e-9; at the cap, per-field
+overflow within 0.01 and HPWL within 1 % of the oracle's.
+Installed charges: the evaluation at spread positions after
+texo_gp_set_charges within 1e-5 of the oracle's with the same charges.
+"""
+import numpy as np
+import pytest
+
+from oracle import ffi
+from texo_gb300 import abi, routability as R
+from texo_gb300.placer import Placer, default_params
+
+from routable_rounds import OracleRounds, routability_case
+
+pytestmark = pytest.mark.gpu
+
+
+def normwise(a, b):
+    return float(np.max(np.abs(a - b))) / float(np.max(np.abs(b)))
+
+
+def test_set_charges_matches_the_oracle():
+    prob, _, _, _ = routability_case()
+    prm = default_params(best_effort=1)
+    o = ffi.Oracle(prob, prm)
+    f, q, _ = o.fillers()
+    rng = np.random.default_rng(3)
+    member = np.asarray(prob.member_charge, dtype=np.float64) * (1.0 + 0.7 * rng.random(len(prob.member_charge)))
+    grow = {k: member[prob.member_field == k].sum() - np.asarray(prob.member_charge)[prob.member_field == k].sum()
+            for k in range(len(prob.fields))}
+    filler = q.copy()
+    for k in range(len(prob.fields)):
+        sel = f == k
+        filler[sel] = q[sel] * (1.0 - grow[k] / q[sel].sum())
+    assert np.all(filler >= 0)
+    o.set_charges(member, filler)
+    c, lo, hi = o.initial()
+    c = (lo + (hi - lo) * rng.random(c.size)).astype(np.float32).astype(np.float64)
+    r = o.evaluate(c, 2.0)
+    with Placer(prob, prm) as g:
+        g.set_charges(member, filler)
+        gf, gq = g.fillers()
+        assert np.array_equal(gq, filler)
+        d = g.evaluate(c, 2.0)
+    for key in ("density", "potential", "field_gradient", "wa_gradient"):
+        assert normwise(d[key], r[key]) <= 1e-5, key
+    for k in range(len(prob.fields)):
+        a, b = d["fields"][k], r["fields"][k]
+        assert abs(a.normalized_overflow - b.normalized_overflow) <= 1e-6 * max(b.normalized_overflow, 1.0)
+        assert abs(a.energy - b.energy) <= 1e-5 * abs(b.energy)
+
+
+def test_routable_rounds_match_the_oracle():
+    prob, ch, cv, ctl = routability_case()
+    prm = default_params(best_effort=1, max_iterations=200)
+    ro = OracleRounds(prob, prm)
+    f0, q0 = ro.fillers()
+    _, c_ref, ref = R.place_routable(prob, prm, ch, cv, register_controls=ctl, rounds=ro)
+    t, c, got = R.place_routable(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
+                                 register_controls=ctl)
+    a_rounds, b_rounds = got["rounds"], ref["rounds"]
+    assert [r["stop"] for r in a_rounds] == [r["stop"] for r in b_rounds]
+    assert got["area_rounds"] == ref["area_rounds"] >= 1 and len(b_rounds) >= 3
+    for a, b in zip(a_rounds, b_rounds):
+        assert abs(a["iterations"] - b["iterations"]) <= max(5, 0.10 * b["iterations"]), (a, b)
+    first_a, first_b = a_rounds[0]["relative_increase"], b_rounds[0]["relative_increase"]
+    assert abs(first_a - first_b) <= 1e-3 * first_b
+    assert normwise(got["member_charge"], ref["member_charge"]) <= 1e-3
+    # the first proposal can use up the fillers entirely (charges 0)
+    fa, fb = got["filler_charge"], ref["filler_charge"]
+    assert np.max(np.abs(fa - fb)) <= 1e-3 * max(np.max(np.abs(fb)), 1.0)
+    m0 = np.asarray(prob.member_charge, dtype=np.float64)
+    for k in range(len(prob.fields)):
+        before = m0[prob.member_field == k].sum() + q0[f0 == k].sum()
+        after = got["member_charge"][prob.member_field == k].sum() + got["filler_charge"][f0 == k].sum()
+        assert abs(after - before) <= 1e-9 * before
+    assert got["iterations"] == ref["iterations"] == 200
+    # both end points measured by the oracle, each with its own installed charges
+    o = ro.o
+    ev_ref = o.evaluate(c_ref, 4.0)
+    o.set_charges(got["member_charge"], got["filler_charge"])
+    ev = o.evaluate(c, 4.0)
+    for fa, fb in zip(ev["fields"], ev_ref["fields"]):
+        assert abs(fa.normalized_overflow - fb.normalized_overflow) <= 0.01
+    h_got, h_ref = o.hpwl(c), o.hpwl(c_ref)
+    assert abs(h_got - h_ref) <= 0.01 * h_ref

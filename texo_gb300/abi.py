@@ -111,6 +111,17 @@ class Iteration(C.Structure):
                 ("lambda_", C.c_double * 4), ("energy_scale", C.c_double * 4), ("overflow", C.c_double * 4)]
 
 
+class Round(C.Structure):
+    """texo_gp_round: one round of the area-adjustment loop."""
+    _fields_ = [("stop", C.c_int32), ("reset_multipliers", C.c_int32), ("density_scales", C.POINTER(C.c_double)),
+                ("completed_iterations", C.c_uint64), ("reserved", C.c_uint32 * 4)]
+
+
+class RoundResult(C.Structure):
+    _fields_ = [("completed_iterations", C.c_uint64), ("exhausted", C.c_uint32), ("reserved", C.c_uint32),
+                ("density_scales", C.c_double * 4)]
+
+
 class FieldEval(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
@@ -196,6 +207,9 @@ SIGNATURES = {
     "texo_gp_run": (C.c_int32, [_P, C.c_uint32, c_u32p, c_f64p, C.POINTER(Stats)]),
     "texo_gp_dct_form": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "texo_gp_reset": (C.c_int32, [_P]),
+    "texo_gp_optimize_round": (C.c_int32, [_P, C.POINTER(Round), c_u32p, c_f64p, C.POINTER(Stats),
+                                           C.POINTER(RoundResult)]),
+    "texo_gp_set_charges": (C.c_int32, [_P, c_f64p, c_f64p]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
     "texo_gp_trace": (C.c_int32, [_P, C.POINTER(Iteration), C.c_uint32, c_u32p]),
     "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),

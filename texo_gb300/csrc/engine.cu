@@ -730,6 +730,14 @@ struct Controller {
   unsigned long long launches = 0;
   static constexpr size_t kTraceMax = 4096;
   std::vector<texo_gp_iteration> trace;   // host engine: one record per completed iteration
+  // One round of eplace::place's area-adjustment loop (texo_gp_optimize_round):
+  // the stop criterion (0 final, 1 area-adjustment ready), the area-reset
+  // multipliers, fixed density scales (E0 of the first round) and the
+  // iterations of the earlier rounds.
+  int stop_mode = 0;
+  bool reset_mult = false;
+  std::vector<double> fixed_scales;
+  uint64_t iter_offset = 0;
 
   explicit Controller(Instance& i) : I(i), hr(i.h_run->run) { std::memset(&hr, 0, sizeof(hr)); }
   ~Controller() {
@@ -738,6 +746,10 @@ struct Controller {
       if (e) cudaEventDestroy(e);
   }
 
+  static int32_t fail_norm(const char* what) {
+    set_last_error(what);
+    return TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
   double margin(double x, double y) const {
     const double eps = std::max(std::numeric_limits<double>::epsilon(), I.m.params.objective_margin_ulps * 0x1p-24);
     return eps * (1.0 + std::fabs(x) + std::fabs(y));
@@ -839,10 +851,49 @@ struct Controller {
     out = wsum == 0.0 ? base : ws / wsum;
     return (std::isfinite(out) && out > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
   }
+  // density_stop_reached (eplace.rs:1397-1415): Final, or AreaAdjustmentReady
+  // (LUT and register fields at 0.15, AREA_ADJUSTMENT_OVERFLOW_TARGET, eplace.rs:130)
   bool stop_reached(const EvalRec& e) const {
-    for (uint32_t f = 0; f < I.m.K; ++f)
-      if (!(e.overflow[f] <= I.m.overflow_target(f))) return false;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      if (stop_mode == 1) {
+        const uint32_t k = I.m.kinds[f].kind;
+        if (k != TEXO_GP_KIND_LUT && k != TEXO_GP_KIND_REGISTER) continue;
+        if (!(e.overflow[f] <= 0.15)) return false;
+      } else if (!(e.overflow[f] <= I.m.overflow_target(f))) {
+        return false;
+      }
+    }
     return true;
+  }
+  // area_adjusted_density_multipliers and area_adjusted_multiplier_step
+  // (eplace.rs:1183-1232), elfPlace eqs. (27)-(28)
+  int32_t area_multipliers(const EvalRec& e) {
+    TRY(validate_fields(e));
+    const double beta = I.m.params.beta;
+    double sg[kMaxFields], dens = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      const double ne = e.energy[f] / e0[f];
+      sg[f] = ne + 0.5 * beta * ne * ne;
+      if (!std::isfinite(sg[f]) || sg[f] < 0.0) return fail_norm("area-reset multipliers: subgradient");
+      dens += e.force[f] * sg[f];
+    }
+    if (!std::isfinite(e.wal1) || e.wal1 <= 0.0 || !std::isfinite(dens) || dens <= 0.0) {
+      set_last_error("area-reset multipliers: wirelength force " + std::to_string(e.wal1) + ", density force " +
+                     std::to_string(dens));
+      return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    }
+    const double scale = 0.1 * e.wal1 / dens;
+    bool any = false;
+    double nn = 0.0;
+    for (uint32_t f = 0; f < I.m.K; ++f) {
+      lambda[f] = scale * sg[f];
+      if (!std::isfinite(lambda[f]) || lambda[f] < 0.0) return fail_norm("area-reset multipliers: multiplier");
+      any = any || lambda[f] > 0.0;
+      nn += lambda[f] * lambda[f];
+    }
+    if (!any) return fail_norm("area-reset multipliers: all zero");
+    mstep = (I.m.params.alpha_high - 1.0) * std::sqrt(nn);
+    return (std::isfinite(mstep) && mstep > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
   }
   void excess(const EvalRec& e, double& mx, double& tot) const {
     mx = 0.0;
@@ -858,7 +909,7 @@ struct Controller {
     for (uint32_t f = 0; f < I.m.K && ok; ++f)
       ok = std::isfinite(e.energy[f]) && e.energy[f] >= 0.0 && std::isfinite(e.overflow[f]) &&
            std::isfinite(e.force[f]) && e.force[f] >= 0.0;
-    return ok ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+    return ok ? TEXO_GP_OK : fail_norm("initial evaluation not finite");
   }
   int32_t validate_fields(const EvalRec& e) const {
     for (uint32_t f = 0; f < I.m.K; ++f)
@@ -890,7 +941,7 @@ struct Controller {
       en += ne * ne;
     }
     const double lg = std::log(beta * std::sqrt(en) + 1.0);
-    if (!std::isfinite(lg) || lg < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    if (!std::isfinite(lg) || lg < 0.0) return fail_norm("multiplier growth logarithm");
     const double lo = I.m.params.alpha_low, hi = I.m.params.alpha_high;
     const double growth = lo + (1.0 - 1.0 / (1.0 + lg)) * (hi - lo);
     if (!(growth >= lo && growth <= hi)) return TEXO_GP_ERR_INVALID_NORMALIZATION;
@@ -910,7 +961,7 @@ struct Controller {
     launch_finalize(D, I.r, nvb, FIN_PRECOND, s);
     EvalRec eo;
     TRY(evaluate(I.bufX, I.gX, gam, density_at_x, eo));
-    if (I.h_iscal[SI_PBAD]) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    if (I.h_iscal[SI_PBAD]) return fail_norm("preconditioner out of range");
     const double pmin = I.h_scal[SC_PMIN], pmax = I.h_scal[SC_PMAX];
     TRY(checked(eo));
     bool restart = false;
@@ -1196,6 +1247,7 @@ struct Controller {
     if (I.m.params.engine == TEXO_GP_ENGINE_DEVICE) return run_device(budget);
     const uint32_t K = I.m.K;
     if (phase == 0) {
+      completed = (uint32_t)iter_offset;
       lambda.assign(K, 0.0);
       e0.assign(K, 1.0);
       TRY(push_inputs());
@@ -1207,7 +1259,7 @@ struct Controller {
       EvalRec initial;
       TRY(evaluate(I.bufX, I.gX, g0, true, initial));
       TRY(validate_initial(initial));
-      for (uint32_t f = 0; f < K; ++f) e0[f] = std::fmax(initial.energy[f], 1.0);
+      for (uint32_t f = 0; f < K; ++f) e0[f] = fixed_scales.empty() ? std::fmax(initial.energy[f], 1.0) : fixed_scales[f];
       TRY(validate_fields(initial));
       CU(cudaMemcpyAsync(I.bufXp, I.bufX, (size_t)I.d.nobj * sizeof(float2), cudaMemcpyDeviceToDevice, I.stream));
       TRY(save_best());
@@ -1221,13 +1273,18 @@ struct Controller {
         converged = true;
         return TEXO_GP_OK;
       }
-      // initial_density_multiplier (eplace.rs:1126-1148)
-      double dens = 0.0;
-      for (uint32_t f = 0; f < K; ++f) dens += initial.rawl1[f];
-      const double m0 = (initial.wal1 == 0.0 || dens == 0.0) ? 1.0 : I.m.params.initial_density_weight * initial.wal1 / dens;
-      if (!(std::isfinite(m0) && m0 > 0.0)) return TEXO_GP_ERR_INVALID_NORMALIZATION;
-      lambda.assign(K, m0);
-      mstep = I.m.params.alpha_high - 1.0;
+      if (reset_mult) {
+        TRY(area_multipliers(initial));
+      } else {
+        // initial_density_multiplier (eplace.rs:1126-1148)
+        double dens = 0.0;
+        for (uint32_t f = 0; f < K; ++f) dens += initial.rawl1[f];
+        const double m0 =
+            (initial.wal1 == 0.0 || dens == 0.0) ? 1.0 : I.m.params.initial_density_weight * initial.wal1 / dens;
+        if (!(std::isfinite(m0) && m0 > 0.0)) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+        lambda.assign(K, m0);
+        mstep = I.m.params.alpha_high - 1.0;
+      }
       TRY(push_inputs());
     }
     uint32_t done_now = 0;
@@ -1928,6 +1985,86 @@ int32_t texo_gp_run(texo_gp_handle h, uint32_t max_iterations, uint32_t* out_tar
   }
   int32_t t = handle_targets(h, out_targets, out_coords, stats, s);
   return t ? t : s;
+}
+
+int32_t texo_gp_set_charges(texo_gp_handle h, const double* member_charge, const double* filler_charge) {
+  if (!h) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  Instance& I = *h->inst;
+  HostModel& m = I.m;
+  const size_t nobj = (size_t)m.U + m.F;
+  if (member_charge)
+    for (uint32_t i = 0; i < m.Mm; ++i)
+      if (!std::isfinite(member_charge[i]) || member_charge[i] <= 0.0) {
+        set_last_error("texo_gp_set_charges: member " + std::to_string(i));
+        return TEXO_GP_ERR_INVALID_MEMBER_CHARGE;
+      }
+  if (filler_charge)
+    for (uint32_t j = 0; j < m.F; ++j) {
+      if (!std::isfinite(filler_charge[j])) return TEXO_GP_ERR_NONFINITE_FILLER;
+      if (filler_charge[j] < 0.0) return TEXO_GP_ERR_NEGATIVE_FILLER_CHARGE;
+    }
+  if (member_charge) {
+    m.real_area.assign(m.K, 0.0);
+    for (uint32_t i = 0; i < m.Mm; ++i) {
+      m.mem_q[i] = (float)member_charge[i];
+      m.real_area[m.mem_field[i]] += member_charge[i];
+    }
+  }
+  if (filler_charge)
+    for (uint32_t j = 0; j < m.F; ++j) m.fil_q[j] = filler_charge[j];
+  // per-field charge of every optimizer object (the preconditioner's)
+  std::fill(m.pre_q.begin(), m.pre_q.end(), 0.0);
+  for (uint32_t u = 0; u < m.U; ++u)
+    for (int i = m.unit_mem_ptr[u]; i < m.unit_mem_ptr[u + 1]; ++i)
+      m.pre_q[(size_t)m.mem_field[i] * nobj + u] += member_charge ? member_charge[i] : (double)m.mem_q[i];
+  for (uint32_t j = 0; j < m.F; ++j) m.pre_q[(size_t)m.fil_field[j] * nobj + m.U + j] = m.fil_q[j];
+  std::vector<float> fq(m.F), pq(m.pre_q.size());
+  for (uint32_t j = 0; j < m.F; ++j) fq[j] = (float)m.fil_q[j];
+  for (size_t i = 0; i < pq.size(); ++i) pq[i] = (float)m.pre_q[i];
+  Dev& D = I.d;
+  if (m.Mm) CU(cudaMemcpyAsync((void*)D.mem_q, m.mem_q.data(), m.Mm * sizeof(float), cudaMemcpyHostToDevice, I.stream));
+  if (m.F) CU(cudaMemcpyAsync((void*)D.fil_q, fq.data(), m.F * sizeof(float), cudaMemcpyHostToDevice, I.stream));
+  if (!pq.empty())
+    CU(cudaMemcpyAsync((void*)D.pre_q, pq.data(), pq.size() * sizeof(float), cudaMemcpyHostToDevice, I.stream));
+  for (uint32_t f = 0; f < m.K; ++f) I.h_scal[SC_REAL_AREA + f] = m.real_area[f];
+  CU(cudaMemcpyAsync(I.r.scal + SC_REAL_AREA, I.h_scal + SC_REAL_AREA, m.K * sizeof(double), cudaMemcpyHostToDevice,
+                     I.stream));
+  CU(cudaStreamSynchronize(I.stream));
+  return TEXO_GP_OK;
+}
+
+int32_t texo_gp_optimize_round(texo_gp_handle h, const texo_gp_round* round, uint32_t* out_targets,
+                               double* out_coords, texo_gp_stats* stats, texo_gp_round_result* result) {
+  if (!h || !round) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  if (round->stop != 0 && round->stop != 1) return TEXO_GP_ERR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lk(h->mu);
+    Instance& I = *h->inst;
+    if (I.m.params.engine != TEXO_GP_ENGINE_HOST) {
+      set_last_error("texo_gp_optimize_round runs with the host engine");
+      return TEXO_GP_ERR_UNSUPPORTED;
+    }
+    // a fresh controller (Nesterov state, multipliers, checkpoint) from the
+    // handle's current coordinates
+    auto c = std::make_unique<Controller>(I);
+    c->stop_mode = round->stop;
+    c->reset_mult = round->reset_multipliers != 0;
+    c->iter_offset = round->completed_iterations;
+    if (round->density_scales) c->fixed_scales.assign(round->density_scales, round->density_scales + I.m.K);
+    h->ctl = std::move(c);
+    CU(cudaMemsetAsync(I.prev_targets, 0, 2 * (size_t)I.m.U * 4, I.stream));
+  }
+  const int32_t s = texo_gp_run(h, 0, out_targets, out_coords, stats);
+  if (result) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    const Controller& C = *h->ctl;
+    std::memset(result, 0, sizeof(*result));
+    result->completed_iterations = C.completed;
+    result->exhausted = C.exhausted ? 1u : 0u;
+    for (size_t f = 0; f < C.e0.size() && f < TEXO_GP_MAX_FIELDS; ++f) result->density_scales[f] = C.e0[f];
+  }
+  return s;
 }
 
 int32_t texo_gp_reset(texo_gp_handle h) {

@@ -348,6 +348,38 @@ class Placer:
             abi.check(code, "texo_gp_run")
         return targets.reshape(-1, 2), coords, _stats_dict(st)
 
+    def optimize_round(self, stop, reset_multipliers, density_scales=None, completed_iterations=0):
+        """One round of eplace::place's area-adjustment loop from the current
+        coordinates (texo_gp_optimize_round): returns (targets [U, 2],
+        coordinates, stats, result dict)."""
+        r = abi.Round()
+        r.stop = int(stop)
+        r.reset_multipliers = 1 if reset_multipliers else 0
+        sc = None
+        if density_scales is not None:
+            sc = np.ascontiguousarray(density_scales, dtype=np.float64)
+            r.density_scales = abi.ptr(sc, C.c_double)
+        r.completed_iterations = int(completed_iterations)
+        t = np.zeros(2 * self.units, np.uint32)
+        c = np.zeros(self.n)
+        s = abi.Stats()
+        res = abi.RoundResult()
+        code = self.lib.texo_gp_optimize_round(self.h, C.byref(r), abi.ptr(t, C.c_uint32), abi.ptr(c, C.c_double),
+                                               C.byref(s), C.byref(res))
+        if code not in (0, abi.CODE["DID_NOT_CONVERGE"]):
+            abi.check(code, "texo_gp_optimize_round")
+        out = {"completed_iterations": res.completed_iterations, "exhausted": bool(res.exhausted),
+               "density_scales": [res.density_scales[f] for f in range(self.num_fields)], "status": code}
+        return t.reshape(-1, 2), c, _stats_dict(s), out
+
+    def set_charges(self, member_charge=None, filler_charge=None):
+        """Installs an area adjustment (texo_gp_set_charges)."""
+        m = None if member_charge is None else np.ascontiguousarray(member_charge, dtype=np.float64)
+        f = None if filler_charge is None else np.ascontiguousarray(filler_charge, dtype=np.float64)
+        abi.check(self.lib.texo_gp_set_charges(self.h, abi.ptr(m, C.c_double) if m is not None else None,
+                                               abi.ptr(f, C.c_double) if f is not None else None),
+                  "texo_gp_set_charges")
+
     def reset(self):
         abi.check(self.lib.texo_gp_reset(self.h), "texo_gp_reset")
 

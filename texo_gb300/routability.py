@@ -151,7 +151,7 @@ def _utilization(demand, capacity, x, y):
 
 
 def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler_field, filler_charge,
-                            member_charge=None, register_controls=None, device=0):
+                            member_charge=None, register_controls=None, device=0, demand=None, clustering=None):
     """`propose_area_adjustment` (eplace.rs:627-740) for one placement state:
     the nets' bounding boxes at the unit origins `coordinates[:2U]`, their
     RUDY demand on the routing-capacity grid (`capacity_h` / `capacity_v`,
@@ -162,8 +162,18 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     ce), for the register members), and `adjust_instance_areas` against the
     fillers (`filler_field`, `filler_charge`, as `Placer.fillers()` gives
     them). `member_charge` overrides the problem's member charges (after an
-    earlier round). Returns (InstanceAreaAdjustment, metrics dict)."""
+    earlier round). `demand(W, H, boxes) -> (h, v)` and `clustering(xy,
+    clock_lsr, ce, count) -> areas` replace the GPU RUDY map and clustering
+    areas (a checker passes its own). Returns (InstanceAreaAdjustment,
+    metrics dict)."""
     from .placer import net_bounding_boxes, routing_demand
+    if demand is None:
+        def demand(w, h, boxes):
+            hd, vd, _ = routing_demand(w, h, boxes, device=device)
+            return hd, vd
+    if clustering is None:
+        def clustering(xy, clock_lsr, ce, count):
+            return register_clustering_areas(xy, clock_lsr, ce, count, device=device)[0]
     cap_h = np.asarray(capacity_h, dtype=np.uint32)
     cap_v = np.asarray(capacity_v, dtype=np.uint32)
     if cap_h.ndim != 2 or cap_h.shape != cap_v.shape or cap_h.size == 0:
@@ -171,7 +181,7 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     H, W = cap_h.shape
     U = problem.num_units
     pos = np.asarray(coordinates, dtype=np.float64)[: 2 * U].reshape(-1, 2)
-    h_dem, v_dem, _ = routing_demand(W, H, net_bounding_boxes(problem, pos), device=device)
+    h_dem, v_dem = demand(W, H, net_bounding_boxes(problem, pos))
     ptr = np.asarray(problem.member_ptr, dtype=np.int64)
     movable = np.any(problem.lower_xy != problem.upper_xy, axis=1)
     members = np.concatenate([np.arange(ptr[u], ptr[u + 1]) for u in np.nonzero(movable)[0]] or [np.zeros(0, int)])
@@ -189,7 +199,7 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     routing = np.array([routability_optimized_area(c, min(a, SQRT_2), min(b, SQRT_2))
                         for c, a, b in zip(charge, hu, vu)])
     routing = np.where(inflatable, routing, charge)
-    clustering = np.zeros(len(members))
+    clus_area = np.zeros(len(members))
     if register_controls:
         cells = np.asarray(problem.member_cell, dtype=np.int64)[members]
         is_reg = np.array([fields[f][0] == abi.KIND_REGISTER for f in field], dtype=bool)
@@ -198,12 +208,11 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
             ctl = np.array([register_controls[int(c)] for c in cells[regs]], dtype=np.uint64).reshape(-1, 3)
             cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
             count = int(np.sum(movable[cell_unit]))   # cells of movable units (movable_instance_count)
-            areas, _ = register_clustering_areas(pos[unit_of[regs]] + off[regs], ctl[:, :2], ctl[:, 2], count,
-                                                 device=device)
-            clustering[regs] = areas
+            areas = clustering(pos[unit_of[regs]] + off[regs], ctl[:, :2], ctl[:, 2], count)
+            clus_area[regs] = areas
     fk = np.array([kind_key(fields[int(f)]) for f in np.asarray(filler_field).reshape(-1)], dtype=np.uint32)
     fq = np.asarray(filler_charge, dtype=np.float64).reshape(-1)
-    adj = adjust_instance_areas(keys, charge, routing, np.zeros(len(members)), fk, fq, clustering)
+    adj = adjust_instance_areas(keys, charge, routing, np.zeros(len(members)), fk, fq, clus_area)
     before, increase = {}, {}
     for k, c, a in zip(keys.tolist(), charge, adj.member_areas):
         before[k] = before.get(k, 0.0) + c
@@ -219,3 +228,113 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
                "total_relative_increase": rel, "maximum_relative_increase": rel_max,
                "members": members}
     return adj, metrics
+
+
+def area_round_limit(problem):
+    """`area_adjustment_round_limit` (eplace.rs:584-626): every round that
+    installs area raises the total by at least 1 %, and the area can only
+    grow into the free capacity of the member kinds, so rounds beyond
+    ceil(log_1.01(available / initial)) + 1 mean a malformed loop."""
+    ptr = np.asarray(problem.member_ptr, dtype=np.int64)
+    movable = np.any(problem.lower_xy != problem.upper_xy, axis=1)
+    mem = np.concatenate([np.arange(ptr[u], ptr[u + 1]) for u in np.nonzero(movable)[0]] or [np.zeros(0, int)])
+    initial = float(np.sum(np.asarray(problem.member_charge, dtype=np.float64)[mem]))
+    fields = sorted(set(int(f) for f in np.asarray(problem.member_field)[mem]))
+    fixed = np.asarray(problem.fixed_occupancy, dtype=np.int64).reshape(-1, 3)
+    available = 0.0
+    for f in fields:
+        available += float(int(np.sum(problem.capacity[f], dtype=np.int64)) - int(np.sum(fixed[:, 0] == f)))
+    if not (np.isfinite(initial) and initial > 0.0 and available >= initial):
+        raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "area_round_limit")
+    threshold, rounds = initial, 0
+    while threshold < available:
+        threshold *= 1.01
+        rounds += 1
+    return rounds + 1
+
+
+class DeviceRounds:
+    """The rounds of place_routable on this library's host engine."""
+
+    def __init__(self, problem, params):
+        from .placer import Placer
+        prm = params
+        prm.engine = abi.ENGINE_HOST
+        self.g = Placer(problem, prm)
+        self.demand = None
+        self.clustering = None
+
+    def fillers(self):
+        return self.g.fillers()
+
+    def round(self, stop, reset, scales, completed, coordinates):
+        # the handle keeps the previous round's final coordinates itself
+        t, c, _, res = self.g.optimize_round(stop, reset, scales, completed)
+        return res["status"], t, c, res
+
+    def set_charges(self, member_charge, filler_charge):
+        self.g.set_charges(member_charge, filler_charge)
+
+    def close(self):
+        self.g.close()
+
+
+def place_routable(problem, params, capacity_h, capacity_v, register_controls=None, rounds=None):
+    """eplace::place with a routing-capacity map (eplace.rs:320-420): density
+    rounds that stop at AreaAdjustmentReady (LUT and register overflow at
+    15 %), each followed by `propose_area_adjustment` (RUDY utilization,
+    elfPlace eq. 29, register clustering, the charge-conserving instance
+    areas); an adjustment that grows any kind is installed (member and filler
+    charges) and the next round restarts the optimizer with the elfPlace
+    eq. (27)-(28) multipliers and the first round's density scales; once the
+    installed increase is below 1 % (or nothing grew) a last round runs to
+    the final targets. `rounds` runs the rounds (default: DeviceRounds, this
+    library's host engine). Returns (targets [U, 2], coordinates, info)."""
+    backend = rounds or DeviceRounds(problem, params)
+    K = len(problem.fields)
+    limit = area_round_limit(problem)
+    member_charge = np.array(problem.member_charge, dtype=np.float64)
+    filler_field, filler_charge = backend.fillers()
+    filler_charge = np.array(filler_charge, dtype=np.float64)
+    completed, area_round, previous, scales, reset = 0, 0, None, None, False
+    coords = None
+    info = {"rounds": [], "area_rounds": 0}
+    try:
+        while True:
+            stop = 0 if (previous is not None and previous < 0.01) else 1
+            status, targets, coords, res = backend.round(stop, reset, scales, completed, coords)
+            if status not in (0, abi.CODE["DID_NOT_CONVERGE"]):
+                raise abi.TexoGpError(status, "place_routable")
+            if scales is None:
+                scales = np.array(res["density_scales"][:K])
+            entry = {"stop": "final" if stop == 0 else "area_ready",
+                     "iterations": int(res["completed_iterations"] - completed), "exhausted": res["exhausted"]}
+            info["rounds"].append(entry)
+            completed = int(res["completed_iterations"])
+            if stop == 0 or res["exhausted"]:
+                if status == abi.CODE["DID_NOT_CONVERGE"]:
+                    raise abi.TexoGpError(status, "place_routable")
+                info["iterations"] = completed
+                info["member_charge"] = member_charge
+                info["filler_charge"] = filler_charge
+                return targets, coords, info
+            adj, metrics = propose_area_adjustment(problem, coords, capacity_h, capacity_v, filler_field,
+                                                   filler_charge, member_charge=member_charge,
+                                                   register_controls=register_controls, demand=backend.demand,
+                                                   clustering=backend.clustering)
+            entry["relative_increase"] = float(metrics["total_relative_increase"])
+            entry["members_inflated"] = int(metrics["members_inflated"])
+            if not adj.requires_optimizer_reset:
+                previous, reset = 0.0, True
+                continue
+            if area_round >= limit:
+                raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "place_routable: area round limit")
+            member_charge[metrics["members"]] = adj.member_areas
+            filler_charge = np.array(adj.filler_areas, dtype=np.float64)
+            backend.set_charges(member_charge, filler_charge)
+            previous, reset = float(metrics["total_relative_increase"]), True
+            area_round += 1
+            info["area_rounds"] = area_round
+    finally:
+        if rounds is None:
+            backend.close()
