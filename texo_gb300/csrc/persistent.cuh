@@ -6,13 +6,15 @@
 namespace tgp {
 
 // Co-resident blocks per SM of the persistent kernels. One instance alone
-// runs 2 per SM (128 registers per thread; each instance has 2 virtual
-// blocks per SM, so a single launch covers all of them). The batch kernel
-// runs 4 per SM (64 registers): many latency-bound instances share the GPU,
-// and more resident warps win over registers there. Measured on GB300 at
-// 42k cells: 2306 it/s with 2 per SM against 2139 with 4; 64 mixed jobs:
-// 193 placements/s with 4 per SM against 146 with 2.
-constexpr int kBlocksPerSm = 2;
+// runs 1 per SM (up to 255 registers per thread; each instance has one
+// virtual block per SM, so a single launch covers all of them): at 42k cells
+// the loop is bound by its grid barriers and the FFT passes' latency, which
+// fewer, larger blocks cut (measured on GB300: 3633 it/s with 1 per SM, 3254
+// with 2, 2139 with 4). The batch kernel runs 4 per SM (64 registers): many
+// latency-bound instances share the GPU, and more resident warps win over
+// registers there (64 mixed jobs: 193 placements/s with 4 per SM against
+// 146 with 2).
+constexpr int kBlocksPerSm = 1;
 constexpr int kBatchBlocksPerSm = 4;
 
 // Grid barrier words (device memory, zeroed before each launch): an arrival
