@@ -369,6 +369,7 @@ def run_serial(jobs, engine):
 
 
 def batch_report(n=64):
+    import numpy as np
     from texo_gb300 import abi
     jobs = batch_workload(n)
     wall_b, res_b, launches, parts = run_batched(jobs)
@@ -378,6 +379,22 @@ def batch_report(n=64):
     same = sum(1 for i in range(n) if res_b[i]["hpwl"] == res_d[i]["hpwl"])
     same_s = sum(1 for i in range(n) if res_s[i]["hpwl"] == res_d[i]["hpwl"])
     iters = sum(s["iterations"] for s in res_b.values())
+    # the batched kernels' roofline: every job's algorithmic bytes (its full
+    # and density-reusing evaluations, line-search trials and vector updates,
+    # as for the single instance) over the time spent advancing the batch
+    total_bytes = 0.0
+    for i, (p, prm) in enumerate(jobs):
+        st = res_b[i]
+        if not st.get("iterations"):
+            continue
+        nj = dict(U=p.num_units, F=int(np.count_nonzero(p.capacity)), M=int(p.member_ptr[-1]),
+                  B=prm.bins_x * prm.bins_y, Hb=prm.bins_y, E=p.num_nets, P=p.num_pins, K=len(p.fields))
+        ev, dv, tr = st["evaluations"], st["density_evaluations"], st["line_search_trials"]
+        total_bytes += (dv * eval_bytes(nj, persistent=True) + (ev - dv) * reused_eval_bytes(nj)
+                        + tr * stage_bytes("candidate", nj)
+                        + st["iterations"] * (stage_bytes("precond", nj) + stage_bytes("extrapolate", nj)))
+    peak, peak_kind = peaks()
+    adv = parts["advance"]
     failed = {i: s["status"] for i, s in res_b.items() if s["status"] not in ("OK", "DID_NOT_CONVERGE")}
     return {"instances": n, "cells": "log-uniform 1k..40k", "placements_per_s_served": n / wall_s,
             "speedup_served_vs_serial_host_fp32": wall_h / wall_s,
@@ -388,7 +405,13 @@ def batch_report(n=64):
             "batched_launches": launches, "identical_to_alone": "%d/%d" % (same, n), "failed": failed,
             "converged": sum(1 for s in res_b.values() if s["converged"]),
             "wall_s": {"served": wall_s, "batched": wall_b, "serial_device": wall_d, "serial_host": wall_h},
-            "batched_wall_split_s": parts}
+            "batched_wall_split_s": parts,
+            "batched_roofline": {"algorithmic_bytes": total_bytes, "advance_s": adv,
+                                 "achieved_gbs": total_bytes / adv / 1e9 if adv > 0 else None,
+                                 "peak_gbs": peak, "peak_source": peak_kind,
+                                 "frac": total_bytes / adv / 1e9 / peak if adv > 0 else None,
+                                 "time": "wall time of the advance calls (the launches and their "
+                                         "state copies, host staging included)"}}
 
 
 def serve_request(i, lo=2000, hi=100000, sigma=6.0):
@@ -414,7 +437,8 @@ def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
     """Serving stream: Poisson arrivals at `load` x the measured batched
     capacity of the same request distribution; placements/s and p50/p99
     time-to-converge (submit to retire) of `n_requests` requests; final HPWL
-    of the smallest requests against the FP64 oracle."""
+    of a size-stratified sample of requests (smallest to largest) against the
+    FP64 oracle."""
     import threading
     import numpy as np
     from texo_gb300.placer import Server
@@ -454,19 +478,26 @@ def serve_report(n_requests=200, probe=32, load=0.8, oracle_sample=6, seed=7):
               "placements_per_s": n_requests / ((last - first) / 1000.0),
               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
               "converged": len(conv), "overflow_le_0.10": len(within), "failed": n_requests - len(ok)}
-    # FP64 oracle on the smallest requests: relative final-HPWL difference
+    # FP64 oracle on a size-stratified sample: the smallest, the largest and
+    # evenly spaced size quantiles between; relative final-HPWL difference
     try:
         from oracle import ffi
-        small = sorted(ok, key=lambda i: sizes[i])[:oracle_sample]
-        errs = []
-        for i in small:
+        by_size = sorted(ok, key=lambda i: sizes[i])
+        picks = sorted({by_size[round(q * (len(by_size) - 1))] for q in np.linspace(0.0, 1.0, oracle_sample)}) \
+            if by_size else []
+        errs, jobs = [], []
+        for i in picks:
             prob, prm = serve_request(i)
             st, _, _, s = ffi.Oracle(prob, prm).place(threads=5)
             if s.hpwl > 0:
-                errs.append(abs(results[i]["hpwl"] - s.hpwl) / s.hpwl)
+                e = abs(results[i]["hpwl"] - s.hpwl) / s.hpwl
+                errs.append(e)
+                jobs.append({"request": int(i), "units": int(sizes[i]), "rel_err": e})
         report["hpwl_rel_err_vs_fp64_oracle"] = {"jobs": len(errs), "max": max(errs) if errs else None,
                                                  "mean": float(np.mean(errs)) if errs else None,
-                                                 "sample": "the %d smallest requests" % len(errs)}
+                                                 "sample": "%d requests at evenly spaced size quantiles "
+                                                           "(smallest to largest)" % len(errs),
+                                                 "per_job": jobs}
     except Exception as e:  # the oracle is optional on the box
         report["hpwl_rel_err_vs_fp64_oracle"] = {"error": str(e)}
     return report
@@ -581,6 +612,38 @@ def scatter_report(workloads=("lfe5u-85-42k", "stress-1m"), reps=20):
                                       np.array_equal(grids[0][1], grids[1][1]))
         out[wl] = res
     return out
+
+
+def probe(spec):
+    """Small, targeted workloads for profiler captures (no timing):
+    "tc:N" three tensor-core Poisson solves on an N x N bin grid (a 48 x 48
+    problem, so little else runs); "scatter:WORKLOAD" two direct and two
+    tiled host-engine scatters of WORKLOAD at spread positions."""
+    import numpy as np
+    from texo_gb300 import abi
+    from texo_gb300.placer import Placer, default_params
+    kind, arg = spec.split(":")
+    if kind == "tc":
+        n = int(arg)
+        prob = make_problem("ecp5-2k", 0)
+        i = np.arange(n * n)
+        d = ((i * 31 + 7) % 101) - 50.0 + ((i * 13 + 5) % 17) / 17.0
+        with Placer(prob, default_params(dct_mode=abi.DCT_TENSOR, engine=abi.ENGINE_HOST, bins_x=n, bins_y=n)) as g:
+            for _ in range(3):
+                g.poisson(d)
+    elif kind == "scatter":
+        prob = make_problem(arg, 0)
+        for mode in (abi.SCATTER_DIRECT, abi.SCATTER_TILED):
+            prm = make_params(arg, abi.ENGINE_HOST, abi.DCT_FP32)
+            prm.scatter_mode = mode
+            with Placer(prob, prm) as g:
+                c, lo, hi = g.initial()
+                c = lo + (hi - lo) * np.random.default_rng(1).random(c.size)
+                for _ in range(2):
+                    g.scatter(c)
+    else:
+        raise SystemExit("unknown probe " + spec)
+    return {"probe": spec, "ok": True}
 
 
 def rudy_report(reps=5):
@@ -874,6 +937,7 @@ def main():
     ap.add_argument("--no-seed", action="store_true", help="skip the quadratic-seed solve report")
     ap.add_argument("--rudy-only", action="store_true", help="print only the RUDY demand report")
     ap.add_argument("--scatter-only", action="store_true", help="print only the density-scatter forms report")
+    ap.add_argument("--probe", default="", help="a small workload for profiler captures: tc:N or scatter:WORKLOAD")
     ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
     ap.add_argument("--clustering-only", action="store_true", help="print only the register-clustering report")
     args = ap.parse_args()
@@ -904,6 +968,9 @@ def main():
         if rank == 0:
             print(json.dumps({"metric": "tensor-core / FP32 / FP64 precision at 1M cells",
                               "precision": precision_report()}), flush=True)
+        return
+    if args.probe:
+        print(json.dumps(probe(args.probe)), flush=True)
         return
     if args.scatter_only:
         if rank == 0:
