@@ -386,6 +386,50 @@ int32_t texo_gp_optimize_round(texo_gp_handle h, const texo_gp_round* round, uin
                                double* out_coordinates, texo_gp_stats* stats, texo_gp_round_result* result);
 int32_t texo_gp_set_charges(texo_gp_handle h, const double* member_charge, const double* filler_charge);
 
+/* eplace::place with its routing_capacity and register_controls arguments
+ * (crates/texo-pnr/src/eplace.rs:242-420) in one call: area rounds that stop
+ * at AreaAdjustmentReady, each followed by propose_area_adjustment
+ * (eplace.rs:627-740: net bounding boxes at the unit origins, the RUDY map on
+ * the capacity grid, each movable member's utilization at its rounded
+ * position capped at sqrt(2), eq. 29 for LUT and register members, the
+ * register-clustering areas, adjust_instance_areas against the fillers); an
+ * adjustment that grows any kind is installed and the optimizer restarts
+ * with the area-reset multipliers and the first round's density scales;
+ * once the installed increase is below 1 % (or nothing grew) a last round
+ * runs to the final targets. The rounds run on the host engine whatever
+ * params->engine says. `capacity` NULL is texo_gp_place (the pure density
+ * objective). A register member whose cell has no control set, a cell with
+ * two, or more area rounds than area_adjustment_round_limit (eplace.rs:
+ * 584-626) return TEXO_GP_ERR_INVALID_NORMALIZATION like the reference.
+ * `out_targets_xy` [2U]: the last round's best rounded targets;
+ * `out_coordinates` [2(U+F)] (may be NULL): its final coordinates. */
+typedef struct texo_gp_routing_capacity {
+  uint32_t width, height;            /* RoutingCapacityMap (routing_demand.rs:22-27) */
+  const uint32_t* horizontal;        /* [height][width] channel capacities */
+  const uint32_t* vertical;          /* [height][width] */
+} texo_gp_routing_capacity;
+typedef struct texo_gp_register_control {   /* RegisterControlSet (lib.rs:2157-2164) */
+  uint32_t cell;
+  uint32_t reserved;
+  uint64_t clock_lsr[2];
+  uint64_t ce;
+} texo_gp_register_control;
+typedef struct texo_gp_routable_report {
+  uint32_t rounds;                   /* density rounds run */
+  uint32_t area_rounds;              /* adjustments installed */
+  uint64_t iterations;               /* eplace iterations over all rounds */
+  double last_relative_increase;     /* of the last proposal: total and largest per kind */
+  double last_maximum_relative_increase;
+  double max_horizontal_utilization; /* of the last proposal */
+  double max_vertical_utilization;
+  uint64_t last_members_inflated;
+  uint32_t reserved[8];
+} texo_gp_routable_report;
+int32_t texo_gp_place_routable(const texo_gp_problem* problem, const texo_gp_params* params,
+                               const texo_gp_routing_capacity* capacity, uint64_t num_register_controls,
+                               const texo_gp_register_control* register_controls, uint32_t* out_targets_xy,
+                               double* out_coordinates, texo_gp_stats* stats, texo_gp_routable_report* report);
+
 /* Per-stage device times: runs each stage of one full objective evaluation at
  * the handle's current coordinates `reps` times and writes the mean time of
  * one launch in milliseconds, measured with CUDA events on the handle's

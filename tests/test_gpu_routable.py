@@ -98,3 +98,56 @@ def test_routable_rounds_match_the_oracle():
         assert abs(fa.normalized_overflow - fb.normalized_overflow) <= 0.01
     h_got, h_ref = o.hpwl(c), o.hpwl(c_ref)
     assert abs(h_got - h_ref) <= 0.01 * h_ref
+
+
+def test_native_rounds_equal_the_python_composition():
+    """texo_gp_place_routable (the whole loop in one C-ABI call) against the
+    Python composition of the same rounds over the C-ABI pieces: both run the
+    same host-engine rounds and the same GPU proposals, so the rounds, the
+    iteration counts, the installed charges and the targets are identical."""
+    from texo_gb300.placer import place_with_routing_capacity
+    prob, ch, cv, ctl = routability_case()
+    t_py, c_py, info = R.place_routable(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
+                                        register_controls=ctl)
+    t, c, st, rep = place_with_routing_capacity(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
+                                                register_controls=ctl, coordinates=True)
+    assert rep["rounds"] == len(info["rounds"]) and rep["area_rounds"] == info["area_rounds"] >= 1
+    assert rep["iterations"] == info["iterations"] == st["iterations"]
+    assert rep["last_relative_increase"] == info["rounds"][-2]["relative_increase"]
+    assert np.array_equal(t, t_py)
+    assert np.array_equal(c, c_py)
+
+
+def test_native_rounds_errors():
+    from texo_gb300.placer import place_with_routing_capacity
+    prob, ch, cv, ctl = routability_case()
+    prm = default_params(best_effort=1, max_iterations=200)
+    # a register member without a control set (clustering_areas returns None)
+    partial = dict(list(ctl.items())[1:])
+    with pytest.raises(abi.TexoGpError) as e:
+        place_with_routing_capacity(prob, prm, ch, cv, register_controls=partial)
+    assert e.value.code == abi.CODE["INVALID_NORMALIZATION"]
+    with pytest.raises(abi.TexoGpError) as e:
+        R.place_routable(prob, prm, ch, cv, register_controls=partial)
+    assert e.value.code == abi.CODE["INVALID_NORMALIZATION"]
+    # an empty capacity map
+    with pytest.raises(abi.TexoGpError) as e:
+        place_with_routing_capacity(prob, prm, ch[:0], cv[:0], register_controls=ctl)
+    assert e.value.code == abi.CODE["INVALID_NORMALIZATION"]
+
+
+def test_native_without_capacity_is_place():
+    """No routing capacity: the pure density objective, texo_gp_place."""
+    from texo_gb300.placer import place
+    prob, _, _, _ = routability_case()
+    prm = default_params(best_effort=1, max_iterations=200)
+    lib = abi.load()
+    pc = prob.c_struct()
+    t = np.zeros(2 * prob.num_units, np.uint32)
+    st, rep = abi.Stats(), abi.RoutableReport()
+    import ctypes as C
+    code = lib.texo_gp_place_routable(C.byref(pc), C.byref(prm), None, 0, None, abi.ptr(t, C.c_uint32), None,
+                                      C.byref(st), C.byref(rep))
+    assert code == 0 and rep.rounds == 1
+    t_ref, _, s_ref = place(prob, default_params(best_effort=1, max_iterations=200))
+    assert np.array_equal(t.reshape(-1, 2), t_ref) and st.iterations == s_ref["iterations"]

@@ -122,6 +122,24 @@ class RoundResult(C.Structure):
                 ("density_scales", C.c_double * 4)]
 
 
+class RoutingCapacity(C.Structure):
+    """texo_gp_routing_capacity: RoutingCapacityMap's channel capacities."""
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("horizontal", C.POINTER(C.c_uint32)),
+                ("vertical", C.POINTER(C.c_uint32))]
+
+
+class RegisterControl(C.Structure):
+    """texo_gp_register_control: RegisterControlSet (cell, clock_lsr, ce)."""
+    _fields_ = [("cell", C.c_uint32), ("reserved", C.c_uint32), ("clock_lsr", C.c_uint64 * 2), ("ce", C.c_uint64)]
+
+
+class RoutableReport(C.Structure):
+    _fields_ = [("rounds", C.c_uint32), ("area_rounds", C.c_uint32), ("iterations", C.c_uint64),
+                ("last_relative_increase", C.c_double), ("last_maximum_relative_increase", C.c_double),
+                ("max_horizontal_utilization", C.c_double), ("max_vertical_utilization", C.c_double),
+                ("last_members_inflated", C.c_uint64), ("reserved", C.c_uint32 * 8)]
+
+
 class FieldEval(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
@@ -210,6 +228,9 @@ SIGNATURES = {
     "texo_gp_optimize_round": (C.c_int32, [_P, C.POINTER(Round), c_u32p, c_f64p, C.POINTER(Stats),
                                            C.POINTER(RoundResult)]),
     "texo_gp_set_charges": (C.c_int32, [_P, c_f64p, c_f64p]),
+    "texo_gp_place_routable": (C.c_int32, [C.POINTER(ProblemC), C.POINTER(Params), C.POINTER(RoutingCapacity),
+                                           C.c_uint64, C.POINTER(RegisterControl), c_u32p, c_f64p,
+                                           C.POINTER(Stats), C.POINTER(RoutableReport)]),
     "texo_gp_hpwl": (C.c_int32, [_P, c_f64p, c_f64p]),
     "texo_gp_trace": (C.c_int32, [_P, C.POINTER(Iteration), C.c_uint32, c_u32p]),
     "texo_gp_stage_times": (C.c_int32, [_P, C.c_uint32, c_f64p, C.c_uint32, c_u32p]),

@@ -53,6 +53,44 @@ def place(problem, params=None, coordinates=False):
     return targets.reshape(-1, 2), None, _stats_dict(st)
 
 
+def place_with_routing_capacity(problem, params, capacity_h, capacity_v, register_controls=None, coordinates=False):
+    """eplace::place with routing_capacity / register_controls
+    (eplace.rs:242-420) through texo_gp_place_routable: the area rounds, the
+    proposals and their installation in one native call. capacity_h /
+    capacity_v: [H, W] channel capacities; register_controls: cell ->
+    (clock, lsr, ce). Returns (targets [U, 2], coordinates or None, stats,
+    report dict)."""
+    lib = abi.load()
+    params = params or default_params()
+    pc = problem.c_struct()
+    ch = np.ascontiguousarray(capacity_h, dtype=np.uint32)
+    cv = np.ascontiguousarray(capacity_v, dtype=np.uint32)
+    if ch.ndim != 2 or ch.shape != cv.shape:
+        raise ValueError("capacity maps must be [H, W] and of one shape")
+    cap = abi.RoutingCapacity(ch.shape[1], ch.shape[0], abi.ptr(ch, C.c_uint32), abi.ptr(cv, C.c_uint32))
+    items = sorted((register_controls or {}).items())
+    ctl = (abi.RegisterControl * max(len(items), 1))()
+    for k, (cell, (clock, lsr, ce)) in enumerate(items):
+        ctl[k].cell = int(cell)
+        ctl[k].clock_lsr[0] = int(clock)
+        ctl[k].clock_lsr[1] = int(lsr)
+        ctl[k].ce = int(ce)
+    targets = np.zeros(2 * problem.num_units, np.uint32)
+    coords = None
+    if coordinates:
+        with Placer(problem, params) as h:
+            coords = np.zeros(h.n)
+    st = abi.Stats()
+    rep = abi.RoutableReport()
+    code = lib.texo_gp_place_routable(C.byref(pc), C.byref(params), C.byref(cap), len(items), ctl,
+                                      abi.ptr(targets, C.c_uint32),
+                                      abi.ptr(coords, C.c_double) if coords is not None else None, C.byref(st),
+                                      C.byref(rep))
+    abi.check(code, "texo_gp_place_routable")
+    report = {f: getattr(rep, f) for f, _ in abi.RoutableReport._fields_ if f != "reserved"}
+    return targets.reshape(-1, 2), coords, _stats_dict(st), report
+
+
 class Batch:
     """Many resident placements advanced together (texo_gp_batch)."""
 

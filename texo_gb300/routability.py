@@ -135,8 +135,13 @@ def kind_key(field):
 
 
 def _rounded(value, extent):
-    # rounded_coordinate (lib.rs:4566-4568): round half away from zero, clamp to the grid
-    r = np.where(value >= 0, np.floor(value + 0.5), np.ceil(value - 0.5))
+    # rounded_coordinate (lib.rs:4566-4568): round half away from zero (value
+    # - trunc(value) is exact, so no addition of 0.5 can round up), clamp to
+    # the grid; NaN goes to 0 like Rust's saturating cast
+    value = np.asarray(value, dtype=np.float64)
+    t = np.trunc(value)
+    r = t + np.where(np.abs(value - t) >= 0.5, np.sign(value), 0.0)
+    r = np.where(np.isnan(r), 0.0, r)
     return np.clip(r, 0, extent - 1).astype(np.int64)
 
 
@@ -205,6 +210,10 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
         is_reg = np.array([fields[f][0] == abi.KIND_REGISTER for f in field], dtype=bool)
         regs = np.nonzero(is_reg)[0]
         if len(regs):
+            missing = [int(c) for c in cells[regs] if int(c) not in register_controls]
+            if missing:   # clustering_areas returns None (register_clustering.rs:33)
+                raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"],
+                                      "propose_area_adjustment: register cell %d has no control set" % missing[0])
             ctl = np.array([register_controls[int(c)] for c in cells[regs]], dtype=np.uint64).reshape(-1, 3)
             cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
             count = int(np.sum(movable[cell_unit]))   # cells of movable units (movable_instance_count)
@@ -217,9 +226,11 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     for k, c, a in zip(keys.tolist(), charge, adj.member_areas):
         before[k] = before.get(k, 0.0) + c
         increase[k] = increase.get(k, 0.0) + (a - c)
-    total_before, total_increase = sum(before.values()), sum(increase.values())
+    # totals in ascending kind order, like the reference's BTreeMap sums
+    total_before = sum(before[k] for k in sorted(before))
+    total_increase = sum(increase[k] for k in sorted(increase))
     rel = total_increase / total_before if total_before else float("nan")
-    rel_max = max([increase[k] / b if b else float("nan") for k, b in before.items()], default=0.0)
+    rel_max = max([increase[k] / before[k] if before[k] else float("nan") for k in sorted(before)], default=0.0)
     if not (np.isfinite(rel) and np.isfinite(rel_max)):   # the reference's InvalidNormalization
         raise abi.TexoGpError(abi.CODE["INVALID_NORMALIZATION"], "propose_area_adjustment")
     metrics = {"maximum_horizontal_utilization": float(np.max(hu, initial=0.0)),
