@@ -108,3 +108,21 @@ def test_seed_solve_at_the_42k_workload():
         assert sg["stop"] == "residual" and sg["final_residual_squared"] <= sg["target_squared"]
         assert abs(sg["iterations"] - sr.iterations) <= 2
         assert np.max(np.abs(xg - xr)) <= 1e-8 * np.max(np.abs(xr))
+
+
+def test_seed_with_macros_and_timed_arcs_matches_the_oracle_path():
+    """The seed of a problem with two-member macros (offsets), fixed units and
+    timed arcs: solve_axis on the GPU against the same steps with the oracle's
+    solve, and the reference's own macro case (lib.rs:14975-15003)."""
+    from rich_problems import rich_problem
+    from test_seed_macros import macro_offsets_case, oracle_solver
+    prob = rich_problem(1)
+    pos = np.asarray(prob.initial_xy).reshape(-1, 2)
+    for axis, center in ((0, prob.width // 2), (1, prob.height // 2)):
+        xg, st = seed.solve_axis(prob, pos, axis, center)
+        xr, _ = seed.solve_axis(prob, pos, axis, center, solver=oracle_solver)
+        assert st["stop"] == "residual"
+        assert np.max(np.abs(xg - xr)) <= 1e-8 * np.max(np.abs(xr)), axis
+    prob = macro_offsets_case()
+    x, _ = seed.solve_axis(prob, np.array([[4.0, 0.0], [4.0, 0.0]]), 0, 4)
+    assert np.allclose(x, [2.5, 5.5], atol=1e-12, rtol=0)

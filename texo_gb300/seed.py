@@ -1,13 +1,18 @@
 """The coarse quadratic seed of Texo's analytical placer, per axis, on the GPU.
 
-Restates for single-cell units the host side of `solve_analytical_axis`
-(crates/texo-pnr/src/lib.rs:4410-4560): the bound-to-bound edges of every net
-at the current positions (`linearize_axis`, analytical_placement.rs:277-352,
-with `axis_bounds`, :793-815), the equations they give with fixed units
-anchored (`analytical_axis_equations`, lib.rs:4466-4528), the gauge of each
-floating component (`finalize_component_gauges`, lib.rs:4419-4460), and the
-recentering after the solve. The solve itself is `texo_gp_quadratic_solve`
+Restates the host side of `solve_analytical_axis` (crates/texo-pnr/src/
+lib.rs:4410-4560): the bound-to-bound edges of every net at the current
+positions and the timed arcs' overlay edges (`linearize_axis`,
+analytical_placement.rs:283-356, with `axis_bounds`, :793-815), the equations
+they give with fixed units anchored and macro members at their offsets from
+the unit origin (`analytical_axis_equations`, lib.rs:4464-4527), the gauge of
+each floating component (`finalize_component_gauges`, lib.rs:4419-4460), and
+the recentering after the solve. The solve itself is `texo_gp_quadratic_solve`
 (the GPU restatement of `solve_quadratic`, lib.rs:4586-4752).
+
+A unit is fixed when its bounds collapse (lower == upper, the problem's
+convention for a unit with one placement choice); its origin is then that
+point, and its cells sit at their fixed coordinates.
 """
 import numpy as np
 
@@ -30,19 +35,27 @@ def _axis_bounds(units, pos):
     return lower, upper
 
 
-def b2b_edges(problem, positions, axis):
-    """Bound-to-bound edges (left unit, right unit, weight) of every net at
-    `positions` ([U, 2] unit origins) along `axis` (0 = x, 1 = y), in the
-    reference's order: nets in order, pins in order, lower bound before upper."""
-    net_ptr = np.asarray(problem.net_ptr, dtype=np.int64)
-    pin_cell = np.asarray(problem.pin_cell, dtype=np.int64)
-    cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
+def _cell_coordinates(problem, positions, axis):
     fixed = np.asarray(problem.cell_fixed, dtype=bool)
     fixed_xy = np.asarray(problem.cell_fixed_xy, dtype=np.float64).reshape(-1, 2)
     offset_xy = np.asarray(problem.cell_offset_xy, dtype=np.float64).reshape(-1, 2)
+    cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
     pos = np.asarray(positions, dtype=np.float64).reshape(-1, 2)
-    coord = np.where(fixed, fixed_xy[:, axis], pos[cell_unit, axis] + offset_xy[:, axis])
-    left, right, weight = [], [], []
+    return np.where(fixed, fixed_xy[:, axis], pos[cell_unit, axis] + offset_xy[:, axis])
+
+
+def b2b_edges(problem, positions, axis, with_cells=False):
+    """Bound-to-bound edges (left unit, right unit, weight) of every net at
+    `positions` ([U, 2] unit origins) along `axis` (0 = x, 1 = y), in the
+    reference's order: nets in order, pins in order, lower bound before upper;
+    then one edge per timed arc whose driver and sink are on different units
+    (weight 64 * extra_weight / separation, analytical_placement.rs:331-352).
+    with_cells=True also returns the cells at the two ends."""
+    net_ptr = np.asarray(problem.net_ptr, dtype=np.int64)
+    pin_cell = np.asarray(problem.pin_cell, dtype=np.int64)
+    cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
+    coord = _cell_coordinates(problem, positions, axis)
+    left, right, lcell, rcell, weight = [], [], [], [], []
     for e in range(len(net_ptr) - 1):
         cells = pin_cell[net_ptr[e]:net_ptr[e + 1]]
         units = cell_unit[cells]
@@ -59,39 +72,64 @@ def b2b_edges(problem, positions, axis):
                 sep = max(abs(p[i] - p[b]), 1.0)
                 left.append(units[i])
                 right.append(units[b])
+                lcell.append(cells[i])
+                rcell.append(cells[b])
                 weight.append(PLACEMENT_WEIGHT_SCALE / (fanout * sep))
-    return np.array(left, np.int64), np.array(right, np.int64), np.array(weight)
+    drivers = np.asarray(problem.arc_driver_cell, dtype=np.int64).reshape(-1)
+    sinks = np.asarray(problem.arc_sink_cell, dtype=np.int64).reshape(-1)
+    extra = np.asarray(problem.arc_extra_weight, dtype=np.uint64).reshape(-1)
+    for a in range(len(drivers)):
+        dc, sc = int(drivers[a]), int(sinks[a])
+        if cell_unit[dc] == cell_unit[sc]:
+            continue
+        sep = max(abs(coord[dc] - coord[sc]), 1.0)
+        left.append(cell_unit[dc])
+        right.append(cell_unit[sc])
+        lcell.append(dc)
+        rcell.append(sc)
+        weight.append(PLACEMENT_WEIGHT_SCALE * float(extra[a]) / sep)
+    out = (np.array(left, np.int64), np.array(right, np.int64), np.array(weight))
+    if with_cells:
+        return out + (np.array(lcell, np.int64), np.array(rcell, np.int64))
+    return out
+
+
+def fixed_units(problem, axis):
+    """(fixed mask [U], origin coordinate along `axis` [U]) of the units."""
+    lower = np.asarray(problem.lower_xy, dtype=np.float64).reshape(-1, 2)
+    upper = np.asarray(problem.upper_xy, dtype=np.float64).reshape(-1, 2)
+    fixed = np.all(lower == upper, axis=1)
+    return fixed, np.where(fixed, lower[:, axis], 0.0)
 
 
 def axis_system(problem, positions, axis):
     """(diagonal, adjacency CSR (ptr, index, weight), rhs, anchored) of one
-    axis: a fixed unit holds its coordinate; an edge to a fixed unit adds to
-    the diagonal and the right-hand side; an edge between movable units adds
-    to both diagonals and to both adjacency rows (in edge order)."""
+    axis (`analytical_axis_equations`, lib.rs:4464-4527): a fixed unit holds
+    its origin; an edge to a fixed unit adds to the diagonal and adds
+    weight * (fixed cell's coordinate - own cell's offset) to the right-hand
+    side; an edge between movable units adds to both diagonals, to both
+    adjacency rows (in edge order) and weight * (other offset - own offset)
+    to each right-hand side."""
     U = problem.num_units
-    cell_unit = np.asarray(problem.cell_unit, dtype=np.int64)
-    fixed_cell = np.asarray(problem.cell_fixed, dtype=bool)
     fixed_xy = np.asarray(problem.cell_fixed_xy, dtype=np.float64).reshape(-1, 2)
-    unit_fixed = np.zeros(U, bool)
-    unit_coord = np.zeros(U)
-    unit_fixed[cell_unit[fixed_cell]] = True
-    unit_coord[cell_unit[fixed_cell]] = fixed_xy[fixed_cell, axis]
+    offset = np.asarray(problem.cell_offset_xy, dtype=np.float64).reshape(-1, 2)[:, axis]
+    unit_fixed, unit_coord = fixed_units(problem, axis)
     diag = np.where(unit_fixed, 1.0, 0.0)
     rhs = np.where(unit_fixed, unit_coord, 0.0)
     anchored = unit_fixed.copy()
-    l, r, w = b2b_edges(problem, positions, axis)
+    l, r, w, lc, rc = b2b_edges(problem, positions, axis, with_cells=True)
     rows, cols, ws = [], [], []
-    for a, b, x in zip(l.tolist(), r.tolist(), w.tolist()):
+    for a, b, x, ca, cb in zip(l.tolist(), r.tolist(), w.tolist(), lc.tolist(), rc.tolist()):
         fa, fb = unit_fixed[a], unit_fixed[b]
         if fa and fb:
             continue
         if fa:
             diag[b] += x
-            rhs[b] += x * unit_coord[a]
+            rhs[b] += x * (fixed_xy[ca, axis] - offset[cb])
             anchored[b] = True
         elif fb:
             diag[a] += x
-            rhs[a] += x * unit_coord[b]
+            rhs[a] += x * (fixed_xy[cb, axis] - offset[ca])
             anchored[a] = True
         else:
             diag[a] += x
@@ -99,6 +137,8 @@ def axis_system(problem, positions, axis):
             rows += [a, b]
             cols += [b, a]
             ws += [x, x]
+            rhs[a] += x * (offset[cb] - offset[ca])
+            rhs[b] += x * (offset[ca] - offset[cb])
     rows = np.array(rows, np.int64)
     order = np.argsort(rows, kind="stable")
     ptr = np.zeros(U + 1, np.int64)
@@ -136,17 +176,22 @@ def finalize_gauges(diag, ptr, index, weight, rhs, anchored):
     return diag, np.cumsum(new_ptr), index[keep], weight[keep], rhs, floating
 
 
-def solve_axis(problem, positions, axis, center, device=0):
+def solve_axis(problem, positions, axis, center, device=0, solver=None):
     """solve_analytical_axis (lib.rs:4531-4560) for one axis: the system at
     `positions`, the gauges, the GPU solve from the current coordinates (each
     floating component shifted so its gauge sits at 0), and each floating
-    component recentred on `center`. Returns (coordinates [U], solve stats)."""
+    component recentred on `center`. `solver(diag, ptr, index, weight, rhs,
+    x0) -> (x, stats)` replaces the GPU solve (a checker passes its own).
+    Returns (coordinates [U], solve stats)."""
     diag, ptr, index, weight, rhs, anchored = axis_system(problem, positions, axis)
     diag, ptr, index, weight, rhs, floating = finalize_gauges(diag, ptr, index, weight, rhs, anchored)
     x = np.asarray(positions, dtype=np.float64).reshape(-1, 2)[:, axis].copy()
     for comp in floating:
         x[comp] -= x[comp[0]]
-    x, stats = quadratic_solve(diag, ptr, index, weight, rhs, x, device=device)
+    if solver is None:
+        x, stats = quadratic_solve(diag, ptr, index, weight, rhs, x, device=device)
+    else:
+        x, stats = solver(diag, ptr, index, weight, rhs, x)
     for comp in floating:
         x[comp] += float(center) - x[comp].sum() / len(comp)
     return x, stats
