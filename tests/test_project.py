@@ -1,0 +1,130 @@
+"""`project` up to its repair (legalization/mod.rs:322-389) with the oracle's
+auctions: fixed units, shared-row families (disjoint ones auctioned,
+overlapping ones seeded nearest-first), singletons, on the reference's
+device fixture and on a seeded ECP5-like fabric.
+
+The composition is host code shared by both auction backends; the oracle's
+FIFO auction is the reference's, its parallel-round form the GPU's. Checked:
+the known answer on the fixture (worked by hand from the rules), every
+placed unit on free BELs with no BEL used twice, each family auction a
+maximum matching whose reduced costs pass the epsilon-complementary-slackness
+certificate, the overlapping seeding equal to a brute-force nearest free
+row, and the parallel-round form within the reference's cost bound of the
+FIFO's."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import ffi
+from texo_gb300 import abi, ecp5, legalize as L
+
+FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "minimal_ecp5.json")
+
+
+def oracle_auction(jacobi):
+    def run(grid, kinds, targets, scale):
+        code, a, _, st = ffi.auction_singletons(grid, kinds, targets, cost_scale=max(int(scale), 1), jacobi=jacobi)
+        assert code == 0, code
+        return a, st
+    return run
+
+
+def test_known_answer_on_the_fixture():
+    with open(FIXTURE) as f:
+        arch = ecp5.read_architecture(json.load(f))
+    luts = ecp5.single_cell_choices(arch, ecp5.LUT4)
+    units = [L.Unit([0, 1], ecp5.carry_chain_assignments(arch, 1)),
+             L.Unit([2, 3], ecp5.lut_ff_assignments(arch)),
+             L.Unit([4], luts, False),
+             L.Unit([5], [[4]], False),
+             L.Unit([6], [[7]], False)]
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    targets = [[0, 0]] * 5
+    for jacobi in (False, True):
+        pj = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1,
+                       auction=oracle_auction(jacobi))
+        # carry before LUT-FF (same scarcity and size, lower first cell):
+        # carry takes BELs 0-1; LUT-FF's first row needs BEL 0, so it takes
+        # row 1 (BELs 8, 10) at distance 1; the lone LUT takes BEL 2, the
+        # lowest free COMB on the target tile
+        assert list(pj.preferred) == [0, 1, 2, 0, 0]
+        assert list(pj.bels(units)) == [0, 1, 8, 10, 2, 4, 7]
+        assert pj.stats["disjoint_shared_families"] == 2 and pj.stats["fixed_units"] == 2
+
+
+def test_fixed_conflict_is_an_error():
+    units = [L.Unit([0], [[3]], False), L.Unit([1], [[3]], False)]
+    with pytest.raises(L.ProjectionError):
+        L.project(2, 2, [[0, 0], [1, 0], [0, 1], [1, 1]], units, [[0, 0], [0, 0]], auction=oracle_auction(False))
+
+
+def fabric_case(seed=0, side=16):
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(side, side))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, seed, luts=500, ffs=250, lut_ff_pairs=150,
+                                                   carry=((12, 4), (6, 6)), io=24)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    prm = abi.default_params_py()
+    prm.best_effort = 1
+    st, targets, _, _ = ffi.Oracle(prob, prm).place(threads=4)
+    assert st == 0
+    return arch, units, targets
+
+
+def brute_nearest(unit, targets_u, occupied, bel_xy):
+    best = None
+    for c, a in enumerate(unit.choices):
+        if occupied[np.asarray(a)].any():
+            continue
+        x, y = bel_xy[a[0]]
+        key = (abs(int(x) - int(targets_u[0])) + abs(int(y) - int(targets_u[1])), (int(x), int(y)), c)
+        best = key if best is None or key < best else best
+    return None if best is None else best[2]
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_projection_on_a_fabric(seed):
+    arch, units, targets = fabric_case(seed)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    res = {}
+    for name, jacobi in (("fifo", False), ("jacobi", True)):
+        pj = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(jacobi))
+        bels = pj.bels(units)
+        placed = bels[bels >= 0]
+        assert len(np.unique(placed)) == len(placed)                 # no BEL twice
+        assert pj.stats["relaxed_unmatched_units"] == 0 and np.all(pj.preferred >= 0)
+        assert pj.stats["overlapping_shared_units"] == 6 and pj.stats["disjoint_shared_families"] == 2
+        for u, unit in enumerate(units):                              # the choice is one of the unit's
+            assert list(bels[unit.cells]) == list(unit.choices[pj.preferred[u]])
+        res[name] = (pj, bels)
+    # the parallel rounds meet the reference's bound: total base cost within
+    # n (the bidder count, s = 1) of the FIFO's on every auctioned cohort
+    cost = {}
+    for name, (pj, _) in res.items():
+        d = 0
+        for u, unit in enumerate(units):
+            if len(unit.choices) > 1:
+                x, y = bel_xy[unit.choices[pj.preferred[u]][0]]
+                d += abs(int(x) - int(targets[u][0])) + abs(int(y) - int(targets[u][1]))
+        cost[name] = d
+    n = sum(1 for u in units if len(u.choices) > 1)
+    assert abs(cost["jacobi"] - cost["fifo"]) <= n
+
+
+def test_overlapping_seeding_is_nearest_free_row():
+    arch, units, targets = fabric_case(0)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    pj = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(False))
+    # replay: fixed units, then the overlapping units in the seeding order
+    occupied = np.zeros(len(bel_xy), bool)
+    for unit in units:
+        if len(unit.choices) == 1:
+            occupied[np.asarray(unit.choices[0])] = True
+    over = [u for u, unit in enumerate(units) if unit.is_shared() and len(unit.choices) > 1
+            and len(unit.cells) == 12]
+    over.sort(key=lambda u: (len(units[u].choices), -len(units[u].cells), units[u].cells[0]))
+    for u in over:
+        c = brute_nearest(units[u], targets[u], occupied, bel_xy)
+        assert pj.preferred[u] == c
+        occupied[np.asarray(units[u].choices[c])] = True

@@ -201,3 +201,259 @@ def project_singletons(problem, targets, cost_scale=0, device=0):
     bel = np.full(problem.num_units, -1, dtype=np.int64)
     bel[bidders] = result.assignment
     return bel, result, np.nonzero(movable & (members > 1))[0]
+
+
+# ---- project: fixed units, shared-row families and singletons ------------
+
+@dataclass
+class Unit:
+    """A placement unit (`PlacementUnit`): its cells and its choices, one BEL
+    per cell each. `shared` False is the reference's SingleCell choice table
+    (one cell, candidates in ascending BEL order), True a Shared table of
+    assignment rows; None picks Shared for multi-cell units. Units whose
+    `choices` are the same list object form one family, as units sharing an
+    Arc'd table do in the reference (`cache_key`, lib.rs:3756-3761)."""
+    cells: list
+    choices: list
+    shared: bool = None
+
+    def is_shared(self):
+        return len(self.cells) > 1 if self.shared is None else bool(self.shared)
+
+
+class ProjectionError(ValueError):
+    """PnrError::InvalidPlacement from `project` (the reason in the message)."""
+
+
+@dataclass
+class Projection:
+    """What `project` leaves for its repair: per unit the preferred choice
+    (-1 where none was found), per BEL whether it is taken, and the cohort
+    statistics (`ProjectionStats`, legalization/mod.rs)."""
+    preferred: np.ndarray
+    occupied: np.ndarray
+    stats: dict
+
+    def bels(self, units):
+        """BEL of every cell (-1 for cells of units without a choice)."""
+        n = 1 + max((c for u in units for c in u.cells), default=-1)
+        out = np.full(n, -1, dtype=np.int64)
+        for u, unit in enumerate(units):
+            if self.preferred[u] >= 0:
+                out[unit.cells] = unit.choices[int(self.preferred[u])]
+        return out
+
+
+def ring_coordinates(center, offset, extent):
+    """`ring_coordinates` (lib.rs:6814-6821): center - offset, then
+    center + offset (once for offset 0), inside [0, extent)."""
+    out = []
+    if center >= offset:
+        out.append(center - offset)
+    if offset != 0:
+        out.append(center + offset)
+    return [v for v in out if v < extent]
+
+
+def _by_point(bel_xy, width, height, choices):
+    """`SpatialChoiceIndex` (lib.rs:3774-3787): choice indices by the tile of
+    the choice's first BEL, ascending within a tile."""
+    by = [[] for _ in range(width * height)]
+    for i, a in enumerate(choices):
+        x, y = bel_xy[a[0]]
+        by[y * width + x].append(i)
+    return by
+
+
+def _nearest_direct_choice(unit, by_point, bel_xy, target, occupied, width, height):
+    """`nearest_direct_choice` (legalization/mod.rs:533-575): the least
+    (point, choice) with every BEL free on the first Manhattan ring around
+    the target that has one."""
+    tx, ty = int(target[0]), int(target[1])
+    for radius in range(0, width - 1 + height - 1 + 1):
+        best = None
+        for dy in range(radius + 1):
+            dx = radius - dy
+            for y in ring_coordinates(ty, dy, height):
+                for x in ring_coordinates(tx, dx, width):
+                    for c in by_point[y * width + x]:
+                        if not occupied[unit.choices[c]].any() and (best is None or ((x, y), c) < best):
+                            best = ((x, y), c)
+        if best is not None:
+            return best[1]
+    return None
+
+
+def _rows_disjoint(choices):
+    seen = set()
+    for a in choices:
+        for b in a:
+            if b in seen:
+                return False
+            seen.add(b)
+    return True
+
+
+def _object_grid(width, height, num_kinds, kind_by_point, num_objects, occupied):
+    """A SiteGrid whose objects of kind q at tile t are kind_by_point[q][t]."""
+    ptr = [0]
+    obj = []
+    for q in range(num_kinds):
+        for t in range(width * height):
+            obj += kind_by_point[q][t]
+            ptr.append(len(obj))
+    return SiteGrid(width, height, num_kinds, np.array(ptr, np.uint32), np.array(obj, np.uint32), num_objects,
+                    np.ascontiguousarray(occupied, dtype=np.uint8))
+
+
+def gpu_auction(grid, bidder_kind, targets, cost_scale):
+    """The object auction of `project` on the GPU: (assignment, stats)."""
+    r = auction_singletons(grid, bidder_kind, targets, cost_scale=cost_scale)
+    return r.assignment, r.stats
+
+
+def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
+    """`project` (legalization/mod.rs:322-389) up to its repair: the units'
+    choices from their rounded targets [U, 2], occupancy being the only
+    legality rule (BELs whose pin-wire or shared-resource rules fail are the
+    caller's to mark by leaving them out of the choices).
+
+    1. `install_fixed_units` (:391-430): one-choice units take their BELs; two
+       on one BEL is an error.
+    2. `classify_units` (:432-471): Shared tables form families (units by
+       first cell); a family whose rows are pairwise BEL-disjoint is auctioned,
+       the others' units are seeded; SingleCell units are singletons.
+    3. `seed_overlapping_units` (:473-531): by (choices, -cells, first cell),
+       each takes the nearest free row (`nearest_direct_choice`).
+    4. `auction_disjoint_families` (:577-655): families in scarcity order
+       (rows x other family's size, then larger units, then first cell), each
+       an auction whose objects are its free rows at the ring distance of the
+       row's first BEL.
+    5. `auction_singletons` (:657-677): one auction over every singleton,
+       objects the BELs of each distinct candidate table.
+
+    `bel_xy` [B, 2]: BEL tiles. `auction(grid, kinds, targets, cost_scale) ->
+    (assignment, stats)` runs the auctions (default: the GPU; a checker passes
+    the oracle's). Unmatched units keep -1 (the reference's repair, which
+    places them by transactional search, is not part of this library)."""
+    bel_xy = np.asarray(bel_xy, dtype=np.int64).reshape(-1, 2)
+    B = bel_xy.shape[0]
+    auction = auction or gpu_auction
+    U = len(units)
+    tg = np.asarray(targets, dtype=np.int64).reshape(-1, 2)
+    if tg.shape[0] != U:
+        raise ValueError("one target per unit")
+    occupied = np.zeros(B, dtype=bool)
+    preferred = np.full(U, -1, dtype=np.int64)
+    stats = {"fixed_units": 0, "overlapping_shared_families": 0, "overlapping_shared_units": 0,
+             "disjoint_shared_families": 0, "disjoint_shared_units": 0, "singleton_units": 0,
+             "relaxed_unmatched_units": 0, "bids": 0, "candidates_examined": 0}
+    for u, unit in enumerate(units):
+        if len(unit.choices) != 1:
+            continue
+        a = np.asarray(unit.choices[0], dtype=np.int64)
+        if occupied[a].any():
+            raise ProjectionError("fixed analytical placement assignments conflict")
+        occupied[a] = True
+        preferred[u] = 0
+        stats["fixed_units"] += 1
+    families, singletons = {}, []
+    for u, unit in enumerate(units):
+        if len(unit.choices) == 1:
+            continue
+        if unit.is_shared():
+            families.setdefault(id(unit.choices), []).append(u)
+        else:
+            singletons.append(u)
+    overlapping, disjoint = [], []
+    for fam in families.values():
+        fam.sort(key=lambda u: units[u].cells[0])
+        if _rows_disjoint(units[fam[0]].choices):
+            stats["disjoint_shared_families"] += 1
+            stats["disjoint_shared_units"] += len(fam)
+            disjoint.append(fam)
+        else:
+            stats["overlapping_shared_families"] += 1
+            stats["overlapping_shared_units"] += len(fam)
+            overlapping += fam
+    singletons.sort(key=lambda u: units[u].cells[0])
+    stats["singleton_units"] = len(singletons)
+    # 3. overlapping families: nearest free row, one unit at a time
+    overlapping.sort(key=lambda u: (len(units[u].choices), -len(units[u].cells), units[u].cells[0]))
+    index_cache = {}
+    for u in overlapping:
+        unit = units[u]
+        key = id(unit.choices)
+        if key not in index_cache:
+            index_cache[key] = _by_point(bel_xy, width, height, unit.choices)
+        c = _nearest_direct_choice(unit, index_cache[key], bel_xy, tg[u], occupied, width, height)
+        if c is None:
+            continue
+        preferred[u] = c
+        occupied[np.asarray(unit.choices[c], dtype=np.int64)] = True
+    # 4. disjoint families, scarcest first
+    import functools
+
+    def scarcity(a, b):
+        ua, ub = units[a[0]], units[b[0]]
+        la, lb = len(ua.choices) * len(b), len(ub.choices) * len(a)
+        if la != lb:
+            return -1 if la < lb else 1
+        if len(ua.cells) != len(ub.cells):
+            return -1 if len(ua.cells) > len(ub.cells) else 1
+        return -1 if ua.cells[0] < ub.cells[0] else (1 if ua.cells[0] > ub.cells[0] else 0)
+    disjoint.sort(key=functools.cmp_to_key(scarcity))
+
+    def record(bidders, assignment, to_choice):
+        for u, obj in zip(bidders, assignment):
+            if obj < 0:
+                stats["relaxed_unmatched_units"] += 1
+                continue
+            c = to_choice(u, int(obj))
+            a = np.asarray(units[u].choices[c], dtype=np.int64)
+            if occupied[a].any():
+                raise ProjectionError("capacity auction returned an occupied assignment")
+            preferred[u] = c
+            occupied[a] = True
+
+    def add_stats(st):
+        stats["bids"] += int(st.get("bids", 0))
+        stats["candidates_examined"] += int(st.get("candidates_examined", 0))
+
+    for fam in disjoint:
+        rows = units[fam[0]].choices
+        free = np.array([not occupied[np.asarray(a, dtype=np.int64)].any() for a in rows], dtype=np.uint8)
+        grid = _object_grid(width, height, 1, [_by_point(bel_xy, width, height, rows)], len(rows), 1 - free)
+        asg, st = auction(grid, np.zeros(len(fam), np.uint32), tg[fam].astype(np.uint32), cost_scale)
+        add_stats(st)
+        record(fam, asg, lambda u, obj: obj)
+    # 5. singletons: one auction, a kind per distinct candidate table
+    if singletons:
+        kind_of, tables = {}, []
+        for u in singletons:
+            key = id(units[u].choices)
+            if key not in kind_of:
+                kind_of[key] = len(tables)
+                tables.append(units[u].choices)
+        kb = []
+        for t in tables:
+            by = [[] for _ in range(width * height)]
+            for a in t:
+                x, y = bel_xy[a[0]]
+                by[y * width + x].append(int(a[0]))
+            kb.append([sorted(v) for v in by])
+        grid = _object_grid(width, height, len(tables), kb, B, occupied.astype(np.uint8))
+        kinds = np.array([kind_of[id(units[u].choices)] for u in singletons], np.uint32)
+        asg, st = auction(grid, kinds, tg[singletons].astype(np.uint32), cost_scale)
+        add_stats(st)
+        pos = {}
+
+        def to_choice(u, bel):
+            key = id(units[u].choices)
+            if key not in pos:
+                pos[key] = {int(a[0]): i for i, a in enumerate(units[u].choices)}
+            if bel not in pos[key]:
+                raise ProjectionError("auction returned a noncandidate BEL")
+            return pos[key][bel]
+        record(singletons, asg, to_choice)
+    return Projection(preferred, occupied, stats)
