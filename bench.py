@@ -26,7 +26,9 @@ DCT forms against FP64), `quadratic_seed` (the coarse seed's PCG solve) and
 single-BEL auction on the placement's targets) and `clustering` (the
 register-clustering areas). `--stage-report`, `--batch-only`,
 `--serve-only`, `--precision-only`, `--seed-only`, `--rudy-only`,
-`--auction-only` and `--clustering-only` print one of these alone.
+`--auction-only`, `--clustering-only` and `--ecp5-only` (the device-snapshot
+adapter, placement and projection on an ECP5-like fabric) print one of these
+alone.
 """
 import argparse
 import json
@@ -782,6 +784,74 @@ def auction_report(reps=5, workloads=("lfe5u-85-42k", "stress-1m")):
     return out
 
 
+def ecp5_report(side=104, seed=0):
+    """The path from a device snapshot to legal BEL choices on an ECP5-like
+    fabric of LFE5U-85 size (side x side tiles, 102^2 PLC tiles of 8 LUT4 +
+    8 FF: 83,232 LUTs; seeded synthetic snapshot and netlist, the real
+    device database being unavailable): the adapter (snapshot read, choice
+    generators, placement problem), the placement on the device engine, and
+    `project` with the GPU auctions against the same composition with the
+    oracle's one-bidder-at-a-time auctions (the reference's) on one host
+    core. Host glue (the composition itself) is timed apart from the
+    auctions."""
+    import numpy as np
+    from oracle import ffi
+    from texo_gb300 import ecp5, legalize
+    from texo_gb300.placer import default_params, place
+    t0 = time.perf_counter()
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(side, side))
+    t1 = time.perf_counter()
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, seed, luts=30000, ffs=12000, lut_ff_pairs=8000,
+                                                   carry=((400, 4), (100, 6)), io=300)
+    t2 = time.perf_counter()
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    t3 = time.perf_counter()
+    targets, _, st = place(prob, default_params(best_effort=1))
+    t4 = time.perf_counter()
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    timed = {"gpu": 0.0, "cpu": 0.0}
+
+    def gpu_auction(grid, k, tg, scale):
+        r = legalize.auction_singletons(grid, k, tg, cost_scale=scale)
+        timed["gpu"] += r.stats["elapsed_ms"]
+        return r.assignment, r.stats
+
+    def cpu_auction(grid, k, tg, scale):
+        c0 = time.perf_counter()
+        code, a, _, s = ffi.auction_singletons(grid, k, tg, cost_scale=max(int(scale), 1))
+        timed["cpu"] += 1000 * (time.perf_counter() - c0)
+        if code != 0:
+            raise RuntimeError("oracle auction status %d" % code)
+        return a, s
+    legalize.project(arch.width, arch.height, bel_xy, units, targets, auction=gpu_auction)   # warm-up
+    timed["gpu"] = 0.0
+    p0 = time.perf_counter()
+    g = legalize.project(arch.width, arch.height, bel_xy, units, targets, auction=gpu_auction)
+    p1 = time.perf_counter()
+    r = legalize.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=cpu_auction)
+    p2 = time.perf_counter()
+
+    def displacement(pj):
+        d = 0
+        for u, unit in enumerate(units):
+            if len(unit.choices) > 1 and pj.preferred[u] >= 0:
+                x, y = bel_xy[unit.choices[pj.preferred[u]][0]]
+                d += abs(int(x) - int(targets[u][0])) + abs(int(y) - int(targets[u][1]))
+        return d
+    bels = g.bels(units)
+    return {"fabric": "%dx%d" % (side, side), "bels": arch.num_bels, "cells": nc, "units": len(units),
+            "nets": prob.num_nets, "stats": g.stats,
+            "adapter_s": {"read_snapshot": t1 - t0, "design": t2 - t1, "placement_problem": t3 - t2},
+            "placement": {"wall_s": t4 - t3, "iterations": st["iterations"], "converged": st["converged"],
+                          "hpwl": st["hpwl"], "overflow": st["overflow"]},
+            "project_gpu": {"wall_s": p1 - p0, "auction_gpu_ms": timed["gpu"], "unplaced": int(np.sum(g.preferred < 0)),
+                            "legal": bool(len(np.unique(bels[bels >= 0])) == int(np.sum(bels >= 0))),
+                            "total_displacement": displacement(g)},
+            "project_reference_auctions": {"wall_s": p2 - p1, "auction_cpu_ms": timed["cpu"], "cores": 1,
+                                           "unplaced": int(np.sum(r.preferred < 0)),
+                                           "total_displacement": displacement(r)}}
+
+
 def clustering_report(reps=5):
     """elfPlace's register-clustering areas (`clustering_areas`,
     register_clustering.rs:17-80) for a synthetic register set: one register
@@ -940,6 +1010,8 @@ def main():
     ap.add_argument("--probe", default="", help="a small workload for profiler captures: tc:N or scatter:WORKLOAD")
     ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
     ap.add_argument("--clustering-only", action="store_true", help="print only the register-clustering report")
+    ap.add_argument("--ecp5-only", action="store_true",
+                    help="print only the device-snapshot-to-legal-choices report on an ECP5-like fabric")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -983,6 +1055,10 @@ def main():
     if args.clustering_only:
         if rank == 0:
             print(json.dumps({"metric": "register clustering areas", "clustering": clustering_report()}), flush=True)
+        return
+    if args.ecp5_only:
+        if rank == 0:
+            print(json.dumps({"metric": "ECP5 device path", "ecp5": ecp5_report()}), flush=True)
         return
     if args.auction_only:
         if rank == 0:

@@ -360,9 +360,13 @@ def placement_problem(arch, num_cells, units, nets, cell_kind=None, initial_xy=N
     init = np.zeros((U, 2))
     centre = (float(W // 2), float(H // 2))
     bounds_of = {}      # choice_bounds per choice table
+    checked = set()     # (choice table, cells) shapes already validated
     for u, unit in enumerate(units):
-        if not unit.choices or any(len(a) != len(unit.cells) for a in unit.choices):
-            raise ValueError("unit %d: every choice assigns one BEL per cell" % u)
+        shape = (id(unit.choices), len(unit.cells))
+        if shape not in checked:
+            if not unit.choices or any(len(a) != len(unit.cells) for a in unit.choices):
+                raise ValueError("unit %d: every choice assigns one BEL per cell" % u)
+            checked.add(shape)
         first = unit.choices[0]
         ox, oy = arch.point(first[0])
         for c, b in zip(unit.cells, first):

@@ -258,11 +258,11 @@ def ring_coordinates(center, offset, extent):
 def _by_point(bel_xy, width, height, choices):
     """`SpatialChoiceIndex` (lib.rs:3774-3787): choice indices by the tile of
     the choice's first BEL, ascending within a tile."""
-    by = [[] for _ in range(width * height)]
-    for i, a in enumerate(choices):
-        x, y = bel_xy[a[0]]
-        by[y * width + x].append(i)
-    return by
+    first = np.fromiter((a[0] for a in choices), dtype=np.int64, count=len(choices))
+    tile = bel_xy[first, 1] * width + bel_xy[first, 0]
+    order = np.argsort(tile, kind="stable")
+    ends = np.searchsorted(tile[order], np.arange(1, width * height + 1))
+    return [v.tolist() for v in np.split(order, ends[:-1])]
 
 
 def _nearest_direct_choice(unit, by_point, bel_xy, target, occupied, width, height):
@@ -296,14 +296,11 @@ def _rows_disjoint(choices):
 
 def _object_grid(width, height, num_kinds, kind_by_point, num_objects, occupied):
     """A SiteGrid whose objects of kind q at tile t are kind_by_point[q][t]."""
-    ptr = [0]
-    obj = []
-    for q in range(num_kinds):
-        for t in range(width * height):
-            obj += kind_by_point[q][t]
-            ptr.append(len(obj))
-    return SiteGrid(width, height, num_kinds, np.array(ptr, np.uint32), np.array(obj, np.uint32), num_objects,
-                    np.ascontiguousarray(occupied, dtype=np.uint8))
+    lists = [v for q in range(num_kinds) for v in kind_by_point[q]]
+    ptr = np.zeros(len(lists) + 1, np.uint32)
+    ptr[1:] = np.cumsum([len(v) for v in lists])
+    obj = np.fromiter((o for v in lists for o in v), dtype=np.uint32, count=int(ptr[-1]))
+    return SiteGrid(width, height, num_kinds, ptr, obj, num_objects, np.ascontiguousarray(occupied, dtype=np.uint8))
 
 
 def gpu_auction(grid, bidder_kind, targets, cost_scale):
@@ -437,11 +434,8 @@ def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
                 tables.append(units[u].choices)
         kb = []
         for t in tables:
-            by = [[] for _ in range(width * height)]
-            for a in t:
-                x, y = bel_xy[a[0]]
-                by[y * width + x].append(int(a[0]))
-            kb.append([sorted(v) for v in by])
+            first = np.fromiter((a[0] for a in t), dtype=np.int64, count=len(t))
+            kb.append([sorted(first[v].tolist()) for v in _by_point(bel_xy, width, height, t)])
         grid = _object_grid(width, height, len(tables), kb, B, occupied.astype(np.uint8))
         kinds = np.array([kind_of[id(units[u].choices)] for u in singletons], np.uint32)
         asg, st = auction(grid, kinds, tg[singletons].astype(np.uint32), cost_scale)
