@@ -2,8 +2,9 @@
 //
 // Each admitted job is a device-engine handle with its own buffers, its own
 // controller state and its own barrier. `advance` gives every resident job a
-// share of the GPU's co-resident blocks (proportional to its virtual block
-// count) and runs all of them in one cooperative launch of k_batch; jobs run
+// share of the GPU's co-resident blocks (by its estimated work per iteration,
+// up to its virtual block count) and runs all of them in one cooperative
+// launch of k_batch; jobs run
 // independently inside it, each over its own physical blocks. A job's results
 // do not depend on how many physical blocks it got, so they are bit-identical
 // to the same job placed alone. When the resident set repeats from one advance
@@ -26,6 +27,7 @@ struct Job {
   texo_gp_handle h = nullptr;
   uint64_t bytes = 0;
   int V = 1;
+  uint64_t W = 1;   // estimated work per iteration
 };
 
 }  // namespace
@@ -136,6 +138,7 @@ int32_t texo_gp_batch_admit(texo_gp_batch b, const texo_gp_problem* problem, con
   j.h = h;
   j.bytes = bytes;
   j.V = handle_virtual_blocks(h);
+  j.W = std::max<uint64_t>(handle_work(h), 1);
   b->used += bytes;
   b->resident.push_back(j);
   if (out_slot) *out_slot = (uint32_t)(b->resident.size() - 1);
@@ -156,6 +159,7 @@ int32_t batch_add_handle(texo_gp_batch b, texo_gp_handle h, uint64_t job_id) {
   j.h = h;
   j.bytes = handle_bytes(h);
   j.V = handle_virtual_blocks(h);
+  j.W = std::max<uint64_t>(handle_work(h), 1);
   b->used += j.bytes;
   b->resident.push_back(j);
   return TEXO_GP_OK;
@@ -177,8 +181,10 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
   b->rr = (b->rr + n) % std::max<size_t>(nres, 1);
   std::vector<char> lg(n, 0);
   // Block maps of the (at most two) launches: one per DCT tile family (a job
-  // runs the same kernel instantiation as it does alone); physical blocks
-  // proportional to virtual blocks, at least one each.
+  // runs the same kernel instantiation as it does alone). Every job gets one
+  // physical block, the rest go by estimated work per iteration, so that the
+  // jobs' iterations take about as long as one another, and no job gets more
+  // than its virtual blocks (blocks a capped job cannot use go to the others).
   auto block_map = [&](int fam, std::vector<int4>& map) {
     std::vector<size_t> jobs;
     for (size_t i = 0; i < n; ++i)
@@ -186,16 +192,30 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
     map.clear();
     if (jobs.empty()) return;
     const int nj = (int)jobs.size();
-    long long vsum = 0;
-    for (size_t i : jobs) vsum += b->resident[pick[i]].V;
-    int used = nj;
-    for (size_t i : jobs) {
-      const int V = b->resident[pick[i]].V;
-      const int want = std::max(1, (int)((long long)(P - nj) * V / std::max(vsum, 1ll)) + 1);
-      const int add = std::max(0, std::min(std::min(want, V) - 1, P - used));
-      used += add;
-      for (int k = 0; k < 1 + add; ++k) map.push_back(make_int4((int)i, k, 1 + add, 0));
+    std::vector<int> give(nj, 1);
+    std::vector<char> full(nj, 0);
+    int left = std::max(0, P - nj);
+    for (int pass = 0; pass < 8 && left > 0; ++pass) {
+      double wsum = 0.0;
+      for (int k = 0; k < nj; ++k)
+        if (!full[k]) wsum += (double)b->resident[pick[jobs[k]]].W;
+      if (wsum <= 0.0) break;
+      int handed = 0;
+      for (int k = 0; k < nj; ++k) {
+        if (full[k]) continue;
+        const Job& jb = b->resident[pick[jobs[k]]];
+        int add = (int)((double)left * (double)jb.W / wsum);
+        if (pass > 0 && add == 0 && handed < left) add = 1;   // spread what rounding left over
+        add = std::min(add, std::min(jb.V - give[k], left - handed));
+        give[k] += add;
+        handed += add;
+        if (give[k] >= jb.V) full[k] = 1;
+      }
+      left -= handed;
+      if (handed == 0) break;
     }
+    for (int k = 0; k < nj; ++k)
+      for (int q = 0; q < give[k]; ++q) map.push_back(make_int4((int)jobs[k], q, give[k], 0));
   };
   int32_t s = TEXO_GP_OK;
   bool graphed = false;

@@ -1421,6 +1421,10 @@ int32_t batch_absorb(texo_gp_handle_s* h) { return h->ctl->absorb_devrun(); }
 bool handle_finished(texo_gp_handle_s* h) { return h->ctl->phase == 2; }
 uint64_t handle_bytes(texo_gp_handle_s* h) { return h->inst->bytes; }
 int handle_virtual_blocks(texo_gp_handle_s* h) { return h->inst->nvb; }
+uint64_t handle_work(texo_gp_handle_s* h) {
+  const HostModel& m = h->inst->m;
+  return (uint64_t)m.U + m.F + m.Mm + m.pin_unit.size() + 2ull * m.K * m.bins();
+}
 int handle_sms(texo_gp_handle_s* h) { return h->inst->sms; }
 Instance* handle_instance(texo_gp_handle_s* h) { return h->inst.get(); }
 int32_t handle_build(const texo_gp_problem* p, const texo_gp_params* prm, texo_gp_handle_s** out,

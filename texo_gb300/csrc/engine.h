@@ -115,6 +115,9 @@ int32_t batch_absorb(texo_gp_handle_s* h);
 bool handle_finished(texo_gp_handle_s* h);
 uint64_t handle_bytes(texo_gp_handle_s* h);
 int handle_virtual_blocks(texo_gp_handle_s* h);
+// Elements one iteration of the instance touches (objects, members, pins,
+// bins per field, the transform counted twice): its share of a batch.
+uint64_t handle_work(texo_gp_handle_s* h);
 int handle_sms(texo_gp_handle_s* h);
 Instance* handle_instance(texo_gp_handle_s* h);
 // texo_gp_create in two steps: the host model (no device work), then the
