@@ -810,10 +810,14 @@ def ecp5_report(side=104, seed=0):
     t4 = time.perf_counter()
     bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
     timed = {"gpu": 0.0, "cpu": 0.0}
+    calls = []
 
     def gpu_auction(grid, k, tg, scale):
         r = legalize.auction_singletons(grid, k, tg, cost_scale=scale)
         timed["gpu"] += r.stats["elapsed_ms"]
+        calls.append({"bidders": int(len(k)), "objects": int(grid.num_objects), "kinds": int(grid.num_kinds),
+                      **{f: r.stats[f] for f in ("cost_scale", "rounds", "tail_rounds", "bids", "elapsed_ms",
+                                                 "total_base_cost", "unmatched")}})
         return r.assignment, r.stats
 
     def cpu_auction(grid, k, tg, scale):
@@ -825,9 +829,18 @@ def ecp5_report(side=104, seed=0):
         return a, s
     legalize.project(arch.width, arch.height, bel_xy, units, targets, auction=gpu_auction)   # warm-up
     timed["gpu"] = 0.0
+    calls.clear()
     p0 = time.perf_counter()
     g = legalize.project(arch.width, arch.height, bel_xy, units, targets, auction=gpu_auction)
     p1 = time.perf_counter()
+    calls_default = list(calls)
+    gpu_default_ms = timed["gpu"]
+    calls.clear()
+    timed["gpu"] = 0.0
+    g1 = legalize.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=gpu_auction)
+    calls_s1 = list(calls)
+    gpu_s1_ms = timed["gpu"]
+    p1b = time.perf_counter()
     r = legalize.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=cpu_auction)
     p2 = time.perf_counter()
 
@@ -844,10 +857,12 @@ def ecp5_report(side=104, seed=0):
             "adapter_s": {"read_snapshot": t1 - t0, "design": t2 - t1, "placement_problem": t3 - t2},
             "placement": {"wall_s": t4 - t3, "iterations": st["iterations"], "converged": st["converged"],
                           "hpwl": st["hpwl"], "overflow": st["overflow"]},
-            "project_gpu": {"wall_s": p1 - p0, "auction_gpu_ms": timed["gpu"], "unplaced": int(np.sum(g.preferred < 0)),
+            "project_gpu": {"wall_s": p1 - p0, "auction_gpu_ms": gpu_default_ms, "unplaced": int(np.sum(g.preferred < 0)),
                             "legal": bool(len(np.unique(bels[bels >= 0])) == int(np.sum(bels >= 0))),
-                            "total_displacement": displacement(g)},
-            "project_reference_auctions": {"wall_s": p2 - p1, "auction_cpu_ms": timed["cpu"], "cores": 1,
+                            "total_displacement": displacement(g), "auctions": calls_default},
+            "project_gpu_reference_scale": {"auction_gpu_ms": gpu_s1_ms, "total_displacement": displacement(g1),
+                                            "auctions": calls_s1},
+            "project_reference_auctions": {"wall_s": p2 - p1b, "auction_cpu_ms": timed["cpu"], "cores": 1,
                                            "unplaced": int(np.sum(r.preferred < 0)),
                                            "total_displacement": displacement(r)}}
 

@@ -692,11 +692,14 @@ int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t num_registers
  * staying one (the reference's `cost_scale`, auction.rs:142, fixed there at
  * 1): the dummy becomes D = n * s * max_base_cost + n + 1 and the total base
  * cost is at most n / s above the least one of the maximum cardinality.
- * s = 1 is the reference's setting. 0 picks the largest of 8, 4, 2, 1 whose
+ * s = 1 is the reference's setting. 0 picks the largest of 4, 2, 1 whose
  * price range fits when every bidder is sure to be matched (the BEL grid
  * below with at least as many free BELs of each kind as bidders of that
- * kind), else 1: bidders left over leave only once prices pass D, about one
- * price step a round, and D grows with s. On placement targets the scaled
+ * kind) and every kind with bidders holds at most two BELs a tile on
+ * average, else 1: bidders left over leave only once prices pass D, about
+ * one price step a round, and D grows with s; with many BELs a tile a
+ * displaced bidder moves a ring out only after s price steps on each of
+ * them. On placement targets the scaled
  * auction lands within a fraction of a percent of the optimum for about a
  * quarter more bids; the reference's setting lands about 12 % above it.
  * Explicit domains take 1 for 0 (whether every bidder can be matched is not

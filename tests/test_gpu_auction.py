@@ -15,13 +15,20 @@ pytestmark = pytest.mark.gpu
 
 
 def expected_scale(grid, kind):
-    """The automatic scale: 8 unless some kind has more bidders than free BELs."""
+    """The automatic scale: 4 unless some kind has more bidders than free
+    BELs, or a kind with bidders more than two BELs a tile on average."""
     where = grid.bel_tiles()
     free = np.ones(grid.num_objects, bool) if grid.occupied is None else grid.occupied == 0
+    tiles = grid.width * grid.height
+    counts = np.diff(np.asarray(grid.tile_ptr, dtype=np.int64))
     for q in range(grid.num_kinds):
-        if (np.asarray(kind) == q).sum() > (free & (where[:, 0] == q)).sum():
+        nq = (np.asarray(kind) == q).sum()
+        if nq > (free & (where[:, 0] == q)).sum():
             return 1
-    return 8
+        c = counts[q * tiles:(q + 1) * tiles]
+        if nq and c.sum() > 2 * np.count_nonzero(c):
+            return 1
+    return 4
 
 
 def _raises(code, fn, *args):
@@ -211,7 +218,7 @@ def test_singletons_on_the_42k_placement():
         assert code == 0 and np.array_equal(r.assignment, ja) and np.array_equal(r.prices.astype(np.uint64), jp)
         assert (r.stats["rounds"], r.stats["bids"]) == (jst["rounds"], jst["bids"])
     # the default (scaled) result moves the units less than the reference's setting does
-    assert r.stats["cost_scale"] == 8 and r.stats["total_base_cost"] <= ost["total_base_cost"]
+    assert r.stats["cost_scale"] == 4 and r.stats["total_base_cost"] <= ost["total_base_cost"]
 
 
 def test_project_singletons_on_a_problem_with_fixed_bels():

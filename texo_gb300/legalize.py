@@ -61,7 +61,8 @@ def _u32(a):
 def assign_implicitly(domains, object_count, max_base_cost, cost_scale=0, device=0):
     """`assign_implicitly` with `explicit_best_two` (auction.rs:253-272):
     `domains[b]` is bidder b's list of (object, base cost); `cost_scale` 1 is
-    the reference's setting, 0 the largest of 8, 4, 2, 1 that fits. Raises
+    the reference's setting, 0 the largest of 4, 2, 1 that fits (explicit
+    domains: 1). Raises
     TexoGpError with AUCTION_RANGE (ArithmeticOverflow), AUCTION_OBJECT_RANGE,
     AUCTION_COST_RANGE or AUCTION_DUPLICATE_OBJECT like the reference's
     AuctionError."""
