@@ -42,3 +42,31 @@ def test_device_snapshot_to_legal_choices_on_the_gpu():
     assert len(np.unique(bels)) == len(bels)
     for u, unit in enumerate(units):
         assert list(bels[unit.cells]) == list(unit.choices[pj.preferred[u]])
+
+
+def test_gpu_edge_cases_equal_the_parallel_restatement():
+    """Capacity shortage (unmatched units), rows blocked by fixed BELs,
+    several candidate tables in one singleton auction: the GPU composition
+    gives the oracle's parallel-round composition's choices."""
+    from test_project import grid_bels
+    cases = []
+    table = [[b] for b in range(4)]
+    cases.append((2, 2, grid_bels(2, 2), [L.Unit([u], table, False) for u in range(6)], [[0, 0]] * 6))
+    rows = [[0, 1], [2, 3], [4, 5], [6, 7]]
+    cases.append((4, 1, grid_bels(4, 1, 2), [L.Unit([0], [[1]], False), L.Unit([1], [[2]], False),
+                                             L.Unit([2, 3], rows), L.Unit([4, 5], rows), L.Unit([6, 7], rows)],
+                  [[0, 0]] * 5))
+    lut = [[b] for b in range(0, 18, 2)]
+    ff = [[b] for b in range(1, 18, 2)]
+    cases.append((3, 3, grid_bels(3, 3, 2), [L.Unit([u], lut if u % 2 else ff, False) for u in range(12)],
+                  [[1, 1]] * 12))
+    for w, h, bel_xy, units, targets in cases:
+        g = L.project(w, h, bel_xy, units, targets, cost_scale=1)
+        o = L.project(w, h, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(True))
+        assert np.array_equal(g.preferred, o.preferred), (w, h)
+        assert g.stats["relaxed_unmatched_units"] == o.stats["relaxed_unmatched_units"]
+        # the automatic scale: same unmatched count, no BEL twice
+        a = L.project(w, h, bel_xy, units, targets)
+        bels = a.bels(units)
+        assert a.stats["relaxed_unmatched_units"] == o.stats["relaxed_unmatched_units"]
+        assert len(np.unique(bels[bels >= 0])) == int(np.sum(bels >= 0))

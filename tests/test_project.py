@@ -128,3 +128,58 @@ def test_overlapping_seeding_is_nearest_free_row():
         c = brute_nearest(units[u], targets[u], occupied, bel_xy)
         assert pj.preferred[u] == c
         occupied[np.asarray(units[u].choices[c])] = True
+
+
+def grid_bels(w, h, per_tile=1):
+    """BEL tiles of a w x h grid with `per_tile` BELs a tile, row-major."""
+    return np.array([(x, y) for y in range(h) for x in range(w) for _ in range(per_tile)], np.int64)
+
+
+@pytest.mark.parametrize("jacobi", [False, True])
+def test_capacity_shortage_leaves_units_unmatched(jacobi):
+    # 6 singleton units for 4 BELs: two go unmatched (the repair's), the rest
+    # on distinct BELs
+    bel_xy = grid_bels(2, 2)
+    table = [[b] for b in range(4)]
+    units = [L.Unit([u], table, False) for u in range(6)]
+    pj = L.project(2, 2, bel_xy, units, [[0, 0]] * 6, cost_scale=1, auction=oracle_auction(jacobi))
+    assert pj.stats["relaxed_unmatched_units"] == 2 and int(np.sum(pj.preferred < 0)) == 2
+    placed = [table[c][0] for c in pj.preferred if c >= 0]
+    assert sorted(placed) == [0, 1, 2, 3]
+
+
+def test_family_rows_blocked_by_fixed_units():
+    # a disjoint family of two-BEL rows whose every row touches a fixed BEL
+    bel_xy = grid_bels(4, 1, 2)           # BELs 2x, 2x+1 on tile x
+    rows = [[0, 1], [2, 3], [4, 5], [6, 7]]
+    units = [L.Unit([0], [[1]], False), L.Unit([1], [[2]], False), L.Unit([2], [[5]], False),
+             L.Unit([3], [[7]], False), L.Unit([4, 5], rows), L.Unit([6, 7], rows)]
+    pj = L.project(4, 1, bel_xy, units, [[0, 0]] * 6, cost_scale=1, auction=oracle_auction(False))
+    assert list(pj.preferred[:4]) == [0, 0, 0, 0]
+    assert list(pj.preferred[4:]) == [-1, -1] and pj.stats["relaxed_unmatched_units"] == 2
+
+
+def test_overlapping_seed_skips_a_blocked_row():
+    # overlapping rows (sliding windows of two tiles); the nearest row to the
+    # target holds a fixed BEL, so the unit takes the next ring's least point
+    bel_xy = grid_bels(5, 1)
+    rows = [[x, x + 1] for x in range(4)]     # rows overlap: BEL x+1 in two rows
+    units = [L.Unit([0], [[2]], False), L.Unit([1, 2], rows)]
+    pj = L.project(5, 1, bel_xy, units, [[0, 0], [2, 0]], cost_scale=1, auction=oracle_auction(False))
+    # rows at x = 1 and 2 use BEL 2; at distance 1 from x = 2: rows 1 (blocked) and 3
+    assert pj.preferred[1] == 3 and pj.stats["overlapping_shared_units"] == 1
+
+
+def test_singletons_of_several_candidate_tables():
+    # two kinds of singleton with their own candidate tables on one grid, one
+    # auction: every unit on a BEL of its own table
+    bel_xy = grid_bels(3, 3, 2)
+    lut = [[b] for b in range(0, 18, 2)]
+    ff = [[b] for b in range(1, 18, 2)]
+    units = [L.Unit([u], lut if u % 2 else ff, False) for u in range(12)]
+    targets = [[1, 1]] * 12
+    for jacobi in (False, True):
+        pj = L.project(3, 3, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(jacobi))
+        bels = pj.bels(units)
+        assert np.all(bels >= 0) and len(set(bels.tolist())) == 12
+        assert all((b % 2 == 0) == (u % 2 == 1) for u, b in enumerate(bels))

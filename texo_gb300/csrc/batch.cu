@@ -11,6 +11,7 @@
 // to the next, the whole advance (state copies in, launches, state copies
 // out) is captured once as a CUDA graph and replayed.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -21,6 +22,10 @@
 
 namespace {
 using namespace tgp;
+
+// A job's weight in the share of physical blocks: its estimated work per
+// iteration.
+inline double share_weight(uint64_t work) { return (double)work; }
 
 struct Job {
   uint64_t id = 0;
@@ -198,13 +203,13 @@ int32_t texo_gp_batch_advance(texo_gp_batch b, uint32_t iterations) {
     for (int pass = 0; pass < 8 && left > 0; ++pass) {
       double wsum = 0.0;
       for (int k = 0; k < nj; ++k)
-        if (!full[k]) wsum += (double)b->resident[pick[jobs[k]]].W;
+        if (!full[k]) wsum += share_weight(b->resident[pick[jobs[k]]].W);
       if (wsum <= 0.0) break;
       int handed = 0;
       for (int k = 0; k < nj; ++k) {
         if (full[k]) continue;
         const Job& jb = b->resident[pick[jobs[k]]];
-        int add = (int)((double)left * (double)jb.W / wsum);
+        int add = (int)((double)left * share_weight(jb.W) / wsum);
         if (pass > 0 && add == 0 && handed < left) add = 1;   // spread what rounding left over
         add = std::min(add, std::min(jb.V - give[k], left - handed));
         give[k] += add;
