@@ -97,7 +97,10 @@ typedef enum texo_gp_status {
   TEXO_GP_ERR_INSTANCE_AREA_MEMBER = 115,       /* InvalidMemberArea { member } (error_index) */
   TEXO_GP_ERR_INSTANCE_AREA_FILLER = 116,       /* InvalidFillerArea { filler } (error_index) */
   TEXO_GP_ERR_INSTANCE_AREA_POSTCONDITION = 117,/* PostconditionViolation */
-  TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW = 118      /* ArithmeticOverflow */
+  TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW = 118,     /* ArithmeticOverflow */
+  /* PnrError::InvalidPlacement of `project` (legalization/mod.rs:391-430,
+   * 679-722): fixed units on one BEL, or an auction result on a taken BEL */
+  TEXO_GP_ERR_PROJECTION_CONFLICT = 119
 } texo_gp_status;
 
 /* Resource kinds in the reference's `ResourceKind` order
@@ -752,6 +755,48 @@ int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, uint32_t heig
                                    const uint8_t* occupied, uint32_t num_bidders, const uint32_t* bidder_kind,
                                    const uint32_t* target_xy, uint32_t cost_scale, int32_t* assignment,
                                    uint32_t* prices, texo_gp_auction_stats* stats);
+
+/* ---- legalization: `project` up to its repair ---------------------------
+ * `project` (crates/texo-pnr/src/legalization/mod.rs:322-389) before
+ * `repair_relaxed`: the preferred choice of every unit from its rounded
+ * target. BELs are 0..num_bels-1 at tiles bel_xy[2b], bel_xy[2b+1]. Unit u
+ * chooses among the rows of tables[unit_table[u]] (one BEL per cell of the
+ * unit); unit_first_cell[u] is its first cell id, the reference's order key.
+ * A table with one row is a fixed unit's (its BELs are taken first; two
+ * fixed units on one BEL is TEXO_GP_ERR_PROJECTION_CONFLICT, the reference's
+ * "fixed analytical placement assignments conflict"). Units of one `shared`
+ * table form a family: pairwise BEL-disjoint rows are auctioned (families
+ * scarcest first: rows x the other family's units, then wider rows, then
+ * first cell), other families' units are seeded one at a time (fewest rows,
+ * widest, first cell) on the least (point, row) free on the first Manhattan
+ * ring around the target that has one. Non-shared tables (SingleCell
+ * candidates, width 1, ascending BEL ids) are one auction, a kind per table.
+ * A row is free when none of its BELs is taken; occupancy is the only
+ * legality rule. Auctions run on the GPU (texo_gp_auction_singletons, cost
+ * scale `cost_scale`, 0 automatic). out_choice[u]: the chosen row, or -1
+ * when the unit was left unmatched (the repair's). */
+typedef struct texo_gp_choice_table {
+  uint32_t num_choices;          /* rows */
+  uint32_t width;                /* BELs a row: the cells of the units using it */
+  const uint32_t* bels;          /* [num_choices][width] */
+  int32_t shared;                /* 1: Shared rows; 0: SingleCell candidates (width 1) */
+  uint32_t reserved;
+} texo_gp_choice_table;
+typedef struct texo_gp_projection_stats {
+  uint64_t fixed_units;
+  uint64_t overlapping_shared_families, overlapping_shared_units;
+  uint64_t disjoint_shared_families, disjoint_shared_units;
+  uint64_t singleton_units;
+  uint64_t relaxed_unmatched_units;
+  uint64_t bids, candidates_examined;   /* over the auctions */
+  uint64_t auctions;
+  double elapsed_ms;                    /* the auctions' device time */
+  uint32_t reserved[8];
+} texo_gp_projection_stats;
+int32_t texo_gp_project(int32_t device, uint32_t width, uint32_t height, uint32_t num_bels, const uint32_t* bel_xy,
+                        uint32_t num_tables, const texo_gp_choice_table* tables, uint32_t num_units,
+                        const uint32_t* unit_table, const uint32_t* unit_first_cell, const uint32_t* target_xy,
+                        uint32_t cost_scale, int32_t* out_choice, texo_gp_projection_stats* stats);
 
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)

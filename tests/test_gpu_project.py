@@ -70,3 +70,24 @@ def test_gpu_edge_cases_equal_the_parallel_restatement():
         bels = a.bels(units)
         assert a.stats["relaxed_unmatched_units"] == o.stats["relaxed_unmatched_units"]
         assert len(np.unique(bels[bels >= 0])) == int(np.sum(bels >= 0))
+
+
+def test_native_projection_equals_the_python_composition_with_gpu_auctions():
+    """texo_gp_project (the composition in native code) against the same
+    steps driven from Python with the same GPU auctions: identical choices
+    and statistics."""
+    arch, units, targets = fabric_case(1)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    for scale in (0, 1):
+        n = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=scale)
+        p = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=scale, auction=L.gpu_auction)
+        assert np.array_equal(n.preferred, p.preferred)
+        for key in ("fixed_units", "overlapping_shared_units", "disjoint_shared_families", "singleton_units",
+                    "relaxed_unmatched_units", "bids", "candidates_examined"):
+            assert n.stats[key] == p.stats[key], key
+
+
+def test_native_projection_conflict_is_an_error():
+    units = [L.Unit([0], [[3]], False), L.Unit([1], [[3]], False)]
+    with pytest.raises(L.ProjectionError):
+        L.project(2, 2, [[0, 0], [1, 0], [0, 1], [1, 1]], units, [[0, 0], [0, 0]])

@@ -31,6 +31,7 @@ STATUS = {
     114: "AUCTION_DUPLICATE_OBJECT",
     115: "INSTANCE_AREA_MEMBER", 116: "INSTANCE_AREA_FILLER", 117: "INSTANCE_AREA_POSTCONDITION",
     118: "INSTANCE_AREA_OVERFLOW",
+    119: "PROJECTION_CONFLICT",
 }
 CODE = {v: k for k, v in STATUS.items()}
 
@@ -140,6 +141,20 @@ class RoutableReport(C.Structure):
                 ("last_members_inflated", C.c_uint64), ("reserved", C.c_uint32 * 8)]
 
 
+class ChoiceTable(C.Structure):
+    """texo_gp_choice_table: a unit's choice rows."""
+    _fields_ = [("num_choices", C.c_uint32), ("width", C.c_uint32), ("bels", C.POINTER(C.c_uint32)),
+                ("shared", C.c_int32), ("reserved", C.c_uint32)]
+
+
+class ProjectionStats(C.Structure):
+    _fields_ = [("fixed_units", C.c_uint64), ("overlapping_shared_families", C.c_uint64),
+                ("overlapping_shared_units", C.c_uint64), ("disjoint_shared_families", C.c_uint64),
+                ("disjoint_shared_units", C.c_uint64), ("singleton_units", C.c_uint64),
+                ("relaxed_unmatched_units", C.c_uint64), ("bids", C.c_uint64), ("candidates_examined", C.c_uint64),
+                ("auctions", C.c_uint64), ("elapsed_ms", C.c_double), ("reserved", C.c_uint32 * 8)]
+
+
 class FieldEval(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
@@ -228,6 +243,9 @@ SIGNATURES = {
     "texo_gp_optimize_round": (C.c_int32, [_P, C.POINTER(Round), c_u32p, c_f64p, C.POINTER(Stats),
                                            C.POINTER(RoundResult)]),
     "texo_gp_set_charges": (C.c_int32, [_P, c_f64p, c_f64p]),
+    "texo_gp_project": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, C.c_uint32,
+                                    C.POINTER(ChoiceTable), C.c_uint32, c_u32p, c_u32p, c_u32p, C.c_uint32,
+                                    C.POINTER(C.c_int32), C.POINTER(ProjectionStats)]),
     "texo_gp_place_routable": (C.c_int32, [C.POINTER(ProblemC), C.POINTER(Params), C.POINTER(RoutingCapacity),
                                            C.c_uint64, C.POINTER(RegisterControl), c_u32p, c_f64p,
                                            C.POINTER(Stats), C.POINTER(RoutableReport)]),

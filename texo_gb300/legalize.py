@@ -330,13 +330,16 @@ def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
     5. `auction_singletons` (:657-677): one auction over every singleton,
        objects the BELs of each distinct candidate table.
 
-    `bel_xy` [B, 2]: BEL tiles. `auction(grid, kinds, targets, cost_scale) ->
-    (assignment, stats)` runs the auctions (default: the GPU; a checker passes
-    the oracle's). Unmatched units keep -1 (the reference's repair, which
-    places them by transactional search, is not part of this library)."""
+    `bel_xy` [B, 2]: BEL tiles. By default the whole composition runs in
+    native code (`texo_gp_project`, auctions on the GPU); `auction(grid, kinds,
+    targets, cost_scale) -> (assignment, stats)` runs these steps here in
+    Python with the given auction instead (a checker passes the oracle's).
+    Unmatched units keep -1 (the reference's repair, which places them by
+    transactional search, is not part of this library)."""
+    if auction is None:
+        return project_native(width, height, bel_xy, units, targets, cost_scale)
     bel_xy = np.asarray(bel_xy, dtype=np.int64).reshape(-1, 2)
     B = bel_xy.shape[0]
-    auction = auction or gpu_auction
     U = len(units)
     tg = np.asarray(targets, dtype=np.int64).reshape(-1, 2)
     if tg.shape[0] != U:
@@ -452,3 +455,45 @@ def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
             return pos[key][bel]
         record(singletons, asg, to_choice)
     return Projection(preferred, occupied, stats)
+
+
+def project_native(width, height, bel_xy, units, targets, cost_scale=0, device=0):
+    """`project` through texo_gp_project: the same steps as `project` with an
+    auction callback, in native code with the GPU auctions. Units sharing a
+    `choices` list share one choice table."""
+    xy = np.ascontiguousarray(np.asarray(bel_xy, dtype=np.uint32).reshape(-1, 2))
+    tg = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32).reshape(-1, 2))
+    U = len(units)
+    if tg.shape[0] != U:
+        raise ValueError("one target per unit")
+    table_of, tables, keep = {}, [], []
+    unit_table = np.zeros(max(U, 1), np.uint32)
+    first = np.zeros(max(U, 1), np.uint32)
+    for u, unit in enumerate(units):
+        key = id(unit.choices)
+        if key not in table_of:
+            rows = np.ascontiguousarray(np.asarray(unit.choices, dtype=np.uint32).reshape(len(unit.choices), -1))
+            keep.append(rows)
+            t = abi.ChoiceTable()
+            t.num_choices, t.width = rows.shape
+            t.bels = abi.ptr(rows, C.c_uint32)
+            t.shared = 1 if unit.is_shared() else 0
+            table_of[key] = len(tables)
+            tables.append(t)
+        elif bool(tables[table_of[key]].shared) != unit.is_shared():
+            raise ValueError("units sharing a choice table must agree on Shared / SingleCell")
+        unit_table[u] = table_of[key]
+        first[u] = unit.cells[0]
+    arr = (abi.ChoiceTable * max(len(tables), 1))(*tables)
+    out = np.full(max(U, 1), -1, np.int32)
+    st = abi.ProjectionStats()
+    lib = abi.load()
+    code = lib.texo_gp_project(device, width, height, xy.shape[0], abi.ptr(xy, C.c_uint32), len(tables), arr, U,
+                               abi.ptr(unit_table, C.c_uint32), abi.ptr(first, C.c_uint32),
+                               abi.ptr(tg if U else np.zeros(2, np.uint32), C.c_uint32), cost_scale,
+                               abi.ptr(out, C.c_int32), C.byref(st))
+    if code == abi.CODE["PROJECTION_CONFLICT"]:
+        raise ProjectionError(lib.texo_gp_last_error().decode())
+    abi.check(code, "texo_gp_project")
+    stats = {f: getattr(st, f) for f, _ in abi.ProjectionStats._fields_ if f != "reserved"}
+    return Projection(out[:U].astype(np.int64), None, stats)
