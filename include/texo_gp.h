@@ -698,8 +698,8 @@ int32_t texo_gp_register_clustering_areas(int32_t device, uint64_t num_registers
  * s = 1 is the reference's setting. 0 picks the largest of 4, 2, 1 whose
  * price range fits when every bidder is sure to be matched (the BEL grid
  * below with at least as many free BELs of each kind as bidders of that
- * kind) and every kind with bidders holds at most two BELs a tile on
- * average, else 1: bidders left over leave only once prices pass D, about
+ * kind, no BEL under two kinds) and every kind with bidders holds at most
+ * two BELs a tile on average, else 1: bidders left over leave only once prices pass D, about
  * one price step a round, and D grows with s; with many BELs a tile a
  * displaced bidder moves a ring out only after s price steps on each of
  * them. On placement targets the scaled
@@ -746,6 +746,9 @@ int32_t texo_gp_auction_explicit(int32_t device, uint32_t num_bidders, uint32_t 
  * target_xy[2b+1]) takes an unoccupied BEL of its kind at base cost
  * |x - tx| + |y - ty|; max_base_cost = width - 1 + height - 1. The ring walk
  * stops after ring r once the second-best reduced cost is below s (r + 1).
+ * A BEL may be listed under several kinds (once in each; bidders of those
+ * kinds then compete for its one price), so kinds can be the distinct
+ * candidate tables of SingleCell units.
  * `occupied` (may be NULL): one byte per BEL, nonzero for BELs held by fixed
  * units or earlier cohorts. Legality beyond occupancy (pin wires, shared
  * resources) is the caller's: a BEL that fails it is passed as occupied.

@@ -281,7 +281,11 @@ int32_t check_grid(const Grid& g, uint32_t m, uint32_t n, const uint32_t* kind, 
     if (g.tile_ptr[t + 1] < g.tile_ptr[t]) return TEXO_GP_ERR_INVALID_ARGUMENT;
   if (g.tile_ptr[slots] && !g.tile_object) return TEXO_GP_ERR_INVALID_ARGUMENT;
   std::vector<uint32_t> stamp(m, 0);
-  if (int32_t e = check_objects(g.tile_object, g.tile_ptr[slots], m, stamp, 1)) return e;
+  const uint64_t per_kind = (uint64_t)g.W * g.H;   // a BEL at most once in each kind's lists
+  for (uint32_t q = 0; q < g.K; ++q) {
+    const uint32_t k0 = g.tile_ptr[q * per_kind], k1 = g.tile_ptr[(q + 1) * per_kind];
+    if (int32_t e = check_objects(g.tile_object + k0, k1 - k0, m, stamp, q + 1)) return e;
+  }
   for (uint32_t b = 0; b < n; ++b)
     if (kind[b] >= g.K || target_xy[2 * b] >= g.W || target_xy[2 * b + 1] >= g.H) return TEXO_GP_ERR_INVALID_ARGUMENT;
   return 0;

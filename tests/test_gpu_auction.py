@@ -275,3 +275,39 @@ def test_singletons_bit_exact_at_one_million_cells():
         code, _, _, fifo = ffi.auction_singletons(grid, kind, xy, cost_scale=scale)
         assert code == 0 and fifo["unmatched"] == 0
         assert abs(fifo["total_base_cost"] - g.stats["total_base_cost"]) <= len(movable) / scale
+
+
+def test_kinds_sharing_bels_bit_exact_against_the_parallel_restatement():
+    """Kinds may list the same BEL (the distinct candidate tables of
+    SingleCell units): one price per BEL, bidders of both kinds compete; the
+    automatic scale falls back to 1."""
+    rng = np.random.default_rng(11)
+    w, h = 10, 10
+    tiles = w * h
+    # kind 0: every BEL; kind 1: the BELs of the left half; kind 2: a random third
+    lists = [list(range(tiles)), [t for t in range(tiles) if t % w < w // 2],
+             sorted(rng.choice(tiles, tiles // 3, replace=False).tolist())]
+    ptr = [0]
+    obj = []
+    for q in range(3):
+        members = set(lists[q])
+        for t in range(tiles):
+            if t in members:
+                obj.append(t)
+            ptr.append(len(obj))
+    grid = legalize.SiteGrid(w, h, 3, np.array(ptr, np.uint32), np.array(obj, np.uint32), tiles)
+    n = 60
+    kind = rng.integers(0, 3, n).astype(np.uint32)
+    xy = np.stack([rng.integers(0, w, n), rng.integers(0, h, n)], 1).astype(np.uint32)
+    for scale in (1, 0):
+        r = legalize.auction_singletons(grid, kind, xy, cost_scale=scale)
+        s = r.stats["cost_scale"]
+        assert s == 1
+        code, a, prices, st = ffi.auction_singletons(grid, kind, xy, cost_scale=s, jacobi=True)
+        assert code == 0 and np.array_equal(r.assignment, a)
+        assert np.array_equal(r.prices.astype(np.uint64), prices)
+        got = r.assignment[r.assignment >= 0]
+        assert len(set(got.tolist())) == len(got)
+        for b in range(n):
+            if r.assignment[b] >= 0:
+                assert int(r.assignment[b]) in set(lists[kind[b]])

@@ -91,3 +91,23 @@ def test_native_projection_conflict_is_an_error():
     units = [L.Unit([0], [[3]], False), L.Unit([1], [[3]], False)]
     with pytest.raises(L.ProjectionError):
         L.project(2, 2, [[0, 0], [1, 0], [0, 1], [1, 1]], units, [[0, 0], [0, 0]])
+
+
+def test_reference_projection_cases_on_the_gpu():
+    """The reference's own projection tests (legalization/mod.rs:1272-1377)
+    through texo_gp_project: overlapping candidate tables (kinds that share
+    BELs), a fixed owner, the candidate past the legacy 64 limit, four BELs
+    at one point, disjoint composite rows before the singletons."""
+    from test_project import REFERENCE_CASES, reference_case
+    for case, expected in REFERENCE_CASES:
+        w, h, bel_xy, units, targets = reference_case(*case)
+        for scale in (0, 1):
+            pj = L.project(w, h, bel_xy, units, targets, cost_scale=scale)
+            assert list(pj.bels(units)) == expected, (case, scale)
+    w, h, bel_xy, units, targets = reference_case([0, 0, 0, 0], [[0, 1, 2, 3]] * 4, [0, 0, 0, 0])
+    assert len(set(L.project(w, h, bel_xy, units, targets).bels(units).tolist())) == 4
+    bel_xy = np.array([(0, 0), (0, 0), (1, 0), (1, 0), (2, 0)], np.int64)
+    rows = [[0, 1], [2, 3]]
+    units = [L.Unit([0, 1], rows), L.Unit([2, 3], rows), L.Unit([4], [[1], [4]], False)]
+    bels = L.project(3, 1, bel_xy, units, [[0, 0]] * 3).bels(units)
+    assert len(set(bels.tolist())) == 5 and bels[4] == 4

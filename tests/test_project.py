@@ -183,3 +183,56 @@ def test_singletons_of_several_candidate_tables():
         bels = pj.bels(units)
         assert np.all(bels >= 0) and len(set(bels.tolist())) == 12
         assert all((b % 2 == 0) == (u % 2 == 1) for u, b in enumerate(bels))
+
+
+# ---- the reference's own projection tests (legalization/mod.rs:1205-1377) ----
+
+def reference_case(coordinates, candidate_sets, targets):
+    """projection_problem (mod.rs:1205-1241): Logic BELs on a one-row device
+    at the given x, one single-cell unit per candidate set (its own table),
+    targets on row 0."""
+    width = max(coordinates) + 1
+    bel_xy = np.array([(x, 0) for x in coordinates], np.int64)
+    units = [L.Unit([c], [[b] for b in cands], False) for c, cands in enumerate(candidate_sets)]
+    return width, 1, bel_xy, units, [[t, 0] for t in targets]
+
+
+REFERENCE_CASES = [
+    # singleton_projection_avoids_far_greedy_spill (:1272-1279)
+    (([0, 1, 100], [[0, 1, 2], [0, 2]], [0, 0]), [1, 0]),
+    # singleton_projection_avoids_false_no_bel_behind_fixed_owner (:1281-1291)
+    (([0, 1, 100], [[0, 1], [0, 2], [2]], [0, 0, 100]), [1, 0, 2]),
+    # projection_reaches_candidate_after_legacy_sixty_four_limit (:1302-1311)
+    (([0] * 66, [[i] for i in range(65)] + [list(range(66))], [0] * 66), list(range(66))),
+]
+
+
+@pytest.mark.parametrize("case,expected", REFERENCE_CASES)
+def test_reference_projection_cases(case, expected):
+    w, h, bel_xy, units, targets = reference_case(*case)
+    for jacobi in (False, True):
+        pj = L.project(w, h, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(jacobi))
+        assert list(pj.bels(units)) == expected
+
+
+def test_reference_four_real_bels_at_one_point():
+    # projection_uses_four_real_bels_at_one_point (:1293-1300)
+    w, h, bel_xy, units, targets = reference_case([0, 0, 0, 0], [[0, 1, 2, 3]] * 4, [0, 0, 0, 0])
+    for jacobi in (False, True):
+        pj = L.project(w, h, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(jacobi))
+        assert len(set(pj.bels(units).tolist())) == 4
+
+
+def test_reference_composite_rows():
+    # composite_slot_classification_requires_disjoint_complete_rows (:1313-1329)
+    assert L._rows_disjoint([[0, 1], [2, 3]]) and not L._rows_disjoint([[0, 1], [1, 2]])
+    # disjoint_composite_rows_remain_atomic_before_singleton_projection (:1331-1377)
+    bel_xy = np.array([(0, 0), (0, 0), (1, 0), (1, 0), (2, 0)], np.int64)
+    rows = [[0, 1], [2, 3]]
+    units = [L.Unit([0, 1], rows), L.Unit([2, 3], rows), L.Unit([4], [[1], [4]], False)]
+    for jacobi in (False, True):
+        pj = L.project(3, 1, bel_xy, units, [[0, 0]] * 3, cost_scale=1, auction=oracle_auction(jacobi))
+        bels = pj.bels(units)
+        assert len(set(bels.tolist())) == 5 and bels[4] == 4
+        for unit in units[:2]:
+            assert list(bels[unit.cells]) in rows

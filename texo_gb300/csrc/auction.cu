@@ -688,11 +688,23 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
       return fail_with(stats, TEXO_GP_ERR_INVALID_ARGUMENT, "auction: tile_ptr decreases");
   if (tile_ptr[slots] && !tile_object)
     return fail_with(stats, TEXO_GP_ERR_INVALID_ARGUMENT, "auction: null tile_object");
+  // a BEL at most once in each kind's lists (kinds may share BELs: bidders of
+  // both compete for its one price)
   std::vector<uint32_t> stamp(num_objects, 0);
-  if (int32_t e = check_objects(tile_object, tile_ptr[slots], num_objects, stamp, 1))
-    return fail_with(stats, e,
-                     e == TEXO_GP_ERR_AUCTION_OBJECT_RANGE ? "auction: BEL out of range"
-                                                           : "auction: a BEL listed twice");
+  std::vector<uint8_t> listed(num_objects, 0);
+  bool shared_bels = false;
+  const uint64_t tiles_per_kind = (uint64_t)width * height;
+  for (uint32_t q = 0; q < num_kinds; ++q) {
+    const uint32_t k0 = tile_ptr[q * tiles_per_kind], k1 = tile_ptr[(q + 1) * tiles_per_kind];
+    if (int32_t e = check_objects(tile_object + k0, k1 - k0, num_objects, stamp, q + 1))
+      return fail_with(stats, e,
+                       e == TEXO_GP_ERR_AUCTION_OBJECT_RANGE ? "auction: BEL out of range"
+                                                             : "auction: a BEL listed twice in one kind");
+    for (uint32_t k = k0; k < k1; ++k) {
+      shared_bels |= listed[tile_object[k]] != 0;
+      listed[tile_object[k]] = 1;
+    }
+  }
   for (uint32_t b = 0; b < num_bidders; ++b)
     if (bidder_kind[b] >= num_kinds || target_xy[2 * b] >= width || target_xy[2 * b + 1] >= height)
       return fail_with(stats, TEXO_GP_ERR_INVALID_ARGUMENT, "auction: bidder kind or target outside the grid");
@@ -725,6 +737,9 @@ extern "C" int32_t texo_gp_auction_singletons(int32_t device, uint32_t width, ui
     for (uint32_t b = 0; b < num_bidders; ++b) bidders[bidder_kind[b]]++;
     for (uint32_t q = 0; q < num_kinds; ++q)
       if (bidders[q] > free_bels[q] || (bidders[q] && bels[q] > 2 * tiles_used[q])) cost_scale = 1;
+    // kinds sharing BELs: whether every bidder can be matched is not known
+    // from the per-kind counts
+    if (shared_bels) cost_scale = 1;
   }
   h.scale = pick_scale(num_bidders, h.max_base_cost, cost_scale);
   if (!h.scale) return fail_with(stats, TEXO_GP_ERR_AUCTION_RANGE, kRangeText);
