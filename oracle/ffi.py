@@ -244,6 +244,9 @@ def lib():
             "orc_field_gamma": (C.c_int32, [C.c_double, C.c_double, C.c_double, c_f64p]),
             "orc_weighted_gamma_mean": (C.c_int32, [c_f64p, c_f64p, C.c_uint64, C.c_double, c_f64p]),
             "orc_overflow_target": (C.c_double, [C.c_uint32]),
+            "orc_area_adjustment_ready": (C.c_int32, [C.c_uint32, c_u32p, c_f64p]),
+            "orc_area_adjusted_multipliers": (C.c_int32, [C.c_uint32, c_f64p, c_f64p, c_f64p, C.c_double, c_f64p,
+                                                          C.c_uint64, c_f64p]),
             "orc_checkpoint_better": (C.c_int32, [C.c_double, C.c_double, C.c_double, C.c_double]),
             "orc_validate_units": (C.c_int32, [c_u32p, C.c_uint64, c_u64p]),
             "orc_routing_demand": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint64, c_f64p, c_f64p, c_f64p]),

@@ -1121,6 +1121,52 @@ int32_t weighted_gamma_mean(const double* gm, const double* w, size_t n, double 
   return TEXO_GP_ERR_INVALID_NORMALIZATION;
 }
 
+// area_adjustment_is_ready (eplace.rs:1403-1408): the LUT and register
+// fields at AREA_ADJUSTMENT_OVERFLOW_TARGET = 0.15 (eplace.rs:130)
+bool area_adjustment_ready(uint32_t K, const uint32_t* kinds, const double* overflow) {
+  for (uint32_t f = 0; f < K; ++f) {
+    if (kinds[f] != TEXO_GP_KIND_LUT && kinds[f] != TEXO_GP_KIND_REGISTER) continue;
+    if (!(overflow[f] <= 0.15)) return false;
+  }
+  return true;
+}
+// normalized_density_subgradient (eplace.rs:1154-1175) with validate_fields
+int32_t density_subgradient(uint32_t K, const double* energy, const double* scales, double beta,
+                            std::vector<double>& sg) {
+  for (uint32_t f = 0; f < K; ++f)
+    if (!std::isfinite(energy[f]) || !std::isfinite(scales[f]) || scales[f] <= 0.0)
+      return TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
+  sg.resize(K);
+  for (uint32_t f = 0; f < K; ++f) {
+    const double ne = energy[f] / scales[f];
+    sg[f] = ne + 0.5 * beta * ne * ne;
+    if (!std::isfinite(sg[f]) || sg[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+  }
+  return TEXO_GP_OK;
+}
+// area_adjusted_density_multipliers (eplace.rs:1183-1218), elfPlace eq. (27):
+// lambda_f = 0.1 |grad W|_1 / (sum_f force_l1_f sg_f) * sg_f; `wa_l1` is
+// |grad W|_1 summed in the reference's order
+int32_t area_adjusted_multipliers(uint32_t K, const double* energy, const double* force_l1, const double* scales,
+                                  double beta, double wa_l1, std::vector<double>& lambda) {
+  std::vector<double> sg;
+  int32_t s = density_subgradient(K, energy, scales, beta, sg);
+  if (s) return s;
+  double dens = 0.0;
+  for (uint32_t f = 0; f < K; ++f) dens += force_l1[f] * sg[f];
+  if (!std::isfinite(wa_l1) || wa_l1 <= 0.0 || !std::isfinite(dens) || dens <= 0.0)
+    return TEXO_GP_ERR_INVALID_NORMALIZATION;
+  const double scale = 0.1 * wa_l1 / dens;
+  lambda.assign(K, 0.0);
+  bool any = false;
+  for (uint32_t f = 0; f < K; ++f) {
+    lambda[f] = scale * sg[f];
+    if (!std::isfinite(lambda[f]) || lambda[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    any = any || lambda[f] > 0.0;
+  }
+  return any ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
+}
+
 struct Eplace {
   Oracle& o;
   int threads;
@@ -1149,42 +1195,36 @@ struct Eplace {
   // register fields at AREA_ADJUSTMENT_OVERFLOW_TARGET = 0.15, eplace.rs:130).
   int stop_mode = 0;
   bool stop_reached(const Evaluation& ev) const {
-    for (uint32_t f = 0; f < o.K; ++f) {
-      if (stop_mode == 1) {
-        const uint32_t k = o.field_kind[f].kind;
-        if (k != TEXO_GP_KIND_LUT && k != TEXO_GP_KIND_REGISTER) continue;
-        if (!(ev.fields[f].overflow <= 0.15)) return false;
-      } else if (!(ev.fields[f].overflow <= target_of(f))) {
-        return false;
+    if (stop_mode == 1) {
+      std::vector<uint32_t> kinds(o.K);
+      std::vector<double> ov(o.K);
+      for (uint32_t f = 0; f < o.K; ++f) {
+        kinds[f] = o.field_kind[f].kind;
+        ov[f] = ev.fields[f].overflow;
       }
+      return area_adjustment_ready(o.K, kinds.data(), ov.data());
     }
+    for (uint32_t f = 0; f < o.K; ++f)
+      if (!(ev.fields[f].overflow <= target_of(f))) return false;
     return true;
   }
   // area_adjusted_density_multipliers (eplace.rs:1183-1218) and
   // area_adjusted_multiplier_step (:1220-1232): elfPlace eqs. (27)-(28).
   int32_t area_multipliers(const Evaluation& ev, const std::vector<double>& scales, std::vector<double>& lambda,
                            double& step) const {
-    std::vector<double> sg;
-    int32_t s = subgradient(ev, scales, sg);
-    if (s) return s;
+    if (ev.fields.size() != scales.size()) return TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
     double wl = 0.0;
     for (uint32_t u = 0; u < o.U; ++u) {
       wl += std::fabs(ev.wa_gx[u]);
       wl += std::fabs(ev.wa_gy[u]);
     }
-    double dens = 0.0;
-    for (uint32_t f = 0; f < o.K; ++f) dens += ev.fields[f].force_l1 * sg[f];
-    if (!std::isfinite(wl) || wl <= 0.0 || !std::isfinite(dens) || dens <= 0.0)
-      return TEXO_GP_ERR_INVALID_NORMALIZATION;
-    const double scale = 0.1 * wl / dens;
-    lambda.assign(o.K, 0.0);
-    bool any = false;
+    std::vector<double> energy(o.K), force(o.K);
     for (uint32_t f = 0; f < o.K; ++f) {
-      lambda[f] = scale * sg[f];
-      if (!std::isfinite(lambda[f]) || lambda[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
-      any = any || lambda[f] > 0.0;
+      energy[f] = ev.fields[f].energy;
+      force[f] = ev.fields[f].force_l1;
     }
-    if (!any) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    int32_t s = area_adjusted_multipliers(o.K, energy.data(), force.data(), scales.data(), o.params.beta, wl, lambda);
+    if (s) return s;
     double nn = 0.0;
     for (double m : lambda) nn += m * m;
     step = (o.params.alpha_high - 1.0) * std::sqrt(nn);
@@ -2062,6 +2102,24 @@ int32_t orc_weighted_gamma_mean(const double* g, const double* w, uint64_t n, do
   return weighted_gamma_mean(g, w, (size_t)n, fallback, *mean);
 }
 double orc_overflow_target(uint32_t kind) { return overflow_target(kind); }
+int32_t orc_area_adjustment_ready(uint32_t K, const uint32_t* kinds, const double* overflow) {
+  return area_adjustment_ready(K, kinds, overflow) ? 1 : 0;
+}
+int32_t orc_area_adjusted_multipliers(uint32_t K, const double* energy, const double* force_l1,
+                                      const double* initial_energies, double beta, const double* wa_gradient_xy,
+                                      uint64_t units, double* out) {
+  // |grad W|_1 in the reference's order: x then y of each unit
+  double wl = 0.0;
+  for (uint64_t u = 0; u < units; ++u) {
+    wl += std::fabs(wa_gradient_xy[2 * u]);
+    wl += std::fabs(wa_gradient_xy[2 * u + 1]);
+  }
+  std::vector<double> lambda;
+  const int32_t s = area_adjusted_multipliers(K, energy, force_l1, initial_energies, beta, wl, lambda);
+  if (s) return s;
+  for (uint32_t f = 0; f < K; ++f) out[f] = lambda[f];
+  return TEXO_GP_OK;
+}
 int32_t orc_checkpoint_better(double mx, double tot, double bmx, double btot) {
   int c = total_cmp(mx, bmx);
   return (c < 0 || (c == 0 && total_cmp(tot, btot) < 0)) ? 1 : 0;

@@ -174,6 +174,10 @@ int32_t orc_field_gamma(double overflow, double target, double base, double* gam
 int32_t orc_weighted_gamma_mean(const double* gammas, const double* weights, uint64_t n,
                                 double fallback, double* mean);          /* :1369-1395 */
 double orc_overflow_target(uint32_t kind);                              /* :1300-1308 */
+int32_t orc_area_adjustment_ready(uint32_t K, const uint32_t* kinds, const double* overflow); /* :1403-1408 */
+int32_t orc_area_adjusted_multipliers(uint32_t K, const double* energy, const double* force_l1,
+                                      const double* initial_energies, double beta, const double* wa_gradient_xy,
+                                      uint64_t units, double* out);      /* :1183-1218 */
 int32_t orc_checkpoint_better(double max_excess, double total_excess, double best_max,
                               double best_total);                       /* :106-119 */
 int32_t orc_validate_units(const uint32_t* member_ptr, uint64_t units, uint64_t* error_index);

@@ -151,3 +151,12 @@ def test_invalid_inputs_name_the_entry():
     assert e.value.code == abi.CODE["INSTANCE_AREA_OVERFLOW"]
     with pytest.raises(abi.TexoGpError):
         R.pin_optimized_area(2 ** 32, 1.0, 1.0)
+
+
+# eplace.rs:1778-1797
+def test_rudy_inflates_exchangeable_slice_area_but_not_hard_memory_charge():
+    congested = 2.0 ** 0.5
+    f = R.routability_adjusted_member_area
+    assert abs(f(abi.KIND_LUT, 1.0, congested, 0.0) - 2.0) <= np.finfo(float).eps
+    assert abs(f(abi.KIND_REGISTER, 1.0, 0.0, congested) - 2.0) <= np.finfo(float).eps
+    assert f(abi.KIND_MEMORY, 1.0, congested, congested) == 1.0

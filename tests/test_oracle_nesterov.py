@@ -300,3 +300,33 @@ def test_checkpoint_retains_the_lowest_field_overflow_excess():
 # :1860-1864 (cap as a parameter; default equals the reference constant)
 def test_paper_iteration_cap_default():
     assert abi.default_params_py().max_iterations == 3000
+
+
+# :1760-1776
+def test_area_adjustment_starts_at_lut_and_register_fifteen_percent():
+    ready = ffi.lib().orc_area_adjustment_ready
+
+    def is_ready(fields):
+        k = np.array([f[0] for f in fields], np.uint32)
+        o = np.array([f[1] for f in fields], np.float64)
+        return ready(len(fields), ffi.P(k, C.c_uint32), ffi.P(o)) == 1
+    assert is_ready([(abi.KIND_LUT, 0.15), (abi.KIND_REGISTER, 0.149), (abi.KIND_MEMORY, 0.99)])
+    assert not is_ready([(abi.KIND_LUT, 0.151), (abi.KIND_REGISTER, 0.149)])
+
+
+# :1799-1822
+def test_area_adjusted_multiplier_matches_elfplace_force_balance():
+    energy = np.array([5.0, 10.0])
+    force = np.array([2.0, 3.0])
+    initial = np.array([10.0, 20.0])
+    wa = np.array([3.0, 4.0, -1.0, 0.0])     # units (3, 4) and (-1, 0): x then y per unit
+    out = np.zeros(2)
+    assert ffi.lib().orc_area_adjusted_multipliers(2, ffi.P(energy), ffi.P(force), ffi.P(initial), 2000.0,
+                                                   ffi.P(wa), 2, ffi.P(out)) == 0
+    assert abs(out[0] - out[1]) <= 1e-15
+    # equation (27): <sum_i q_i ||xi_i||_1, lambda'> = eta' ||grad W||_1
+    assert abs(2.0 * out[0] + 3.0 * out[1] - 0.8) <= 1e-14
+    # a non-finite energy is the reference's DensityFieldChanged
+    bad = np.array([np.nan, 10.0])
+    assert ffi.lib().orc_area_adjusted_multipliers(2, ffi.P(bad), ffi.P(force), ffi.P(initial), 2000.0,
+                                                   ffi.P(wa), 2, ffi.P(out)) == abi.CODE["DENSITY_FIELD_CHANGED"]

@@ -134,6 +134,14 @@ def kind_key(field):
     return int(kind) << 8 | int(lut)
 
 
+def routability_adjusted_member_area(kind, current_area, horizontal_utilization, vertical_utilization):
+    """`routability_adjusted_member_area` (eplace.rs:741-758): eq. (29) for
+    LUT and register members; every other kind keeps its area (a hard block
+    inflated in its own field reserves none of the congested slice routing)."""
+    area = routability_optimized_area(current_area, horizontal_utilization, vertical_utilization)
+    return area if int(kind) in (abi.KIND_LUT, abi.KIND_REGISTER) else float(current_area)
+
+
 def _rounded(value, extent):
     # rounded_coordinate (lib.rs:4566-4568): round half away from zero (value
     # - trunc(value) is exact, so no addition of 0.5 can round up), clamp to
@@ -200,10 +208,8 @@ def propose_area_adjustment(problem, coordinates, capacity_h, capacity_v, filler
     y = _rounded(pos[unit_of, 1] + off[:, 1], H)
     hu = _utilization(h_dem, cap_h, x, y)
     vu = _utilization(v_dem, cap_v, x, y)
-    inflatable = np.array([fields[f][0] in (abi.KIND_LUT, abi.KIND_REGISTER) for f in field], dtype=bool)
-    routing = np.array([routability_optimized_area(c, min(a, SQRT_2), min(b, SQRT_2))
-                        for c, a, b in zip(charge, hu, vu)])
-    routing = np.where(inflatable, routing, charge)
+    routing = np.array([routability_adjusted_member_area(fields[f][0], c, min(a, SQRT_2), min(b, SQRT_2))
+                        for f, c, a, b in zip(field, charge, hu, vu)])
     clus_area = np.zeros(len(members))
     if register_controls:
         cells = np.asarray(problem.member_cell, dtype=np.int64)[members]
