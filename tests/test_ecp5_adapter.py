@@ -130,3 +130,11 @@ def test_units_must_cover_every_cell(arch):
     bad = units[:2] + [ecp5.Unit([4], [[0, 1]])] + units[3:]
     with pytest.raises(ValueError):
         ecp5.placement_problem(arch, 7, bad, nets)
+
+
+# eplace.rs:1905-1914 (only_interchangeable_ecp5_resource_classes_get_density_fields)
+def test_only_interchangeable_resource_classes_get_density_fields():
+    ex = ecp5.EXCHANGEABLE
+    assert abi.KIND_LUT in ex and abi.KIND_REGISTER in ex and abi.KIND_MEMORY in ex
+    for k in (abi.KIND_CLOCK, abi.KIND_LOGIC, abi.KIND_IO, abi.KIND_CONSTANT):
+        assert k not in ex
