@@ -1,0 +1,76 @@
+"""The analytical placement pass (`analytical_place`, lib.rs:3990-4150) on
+the GPU over an ECP5-like fabric: the seed's two axis solves against the same
+steps with the oracle's solve, and each mode (coarse, electrostatic, an
+anchored timing iteration) through `project` to legal choices."""
+import numpy as np
+import pytest
+
+from oracle import ffi
+from texo_gb300 import analytical as A, ecp5, seed
+
+pytestmark = pytest.mark.gpu
+
+
+def fabric(seed_no=0, side=16):
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(side, side))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, seed_no, luts=500, ffs=250, lut_ff_pairs=150,
+                                                   carry=((12, 4), (6, 6)), io=24)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    return arch, prob, units
+
+
+def oracle_solver(d, ptr, idx, w, rhs, x0):
+    x, st, ok = ffi.solve_quadratic(d, ptr, idx, w, rhs, x0)
+    assert ok
+    return x, st
+
+
+def legal(res, units):
+    bels = np.full(1 + max(c for u in units for c in u.cells), -1)
+    for i, u in enumerate(units):
+        if res.preferred[i] >= 0:
+            bels[u.cells] = u.choices[res.preferred[i]]
+    placed = bels[bels >= 0]
+    return len(np.unique(placed)) == len(placed)
+
+
+@pytest.mark.parametrize("mode", [A.COARSE, A.ELECTROSTATIC, A.ELECTROSTATIC_BEST_EFFORT])
+def test_modes_reach_legal_choices(mode):
+    arch, prob, units = fabric()
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    res = A.analytical_place(prob, units, bel_xy, mode=mode)
+    assert np.all(res.preferred >= 0) and legal(res, units)
+    if mode != A.COARSE:
+        assert res.info["placement"]["converged"]
+
+
+def test_seed_matches_the_oracle_path():
+    arch, prob, units = fabric(1)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    res = A.analytical_place(prob, units, bel_xy, mode=A.COARSE)
+    # the same seed with the oracle's solve
+    fixed = np.array([len(u.choices) == 1 for u in units])
+    import copy
+    sp = copy.copy(prob)
+    lo = np.array([bel_xy[[a[0] for a in u.choices]].min(axis=0) for u in units], np.float64)
+    hi = np.array([bel_xy[[a[0] for a in u.choices]].max(axis=0) for u in units], np.float64)
+    sp.lower_xy, sp.upper_xy = lo, hi
+    cx, cy = prob.width // 2, prob.height // 2
+    centre = np.where(fixed[:, None], lo, np.array([float(cx), float(cy)]))
+    x, _ = seed.solve_axis(sp, centre, 0, cx, solver=oracle_solver, fixed=fixed)
+    y, _ = seed.solve_axis(sp, centre, 1, cy, solver=oracle_solver, fixed=fixed)
+    ref = np.stack([x, y], 1)
+    assert np.max(np.abs(res.seed_xy - ref)) <= 1e-8 * np.max(np.abs(ref))
+
+
+def test_anchored_iteration_moves_towards_the_incumbent():
+    arch, prob, units = fabric(2)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    first = A.analytical_place(prob, units, bel_xy, mode=A.ELECTROSTATIC)
+    incumbent = np.array([bel_xy[u.choices[c][0]] for u, c in zip(units, first.preferred)], np.float64)
+    free = np.array([len(u.choices) > 1 for u in units])
+    d0 = np.abs(first.seed_xy - incumbent).sum(axis=1)[free].sum()
+    res = A.analytical_place(prob, units, bel_xy, anchor=(incumbent, 4))
+    d1 = np.abs(res.seed_xy - incumbent).sum(axis=1)[free].sum()
+    assert res.info.get("anchored") and d1 < d0
+    assert np.all(res.preferred >= 0) and legal(res, units)

@@ -111,3 +111,28 @@ def test_timed_arcs_add_overlay_edges():
     sep = np.maximum(np.abs(coord[drv[keep]] - coord[snk[keep]]), 1.0)
     extra = np.asarray(prob.arc_extra_weight, dtype=np.float64)[keep]
     assert np.array_equal(w[-n:], 64.0 * extra / sep)
+
+
+def test_anchor_pulls_a_free_unit_to_its_incumbent():
+    """add_anchor (lib.rs:4410-4415): a unit with no edges but an anchor sits
+    on the anchor; the weights follow lib.rs:4094-4105."""
+    prob = macro_offsets_case()
+    pos = np.array([[4.0, 0.0], [4.0, 0.0]])
+    anchor = np.array([[1.0, 0.0], [7.0, 0.0]])
+    dx = seed.axis_system(prob, pos, 0)[0]
+    dy = seed.axis_system(prob, pos, 1)[0]
+    wx, wy = seed.anchor_weights(prob, pos, anchor, 3, dx, dy)
+    # distances 3 and 3; diagonals max(d, 1); 0.1 * 3 / 3
+    assert np.allclose(wx, np.maximum(dx, 1.0) * 0.1, rtol=0, atol=1e-15)
+    assert np.allclose(wy, np.maximum(dy, 1.0) * 0.1, rtol=0, atol=1e-15)
+    # the anchored system: no floating component any more, both units pulled
+    x, _ = seed.solve_axis(prob, pos, 0, 4, solver=exact_solver, anchors=(wx, anchor[:, 0]))
+    d, ptr, idx, w, rhs, _ = seed.axis_system(prob, pos, 0)
+    # stationarity of edges + anchors: the gradient of the edge part equals
+    # the anchors' pull
+    g, _ = b2b_gradient(prob, pos, 0, x)
+    assert np.allclose(g + wx * (x - anchor[:, 0]), 0.0, atol=1e-9)
+    # an explicit fixed mask overrides the collapsed-bounds rule
+    fixed = np.array([True, False])
+    f, c = seed.fixed_units(prob, 0, fixed)
+    assert list(f) == [True, False] and c[0] == 0.0

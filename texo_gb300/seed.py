@@ -94,15 +94,19 @@ def b2b_edges(problem, positions, axis, with_cells=False):
     return out
 
 
-def fixed_units(problem, axis):
-    """(fixed mask [U], origin coordinate along `axis` [U]) of the units."""
+def fixed_units(problem, axis, fixed=None):
+    """(fixed mask [U], origin coordinate along `axis` [U]) of the units;
+    `fixed` (optional) overrides the collapsed-bounds rule (the reference's
+    rule is one placement choice)."""
     lower = np.asarray(problem.lower_xy, dtype=np.float64).reshape(-1, 2)
     upper = np.asarray(problem.upper_xy, dtype=np.float64).reshape(-1, 2)
-    fixed = np.all(lower == upper, axis=1)
+    if fixed is None:
+        fixed = np.all(lower == upper, axis=1)
+    fixed = np.asarray(fixed, dtype=bool)
     return fixed, np.where(fixed, lower[:, axis], 0.0)
 
 
-def axis_system(problem, positions, axis):
+def axis_system(problem, positions, axis, fixed=None):
     """(diagonal, adjacency CSR (ptr, index, weight), rhs, anchored) of one
     axis (`analytical_axis_equations`, lib.rs:4464-4527): a fixed unit holds
     its origin; an edge to a fixed unit adds to the diagonal and adds
@@ -113,7 +117,7 @@ def axis_system(problem, positions, axis):
     U = problem.num_units
     fixed_xy = np.asarray(problem.cell_fixed_xy, dtype=np.float64).reshape(-1, 2)
     offset = np.asarray(problem.cell_offset_xy, dtype=np.float64).reshape(-1, 2)[:, axis]
-    unit_fixed, unit_coord = fixed_units(problem, axis)
+    unit_fixed, unit_coord = fixed_units(problem, axis, fixed)
     diag = np.where(unit_fixed, 1.0, 0.0)
     rhs = np.where(unit_fixed, unit_coord, 0.0)
     anchored = unit_fixed.copy()
@@ -176,14 +180,42 @@ def finalize_gauges(diag, ptr, index, weight, rhs, anchored):
     return diag, np.cumsum(new_ptr), index[keep], weight[keep], rhs, floating
 
 
-def solve_axis(problem, positions, axis, center, device=0, solver=None):
+ANCHOR_ALPHA = 0.1   # lib.rs:4001
+
+
+def anchor_weights(problem, solved, anchor_xy, iteration, diag_x, diag_y, fixed=None):
+    """The incumbent anchors of a timing iteration (lib.rs:4084-4108): for
+    every movable unit, weight max(diagonal, 1) * 0.1 * iteration /
+    max(distance, 1) per axis, `distance` the Manhattan distance from the
+    solved position to the incumbent's tile, `diag_*` the axis systems'
+    diagonals before the anchors. Returns (wx, wy) [U], zero for fixed units."""
+    fixed, _ = fixed_units(problem, 0, fixed)
+    s = np.asarray(solved, dtype=np.float64).reshape(-1, 2)
+    a = np.asarray(anchor_xy, dtype=np.float64).reshape(-1, 2)
+    dist = np.maximum(np.abs(s[:, 0] - a[:, 0]) + np.abs(s[:, 1] - a[:, 1]), 1.0)
+    scale = ANCHOR_ALPHA * float(iteration) / dist
+    wx = np.where(fixed, 0.0, np.maximum(diag_x, 1.0) * scale)
+    wy = np.where(fixed, 0.0, np.maximum(diag_y, 1.0) * scale)
+    return wx, wy
+
+
+def solve_axis(problem, positions, axis, center, device=0, solver=None, anchors=None, fixed=None):
     """solve_analytical_axis (lib.rs:4531-4560) for one axis: the system at
     `positions`, the gauges, the GPU solve from the current coordinates (each
     floating component shifted so its gauge sits at 0), and each floating
     component recentred on `center`. `solver(diag, ptr, index, weight, rhs,
     x0) -> (x, stats)` replaces the GPU solve (a checker passes its own).
-    Returns (coordinates [U], solve stats)."""
-    diag, ptr, index, weight, rhs, anchored = axis_system(problem, positions, axis)
+    `anchors` (weights [U], coordinates [U]) are added first (`add_anchor`,
+    lib.rs:4410-4415: weight on the diagonal, weight * coordinate on the
+    right-hand side, the unit anchored) where the weight is positive.
+    `fixed` as in `fixed_units`. Returns (coordinates [U], solve stats)."""
+    diag, ptr, index, weight, rhs, anchored = axis_system(problem, positions, axis, fixed)
+    if anchors is not None:
+        w, c = (np.asarray(v, dtype=np.float64) for v in anchors)
+        on = w > 0.0
+        diag = diag + np.where(on, w, 0.0)
+        rhs = rhs + np.where(on, w * c, 0.0)
+        anchored = anchored | on
     diag, ptr, index, weight, rhs, floating = finalize_gauges(diag, ptr, index, weight, rhs, anchored)
     x = np.asarray(positions, dtype=np.float64).reshape(-1, 2)[:, axis].copy()
     for comp in floating:
