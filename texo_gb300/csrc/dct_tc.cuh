@@ -88,7 +88,7 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN 
 // (32 KB), a B block a 64 x 128 box (16 KB). The data are already in the
 // MMA's shared-memory layout, so the copies use no swizzle.
 enum TcMap { TM_OPA = 0, TM_OPB, TM_CXB, TM_CYA, TM_CYTA, TM_CXTB, TM_COUNT };
-struct alignas(64) TcMaps {
+struct TcMaps {   // aligned as CUtensorMap requires
   CUtensorMap m[TM_COUNT];
 };
 
