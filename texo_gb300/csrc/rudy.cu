@@ -101,31 +101,56 @@ __global__ void k_rudy_boxes(const double* boxes, long long nbox, int W, int H, 
     }
 }
 
-// inclusive scan along each row of both planes (one thread per row)
-__global__ void k_rudy_rows(unsigned long long* diff, int W, int H) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= 2 * H) return;
-  const int plane = r / H, y = r % H;
-  long long* row = (long long*)diff + (size_t)plane * (W + 1) * (H + 1) + (size_t)y * (W + 1);
-  long long s = 0;
-  for (int x = 0; x < W; ++x) {
-    s += row[x];
-    row[x] = s;
+// Inclusive scan along each row of both planes: a warp per row, 32 columns
+// a step (a shuffle scan plus the carry of the previous step). The sums are
+// exact integers, so any order gives the same values.
+__global__ void k_rudy_rows(unsigned long long* __restrict__ diff, int W, int H) {
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = (int)(threadIdx.x & 31);
+  if (warp >= 2 * H) return;   // uniform across the warp
+  const int plane = warp / H, y = warp % H;
+  unsigned long long* row = diff + (size_t)plane * (W + 1) * (H + 1) + (size_t)y * (W + 1);
+  unsigned long long carry = 0;
+  for (int x0 = 0; x0 < W; x0 += 32) {
+    const int x = x0 + lane;
+    unsigned long long v = x < W ? row[x] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    v += carry;
+    if (x < W) row[x] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
   }
 }
 
-// inclusive scan along each column, written out as FP64 demand
-__global__ void k_rudy_cols(const unsigned long long* diff, int W, int H, double* horizontal, double* vertical) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= 2 * W) return;
-  const int plane = c / W, x = c % W;
-  const long long* col = (const long long*)diff + (size_t)plane * (W + 1) * (H + 1) + x;
+// Inclusive scan along each column, written out as FP64 demand: a block per
+// strip of 32 columns of one plane; its warps take consecutive row segments,
+// sum them, add the totals of the segments above and scan their own (the
+// loads of a segment do not depend on one another).
+constexpr int kColWarps = 8;
+__global__ void __launch_bounds__(32 * kColWarps) k_rudy_cols(const unsigned long long* __restrict__ diff, int W,
+                                                              int H, double* __restrict__ horizontal,
+                                                              double* __restrict__ vertical) {
+  __shared__ unsigned long long seg[kColWarps][32];
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+  const int strips = (W + 31) / 32;
+  const int plane = (int)blockIdx.x / strips, x = ((int)blockIdx.x % strips) * 32 + lane;
+  const unsigned long long* col = diff + (size_t)plane * (W + 1) * (H + 1) + x;
   double* out = plane ? vertical : horizontal;
-  long long s = 0;
-  for (int y = 0; y < H; ++y) {
-    s += col[(size_t)y * (W + 1)];
-    out[(size_t)y * W + x] = (double)s / kRudyFix;
-  }
+  const int per = (H + kColWarps - 1) / kColWarps, y0 = min(H, w * per), y1 = min(H, y0 + per);
+  unsigned long long s = 0;
+  if (x < W)
+    for (int y = y0; y < y1; ++y) s += col[(size_t)y * (W + 1)];
+  seg[w][lane] = s;
+  __syncthreads();
+  unsigned long long c = 0;
+  for (int k = 0; k < w; ++k) c += seg[k][lane];
+  if (x < W)
+    for (int y = y0; y < y1; ++y) {
+      c += col[(size_t)y * (W + 1)];
+      out[(size_t)y * W + x] = (double)(long long)c / kRudyFix;
+    }
 }
 
 }  // namespace
@@ -177,8 +202,8 @@ extern "C" int32_t texo_gp_routing_demand(int32_t device, uint32_t width, uint32
     note_launch();
   }
   if (ok) {
-    k_rudy_rows<<<(2 * H + 127) / 128, 128, 0, s>>>(diff, W, H);
-    k_rudy_cols<<<(2 * W + 127) / 128, 128, 0, s>>>(diff, W, H, dh, dv);
+    k_rudy_rows<<<(unsigned)((2 * (size_t)H * 32 + kThreads - 1) / kThreads), kThreads, 0, s>>>(diff, W, H);
+    k_rudy_cols<<<(unsigned)(2 * ((W + 31) / 32)), 32 * kColWarps, 0, s>>>(diff, W, H, dh, dv);
     note_launch();
     note_launch();
     ok = cudaGetLastError() == cudaSuccess &&
