@@ -111,3 +111,28 @@ def test_reference_projection_cases_on_the_gpu():
     units = [L.Unit([0, 1], rows), L.Unit([2, 3], rows), L.Unit([4], [[1], [4]], False)]
     bels = L.project(3, 1, bel_xy, units, [[0, 0]] * 3).bels(units)
     assert len(set(bels.tolist())) == 5 and bels[4] == 4
+
+
+def test_projection_at_scale_equals_the_parallel_restatement():
+    """A 64 x 64-tile ECP5-like fabric (27,744 LUT and 27,744 FF BELs), 15,000
+    singletons, 2,000 LUT-FF pairs, 160 carry chains of 4 and 40 of 6 pairs,
+    at the oracle placement's targets: the native composition with the GPU
+    auctions gives the choices of the Python composition with the oracle's
+    parallel rounds, bit for bit, at the reference's scale and the automatic
+    one."""
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(64, 64))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, 5, luts=10000, ffs=5000, lut_ff_pairs=2000,
+                                                   carry=((160, 4), (40, 6)), io=100)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    prm = abi.default_params_py()
+    prm.best_effort = 1
+    st, targets, _, _ = ffi.Oracle(prob, prm).place(threads=8)
+    assert st == 0
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    g = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1)
+    o = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(True))
+    assert np.array_equal(g.preferred, o.preferred) and np.all(g.preferred >= 0)
+    assert g.stats["bids"] == o.stats["bids"]
+    a = L.project(arch.width, arch.height, bel_xy, units, targets)
+    bels = a.bels(units)
+    assert np.all(bels >= 0) and len(np.unique(bels)) == len(bels)
