@@ -74,3 +74,20 @@ def test_anchored_iteration_moves_towards_the_incumbent():
     d1 = np.abs(res.seed_xy - incumbent).sum(axis=1)[free].sum()
     assert res.info.get("anchored") and d1 < d0
     assert np.all(res.preferred >= 0) and legal(res, units)
+
+
+def test_anchored_iteration_projects_from_the_incumbent():
+    arch, prob, units = fabric(3)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    first = A.analytical_place(prob, units, bel_xy, mode=A.ELECTROSTATIC)
+    bels = np.full(1 + max(c for u in units for c in u.cells), -1)
+    for i, u in enumerate(units):
+        bels[u.cells] = u.choices[first.preferred[i]]
+    incumbent = np.array([bel_xy[bels[u.cells[0]]] for u in units], np.float64)
+    res = A.analytical_place(prob, units, bel_xy, anchor=(incumbent, 4, bels))
+    assert res.info["project"] == {"anchored": True}
+    assert np.all(res.preferred >= 0) and legal(res, units)
+    # a unit whose new target is its incumbent tile keeps its choice
+    for i, u in enumerate(units):
+        if len(u.choices) > 1 and np.array_equal(res.targets[i], incumbent[i].astype(np.uint32)):
+            assert res.preferred[i] == first.preferred[i]

@@ -236,3 +236,26 @@ def test_reference_composite_rows():
         assert len(set(bels.tolist())) == 5 and bels[4] == 4
         for unit in units[:2]:
             assert list(bels[unit.cells]) in rows
+
+
+def test_anchored_projection_keeps_or_improves_each_unit():
+    """project_anchored_targets (lib.rs:4157-4231): a unit already on its
+    target tile keeps its BELs; one whose target moved takes the first free
+    choice strictly closer to the target in ring order; farther units go
+    first."""
+    bel_xy = grid_bels(6, 1)                  # one BEL a tile on a 6 x 1 row
+    table = [[b] for b in range(6)]
+    units = [L.Unit([0], table, False), L.Unit([1], table, False), L.Unit([2], [[5]], False)]
+    incumbent = np.array([0, 1, 5])
+    # unit 0: target 3 (distance 3): ring 0 at 3 is free -> BEL 3
+    # unit 1: target 1 (distance 0): stays on BEL 1
+    bels = L.project_anchored(6, 1, bel_xy, units, [[3, 0], [1, 0], [5, 0]], incumbent)
+    assert list(bels) == [3, 1, 5]
+    # both target tile 4 (unit 0 from 0 at distance 4, unit 1 from 1 at 3):
+    # unit 0 goes first and takes BEL 4; unit 1 then finds 3 (distance 1 < 3)
+    bels = L.project_anchored(6, 1, bel_xy, units, [[4, 0], [4, 0], [5, 0]], incumbent)
+    assert list(bels) == [4, 3, 5]
+    # a target past a fixed BEL with nothing free closer: the incumbent stays
+    units2 = [L.Unit([0], [[0], [5]], False), L.Unit([1], [[5]], False)]
+    bels = L.project_anchored(6, 1, bel_xy, units2, [[5, 0], [5, 0]], np.array([0, 5]))
+    assert list(bels) == [0, 5]

@@ -13,9 +13,9 @@ reference runs it:
    map texo_gp_place_routable), best effort or not;
 4. `project` up to its repair (texo_gp_project).
 
-The reference projects a timing iteration's targets from the incumbent
-(`project_anchored_targets`, lib.rs:4157-4230); this pass projects them
-afresh. The repair after `project` is not part of this library.
+A timing iteration's targets are projected from the incumbent when its BELs
+are given (`project_anchored_targets`, lib.rs:4157-4231). The repair after
+`project` is not part of this library.
 """
 import copy
 from dataclasses import dataclass
@@ -49,7 +49,9 @@ def analytical_place(problem, units, bel_xy, mode=ELECTROSTATIC, params=None, an
     """One analytical placement pass. `problem` and `units` describe the same
     placement units (texo_gb300.ecp5.placement_problem builds both from a
     device snapshot); `bel_xy` [B, 2] the BEL tiles. `anchor`: (incumbent
-    unit tiles [U, 2], timing iteration). `routing_capacity`: (horizontal,
+    unit tiles [U, 2], timing iteration[, incumbent BEL of every cell]); with
+    the BELs the targets are projected from the incumbent
+    (`project_anchored_targets`), else afresh. `routing_capacity`: (horizontal,
     vertical) [H, W] channel capacities for the routability rounds."""
     W, H = problem.width, problem.height
     cx, cy = W // 2, H // 2
@@ -80,7 +82,7 @@ def analytical_place(problem, units, bel_xy, mode=ELECTROSTATIC, params=None, an
     info["seed"] = {"x_iterations": sx["iterations"], "y_iterations": sy["iterations"]}
     solved = np.stack([x, y], 1)
     if anchor is not None:
-        anchor_xy, iteration = anchor
+        anchor_xy, iteration = anchor[0], anchor[1]
         dx = seed.axis_system(seed_problem, solved, 0, fixed)[0]
         dy = seed.axis_system(seed_problem, solved, 1, fixed)[0]
         wx, wy = seed.anchor_weights(seed_problem, solved, anchor_xy, iteration, dx, dy, fixed)
@@ -113,6 +115,18 @@ def analytical_place(problem, units, bel_xy, mode=ELECTROSTATIC, params=None, an
             info["routable"] = rep
         info["placement"] = {"iterations": st["iterations"], "converged": st["converged"], "hpwl": st["hpwl"],
                              "overflow": st["overflow"]}
+    if anchor is not None and len(anchor) > 2:
+        # a timing iteration with the incumbent's cell BELs: project from it
+        bels = legalize.project_anchored(W, H, bel_xy.astype(np.int64), units, targets, anchor[2])
+        pos = {}
+        preferred = np.full(U, -1, dtype=np.int64)
+        for i, u in enumerate(units):
+            key = id(u.choices)
+            if key not in pos:
+                pos[key] = {tuple(int(b) for b in a): c for c, a in enumerate(u.choices)}
+            preferred[i] = pos[key][tuple(int(b) for b in bels[u.cells])]
+        info["project"] = {"anchored": True}
+        return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), preferred, info)
     proj = legalize.project(W, H, bel_xy, units, targets)
     info["project"] = proj.stats
     return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), proj.preferred, info)

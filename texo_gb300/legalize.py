@@ -497,3 +497,64 @@ def project_native(width, height, bel_xy, units, targets, cost_scale=0, device=0
     abi.check(code, "texo_gp_project")
     stats = {f: getattr(st, f) for f, _ in abi.ProjectionStats._fields_ if f != "reserved"}
     return Projection(out[:U].astype(np.int64), None, stats)
+
+
+def spatial_choices_within(by_point, center, max_distance, width, height):
+    """`spatial_choices_within` (lib.rs:3789-3811): the choices anchored at
+    every tile up to Manhattan distance `max_distance` of `center`, ring by
+    ring in the ring-walk order."""
+    max_radius = int(min(max_distance, width + height))
+    out = []
+    cx, cy = int(center[0]), int(center[1])
+    for radius in range(max_radius + 1):
+        for dy in range(radius + 1):
+            dx = radius - dy
+            for y in ring_coordinates(cy, dy, height):
+                for x in ring_coordinates(cx, dx, width):
+                    out.extend(by_point[y * width + x])
+    return out
+
+
+def project_anchored(width, height, bel_xy, units, targets, incumbent):
+    """`project_anchored_targets` (lib.rs:4157-4231): a timing iteration's
+    targets projected from the legal incumbent (`incumbent`: the BEL of every
+    cell). Every unit starts on its incumbent BELs; units in order of
+    decreasing distance from their incumbent origin to their target (then
+    index) with more than one choice and a nonzero distance are lifted and
+    take the first free choice strictly closer to the target (the choices
+    within distance - 1 in ring order), else their incumbent again.
+    Occupancy is the only legality rule. Returns the BEL of every cell."""
+    bel_xy = np.asarray(bel_xy, dtype=np.int64).reshape(-1, 2)
+    placed = np.asarray(incumbent, dtype=np.int64).copy()
+    occupied = np.zeros(bel_xy.shape[0], dtype=bool)
+    tg = np.asarray(targets, dtype=np.int64).reshape(-1, 2)
+    for unit in units:
+        occupied[placed[unit.cells]] = True
+
+    def dist(u):
+        ox, oy = bel_xy[placed[units[u].cells[0]]]
+        return abs(int(ox) - int(tg[u][0])) + abs(int(oy) - int(tg[u][1]))
+    order = sorted(range(len(units)), key=lambda u: (-dist(u), u))
+    index_cache = {}
+    for u in order:
+        unit = units[u]
+        if len(unit.choices) == 1:
+            continue
+        old = placed[unit.cells].copy()
+        ox, oy = bel_xy[old[0]]
+        distance = abs(int(ox) - int(tg[u][0])) + abs(int(oy) - int(tg[u][1]))
+        if distance == 0:
+            continue
+        occupied[old] = False
+        key = id(unit.choices)
+        if key not in index_cache:
+            index_cache[key] = _by_point(bel_xy, width, height, unit.choices)
+        chosen = old
+        for c in spatial_choices_within(index_cache[key], tg[u], distance - 1, width, height):
+            a = np.asarray(unit.choices[c], dtype=np.int64)
+            if not occupied[a].any():
+                chosen = a
+                break
+        placed[unit.cells] = chosen
+        occupied[chosen] = True
+    return placed
