@@ -95,3 +95,37 @@ def test_crowded_batch_is_deterministic(chunk):
         assert s["status"] == s0["status"]
         assert t is not None and np.array_equal(t, t0), "copy %d diverged" % i
         assert s["iterations"] == s0["iterations"] and s["hpwl"] == s0["hpwl"]
+
+
+def test_batch_of_multi_field_macro_problems_equals_alone():
+    """Jobs with two density fields, two-member macros, fixed occupancy and
+    timed arcs (rich_problems), and ECP5-adapter problems (LUT-FF pairs,
+    carry chains, units without density members), batched with a synthetic
+    job: each gives its result alone, bit for bit."""
+    from rich_problems import rich_problem
+    from texo_gb300 import ecp5
+    probs = [rich_problem(0), rich_problem(3, side=40, cells=1300, io=80, nets=1600)]
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(16, 16))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, 2, luts=500, ffs=250, lut_ff_pairs=150,
+                                                   carry=((12, 4), (6, 6)), io=24)
+    probs.append(ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)[0])
+    probs.append(P.synthetic(36, 1100, 60, 1300, 6.0, 4))
+    alone = [Placer(p, params()).run(allow_nonconverged=True) for p in probs]
+    b = Batch(params())
+    for i, p in enumerate(probs):
+        assert b.admit(p, 200 + i)
+    got = {}
+    for _ in range(400):
+        b.advance(9)
+        while True:
+            r = b.retire()
+            if r is None:
+                break
+            got[r[0]] = r
+        if len(got) == len(probs):
+            break
+    assert len(got) == len(probs)
+    for i, (t, _, s) in enumerate(alone):
+        _, tb, sb = got[200 + i]
+        assert np.array_equal(t, tb), "job %d differs in the mix" % i
+        assert sb["iterations"] == s["iterations"] and sb["hpwl"] == s["hpwl"]

@@ -208,3 +208,25 @@ def test_controller_trace_matches_oracle_config0():
 
 def test_controller_trace_matches_oracle_rich():
     check_trace(rich_problem(0), dict(best_effort=1))
+
+
+def test_rich_problem_at_scale_scatter_and_evaluation():
+    """The same features at 12,000 cells on a 128 x 128 fabric with two BELs
+    of each kind a tile (two fields, macros, fixed exchangeable occupancy,
+    timed arcs), on the tile grid and on a 256 x 256 bin grid."""
+    prob = rich_problem(5, side=128, cells=12000, io=240, nets=14400, sigma=8.0, capacity=2)
+    assert len(prob.fields) == 2 and prob.fixed_occupancy.shape[0] > 0 and prob.arc_driver_cell.size > 0
+    check_evaluation(prob, dict(best_effort=1), 7, 2.0)
+    check_evaluation(prob, dict(best_effort=1, bins_x=256, bins_y=256, target_density=0.9), 8, 4.0)
+
+
+def test_ecp5_adapter_problem_evaluation():
+    """A placement problem built by the ECP5 adapter (LUT-FF pairs, carry
+    chains, units without density members, fixed IO) on a 24 x 24 fabric of
+    8 LUT4 and 8 FF a tile: grids bit-exact, evaluation within 1e-5."""
+    from texo_gb300 import ecp5
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(24, 24))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, 4, luts=1200, ffs=600, lut_ff_pairs=400,
+                                                   carry=((30, 4), (10, 6)), io=40)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds, sink_weights={(0, 0): 3, (5, 1): 2})
+    check_evaluation(prob, dict(best_effort=1), 9, 1.0)
