@@ -1107,11 +1107,13 @@ struct Controller {
   // The device engine: the same loop inside one persistent cooperative kernel.
   DevRun& hr;                 // the pinned mirror's controller state
   bool dev_ready = false;
-  // The device-engine step captured as a CUDA graph on first use (the
-  // descriptor it was captured with is kept: a different one recaptures),
-  // and the CUDA events that time the step's device work.
+  // The device-engine step captured as a CUDA graph once it repeats (the
+  // descriptor it was captured with is kept: a different one recaptures; a
+  // one-shot placement, a single step to convergence, pays no capture), and
+  // the CUDA events that time the step's device work.
   cudaGraphExec_t step_exec = nullptr;
   bool step_graph_off = false;
+  unsigned device_steps = 0;
   Dev step_dev{};
   cudaEvent_t step_ev[2] = {nullptr, nullptr};
   double device_ms = -1.0;    // device time of the last device-engine step
@@ -1174,7 +1176,7 @@ struct Controller {
       cudaGraphExecDestroy(step_exec);
       step_exec = nullptr;
     }
-    if (!step_exec && !step_graph_off) {
+    if (!step_exec && !step_graph_off && device_steps++ > 0) {
       if (capture_persistent(I.d, I.r, buffers(), I.run_dev, I.h_run, blocks, I.nvb, I.stream, &step_exec))
         step_graph_off = true;   // the direct launch below takes over
       else
