@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <thread>
 
 #include "engine.h"
@@ -125,7 +126,6 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     }
     return TEXO_GP_OK;
   };
-  hyper_status = hyper_check();
   const size_t arcs = p->num_timed_arcs;
   auto pin_of = [&](uint32_t cell, int& unit, double& bx, double& by) {
     if (p->cell_fixed[cell]) {
@@ -150,7 +150,7 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   auto cls = [](uint32_t deg) {
     return deg <= 2 ? 0 : deg <= 4 ? 1 : deg <= 8 ? 2 : deg <= 16 ? 3 : deg <= 32 ? 4 : 5;
   };
-  const size_t pins = (E && !hyper_status) ? p->net_ptr[E] : 0;
+  size_t pins = 0;   // set once the hypergraph is validated
   std::vector<double> pin_count(U, 0.0);
   bool layout_ok = true;
   auto layout = [&]() {
@@ -210,16 +210,32 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   // buffers of this thread's pass over the nets (further below)
   std::vector<double> wl(U, 0.0), inc(C, 0.0), pin_weight_sum(U, 0.0);
   std::vector<uint32_t> unit_seen(U, ~0u), cell_seen(C, ~0u);
-  // small problems are not worth a thread; the guard joins the thread on
-  // every way out of this function, an early error return included
+  // Large hypergraphs are validated and laid out on a second thread while
+  // this one builds the density side; small problems are not worth a thread.
+  // The guards join the threads on every way out of this function, an early
+  // error return included. Every sum keeps its order, so the threading
+  // changes no value.
   struct Joiner {
     std::thread t;
     ~Joiner() {
       if (t.joinable()) t.join();
     }
-  } layout_thread;
-  const bool threaded = !hyper_status && pins >= 65536;
-  if (threaded) layout_thread.t = std::thread(layout);
+  } layout_thread, smooth_thread;
+  const bool threaded = E && p->net_ptr && p->pin_cell && p->net_ptr[E] >= 65536;
+  std::promise<void> hyper_checked;
+  std::future<void> hyper_ready = hyper_checked.get_future();
+  auto check_and_layout = [&]() {
+    hyper_status = hyper_check();
+    pins = (E && !hyper_status) ? p->net_ptr[E] : 0;
+    hyper_checked.set_value();
+    if (!hyper_status) layout();
+  };
+  if (threaded) {
+    layout_thread.t = std::thread(check_and_layout);
+  } else {
+    hyper_status = hyper_check();
+    pins = (E && !hyper_status) ? p->net_ptr[E] : 0;
+  }
   // capacity minus fixed occupancy (electrostatic_placement.rs:146-172)
   std::vector<std::vector<uint32_t>> caps(p->num_fields);
   for (uint32_t f = 0; f < p->num_fields; ++f)
@@ -247,20 +263,29 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
   if (m.K > (uint32_t)kMaxFields) return TEXO_GP_ERR_UNSUPPORTED;
   m.available.assign(m.K, 0);
   m.smoothed.assign(m.K, std::vector<double>());
-  for (uint32_t f = 0; f < m.K; ++f) {
+  for (uint32_t f = 0; f < m.K; ++f)
     for (auto c : m.cap[f]) m.available[f] += c;
-    m.smoothed[f].assign((size_t)m.Wb * m.Hb, 0.0);
-    for (size_t i = 0; i < tiles; ++i) {
-      const uint32_t c = m.cap[f][i];
-      if (!c) continue;
-      double bx = (double)(uint32_t)(i % m.W), by = (double)(uint32_t)(i / m.W);
-      if (!m.identity) {
-        bx = (bx + 0.5) * m.sx - 0.5;
-        by = (by + 0.5) * m.sy - 0.5;
+  // the smoothed capacity (a third thread on large problems; nothing below
+  // reads it)
+  auto smooth = [&]() {
+    for (uint32_t f = 0; f < m.K; ++f) {
+      m.smoothed[f].assign((size_t)m.Wb * m.Hb, 0.0);
+      for (size_t i = 0; i < tiles; ++i) {
+        const uint32_t c = m.cap[f][i];
+        if (!c) continue;
+        double bx = (double)(uint32_t)(i % m.W), by = (double)(uint32_t)(i / m.W);
+        if (!m.identity) {
+          bx = (bx + 0.5) * m.sx - 0.5;
+          by = (by + 0.5) * m.sy - 0.5;
+        }
+        deposit64(m.smoothed[f], m.Wb, m.Hb, bx, by, m.td * (double)c);
       }
-      deposit64(m.smoothed[f], m.Wb, m.Hb, bx, by, m.td * (double)c);
     }
-  }
+  };
+  if (threaded)
+    smooth_thread.t = std::thread(smooth);
+  else
+    smooth();
   // density units and members (eplace.rs:261-301)
   m.U = U;
   m.unit_mem_ptr.assign(U + 1, 0);
@@ -370,8 +395,9 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     m.hi[i + 1] = (double)(m.H - 1);
   }
   for (size_t i = 0; i < 2 * nobj; ++i) m.init[i] = clampd(m.init[i], m.lo[i], m.hi[i]);
-  // hypergraph (validated and laid out above): report its errors here, in
+  // hypergraph (validated and laid out beside): report its errors here, in
   // the reference's order
+  if (threaded) hyper_ready.wait();
   if (hyper_status) {
     *err = hyper_err;
     return hyper_status;
@@ -417,8 +443,12 @@ int32_t build_model(const texo_gp_problem* p, const texo_gp_params* prm, HostMod
     pin_weight_sum[du] += w;
     pin_weight_sum[su] += w;
   }
-  if (threaded) layout_thread.t.join();
-  else layout();
+  if (threaded) {
+    layout_thread.t.join();
+    smooth_thread.t.join();
+  } else {
+    layout();
+  }
   if (!layout_ok) return TEXO_GP_ERR_INVALID_ARGUMENT;
   for (uint32_t u = 0; u < U; ++u) pin_weight_sum[u] += pin_count[u];
   m.n_classes = kNetClasses + 1;
