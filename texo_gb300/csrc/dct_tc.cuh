@@ -36,14 +36,22 @@
 // columns x K) a grid of 64 x 32 blocks; a block stores its four slices one
 // after another, blocks ordered K-chunk fastest, zero-padded.
 //
-// One 128 x 64 output tile per block iteration. Thread 0 runs a four-stage
-// pipeline: TMA tensor copies (cp.async.bulk.tensor through the operands'
-// tensor maps, complete_tx on a "full" mbarrier) keep the next three K-chunks
-// in flight while the twenty MMAs of chunk c (two K = 16 steps x ten slice
-// pairs) run, and each commit arrives on that stage's "empty" mbarrier
-// before the stage is reloaded. The four accumulators occupy 4 x 64 TMEM
-// columns (row i = lane i); the epilogue reads them with tcgen05.ld, warp w
-// taking lanes 32 (w mod 4) ... + 31 and columns 32 (w / 4) ... + 31.
+// One 128 x 64 output tile per block iteration, on a four-stage pipeline of
+// two threads: thread 0 issues the TMA tensor copies (cp.async.bulk.tensor
+// through the operands' tensor maps, complete_tx on a stage's "full"
+// mbarrier), thread 32 the MMAs of each chunk and a commit to the stage's
+// "empty" mbarrier, which releases the stage to the next copy. The four B
+// slices of a block lie one after another in the K-major layout, so their
+// first 64 (4 - i) rows read as one operand of slices 0 .. 3 - i: one MMA of
+// N = 64 (4 - i) multiplies A slice i by all of them, into TMEM columns
+// 64 i ..., which puts A_i B_j on accumulator i + j (columns 64 (i + j)).
+// Eight MMAs of N = 256, 192, 128, 64 a chunk (two K = 16 steps x four A
+// slices) instead of twenty of N = 64: a tcgen05.mma of N = 64 costs the
+// tensor pipe far more than a quarter of one of N = 256. The four
+// accumulators occupy 4 x 64 TMEM columns (row i = lane i); the epilogue
+// reads them with tcgen05.ld, warp w taking lanes 32 (w mod 4) ... + 31 and
+// columns 32 (w / 4) ... + 31, and turns them through shared memory for
+// row-wise global accesses.
 //
 // Every wait is bounded. When one runs out the block records it (shared
 // `failed` and the caller's error word), waits once more (bounded) for its
@@ -61,15 +69,13 @@ namespace tgp {
 namespace tc {
 
 constexpr int kM = 128;                        // accumulator rows (TMEM lanes)
-#ifndef TGP_TC_N
-#define TGP_TC_N 64
-#endif
-constexpr int kN = TGP_TC_N;                   // accumulator columns per tile (64 or 128)
+constexpr int kN = 64;                         // accumulator columns per tile
 constexpr int kKC = 32;                        // K per block / pipeline stage
-constexpr int kStages = kN == 64 ? 4 : 3;     // chunks in flight (TMA prefetch depth)
+constexpr int kStages = 4;                     // chunks in flight (TMA prefetch depth)
 constexpr int kSlices = 4;                     // 8-bit integer slices per value
 constexpr int kLevels = 4;                     // accumulators: slice pairs with i + j = level
-constexpr uint32_t kCols = kLevels * kN;       // TMEM columns per block
+constexpr uint32_t kCols = kLevels * kN;       // TMEM columns per block: accumulator L at kN L
+static_assert(kSlices == kLevels, "A slice i meets B slices 0 .. kLevels - 1 - i");
 constexpr uint32_t kCore = 128;                // one 8 x 16 B core matrix
 constexpr uint32_t kSbo = (kKC / 8) * kCore;   // next 8-row group
 constexpr uint32_t kLbo = kCore;               // next 8-element K group
@@ -80,8 +86,9 @@ constexpr uint32_t kBBlock = kSlices * kBSlice;
 constexpr uint32_t kTx = (kABlock + kBBlock) * 2u;  // bytes per stage
 constexpr unsigned kWaitLimit = 1u << 22;      // mbarrier polls before giving up
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N, M.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) |
-                            ((uint32_t)(kM >> 4) << 24);
+__host__ __device__ constexpr uint32_t idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
 
 // TMA descriptors of the sliced operands, each a 2-D view of one operand
 // buffer as rows of 128 bytes (64 bf16 values): an A block is a 64 x 256 box
@@ -181,10 +188,17 @@ struct alignas(128) Stage {
 struct alignas(128) Smem {
   Stage st[kStages];
   unsigned long long full[kStages], empty[kStages];
+  unsigned long long done;   // every MMA of the tile has completed
   uint32_t tmem;
-  uint32_t full_ph[kStages], empty_ph[kStages];   // completed phases waited on (thread 0)
+  uint32_t issued, consumed;   // chunks copied / taken by the MMA issuer (the cleanup after a failure)
   int failed;
 };
+// The epilogue stages each warp's 32 rows x kN/2 columns of (hi, lo) pairs
+// in the pipeline's shared memory (free once the tile's MMAs completed) to
+// write and read global memory a row at a time.
+constexpr int kEpiCols = kN / 2;
+constexpr int kEpiStride = kEpiCols + 1;   // pairs per staged row (conflict-free both ways)
+static_assert(8 * 32 * kEpiStride * 8 <= (int)(kStages * sizeof(Stage)), "epilogue staging fits the stages");
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -198,13 +212,19 @@ __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::aft
 // generic-proxy global writes ordered with later TMA (async-proxy) reads
 __device__ __forceinline__ void fence_global_async() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
-__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
+// One MMA (M = 128, K = 16, N in the descriptor), accumulating into D when acc != 0.
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      "l"(a), "l"(b), "r"(id), "r"(acc)
       : "memory");
 }
+__device__ __forceinline__ void commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+// generic-proxy shared-memory accesses ordered with later TMA writes
+__device__ __forceinline__ void fence_shared_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ bool try_wait(uint32_t mbar, uint32_t parity) {
   uint32_t ok;
@@ -237,11 +257,11 @@ __device__ __forceinline__ void setup(Smem& sm) {
     for (int i = 0; i < kStages; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.full[i])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.empty[i])) : "memory");
-      sm.full_ph[i] = 0;
-      sm.empty_ph[i] = 0;
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.done)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sm.failed = 0;
+    sm.issued = sm.consumed = 0;
   }
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&sm.tmem)),
@@ -283,7 +303,6 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* v) {
 // next slice phase needs for epi 0 and 1 (a B operand's rows are the grid's
 // columns), or the FP32 potential with the energy <rho, phi> (epi 3).
 struct Out {
-  int epi;
   float2* tp;            // [K][M][N] pair grid (epi 0..2)
   unsigned* mx;          // column maxima [K][N] for the next B operand (epi 0, 1)
   float* phi;            // epi 3
@@ -298,145 +317,182 @@ struct Out {
 // C[f] = A[f] (M x K) * B[f]^T, B given as N x K, both sliced; output tiles
 // t = vb, vb + nvb, ... of 128 x 64, written by `out`. kp = K padded to 32.
 // The block must have called setup(); blockDim.x must be 256.
+//
+// Thread 0 copies K-chunks into the stages, each copy waiting for the MMAs
+// that last read its stage (the stage's "empty" commit); thread 32 issues the
+// MMAs of each chunk once its copy landed ("full") and commits them to the
+// stage's "empty" barrier without waiting, so the tensor pipe keeps up to
+// kStages chunks queued. Chunk counters run on across the block's tiles, so
+// the k-th use of a stage waits for the (k-1)-th release. After the last
+// chunk the issuer commits to "done" and waits for it; then the block runs
+// the epilogue: each warp moves its 32 x 32 accumulator block from tensor
+// memory (lane = row) through shared memory (lane = column), so that every
+// global load and store of the epilogue covers a row segment.
+template <int EPI>
 static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* mB, long sb, int M, int N, int kp,
                             int nf, const Out& out, double* eacc, int vb, int nvb, Smem& sm, unsigned long long* err) {
   const int tiles_m = (M + kM - 1) / kM, tiles_n = (N + kN - 1) / kN;
   const int tiles = tiles_m * tiles_n * nf;
   const int nkc = kp / kKC;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int* failed = &sm.failed;
+  auto fail = [&]() {
+    *failed = 1;
+    if (err) atomicExch(err, 1ull);
+  };
+  uint32_t gp = 0, gm = 0, done_ph = 0;   // thread 0's copies, thread 32's chunks and tiles
   __syncthreads();
   for (int t = vb; t < tiles; t += nvb) {
-    if (sm.failed) break;
+    if (*failed) break;
     const int f = t / (tiles_m * tiles_n);
     const int rr = t % (tiles_m * tiles_n);
     const int mt = rr / tiles_n, nt = rr % tiles_n;
     if (threadIdx.x == 0) {
       fence_global_async();
+      fence_shared_async();
       // first 128-byte row of this tile's K-chunk 0 in each operand
       const int a0 = (int)(((size_t)f * sa + (size_t)mt * nkc * kABlock) / 64);
       const int b0 = (int)(((size_t)f * sb + (size_t)nt * nkc * kBBlock) / 64);
-      bool bad = false;
-      bool busy[kStages], loading[kStages];   // a commit / a copy not yet waited for
-      for (int s = 0; s < kStages; ++s) busy[s] = loading[s] = false;
-      auto wait_empty = [&](int s) {
-        if (!busy[s] || bad) return;
-        if (wait_phase(saddr(&sm.empty[s]), sm.empty_ph[s] & 1u)) {
-          ++sm.empty_ph[s];
-          busy[s] = false;
-        } else {
-          bad = true;
+      for (int c = 0; c < nkc; ++c) {
+        if (*failed) break;
+        const uint32_t s = gp % kStages;
+        if (gp >= (uint32_t)kStages && !wait_phase(saddr(&sm.empty[s]), (gp / kStages - 1) & 1u)) {
+          fail();
+          break;
         }
-      };
-      auto produce = [&](int c) {
-        const int s = c % kStages;
-        wait_empty(s);
-        if (bad) return;
         const uint32_t fb = saddr(&sm.full[s]);
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(kTx) : "memory");
         tensor_load(saddr(sm.st[s].a), mA, a0 + c * (int)(kABlock / 64), fb);
         tensor_load(saddr(sm.st[s].b), mB, b0 + c * (int)(kBBlock / 64), fb);
-        loading[s] = true;
-      };
-      for (int c = 0; c < kStages - 1 && c < nkc; ++c) produce(c);
-      for (int c = 0; c < nkc && !bad; ++c) {
-        const int s = c % kStages;
-        if (!wait_phase(saddr(&sm.full[s]), sm.full_ph[s] & 1u)) {
-          bad = true;
+        ++gp;
+      }
+      sm.issued = gp;
+    } else if (threadIdx.x == 32) {
+      for (int c = 0; c < nkc; ++c) {
+        if (*failed) break;
+        const uint32_t s = gm % kStages;
+        if (!wait_phase(saddr(&sm.full[s]), (gm / kStages) & 1u)) {
+          fail();
           break;
         }
-        ++sm.full_ph[s];
-        loading[s] = false;
+        ++gm;
         fence_after();
         const uint32_t abase = saddr(sm.st[s].a), bbase = saddr(sm.st[s].b);
 #pragma unroll
         for (int q = 0; q < kKC / 16; ++q) {
           const uint32_t ko = (uint32_t)q * 2u * kCore;   // two K groups of 8 per MMA
+          const uint64_t bd = sdesc(bbase + ko);          // B slices 0..3 as 4 kN rows
 #pragma unroll
-          for (int i = 0; i < kSlices; ++i)
-#pragma unroll
-            for (int j = 0; j < kSlices; ++j)
-              if (i + j < kLevels) {
-                // the first product of each accumulator (i = 0) starts it afresh
-                const uint32_t acc = (c > 0 || q > 0 || i > 0) ? 1u : 0u;
-                mma(sm.tmem + (uint32_t)((i + j) * kN), sdesc(abase + i * kASlice * 2u + ko),
-                    sdesc(bbase + j * kBSlice * 2u + ko), acc);
-              }
-        }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         saddr(&sm.empty[s]))
-                     : "memory");
-        busy[s] = true;
-        // with chunk c queued on the tensor pipe, reload the stage of chunk
-        // c - 1 (its MMAs finish first) with chunk c + kStages - 1
-        if (c + kStages - 1 < nkc) produce(c + kStages - 1);
-      }
-      for (int s = 0; s < kStages; ++s) wait_empty(s);   // every MMA of the tile has completed
-      if (bad) {
-        sm.failed = 1;
-        if (err) atomicExch(err, 1ull);
-        // one more bounded wait for the copies and MMAs still in flight
-        for (int s = 0; s < kStages; ++s) {
-          if (loading[s]) wait_phase(saddr(&sm.full[s]), sm.full_ph[s] & 1u);
-          if (busy[s]) wait_phase(saddr(&sm.empty[s]), sm.empty_ph[s] & 1u);
-        }
-      }
-    }
-    __syncthreads();
-    if (sm.failed) break;
-    fence_after();
-    // epilogue: this warp's 32 rows x 32 columns of the tile
-    const int q = warp & 3, h = warp >> 2;
-    const int row = mt * kM + q * 32 + lane;
-    const bool row_ok = row < M;
-    const float row_scale = pow2f((row_ok ? out.eA[(size_t)f * out.sa_e + row] : 0) - 14);
-    float e = 0.f;
-#pragma unroll
-    for (int part = 0; part < kN / 32; ++part) {
-      uint32_t v[kLevels][16];
-#pragma unroll
-      for (int L = 0; L < kLevels; ++L)
-        ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * kN + h * (kN / 2) + part * 16), v[L]);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int col = nt * kN + h * (kN / 2) + part * 16 + j;
-        const bool ok = row_ok && col < N;
-        // join the exact level sums: a0 + 2^-8 a1 + 2^-16 a2 + 2^-24 a3
-        float s, r;
-        two_sum(__uint_as_float(v[0][j]), __uint_as_float(v[1][j]) * 0x1p-8f, s, r);
-        r += __uint_as_float(v[2][j]) * 0x1p-16f;
-        r += __uint_as_float(v[3][j]) * 0x1p-24f;
-        float hi, lo;
-        two_sum(s, r, hi, lo);
-        const float sc = row_scale * pow2f(col < N ? out.eB[(size_t)f * out.sb_e + col] : 0);
-        hi *= sc;
-        lo *= sc;
-        unsigned cbits = 0;
-        if (ok) {
-          const size_t idx = (size_t)row * N + col;
-          if (out.epi == 3) {
-            const float p = hi + lo;
-            out.phi[(size_t)f * M * N + idx] = p;
-            e = fmaf(out.rho[(size_t)f * M * N + idx], p, e);
-          } else {
-            if (out.epi == 1) {   // (hi + lo)(ie_hi + ie_lo) in double-float
-              const float ih = out.ie_hi[idx], il = out.ie_lo[idx];
-              const float p = hi * ih;
-              float pe = fmaf(hi, ih, -p);
-              pe = fmaf(hi, il, fmaf(lo, ih, pe));
-              two_sum(p, pe, hi, lo);
-            }
-            out.tp[(size_t)f * M * N + idx] = make_float2(hi, lo);
-            cbits = __float_as_uint(fabsf(hi));
+          for (int i = 0; i < kSlices; ++i) {
+            // A slice i times B slices 0 .. 3 - i (the first kN (4 - i) rows)
+            // into columns kN i ...: A_i B_j lands on accumulator i + j. The
+            // first MMA of the tile starts accumulators 0..3 afresh.
+            const uint32_t acc = (c > 0 || q > 0 || i > 0) ? 1u : 0u;
+            mma(sm.tmem + (uint32_t)(i * kN), sdesc(abase + i * kASlice * 2u + ko), bd, idesc(kN * (kLevels - i)),
+                acc);
           }
         }
-        if (out.epi == 0 || out.epi == 1) {   // column maxima: one atomic per column and warp
-          const unsigned m = __reduce_max_sync(0xffffffffu, cbits);
-          if (lane == 0 && m && col < N) atomicMax(out.mx + (size_t)f * N + col, m);
+        commit(saddr(&sm.empty[s]));
+      }
+      // every MMA issued so far (a failure included) completes before the
+      // epilogue or the teardown touches tensor memory
+      commit(saddr(&sm.done));
+      if (!wait_phase(saddr(&sm.done), done_ph & 1u)) fail();
+      ++done_ph;
+      sm.consumed = gm;
+      fence_before();
+    }
+    __syncthreads();
+    if (*failed) {
+      // one more bounded wait for the copies still in flight
+      if (threadIdx.x == 0)
+        for (uint32_t g = sm.consumed; g < sm.issued; ++g)
+          wait_phase(saddr(&sm.full[g % kStages]), (g / kStages) & 1u);
+      break;
+    }
+    fence_after();
+    // epilogue. This warp's block: 32 rows (TMEM lanes 32 q ...) x 32 columns
+    // (h). Its global inputs (epi 1: 1 / lambda pairs, epi 3: rho), one row
+    // per step with lane = column, are loaded first, so that their latency
+    // overlaps the accumulators' staging.
+    const int q = warp & 3, h = warp >> 2;
+    const int rows = min(32, M - (mt * kM + q * 32));
+    const int col = nt * kN + h * kEpiCols + lane;
+    const bool col_ok = col < N;
+    float in0[32], in1[32];
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      in0[r] = in1[r] = 0.f;
+      if (r < rows && col_ok) {
+        const size_t idx = (size_t)(mt * kM + q * 32 + r) * N + col;
+        if constexpr (EPI == 3) {
+          in0[r] = out.rho[(size_t)f * M * N + idx];
+        } else if constexpr (EPI == 1) {
+          in0[r] = out.ie_hi[idx];
+          in1[r] = out.ie_lo[idx];
         }
       }
     }
-    if (out.epi == 3) eacc[f] += (double)e;
+    // first half: lane = row, the four accumulators joined and scaled by
+    // the row, into this warp's staging rows
+    float2* stage = reinterpret_cast<float2*>(&sm.st[0]) + (size_t)warp * 32 * kEpiStride;
+    {
+      const int row = mt * kM + q * 32 + lane;
+      const float row_scale = pow2f((row < M ? out.eA[(size_t)f * out.sa_e + row] : 0) - 14);
+#pragma unroll
+      for (int part = 0; part < kEpiCols / 16; ++part) {
+        uint32_t v[kLevels][16];
+#pragma unroll
+        for (int L = 0; L < kLevels; ++L)
+          ld16(sm.tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(L * kN + h * kEpiCols + part * 16), v[L]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          // join the exact level sums: a0 + 2^-8 a1 + 2^-16 a2 + 2^-24 a3
+          float s, r;
+          two_sum(__uint_as_float(v[0][j]), __uint_as_float(v[1][j]) * 0x1p-8f, s, r);
+          r += __uint_as_float(v[2][j]) * 0x1p-16f;
+          r += __uint_as_float(v[3][j]) * 0x1p-24f;
+          float hi, lo;
+          two_sum(s, r, hi, lo);
+          stage[lane * kEpiStride + part * 16 + j] = make_float2(hi * row_scale, lo * row_scale);
+        }
+      }
+    }
+    __syncwarp();
+    // second half: lane = column, a row of the warp's block per step
+    float e = 0.f;
+    if (col_ok) {
+      const float col_scale = pow2f(out.eB[(size_t)f * out.sb_e + col]);
+      unsigned cmax = 0;
+#pragma unroll
+      for (int r = 0; r < 32; ++r) {
+        if (r >= rows) break;
+        const size_t idx = (size_t)(mt * kM + q * 32 + r) * N + col;
+        const float2 pr = stage[r * kEpiStride + lane];
+        float hi = pr.x * col_scale, lo = pr.y * col_scale;
+        if constexpr (EPI == 3) {
+          const float p = hi + lo;
+          out.phi[(size_t)f * M * N + idx] = p;
+          e = fmaf(in0[r], p, e);
+        } else {
+          if constexpr (EPI == 1) {   // (hi + lo)(ie_hi + ie_lo) in double-float
+            const float ih = in0[r], il = in1[r];
+            const float p = hi * ih;
+            float pe = fmaf(hi, ih, -p);
+            pe = fmaf(hi, il, fmaf(lo, ih, pe));
+            two_sum(p, pe, hi, lo);
+          }
+          out.tp[(size_t)f * M * N + idx] = make_float2(hi, lo);
+          cmax = max(cmax, __float_as_uint(fabsf(hi)));
+        }
+      }
+      // column maxima: one atomic per column and warp
+      if constexpr (EPI == 0 || EPI == 1)
+        if (cmax) atomicMax(out.mx + (size_t)f * N + col, cmax);
+    }
+    if constexpr (EPI == 3) eacc[f] += (double)e;
+    fence_shared_async();   // the staging writes before the next tile's copies
     fence_before();
     __syncthreads();
   }
@@ -454,7 +510,10 @@ __device__ __forceinline__ unsigned* tmx_of(const Dev& d, int which) {
 }
 
 // One of the four GEMM passes of the spectral solve.
-static __device__ void dct_pass(const Dev& d, const TcMaps& tm, int step, int vb, int nvb, Smem& sm, double* eacc,
+// Each pass is its own kernel instance (STEP = the pass), so that an
+// instance holds only its own epilogue's code.
+template <int STEP>
+static __device__ void dct_pass(const Dev& d, const TcMaps& tm, int vb, int nvb, Smem& sm, double* eacc,
                                 unsigned long long* err) {
   const int W = d.g.Wb, H = d.g.Hb;
   const long sA = (long)a_elems(H, W, 1), sB = (long)b_elems(W, H, 1);
@@ -462,42 +521,33 @@ static __device__ void dct_pass(const Dev& d, const TcMaps& tm, int step, int vb
   o.tp = d.tp;
   o.ie_hi = d.inv_eig;
   o.ie_lo = d.inv_eig_lo;
-  switch (step) {
-    case 0:   // t1 = rho Cx^T: A = rho (rows y), B = rows of Cx (frequency kx)
-      o.epi = 0;
-      o.mx = tmx_of(d, 0);
-      o.eA = d.eA, o.sa_e = d.Hp128;
-      o.eB = d.eCx, o.sb_e = 0;
-      gemm(&tm.m[TM_OPA], sA, &tm.m[TM_CXB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
-      break;
-    case 1:   // t2 = (Cy t1) / lambda: A = rows of Cy (ky), B = t1 columns (kx)
-      o.epi = 1;
-      o.mx = tmx_of(d, 1);
-      o.eA = d.eCy, o.sa_e = 0;
-      o.eB = d.eB, o.sb_e = d.Wp64;
-      gemm(&tm.m[TM_CYA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
-      break;
-    case 2:   // t3 = Cy^T t2: A = rows of Cy^T (y), B = t2 columns (kx)
-      o.epi = 2;
-      o.eA = d.eCy + d.g.Hb, o.sa_e = 0;
-      o.eB = d.eB, o.sb_e = d.Wp64;
-      gemm(&tm.m[TM_CYTA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
-      break;
-    default:  // phi = t3 Cx: A = t3 (rows y), B = rows of Cx^T (x)
-      o.epi = 3;
-      o.phi = d.phi;
-      o.rho = d.rho;
-      o.eA = d.eA, o.sa_e = d.Hp128;
-      o.eB = d.eCx + d.g.Wb, o.sb_e = 0;
-      gemm(&tm.m[TM_OPA], sA, &tm.m[TM_CXTB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
-      break;
+  if constexpr (STEP == 0) {   // t1 = rho Cx^T: A = rho (rows y), B = rows of Cx (frequency kx)
+    o.mx = tmx_of(d, 0);
+    o.eA = d.eA, o.sa_e = d.Hp128;
+    o.eB = d.eCx, o.sb_e = 0;
+    gemm<0>(&tm.m[TM_OPA], sA, &tm.m[TM_CXB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
+  } else if constexpr (STEP == 1) {   // t2 = (Cy t1) / lambda: A = rows of Cy (ky), B = t1 columns (kx)
+    o.mx = tmx_of(d, 1);
+    o.eA = d.eCy, o.sa_e = 0;
+    o.eB = d.eB, o.sb_e = d.Wp64;
+    gemm<1>(&tm.m[TM_CYA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+  } else if constexpr (STEP == 2) {   // t3 = Cy^T t2: A = rows of Cy^T (y), B = t2 columns (kx)
+    o.eA = d.eCy + d.g.Hb, o.sa_e = 0;
+    o.eB = d.eB, o.sb_e = d.Wp64;
+    gemm<2>(&tm.m[TM_CYTA], 0, &tm.m[TM_OPB], sB, H, W, d.Hp32, d.K, o, eacc, vb, nvb, sm, err);
+  } else {   // phi = t3 Cx: A = t3 (rows y), B = rows of Cx^T (x)
+    o.phi = d.phi;
+    o.rho = d.rho;
+    o.eA = d.eA, o.sa_e = d.Hp128;
+    o.eB = d.eCx + d.g.Wb, o.sb_e = 0;
+    gemm<3>(&tm.m[TM_OPA], sA, &tm.m[TM_CXTB], 0, H, W, d.Wp32, d.K, o, eacc, vb, nvb, sm, err);
   }
 }
 
 // The slice phase before GEMM pass `step`: the dynamic operand of the pass
 // from its FP32 / pair grid. An A operand (rho before pass 0, t3 before pass
-// 3; rows y over K = x) takes one warp per row, which finds the row's maximum
-// itself; a B operand (t1 before pass 1, t2 before pass 2; rows kx over K =
+// 3; rows y over K = x) takes 128 threads per row, which find the row's
+// maximum themselves (blockDim.x must be 256); a B operand (t1 before pass 1, t2 before pass 2; rows kx over K =
 // y) takes its column maxima from the previous pass's epilogue. Before pass
 // 0 it clears the t1 maxima and before pass 1 the t2 maxima (both last read
 // one solve ago), so each is empty when its pass gathers into it.
@@ -509,22 +559,38 @@ static __device__ void slice_phase(const Dev& d, int step, int vb, int nvb) {
     for (int i = vb * blockDim.x + threadIdx.x; i < K * W; i += nvb * blockDim.x) z[i] = 0u;
   }
   if (step == 0 || step == 3) {
-    const int wpb = blockDim.x >> 5;
+    // A operand: a row per 128 threads (two rows a block), each thread one
+    // group of 8 consecutive x (more past 1024 columns), read once for the
+    // row's maximum and again, from L1, for the slices
+    __shared__ unsigned red[2][4];
+    const int slot = threadIdx.x >> 7, t = threadIdx.x & 127;
     const int ng = d.Wp32 / 8;
     const size_t fs = a_elems(H, W, 1);
-    for (int rw = vb * wpb + (threadIdx.x >> 5); rw < K * H; rw += nvb * wpb) {
-      const int f = rw / H, y = rw % H;
+    for (int base = vb * 2; base < K * H; base += nvb * 2) {   // the same trips for the whole block
+      const int rw = base + slot;
+      const bool ok = rw < K * H;
+      const int f = ok ? rw / H : 0, y = ok ? rw % H : 0;
       const float* rrow = d.rho + (size_t)f * d.B + (size_t)y * W;
       const float2* prow = d.tp + (size_t)f * d.B + (size_t)y * W;
       unsigned m = 0;
-      for (int x = lane; x < W; x += 32)
-        m = max(m, __float_as_uint(fabsf(step == 0 ? rrow[x] : prow[x].x)));
+      if (ok)
+        for (int g = t; g < ng; g += 128)
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int x = g * 8 + k;
+            if (x < W) m = max(m, __float_as_uint(fabsf(step == 0 ? rrow[x] : prow[x].x)));
+          }
       m = __reduce_max_sync(0xffffffffu, m);
+      if ((t & 31) == 0) red[slot][t >> 5] = m;
+      __syncthreads();
+      m = max(max(red[slot][0], red[slot][1]), max(red[slot][2], red[slot][3]));
+      __syncthreads();   // the next row pair rewrites red
+      if (!ok) continue;
       const int e = row_exponent(m);
-      if (lane == 0) d.eA[(size_t)f * d.Hp128 + y] = e;
+      if (t == 0) d.eA[(size_t)f * d.Hp128 + y] = e;
       const float sc = pow2f(7 - e);
       uint16_t* dst = d.opA + (size_t)f * fs;
-      for (int g = lane; g < ng; g += 32) {
+      for (int g = t; g < ng; g += 128) {
         uint16_t sl[kSlices][8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {

@@ -30,17 +30,26 @@ __global__ void __launch_bounds__(kThreads) k_tc_slice(Dev d, int step) {
 // One DCT pass on tcgen05 tensor cores, one 128 x 64 tile per block
 // iteration; gridDim.x <= the pass's tiles. The energy partials of pass 3 are
 // those of the blocks launched; the slice phase before it zeroes the rest.
-__global__ void __launch_bounds__(kThreads, 1) k_dct_tc(Dev d, Partials p, int step, unsigned long long* err,
+template <int STEP>
+__global__ void __launch_bounds__(kThreads, 1) k_dct_tc(Dev d, Partials p, unsigned long long* err,
                                                        const __grid_constant__ tc::TcMaps maps) {
   extern __shared__ __align__(128) unsigned char tc_dyn[];
   tc::Smem& sm = *reinterpret_cast<tc::Smem*>(tc_dyn);
-  __shared__ Shared sh;
   double eacc[kMaxFields] = {0.0, 0.0, 0.0, 0.0};
   tc::setup(sm);
-  tc::dct_pass(d, maps, step, blockIdx.x, gridDim.x, sm, eacc, err);
+  tc::dct_pass<STEP>(d, maps, blockIdx.x, gridDim.x, sm, eacc, err);
   tc::teardown(sm);
-  if (step == 3)
+  if constexpr (STEP == 3) {
+    __shared__ Shared sh;
     for (int f = 0; f < d.K; ++f) write_partial(eacc[f], pslot(p, SLOT_ENERGY + f), (int)blockIdx.x, sh.d);
+  }
+}
+template <int STEP>
+void launch_dct_tc(const Dev& d, const Reduce& r, int gb, cudaStream_t s, const tc::TcMaps& maps) {
+  static const bool attr = cudaFuncSetAttribute(k_dct_tc<STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)sizeof(tc::Smem)) == cudaSuccess;
+  (void)attr;
+  k_dct_tc<STEP><<<gb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, (unsigned long long*)(r.iscal + SI_TC_FAIL), maps);
 }
 // Zero energy partials of the virtual blocks [from, nvb) (pass 3 runs fewer).
 __global__ void __launch_bounds__(kThreads) k_zero_energy(Dev d, Partials p, int from) {
@@ -284,9 +293,6 @@ void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s
   }
   if (d.tc) {
     if (!maps) return;   // the tensor-core form needs the instance's tensor maps
-    static const bool attr = cudaFuncSetAttribute(k_dct_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)sizeof(tc::Smem)) == cudaSuccess;
-    (void)attr;
     // one block a tile (at most one resident a multiprocessor: the pipeline
     // holds 192 KB of shared memory and 256 TMEM columns)
     const int gb = std::max(1, std::min(nvb, tc::pass_tiles_host(d)));
@@ -297,8 +303,12 @@ void launch_dct(const Dev& d, const Reduce& r, int step, int nvb, cudaStream_t s
       k_zero_energy<<<nvb, kThreads, 0, s>>>(d, r.p, gb);
     }
     COUNT;
-    k_dct_tc<<<gb, kThreads, sizeof(tc::Smem), s>>>(d, r.p, step, (unsigned long long*)(r.iscal + SI_TC_FAIL),
-                                                    *maps);
+    switch (step) {
+      case 0: launch_dct_tc<0>(d, r, gb, s, *maps); break;
+      case 1: launch_dct_tc<1>(d, r, gb, s, *maps); break;
+      case 2: launch_dct_tc<2>(d, r, gb, s, *maps); break;
+      default: launch_dct_tc<3>(d, r, gb, s, *maps); break;
+    }
     return;
   }
   COUNT;

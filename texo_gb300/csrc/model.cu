@@ -17,8 +17,6 @@
 namespace tgp {
 
 namespace {
-constexpr double kPi = 3.14159265358979323846;
-
 inline double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // quadratic_bspline_axis / deposit_quadratic_bspline in FP64
