@@ -100,7 +100,9 @@ typedef enum texo_gp_status {
   TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW = 118,     /* ArithmeticOverflow */
   /* PnrError::InvalidPlacement of `project` (legalization/mod.rs:391-430,
    * 679-722): fixed units on one BEL, or an auction result on a taken BEL */
-  TEXO_GP_ERR_PROJECTION_CONFLICT = 119
+  TEXO_GP_ERR_PROJECTION_CONFLICT = 119,
+  /* legalization::repair (repair.rs) */
+  TEXO_GP_ERR_NO_BEL = 120                    /* PnrError::NoBel { cell }: no legal completion exists */
 } texo_gp_status;
 
 /* Resource kinds in the reference's `ResourceKind` order
@@ -800,6 +802,65 @@ int32_t texo_gp_project(int32_t device, uint32_t width, uint32_t height, uint32_
                         uint32_t num_tables, const texo_gp_choice_table* tables, uint32_t num_units,
                         const uint32_t* unit_table, const uint32_t* unit_first_cell, const uint32_t* target_xy,
                         uint32_t cost_scale, int32_t* out_choice, texo_gp_projection_stats* stats);
+
+/* ---- legalization: the transactional repair of `project` ----------------
+ * `repair_relaxed` (crates/texo-pnr/src/legalization/repair.rs:60-151), the
+ * last step of `project`: a relaxed proposal (preferred[u] a row of
+ * tables[unit_table[u]], or -1 unmatched; rows may conflict) becomes a legal
+ * placement. Unit u's cells are unit_cells[unit_cell_ptr[u] ..
+ * unit_cell_ptr[u+1]] (one per row BEL, the first the order key), cells
+ * 0..num_cells-1; fixed[u] nonzero marks a fixed unit (never evicted; it must
+ * have a choice). Legality: BEL occupancy and, with `legality` (may be
+ * NULL), pin wires and shared resources:
+ *   - a connected cell pin (cell_pin_cell[k], key cell_pin_key[k], net
+ *     cell_pin_net[k]) placed on BEL b takes the wire bel_pin_wire[j] of the
+ *     entry with bel_pin_bel[j] = b and bel_pin_key[j] = key; wire w admits
+ *     wire_capacity[w] distinct nets (`visit_assignment_pin_resources`,
+ *     lib.rs:6989-7005). A candidate BEL without the key is an error;
+ *   - under rule r a cell carries a value (cell_value_*) and a BEL belongs
+ *     to a resource (bel_resource_*); a (rule, resource) holds one value
+ *     (`visit_assignment_shared_resources`, lib.rs:6972-6987).
+ * The search (initial pending units, the direct and single-blocker fast
+ * paths, the exact search over every blocker set with memoised states;
+ * choices from the preferred one outwards ring by ring around target_xy) is
+ * the reference's, so the placement and the counters equal its own.
+ * out_cell_bel[c]: the BEL of cell c (-1 for cells of no unit). Errors:
+ * TEXO_GP_ERR_PROJECTION_CONFLICT for the reference's invalid-placement
+ * cases (two fixed units on a BEL, incompatible fixed values or nets, an
+ * out-of-range or missing fixed choice), TEXO_GP_ERR_NO_BEL when no legal
+ * completion exists (stats->failed_cell: the first unplaced unit's first
+ * cell). Host code; no device work. */
+typedef struct texo_gp_legality {
+  uint32_t num_wires;
+  const uint32_t* wire_capacity;
+  uint32_t num_cell_pins;
+  const uint32_t *cell_pin_cell, *cell_pin_key, *cell_pin_net;
+  uint32_t num_bel_pins;
+  const uint32_t *bel_pin_bel, *bel_pin_key, *bel_pin_wire;
+  uint32_t num_rules;
+  uint32_t num_cell_values;
+  const uint32_t *cell_value_rule, *cell_value_cell;
+  const uint64_t* cell_value;
+  uint32_t num_bel_resources;
+  const uint32_t *bel_resource_rule, *bel_resource_bel;
+  const uint64_t* bel_resource;
+} texo_gp_legality;
+typedef struct texo_gp_repair_stats {   /* RepairStats (repair.rs:35-49) */
+  uint64_t initial_pending;
+  uint64_t direct_fast_choices, direct_fast_moves, direct_fast_fallbacks;
+  uint64_t augmenting_roots, augmenting_fallbacks;
+  uint64_t states_visited, failed_states, max_unplaced, max_blocker_branches;
+  uint64_t units_evicted, choices_examined;
+  double elapsed_ms;
+  uint32_t failed_cell;
+  uint32_t reserved[7];
+} texo_gp_repair_stats;
+int32_t texo_gp_repair(uint32_t width, uint32_t height, uint32_t num_bels, const uint32_t* bel_xy,
+                       uint32_t num_tables, const texo_gp_choice_table* tables, uint32_t num_units,
+                       const uint32_t* unit_table, const uint32_t* unit_cell_ptr, const uint32_t* unit_cells,
+                       uint32_t num_cells, const uint32_t* target_xy, const int32_t* preferred,
+                       const uint8_t* fixed, const texo_gp_legality* legality, int32_t* out_cell_bel,
+                       texo_gp_repair_stats* stats);
 
 /* Diagnostic: runs the engine's bounded device waits (the grid barrier of
  * the persistent loop and the mbarrier wait of the tensor-core pipeline)

@@ -40,6 +40,11 @@ def test_modes_reach_legal_choices(mode):
     bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
     res = A.analytical_place(prob, units, bel_xy, mode=mode)
     assert np.all(res.preferred >= 0) and legal(res, units)
+    # the repair keeps a complete, legal projection
+    expected = np.full(len(res.bels), -1)
+    for i, u in enumerate(units):
+        expected[u.cells] = u.choices[res.preferred[i]]
+    assert np.array_equal(res.bels, expected) and res.info["repair"]["initial_pending"] == 0
     if mode != A.COARSE:
         assert res.info["placement"]["converged"]
 

@@ -136,3 +136,29 @@ def test_projection_at_scale_equals_the_parallel_restatement():
     a = L.project(arch.width, arch.height, bel_xy, units, targets)
     bels = a.bels(units)
     assert np.all(bels >= 0) and len(np.unique(bels)) == len(bels)
+
+
+def test_project_and_repair_on_the_gpu():
+    """The whole `project` (GPU auctions, then the transactional repair) on
+    the 24 x 24 fabric: every cell on a BEL of its unit's rows, no BEL twice,
+    and the repair keeps the projection where it was already legal; with
+    more units than BELs of a kind, the repair's NoBel."""
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(24, 24))
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, 3, luts=1200, ffs=600, lut_ff_pairs=400,
+                                                   carry=((30, 4), (10, 6)), io=40)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    targets, _, st = place(prob, default_params(best_effort=1))
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    placed, ps, rs = L.project_and_repair(arch.width, arch.height, bel_xy, units, targets)
+    assert np.all(placed >= 0) and len(np.unique(placed)) == len(placed)
+    for unit in units:
+        assert list(placed[unit.cells]) in [list(r) for r in unit.choices]
+    pj = L.project(arch.width, arch.height, bel_xy, units, targets)
+    assert np.array_equal(placed, pj.bels(units)) and rs["initial_pending"] == 0
+    # more LUT singletons than LUT BELs on a 2 x 2 fabric
+    small = ecp5.read_architecture(ecp5.synthetic_architecture(2, 2))
+    luts = ecp5.single_cell_choices(small, ecp5.LUT4)
+    many = [L.Unit([c], luts, False) for c in range(len(luts) + 1)]
+    sxy = np.stack([small.bel_x, small.bel_y], 1)
+    with pytest.raises(L.NoBelError):
+        L.project_and_repair(small.width, small.height, sxy, many, [[0, 0]] * len(many))

@@ -32,6 +32,7 @@ STATUS = {
     115: "INSTANCE_AREA_MEMBER", 116: "INSTANCE_AREA_FILLER", 117: "INSTANCE_AREA_POSTCONDITION",
     118: "INSTANCE_AREA_OVERFLOW",
     119: "PROJECTION_CONFLICT",
+    120: "NO_BEL",
 }
 CODE = {v: k for k, v in STATUS.items()}
 
@@ -155,6 +156,30 @@ class ProjectionStats(C.Structure):
                 ("auctions", C.c_uint64), ("elapsed_ms", C.c_double), ("reserved", C.c_uint32 * 8)]
 
 
+class Legality(C.Structure):
+    """texo_gp_legality: pin wires and shared resources of the repair."""
+    _fields_ = [("num_wires", C.c_uint32), ("wire_capacity", C.POINTER(C.c_uint32)),
+                ("num_cell_pins", C.c_uint32), ("cell_pin_cell", C.POINTER(C.c_uint32)),
+                ("cell_pin_key", C.POINTER(C.c_uint32)), ("cell_pin_net", C.POINTER(C.c_uint32)),
+                ("num_bel_pins", C.c_uint32), ("bel_pin_bel", C.POINTER(C.c_uint32)),
+                ("bel_pin_key", C.POINTER(C.c_uint32)), ("bel_pin_wire", C.POINTER(C.c_uint32)),
+                ("num_rules", C.c_uint32), ("num_cell_values", C.c_uint32),
+                ("cell_value_rule", C.POINTER(C.c_uint32)), ("cell_value_cell", C.POINTER(C.c_uint32)),
+                ("cell_value", C.POINTER(C.c_uint64)), ("num_bel_resources", C.c_uint32),
+                ("bel_resource_rule", C.POINTER(C.c_uint32)), ("bel_resource_bel", C.POINTER(C.c_uint32)),
+                ("bel_resource", C.POINTER(C.c_uint64))]
+
+
+class RepairStats(C.Structure):
+    _fields_ = [("initial_pending", C.c_uint64), ("direct_fast_choices", C.c_uint64),
+                ("direct_fast_moves", C.c_uint64), ("direct_fast_fallbacks", C.c_uint64),
+                ("augmenting_roots", C.c_uint64), ("augmenting_fallbacks", C.c_uint64),
+                ("states_visited", C.c_uint64), ("failed_states", C.c_uint64), ("max_unplaced", C.c_uint64),
+                ("max_blocker_branches", C.c_uint64), ("units_evicted", C.c_uint64),
+                ("choices_examined", C.c_uint64), ("elapsed_ms", C.c_double), ("failed_cell", C.c_uint32),
+                ("reserved", C.c_uint32 * 7)]
+
+
 class FieldEval(C.Structure):
     _fields_ = [
         ("energy", C.c_double), ("normalized_overflow", C.c_double), ("net_charge", C.c_double),
@@ -246,6 +271,9 @@ SIGNATURES = {
     "texo_gp_project": (C.c_int32, [C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, C.c_uint32,
                                     C.POINTER(ChoiceTable), C.c_uint32, c_u32p, c_u32p, c_u32p, C.c_uint32,
                                     C.POINTER(C.c_int32), C.POINTER(ProjectionStats)]),
+    "texo_gp_repair": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_uint32, c_u32p, C.c_uint32, C.POINTER(ChoiceTable),
+                                   C.c_uint32, c_u32p, c_u32p, c_u32p, C.c_uint32, c_u32p, C.POINTER(C.c_int32),
+                                   c_u8p, C.POINTER(Legality), C.POINTER(C.c_int32), C.POINTER(RepairStats)]),
     "texo_gp_place_routable": (C.c_int32, [C.POINTER(ProblemC), C.POINTER(Params), C.POINTER(RoutingCapacity),
                                            C.c_uint64, C.POINTER(RegisterControl), c_u32p, c_f64p,
                                            C.POINTER(Stats), C.POINTER(RoutableReport)]),
@@ -323,7 +351,7 @@ def load(path=None):
 def check(code, where=""):
     if code != 0:
         detail = ""
-        if code == CODE["CUDA"] and _lib is not None:
+        if code in (CODE["CUDA"], CODE["INVALID_ARGUMENT"]) and _lib is not None:
             detail = (_lib.texo_gp_last_error() or b"").decode()
         raise TexoGpError(code, where, detail)
     return code

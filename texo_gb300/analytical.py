@@ -11,11 +11,11 @@ reference runs it:
 3. the global placement: the seed rounded to tiles (coarse), or
    `eplace::place` from the seed (texo_gp_place, or with a routing-capacity
    map texo_gp_place_routable), best effort or not;
-4. `project` up to its repair (texo_gp_project).
+4. `project`: the relaxed projection (texo_gp_project) and its
+   transactional repair (texo_gp_repair), a BEL for every cell.
 
 A timing iteration's targets are projected from the incumbent when its BELs
-are given (`project_anchored_targets`, lib.rs:4157-4231). The repair after
-`project` is not part of this library.
+are given (`project_anchored_targets`, lib.rs:4157-4231).
 """
 import copy
 from dataclasses import dataclass
@@ -34,8 +34,9 @@ ELECTROSTATIC_BEST_EFFORT = "electrostatic_best_effort"
 class AnalyticalResult:
     seed_xy: np.ndarray        # [U, 2] solved seed positions (unit origins)
     targets: np.ndarray        # [U, 2] rounded tile targets handed to project
-    preferred: np.ndarray      # [U] chosen row per unit (-1: left to the repair)
+    preferred: np.ndarray      # [U] the projection's row per unit (-1: left to the repair)
     info: dict
+    bels: np.ndarray = None    # [cells] the legal BEL of every cell (after the repair)
 
 
 def _rounded(values, extent):
@@ -126,7 +127,9 @@ def analytical_place(problem, units, bel_xy, mode=ELECTROSTATIC, params=None, an
                 pos[key] = {tuple(int(b) for b in a): c for c, a in enumerate(u.choices)}
             preferred[i] = pos[key][tuple(int(b) for b in bels[u.cells])]
         info["project"] = {"anchored": True}
-        return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), preferred, info)
+        return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), preferred, info,
+                                np.asarray(bels, np.int64))
     proj = legalize.project(W, H, bel_xy, units, targets)
     info["project"] = proj.stats
-    return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), proj.preferred, info)
+    placed, info["repair"] = legalize.repair(W, H, bel_xy, units, targets, proj.preferred, fixed)
+    return AnalyticalResult(solved, np.asarray(targets, np.uint32).reshape(-1, 2), proj.preferred, info, placed)

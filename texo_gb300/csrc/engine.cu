@@ -1774,6 +1774,7 @@ const char* texo_gp_status_name(int32_t s) {
     case TEXO_GP_ERR_INSTANCE_AREA_POSTCONDITION: return "INSTANCE_AREA_POSTCONDITION";
     case TEXO_GP_ERR_INSTANCE_AREA_OVERFLOW: return "INSTANCE_AREA_OVERFLOW";
     case TEXO_GP_ERR_PROJECTION_CONFLICT: return "PROJECTION_CONFLICT";
+    case TEXO_GP_ERR_NO_BEL: return "NO_BEL";
     default: return "UNKNOWN";
   }
 }

@@ -14,7 +14,12 @@ exposes the auction, which runs on the GPU through include/texo_gp.h:
 - `SiteGrid` / `site_grid`: the BEL layout those walks read;
 - `project_singletons(problem, targets)`: the single-cell part of `project`
   for a placement problem: fixed units' BELs occupied, singleton bidders,
-  the auction, one BEL per unit.
+  the auction, one BEL per unit;
+- `project` / `project_native`: `project` up to its repair (fixed units,
+  shared-row families, singletons; texo_gp_project);
+- `repair`: the transactional repair (`repair_relaxed`, repair.rs) with
+  occupancy, pin-wire and shared-resource legality (texo_gp_repair, host
+  code), and `project_and_repair`, the whole `project`.
 
 The GPU bids all unassigned bidders at once each round; the result carries
 the reference's guarantees (exact maximum cardinality, total base cost at
@@ -334,8 +339,9 @@ def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
     native code (`texo_gp_project`, auctions on the GPU); `auction(grid, kinds,
     targets, cost_scale) -> (assignment, stats)` runs these steps here in
     Python with the given auction instead (a checker passes the oracle's).
-    Unmatched units keep -1 (the reference's repair, which places them by
-    transactional search, is not part of this library)."""
+    Unmatched units keep -1; `repair` (texo_gp_repair) then places them by
+    the reference's transactional search, and `project_and_repair` runs
+    both steps."""
     if auction is None:
         return project_native(width, height, bel_xy, units, targets, cost_scale)
     bel_xy = np.asarray(bel_xy, dtype=np.int64).reshape(-1, 2)
@@ -457,18 +463,12 @@ def project(width, height, bel_xy, units, targets, cost_scale=0, auction=None):
     return Projection(preferred, occupied, stats)
 
 
-def project_native(width, height, bel_xy, units, targets, cost_scale=0, device=0):
-    """`project` through texo_gp_project: the same steps as `project` with an
-    auction callback, in native code with the GPU auctions. Units sharing a
-    `choices` list share one choice table."""
-    xy = np.ascontiguousarray(np.asarray(bel_xy, dtype=np.uint32).reshape(-1, 2))
-    tg = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32).reshape(-1, 2))
-    U = len(units)
-    if tg.shape[0] != U:
-        raise ValueError("one target per unit")
+def _native_tables(units):
+    """The units' choice tables for the C ABI (units sharing a `choices` list
+    share one table): (table array, count, table of every unit, the row
+    arrays the tables point into)."""
     table_of, tables, keep = {}, [], []
-    unit_table = np.zeros(max(U, 1), np.uint32)
-    first = np.zeros(max(U, 1), np.uint32)
+    unit_table = np.zeros(max(len(units), 1), np.uint32)
     for u, unit in enumerate(units):
         key = id(unit.choices)
         if key not in table_of:
@@ -483,12 +483,27 @@ def project_native(width, height, bel_xy, units, targets, cost_scale=0, device=0
         elif bool(tables[table_of[key]].shared) != unit.is_shared():
             raise ValueError("units sharing a choice table must agree on Shared / SingleCell")
         unit_table[u] = table_of[key]
-        first[u] = unit.cells[0]
     arr = (abi.ChoiceTable * max(len(tables), 1))(*tables)
+    return arr, len(tables), unit_table, keep
+
+
+def project_native(width, height, bel_xy, units, targets, cost_scale=0, device=0):
+    """`project` through texo_gp_project: the same steps as `project` with an
+    auction callback, in native code with the GPU auctions. Units sharing a
+    `choices` list share one choice table."""
+    xy = np.ascontiguousarray(np.asarray(bel_xy, dtype=np.uint32).reshape(-1, 2))
+    tg = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32).reshape(-1, 2))
+    U = len(units)
+    if tg.shape[0] != U:
+        raise ValueError("one target per unit")
+    arr, ntables, unit_table, keep = _native_tables(units)
+    first = np.zeros(max(U, 1), np.uint32)
+    for u, unit in enumerate(units):
+        first[u] = unit.cells[0]
     out = np.full(max(U, 1), -1, np.int32)
     st = abi.ProjectionStats()
     lib = abi.load()
-    code = lib.texo_gp_project(device, width, height, xy.shape[0], abi.ptr(xy, C.c_uint32), len(tables), arr, U,
+    code = lib.texo_gp_project(device, width, height, xy.shape[0], abi.ptr(xy, C.c_uint32), ntables, arr, U,
                                abi.ptr(unit_table, C.c_uint32), abi.ptr(first, C.c_uint32),
                                abi.ptr(tg if U else np.zeros(2, np.uint32), C.c_uint32), cost_scale,
                                abi.ptr(out, C.c_int32), C.byref(st))
@@ -558,3 +573,114 @@ def project_anchored(width, height, bel_xy, units, targets, incumbent):
         placed[unit.cells] = chosen
         occupied[chosen] = True
     return placed
+
+
+class NoBelError(RuntimeError):
+    """PnrError::NoBel { cell } from the repair: no legal completion exists."""
+
+    def __init__(self, cell, message):
+        super().__init__(message)
+        self.cell = cell
+
+
+@dataclass
+class Legality:
+    """Legality beyond BEL occupancy for the repair (texo_gp_legality):
+    `wire_capacity[w]` distinct nets a wire admits; `cell_pins`: cell ->
+    [(pin key, net)] of its connected pins; `bel_pins`: BEL -> {pin key:
+    wire}; `rules`: [(cell -> value, BEL -> resource)], a (rule, resource)
+    holding one value."""
+    wire_capacity: list = None
+    cell_pins: dict = None
+    bel_pins: dict = None
+    rules: list = None
+
+
+def _legality_struct(leg):
+    L = abi.Legality()
+    keep = []
+
+    def arr(values, dtype):
+        a = np.ascontiguousarray(np.asarray(values, dtype=dtype).reshape(-1))
+        if a.size == 0:
+            a = np.zeros(1, dtype)
+        keep.append(a)
+        return abi.ptr(a, C.c_uint64 if dtype == np.uint64 else C.c_uint32)
+
+    cap = list(leg.wire_capacity or [])
+    L.num_wires = len(cap)
+    L.wire_capacity = arr(cap, np.uint32)
+    cp = [(c, k, n) for c, pins in sorted((leg.cell_pins or {}).items()) for k, n in pins]
+    L.num_cell_pins = len(cp)
+    L.cell_pin_cell = arr([e[0] for e in cp], np.uint32)
+    L.cell_pin_key = arr([e[1] for e in cp], np.uint32)
+    L.cell_pin_net = arr([e[2] for e in cp], np.uint32)
+    bp = [(b, k, w) for b, pins in sorted((leg.bel_pins or {}).items()) for k, w in sorted(pins.items())]
+    L.num_bel_pins = len(bp)
+    L.bel_pin_bel = arr([e[0] for e in bp], np.uint32)
+    L.bel_pin_key = arr([e[1] for e in bp], np.uint32)
+    L.bel_pin_wire = arr([e[2] for e in bp], np.uint32)
+    rules = list(leg.rules or [])
+    L.num_rules = len(rules)
+    cv = [(r, c, v) for r, (cells, _) in enumerate(rules) for c, v in sorted(cells.items())]
+    br = [(r, b, x) for r, (_, bels) in enumerate(rules) for b, x in sorted(bels.items())]
+    L.num_cell_values = len(cv)
+    L.cell_value_rule = arr([e[0] for e in cv], np.uint32)
+    L.cell_value_cell = arr([e[1] for e in cv], np.uint32)
+    L.cell_value = arr([e[2] for e in cv], np.uint64)
+    L.num_bel_resources = len(br)
+    L.bel_resource_rule = arr([e[0] for e in br], np.uint32)
+    L.bel_resource_bel = arr([e[1] for e in br], np.uint32)
+    L.bel_resource = arr([e[2] for e in br], np.uint64)
+    return L, keep
+
+
+def repair(width, height, bel_xy, units, targets, preferred, fixed, legality=None, num_cells=None):
+    """`repair_relaxed` (legalization/repair.rs:60-151) through
+    texo_gp_repair: the relaxed proposal `preferred` (a row per unit, -1
+    unmatched; rows may conflict) made legal by transactional search. `fixed`
+    marks units never evicted. Returns (BEL per cell, -1 for cells of no
+    unit; the search counters `RepairStats`). Raises ProjectionError for the
+    reference's invalid-placement cases and NoBelError when no legal
+    completion exists."""
+    U = len(units)
+    xy = np.ascontiguousarray(np.asarray(bel_xy, dtype=np.uint32).reshape(-1, 2))
+    tg = np.ascontiguousarray(np.asarray(targets, dtype=np.uint32).reshape(-1, 2))
+    pref = np.ascontiguousarray(np.asarray(preferred, dtype=np.int32).reshape(-1))
+    fx = np.ascontiguousarray(np.asarray(fixed, dtype=np.uint8).reshape(-1))
+    if tg.shape[0] != U or pref.size != U or fx.size != U:
+        raise ProjectionError("transactional repair input lengths do not match placement units")
+    if num_cells is None:
+        num_cells = 1 + max((c for u in units for c in u.cells), default=-1)
+    arr, ntables, unit_table, keep = _native_tables(units)
+    ptr = np.zeros(U + 1, np.uint32)
+    ptr[1:] = np.cumsum([len(u.cells) for u in units]) if U else []
+    cells = np.ascontiguousarray(np.asarray([c for u in units for c in u.cells] or [0], dtype=np.uint32))
+    out = np.full(max(num_cells, 1), -1, np.int32)
+    st = abi.RepairStats()
+    L, keep_l = (None, []) if legality is None else _legality_struct(legality)
+    lib = abi.load()
+    code = lib.texo_gp_repair(width, height, xy.shape[0], abi.ptr(xy, C.c_uint32), ntables, arr, U,
+                              abi.ptr(unit_table, C.c_uint32), abi.ptr(ptr, C.c_uint32), abi.ptr(cells, C.c_uint32),
+                              num_cells, abi.ptr(tg if U else np.zeros(2, np.uint32), C.c_uint32),
+                              abi.ptr(pref if U else np.zeros(1, np.int32), C.c_int32),
+                              abi.ptr(fx if U else np.zeros(1, np.uint8), C.c_uint8),
+                              C.byref(L) if L is not None else None, abi.ptr(out, C.c_int32), C.byref(st))
+    if code == abi.CODE["PROJECTION_CONFLICT"]:
+        raise ProjectionError(lib.texo_gp_last_error().decode())
+    if code == abi.CODE["NO_BEL"]:
+        raise NoBelError(st.failed_cell, lib.texo_gp_last_error().decode())
+    abi.check(code, "texo_gp_repair")
+    stats = {f: getattr(st, f) for f, _ in abi.RepairStats._fields_ if f not in ("reserved", "failed_cell")}
+    return out[:num_cells].astype(np.int64), stats
+
+
+def project_and_repair(width, height, bel_xy, units, targets, legality=None, cost_scale=0, device=0):
+    """The whole `project` (legalization/mod.rs:322-389): the relaxed
+    projection (texo_gp_project, GPU auctions) and its transactional repair
+    (texo_gp_repair), fixed units being those with one choice. Returns (BEL
+    per cell, projection statistics, repair statistics)."""
+    pj = project_native(width, height, bel_xy, units, targets, cost_scale, device)
+    fixed = [len(u.choices) == 1 for u in units]
+    placed, rs = repair(width, height, bel_xy, units, targets, pj.preferred, fixed, legality)
+    return placed, pj.stats, rs
