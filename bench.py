@@ -852,6 +852,36 @@ def ecp5_report(side=104, seed=0):
                 d += abs(int(x) - int(targets[u][0])) + abs(int(y) - int(targets[u][1]))
         return d
     bels = g.bels(units)
+    # the repair (texo_gp_repair, host code) of the GPU projection, and of the
+    # same projection with every tenth movable unit unmatched
+    fixed = [len(u.choices) == 1 for u in units]
+    q0 = time.perf_counter()
+    placed, rs = legalize.repair(arch.width, arch.height, bel_xy, units, targets, g.preferred, fixed)
+    q1 = time.perf_counter()
+    spoiled = np.array(g.preferred)
+    spoiled[[u for u in range(len(units)) if not fixed[u] and u % 10 == 0]] = -1
+    q2 = time.perf_counter()
+    placed2, rs2 = legalize.repair(arch.width, arch.height, bel_xy, units, targets, spoiled, fixed)
+    q3 = time.perf_counter()
+    # register control sets (clock, LSR, CE) as shared resources
+    rules = ecp5.ff_control_set_rules(arch, ecp5.synthetic_control_sets(kinds, seed=1))
+    q4 = time.perf_counter()
+    placed3, rs3 = legalize.repair(arch.width, arch.height, bel_xy, units, targets, g.preferred, fixed,
+                                   legalize.Legality(rules=rules))
+    q5 = time.perf_counter()
+    ok3 = bool(np.all(placed3 >= 0) and len(np.unique(placed3)) == len(placed3))
+    for cell_values, bel_res in rules:
+        seen = {}
+        for c, v in cell_values.items():
+            ok3 = ok3 and seen.setdefault(bel_res[int(placed3[c])], v) == v
+    repair = {"wall_ms": 1e3 * (q1 - q0), "initial_pending": rs["initial_pending"],
+              "legal": bool(np.all(placed >= 0) and len(np.unique(placed)) == len(placed)),
+              "tenth_unmatched": {"wall_ms": 1e3 * (q3 - q2), "initial_pending": rs2["initial_pending"],
+                                  "states_visited": rs2["states_visited"], "units_evicted": rs2["units_evicted"],
+                                  "legal": bool(np.all(placed2 >= 0) and len(np.unique(placed2)) == len(placed2))},
+              "control_sets": {"registers": len(rules[0][0]) if rules else 0, "wall_ms": 1e3 * (q5 - q4),
+                               "initial_pending": rs3["initial_pending"], "states_visited": rs3["states_visited"],
+                               "units_evicted": rs3["units_evicted"], "legal": ok3}}
     return {"fabric": "%dx%d" % (side, side), "bels": arch.num_bels, "cells": nc, "units": len(units),
             "nets": prob.num_nets, "stats": g.stats,
             "adapter_s": {"read_snapshot": t1 - t0, "design": t2 - t1, "placement_problem": t3 - t2},
@@ -860,6 +890,7 @@ def ecp5_report(side=104, seed=0):
             "project_gpu": {"wall_s": p1 - p0, "auction_gpu_ms": gpu_default_ms, "unplaced": int(np.sum(g.preferred < 0)),
                             "legal": bool(len(np.unique(bels[bels >= 0])) == int(np.sum(bels >= 0))),
                             "total_displacement": displacement(g), "auctions": calls_default},
+            "repair": repair,
             "project_gpu_reference_scale": {"auction_gpu_ms": gpu_s1_ms, "total_displacement": displacement(g1),
                                             "auctions": calls_s1},
             "project_reference_auctions": {"wall_s": p2 - p1b, "auction_cpu_ms": timed["cpu"], "cores": 1,

@@ -155,9 +155,20 @@ def test_project_and_repair_on_the_gpu():
         assert list(placed[unit.cells]) in [list(r) for r in unit.choices]
     pj = L.project(arch.width, arch.height, bel_xy, units, targets)
     assert np.array_equal(placed, pj.bels(units)) and rs["initial_pending"] == 0
-    # more LUT singletons than LUT BELs on a 2 x 2 fabric
-    small = ecp5.read_architecture(ecp5.synthetic_architecture(2, 2))
+    # with the registers' control sets as shared resources the repair
+    # separates what the occupancy-only projection put together
+    rules = ecp5.ff_control_set_rules(arch, ecp5.synthetic_control_sets(kinds, seed=4))
+    placed, _, rs = L.project_and_repair(arch.width, arch.height, bel_xy, units, targets,
+                                         legality=L.Legality(rules=rules))
+    assert rs["initial_pending"] > 0 and np.all(placed >= 0) and len(np.unique(placed)) == len(placed)
+    for cell_values, bel_res in rules:
+        seen = {}
+        for c, v in cell_values.items():
+            assert seen.setdefault(bel_res[int(placed[c])], v) == v
+    # more LUT singletons than the 8 LUT BELs of a 3 x 3 fabric
+    small = ecp5.read_architecture(ecp5.synthetic_architecture(3, 3))
     luts = ecp5.single_cell_choices(small, ecp5.LUT4)
+    assert len(luts) == 8
     many = [L.Unit([c], luts, False) for c in range(len(luts) + 1)]
     sxy = np.stack([small.bel_x, small.bel_y], 1)
     with pytest.raises(L.NoBelError):

@@ -304,3 +304,37 @@ def test_fabric_projection_repaired_like_the_restatement():
     for unit in units:
         assert list(placed[unit.cells]) in [list(r) for r in unit.choices]
     assert n[1]["initial_pending"] > 0
+
+
+def test_fabric_control_sets_repaired_like_the_restatement():
+    """ECP5 register control sets (`constrain_ff_control_sets`) as the
+    repair's shared-resource rules on the 16^2 fabric: the occupancy-only
+    projection puts registers of different clocks, resets or enables
+    together; the repair separates them. Native equals the restatement, and
+    every tile's registers share one clock and one LSR value, every slice's
+    one CE value."""
+    from test_project import fabric_case, oracle_auction
+    from texo_gb300 import ecp5
+    arch, units, targets = fabric_case(0)
+    kinds = [None] * (1 + max(c for u in units for c in u.cells))
+    for u in units:
+        for c, b in zip(u.cells, u.choices[0]):
+            kinds[c] = arch.bel_kind[b]
+    sets = ecp5.synthetic_control_sets(kinds, seed=3)
+    rules = ecp5.ff_control_set_rules(arch, sets)
+    assert len(rules) == 3 and len(sets) > 300
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    pj = L.project(arch.width, arch.height, bel_xy, units, targets, cost_scale=1, auction=oracle_auction(False))
+    fixed = [len(u.choices) == 1 for u in units]
+    pref = [int(p) for p in pj.preferred]
+    o = R.repair(arch.width, arch.height, bel_xy, units, targets, pref, fixed, R.Legality(rules=rules))
+    n = L.repair(arch.width, arch.height, bel_xy, units, targets, pref, fixed, L.Legality(rules=rules))
+    same(o, n)
+    assert n[1]["initial_pending"] > 0
+    placed = np.asarray(n[0])
+    assert np.all(placed >= 0) and len(np.unique(placed)) == len(placed)
+    for r, (cell_values, bel_res) in enumerate(rules):
+        seen = {}
+        for c, v in cell_values.items():
+            res = bel_res[int(placed[c])]
+            assert seen.setdefault(res, v) == v, (r, c)

@@ -524,6 +524,45 @@ def synthetic_architecture(width, height, io_per_edge_tile=2):
             "location_types": [plc, plc_edge, io], "locations": locations}
 
 
+def ff_control_set_rules(arch, control_sets):
+    """The shared-resource rules of ECP5 register control sets
+    (`constrain_ff_control_sets`, texo-target-ecp5/src/lib.rs:1184-1200),
+    for the repair's legality (`legalize.Legality(rules=...)`):
+    `control_sets` [(cell, slice CE value, tile clock value, tile LSR value)]
+    (`FfControlSet`, :803-812; values are opaque identifiers of the control
+    net, polarity and mode). Three rules, each (cell -> value, BEL ->
+    resource) over the TRELLIS_FF BELs in BEL order, resource ids numbered by
+    first appearance:
+    - the slice CE mux (`constrain_ff_slice_ce_muxes`, :1074-1108): one
+      resource per (tile, z >> 3), the two registers of a slice;
+    - the tile clock (`constrain_ff_clock_muxes`, :1110-1144) and the tile
+      LSR (`constrain_ff_lsr_muxes`, :1146-1181): one resource per tile, its
+      eight registers.
+    No control sets: no rules."""
+    sets = list(control_sets)
+    if not sets:
+        return []
+    ffs = [b for b in arch.bels_of_kind(REGISTER) if arch.bel_type[b] == "TRELLIS_FF"]
+    rules = []
+    for column, key in ((1, lambda b: (*arch.point(b), int(arch.bel_z[b]) >> 3)),
+                        (2, lambda b: arch.point(b)), (3, lambda b: arch.point(b))):
+        ids, bel_res = {}, {}
+        for b in ffs:
+            bel_res[b] = ids.setdefault(key(b), len(ids))
+        rules.append(({int(e[0]): int(e[column]) for e in sets}, bel_res))
+    return rules
+
+
+def synthetic_control_sets(kinds, seed=0, clocks=2, resets=2, enables=3):
+    """Seeded control sets for every register cell of a synthetic design:
+    [(cell, slice CE, tile clock, tile LSR)] drawn from `enables`, `clocks`
+    and `resets` distinct values."""
+    rng = np.random.default_rng(seed)
+    regs = [c for c, k in enumerate(kinds) if tuple(k) == tuple(REGISTER)]
+    return [(c, int(rng.integers(0, enables)), int(rng.integers(0, clocks)), int(rng.integers(0, resets)))
+            for c in regs]
+
+
 def synthetic_design(arch, seed=0, luts=0, ffs=0, lut_ff_pairs=0, carry=(), io=0, nets_per_unit=1.2,
                      sigma=4.0, max_fanout=8):
     """A seeded netlist for `arch` as placement units: `luts` and `ffs`
