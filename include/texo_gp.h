@@ -355,7 +355,9 @@ int32_t texo_gp_reset(texo_gp_handle h);
 
 /* ---- routability-driven area rounds ------------------------------------
  * The pieces of eplace::place's area-adjustment loop (eplace.rs:320-420),
- * host engine. texo_gp_optimize_round runs one `optimize_density_once`
+ * on the handle's engine (host or device: the persistent kernel's
+ * controller takes the same stop criterion, multipliers and scales).
+ * texo_gp_optimize_round runs one `optimize_density_once`
  * (eplace.rs:439-582) from the handle's current coordinates with a fresh
  * optimizer, multipliers and checkpoint: `stop` 0 stops at the final
  * targets (10 / 10 / 20 %), 1 at AreaAdjustmentReady (LUT and register
@@ -401,8 +403,8 @@ int32_t texo_gp_set_charges(texo_gp_handle h, const double* member_charge, const
  * adjustment that grows any kind is installed and the optimizer restarts
  * with the area-reset multipliers and the first round's density scales;
  * once the installed increase is below 1 % (or nothing grew) a last round
- * runs to the final targets. The rounds run on the host engine whatever
- * params->engine says. `capacity` NULL is texo_gp_place (the pure density
+ * runs to the final targets. The rounds run on params->engine's engine.
+ * `capacity` NULL is texo_gp_place (the pure density
  * objective). A register member whose cell has no control set, a cell with
  * two, or more area rounds than area_adjustment_round_limit (eplace.rs:
  * 584-626) return TEXO_GP_ERR_INVALID_NORMALIZATION like the reference.

@@ -1,5 +1,6 @@
 """The routability-driven rounds of eplace::place (eplace.rs:320-420) on the
-GPU's host engine against the FP64 oracle's rounds, through the C ABI, on
+GPU (host-driven stages and the persistent kernel) against the FP64
+oracle's rounds, through the C ABI, on
 the two-kind routability case (tests/routable_rounds.py).
 
 The area rounds drive the register field's area up until it fills the free
@@ -64,13 +65,14 @@ def test_set_charges_matches_the_oracle():
         assert abs(a.energy - b.energy) <= 1e-5 * abs(b.energy)
 
 
-def test_routable_rounds_match_the_oracle():
+@pytest.mark.parametrize("engine", [abi.ENGINE_HOST, abi.ENGINE_DEVICE])
+def test_routable_rounds_match_the_oracle(engine):
     prob, ch, cv, ctl = routability_case()
     prm = default_params(best_effort=1, max_iterations=200)
     ro = OracleRounds(prob, prm)
     f0, q0 = ro.fillers()
     _, c_ref, ref = R.place_routable(prob, prm, ch, cv, register_controls=ctl, rounds=ro)
-    t, c, got = R.place_routable(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
+    t, c, got = R.place_routable(prob, default_params(best_effort=1, max_iterations=200, engine=engine), ch, cv,
                                  register_controls=ctl)
     a_rounds, b_rounds = got["rounds"], ref["rounds"]
     assert [r["stop"] for r in a_rounds] == [r["stop"] for r in b_rounds]
@@ -100,17 +102,18 @@ def test_routable_rounds_match_the_oracle():
     assert abs(h_got - h_ref) <= 0.01 * h_ref
 
 
-def test_native_rounds_equal_the_python_composition():
+@pytest.mark.parametrize("engine", [abi.ENGINE_HOST, abi.ENGINE_DEVICE])
+def test_native_rounds_equal_the_python_composition(engine):
     """texo_gp_place_routable (the whole loop in one C-ABI call) against the
     Python composition of the same rounds over the C-ABI pieces: both run the
-    same host-engine rounds and the same GPU proposals, so the rounds, the
-    iteration counts, the installed charges and the targets are identical."""
+    same rounds on the same engine and the same GPU proposals, so the rounds,
+    the iteration counts, the installed charges and the targets are
+    identical."""
     from texo_gb300.placer import place_with_routing_capacity
     prob, ch, cv, ctl = routability_case()
-    t_py, c_py, info = R.place_routable(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
-                                        register_controls=ctl)
-    t, c, st, rep = place_with_routing_capacity(prob, default_params(best_effort=1, max_iterations=200), ch, cv,
-                                                register_controls=ctl, coordinates=True)
+    prm = lambda: default_params(best_effort=1, max_iterations=200, engine=engine)
+    t_py, c_py, info = R.place_routable(prob, prm(), ch, cv, register_controls=ctl)
+    t, c, st, rep = place_with_routing_capacity(prob, prm(), ch, cv, register_controls=ctl, coordinates=True)
     assert rep["rounds"] == len(info["rounds"]) and rep["area_rounds"] == info["area_rounds"] >= 1
     assert rep["iterations"] == info["iterations"] == st["iterations"]
     assert rep["last_relative_increase"] == info["rounds"][-2]["relative_increase"]

@@ -1146,6 +1146,16 @@ struct Controller {
         weight_sum += m.gamma_weight[f];
       }
       hr.inv_gamma_weight_sum = weight_sum == 0.0 ? 0.0 : 1.0 / weight_sum;
+      // a round of the area-adjustment loop (texo_gp_optimize_round)
+      hr.stop_mode = stop_mode;
+      hr.reset_mult = reset_mult ? 1 : 0;
+      hr.fixed_e0 = fixed_scales.empty() ? 0 : 1;
+      for (uint32_t f = 0; f < m.K; ++f) {
+        const uint32_t k = m.kinds[f].kind;
+        hr.area_field[f] = (k == TEXO_GP_KIND_LUT || k == TEXO_GP_KIND_REGISTER) ? 1 : 0;
+        if (!fixed_scales.empty()) hr.e0[f] = fixed_scales[f];
+      }
+      hr.completed = (unsigned)iter_offset;
       hr.a = 1.0;
       hr.ix = 0;
       hr.ixp = 1;
@@ -1227,6 +1237,8 @@ struct Controller {
     exhausted = hr.exhausted != 0;
     gamma = hr.gamma;
     last_objective = hr.last_objective;
+    e0.assign(hr.e0, hr.e0 + m.K);
+    lambda.assign(hr.lambda, hr.lambda + m.K);
     for (uint32_t f = 0; f < m.K; ++f) {
       current.overflow[f] = hr.cur_overflow[f];
       current.energy[f] = hr.cur_energy[f];
@@ -2049,10 +2061,6 @@ int32_t texo_gp_optimize_round(texo_gp_handle h, const texo_gp_round* round, uin
   {
     std::lock_guard<std::mutex> lk(h->mu);
     Instance& I = *h->inst;
-    if (I.m.params.engine != TEXO_GP_ENGINE_HOST) {
-      set_last_error("texo_gp_optimize_round runs with the host engine");
-      return TEXO_GP_ERR_UNSUPPORTED;
-    }
     // a fresh controller (Nesterov state, multipliers, checkpoint) from the
     // handle's current coordinates
     auto c = std::make_unique<Controller>(I);

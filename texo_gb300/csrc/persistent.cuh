@@ -44,6 +44,12 @@ struct DevRun {
   double inv_real_area[kMaxFields];   // 1 / real_area (FP64 division is slow on the device)
   double gamma_slope[kMaxFields];     // 2 / (1 - target) of field_wirelength_gamma
   double inv_gamma_weight_sum;        // 1 / sum of gamma_weight
+  // one round of the area-adjustment loop (texo_gp_optimize_round): stop at
+  // AreaAdjustmentReady (the area fields at 0.15) instead of the targets;
+  // the density scales e0 given (not from the initial energy); the
+  // multipliers from the area-reset formula
+  int stop_mode, fixed_e0, reset_mult;
+  int area_field[kMaxFields];         // LUT and register fields
   // loop state (optimize_density_once, eplace.rs:439-582)
   int phase;                    // 0 fresh, 1 running, 2 finished
   int status;                   // texo_gp_status

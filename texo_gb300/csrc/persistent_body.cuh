@@ -347,10 +347,41 @@ static __device__ int adaptive_gamma_dev(const DevRun& S, const double* overflow
   out = wsum == 0.0 ? S.gamma_base : ws * S.inv_gamma_weight_sum;
   return (isfinite(out) && out > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
 }
+// density_stop_reached (eplace.rs:1397-1415): Final, or AreaAdjustmentReady
+// (LUT and register fields at 0.15, AREA_ADJUSTMENT_OVERFLOW_TARGET)
 static __device__ bool stop_dev(const DevRun& S, const double* overflow) {
-  for (int f = 0; f < S.K; ++f)
-    if (!(overflow[f] <= S.target[f])) return false;
+  for (int f = 0; f < S.K; ++f) {
+    if (S.stop_mode == 1) {
+      if (S.area_field[f] && !(overflow[f] <= 0.15)) return false;
+    } else if (!(overflow[f] <= S.target[f])) {
+      return false;
+    }
+  }
   return true;
+}
+// area_adjusted_density_multipliers and area_adjusted_multiplier_step
+// (eplace.rs:1183-1232), elfPlace eqs. (27)-(28)
+static __device__ int area_multipliers_dev(DevRun& S, const ERec& e) {
+  double sg[kMaxFields], dens = 0.0;
+  for (int f = 0; f < S.K; ++f) {
+    const double ne = e.energy[f] * S.inv_e0[f];
+    sg[f] = ne + 0.5 * S.beta * ne * ne;
+    if (!isfinite(sg[f]) || sg[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    dens += e.force[f] * sg[f];
+  }
+  if (!isfinite(e.wal1) || e.wal1 <= 0.0 || !isfinite(dens) || dens <= 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+  const double scale = 0.1 * e.wal1 / dens;
+  bool any = false;
+  double nn = 0.0;
+  for (int f = 0; f < S.K; ++f) {
+    S.lambda[f] = scale * sg[f];
+    if (!isfinite(S.lambda[f]) || S.lambda[f] < 0.0) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+    any = any || S.lambda[f] > 0.0;
+    nn += S.lambda[f] * S.lambda[f];
+  }
+  if (!any) return TEXO_GP_ERR_INVALID_NORMALIZATION;
+  S.mstep = (S.alpha_high - 1.0) * sqrt(nn);
+  return (isfinite(S.mstep) && S.mstep > 0.0) ? TEXO_GP_OK : TEXO_GP_ERR_INVALID_NORMALIZATION;
 }
 static __device__ void excess_dev(const DevRun& S, const double* overflow, double& mx, double& tot) {
   mx = 0.0;
@@ -523,7 +554,8 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
     T0 {
       int st = validate_initial_dev(S, eo);
       for (int f = 0; f < S.K; ++f) {
-        S.e0[f] = fmax(eo.energy[f], 1.0);
+        if (!S.fixed_e0) S.e0[f] = fmax(eo.energy[f], 1.0);
+        if (!st && !(isfinite(S.e0[f]) && S.e0[f] > 0.0)) st = TEXO_GP_ERR_DENSITY_FIELD_CHANGED;
         S.inv_e0[f] = 1.0 / S.e0[f];
       }
       S.status = st;
@@ -535,6 +567,8 @@ static __device__ void run_body(const Dev& d, const Reduce& r, const Buffers& B,
       if (!st && stop_dev(S, eo.overflow)) {
         S.phase = 2;
         S.converged = 1;
+      } else if (!st && S.reset_mult) {
+        S.status = area_multipliers_dev(S, eo);
       } else if (!st) {
         // initial_density_multiplier (eplace.rs:1126-1148)
         double dens = 0.0;

@@ -2,7 +2,7 @@
 // (crates/texo-pnr/src/eplace.rs:242-420) behind one C-ABI call.
 //
 // The loop is host code over this library's own entry points: density rounds
-// on one host-engine handle (texo_gp_optimize_round), between them the
+// on one handle (texo_gp_optimize_round, host or device engine), between them the
 // area-adjustment proposal of eplace.rs:627-740 (the nets' bounding boxes,
 // the RUDY map on the GPU, every movable member's utilization, elfPlace
 // eq. 29 for LUT and register members, the register-clustering areas on the
@@ -288,7 +288,6 @@ extern "C" int32_t texo_gp_place_routable(const texo_gp_problem* problem, const 
     prm = *params;
   else
     texo_gp_default_params(&prm);
-  prm.engine = TEXO_GP_ENGINE_HOST;   // the rounds run on the host engine
   texo_gp_handle h = nullptr;
   int32_t s = texo_gp_create(problem, &prm, &h);
   if (s) return fail(stats, s);

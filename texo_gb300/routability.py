@@ -271,13 +271,12 @@ def area_round_limit(problem):
 
 
 class DeviceRounds:
-    """The rounds of place_routable on this library's host engine."""
+    """The rounds of place_routable on this library's GPU engines (the
+    params' engine: host-driven stages or the persistent kernel)."""
 
     def __init__(self, problem, params):
         from .placer import Placer
-        prm = params
-        prm.engine = abi.ENGINE_HOST
-        self.g = Placer(problem, prm)
+        self.g = Placer(problem, params)
         self.demand = None
         self.clustering = None
 
@@ -306,7 +305,8 @@ def place_routable(problem, params, capacity_h, capacity_v, register_controls=No
     eq. (27)-(28) multipliers and the first round's density scales; once the
     installed increase is below 1 % (or nothing grew) a last round runs to
     the final targets. `rounds` runs the rounds (default: DeviceRounds, this
-    library's host engine). Returns (targets [U, 2], coordinates, info)."""
+    library's engine named by `params`). Returns (targets [U, 2], coordinates,
+    info)."""
     backend = rounds or DeviceRounds(problem, params)
     K = len(problem.fields)
     limit = area_round_limit(problem)
