@@ -898,6 +898,44 @@ def ecp5_report(side=104, seed=0):
                                            "total_displacement": displacement(r)}}
 
 
+def routable_report(side=48, seed=0, capacity=10):
+    """`eplace::place` with a routing-capacity map (texo_gp_place_routable:
+    the area rounds, RUDY and register-clustering proposals, their
+    installation) on the ECP5 adapter's problem for a side x side fabric
+    (seeded synthetic snapshot and netlist; every register with a seeded
+    control set; `capacity` routing tracks per tile edge in each direction),
+    on the host-driven engine and on the persistent device engine."""
+    import numpy as np
+    from texo_gb300 import ecp5
+    from texo_gb300.placer import default_params, place_with_routing_capacity
+    arch = ecp5.read_architecture(ecp5.synthetic_architecture(side, side))
+    n_plc = (side - 2) ** 2
+    nc, units, kinds, nets = ecp5.synthetic_design(arch, seed, luts=2 * n_plc, ffs=n_plc,
+                                                   lut_ff_pairs=n_plc, carry=((n_plc // 40, 4),), io=4 * side)
+    prob, _ = ecp5.placement_problem(arch, nc, units, nets, cell_kind=kinds)
+    controls = {c: (clk, lsr, ce) for c, ce, clk, lsr in ecp5.synthetic_control_sets(kinds, seed)}
+    cap = np.full((arch.height, arch.width), capacity, np.uint32)
+    from texo_gb300 import abi
+    out = {"fabric": "%dx%d" % (side, side), "cells": nc, "units": len(units), "nets": prob.num_nets,
+           "registers": len(controls), "capacity_per_tile": capacity}
+    for name, engine in (("host_engine", abi.ENGINE_HOST), ("device_engine", abi.ENGINE_DEVICE)):
+        prm = lambda: default_params(best_effort=1, engine=engine)
+        try:
+            place_with_routing_capacity(prob, prm(), cap, cap, controls)   # warm-up (module loads)
+            t0 = time.perf_counter()
+            _, _, st, rep = place_with_routing_capacity(prob, prm(), cap, cap, controls)
+            t1 = time.perf_counter()
+        except abi.TexoGpError as e:
+            out[name] = {"error": e.name}
+            continue
+        out[name] = {"wall_s": t1 - t0, "rounds": rep["rounds"], "area_rounds": rep["area_rounds"],
+                     "iterations": rep["iterations"], "hpwl": st["hpwl"], "overflow": st["overflow"],
+                     "converged": st["converged"], "last_relative_increase": rep["last_relative_increase"]}
+    if "wall_s" in out["host_engine"] and "wall_s" in out["device_engine"]:
+        out["device_vs_host_speedup"] = out["host_engine"]["wall_s"] / out["device_engine"]["wall_s"]
+    return out
+
+
 def clustering_report(reps=5):
     """elfPlace's register-clustering areas (`clustering_areas`,
     register_clustering.rs:17-80) for a synthetic register set: one register
@@ -1056,6 +1094,8 @@ def main():
     ap.add_argument("--probe", default="", help="a small workload for profiler captures: tc:N or scatter:WORKLOAD")
     ap.add_argument("--auction-only", action="store_true", help="print only the legalizer auction report")
     ap.add_argument("--clustering-only", action="store_true", help="print only the register-clustering report")
+    ap.add_argument("--routable-only", action="store_true",
+                    help="print only the routing-capacity (area rounds) report, host vs device engine")
     ap.add_argument("--ecp5-only", action="store_true",
                     help="print only the device-snapshot-to-legal-choices report on an ECP5-like fabric")
     args = ap.parse_args()
@@ -1101,6 +1141,11 @@ def main():
     if args.clustering_only:
         if rank == 0:
             print(json.dumps({"metric": "register clustering areas", "clustering": clustering_report()}), flush=True)
+        return
+    if args.routable_only:
+        if rank == 0:
+            print(json.dumps({"metric": "eplace with a routing-capacity map", "routable": routable_report()}),
+                  flush=True)
         return
     if args.ecp5_only:
         if rank == 0:
