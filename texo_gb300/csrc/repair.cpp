@@ -148,8 +148,9 @@ struct Cursor {
   uint32_t bk = 0, bend = 0;
 
   Cursor() = default;
-  Cursor(const Model& m, uint32_t u, int64_t preferred) {
+  Cursor(Model& m, uint32_t u, int64_t preferred) {
     const uint32_t t = m.unit_table[u];
+    m.spatial(t);   // built on a table's first cursor: most tables never need one
     ptr = m.sp_ptr[t].data();
     idx = m.sp_idx[t].data();
     W = m.W, H = m.H;
@@ -870,7 +871,6 @@ extern "C" int32_t texo_gp_repair(uint32_t width, uint32_t height, uint32_t num_
   }
   m.sp_ptr.resize(num_tables);
   m.sp_idx.resize(num_tables);
-  for (uint32_t u = 0; u < num_units; ++u) m.spatial(unit_table[u]);
 
   std::vector<int64_t> pref(num_units);
   std::vector<uint8_t> fx(fixed, fixed + num_units);
