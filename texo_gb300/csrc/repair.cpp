@@ -49,6 +49,12 @@ using SharedClaim = std::pair<SharedKey, uint64_t>;                  // resource
 using Key = std::vector<std::pair<uint32_t, int64_t>>;               // deviations from the proposal
 constexpr int64_t kUnplaced = -1;
 
+struct SharedKeyHash {
+  size_t operator()(const SharedKey& k) const {
+    return std::hash<uint64_t>()(k.second * 0x9E3779B97F4A7C15ull ^ (uint64_t)k.first);
+  }
+};
+
 struct Footprint {
   std::vector<PinClaim> pins;
   std::vector<SharedClaim> shared;
@@ -108,6 +114,12 @@ struct Model {
   // `assignment_footprint` (repair.rs:161-188): sorted distinct claims
   Footprint footprint(uint32_t u, uint32_t c) const {
     Footprint f;
+    footprint_into(u, c, f);
+    return f;
+  }
+  void footprint_into(uint32_t u, uint32_t c, Footprint& f) const {
+    f.pins.clear();
+    f.shared.clear();
     const uint32_t* r = row(u, c);
     for (uint32_t i = 0; i < ncells(u); ++i) {
       const uint32_t cl = cell(u, i), b = r[i];
@@ -132,7 +144,6 @@ struct Model {
     f.pins.erase(std::unique(f.pins.begin(), f.pins.end()), f.pins.end());
     std::sort(f.shared.begin(), f.shared.end());
     f.shared.erase(std::unique(f.shared.begin(), f.shared.end()), f.shared.end());
-    return f;
   }
 };
 
@@ -209,7 +220,7 @@ struct State {
   std::map<uint32_t, int64_t> dev;
   std::vector<int32_t> placed, bel_owner;
   std::unordered_map<uint32_t, std::map<uint32_t, std::set<uint32_t>>> pin_owner;
-  std::map<SharedKey, std::map<uint64_t, std::set<uint32_t>>> shared_owner;
+  std::unordered_map<SharedKey, std::map<uint64_t, std::set<uint32_t>>, SharedKeyHash> shared_owner;
   struct Entry {
     bool installed;
     uint32_t unit;
@@ -232,17 +243,28 @@ struct State {
   };
   std::set<uint32_t, Order> unplaced;
 
+  bool legality = false;   // any pin or shared claims at all
+  const Footprint none{};
+
   State(Model& mm, const std::vector<int64_t>& pref, const std::vector<uint8_t>& fx)
       : m(mm), preferred(pref), fixed(fx), unplaced(Order{&mm}) {
     choice.assign(m.U, -1);
     placed.assign(m.C, -1);
     bel_owner.assign(m.B, -1);
-    for (uint32_t u = 0; u < m.U; ++u) {
-      unplaced.insert(u);
-      if (pref[u] >= 0) dev[u] = kUnplaced;
-    }
+    legality = !m.cp.empty() || !m.cv.empty();
+  }
+  // After the legal base is installed: the unplaced units and their
+  // deviations (the state the reference reaches by installing from an empty
+  // placement, without visiting the installed units twice)
+  void seed_unplaced() {
+    for (uint32_t u = 0; u < m.U; ++u)
+      if (choice[u] < 0) {
+        unplaced.insert(u);
+        if (preferred[u] >= 0) dev[u] = kUnplaced;
+      }
   }
   const Footprint& fp(uint32_t u, int64_t c) {
+    if (!legality) return none;
     const uint64_t k = ((uint64_t)u << 32) | (uint64_t)c;
     auto it = fps.find(k);
     if (it == fps.end()) it = fps.emplace(k, m.footprint(u, (uint32_t)c)).first;
@@ -254,11 +276,16 @@ struct State {
     else
       dev[u] = c < 0 ? kUnplaced : c;
   }
+  Footprint probe;   // the footprint of a choice only tested (not cached)
   bool can_install(uint32_t u, int64_t c) {
     const uint32_t* r = m.row(u, (uint32_t)c);
     for (uint32_t i = 0; i < m.ncells(u); ++i)
       if (bel_owner[r[i]] >= 0) return false;
-    const Footprint& f = fp(u, c);
+    if (!legality) return true;
+    const uint64_t k = ((uint64_t)u << 32) | (uint64_t)c;
+    auto hit = fps.find(k);
+    if (hit == fps.end()) m.footprint_into(u, (uint32_t)c, probe);
+    const Footprint& f = hit == fps.end() ? probe : hit->second;
     for (size_t i = 0; i < f.pins.size();) {
       const uint32_t w = f.pins[i].first;
       auto it = pin_owner.find(w);
@@ -662,7 +689,7 @@ struct Search {
 // `initial_pending_units` (repair.rs:325-414)
 std::set<uint32_t> initial_pending(State& s) {
   const Model& m = s.m;
-  std::vector<std::vector<uint32_t>> bel_owners(m.B);
+  std::vector<uint32_t> claims(m.B, 0);   // proposals naming each BEL
   std::map<uint32_t, std::map<uint32_t, std::set<uint32_t>>> pins;
   std::map<SharedKey, std::map<uint64_t, std::set<uint32_t>>> shared;
   std::set<uint32_t> pending;
@@ -673,13 +700,22 @@ std::set<uint32_t> initial_pending(State& s) {
       continue;
     }
     const uint32_t* r = m.row(u, (uint32_t)c);
-    for (uint32_t i = 0; i < m.ncells(u); ++i) bel_owners[r[i]].push_back(u);
+    for (uint32_t i = 0; i < m.ncells(u); ++i) ++claims[r[i]];
     const Footprint& f = s.fp(u, c);
     for (const PinClaim& p : f.pins) pins[p.first][p.second].insert(u);
     for (const SharedClaim& sc : f.shared) shared[sc.first][sc.second].insert(u);
   }
-  for (const auto& owners : bel_owners) {
-    if (owners.size() < 2) continue;
+  // owners of the BELs claimed twice or more, in unit order
+  std::map<uint32_t, std::vector<uint32_t>> contested;
+  for (uint32_t u = 0; u < m.U; ++u) {
+    const int64_t c = s.preferred[u];
+    if (c < 0) continue;
+    const uint32_t* r = m.row(u, (uint32_t)c);
+    for (uint32_t i = 0; i < m.ncells(u); ++i)
+      if (claims[r[i]] > 1) contested[r[i]].push_back(u);
+  }
+  for (const auto& bo : contested) {
+    const std::vector<uint32_t>& owners = bo.second;
     std::vector<uint32_t> fx;
     for (uint32_t u : owners)
       if (s.fixed[u]) fx.push_back(u);
@@ -893,6 +929,7 @@ extern "C" int32_t texo_gp_repair(uint32_t width, uint32_t height, uint32_t num_
           return fail("relaxed-conflict removal did not leave a legal repair base", TEXO_GP_ERR_PROJECTION_CONFLICT);
         s.raw_install(u, pref[u]);
       }
+    s.seed_unplaced();
     const int64_t first = s.next_unplaced();
     Search search{s, st, {}, {}};
     const bool ok = search.solve();
