@@ -467,22 +467,27 @@ def _native_tables(units):
     """The units' choice tables for the C ABI (units sharing a `choices` list
     share one table): (table array, count, table of every unit, the row
     arrays the tables point into)."""
-    table_of, tables, keep = {}, [], []
-    unit_table = np.zeros(max(len(units), 1), np.uint32)
-    for u, unit in enumerate(units):
+    table_of, shared_of, tables, keep = {}, [], [], []
+    index = []
+    for unit in units:
         key = id(unit.choices)
-        if key not in table_of:
+        t = table_of.get(key)
+        shared = unit.is_shared()
+        if t is None:
+            t = table_of[key] = len(shared_of)
+            shared_of.append(shared)
             rows = np.ascontiguousarray(np.asarray(unit.choices, dtype=np.uint32).reshape(len(unit.choices), -1))
             keep.append(rows)
-            t = abi.ChoiceTable()
-            t.num_choices, t.width = rows.shape
-            t.bels = abi.ptr(rows, C.c_uint32)
-            t.shared = 1 if unit.is_shared() else 0
-            table_of[key] = len(tables)
-            tables.append(t)
-        elif bool(tables[table_of[key]].shared) != unit.is_shared():
+            ct = abi.ChoiceTable()
+            ct.num_choices, ct.width = rows.shape
+            ct.bels = abi.ptr(rows, C.c_uint32)
+            ct.shared = 1 if shared else 0
+            tables.append(ct)
+        elif shared_of[t] != shared:
             raise ValueError("units sharing a choice table must agree on Shared / SingleCell")
-        unit_table[u] = table_of[key]
+        index.append(t)
+    unit_table = np.zeros(max(len(units), 1), np.uint32)
+    unit_table[:len(index)] = index
     arr = (abi.ChoiceTable * max(len(tables), 1))(*tables)
     return arr, len(tables), unit_table, keep
 
