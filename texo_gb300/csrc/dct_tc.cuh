@@ -36,18 +36,23 @@
 // columns x K) a grid of 64 x 32 blocks; a block stores its four slices one
 // after another, blocks ordered K-chunk fastest, zero-padded.
 //
-// One 128 x 64 output tile per block iteration, on a four-stage pipeline of
-// two threads: thread 0 issues the TMA tensor copies (cp.async.bulk.tensor
-// through the operands' tensor maps, complete_tx on a stage's "full"
-// mbarrier), thread 32 the MMAs of each chunk and a commit to the stage's
-// "empty" mbarrier, which releases the stage to the next copy. The four B
-// slices of a block lie one after another in the K-major layout, so their
+// One 128 x 64 output tile per block iteration, on a four-stage pipeline:
+// thread 0 issues the TMA tensor copies (cp.async.bulk.tensor through the
+// operands' tensor maps, complete_tx on a stage's "full" mbarrier); lane 0
+// of warps 1..4 each issues the MMAs of one A slice of each chunk and a
+// commit to the stage's "empty" mbarrier (four arrivals), which releases the
+// stage to the next copy. The accumulators are zeroed (tcgen05.st) at the
+// start of a tile and every MMA accumulates, so the issuers need no order
+// among themselves: every level sum is an exact integer. The MMA issue
+// limits the main loop: a 1024^2 solve takes 148 us with one issuer, 134
+// with two, 124 with four. The four B slices of a block lie one after
+// another in the K-major layout, so their
 // first 64 (4 - i) rows read as one operand of slices 0 .. 3 - i: one MMA of
 // N = 64 (4 - i) multiplies A slice i by all of them, into TMEM columns
 // 64 i ..., which puts A_i B_j on accumulator i + j (columns 64 (i + j)).
 // Eight MMAs of N = 256, 192, 128, 64 a chunk (two K = 16 steps x four A
-// slices) instead of twenty of N = 64: a tcgen05.mma of N = 64 costs the
-// tensor pipe far more than a quarter of one of N = 256. The four
+// slices) instead of twenty of N = 64: an MMA costs about the same to issue
+// whatever its N. The four
 // accumulators occupy 4 x 64 TMEM columns (row i = lane i); the epilogue
 // reads them with tcgen05.ld, warp w taking lanes 32 (w mod 4) ... + 31 and
 // columns 32 (w / 4) ... + 31, and turns them through shared memory for
@@ -85,6 +90,7 @@ constexpr uint32_t kABlock = kSlices * kASlice;     // elements of one A block (
 constexpr uint32_t kBBlock = kSlices * kBSlice;
 constexpr uint32_t kTx = (kABlock + kBBlock) * 2u;  // bytes per stage
 constexpr unsigned kWaitLimit = 1u << 22;      // mbarrier polls before giving up
+constexpr int kIssuers = 4;                    // MMA-issuing threads: lane 0 of warps 1 .. kIssuers
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, N, M.
 __host__ __device__ constexpr uint32_t idesc(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
@@ -190,7 +196,7 @@ struct alignas(128) Smem {
   unsigned long long full[kStages], empty[kStages];
   unsigned long long done;   // every MMA of the tile has completed
   uint32_t tmem;
-  uint32_t issued, consumed;   // chunks copied / taken by the MMA issuer (the cleanup after a failure)
+  uint32_t issued, consumed[kIssuers];   // chunks copied / taken by each MMA issuer (cleanup after a failure)
   int failed;
 };
 // The epilogue stages each warp's 32 rows x kN/2 columns of (hi, lo) pairs
@@ -256,12 +262,13 @@ __device__ __forceinline__ void setup(Smem& sm) {
   if (threadIdx.x == 0) {
     for (int i = 0; i < kStages; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.full[i])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.empty[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(&sm.empty[i])), "r"(kIssuers) : "memory");
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(&sm.done)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(&sm.done)), "r"(kIssuers) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     sm.failed = 0;
-    sm.issued = sm.consumed = 0;
+    sm.issued = 0;
+    for (int k = 0; k < kIssuers; ++k) sm.consumed[k] = 0;
   }
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&sm.tmem)),
@@ -297,6 +304,15 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* v) {
       : "memory");
 }
 #undef TGP_TC_R
+// Zeroes 16 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void st16_zero(uint32_t taddr) {
+  const uint32_t z = 0;
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+      "%1};\n" ::"r"(taddr),
+      "r"(z)
+      : "memory");
+}
 
 // Where a pass puts its result: the double-float pair grid (epi 0 and 2,
 // epi 1 after the inverse-eigenvalue scaling), with the column maxima the
@@ -319,12 +335,12 @@ struct Out {
 // The block must have called setup(); blockDim.x must be 256.
 //
 // Thread 0 copies K-chunks into the stages, each copy waiting for the MMAs
-// that last read its stage (the stage's "empty" commit); thread 32 issues the
-// MMAs of each chunk once its copy landed ("full") and commits them to the
-// stage's "empty" barrier without waiting, so the tensor pipe keeps up to
-// kStages chunks queued. Chunk counters run on across the block's tiles, so
-// the k-th use of a stage waits for the (k-1)-th release. After the last
-// chunk the issuer commits to "done" and waits for it; then the block runs
+// that last read its stage (the stage's "empty" commits); the issuers issue
+// their MMAs of each chunk once its copy landed ("full") and commit them to
+// the stage's "empty" barrier without waiting, so the tensor pipe keeps up
+// to kStages chunks queued. Chunk counters run on across the block's tiles,
+// so the k-th use of a stage waits for the (k-1)-th release. After the last
+// chunk each issuer commits to "done" and waits for it; then the block runs
 // the epilogue: each warp moves its 32 x 32 accumulator block from tensor
 // memory (lane = row) through shared memory (lane = column), so that every
 // global load and store of the epilogue covers a row segment.
@@ -347,6 +363,17 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
     const int f = t / (tiles_m * tiles_n);
     const int rr = t % (tiles_m * tiles_n);
     const int mt = rr / tiles_n, nt = rr % tiles_n;
+    {
+      // the accumulators start at zero, so that the two issuers' MMAs all
+      // accumulate (their order is free: every sum is an exact integer)
+      const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+#pragma unroll
+      for (int part = 0; part < (int)kCols / 2 / 16; ++part)
+        st16_zero(sm.tmem + lanes + (uint32_t)((warp >> 2) * (kCols / 2) + part * 16));
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      fence_before();
+      __syncthreads();
+    }
     if (threadIdx.x == 0) {
       fence_global_async();
       fence_shared_async();
@@ -367,7 +394,9 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
         ++gp;
       }
       sm.issued = gp;
-    } else if (threadIdx.x == 32) {
+    } else if ((threadIdx.x & 31) == 0 && threadIdx.x >= 32 && threadIdx.x <= 32 * kIssuers) {
+      // issuer k takes A slices kSlices / kIssuers * k ... of every K step
+      const int k = (int)(threadIdx.x >> 5) - 1;
       for (int c = 0; c < nkc; ++c) {
         if (*failed) break;
         const uint32_t s = gm % kStages;
@@ -383,13 +412,12 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
           const uint32_t ko = (uint32_t)q * 2u * kCore;   // two K groups of 8 per MMA
           const uint64_t bd = sdesc(bbase + ko);          // B slices 0..3 as 4 kN rows
 #pragma unroll
-          for (int i = 0; i < kSlices; ++i) {
+          for (int ii = 0; ii < kSlices / kIssuers; ++ii) {
             // A slice i times B slices 0 .. 3 - i (the first kN (4 - i) rows)
-            // into columns kN i ...: A_i B_j lands on accumulator i + j. The
-            // first MMA of the tile starts accumulators 0..3 afresh.
-            const uint32_t acc = (c > 0 || q > 0 || i > 0) ? 1u : 0u;
+            // into columns kN i ...: A_i B_j lands on accumulator i + j
+            const int i = kSlices / kIssuers * k + ii;
             mma(sm.tmem + (uint32_t)(i * kN), sdesc(abase + i * kASlice * 2u + ko), bd, idesc(kN * (kLevels - i)),
-                acc);
+                1u);
           }
         }
         commit(saddr(&sm.empty[s]));
@@ -399,14 +427,17 @@ static __device__ void gemm(const CUtensorMap* mA, long sa, const CUtensorMap* m
       commit(saddr(&sm.done));
       if (!wait_phase(saddr(&sm.done), done_ph & 1u)) fail();
       ++done_ph;
-      sm.consumed = gm;
+      sm.consumed[k] = gm;
       fence_before();
     }
     __syncthreads();
     if (*failed) {
-      // one more bounded wait for the copies still in flight
+      // one more bounded wait for the copies still in flight (from the
+      // fewest chunks any issuer took)
       if (threadIdx.x == 0)
-        for (uint32_t g = sm.consumed; g < sm.issued; ++g)
+        for (int k = 1; k < kIssuers; ++k) sm.consumed[0] = min(sm.consumed[0], sm.consumed[k]);
+      if (threadIdx.x == 0)
+        for (uint32_t g = sm.consumed[0]; g < sm.issued; ++g)
           wait_phase(saddr(&sm.full[g % kStages]), (g / kStages) & 1u);
       break;
     }
