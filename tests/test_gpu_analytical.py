@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import ffi
-from texo_gb300 import analytical as A, ecp5, seed
+from texo_gb300 import abi, analytical as A, ecp5, seed
 
 pytestmark = pytest.mark.gpu
 
@@ -96,3 +96,37 @@ def test_anchored_iteration_projects_from_the_incumbent():
     for i, u in enumerate(units):
         if len(u.choices) > 1 and np.array_equal(res.targets[i], incumbent[i].astype(np.uint32)):
             assert res.preferred[i] == first.preferred[i]
+
+
+@pytest.mark.parametrize("engine", [abi.ENGINE_HOST, abi.ENGINE_DEVICE])
+def test_routable_pass_ends_on_legal_bels(engine):
+    """The whole pass with a routing-capacity map on either engine: the seed,
+    the area rounds (RUDY, register clustering with the registers' control
+    sets, instance areas), `project` and its repair with the control sets as
+    shared-resource rules: a legal BEL for every cell."""
+    from texo_gb300 import legalize
+    from texo_gb300.placer import default_params
+    arch, prob, units = fabric(4)
+    bel_xy = np.stack([arch.bel_x, arch.bel_y], 1)
+    kinds = [None] * (1 + max(c for u in units for c in u.cells))
+    for u in units:
+        for c, b in zip(u.cells, u.choices[0]):
+            kinds[c] = arch.bel_kind[b]
+    sets = ecp5.synthetic_control_sets(kinds, seed=2)
+    controls = {c: (clk, lsr, ce) for c, ce, clk, lsr in sets}
+    cap = np.full((arch.height, arch.width), 8, np.uint32)
+    res = A.analytical_place(prob, units, bel_xy, mode=A.ELECTROSTATIC,
+                             params=default_params(best_effort=1, engine=engine),
+                             routing_capacity=(cap, cap), register_controls=controls)
+    assert res.info["routable"]["rounds"] >= 1
+    placed = res.bels
+    assert np.all(placed >= 0) and len(np.unique(placed)) == len(placed)
+    # the control sets, checked on the repair's output with them as rules
+    rules = ecp5.ff_control_set_rules(arch, sets)
+    fixed = [len(u.choices) == 1 for u in units]
+    legal_bels, _ = legalize.repair(arch.width, arch.height, bel_xy, units, res.targets, res.preferred, fixed,
+                                    legalize.Legality(rules=rules))
+    for cell_values, bel_res in rules:
+        seen = {}
+        for c, v in cell_values.items():
+            assert seen.setdefault(bel_res[int(legal_bels[c])], v) == v
